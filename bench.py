@@ -1,0 +1,323 @@
+"""Benchmark: incoherent closest-hit traversal on the 1M-triangle scene (the headline Mrays/s metric).
+
+Workload: a seeded mesh of 1 000 000 triangles (icosphere of frequency 200 displaced by 3-octave value noise,
+plus 200 000 random small triangles in [-2, 2]^3) and 4 194 304 incoherent rays (area-uniform surface origins,
+cosine-distributed directions). One step = one lgb_trace_closest over all rays.
+
+  value  rays / device time of the trace kernel (CUDA events on the launching stream), L2 flushed with a
+         256 MB write before every step so each step starts cold
+  e2e    the same call with host buffers: pinned host rays -> device, trace, hits -> pinned host
+  cpu_baseline  the CPU oracle (binary SAH BVH, same watertight test) on a bounded sample of the rays,
+         all host threads
+
+--impl reference times the CPU oracle (the reference path restated on the CPU; Lumen itself needs a
+Vulkan ray-tracing device) on the same workload. N > 1 GPUs run independent replicas (the path shards by
+ray with no exchange step), one rank per GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_INCOHERENT = 4 * 1024 * 1024
+METRIC = "Mrays/s incoherent closest-hit"
+WORKLOAD = "traversal: 1M-triangle displaced icosphere + random triangles, 4M incoherent closest-hit rays"
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[3:7]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(cache=True):
+    from lumen_gb300 import procedural
+    path = os.path.join("/tmp", "lgb_bench_traversal_v1.npz")
+    if cache and os.path.exists(path):
+        z = np.load(path, allow_pickle=True)
+        arrays = procedural.traversal_scene(sphere_freq=1, n_random=0)  # shell with the right meshes/materials
+        for k in ("positions", "normals", "uvs", "indices", "meshes"):
+            setattr(arrays, k, z[k])
+        return arrays, z["rays"]
+    arrays = procedural.traversal_scene()
+    rays = procedural.incoherent_rays(arrays, N_INCOHERENT, seed=3)
+    if cache:
+        try:
+            np.savez(path, positions=arrays.positions, normals=arrays.normals, uvs=arrays.uvs, indices=arrays.indices,
+                     meshes=arrays.meshes, rays=rays)
+        except OSError:
+            pass
+    return arrays, rays
+
+
+def measure_l2_peak(torch):
+    """Read bandwidth of an L2-resident buffer (32 MB, read 64 times per launch with a reduction)."""
+    x = torch.ones(8 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        x.sum()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 0.0
+    for _ in range(5):
+        s.record()
+        for _ in range(64):
+            x.sum()
+        e.record()
+        e.synchronize()
+        best = max(best, 64 * x.numel() * 4 / (s.elapsed_time(e) * 1e-3) / 1e9)
+    return best
+
+
+def cpu_oracle_rate(arrays, rays, seconds=12.0, threads=None):
+    """Rays/s of the CPU oracle on a bounded sample; returns (rays_per_s, sample_rays, threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    ora = oracle_lib.Oracle()
+    threads = threads or (os.cpu_count() or 1)
+    bvh = ora.bvh(arrays.tri_verts())
+    probe = rays[:20000]
+    t0 = time.perf_counter()
+    bvh.closest(probe, threads)
+    rate = len(probe) / (time.perf_counter() - t0)
+    n = int(min(len(rays), max(20000, rate * seconds)))
+    t0 = time.perf_counter()
+    bvh.closest(rays[:n], threads)
+    dt = time.perf_counter() - t0
+    return n / dt, n, threads
+
+
+def run_reference(args):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return
+    arrays, rays = make_workload()
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    ora = oracle_lib.Oracle()
+    threads = os.cpu_count() or 1
+    bvh = ora.bvh(arrays.tri_verts())
+    sample = 100_000
+    rng = np.random.default_rng(11)
+    vals = []
+    for step in range(args.warmup + args.steps):
+        idx = rng.integers(0, len(rays) - sample)
+        t0 = time.perf_counter()
+        bvh.closest(rays[idx:idx + sample], threads)
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            vals.append(sample / dt / 1e6)
+    value = float(np.median(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sample / (value * 1e6) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "rays_per_step": sample, "sample": "contiguous 100k-ray windows"},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} rays per step of the 4M incoherent set"},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of the reference path (Lumen runs only through Vulkan ray tracing, "
+                "unavailable on this box); binary SAH BVH, watertight FP32 test",
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import torch
+    rank, world, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from lumen_gb300 import abi
+    from lumen_gb300.scene import Context, GpuScene
+    arrays, rays = make_workload()
+    ctx = Context(local)
+    sc = GpuScene(ctx, arrays)
+    stats = sc.build()
+    n = len(rays)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    d_rays = torch.from_numpy(rays).cuda()
+    d_hits = torch.empty((n, 4), dtype=torch.int32, device="cuda")
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    # bytes/ray accounting from the counting variant (untimed)
+    counters = torch.zeros(2, dtype=torch.int64, device="cuda")
+    sc.trace_closest_counted(d_rays, d_hits, counters, stream=sptr)
+    sc.sync(sptr)
+    n_nodes, n_tris = (counters.cpu().numpy() / n).tolist()
+    bytes_per_ray = 32 + 16 + 80 * n_nodes + 48 * n_tris
+
+    for _ in range(args.warmup):
+        flush.fill_(1.0)
+        sc.trace_closest(d_rays, d_hits, stream=sptr)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    for s, e in ev:
+        flush.fill_(1.0)
+        s.record(stream)
+        sc.trace_closest(d_rays, d_hits, stream=sptr)
+        e.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    ms = [s.elapsed_time(e) for s, e in ev]
+    # end-to-end through the C ABI with host buffers
+    h_rays = torch.from_numpy(rays).pin_memory()
+    h_hits = torch.empty((n, 4), dtype=torch.int32).pin_memory()
+    e2e_ms = []
+    for step in range(args.warmup + args.steps):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        flush.fill_(1.0)
+        s.record(stream)
+        d_rays.copy_(h_rays, non_blocking=True)
+        sc.trace_closest(d_rays, d_hits, stream=sptr)
+        h_hits.copy_(d_hits, non_blocking=True)
+        e.record(stream)
+        e.synchronize()
+        if step >= args.warmup:
+            e2e_ms.append(s.elapsed_time(e))
+    clk = clocks.stop()
+    sc.sync(sptr)
+    step_ms = float(np.mean(ms))
+    e2e_step = float(np.mean(e2e_ms))
+    if world > 1:
+        t = torch.tensor([step_ms, e2e_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_ms, e2e_step = t.tolist()
+    if rank != 0:
+        return
+    value = world * n / (step_ms * 1e-3) / 1e6
+    e2e = world * n / (e2e_step * 1e-3) / 1e6
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    hbm_peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as f:
+            hbm_peak = float(json.load(f).get("hbm_gbs", hbm_peak))
+        peak_src = "measured"
+    l2_peak = measure_l2_peak(torch)
+    achieved = bytes_per_ray * n / (step_ms * 1e-3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "trace_closest_incoherent_1M.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            p = json.load(f)
+        traffic = p.get("dram_bytes_per_ray") and p["dram_bytes_per_ray"] * n
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        rate, sample, threads = cpu_oracle_rate(arrays, rays)
+        cpu = {"value": rate / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": f"first {sample} of the 4M incoherent rays, binary SAH BVH"}
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "rays_per_step": n, "triangles": stats.num_tris,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "flushed with a 256 MB write before every step", "bvh_nodes": stats.num_nodes,
+                   "bvh_depth": stats.max_depth, "bvh_build_ms": stats.build_ms, "sah_cost": stats.sah_cost,
+                   "wall_s_timed_region": wall},
+        "e2e": {"value": e2e, "unit": "Mrays/s", "h2d_bytes_per_step": int(rays.nbytes),
+                "d2h_bytes_per_step": int(n * 16)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_src,
+                     "bytes_per_ray": bytes_per_ray, "nodes_per_ray": n_nodes, "tris_per_ray": n_tris,
+                     "l2_read_peak_gbs": l2_peak, "frac_of_l2_peak": achieved / l2_peak,
+                     "note": "achieved counts ray + hit + 80 B per node and 48 B per triangle fetched; the "
+                             "working set (BVH + triangles) is L2-resident, so frac_of_l2_peak is the binding one"},
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "gpu_launches": args.steps,
+    }
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

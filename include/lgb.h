@@ -1,0 +1,215 @@
+/* lgb.h -- C ABI of the GB300-native ray-tracing core (BVH build, traversal, MIS path tracer).
+ *
+ * This header is the drop-in boundary. Lumen has no FFI of its own: its path is one C++ class per
+ * integrator (src/RayTracer/Integrator.h:14-33) that records Vulkan ray-tracing passes, with the BVH built
+ * and traversed inside the driver. Each entry point below replaces one piece of that path; the comment on
+ * each names the reference code it stands in for.
+ *
+ * Conventions
+ *   - Plain C types and pointers only; no CUDA or C++ types in signatures. A `stream` argument is a
+ *     cudaStream_t passed as void* (NULL = the legacy default stream).
+ *   - Pointers named d_* are device pointers owned by the caller. Every other pointer is a host pointer
+ *     that the library reads during the call only.
+ *   - Every entry point returns an lgb_status; on failure lgb_last_error() describes it. No exception or
+ *     longjmp crosses this boundary.
+ *   - A context is externally synchronised: one host thread at a time per context. Work is stream-ordered.
+ */
+#ifndef LGB_H
+#define LGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define LGB_API __attribute__((visibility("default")))
+#else
+#define LGB_API
+#endif
+
+typedef int32_t lgb_status;
+#define LGB_OK 0
+#define LGB_ERR_INVALID_ARGUMENT 1 /* bad pointer, size or scene content */
+#define LGB_ERR_CUDA 2             /* a CUDA runtime call failed */
+#define LGB_ERR_OUT_OF_MEMORY 3
+#define LGB_ERR_NOT_READY 4        /* e.g. a trace before lgb_bvh_build */
+#define LGB_ERR_DEVICE_STATUS 5    /* a kernel reported a fault through the device status word */
+#define LGB_ERR_UNSUPPORTED 6      /* scene feature outside the supported subset */
+
+typedef struct lgb_ctx lgb_ctx;
+typedef struct lgb_scene lgb_scene;
+
+/* Ray, 32 bytes: origin, tmin, direction, tmax (the arguments of traceRayEXT, path.rgen:48). */
+typedef struct lgb_ray {
+    float ox, oy, oz, tmin;
+    float dx, dy, dz, tmax;
+} lgb_ray;
+
+/* Closest hit, 16 bytes. prim is the global triangle id (LGB_NO_HIT on a miss); u, v are the Vulkan
+ * barycentrics (hitAttributeEXT, ray.rchit:13,57): u weights vertex 1, v weights vertex 2. */
+typedef struct lgb_hit {
+    uint32_t prim;
+    float t, u, v;
+} lgb_hit;
+#define LGB_NO_HIT 0xFFFFFFFFu
+
+/* Material, 104 bytes, the scalar layout of src/shaders/commons.h:212-234. */
+typedef struct lgb_material {
+    float albedo[3];
+    float ior;
+    float emissive_factor[3];
+    uint32_t bsdf_type;  /* LGB_BSDF_* (commons.h:13-18) */
+    uint32_t bsdf_props; /* LGB_FLAG_* (commons.h:22-26) */
+    float k[3];
+    int32_t texture_id; /* -1 = none */
+    float roughness, diffuse_trans, spec_trans, metallic, specular_tint, sheen_tint, clearcoat, clearcoat_gloss,
+        sheen, subsurface, flatness, anisotropy;
+    uint32_t thin;
+} lgb_material;
+
+#define LGB_BSDF_DIFFUSE (1u << 0)
+#define LGB_BSDF_MIRROR (1u << 1)
+#define LGB_BSDF_GLASS (1u << 2)
+#define LGB_BSDF_DIELECTRIC (1u << 3)
+#define LGB_BSDF_CONDUCTOR (1u << 4)
+#define LGB_BSDF_PRINCIPLED (1u << 5)
+#define LGB_FLAG_DIFFUSE (1u << 0)
+#define LGB_FLAG_SPECULAR (1u << 1)
+#define LGB_FLAG_GLOSSY (1u << 2)
+#define LGB_FLAG_REFLECTION (1u << 3)
+#define LGB_FLAG_TRANSMISSION (1u << 4)
+
+/* Light, 128 bytes, src/shaders/commons.h:200-210. light_flags: bits 0-2 type (LGB_LIGHT_*),
+ * bit 4 finite, bit 5 delta (LumenScene.cpp:89-91,500-509). world_matrix must be the identity: Lumen's
+ * loaders never set anything else (LumenScene.cpp:328). */
+typedef struct lgb_light {
+    float world_matrix[16];
+    float pos[3];
+    uint32_t prim_mesh_idx;
+    float to[3];
+    uint32_t num_triangles;
+    float L[3];
+    uint32_t light_flags;
+    float world_center[3];
+    float world_radius;
+} lgb_light;
+#define LGB_LIGHT_SPOT 1u
+#define LGB_LIGHT_AREA 2u
+#define LGB_LIGHT_DIRECTIONAL 3u
+
+/* One mesh (the PrimMeshInfo fields of commons.h:333-340 that the path reads, plus its triangle count). */
+typedef struct lgb_mesh {
+    uint32_t index_offset;  /* first index of the mesh in indices[] (a multiple of 3) */
+    uint32_t vertex_offset; /* added to every index of the mesh */
+    uint32_t material_index;
+    uint32_t tri_count;
+} lgb_mesh;
+
+/* Linear FP32 RGBA texture, sampled bilinearly with REPEAT at LOD 0. */
+typedef struct lgb_texture {
+    uint32_t width, height;
+    const float* rgba; /* host, width*height*4 floats, row-major from v = 0 */
+} lgb_texture;
+
+/* Host scene arrays (LumenScene::load_scene's output, LumenScene.cpp:52-229). The library copies them;
+ * the caller keeps ownership. Global triangle g of mesh m is local triangle g - first_tri(m), where meshes
+ * are numbered in order and first_tri is the running sum of tri_count. */
+typedef struct lgb_scene_desc {
+    const float* positions; /* 3 floats per vertex */
+    const float* normals;   /* 3 floats per vertex */
+    const float* uvs;       /* 2 floats per vertex */
+    uint32_t num_vertices;
+    const uint32_t* indices;
+    uint32_t num_indices;
+    const lgb_mesh* meshes;
+    uint32_t num_meshes;
+    const lgb_material* materials;
+    uint32_t num_materials;
+    const lgb_light* lights;
+    uint32_t num_lights;
+    const lgb_texture* textures;
+    uint32_t num_textures;
+} lgb_scene_desc;
+
+typedef struct lgb_build_opts {
+    uint32_t leaf_max;        /* triangles per 8-wide leaf slot, 1..3 (0 = default 3) */
+    uint32_t reserved[7];
+} lgb_build_opts;
+
+typedef struct lgb_build_stats {
+    float build_ms;           /* device time of the whole build */
+    uint32_t num_tris;
+    uint32_t num_nodes;       /* 8-wide nodes */
+    uint32_t max_depth;       /* deepest 8-wide level (root = 1) */
+    uint64_t node_bytes;
+    uint64_t tri_bytes;
+    float sah_cost;           /* SAH cost of the 8-wide tree (node cost 1, triangle cost 1) */
+    uint32_t reserved[5];
+} lgb_build_stats;
+
+/* Camera for the path integrator: the two matrices path.rgen:36-38 and commons.glsl:30-33 read
+ * (column-major, as glm stores them) and the launch size. */
+typedef struct lgb_camera {
+    float inv_view[16];
+    float inv_projection[16];
+    uint32_t width, height;
+} lgb_camera;
+
+/* PCPath (src/shaders/integrators/path/path_commons.h:3-15), minus the per-frame fields. */
+typedef struct lgb_path_params {
+    float sky_col[3];
+    int32_t max_depth;             /* path_length (SceneConfig.h:16, default 6) */
+    int32_t num_lights;
+    int32_t light_triangle_count;  /* LumenScene::total_light_triangle_cnt */
+    uint32_t dir_light_idx;        /* 0xFFFFFFFF = none; the atmosphere model is not supported */
+    uint32_t direct_lighting;      /* 1 = default (Path.h:18) */
+    uint32_t film_mode;            /* 0 = progressive mean as path.rgen:106-112; 1 = write each frame's raw sample */
+    uint32_t reserved[3];
+} lgb_path_params;
+
+/* ---- context (stands in for the Vulkan device/context, VulkanBase.cpp) ---- */
+LGB_API lgb_status lgb_create(lgb_ctx** out, int device);
+LGB_API void lgb_destroy(lgb_ctx* ctx);
+LGB_API const char* lgb_last_error(const lgb_ctx* ctx);
+LGB_API uint32_t lgb_abi_version(void);
+
+/* ---- scene upload (LumenScene::load_scene's GPU buffers, LumenScene.cpp:146-190) ---- */
+LGB_API lgb_status lgb_scene_create(lgb_ctx* ctx, const lgb_scene_desc* desc, lgb_scene** out);
+LGB_API void lgb_scene_destroy(lgb_scene* scene);
+
+/* ---- acceleration structure (Integrator::create_accel, Integrator.cpp:137-160; vk::build_blas/build_tlas,
+ *      AccelerationStructure.cpp:171-315). One 8-wide BVH over all meshes' triangles. ---- */
+LGB_API lgb_status lgb_bvh_build(lgb_scene* scene, const lgb_build_opts* opts, lgb_build_stats* stats);
+
+/* ---- ray queries (traceRayEXT: closest, path.rgen:48 / pt_commons.glsl:32; any-hit shadow,
+ *      pt_commons.glsl:20-23 with ray.rahit:18-21 and ray_shadow.rmiss:12). ----
+ * Closest: the triangle with the smallest watertight t in [tmin, tmax]; equal t goes to the lowest prim.
+ * Any: bit i of d_occluded_bits[i / 32] is set iff some triangle is hit in [tmin, tmax]. */
+LGB_API lgb_status lgb_trace_closest(lgb_scene* scene, const lgb_ray* d_rays, lgb_hit* d_hits, uint32_t n,
+                                     void* stream);
+LGB_API lgb_status lgb_trace_any(lgb_scene* scene, const lgb_ray* d_rays, uint32_t* d_occluded_bits, uint32_t n,
+                                 void* stream);
+/* Same query as lgb_trace_closest, also adding the 8-wide nodes and triangles each ray fetched into
+ * d_counters[0] and d_counters[1] (device uint64). For bytes-per-ray accounting. */
+LGB_API lgb_status lgb_trace_closest_counted(lgb_scene* scene, const lgb_ray* d_rays, lgb_hit* d_hits, uint32_t n,
+                                             uint64_t* d_counters, void* stream);
+
+/* ---- camera helper (Camera.h:67-123, Integrator.cpp:60-72): fills out->inv_view/inv_projection ---- */
+LGB_API lgb_status lgb_camera_lookat(const float pos[3], const float dir[3], float fov_deg, uint32_t width,
+                                     uint32_t height, lgb_camera* out);
+
+/* ---- the Path integrator (Path::render, Path.cpp:27-59, i.e. path.rgen for frames frame0..frame0+spp-1).
+ *      d_film is RGBA32F width*height (float4 per pixel), updated in place. ---- */
+LGB_API lgb_status lgb_render_path(lgb_scene* scene, const lgb_camera* camera, const lgb_path_params* params,
+                                   uint32_t frame0, uint32_t spp, float* d_film, void* stream);
+
+/* Waits for `stream` and reports any fault a kernel recorded in the scene's device status word. */
+LGB_API lgb_status lgb_sync(lgb_scene* scene, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LGB_H */

@@ -1,0 +1,596 @@
+// GPU BVH construction for the 8-wide quantised BVH.
+//
+// Replaces the driver-side BLAS/TLAS build that Lumen requests through vk::build_blas / vk::build_tlas
+// (src/Framework/AccelerationStructure.cpp:171-315, called from src/RayTracer/Integrator.cpp:137-160).
+// All meshes are flattened into one tree over global triangle ids.
+//
+// Pipeline (one stream, all on the device):
+//   1. triangle bounds + centroid bounds (ordered-integer atomics)
+//   2. 63-bit Morton codes of triangle centroids
+//   3. LSD radix sort of (code, triangle) pairs, 8 passes of 8 bits, stable block-local ranking
+//   4. binary radix tree over the sorted codes (Karras, HPG 2012), ties broken by position
+//   5. bottom-up node boxes (first arrival stops, second merges)
+//   6. top-down collapse to 8-wide nodes, one level per launch: each binary node becomes a wide node
+//      by repeatedly opening its largest-area internal child; children are placed in octant slots, boxes
+//      quantised to 8 bits with outward rounding, and leaf triangles copied into leaf order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "lgb_internal.cuh"
+
+namespace lgb {
+namespace {
+
+constexpr uint32_t kLeafFlag = 0x80000000u;
+
+__device__ __forceinline__ uint32_t f2o(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float o2f(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// bounds[0..2] = centroid min (ordered), [3..5] = centroid max
+__global__ void k_centroid_bounds(const float* __restrict__ tv, uint32_t n, uint32_t* bounds) {
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float* v = tv + 9 * (size_t)i;
+        for (int a = 0; a < 3; a++) {
+            float mn = fminf(fminf(v[a], v[3 + a]), v[6 + a]);
+            float mx = fmaxf(fmaxf(v[a], v[3 + a]), v[6 + a]);
+            float c = 0.5f * (mn + mx);
+            lo[a] = fminf(lo[a], c);
+            hi[a] = fmaxf(hi[a], c);
+        }
+    }
+    for (int a = 0; a < 3; a++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int a = 0; a < 3; a++) {
+            atomicMin(&bounds[a], f2o(lo[a]));
+            atomicMax(&bounds[3 + a], f2o(hi[a]));
+        }
+    }
+}
+
+__device__ __forceinline__ uint64_t split3(uint32_t a) {
+    uint64_t x = a & 0x1fffffu;
+    x = (x | x << 32) & 0x1f00000000ffffull;
+    x = (x | x << 16) & 0x1f0000ff0000ffull;
+    x = (x | x << 8) & 0x100f00f00f00f00full;
+    x = (x | x << 4) & 0x10c30c30c30c30c3ull;
+    x = (x | x << 2) & 0x1249249249249249ull;
+    return x;
+}
+
+__global__ void k_morton(const float* __restrict__ tv, uint32_t n, const uint32_t* bounds, uint64_t* keys,
+                         uint32_t* vals, float* tri_box /* 6 per tri: lo xyz, hi xyz */) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* v = tv + 9 * (size_t)i;
+    uint32_t q[3];
+    for (int a = 0; a < 3; a++) {
+        float mn = fminf(fminf(v[a], v[3 + a]), v[6 + a]);
+        float mx = fmaxf(fmaxf(v[a], v[3 + a]), v[6 + a]);
+        tri_box[6 * (size_t)i + a] = mn;
+        tri_box[6 * (size_t)i + 3 + a] = mx;
+        float c = 0.5f * (mn + mx);
+        float clo = o2f(bounds[a]), chi = o2f(bounds[3 + a]);
+        float ext = chi - clo;
+        float t = ext > 0.0f ? (c - clo) / ext : 0.0f;
+        float s = t * 2097152.0f;
+        s = fminf(fmaxf(s, 0.0f), 2097151.0f);
+        q[a] = (uint32_t)s;
+    }
+    keys[i] = (split3(q[0]) << 2) | (split3(q[1]) << 1) | split3(q[2]);
+    vals[i] = i;
+}
+
+// ---------------- LSD radix sort (64-bit keys, 32-bit values) ----------------
+constexpr int RS_THREADS = 256;
+constexpr int RS_ITEMS = 8;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint64_t* __restrict__ keys, uint32_t n, int shift,
+                                                        uint32_t* counts, uint32_t nblocks) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    size_t base = (size_t)blockIdx.x * RS_TILE;
+    for (int k = 0; k < RS_ITEMS; k++) {
+        size_t idx = base + (size_t)k * RS_THREADS + threadIdx.x;
+        if (idx < n) atomicAdd(&h[(uint32_t)(keys[idx] >> shift) & 0xffu], 1u);
+    }
+    __syncthreads();
+    counts[(size_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+// Exclusive scan of m counts in place, one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_scan_single(uint32_t* data, uint32_t m) {
+    __shared__ uint32_t warp_sums[32];
+    const uint32_t per = (m + 1023) / 1024;
+    const uint32_t b = threadIdx.x * per, e = min(m, b + per);
+    uint32_t sum = 0;
+    for (uint32_t i = b; i < e; i++) sum += data[i];
+    // block exclusive scan of sum
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warp_sums[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        warp_sums[lane] = w;
+    }
+    __syncthreads();
+    uint32_t excl = x - sum + (warp > 0 ? warp_sums[warp - 1] : 0u);
+    for (uint32_t i = b; i < e; i++) {
+        uint32_t c = data[i];
+        data[i] = excl;
+        excl += c;
+    }
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                                           uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                           uint32_t n, int shift, const uint32_t* __restrict__ offsets,
+                                                           uint32_t nblocks) {
+    __shared__ uint32_t base_off[256];
+    __shared__ uint32_t warp_cnt[RS_THREADS / 32][256];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    base_off[tid] = offsets[(size_t)tid * nblocks + blockIdx.x];
+    const uint32_t lanemask_lt = (1u << lane) - 1u;
+    const size_t tile = (size_t)blockIdx.x * RS_TILE;
+    for (int r = 0; r < RS_ITEMS; r++) {
+        for (int w = 0; w < RS_THREADS / 32; w++) warp_cnt[w][tid] = 0;
+        __syncthreads();
+        const size_t idx = tile + (size_t)r * RS_THREADS + tid;
+        const bool valid = idx < n;
+        uint64_t key = valid ? kin[idx] : 0ull;
+        uint32_t val = valid ? vin[idx] : 0u;
+        uint32_t digit = valid ? ((uint32_t)(key >> shift) & 0xffu) : (256u + lane);
+        uint32_t peers = __match_any_sync(0xffffffffu, digit);
+        uint32_t rank = __popc(peers & lanemask_lt);
+        int leader = __ffs(peers) - 1;
+        if (valid && lane == leader) warp_cnt[warp][digit] = __popc(peers);
+        __syncthreads();
+        uint32_t running = 0;
+        for (int w = 0; w < RS_THREADS / 32; w++) {
+            uint32_t c = warp_cnt[w][tid];
+            warp_cnt[w][tid] = running;
+            running += c;
+        }
+        __syncthreads();
+        if (valid) {
+            uint32_t pos = base_off[digit] + warp_cnt[warp][digit] + rank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+        base_off[tid] += running;
+        __syncthreads();
+    }
+}
+
+// ---------------- binary radix tree (Karras 2012) ----------------
+__device__ __forceinline__ int delta(const uint64_t* keys, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    uint64_t a = keys[i], b = keys[j];
+    if (a == b) return 64 + __clz((uint32_t)(i ^ j));
+    return __clzll(a ^ b);
+}
+
+__global__ void k_radix_tree(const uint64_t* __restrict__ keys, int n, uint32_t* left, uint32_t* right,
+                             uint32_t* parent_int, uint32_t* parent_leaf, uint32_t* range_lo, uint32_t* range_hi) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = delta(keys, n, i, i - d);
+    int lmax = 2;
+    while (delta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = delta(keys, n, i, j);
+    int s = 0, t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    int gamma = i + s * d + min(d, 0);
+    int lo = min(i, j), hi = max(i, j);
+    uint32_t lc = (lo == gamma) ? ((uint32_t)gamma | kLeafFlag) : (uint32_t)gamma;
+    uint32_t rc = (hi == gamma + 1) ? ((uint32_t)(gamma + 1) | kLeafFlag) : (uint32_t)(gamma + 1);
+    left[i] = lc;
+    right[i] = rc;
+    range_lo[i] = lo;
+    range_hi[i] = hi;
+    if (lc & kLeafFlag) parent_leaf[lc & ~kLeafFlag] = i; else parent_int[lc] = i;
+    if (rc & kLeafFlag) parent_leaf[rc & ~kLeafFlag] = i; else parent_int[rc] = i;
+}
+
+// Bottom-up boxes. node_box: 6 floats per internal node; leaf boxes come from tri_box via sorted vals.
+__global__ void k_bottom_up(int n, const uint32_t* __restrict__ vals, const float* __restrict__ tri_box,
+                            const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
+                            const uint32_t* __restrict__ parent_int, const uint32_t* __restrict__ parent_leaf,
+                            float* node_box, uint32_t* flags) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t node = parent_leaf[k];
+    // A radix tree over n keys is at most n - 1 levels deep; the bound only guards against a malformed tree.
+    for (int steps = 0; steps < n; steps++) {
+        __threadfence();
+        if (atomicAdd(&flags[node], 1u) == 0u) return;
+        __threadfence();
+        float b[6];
+        uint32_t cl = left[node], cr = right[node];
+        const float* A = (cl & kLeafFlag) ? &tri_box[6 * (size_t)vals[cl & ~kLeafFlag]] : &node_box[6 * (size_t)cl];
+        const float* B = (cr & kLeafFlag) ? &tri_box[6 * (size_t)vals[cr & ~kLeafFlag]] : &node_box[6 * (size_t)cr];
+        for (int a = 0; a < 3; a++) {
+            b[a] = fminf(__ldcg(&A[a]), __ldcg(&B[a]));
+            b[3 + a] = fmaxf(__ldcg(&A[3 + a]), __ldcg(&B[3 + a]));
+        }
+        for (int a = 0; a < 6; a++) __stcg(&node_box[6 * (size_t)node + a], b[a]);
+        if (node == 0) return;
+        node = parent_int[node];
+    }
+}
+
+// ---------------- collapse to 8-wide ----------------
+struct CollapseArgs {
+    const uint32_t* left;
+    const uint32_t* right;
+    const uint32_t* range_lo;
+    const uint32_t* range_hi;
+    const float* node_box;
+    const float* tri_box;
+    const uint32_t* vals;   // sorted position -> original triangle
+    const float* tri_verts;
+    WideNode* nodes;
+    WideTri* tris;
+    uint32_t* counters;     // [0] = nodes allocated, [1] = triangles written, [2] = next queue size
+    float* sah;             // accumulated SAH numerator
+    int leaf_max;
+    int e_min[3];           // minimum biased-less exponent per axis
+    float inv_root_area;
+};
+
+__device__ __forceinline__ void ref_box(const CollapseArgs& A, uint32_t ref, float* b) {
+    const float* src = (ref & kLeafFlag) ? &A.tri_box[6 * (size_t)A.vals[ref & ~kLeafFlag]] : &A.node_box[6 * (size_t)ref];
+    for (int a = 0; a < 6; a++) b[a] = src[a];
+}
+__device__ __forceinline__ uint32_t ref_count(const CollapseArgs& A, uint32_t ref) {
+    return (ref & kLeafFlag) ? 1u : (A.range_hi[ref] - A.range_lo[ref] + 1u);
+}
+__device__ __forceinline__ uint32_t ref_first(const CollapseArgs& A, uint32_t ref) {
+    return (ref & kLeafFlag) ? (ref & ~kLeafFlag) : A.range_lo[ref];
+}
+__device__ __forceinline__ float half_area(const float* b) {
+    float dx = fmaxf(b[3] - b[0], 0.0f), dy = fmaxf(b[4] - b[1], 0.0f), dz = fmaxf(b[5] - b[2], 0.0f);
+    return dx * dy + dy * dz + dz * dx;
+}
+
+__global__ void k_collapse(CollapseArgs A, const uint2* __restrict__ qin, uint32_t nin, uint2* __restrict__ qout) {
+    uint32_t qi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (qi >= nin) return;
+    const uint32_t bref = qin[qi].x, widx = qin[qi].y;
+    uint32_t ch[8];
+    int nc = 0;
+    if (bref & kLeafFlag) {
+        ch[nc++] = bref;
+    } else {
+        ch[nc++] = A.left[bref];
+        ch[nc++] = A.right[bref];
+        while (nc < 8) {
+            int best = -1;
+            float best_area = -1.0f;
+            for (int c = 0; c < nc; c++) {
+                if (ch[c] & kLeafFlag) continue;
+                float b[6];
+                ref_box(A, ch[c], b);
+                float ar = half_area(b);
+                if (ar > best_area) { best_area = ar; best = c; }
+            }
+            if (best < 0) break;
+            uint32_t r = ch[best];
+            ch[best] = A.left[r];
+            ch[nc++] = A.right[r];
+        }
+    }
+    // node box = union of children
+    float nb[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+    float cb[8][6];
+    for (int c = 0; c < nc; c++) {
+        ref_box(A, ch[c], cb[c]);
+        for (int a = 0; a < 3; a++) { nb[a] = fminf(nb[a], cb[c][a]); nb[3 + a] = fmaxf(nb[3 + a], cb[c][3 + a]); }
+    }
+    // slot assignment: greedy on alignment of the child centre offset with each octant direction
+    float pc[3] = {0.5f * (nb[0] + nb[3]), 0.5f * (nb[1] + nb[4]), 0.5f * (nb[2] + nb[5])};
+    int child_in_slot[8];
+    for (int s = 0; s < 8; s++) child_in_slot[s] = -1;
+    bool assigned[8] = {false, false, false, false, false, false, false, false};
+    for (int it = 0; it < nc; it++) {
+        float best = -FLT_MAX;
+        int bc = -1, bs = -1;
+        for (int c = 0; c < nc; c++) {
+            if (assigned[c]) continue;
+            float off[3];
+            for (int a = 0; a < 3; a++) off[a] = 0.5f * (cb[c][a] + cb[c][3 + a]) - pc[a];
+            for (int s = 0; s < 8; s++) {
+                if (child_in_slot[s] >= 0) continue;
+                float score = ((s & 1) ? off[0] : -off[0]) + ((s & 2) ? off[1] : -off[1]) + ((s & 4) ? off[2] : -off[2]);
+                if (score > best) { best = score; bc = c; bs = s; }
+            }
+        }
+        if (bc < 0) {  // non-finite boxes: take the first free child and slot
+            for (int c = 0; c < nc && bc < 0; c++) if (!assigned[c]) bc = c;
+            for (int s2 = 0; s2 < 8 && bs < 0; s2++) if (child_in_slot[s2] < 0) bs = s2;
+        }
+        assigned[bc] = true;
+        child_in_slot[bs] = bc;
+    }
+    // classify, allocate
+    const int leaf_max = A.leaf_max;
+    uint32_t imask = 0, n_int = 0, n_tri = 0;
+    for (int s = 0; s < 8; s++) {
+        int c = child_in_slot[s];
+        if (c < 0) continue;
+        uint32_t cnt = ref_count(A, ch[c]);
+        if ((int)cnt > leaf_max) { imask |= 1u << s; n_int++; }
+        else n_tri += cnt;
+    }
+    uint32_t child_base = n_int ? atomicAdd(&A.counters[0], n_int) : 0u;
+    uint32_t tri_base = n_tri ? atomicAdd(&A.counters[1], n_tri) : 0u;
+    uint32_t qbase = n_int ? atomicAdd(&A.counters[2], n_int) : 0u;
+    // quantisation frame
+    WideNode node;
+    float scale[3];
+    int eb[3];
+    for (int a = 0; a < 3; a++) {
+        float ext = nb[3 + a] - nb[a];
+        int e;
+        if (ext > 0.0f) {
+            frexpf(ext / 252.0f, &e);  // 2^e >= ext / 252
+        } else {
+            e = A.e_min[a];
+        }
+        e = max(e, A.e_min[a]);
+        eb[a] = e;
+        scale[a] = ldexpf(1.0f, e);
+    }
+    node.px = nb[0] - scale[0];
+    node.py = nb[1] - scale[1];
+    node.pz = nb[2] - scale[2];
+    const float p[3] = {node.px, node.py, node.pz};
+    node.e_imask = (uint32_t)(eb[0] + 127) | ((uint32_t)(eb[1] + 127) << 8) | ((uint32_t)(eb[2] + 127) << 16) | (imask << 24);
+    node.child_base = child_base;
+    node.tri_base = tri_base;
+    uint8_t meta[8];
+    uint8_t qlo[3][8], qhi[3][8];
+    uint32_t int_rank = 0, tri_off = 0;
+    float sah = half_area(nb) * A.inv_root_area;
+    for (int s = 0; s < 8; s++) {
+        int c = child_in_slot[s];
+        if (c < 0) {
+            meta[s] = 0;
+            for (int a = 0; a < 3; a++) { qlo[a][s] = 255; qhi[a][s] = 0; }
+            continue;
+        }
+        for (int a = 0; a < 3; a++) {
+            float lo = floorf((cb[c][a] - p[a]) / scale[a]) - 1.0f;
+            float hi = ceilf((cb[c][3 + a] - p[a]) / scale[a]) + 1.0f;
+            qlo[a][s] = (uint8_t)fminf(fmaxf(lo, 0.0f), 255.0f);
+            qhi[a][s] = (uint8_t)fminf(fmaxf(hi, 0.0f), 255.0f);
+        }
+        uint32_t cnt = ref_count(A, ch[c]);
+        if (imask & (1u << s)) {
+            meta[s] = 0;
+            qout[qbase + int_rank] = make_uint2(ch[c], child_base + int_rank);
+            int_rank++;
+        } else {
+            meta[s] = (uint8_t)((((1u << cnt) - 1u) << 5) | tri_off);
+            uint32_t first = ref_first(A, ch[c]);
+            for (uint32_t k = 0; k < cnt; k++) {
+                uint32_t prim = A.vals[first + k];
+                const float* v = A.tri_verts + 9 * (size_t)prim;
+                WideTri t;
+                t.a = make_float4(v[0], v[1], v[2], __uint_as_float(prim));
+                t.b = make_float4(v[3], v[4], v[5], 0.0f);
+                t.c = make_float4(v[6], v[7], v[8], 0.0f);
+                A.tris[tri_base + tri_off + k] = t;
+            }
+            sah += half_area(cb[c]) * A.inv_root_area * (float)cnt;
+            tri_off += cnt;
+        }
+    }
+    node.meta_lo = meta[0] | (meta[1] << 8) | (meta[2] << 16) | ((uint32_t)meta[3] << 24);
+    node.meta_hi = meta[4] | (meta[5] << 8) | (meta[6] << 16) | ((uint32_t)meta[7] << 24);
+    for (int s = 0; s < 8; s++) {
+        node.qlo_x[s] = qlo[0][s]; node.qlo_y[s] = qlo[1][s]; node.qlo_z[s] = qlo[2][s];
+        node.qhi_x[s] = qhi[0][s]; node.qhi_y[s] = qhi[1][s]; node.qhi_z[s] = qhi[2][s];
+    }
+    A.nodes[widx] = node;
+    atomicAdd(A.sah, sah);
+}
+
+template <class T> cudaError_t dalloc(T** p, size_t count) { return cudaMalloc((void**)p, sizeof(T) * (count ? count : 1)); }
+
+}  // namespace
+
+lgb_status build_bvh(Scene* s, const lgb_build_opts* opts, lgb_build_stats* stats) {
+    Ctx* ctx = s->ctx;
+    const uint32_t n = s->num_tris;
+    int leaf_max = (opts && opts->leaf_max) ? (int)opts->leaf_max : 3;
+    if (leaf_max < 1 || leaf_max > 3) return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "leaf_max must be 1..3");
+    if (n == 0) return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "scene has no triangles");
+    cudaStream_t st = 0;
+    cudaEvent_t e0, e1;
+    LGB_CUDA_TRY(ctx, cudaEventCreate(&e0));
+    LGB_CUDA_TRY(ctx, cudaEventCreate(&e1));
+    LGB_CUDA_TRY(ctx, cudaEventRecord(e0, st));
+
+    // scratch
+    uint64_t *keys = nullptr, *keys2 = nullptr;
+    uint32_t *vals = nullptr, *vals2 = nullptr, *counts = nullptr, *bounds = nullptr;
+    uint32_t *left = nullptr, *right = nullptr, *pint = nullptr, *pleaf = nullptr, *rlo = nullptr, *rhi = nullptr, *flags = nullptr;
+    float *tri_box = nullptr, *node_box = nullptr, *sah = nullptr;
+    uint2 *qa = nullptr, *qb = nullptr;
+    uint32_t* counters = nullptr;
+    WideNode* nodes = nullptr;
+    WideTri* tris = nullptr;
+    const uint32_t nblocks = (n + RS_TILE - 1) / RS_TILE;
+    const uint32_t nint = n > 1 ? n - 1 : 1;
+    lgb_status status = LGB_OK;
+    auto fail = [&](cudaError_t e, const char* what) { status = cuda_error(ctx, e, what); };
+#define STEP(expr)                       \
+    do {                                 \
+        cudaError_t _e = (expr);         \
+        if (_e != cudaSuccess) { fail(_e, #expr); goto cleanup; } \
+    } while (0)
+    {
+        STEP(dalloc(&keys, n)); STEP(dalloc(&keys2, n)); STEP(dalloc(&vals, n)); STEP(dalloc(&vals2, n));
+        STEP(dalloc(&counts, (size_t)256 * nblocks)); STEP(dalloc(&bounds, 6));
+        STEP(dalloc(&left, nint)); STEP(dalloc(&right, nint)); STEP(dalloc(&pint, nint)); STEP(dalloc(&pleaf, n));
+        STEP(dalloc(&rlo, nint)); STEP(dalloc(&rhi, nint)); STEP(dalloc(&flags, nint));
+        STEP(dalloc(&tri_box, 6 * (size_t)n)); STEP(dalloc(&node_box, 6 * (size_t)nint)); STEP(dalloc(&sah, 1));
+        STEP(dalloc(&qa, nint + 1)); STEP(dalloc(&qb, nint + 1)); STEP(dalloc(&counters, 4));
+        STEP(dalloc(&nodes, nint)); STEP(dalloc(&tris, n));
+
+        uint32_t binit[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
+        STEP(cudaMemcpyAsync(bounds, binit, sizeof(binit), cudaMemcpyHostToDevice, st));
+        int grid = std::min<uint32_t>((n + 255) / 256, (uint32_t)ctx->sm_count * 8);
+        k_centroid_bounds<<<grid, 256, 0, st>>>(s->d_tri_verts, n, bounds);
+        k_morton<<<(n + 255) / 256, 256, 0, st>>>(s->d_tri_verts, n, bounds, keys, vals, tri_box);
+        STEP(cudaGetLastError());
+        for (int pass = 0; pass < 8; pass++) {
+            int shift = pass * 8;
+            k_rs_hist<<<nblocks, RS_THREADS, 0, st>>>(keys, n, shift, counts, nblocks);
+            k_scan_single<<<1, 1024, 0, st>>>(counts, 256 * nblocks);
+            k_rs_scatter<<<nblocks, RS_THREADS, 0, st>>>(keys, vals, keys2, vals2, n, shift, counts, nblocks);
+            std::swap(keys, keys2);
+            std::swap(vals, vals2);
+        }
+        STEP(cudaGetLastError());
+        uint32_t root_ref;
+        if (n > 1) {
+            k_radix_tree<<<(n - 1 + 255) / 256, 256, 0, st>>>(keys, (int)n, left, right, pint, pleaf, rlo, rhi);
+            STEP(cudaMemsetAsync(flags, 0, sizeof(uint32_t) * nint, st));
+            k_bottom_up<<<(n + 255) / 256, 256, 0, st>>>((int)n, vals, tri_box, left, right, pint, pleaf, node_box, flags);
+            STEP(cudaGetLastError());
+            root_ref = 0;
+        } else {
+            root_ref = kLeafFlag;
+        }
+        // root area for SAH statistics
+        float rb[6];
+        if (n > 1) {
+            STEP(cudaMemcpyAsync(rb, node_box, sizeof(rb), cudaMemcpyDeviceToHost, st));
+        } else {
+            STEP(cudaMemcpyAsync(rb, tri_box, sizeof(rb), cudaMemcpyDeviceToHost, st));
+        }
+        STEP(cudaStreamSynchronize(st));
+        float ra = fmaxf(rb[3] - rb[0], 0.f) * fmaxf(rb[4] - rb[1], 0.f) + fmaxf(rb[4] - rb[1], 0.f) * fmaxf(rb[5] - rb[2], 0.f) +
+                   fmaxf(rb[5] - rb[2], 0.f) * fmaxf(rb[3] - rb[0], 0.f);
+
+        CollapseArgs A;
+        A.left = left; A.right = right; A.range_lo = rlo; A.range_hi = rhi; A.node_box = node_box; A.tri_box = tri_box;
+        A.vals = vals; A.tri_verts = s->d_tri_verts; A.nodes = nodes; A.tris = tris; A.counters = counters; A.sah = sah;
+        A.leaf_max = leaf_max;
+        A.inv_root_area = ra > 0.0f ? 1.0f / ra : 0.0f;
+        // The minimum quantisation step keeps one step of margin above FP32 rounding of ray distances
+        // measured across the whole scene (about 2^-18 of the scene's largest extent).
+        float ext = fmaxf(fmaxf(s->bmax.x - s->bmin.x, s->bmax.y - s->bmin.y), s->bmax.z - s->bmin.z);
+        float mag = fmaxf(fmaxf(fmaxf(fabsf(s->bmin.x), fabsf(s->bmax.x)), fmaxf(fabsf(s->bmin.y), fabsf(s->bmax.y))),
+                          fmaxf(fabsf(s->bmin.z), fabsf(s->bmax.z)));
+        float ref = fmaxf(fmaxf(ext, mag), 1e-30f);
+        int eref;
+        frexpf(ref, &eref);
+        for (int a = 0; a < 3; a++) A.e_min[a] = std::max(eref - 18, -100);
+
+        uint32_t zero4[4] = {1u, 0u, 0u, 0u};  // node 0 = root already allocated
+        STEP(cudaMemcpyAsync(counters, zero4, sizeof(zero4), cudaMemcpyHostToDevice, st));
+        STEP(cudaMemsetAsync(sah, 0, sizeof(float), st));
+        uint2 root = make_uint2(root_ref, 0u);
+        STEP(cudaMemcpyAsync(qa, &root, sizeof(root), cudaMemcpyHostToDevice, st));
+        uint32_t qn = 1, depth = 0;
+        while (qn > 0) {
+            depth++;
+            if (depth > (uint32_t)kStackSize + 1u) {
+                status = set_error(ctx, LGB_ERR_UNSUPPORTED, "8-wide BVH deeper than the traversal stack");
+                goto cleanup;
+            }
+            STEP(cudaMemsetAsync(counters + 2, 0, sizeof(uint32_t), st));
+            k_collapse<<<(qn + 127) / 128, 128, 0, st>>>(A, qa, qn, qb);
+            STEP(cudaGetLastError());
+            STEP(cudaMemcpyAsync(&qn, counters + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+            STEP(cudaStreamSynchronize(st));
+            std::swap(qa, qb);
+        }
+        uint32_t hc[4];
+        float hsah = 0.0f;
+        STEP(cudaMemcpy(hc, counters, sizeof(hc), cudaMemcpyDeviceToHost));
+        STEP(cudaMemcpy(&hsah, sah, sizeof(float), cudaMemcpyDeviceToHost));
+        if (hc[1] != n) {
+            status = set_error(ctx, LGB_ERR_DEVICE_STATUS, "BVH collapse wrote an unexpected triangle count");
+            goto cleanup;
+        }
+        // shrink the node array to its used size
+        WideNode* tight = nullptr;
+        STEP(dalloc(&tight, hc[0]));
+        STEP(cudaMemcpyAsync(tight, nodes, sizeof(WideNode) * hc[0], cudaMemcpyDeviceToDevice, st));
+        STEP(cudaEventRecord(e1, st));
+        STEP(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaFree(nodes);
+        nodes = nullptr;
+        if (s->bvh.nodes) cudaFree(s->bvh.nodes);
+        if (s->bvh.tris) cudaFree(s->bvh.tris);
+        s->bvh.nodes = tight;
+        s->bvh.tris = tris;
+        tris = nullptr;
+        s->bvh.num_nodes = hc[0];
+        s->bvh.num_tris = n;
+        s->bvh.max_depth = depth;
+        if (stats) {
+            std::memset(stats, 0, sizeof(*stats));
+            stats->build_ms = ms;
+            stats->num_tris = n;
+            stats->num_nodes = hc[0];
+            stats->max_depth = depth;
+            stats->node_bytes = (uint64_t)hc[0] * sizeof(WideNode);
+            stats->tri_bytes = (uint64_t)n * sizeof(WideTri);
+            stats->sah_cost = hsah;
+        }
+    }
+cleanup:
+#undef STEP
+    cudaFree(keys); cudaFree(keys2); cudaFree(vals); cudaFree(vals2); cudaFree(counts); cudaFree(bounds);
+    cudaFree(left); cudaFree(right); cudaFree(pint); cudaFree(pleaf); cudaFree(rlo); cudaFree(rhi); cudaFree(flags);
+    cudaFree(tri_box); cudaFree(node_box); cudaFree(sah); cudaFree(qa); cudaFree(qb); cudaFree(counters);
+    if (nodes) cudaFree(nodes);
+    if (tris) cudaFree(tris);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return status;
+}
+
+}  // namespace lgb

@@ -1,0 +1,130 @@
+// Internal definitions shared by the CUDA translation units of liblgb.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "lgb.h"
+
+namespace lgb {
+
+// Entries of the per-thread traversal stack; a tree deeper than kStackSize + 1 levels is rejected.
+constexpr int kStackSize = 48;
+
+// ---------------------------------------------------------------------------------------------
+// 8-wide BVH node, 80 bytes = five 16-byte loads.
+//   chunk 0: px, py, pz (quantisation origin), e_imask = ex | ey << 8 | ez << 16 | imask << 24
+//            (exponent bytes are biased by 127: the step along axis a is 2^(e_a - 127))
+//   chunk 1: child_base, tri_base, meta[0..3], meta[4..7]
+//   chunk 2: qlo_x[8], qlo_y[8]
+//   chunk 3: qlo_z[8], qhi_x[8]
+//   chunk 4: qhi_y[8], qhi_z[8]
+// Slot s holds the child whose centre lies in octant s of the node (bit a of s set = positive side on
+// axis a), so a ray visits children front to back by ranking slots with s ^ octant mask.
+// imask bit s: slot s is an internal node, at child_base + popc(imask & ((1 << s) - 1)).
+// meta[s] of a leaf slot: bits 0-4 = first triangle offset from tri_base, bits 5-7 = unary count
+// (1 -> 0b001, 2 -> 0b011, 3 -> 0b111). Empty slots have meta 0 and an inverted box (qlo 255, qhi 0).
+// Quantised boxes are rounded outwards with one extra step on every side, so they strictly contain the
+// exact child boxes.
+// ---------------------------------------------------------------------------------------------
+struct __align__(16) WideNode {
+    float px, py, pz;
+    uint32_t e_imask;
+    uint32_t child_base, tri_base;
+    uint32_t meta_lo, meta_hi;
+    uint8_t qlo_x[8], qlo_y[8], qlo_z[8];
+    uint8_t qhi_x[8], qhi_y[8], qhi_z[8];
+};
+static_assert(sizeof(WideNode) == 80, "WideNode must be 80 bytes");
+
+// Triangle in leaf order, 48 bytes = three 16-byte loads: (v0, prim), (v1, 0), (v2, 0).
+struct __align__(16) WideTri {
+    float4 a, b, c;
+};
+static_assert(sizeof(WideTri) == 48, "WideTri must be 48 bytes");
+
+// Vertex as ray.rchit reads it (commons.h:194-198): position, normal, uv.
+struct DevVertex {
+    float px, py, pz;
+    float nx, ny, nz;
+    float u, v;
+};
+
+struct DevTexture {
+    uint32_t width, height;
+    const float4* texels;
+};
+
+// Device status word bits.
+enum : uint32_t {
+    STATUS_STACK_OVERFLOW = 1u << 0,
+    STATUS_BAD_INDEX = 1u << 1,
+    STATUS_VISIT_LIMIT = 1u << 2,  // a ray visited more nodes than any well-formed tree allows
+};
+
+// Upper bound on node visits of one ray: far above any real query, it only stops a malformed tree from
+// looping.
+constexpr uint32_t kMaxVisits = 1u << 22;
+
+struct Scene;
+
+struct Ctx {
+    int device = 0;
+    std::string last_error;
+    int sm_count = 0;
+};
+
+struct BvhDevice {
+    WideNode* nodes = nullptr;
+    WideTri* tris = nullptr;
+    uint32_t num_nodes = 0;
+    uint32_t num_tris = 0;
+    uint32_t max_depth = 0;
+};
+
+struct Scene {
+    Ctx* ctx = nullptr;
+    uint32_t num_tris = 0;
+    uint32_t num_vertices = 0;
+    float3 bmin, bmax;           // scene bounds
+    float* d_tri_verts = nullptr;  // 9 floats per global triangle (world space)
+    DevVertex* d_vertices = nullptr;
+    uint32_t* d_indices = nullptr;
+    uint32_t* d_tri_mesh = nullptr;  // global triangle -> mesh
+    lgb_mesh* d_meshes = nullptr;
+    uint32_t* d_mesh_first_tri = nullptr;
+    lgb_material* d_materials = nullptr;
+    lgb_light* d_lights = nullptr;
+    DevTexture* d_textures = nullptr;
+    std::vector<void*> texture_buffers;
+    uint32_t num_meshes = 0, num_materials = 0, num_lights = 0, num_textures = 0;
+    std::vector<uint32_t> h_mesh_first_tri;
+    std::vector<lgb_mesh> h_meshes;
+    BvhDevice bvh;
+    uint32_t* d_status = nullptr;  // device status word
+    // path-tracer work buffers (grown on demand)
+    void* pt_buf = nullptr;
+    size_t pt_buf_bytes = 0;
+};
+
+// Error helpers: record a message on the context and return a status.
+lgb_status set_error(Ctx* ctx, lgb_status st, const std::string& msg);
+lgb_status cuda_error(Ctx* ctx, cudaError_t e, const char* what);
+
+#define LGB_CUDA_TRY(ctx, expr)                                          \
+    do {                                                                 \
+        cudaError_t _e = (expr);                                         \
+        if (_e != cudaSuccess) return ::lgb::cuda_error((ctx), _e, #expr); \
+    } while (0)
+
+// Entry points implemented per translation unit.
+lgb_status build_bvh(Scene* s, const lgb_build_opts* opts, lgb_build_stats* stats);
+lgb_status launch_trace_closest(Scene* s, const lgb_ray* rays, lgb_hit* hits, uint32_t n, cudaStream_t st,
+                                uint64_t* counters);
+lgb_status launch_trace_any(Scene* s, const lgb_ray* rays, uint32_t* bits, uint32_t n, cudaStream_t st);
+lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* p, uint32_t frame0, uint32_t spp,
+                       float* film, cudaStream_t st);
+
+}  // namespace lgb

@@ -1,0 +1,648 @@
+// Wavefront unidirectional MIS path tracer (the Path integrator).
+//
+// Restates src/shaders/integrators/path/path.rgen:22-113 and pt_commons.glsl:3-48 as a sequence of
+// kernels over path state kept as structure-of-arrays in HBM:
+//   k_camera          path.rgen:28-46   one path per (pixel, frame), jittered camera ray
+//   k_q_trace_closest path.rgen:48      continuation rays of the live queue
+//   k_classify        path.rgen:49-55   misses add the sky and end; hits are binned by material class
+//   k_shade<CLASS>    path.rgen:56-100  ray.rchit hit resolve, emission, NEE light sample + shadow ray,
+//                                       BSDF-MIS ray, BSDF sample, throughput, Russian roulette, enqueue
+//   k_q_trace_any / k_q_trace_closest   shadow and BSDF-MIS rays (pt_commons.glsl:21,32)
+//   k_nee_resolve     pt_commons.glsl:20-41 combination of the two light-sampling strategies
+//   k_film            path.rgen:102-112 NaN drop and progressive mean, frames in order
+// Every kernel reads its work count from device memory, so one render issues no host synchronisation.
+// Queues are compacted with warp-aggregated atomics. RNG state is the counter-based PCG4D seed
+// (x, y, frame, w): a path carries only w. Compiled with -fmad=false to keep the shader's FP32 sequence.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "bsdf.cuh"
+#include "lgb_internal.cuh"
+#include "traverse.cuh"
+
+namespace lgb {
+namespace {
+using namespace sh;
+
+constexpr float kTMin = 0.001f;    // path.rgen:19
+constexpr float kTMax = 10000.0f;  // path.rgen:20
+constexpr float kEps = 0.001f;     // utils.glsl:8
+constexpr int kRRMinDepth = 3;     // path.rgen:21
+constexpr uint32_t kMaxPaths = 1u << 21;
+constexpr int kThreads = 128;
+
+enum MatClass { CLS_DIFFUSE = 0, CLS_CONDUCTOR = 1, CLS_SPECULAR = 2, CLS_PRINCIPLED = 3, NUM_CLS = 4 };
+
+// NEE record: the light-sampling state that pt_commons.glsl keeps in registers across its two traces.
+struct __align__(16) NeeRec {
+    float4 term1;   // xyz: mis * f * |cos| * Le / pdf_w of the light sample; w: pdf_pos_w
+    float4 T;       // xyz: throughput at the shading point; w: light_pick_pdf
+    float4 f2;      // xyz: BSDF-MIS sample value; w: its pdf (0 = no MIS ray)
+    float4 m;       // x: |cos| of the MIS sample, y: light pdf_pos_a, z: light prim (bits), w: flags (bits)
+    float4 Le;      // xyz: light radiance, w: path id (bits)
+    float4 pos;     // xyz: shading position; w: shading prim (bits)
+    float4 ns;      // xyz: shading normal as the hit payload holds it (not face-forwarded); w unused
+    float4 wi2;     // xyz: BSDF-MIS direction
+};
+enum : uint32_t { NEE_AREA = 1u };
+
+struct Buffers {
+    uint32_t* pix;      // pixel index
+    uint32_t* frame;
+    uint32_t* w;        // RNG counter
+    uint32_t* flags;    // bits 0-15 depth, bit 16 last_specular
+    float4* T;          // throughput
+    float4* col;        // radiance
+    uint32_t* q_cur;
+    uint32_t* q_next;
+    uint32_t* q_cls;    // NUM_CLS * cap: queue positions binned by material class
+    lgb_ray* rays;       // rays of the current queue
+    lgb_ray* rays_next;  // continuation rays being enqueued
+    lgb_hit* hits;
+    NeeRec* nee;
+    lgb_ray* srays;
+    lgb_ray* mrays;
+    lgb_hit* mhits;
+    uint32_t* sbits;
+    uint32_t* counters; // [0] cur, [1] next, [2] nee, [3..6] class counts
+};
+
+struct Params {
+    float iv[16], ip[16];
+    uint32_t width, height, npix;
+    float sky[3];
+    int max_depth, num_lights, light_tri_count;
+    uint32_t direct_lighting, film_mode;
+    uint32_t frame0;   // first frame of this chunk
+    uint32_t nframes;  // frames in this chunk
+    uint32_t cap;      // path capacity of the buffers
+};
+
+struct SceneView {
+    const WideNode* nodes;
+    const WideTri* tris;
+    const DevVertex* verts;
+    const uint32_t* idx;
+    const uint32_t* tri_mesh;
+    const lgb_mesh* meshes;
+    const uint32_t* mesh_first;
+    const lgb_material* mats;
+    const lgb_light* lights;
+    const DevTexture* texs;
+    uint32_t* status;
+};
+
+__device__ __forceinline__ uint32_t agg_slot(uint32_t* ctr, bool pred) {
+    const uint32_t m = __ballot_sync(0xffffffffu, pred);
+    const int lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (lane == 0 && m) base = atomicAdd(ctr, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    return base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ v3 f3(float4 a) { return V3(a.x, a.y, a.z); }
+__device__ __forceinline__ float4 f4(v3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
+__device__ __forceinline__ lgb_ray make_ray(v3 o, float tmin, v3 d, float tmax) {
+    lgb_ray r;
+    r.ox = o.x; r.oy = o.y; r.oz = o.z; r.tmin = tmin;
+    r.dx = d.x; r.dy = d.y; r.dz = d.z; r.tmax = tmax;
+    return r;
+}
+__device__ __forceinline__ void store_ray(lgb_ray* dst, const lgb_ray& r) {
+    float4* p = reinterpret_cast<float4*>(dst);
+    p[0] = make_float4(r.ox, r.oy, r.oz, r.tmin);
+    p[1] = make_float4(r.dx, r.dy, r.dz, r.tmax);
+}
+__device__ __forceinline__ uint4 seed_of(uint32_t pix, uint32_t width, uint32_t frame, uint32_t w) {
+    return make_uint4(pix % width, pix / width, frame, w);
+}
+
+// GLSL mat4 * vec4 on column-major storage, summed over columns in order.
+__device__ __forceinline__ float4 mat_vec(const float* m, float x, float y, float z, float w) {
+    float r[4];
+#pragma unroll
+    for (int row = 0; row < 4; row++) r[row] = m[row] * x + m[4 + row] * y + m[8 + row] * z + m[12 + row] * w;
+    return make_float4(r[0], r[1], r[2], r[3]);
+}
+
+// Bilinear REPEAT lookup at LOD 0 in linear FP32.
+__device__ __forceinline__ v3 tex_lookup(const DevTexture& t, float u, float v) {
+    if (!isfinite(u) || !isfinite(v)) { u = 0.0f; v = 0.0f; }  // keep the wrap arithmetic in range
+    const float x = u * (float)t.width - 0.5f, y = v * (float)t.height - 0.5f;
+    const float x0 = floorf(x), y0 = floorf(y);
+    const float fx = x - x0, fy = y - y0;
+    const long long W = t.width, H = t.height;
+    long long ix = (long long)x0 % W; if (ix < 0) ix += W;
+    long long iy = (long long)y0 % H; if (iy < 0) iy += H;
+    const long long ix1 = (ix + 1) % W, iy1 = (iy + 1) % H;
+    const float4 c00 = t.texels[iy * W + ix], c10 = t.texels[iy * W + ix1];
+    const float4 c01 = t.texels[iy1 * W + ix], c11 = t.texels[iy1 * W + ix1];
+    const float w00 = (1.0f - fx) * (1.0f - fy), w10 = fx * (1.0f - fy), w01 = (1.0f - fx) * fy, w11 = fx * fy;
+    return f3(c00) * w00 + f3(c10) * w10 + f3(c01) * w01 + f3(c11) * w11;
+}
+
+// ray.rchit:24-84 for an identity object-to-world transform: the matrix products reduce to their
+// arguments while the second normalisation of the shading normal is kept.
+struct HitAttr {
+    v3 n_g, n_s, pos;
+    float u, v;
+    uint32_t mat;
+};
+__device__ __forceinline__ HitAttr resolve_hit(const SceneView& S, uint32_t prim, float bu, float bv) {
+    HitAttr h;
+    const uint32_t mesh = S.tri_mesh[prim];
+    const lgb_mesh pm = S.meshes[mesh];
+    const uint32_t local = prim - S.mesh_first[mesh];
+    const uint32_t io = pm.index_offset + 3u * local;
+    const DevVertex a = S.verts[S.idx[io] + pm.vertex_offset];
+    const DevVertex b = S.verts[S.idx[io + 1] + pm.vertex_offset];
+    const DevVertex c = S.verts[S.idx[io + 2] + pm.vertex_offset];
+    const float b0 = 1.0f - bu - bv, b1 = bu, b2 = bv;
+    const v3 v0 = V3(a.px, a.py, a.pz), v1 = V3(b.px, b.py, b.pz), v2 = V3(c.px, c.py, c.pz);
+    const v3 n0 = V3(a.nx, a.ny, a.nz), n1 = V3(b.nx, b.ny, b.nz), n2 = V3(c.nx, c.ny, c.nz);
+    h.pos = v0 * b0 + v1 * b1 + v2 * b2;
+    h.n_s = normalize(normalize(n0 * b0 + n1 * b1 + n2 * b2));
+    h.u = a.u * b0 + b.u * b1 + c.u * b2;
+    h.v = a.v * b0 + b.v * b1 + c.v * b2;
+    h.n_g = normalize(cross(v2 - v0, v1 - v0));
+    h.mat = pm.material_index;
+    return h;
+}
+
+__device__ __forceinline__ Mat load_material(const SceneView& S, uint32_t idx, float u, float v) {
+    Mat m = load_mat(&S.mats[idx]);
+    const int tid = S.mats[idx].texture_id;
+    if (tid > -1) m.albedo = m.albedo * tex_lookup(S.texs[tid], u, v);
+    return m;
+}
+
+__device__ __forceinline__ int class_of(uint32_t bsdf_type) {
+    switch (bsdf_type) {
+        case LGB_BSDF_DIFFUSE: return CLS_DIFFUSE;
+        case LGB_BSDF_CONDUCTOR: return CLS_CONDUCTOR;
+        case LGB_BSDF_PRINCIPLED: return CLS_PRINCIPLED;
+        default: return CLS_SPECULAR;
+    }
+}
+
+
+// ---------------- kernels ----------------
+
+// path.rgen:22-46: the seed is (x, y, frame, 0); two draws jitter the pixel.
+__global__ void __launch_bounds__(kThreads) k_camera(Params P, Buffers B) {
+    const uint32_t n = P.npix * P.nframes;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t pix = i % P.npix, f = P.frame0 + i / P.npix;
+        const uint32_t x = pix % P.width, y = pix / P.width;
+        uint4 seed = make_uint4(x, y, f, 0u);
+        const float px = (float)x + 0.5f, py = (float)y + 0.5f;
+        const float r0 = rnd(seed) - 0.5f;
+        const float r1 = rnd(seed) - 0.5f;
+        const float u = (px + r0) / (float)P.width, v = (py + r1) / (float)P.height;
+        const float dx = u * 2.0f - 1.0f, dy = v * 2.0f - 1.0f;
+        const float4 origin = mat_vec(P.iv, 0.0f, 0.0f, 0.0f, 1.0f);
+        const float4 target = mat_vec(P.ip, dx, dy, 1.0f, 1.0f);
+        const v3 tn = normalize(V3(target.x, target.y, target.z));
+        const float4 dir = mat_vec(P.iv, tn.x, tn.y, tn.z, 0.0f);
+        B.pix[i] = pix;
+        B.frame[i] = f;
+        B.w[i] = seed.w;
+        B.flags[i] = 0u;
+        B.T[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        B.col[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        B.q_cur[i] = i;
+        store_ray(&B.rays[i], make_ray(V3(origin.x, origin.y, origin.z), kTMin, V3(dir.x, dir.y, dir.z), kTMax));
+    }
+}
+
+// Closest-hit over a device-counted queue of rays.
+__global__ void __launch_bounds__(kThreads) k_q_trace_closest(SceneView S, const lgb_ray* __restrict__ rays,
+                                                              lgb_hit* __restrict__ hits, const uint32_t* count_ptr) {
+    const uint32_t n = *count_ptr;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 r0 = ldg4f(&rays[i].ox), r1 = ldg4f(&rays[i].dx);
+        const RayQ r = make_rayq(r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w);
+        uint4 out = make_uint4(LGB_NO_HIT, 0u, 0u, 0u);
+        if (r0.w <= r1.w) {
+            float t, u, v;
+            uint32_t nn = 0, nt = 0;
+            const uint32_t prim = trace_closest_dev<false>(S.nodes, S.tris, r, t, u, v, S.status, nn, nt);
+            if (prim != LGB_NO_HIT) out = make_uint4(prim, __float_as_uint(t), __float_as_uint(u), __float_as_uint(v));
+        }
+        reinterpret_cast<uint4*>(hits)[i] = out;
+    }
+}
+
+// Any-hit over a device-counted queue; bit (i & 31) of bits[i >> 5] = occluded.
+__global__ void __launch_bounds__(kThreads) k_q_trace_any(SceneView S, const lgb_ray* __restrict__ rays,
+                                                          uint32_t* __restrict__ bits, const uint32_t* count_ptr) {
+    const uint32_t n = *count_ptr;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        bool occ = false;
+        if (i < n) {
+            const float4 r0 = ldg4f(&rays[i].ox), r1 = ldg4f(&rays[i].dx);
+            if (r0.w <= r1.w) {
+                const RayQ r = make_rayq(r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w);
+                occ = trace_any_dev(S.nodes, S.tris, r, S.status);
+            }
+        }
+        const uint32_t word = __ballot_sync(0xffffffffu, occ);
+        if ((threadIdx.x & 31) == 0 && i < n) bits[i >> 5] = word;
+    }
+}
+
+// path.rgen:49-55: a miss adds the sky colour (shade_atmosphere without a directional light returns
+// sky_col, commons.glsl:157-159) and ends the path; hits are binned by material class.
+__global__ void __launch_bounds__(kThreads) k_classify(SceneView S, Params P, Buffers B) {
+    const uint32_t n = B.counters[0];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        int cls = -1;
+        if (i < n) {
+            const uint32_t prim = B.hits[i].prim;
+            if (prim == LGB_NO_HIT) {
+                const uint32_t p = B.q_cur[i];
+                const uint32_t depth = B.flags[p] & 0xffffu;
+                if (depth > 0 || P.direct_lighting == 1u) {
+                    const float4 T = B.T[p];
+                    float4 c = B.col[p];
+                    c.x = c.x + T.x * P.sky[0];
+                    c.y = c.y + T.y * P.sky[1];
+                    c.z = c.z + T.z * P.sky[2];
+                    B.col[p] = c;
+                }
+            } else {
+                cls = class_of(S.mats[S.meshes[S.tri_mesh[prim]].material_index].bsdf_type);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < NUM_CLS; c++) {
+            const uint32_t slot = agg_slot(&B.counters[3 + c], cls == c);
+            if (cls == c) B.q_cls[(size_t)c * P.cap + slot] = i;
+        }
+    }
+}
+
+// Restricted BSDF dispatch per material class, so each shading kernel compiles only its own lobes.
+template <int CLS>
+__device__ __forceinline__ v3 cls_sample(v3 n_s, v3 wo, const Mat& m, bool ff, v3& wi, float& pdf, float& cos_t, v3 r) {
+    if (CLS == CLS_DIFFUSE) {
+        v3 T, B;
+        branchless_onb(n_s, T, B);
+        const v3 wl = to_local(wo, T, B, n_s);
+        v3 wil;
+        const v3 f = sample_diffuse(m, wl, wil, pdf, cos_t, V2(r.x, r.y));
+        wi = to_world(wil, T, B, n_s);
+        return f;
+    }
+    return sample_bsdf(n_s, wo, m, ff, wi, pdf, cos_t, r);
+}
+template <int CLS>
+__device__ __forceinline__ v3 cls_eval(v3 n_s, v3 wo, const Mat& m, bool ff, v3 wi, float& pdf) {
+    if (CLS == CLS_DIFFUSE) {
+        v3 T, B;
+        branchless_onb(n_s, T, B);
+        return eval_diffuse(m, to_local(wo, T, B, n_s), to_local(wi, T, B, n_s), pdf);
+    }
+    return eval_bsdf(n_s, wo, m, ff, wi, pdf);
+}
+
+// One bounce of path.rgen:56-100 for the hits of one material class.
+template <int CLS>
+__global__ void __launch_bounds__(kThreads) k_shade(SceneView S, Params P, Buffers B, int depth) {
+    const uint32_t n = B.counters[3 + CLS];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t* list = B.q_cls + (size_t)CLS * P.cap;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+        const uint32_t k = base + threadIdx.x;
+        bool cont = false, nee = false;
+        uint32_t p = 0;
+        lgb_ray next_ray, sray, mray;
+        NeeRec rec;
+        if (k < n) {
+            const uint32_t qi = list[k];
+            p = B.q_cur[qi];
+            const lgb_hit hit = B.hits[qi];
+            const lgb_ray ray = B.rays[qi];
+            const uint32_t pix = B.pix[p], frame = B.frame[p];
+            uint4 seed = seed_of(pix, P.width, frame, B.w[p]);
+            const uint32_t fl = B.flags[p];
+            const bool last_specular = (fl >> 16) & 1u;
+            v3 T = f3(B.T[p]);
+            v3 col = f3(B.col[p]);
+            const HitAttr h = resolve_hit(S, hit.prim, hit.u, hit.v);
+            const Mat m = load_material(S, h.mat, h.u, h.v);
+            if ((depth == 0 && P.direct_lighting == 1u) || last_specular) col = col + T * m.emissive;
+            if (depth < P.max_depth - 1) {
+                const v3 direction = V3(ray.dx, ray.dy, ray.dz);
+                const v3 wo = -direction;
+                v3 n_s = h.n_s;
+                bool side = true;
+                v3 n_g = h.n_g;
+                if (dot(h.n_g, wo) < 0.0f) n_g = -n_g;
+                if (dot(n_g, h.n_s) < 0.0f) { n_s = -n_s; side = false; }
+                const v3 origin = offset_ray(h.pos, n_g);
+                const bool spec = has_prop(m.props, LGB_FLAG_SPECULAR);
+                if (!spec && (depth > 0 || P.direct_lighting == 1u) && P.num_lights <= 0) {
+                    // No light to sample: Lumen would read past its light buffer; here the four draws are
+                    // consumed and nothing is added.
+                    for (int k = 0; k < 4; k++) (void)rnd(seed);
+                } else if (!spec && (depth > 0 || P.direct_lighting == 1u)) {
+                    // uniform_sample_light (pt_commons.glsl:3-42) and sample_light_Li (commons.glsl:224-300)
+                    nee = true;
+                    const float lpp = 1.0f / (float)P.light_tri_count;
+                    const float q0 = rnd(seed), q1 = rnd(seed), q2 = rnd(seed), q3 = rnd(seed);
+                    const uint32_t li = (uint32_t)(q0 * (float)P.num_lights);
+                    const lgb_light* L = &S.lights[li];
+                    const uint32_t lflags = L->light_flags, ltype = lflags & 7u;
+                    v3 Le = V3(0.0f), wi = V3(0.0f);
+                    float wi_len = 0.0f, pdf_w = 0.0f, pdf_a = 0.0f;
+                    uint32_t lprim = LGB_NO_HIT;
+                    if (ltype == LGB_LIGHT_AREA) {
+                        const lgb_mesh pm = S.meshes[L->prim_mesh_idx];
+                        const uint32_t tri = (uint32_t)(q1 * (float)L->num_triangles);
+                        lprim = S.mesh_first[L->prim_mesh_idx] + tri;
+                        const uint32_t io = pm.index_offset + 3u * tri;
+                        const DevVertex a = S.verts[S.idx[io] + pm.vertex_offset];
+                        const DevVertex b = S.verts[S.idx[io + 1] + pm.vertex_offset];
+                        const DevVertex c = S.verts[S.idx[io + 2] + pm.vertex_offset];
+                        const float su = 1.0f - sqrtf(q2), sv = q3 * sqrtf(q2);
+                        const float b0 = 1.0f - su - sv;
+                        const v3 v0 = V3(a.px, a.py, a.pz), v1 = V3(b.px, b.py, b.pz), v2 = V3(c.px, c.py, c.pz);
+                        const v3 et0 = v1 - v0, et1 = v2 - v0;
+                        const v3 lpos = v0 * b0 + v1 * su + v2 * sv;
+                        const v3 ln = normalize(normalize(V3(a.nx, a.ny, a.nz) * b0 + V3(b.nx, b.ny, b.nz) * su +
+                                                          V3(c.nx, c.ny, c.nz) * sv));
+                        const float tri_pdf = 2.0f / length(cross(et0, et1));
+                        const lgb_material* lm = &S.mats[pm.material_index];
+                        Le = V3(lm->emissive_factor[0], lm->emissive_factor[1], lm->emissive_factor[2]);
+                        wi = lpos - h.pos;
+                        const float l2 = dot(wi, wi);
+                        wi_len = sqrtf(l2);
+                        wi = wi / wi_len;
+                        const float cfl = fabsf(dot(ln, -wi));
+                        pdf_a = tri_pdf;
+                        pdf_w = pdf_a * l2 / cfl;
+                    } else if (ltype == LGB_LIGHT_SPOT) {
+                        const v3 lp = V3(L->pos[0], L->pos[1], L->pos[2]);
+                        wi = lp - h.pos;
+                        const float l2 = dot(wi, wi);
+                        wi_len = sqrtf(l2);
+                        wi = wi / wi_len;
+                        const v3 ldir = normalize(V3(L->to[0], L->to[1], L->to[2]) - lp);
+                        const float cfl = dot(-wi, ldir);
+                        const float cw = cosf(LGB_PI / 6.0f), cf = cosf(25.0f * LGB_PI / 180.0f);
+                        float fall;
+                        if (cfl < cw) fall = 0.0f;
+                        else if (cfl >= cf) fall = 1.0f;
+                        else { const float d = (cfl - cw) / (cf - cw); fall = (d * d) * (d * d); }
+                        pdf_a = 1.0f;
+                        pdf_w = l2;
+                        Le = V3(L->L[0], L->L[1], L->L[2]) * fall;
+                    } else {
+                        const v3 dir = normalize(V3(L->pos[0], L->pos[1], L->pos[2]) - V3(L->to[0], L->to[1], L->to[2]));
+                        const v3 lp = h.pos + dir * (2.0f * L->world_radius);
+                        wi = lp - h.pos;
+                        wi_len = length(wi);
+                        wi = wi / wi_len;
+                        pdf_a = 1.0f;
+                        pdf_w = 1.0f;
+                        Le = V3(L->L[0], L->L[1], L->L[2]);
+                    }
+                    const v3 sp = offset_ray2(h.pos, n_s);
+                    float bsdf_pdf;
+                    const float cos_x = dot(n_s, wi);
+                    const v3 f = cls_eval<CLS>(n_s, wo, m, side, wi, bsdf_pdf);
+                    v3 term1 = V3(0.0f);
+                    if (pdf_w > 0.0f) {
+                        const float mis = ((lflags >> 5) & 1u) ? 1.0f : 1.0f / (1.0f + bsdf_pdf / pdf_w);
+                        term1 = mis * f * fabsf(cos_x) * Le / pdf_w;
+                    }
+                    // The shadow ray only matters when the light sample can contribute.
+                    sray = make_ray(sp, 0.0f, wi, pdf_w > 0.0f ? wi_len - kEps : -1.0f);
+                    v3 f2 = V3(0.0f), wi2 = V3(0.0f);
+                    float pdf2 = 0.0f, cos2 = 0.0f;
+                    if (ltype == LGB_LIGHT_AREA) {
+                        const float b0r = rnd(seed), b1r = rnd(seed), b2r = rnd(seed);
+                        f2 = cls_sample<CLS>(n_s, wo, m, side, wi2, pdf2, cos2, V3(b0r, b1r, b2r));
+                    }
+                    mray = make_ray(sp, kTMin, wi2, pdf2 != 0.0f ? kTMax : -1.0f);
+                    rec.term1 = f4(term1, pdf_w);
+                    rec.T = f4(T, lpp);
+                    rec.f2 = f4(f2, pdf2);
+                    rec.m = make_float4(fabsf(cos2), pdf_a, __uint_as_float(lprim),
+                                        __uint_as_float(ltype == LGB_LIGHT_AREA ? NEE_AREA : 0u));
+                    rec.Le = f4(Le, __uint_as_float(p));
+                    rec.pos = f4(h.pos, __uint_as_float(hit.prim));
+                    rec.ns = f4(h.n_s, 0.0f);
+                    rec.wi2 = f4(wi2, 0.0f);
+                }
+                float pdf, cos_t;
+                v3 dir_next;
+                const float c0 = rnd(seed), c1 = rnd(seed), c2 = rnd(seed);
+                const v3 f = cls_sample<CLS>(n_s, wo, m, side, dir_next, pdf, cos_t, V3(c0, c1, c2));
+                if (pdf != 0.0f) {
+                    T = T * (f * fabsf(cos_t) / pdf);
+                    float rr_scale = 1.0f;
+                    if (has_prop(m.props, LGB_FLAG_TRANSMISSION)) rr_scale *= side ? 1.0f / m.ior : m.ior;
+                    cont = true;
+                    if (depth > kRRMinDepth) {
+                        const float rr = fminf(0.95f, luminance(T) * rr_scale);
+                        if (rr == 0.0f || rr < rnd(seed)) cont = false;
+                        else T = T / rr;
+                    }
+                    next_ray = make_ray(origin, kTMin, dir_next, kTMax);
+                }
+                B.flags[p] = (uint32_t)(depth + 1) | (spec ? (1u << 16) : 0u);
+            }
+            B.w[p] = seed.w;
+            B.T[p] = f4(T, 0.0f);
+            B.col[p] = f4(col, 0.0f);
+        }
+        const uint32_t cslot = agg_slot(&B.counters[1], cont);
+        if (cont) {
+            B.q_next[cslot] = p;
+            store_ray(&B.rays_next[cslot], next_ray);
+        }
+        const uint32_t nslot = agg_slot(&B.counters[2], nee);
+        if (nee) {
+            B.nee[nslot] = rec;
+            store_ray(&B.srays[nslot], sray);
+            store_ray(&B.mrays[nslot], mray);
+        }
+    }
+}
+
+// pt_commons.glsl:20-41 after both traces: combine the light sample (if unoccluded) with the BSDF-MIS
+// sample (if it hit the sampled light triangle), then col += T * res / light_pick_pdf (path.rgen:78).
+// A missed MIS ray leaves the previous closest-hit payload in place (ray.rmiss:13 only marks the
+// material), so the comparison then uses the shading point's own triangle, position and normal.
+__global__ void __launch_bounds__(kThreads) k_nee_resolve(SceneView S, Buffers B) {
+    const uint32_t n = B.counters[2];
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const NeeRec rec = B.nee[r];
+        const uint32_t p = __float_as_uint(rec.Le.w);
+        const bool occluded = (B.sbits[r >> 5] >> (r & 31)) & 1u;
+        v3 res = V3(0.0f);
+        if (!occluded && rec.term1.w > 0.0f) res = res + f3(rec.term1);
+        const uint32_t flags = __float_as_uint(rec.m.w);
+        const float pdf2 = rec.f2.w;
+        if ((flags & NEE_AREA) && pdf2 != 0.0f) {
+            const lgb_hit mh = B.mhits[r];
+            const uint32_t lprim = __float_as_uint(rec.m.z);
+            const uint32_t pl_prim = mh.prim == LGB_NO_HIT ? __float_as_uint(rec.pos.w) : mh.prim;
+            if (pl_prim == lprim) {
+                v3 pl_pos, pl_ns;
+                if (mh.prim == LGB_NO_HIT) {
+                    pl_pos = f3(rec.pos);
+                    pl_ns = f3(rec.ns);
+                } else {
+                    const HitAttr h = resolve_hit(S, mh.prim, mh.u, mh.v);
+                    pl_pos = h.pos;
+                    pl_ns = h.n_s;
+                }
+                const v3 wi2 = f3(rec.wi2);
+                const float wl = length(pl_pos - f3(rec.pos));
+                const float g = fabsf(dot(pl_ns, -wi2)) / (wl * wl);
+                const float mis = 1.0f / (1.0f + rec.m.y / (g * pdf2));
+                res = res + f3(rec.f2) * mis * rec.m.x * f3(rec.Le) / pdf2;
+            }
+        }
+        float4 c = B.col[p];
+        const v3 add = f3(rec.T) * res / rec.T.w;
+        c.x = c.x + add.x; c.y = c.y + add.y; c.z = c.z + add.z;
+        B.col[p] = c;
+    }
+}
+
+// Queue rotation between bounces: the enqueued continuation count becomes the live count.
+__global__ void k_rotate(uint32_t* counters) {
+    if (threadIdx.x == 0) {
+        counters[0] = counters[1];
+        counters[1] = 0u;
+        counters[2] = 0u;
+        for (int c = 0; c < NUM_CLS; c++) counters[3 + c] = 0u;
+    }
+}
+
+// path.rgen:102-112 applied to the chunk's frames in order.
+__global__ void __launch_bounds__(kThreads) k_film(Params P, Buffers B, float4* __restrict__ film) {
+    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < P.npix; pix += gridDim.x * blockDim.x) {
+        float4 px = film[pix];
+        for (uint32_t k = 0; k < P.nframes; k++) {
+            const uint32_t f = P.frame0 + k;
+            const float4 c4 = B.col[(size_t)k * P.npix + pix];
+            const v3 col = f3(c4);
+            if (P.film_mode == 1u) {
+                px = make_float4(col.x, col.y, col.z, 1.0f);
+                continue;
+            }
+            if (isnan(luminance(col))) continue;
+            if (f > 0u) {
+                const float w = 1.0f / (float)(f + 1u);
+                px = make_float4(mixf(px.x, col.x, w), mixf(px.y, col.y, w), mixf(px.z, col.z, w), 1.0f);
+            } else {
+                px = make_float4(col.x, col.y, col.z, 1.0f);
+            }
+        }
+        film[pix] = px;
+    }
+}
+
+__global__ void k_init_counters(uint32_t* counters, uint32_t n) {
+    if (threadIdx.x < 8) counters[threadIdx.x] = threadIdx.x == 0 ? n : 0u;
+}
+
+size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Carves the work arena for `cap` paths; returns the byte size when base is null.
+size_t carve(char* base, uint32_t cap, Buffers& B) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) { char* p = base ? base + off : nullptr; off += align_up(bytes); return p; };
+    B.pix = (uint32_t*)take(4ull * cap);
+    B.frame = (uint32_t*)take(4ull * cap);
+    B.w = (uint32_t*)take(4ull * cap);
+    B.flags = (uint32_t*)take(4ull * cap);
+    B.T = (float4*)take(16ull * cap);
+    B.col = (float4*)take(16ull * cap);
+    B.q_cur = (uint32_t*)take(4ull * cap);
+    B.q_next = (uint32_t*)take(4ull * cap);
+    B.q_cls = (uint32_t*)take(4ull * NUM_CLS * cap);
+    B.rays = (lgb_ray*)take(sizeof(lgb_ray) * (size_t)cap);
+    B.rays_next = (lgb_ray*)take(sizeof(lgb_ray) * (size_t)cap);
+    B.hits = (lgb_hit*)take(sizeof(lgb_hit) * (size_t)cap);
+    B.nee = (NeeRec*)take(sizeof(NeeRec) * (size_t)cap);
+    B.srays = (lgb_ray*)take(sizeof(lgb_ray) * (size_t)cap);
+    B.mrays = (lgb_ray*)take(sizeof(lgb_ray) * (size_t)cap);
+    B.mhits = (lgb_hit*)take(sizeof(lgb_hit) * (size_t)cap);
+    B.sbits = (uint32_t*)take(4ull * ((cap + 31) / 32));
+    B.counters = (uint32_t*)take(64);
+    return off;
+}
+
+}  // namespace
+
+lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* pp, uint32_t frame0, uint32_t spp,
+                       float* film, cudaStream_t st) {
+    Ctx* ctx = s->ctx;
+    const uint32_t npix = cam->width * cam->height;
+    if ((uint64_t)cam->width * cam->height > kMaxPaths)
+        return set_error(ctx, LGB_ERR_UNSUPPORTED, "image larger than the path capacity (2^21 pixels)");
+    const uint32_t frames_per_chunk = std::max(1u, std::min(spp, kMaxPaths / npix));
+    const uint32_t cap = npix * frames_per_chunk;
+    Buffers B;
+    const size_t bytes = carve(nullptr, cap, B);
+    if (s->pt_buf_bytes < bytes) {
+        cudaFree(s->pt_buf);
+        s->pt_buf = nullptr;
+        s->pt_buf_bytes = 0;
+        LGB_CUDA_TRY(ctx, cudaMalloc(&s->pt_buf, bytes));
+        s->pt_buf_bytes = bytes;
+    }
+    carve((char*)s->pt_buf, cap, B);
+    SceneView S;
+    S.nodes = s->bvh.nodes; S.tris = s->bvh.tris; S.verts = s->d_vertices; S.idx = s->d_indices;
+    S.tri_mesh = s->d_tri_mesh; S.meshes = s->d_meshes; S.mesh_first = s->d_mesh_first_tri; S.mats = s->d_materials;
+    S.lights = s->d_lights; S.texs = s->d_textures; S.status = s->d_status;
+    Params P;
+    for (int i = 0; i < 16; i++) { P.iv[i] = cam->inv_view[i]; P.ip[i] = cam->inv_projection[i]; }
+    P.width = cam->width; P.height = cam->height; P.npix = npix;
+    for (int i = 0; i < 3; i++) P.sky[i] = pp->sky_col[i];
+    P.max_depth = pp->max_depth; P.num_lights = pp->num_lights; P.light_tri_count = pp->light_triangle_count;
+    P.direct_lighting = pp->direct_lighting; P.film_mode = pp->film_mode;
+    P.cap = cap;
+    const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    const int grid_work = sms * 8, grid_trace = sms * 16;
+    const int bounces = std::max(pp->max_depth, 1);
+    for (uint32_t done = 0; done < spp; done += frames_per_chunk) {
+        P.frame0 = frame0 + done;
+        P.nframes = std::min(frames_per_chunk, spp - done);
+        const uint32_t npaths = npix * P.nframes;
+        k_init_counters<<<1, 32, 0, st>>>(B.counters, npaths);
+        k_camera<<<grid_work, kThreads, 0, st>>>(P, B);
+        for (int depth = 0; depth < bounces; depth++) {
+            k_q_trace_closest<<<grid_trace, kThreads, 0, st>>>(S, B.rays, B.hits, B.counters + 0);
+            k_classify<<<grid_work, kThreads, 0, st>>>(S, P, B);
+            k_shade<CLS_DIFFUSE><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
+            k_shade<CLS_CONDUCTOR><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
+            k_shade<CLS_SPECULAR><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
+            k_shade<CLS_PRINCIPLED><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
+            k_q_trace_any<<<grid_trace, kThreads, 0, st>>>(S, B.srays, B.sbits, B.counters + 2);
+            k_q_trace_closest<<<grid_trace, kThreads, 0, st>>>(S, B.mrays, B.mhits, B.counters + 2);
+            k_nee_resolve<<<grid_work, kThreads, 0, st>>>(S, B);
+            k_rotate<<<1, 32, 0, st>>>(B.counters);
+            std::swap(B.rays, B.rays_next);
+            std::swap(B.q_cur, B.q_next);
+        }
+        k_film<<<grid_work, kThreads, 0, st>>>(P, B, reinterpret_cast<float4*>(film));
+        LGB_CUDA_TRY(ctx, cudaGetLastError());
+    }
+    return LGB_OK;
+}
+
+}  // namespace lgb

@@ -1,0 +1,259 @@
+"""Host-side scene arrays and the Python face of the C ABI.
+
+`SceneArrays` holds what Lumen's LumenScene::load_scene produces (src/RayTracer/LumenScene.cpp:52-229):
+flattened vertex/index buffers, per-mesh records, materials, lights. `Context`/`GpuScene` wrap the
+lgb_* entry points for callers working with torch CUDA tensors.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+
+MATERIAL_DTYPE = np.dtype([
+    ("albedo", "<f4", 3), ("ior", "<f4"), ("emissive_factor", "<f4", 3), ("bsdf_type", "<u4"),
+    ("bsdf_props", "<u4"), ("k", "<f4", 3), ("texture_id", "<i4"), ("roughness", "<f4"), ("diffuse_trans", "<f4"),
+    ("spec_trans", "<f4"), ("metallic", "<f4"), ("specular_tint", "<f4"), ("sheen_tint", "<f4"),
+    ("clearcoat", "<f4"), ("clearcoat_gloss", "<f4"), ("sheen", "<f4"), ("subsurface", "<f4"), ("flatness", "<f4"),
+    ("anisotropy", "<f4"), ("thin", "<u4"),
+])
+LIGHT_DTYPE = np.dtype([
+    ("world_matrix", "<f4", 16), ("pos", "<f4", 3), ("prim_mesh_idx", "<u4"), ("to", "<f4", 3),
+    ("num_triangles", "<u4"), ("L", "<f4", 3), ("light_flags", "<u4"), ("world_center", "<f4", 3),
+    ("world_radius", "<f4"),
+])
+MESH_DTYPE = np.dtype([("index_offset", "<u4"), ("vertex_offset", "<u4"), ("material_index", "<u4"),
+                       ("tri_count", "<u4")])
+assert MATERIAL_DTYPE.itemsize == 104 and LIGHT_DTYPE.itemsize == 128 and MESH_DTYPE.itemsize == 16
+
+
+def new_material(**kw) -> np.ndarray:
+    """A material record with Lumen's loader defaults (albedo 1, texture -1, clearcoat_gloss 1)."""
+    m = np.zeros(1, MATERIAL_DTYPE)
+    m["albedo"] = 1.0
+    m["texture_id"] = -1
+    m["clearcoat_gloss"] = 1.0
+    m["sheen_tint"] = 0.5
+    for k, v in kw.items():
+        m[k] = v
+    return m
+
+
+def diffuse(albedo, emissive=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """"type": "diffuse" as LumenScene.cpp:372-375 maps it."""
+    return new_material(albedo=albedo, emissive_factor=emissive, bsdf_type=abi.BSDF_DIFFUSE,
+                        bsdf_props=abi.FLAG_DIFFUSE | abi.FLAG_REFLECTION)
+
+
+def conductor(reflectance, roughness) -> np.ndarray:
+    """"type": "conductor" with "reflectance" (LumenScene.cpp:406-443, reflectance_to_conductor_eta_k :47-50)."""
+    r = np.clip(np.asarray(reflectance, np.float32), 0.0, 0.9999).astype(np.float32)
+    eta = np.ones(3, np.float32)
+    k = (np.float32(2.0) * np.sqrt(r) / np.sqrt(np.maximum(np.float32(1.0) - r, np.float32(0.001)))).astype(np.float32)
+    props = abi.FLAG_REFLECTION | (abi.FLAG_GLOSSY if roughness > 0.08 else abi.FLAG_SPECULAR)
+    return new_material(albedo=eta, k=k, roughness=roughness, bsdf_type=abi.BSDF_CONDUCTOR, bsdf_props=props)
+
+
+def dielectric(ior, roughness=0.0, albedo=(1.0, 1.0, 1.0), thin=0) -> np.ndarray:
+    """"type": "dielectric" (LumenScene.cpp:385-405)."""
+    props = abi.FLAG_TRANSMISSION | abi.FLAG_REFLECTION
+    props |= abi.FLAG_GLOSSY if (ior != 1.0 and roughness > 0.08) else abi.FLAG_SPECULAR
+    return new_material(albedo=albedo, ior=ior, roughness=roughness, bsdf_type=abi.BSDF_DIELECTRIC, bsdf_props=props,
+                        thin=thin)
+
+
+def principled(albedo, roughness=0.5, metallic=0.0, ior=1.0, spec_trans=0.0, clearcoat=0.0, clearcoat_gloss=1.0,
+               specular_tint=0.0, anisotropy=0.0, flatness=0.0) -> np.ndarray:
+    """"type": "principled" (LumenScene.cpp:444-475)."""
+    props = 0
+    if roughness < 1.0:
+        props |= abi.FLAG_REFLECTION
+    if spec_trans > 0.0:
+        props |= abi.FLAG_TRANSMISSION
+    props |= abi.FLAG_GLOSSY if roughness > 0.08 else abi.FLAG_SPECULAR
+    return new_material(albedo=albedo, roughness=roughness, metallic=metallic, ior=ior, spec_trans=spec_trans,
+                        clearcoat=clearcoat, clearcoat_gloss=clearcoat_gloss, specular_tint=specular_tint,
+                        anisotropy=anisotropy, flatness=flatness, bsdf_type=abi.BSDF_PRINCIPLED, bsdf_props=props)
+
+
+@dataclass
+class SceneArrays:
+    positions: np.ndarray            # (V, 3) f32
+    normals: np.ndarray              # (V, 3) f32
+    uvs: np.ndarray                  # (V, 2) f32
+    indices: np.ndarray              # (I,) u32
+    meshes: np.ndarray               # MESH_DTYPE
+    materials: np.ndarray            # MATERIAL_DTYPE
+    lights: np.ndarray               # LIGHT_DTYPE
+    textures: list = field(default_factory=list)  # list of (H, W, 4) f32
+    light_triangle_count: int = 0
+    camera_pos: tuple = (0.0, 0.0, 0.0)
+    camera_dir: tuple = (0.0, 0.0, 1.0)
+    fov: float = 45.0
+
+    @property
+    def num_tris(self) -> int:
+        return int(self.meshes["tri_count"].sum())
+
+    def tri_verts(self) -> np.ndarray:
+        """(T, 9) world-space vertices of every global triangle, meshes in order."""
+        out = []
+        for m in self.meshes:
+            n = int(m["tri_count"])
+            idx = self.indices[int(m["index_offset"]):int(m["index_offset"]) + 3 * n].astype(np.int64)
+            idx = idx + int(m["vertex_offset"])
+            out.append(self.positions[idx].reshape(n, 9))
+        return np.ascontiguousarray(np.concatenate(out).astype(np.float32))
+
+    def make_desc(self, desc_cls=abi.SceneDesc, mesh_cls=abi.Mesh, mat_cls=abi.Material, light_cls=abi.Light,
+                  tex_cls=abi.Texture):
+        """Builds a ctypes scene description; returns (desc, keepalive)."""
+        keep = []
+
+        def ptr(a, ct):
+            a = np.ascontiguousarray(a)
+            keep.append(a)
+            return a.ctypes.data_as(C.POINTER(ct))
+
+        d = desc_cls()
+        d.positions = ptr(self.positions.astype(np.float32), C.c_float)
+        d.normals = ptr(self.normals.astype(np.float32), C.c_float)
+        d.uvs = ptr(self.uvs.astype(np.float32), C.c_float)
+        d.num_vertices = len(self.positions)
+        d.indices = ptr(self.indices.astype(np.uint32), C.c_uint32)
+        d.num_indices = len(self.indices)
+        d.meshes = ptr(self.meshes, mesh_cls)
+        d.num_meshes = len(self.meshes)
+        d.materials = ptr(self.materials, mat_cls)
+        d.num_materials = len(self.materials)
+        d.lights = ptr(self.lights, light_cls) if len(self.lights) else None
+        d.num_lights = len(self.lights)
+        if self.textures:
+            arr = (tex_cls * len(self.textures))()
+            for i, t in enumerate(self.textures):
+                t = np.ascontiguousarray(t, np.float32)
+                keep.append(t)
+                arr[i].width = t.shape[1]
+                arr[i].height = t.shape[0]
+                arr[i].rgba = t.ctypes.data_as(C.POINTER(C.c_float))
+            keep.append(arr)
+            d.textures = C.cast(arr, C.POINTER(tex_cls))
+        d.num_textures = len(self.textures)
+        keep.append(d)
+        return d, keep
+
+
+def _check(lib, ctx, st):
+    if st != abi.LGB_OK:
+        msg = lib.lgb_last_error(ctx)
+        raise abi.LgbError(st, msg.decode() if msg else "")
+
+
+def camera_lookat(pos, direction, fov, width, height) -> abi.Camera:
+    lib = abi.load()
+    cam = abi.Camera()
+    p = (C.c_float * 3)(*pos)
+    d = (C.c_float * 3)(*direction)
+    st = lib.lgb_camera_lookat(p, d, float(fov), int(width), int(height), C.byref(cam))
+    if st != abi.LGB_OK:
+        raise abi.LgbError(st, "lgb_camera_lookat")
+    return cam
+
+
+class Context:
+    """An lgb_ctx on one CUDA device (the counterpart of Lumen's Vulkan context)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = abi.load()
+        h = C.c_void_p()
+        st = self.lib.lgb_create(C.byref(h), device)
+        if st != abi.LGB_OK:
+            raise abi.LgbError(st, f"lgb_create(device={device})")
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            self.lib.lgb_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GpuScene:
+    """A scene uploaded with lgb_scene_create; owns its BVH (lgb_bvh_build)."""
+
+    def __init__(self, ctx: Context, arrays: SceneArrays):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.arrays = arrays
+        desc, keep = arrays.make_desc()
+        h = C.c_void_p()
+        _check(self.lib, ctx.handle, self.lib.lgb_scene_create(ctx.handle, C.byref(desc), C.byref(h)))
+        self.handle = h
+        self.stats = None
+
+    def build(self, leaf_max: int = 0) -> abi.BuildStats:
+        opts = abi.BuildOpts()
+        opts.leaf_max = leaf_max
+        stats = abi.BuildStats()
+        _check(self.lib, self.ctx.handle, self.lib.lgb_bvh_build(self.handle, C.byref(opts), C.byref(stats)))
+        self.stats = stats
+        return stats
+
+    def trace_closest(self, rays, hits, n=None, stream=None):
+        n = rays.shape[0] if n is None else n
+        _check(self.lib, self.ctx.handle,
+               self.lib.lgb_trace_closest(self.handle, C.c_void_p(rays.data_ptr()), C.c_void_p(hits.data_ptr()), n,
+                                          C.c_void_p(stream)))
+
+    def trace_closest_counted(self, rays, hits, counters, stream=None):
+        _check(self.lib, self.ctx.handle,
+               self.lib.lgb_trace_closest_counted(self.handle, C.c_void_p(rays.data_ptr()),
+                                                  C.c_void_p(hits.data_ptr()), rays.shape[0],
+                                                  C.c_void_p(counters.data_ptr()), C.c_void_p(stream)))
+
+    def trace_any(self, rays, bits, n=None, stream=None):
+        n = rays.shape[0] if n is None else n
+        _check(self.lib, self.ctx.handle,
+               self.lib.lgb_trace_any(self.handle, C.c_void_p(rays.data_ptr()), C.c_void_p(bits.data_ptr()), n,
+                                      C.c_void_p(stream)))
+
+    def render_path(self, cam: abi.Camera, params: abi.PathParams, frame0: int, spp: int, film, stream=None):
+        _check(self.lib, self.ctx.handle,
+               self.lib.lgb_render_path(self.handle, C.byref(cam), C.byref(params), frame0, spp,
+                                        C.c_void_p(film.data_ptr()), C.c_void_p(stream)))
+
+    def sync(self, stream=None):
+        _check(self.lib, self.ctx.handle, self.lib.lgb_sync(self.handle, C.c_void_p(stream)))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.lgb_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def path_params(arrays: SceneArrays, max_depth: int, sky=(0.0, 0.0, 0.0), direct_lighting: int = 1,
+                film_mode: int = 0) -> abi.PathParams:
+    """PCPath as Path::render fills it (src/RayTracer/Path.cpp:28-38)."""
+    p = abi.PathParams()
+    p.sky_col[:] = list(sky)
+    p.max_depth = max_depth
+    p.num_lights = len(arrays.lights)
+    p.light_triangle_count = arrays.light_triangle_count
+    p.dir_light_idx = 0xFFFFFFFF
+    p.direct_lighting = direct_lighting
+    p.film_mode = film_mode
+    return p

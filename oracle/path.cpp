@@ -1,0 +1,453 @@
+// Oracle (test infrastructure only): CPU restatement of Lumen's unidirectional MIS path integrator.
+//
+// Follows src/shaders/integrators/path/path.rgen:22-113 (camera ray, bounce loop, RR, film),
+// src/shaders/integrators/pt_commons.glsl:3-48 (uniform_sample_light: NEE + BSDF-MIS),
+// src/shaders/commons.glsl:30-33 (sample_camera), 112-149 (sample_triangle), 173-215 (sample_area_light),
+// 224-300 (sample_light_Li), 156-168 (shade_atmosphere, sky colour only),
+// src/shaders/ray.rchit:24-84 (hit attributes) and ray.rmiss:13 (miss marks material_idx = -1 only).
+//
+// Payload semantics are kept: a miss of the BSDF-MIS ray (pt_commons.glsl:32-33) leaves the previous
+// closest-hit payload in place, so its triangle/instance ids and position are the ones compared and used.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "oracle.h"
+#include "shading.h"
+
+namespace orc {
+void* bvh_build_internal(const float* tri_verts, uint32_t n);
+bool bvh_closest(void* bvh, const float* o, const float* d, float tmin, float tmax, uint32_t& prim, float& t, float& u,
+                 float& v);
+bool bvh_any(void* bvh, const float* o, const float* d, float tmin, float tmax);
+}  // namespace orc
+
+namespace {
+using namespace orc;
+
+struct Scene {
+    std::vector<float> pos, nrm, uv;
+    std::vector<uint32_t> idx;
+    std::vector<orc_mesh> meshes;
+    std::vector<orc_material> mats;
+    std::vector<orc_light> lights;
+    struct Tex { uint32_t w, h; std::vector<float> rgba; };
+    std::vector<Tex> texs;
+    std::vector<uint32_t> tri_mesh;   // global triangle -> mesh
+    std::vector<uint32_t> mesh_first_tri;
+    void* bvh = nullptr;
+};
+
+const float EPS = 0.001f;          // utils.glsl:8
+const float TMIN = 0.001f;         // path.rgen:19
+const float TMAX = 10000.0f;       // path.rgen:20
+const int RR_MIN_DEPTH = 3;        // path.rgen:21
+
+template <class T> struct Payload {
+    V3<T> n_g, n_s, pos;
+    V2<T> uv;
+    int32_t material_idx;
+    uint32_t triangle_idx, instance_idx;
+};
+
+// Bilinear REPEAT lookup at LOD 0 in linear FP32 (stands in for texture() on the sampled image).
+template <class T> V3<T> tex_lookup(const Scene& s, int id, V2<T> uv) {
+    const Scene::Tex& t = s.texs[id];
+    if (!std::isfinite(uv.x) || !std::isfinite(uv.y)) uv = V2<T>(0, 0);
+    T x = uv.x * T(t.w) - T(0.5f), y = uv.y * T(t.h) - T(0.5f);
+    T x0 = std::floor(x), y0 = std::floor(y);
+    T fx = x - x0, fy = y - y0;
+    auto wrap = [](long long i, uint32_t n) { long long m = i % (long long)n; return (uint32_t)(m < 0 ? m + n : m); };
+    uint32_t i0 = wrap((long long)x0, t.w), i1 = wrap((long long)x0 + 1, t.w);
+    uint32_t j0 = wrap((long long)y0, t.h), j1 = wrap((long long)y0 + 1, t.h);
+    auto texel = [&](uint32_t i, uint32_t j) {
+        const float* p = &t.rgba[4 * ((size_t)j * t.w + i)];
+        return V3<T>(p[0], p[1], p[2]);
+    };
+    V3<T> c00 = texel(i0, j0), c10 = texel(i1, j0), c01 = texel(i0, j1), c11 = texel(i1, j1);
+    T w00 = (T(1) - fx) * (T(1) - fy), w10 = fx * (T(1) - fy), w01 = (T(1) - fx) * fy, w11 = fx * fy;
+    return c00 * w00 + c10 * w10 + c01 * w01 + c11 * w11;
+}
+
+template <class T> Mat<T> load_material(const Scene& s, uint32_t idx, V2<T> uv) {
+    Mat<T> m = to_mat<T>(s.mats[idx]);
+    if (m.texture_id > -1) m.albedo *= tex_lookup<T>(s, m.texture_id, uv);
+    return m;
+}
+
+template <class T> V3<T> vtx_pos(const Scene& s, uint32_t v) { return V3<T>(s.pos[3 * v], s.pos[3 * v + 1], s.pos[3 * v + 2]); }
+template <class T> V3<T> vtx_nrm(const Scene& s, uint32_t v) { return V3<T>(s.nrm[3 * v], s.nrm[3 * v + 1], s.nrm[3 * v + 2]); }
+template <class T> V2<T> vtx_uv(const Scene& s, uint32_t v) { return V2<T>(s.uv[2 * v], s.uv[2 * v + 1]); }
+
+// traceRayEXT closest + ray.rchit / ray.rmiss. Origins and directions are FP32 at the traversal boundary.
+template <class T> void trace_closest(const Scene& s, V3<T> o, V3<T> d, float tmin, float tmax, Payload<T>& pl) {
+    float of[3] = {(float)o.x, (float)o.y, (float)o.z}, df[3] = {(float)d.x, (float)d.y, (float)d.z};
+    uint32_t prim; float t, bu, bv;
+    if (!bvh_closest(s.bvh, of, df, tmin, tmax, prim, t, bu, bv)) {
+        pl.material_idx = -1;  // ray.rmiss:13; every other payload field keeps its value
+        return;
+    }
+    uint32_t mesh = s.tri_mesh[prim];
+    const orc_mesh& pm = s.meshes[mesh];
+    uint32_t local = prim - s.mesh_first_tri[mesh];
+    uint32_t io = pm.index_offset + 3 * local;
+    uint32_t i0 = s.idx[io] + pm.vertex_offset, i1 = s.idx[io + 1] + pm.vertex_offset, i2 = s.idx[io + 2] + pm.vertex_offset;
+    V3<T> v0 = vtx_pos<T>(s, i0), v1 = vtx_pos<T>(s, i1), v2 = vtx_pos<T>(s, i2);
+    V3<T> n0 = vtx_nrm<T>(s, i0), n1 = vtx_nrm<T>(s, i1), n2 = vtx_nrm<T>(s, i2);
+    V2<T> uv0 = vtx_uv<T>(s, i0), uv1 = vtx_uv<T>(s, i1), uv2 = vtx_uv<T>(s, i2);
+    V3<T> bary(T(1) - T(bu) - T(bv), T(bu), T(bv));
+    V3<T> p = v0 * bary.x + v1 * bary.y + v2 * bary.z;
+    V3<T> nrm = normalize(n0 * bary.x + n1 * bary.y + n2 * bary.z);
+    // Object-to-world is the identity for every mesh Lumen's loader produces (LumenScene.cpp:328), so the
+    // matrix products in ray.rchit:60,65,74 reduce to their arguments; the second normalize stays.
+    V3<T> world_nrm = normalize(nrm);
+    V2<T> uv = uv0 * bary.x + uv1 * bary.y + uv2 * bary.z;
+    V3<T> e0 = v2 - v0, e1 = v1 - v0;
+    pl.n_g = normalize(cross(e0, e1));
+    pl.n_s = world_nrm;
+    pl.pos = p;
+    pl.uv = uv;
+    pl.material_idx = (int32_t)pm.material_index;
+    pl.triangle_idx = local;
+    pl.instance_idx = mesh;
+}
+
+// commons.glsl:112-149 with an identity world matrix.
+template <class T> void sample_triangle(const Scene& s, const orc_mesh& pm, V2<T> rands, uint32_t tri, V3<T>& pos, V3<T>& n_s,
+                                        T& tri_pdf, V2<T>& uv) {
+    uint32_t io = pm.index_offset + 3 * tri;
+    uint32_t i0 = s.idx[io] + pm.vertex_offset, i1 = s.idx[io + 1] + pm.vertex_offset, i2 = s.idx[io + 2] + pm.vertex_offset;
+    V3<T> v0 = vtx_pos<T>(s, i0), v1 = vtx_pos<T>(s, i1), v2 = vtx_pos<T>(s, i2);
+    V3<T> n0 = vtx_nrm<T>(s, i0), n1 = vtx_nrm<T>(s, i1), n2 = vtx_nrm<T>(s, i2);
+    uv = V2<T>(T(1) - std::sqrt(rands.x), rands.y * std::sqrt(rands.x));
+    V3<T> b(T(1) - uv.x - uv.y, uv.x, uv.y);
+    V3<T> et0 = v1 - v0, et1 = v2 - v0;
+    V3<T> p = v0 * b.x + v1 * b.y + v2 * b.z;
+    V3<T> nrm = normalize(n0 * b.x + n1 * b.y + n2 * b.z);
+    n_s = normalize(nrm);
+    tri_pdf = T(2) / length(cross(et0, et1));
+    pos = p;
+}
+
+template <class T> struct LightSample {
+    V3<T> L, wi;
+    T wi_len, pdf_pos_w, pdf_pos_a, cos_from_light;
+    uint32_t flags, triangle_idx, instance_idx;
+};
+
+// commons.glsl:224-300
+template <class T> LightSample<T> sample_light_Li(const Scene& s, V4<T> rands, V3<T> p, int num_lights) {
+    LightSample<T> r;
+    uint32_t light_idx = (uint32_t)(rands.x * T(num_lights));
+    const orc_light& light = s.lights[light_idx];
+    uint32_t light_type = light.light_flags & 0x7;
+    r.L = V3<T>(0); r.flags = light.light_flags; r.pdf_pos_w = T(0); r.wi = V3<T>(0); r.wi_len = T(0);
+    r.pdf_pos_a = T(0); r.cos_from_light = T(0); r.triangle_idx = 0; r.instance_idx = 0;
+    if (light_type == LIGHT_AREA) {
+        const orc_mesh& pm = s.meshes[light.prim_mesh_idx];
+        uint32_t tri = (uint32_t)(rands.y * T(light.num_triangles));
+        V3<T> lpos, ln; T tri_pdf; V2<T> bary;
+        sample_triangle<T>(s, pm, V2<T>(rands.z, rands.w), tri, lpos, ln, tri_pdf, bary);
+        Mat<T> light_mat = load_material<T>(s, pm.material_index, bary);
+        V3<T> wi = lpos - p;
+        T wi_len_sqr = dot(wi, wi);
+        r.wi_len = std::sqrt(wi_len_sqr);
+        wi /= r.wi_len;
+        r.wi = wi;
+        r.cos_from_light = std::fabs(dot(ln, -wi));
+        r.L = light_mat.emissive_factor;
+        r.pdf_pos_a = tri_pdf;
+        r.pdf_pos_w = r.pdf_pos_a * wi_len_sqr / r.cos_from_light;
+        r.triangle_idx = tri;
+        r.instance_idx = light.prim_mesh_idx;
+    } else if (light_type == LIGHT_SPOT) {
+        V3<T> lp(light.pos[0], light.pos[1], light.pos[2]);
+        V3<T> wi = lp - p;
+        T wi_len_sqr = dot(wi, wi);
+        r.wi_len = std::sqrt(wi_len_sqr);
+        wi /= r.wi_len;
+        r.wi = wi;
+        V3<T> to(light.to[0], light.to[1], light.to[2]);
+        const V3<T> light_dir = normalize(to - lp);
+        r.cos_from_light = dot(-wi, light_dir);
+        const T cos_width = std::cos(K<T>::PI() / T(6));
+        const T cos_faloff = std::cos(T(25) * K<T>::PI() / T(180));
+        T faloff;
+        if (r.cos_from_light < cos_width) faloff = T(0);
+        else if (r.cos_from_light >= cos_faloff) faloff = T(1);
+        else {
+            T dd = (r.cos_from_light - cos_width) / (cos_faloff - cos_width);
+            faloff = (dd * dd) * (dd * dd);
+        }
+        r.pdf_pos_a = T(1);
+        r.pdf_pos_w = wi_len_sqr;
+        r.L = V3<T>(light.L[0], light.L[1], light.L[2]) * faloff;
+    } else if (light_type == LIGHT_DIRECTIONAL) {
+        V3<T> lp(light.pos[0], light.pos[1], light.pos[2]), to(light.to[0], light.to[1], light.to[2]);
+        const V3<T> dir = normalize(lp - to);
+        const V3<T> light_p = p + dir * (T(2) * T(light.world_radius));
+        V3<T> wi = light_p - p;
+        r.wi_len = length(wi);
+        wi /= r.wi_len;
+        r.wi = wi;
+        r.pdf_pos_a = T(1);
+        r.pdf_pos_w = T(1);
+        r.L = V3<T>(light.L[0], light.L[1], light.L[2]);
+        r.cos_from_light = T(1);
+    }
+    return r;
+}
+
+template <class T> V3<T> sample_camera(const M4<T>& inv_view, const M4<T>& inv_proj, V2<T> d) {
+    V4<T> target = inv_proj * V4<T>(d.x, d.y, T(1), T(1));
+    V3<T> n = normalize(target.xyz());
+    V4<T> r = inv_view * V4<T>(n.x, n.y, n.z, T(0));
+    return r.xyz();
+}
+
+template <class T> M4<T> load_m4(const float* m) {
+    M4<T> r;
+    for (int c = 0; c < 4; c++)
+        for (int k = 0; k < 4; k++) r.m[c][k] = T(m[4 * c + k]);
+    return r;
+}
+
+// One invocation of path.rgen main() for pixel (x, y) at frame params.frame_num. Returns col.
+template <class T>
+V3<T> path_sample(const Scene& s, const M4<T>& inv_view, const M4<T>& inv_proj, const orc_path_params& pc, uint32_t x,
+                  uint32_t y) {
+    U4 seed{x, y, pc.frame_num, 0u};  // init_rng (utils.glsl:142)
+    const V2<T> pixel(T(x) + T(0.5f), T(y) + T(0.5f));
+    float r0 = rand(seed);
+    float r1 = rand(seed);
+    V2<T> rands(T(r0) - T(0.5f), T(r1) - T(0.5f));
+    const V2<T> in_uv((pixel.x + rands.x) / T(pc.size_x), (pixel.y + rands.y) / T(pc.size_y));
+    V2<T> d(in_uv.x * T(2) - T(1), in_uv.y * T(2) - T(1));
+    V4<T> origin = inv_view * V4<T>(T(0), T(0), T(0), T(1));
+    V3<T> direction = sample_camera(inv_view, inv_proj, d);
+    V3<T> col(0);
+    bool last_specular = false;
+    V3<T> throughput(1);
+    Payload<T> payload;
+    payload.material_idx = -1; payload.triangle_idx = 0xFFFFFFFFu; payload.instance_idx = 0xFFFFFFFFu;
+    const V3<T> sky(pc.sky_col[0], pc.sky_col[1], pc.sky_col[2]);
+    for (int depth = 0;; depth++) {
+        trace_closest<T>(s, origin.xyz(), direction, TMIN, TMAX, payload);
+        const bool found_isect = payload.material_idx != -1;
+        if (!found_isect) {
+            // shade_atmosphere with dir_light_idx == -1 returns sky_col (commons.glsl:157-159)
+            if (depth > 0 || pc.direct_lighting == 1) col += throughput * sky;
+            break;
+        }
+        const Mat<T> hit_mat = load_material<T>(s, (uint32_t)payload.material_idx, payload.uv);
+        if ((depth == 0 && pc.direct_lighting == 1) || last_specular) col += throughput * hit_mat.emissive_factor;
+        if (depth >= pc.max_depth - 1) break;
+        const V3<T> wo = -direction;
+        V3<T> n_s = payload.n_s;
+        bool side = true;
+        V3<T> n_g = payload.n_g;
+        if (dot(payload.n_g, wo) < T(0)) n_g = -n_g;
+        if (dot(n_g, payload.n_s) < T(0)) { n_s = -n_s; side = false; }
+        {
+            V3<float> pf((float)payload.pos.x, (float)payload.pos.y, (float)payload.pos.z);
+            V3<float> nf((float)n_g.x, (float)n_g.y, (float)n_g.z);
+            V3<float> of = offset_ray(pf, nf);
+            origin = V4<T>(T(of.x), T(of.y), T(of.z), origin.w);
+        }
+        last_specular = (hit_mat.bsdf_props & BSDF_FLAG_SPECULAR) != 0;
+        if (!last_specular) {
+            const T light_pick_pdf = T(1) / T(pc.light_triangle_count);
+            if ((depth > 0 || pc.direct_lighting == 1) && pc.num_lights <= 0) {
+                // No light to sample (Lumen would read past its light buffer): consume the four draws only.
+                for (int k = 0; k < 4; k++) (void)rand(seed);
+            } else if (depth > 0 || pc.direct_lighting == 1) {
+                // uniform_sample_light (pt_commons.glsl:3-42)
+                const V3<T> pos = payload.pos;
+                V3<T> res(0);
+                float q0 = rand(seed), q1 = rand(seed), q2 = rand(seed), q3 = rand(seed);
+                LightSample<T> ls = sample_light_Li<T>(s, V4<T>(T(q0), T(q1), T(q2), T(q3)), pos, pc.num_lights);
+                const V3<T> p = offset_ray2(pos, n_s);
+                T bsdf_pdf, unused_rev;
+                T cos_x = dot(n_s, ls.wi);
+                V3<T> f = eval_bsdf(n_s, wo, hit_mat, 1u, side, ls.wi, bsdf_pdf, unused_rev, false);
+                float pf[3] = {(float)p.x, (float)p.y, (float)p.z};
+                float wf[3] = {(float)ls.wi.x, (float)ls.wi.y, (float)ls.wi.z};
+                bool visible = !bvh_any(s.bvh, pf, wf, 0.0f, (float)(ls.wi_len - T(EPS)));
+                if (visible && ls.pdf_pos_w > T(0)) {
+                    const T mis_weight = ((ls.flags >> 5) & 1u) ? T(1) : T(1) / (T(1) + bsdf_pdf / ls.pdf_pos_w);
+                    res += mis_weight * f * std::fabs(cos_x) * ls.L / ls.pdf_pos_w;
+                }
+                if ((ls.flags & 0x7) == LIGHT_AREA) {
+                    V3<T> wi;
+                    float b0 = rand(seed), b1 = rand(seed), b2 = rand(seed);
+                    f = sample_bsdf(n_s, wo, hit_mat, 1u, side, wi, bsdf_pdf, cos_x, V3<T>(T(b0), T(b1), T(b2)));
+                    if (bsdf_pdf != T(0)) {
+                        trace_closest<T>(s, p, wi, TMIN, TMAX, payload);
+                        if (payload.triangle_idx == ls.triangle_idx && payload.instance_idx == ls.instance_idx) {
+                            const T wl = length(payload.pos - pos);
+                            const T g = std::fabs(dot(payload.n_s, -wi)) / (wl * wl);
+                            const T mis_weight = T(1) / (T(1) + ls.pdf_pos_a / (g * bsdf_pdf));
+                            res += f * mis_weight * std::fabs(cos_x) * ls.L / bsdf_pdf;
+                        }
+                    }
+                }
+                col += throughput * res / light_pick_pdf;
+            }
+        }
+        T pdf, cos_theta;
+        float c0 = rand(seed), c1 = rand(seed), c2 = rand(seed);
+        const V3<T> f = sample_bsdf(n_s, wo, hit_mat, 1u, side, direction, pdf, cos_theta, V3<T>(T(c0), T(c1), T(c2)));
+        if (pdf == T(0)) break;
+        throughput *= f * std::fabs(cos_theta) / pdf;
+        T rr_scale = T(1);
+        if (bsdf_has_property(hit_mat.bsdf_props, BSDF_FLAG_TRANSMISSION)) rr_scale *= side ? T(1) / hit_mat.ior : hit_mat.ior;
+        if (depth > RR_MIN_DEPTH) {
+            T rr_prob = gmin(T(0.95f), luminance(throughput) * rr_scale);
+            if (rr_prob == T(0) || rr_prob < T(rand(seed))) break;
+            else throughput /= rr_prob;
+        }
+    }
+    return col;
+}
+
+template <class F> void parallel_for(uint32_t n, int nthreads, F f) {
+    if (nthreads <= 1 || n < 64) {
+        for (uint32_t i = 0; i < n; i++) f(i);
+        return;
+    }
+    std::atomic<uint32_t> next(0);
+    std::vector<std::thread> th;
+    for (int k = 0; k < nthreads; k++) {
+        th.emplace_back([&]() {
+            for (;;) {
+                uint32_t b = next.fetch_add(64);
+                if (b >= n) break;
+                uint32_t e = std::min(n, b + 64);
+                for (uint32_t i = b; i < e; i++) f(i);
+            }
+        });
+    }
+    for (auto& t : th) t.join();
+}
+
+}  // namespace
+
+extern "C" {
+
+void* orc_scene_create(const orc_scene_desc* d) {
+    Scene* s = new Scene();
+    s->pos.assign(d->positions, d->positions + 3 * (size_t)d->num_vertices);
+    s->nrm.assign(d->normals, d->normals + 3 * (size_t)d->num_vertices);
+    s->uv.assign(d->uvs, d->uvs + 2 * (size_t)d->num_vertices);
+    s->idx.assign(d->indices, d->indices + d->num_indices);
+    s->meshes.assign(d->meshes, d->meshes + d->num_meshes);
+    s->mats.assign(d->materials, d->materials + d->num_materials);
+    s->lights.assign(d->lights, d->lights + d->num_lights);
+    for (uint32_t i = 0; i < d->num_textures; i++) {
+        Scene::Tex t;
+        t.w = d->textures[i].width; t.h = d->textures[i].height;
+        t.rgba.assign(d->textures[i].rgba, d->textures[i].rgba + 4 * (size_t)t.w * t.h);
+        s->texs.push_back(std::move(t));
+    }
+    // Flatten: global triangle g of mesh m has index triple at index_offset + 3 * local.
+    std::vector<float> tv;
+    for (uint32_t m = 0; m < d->num_meshes; m++) {
+        s->mesh_first_tri.push_back((uint32_t)s->tri_mesh.size());
+        const orc_mesh& pm = d->meshes[m];
+        for (uint32_t t = 0; t < pm.tri_count; t++) {
+            s->tri_mesh.push_back(m);
+            for (int k = 0; k < 3; k++) {
+                uint32_t v = d->indices[pm.index_offset + 3 * t + k] + pm.vertex_offset;
+                tv.push_back(d->positions[3 * v]); tv.push_back(d->positions[3 * v + 1]); tv.push_back(d->positions[3 * v + 2]);
+            }
+        }
+    }
+    s->bvh = orc::bvh_build_internal(tv.data(), (uint32_t)s->tri_mesh.size());
+    return s;
+}
+
+void orc_bvh_free(void* bvh);
+void orc_scene_free(void* h) {
+    Scene* s = (Scene*)h;
+    if (s->bvh) orc_bvh_free(s->bvh);
+    delete s;
+}
+
+void orc_render_samples(void* h, const float inv_view[16], const float inv_proj[16], const orc_path_params* params,
+                        const uint32_t* pixels, uint32_t n_pixels, float* out_rgb, uint8_t* out_nan, int fp64,
+                        int nthreads) {
+    const Scene& s = *(Scene*)h;
+    parallel_for(n_pixels, nthreads, [&](uint32_t i) {
+        uint32_t pix = pixels[i];
+        uint32_t x = pix % params->size_x, y = pix / params->size_x;
+        double c[3];
+        if (fp64) {
+            V3<double> col = path_sample<double>(s, load_m4<double>(inv_view), load_m4<double>(inv_proj), *params, x, y);
+            c[0] = col.x; c[1] = col.y; c[2] = col.z;
+            out_nan[i] = std::isnan(luminance(col)) ? 1 : 0;
+        } else {
+            V3<float> col = path_sample<float>(s, load_m4<float>(inv_view), load_m4<float>(inv_proj), *params, x, y);
+            c[0] = col.x; c[1] = col.y; c[2] = col.z;
+            out_nan[i] = std::isnan(luminance(col)) ? 1 : 0;
+        }
+        out_rgb[3 * i] = (float)c[0]; out_rgb[3 * i + 1] = (float)c[1]; out_rgb[3 * i + 2] = (float)c[2];
+    });
+}
+
+void orc_render_film(void* h, const float inv_view[16], const float inv_proj[16], const orc_path_params* params,
+                     uint32_t frame0, uint32_t spp, float* film, int fp64, int nthreads) {
+    const Scene& s = *(Scene*)h;
+    uint32_t n = params->size_x * params->size_y;
+    parallel_for(n, nthreads, [&](uint32_t pix) {
+        uint32_t x = pix % params->size_x, y = pix / params->size_x;
+        orc_path_params pc = *params;
+        for (uint32_t f = frame0; f < frame0 + spp; f++) {
+            pc.frame_num = f;
+            float* px = &film[4 * (size_t)pix];
+            if (fp64) {
+                V3<double> col = path_sample<double>(s, load_m4<double>(inv_view), load_m4<double>(inv_proj), pc, x, y);
+                if (std::isnan(luminance(col))) continue;
+                if (f > 0) {
+                    double w = 1.0 / double(f + 1);
+                    for (int k = 0; k < 3; k++) px[k] = (float)(px[k] * (1.0 - w) + (&col.x)[k] * w);
+                } else {
+                    px[0] = (float)col.x; px[1] = (float)col.y; px[2] = (float)col.z;
+                }
+                px[3] = 1.0f;
+            } else {
+                V3<float> col = path_sample<float>(s, load_m4<float>(inv_view), load_m4<float>(inv_proj), pc, x, y);
+                if (std::isnan(luminance(col))) continue;
+                if (f > 0) {
+                    // path.rgen:107-109: w = 1 / float(frame + 1); mix(old, col, w)
+                    float w = 1.0f / float(f + 1);
+                    V3<float> old(px[0], px[1], px[2]);
+                    V3<float> m = mix(old, col, w);
+                    px[0] = m.x; px[1] = m.y; px[2] = m.z;
+                } else {
+                    px[0] = col.x; px[1] = col.y; px[2] = col.z;
+                }
+                px[3] = 1.0f;
+            }
+        }
+    });
+}
+
+void orc_pcg4d(const uint32_t* in, uint32_t* out, uint32_t n) {
+    for (uint32_t i = 0; i < n; i++) {
+        U4 v{in[4 * i], in[4 * i + 1], in[4 * i + 2], in[4 * i + 3]};
+        U4 r = pcg4d(v);
+        out[4 * i] = r.x; out[4 * i + 1] = r.y; out[4 * i + 2] = r.z; out[4 * i + 3] = r.w;
+    }
+}
+
+void orc_offset_ray(const float* p, const float* nrm, float* out, uint32_t n) {
+    for (uint32_t i = 0; i < n; i++) {
+        V3<float> r = offset_ray(V3<float>(p[3 * i], p[3 * i + 1], p[3 * i + 2]), V3<float>(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]));
+        out[3 * i] = r.x; out[3 * i + 1] = r.y; out[3 * i + 2] = r.z;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,187 @@
+"""CPU tests of the oracle: known answers for the integer utilities, the watertight ray/triangle contract,
+BVH queries against exhaustive testing, and the path integrator's internal consistency."""
+import numpy as np
+import pytest
+
+import reference_py
+from lumen_gb300 import procedural
+
+
+def test_pcg4d_known_answers(oracle):
+    rng = np.random.default_rng(0)
+    v = rng.integers(0, 2**32, (512, 4), dtype=np.uint64).astype(np.uint32)
+    v[0] = [0, 0, 0, 0]
+    v[1] = [0xFFFFFFFF] * 4
+    got = oracle.pcg4d(v)
+    want = np.array([reference_py.pcg4d([int(c) for c in row]) for row in v], np.uint32)
+    assert np.array_equal(got, want)
+
+
+def test_rand_stream_in_unit_interval():
+    xs = reference_py.rand_stream(3, 7, 11, 4096)
+    assert min(xs) >= 0.0 and max(xs) < 1.0
+    assert abs(np.mean(xs) - 0.5) < 0.02
+
+
+def test_offset_ray_known_answers(oracle):
+    rng = np.random.default_rng(1)
+    p = rng.uniform(-3, 3, (2000, 3)).astype(np.float32)
+    p[:200] *= np.float32(0.01)  # inside the |p| < 1/32 band
+    p[200, :] = 0.0
+    n = rng.standard_normal((2000, 3)).astype(np.float32)
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    got = oracle.offset_ray(p, n)
+    want = np.array([reference_py.offset_ray(a, b) for a, b in zip(p.tolist(), n.tolist())], np.float32)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    np.testing.assert_array_equal(procedural.offset_ray(p, n).view(np.uint32), want.view(np.uint32))
+
+
+def _fan(n=16, z=0.0):
+    """A closed fan of n triangles around the origin in the plane z, sharing the centre vertex and edges."""
+    ang = np.linspace(0, 2 * np.pi, n + 1)
+    ring = np.stack([np.cos(ang), np.sin(ang), np.full_like(ang, z)], -1).astype(np.float32)
+    tv = np.zeros((n, 9), np.float32)
+    for i in range(n):
+        tv[i, 0:3] = (0, 0, z)
+        tv[i, 3:6] = ring[i]
+        tv[i, 6:9] = ring[i + 1]
+    return tv
+
+
+def _rays(o, d, tmin=0.0, tmax=1e30):
+    o = np.atleast_2d(np.asarray(o, np.float32))
+    d = np.atleast_2d(np.asarray(d, np.float32))
+    r = np.zeros((max(len(o), len(d)), 8), np.float32)
+    r[:, 0:3] = o
+    r[:, 3] = tmin
+    r[:, 4:7] = d
+    r[:, 7] = tmax
+    return r
+
+
+def test_watertight_shared_vertex_and_edges(oracle):
+    tv = _fan(16)
+    # rays straight down through the shared centre vertex and through points on shared edges
+    pts = [(0.0, 0.0)]
+    for i in range(16):
+        a = 2 * np.pi * i / 16
+        for r in (0.25, 0.5, 0.75):
+            pts.append((r * np.cos(a), r * np.sin(a)))
+    o = [(x, y, 1.0) for x, y in pts]
+    rays = _rays(o, (0, 0, -1))
+    hits = oracle.brute_closest(tv, rays)
+    assert (hits["prim"] != 0xFFFFFFFF).all(), "a ray through a shared vertex or edge leaked through the fan"
+    np.testing.assert_allclose(hits["t"], 1.0, rtol=1e-6)
+    # tilted rays through the centre vertex from many directions
+    rng = np.random.default_rng(2)
+    d = rng.standard_normal((500, 3))
+    d[:, 2] = -np.abs(d[:, 2]) - 0.2
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    o = -d * 2.0
+    hits = oracle.brute_closest(tv, _rays(o.astype(np.float32), d.astype(np.float32)))
+    assert (hits["prim"] != 0xFFFFFFFF).all()
+
+
+def test_tie_break_lowest_prim(oracle):
+    tri = np.array([[-1, -1, 0, 1, -1, 0, 0, 1, 0]], np.float32)
+    tv = np.concatenate([tri, tri, tri])  # three coincident triangles
+    rays = _rays([(0.1, 0.0, 1.0), (-0.2, -0.3, -2.0)], [(0, 0, -1), (0, 0, 1)])
+    for hits in (oracle.brute_closest(tv, rays), oracle.bvh(tv).closest(rays)):
+        assert (hits["prim"] == 0).all()
+
+
+def test_axis_parallel_and_degenerate(oracle):
+    tv = np.array([
+        [0, 0, 1, 1, 0, 1, 0, 1, 1],        # triangle in z = 1
+        [0, 0, 2, 0, 0, 2, 0, 0, 2],        # degenerate point triangle
+        [0, 0, 3, 1, 1, 3, 2, 2, 3],        # degenerate line triangle
+    ], np.float32)
+    rays = _rays([(0.25, 0.25, 0.0), (0.25, 0.25, 5.0), (5.0, 0.25, 1.0)], [(0, 0, 1), (0, 0, -1), (-1, 0, 0)])
+    hits = oracle.brute_closest(tv, rays)
+    assert hits["prim"][0] == 0 and hits["prim"][1] == 0
+    assert hits["prim"][2] == 0xFFFFFFFF  # grazing a triangle in its own plane never hits (det == 0)
+    b = oracle.bvh(tv)
+    assert np.array_equal(b.closest(rays), hits)
+
+
+def test_tmin_tmax_window(oracle):
+    tv = np.array([[-1, -1, 2, 1, -1, 2, 0, 1, 2]], np.float32)
+    rays = _rays([(0, 0, 0)] * 4, [(0, 0, 1)] * 4)
+    rays[:, 3] = [0.0, 2.0, 2.5, 0.0]
+    rays[:, 7] = [10.0, 10.0, 10.0, 1.5]
+    hits = oracle.brute_closest(tv, rays)
+    assert list(hits["prim"]) == [0, 0, 0xFFFFFFFF, 0xFFFFFFFF]
+    occ = oracle.brute_any(tv, rays)
+    assert list(occ) == [1, 1, 0, 0]
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_bvh_matches_brute_force(oracle, seed):
+    arrays = procedural.traversal_scene(sphere_freq=8, n_random=3000, seed=seed + 1)
+    tv = arrays.tri_verts()
+    rays = np.concatenate([
+        procedural.incoherent_rays(arrays, 3000, seed=seed + 10),
+        procedural.primary_rays(48, 48),
+    ])
+    b = oracle.bvh(tv)
+    got = b.closest(rays)
+    want = oracle.brute_closest(tv, rays)
+    assert np.array_equal(got, want)
+    anyr = rays.copy()
+    anyr[:, 7] = 0.5
+    assert np.array_equal(b.any(anyr), oracle.brute_any(tv, anyr))
+
+
+def test_empty_scene(oracle):
+    tv = np.zeros((0, 9), np.float32)
+    rays = _rays([(0, 0, 0)], [(0, 0, 1)])
+    b = oracle.bvh(tv)
+    assert b.closest(rays)["prim"][0] == 0xFFFFFFFF
+    assert b.any(rays)[0] == 0
+
+
+class _Cam:
+    pass
+
+
+def _camera(oracle, arrays, w, h):
+    c = _Cam()
+    c.inv_view, c.inv_projection = oracle.camera(arrays.camera_pos, arrays.camera_dir, arrays.fov, w, h)
+    return c
+
+
+def test_path_film_is_progressive_mean_of_samples(oracle):
+    cb = procedural.cornell_box()
+    sc = oracle.scene(cb)
+    cam = _camera(oracle, cb, 24, 16)
+    film = sc.film(cam, 8, 24, 16, 0, 3)
+    s = [sc.samples(cam, 8, 24, 16, f)[0] for f in range(3)]
+    m = s[0].copy()
+    for f in (1, 2):
+        w = np.float32(1.0) / np.float32(f + 1)
+        m = m * (np.float32(1.0) - w) + s[f] * w
+    np.testing.assert_array_equal(film[:, :3], m)
+
+
+def test_path_deterministic_and_fp64_close(oracle):
+    cb = procedural.cornell_box()
+    sc = oracle.scene(cb)
+    cam = _camera(oracle, cb, 32, 32)
+    a, _ = sc.samples(cam, 8, 32, 32, 4)
+    b, _ = sc.samples(cam, 8, 32, 32, 4)
+    assert np.array_equal(a, b)
+    d, _ = sc.samples(cam, 8, 32, 32, 4, fp64=True)
+    close = np.abs(a - d) <= 1e-3 * np.maximum(np.abs(d), 1e-2)
+    assert close.mean() > 0.97
+    assert a.mean() > 0.05  # the box is lit
+
+
+def test_camera_center_ray_looks_along_minus_dir(oracle):
+    cb = procedural.cornell_box()
+    iv, ip = oracle.camera(cb.camera_pos, cb.camera_dir, 45.0, 64, 64)
+    IV = iv.reshape(4, 4).T
+    IP = ip.reshape(4, 4).T
+    t = IP @ np.array([0, 0, 1, 1.0])
+    d = IV @ np.array([*(t[:3] / np.linalg.norm(t[:3])), 0.0])
+    np.testing.assert_allclose(d[:3], [0, 0, -1], atol=1e-6)
+    np.testing.assert_allclose((IV @ np.array([0, 0, 0, 1.0]))[:3], cb.camera_pos, atol=1e-6)

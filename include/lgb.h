@@ -12,7 +12,8 @@
  *     that the library reads during the call only.
  *   - Every entry point returns an lgb_status; on failure lgb_last_error() describes it. No exception or
  *     longjmp crosses this boundary.
- *   - A context is externally synchronised: one host thread at a time per context. Work is stream-ordered.
+ *   - A context is externally synchronised: one host thread at a time per context. Work is stream-ordered;
+ *     the queries of one scene share a device work counter, so issue them on one stream at a time.
  */
 #ifndef LGB_H
 #define LGB_H

@@ -38,6 +38,7 @@ void free_scene(Scene* s) {
     cudaFree(s->bvh.nodes);
     cudaFree(s->bvh.tris);
     cudaFree(s->d_status);
+    cudaFree(s->d_ray_counter);
     cudaFree(s->pt_buf);
 }
 
@@ -223,6 +224,7 @@ LGB_API lgb_status lgb_scene_create(lgb_ctx* ctx, const lgb_scene_desc* d, lgb_s
     UP(&s->d_textures, texs.data(), texs.size());
     uint32_t zero = 0;
     UP(&s->d_status, &zero, 1);
+    UP(&s->d_ray_counter, &zero, 1);
 #undef UP
     if (e != cudaSuccess) {
         lgb_status st = cuda_error(ctx, e, what);
@@ -254,6 +256,7 @@ static lgb_status check_trace(lgb_scene* s, const void* rays, const void* out, u
     if (!s) return LGB_ERR_INVALID_ARGUMENT;
     if (n == 0) return LGB_OK;
     if (!rays || !out) return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "null ray or result buffer");
+    if (n >= 0x80000000u) return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "at most 2^31 - 1 rays per call");
     if ((reinterpret_cast<uintptr_t>(rays) & 15u) || (reinterpret_cast<uintptr_t>(out) & 3u))
         return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "ray buffer must be 16-byte aligned");
     if (!s->bvh.nodes) return set_error(s->ctx, LGB_ERR_NOT_READY, "lgb_bvh_build has not been called");

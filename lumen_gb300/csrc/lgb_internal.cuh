@@ -104,6 +104,7 @@ struct Scene {
     std::vector<lgb_mesh> h_meshes;
     BvhDevice bvh;
     uint32_t* d_status = nullptr;  // device status word
+    uint32_t* d_ray_counter = nullptr;  // work counter of the persistent trace kernels
     // path-tracer work buffers (grown on demand)
     void* pt_buf = nullptr;
     size_t pt_buf_bytes = 0;

@@ -65,7 +65,7 @@ struct Buffers {
     lgb_ray* mrays;
     lgb_hit* mhits;
     uint32_t* sbits;
-    uint32_t* counters; // [0] cur, [1] next, [2] nee, [3..6] class counts
+    uint32_t* counters; // [0] cur, [1] next, [2] nee, [3..6] class counts, [8..10] trace work counters
 };
 
 struct Params {
@@ -217,42 +217,16 @@ __global__ void __launch_bounds__(kThreads) k_camera(Params P, Buffers B) {
     }
 }
 
-// Closest-hit over a device-counted queue of rays.
+// Closest-hit / any-hit over a device-counted queue of rays, persistent with dynamic fetch.
 __global__ void __launch_bounds__(kThreads) k_q_trace_closest(SceneView S, const lgb_ray* __restrict__ rays,
-                                                              lgb_hit* __restrict__ hits, const uint32_t* count_ptr) {
-    const uint32_t n = *count_ptr;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 r0 = ldg4f(&rays[i].ox), r1 = ldg4f(&rays[i].dx);
-        const RayQ r = make_rayq(r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w);
-        uint4 out = make_uint4(LGB_NO_HIT, 0u, 0u, 0u);
-        if (r0.w <= r1.w) {
-            float t, u, v;
-            uint32_t nn = 0, nt = 0;
-            const uint32_t prim = trace_closest_dev<false>(S.nodes, S.tris, r, t, u, v, S.status, nn, nt);
-            if (prim != LGB_NO_HIT) out = make_uint4(prim, __float_as_uint(t), __float_as_uint(u), __float_as_uint(v));
-        }
-        reinterpret_cast<uint4*>(hits)[i] = out;
-    }
+                                                              lgb_hit* __restrict__ hits, const uint32_t* count_ptr,
+                                                              uint32_t* ray_counter) {
+    trace_persistent<false, false>(S.nodes, S.tris, rays, hits, nullptr, 0u, count_ptr, ray_counter, S.status, nullptr);
 }
-
-// Any-hit over a device-counted queue; bit (i & 31) of bits[i >> 5] = occluded.
 __global__ void __launch_bounds__(kThreads) k_q_trace_any(SceneView S, const lgb_ray* __restrict__ rays,
-                                                          uint32_t* __restrict__ bits, const uint32_t* count_ptr) {
-    const uint32_t n = *count_ptr;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
-        const uint32_t i = base + threadIdx.x;
-        bool occ = false;
-        if (i < n) {
-            const float4 r0 = ldg4f(&rays[i].ox), r1 = ldg4f(&rays[i].dx);
-            if (r0.w <= r1.w) {
-                const RayQ r = make_rayq(r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w);
-                occ = trace_any_dev(S.nodes, S.tris, r, S.status);
-            }
-        }
-        const uint32_t word = __ballot_sync(0xffffffffu, occ);
-        if ((threadIdx.x & 31) == 0 && i < n) bits[i >> 5] = word;
-    }
+                                                          uint32_t* __restrict__ bits, const uint32_t* count_ptr,
+                                                          uint32_t* ray_counter) {
+    trace_persistent<true, false>(S.nodes, S.tris, rays, nullptr, bits, 0u, count_ptr, ray_counter, S.status, nullptr);
 }
 
 // path.rgen:49-55: a miss adds the sky colour (shade_atmosphere without a directional light returns
@@ -527,6 +501,7 @@ __global__ void k_rotate(uint32_t* counters) {
         counters[1] = 0u;
         counters[2] = 0u;
         for (int c = 0; c < NUM_CLS; c++) counters[3 + c] = 0u;
+        counters[8] = counters[9] = counters[10] = 0u;
     }
 }
 
@@ -555,7 +530,7 @@ __global__ void __launch_bounds__(kThreads) k_film(Params P, Buffers B, float4* 
 }
 
 __global__ void k_init_counters(uint32_t* counters, uint32_t n) {
-    if (threadIdx.x < 8) counters[threadIdx.x] = threadIdx.x == 0 ? n : 0u;
+    if (threadIdx.x < 16) counters[threadIdx.x] = threadIdx.x == 0 ? n : 0u;
 }
 
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -617,7 +592,9 @@ lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* p
     P.direct_lighting = pp->direct_lighting; P.film_mode = pp->film_mode;
     P.cap = cap;
     const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
-    const int grid_work = sms * 8, grid_trace = sms * 16;
+    int trace_blocks = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&trace_blocks, k_q_trace_closest, kThreads, 0);
+    const int grid_work = sms * 8, grid_trace = sms * std::max(trace_blocks, 1);
     const int bounces = std::max(pp->max_depth, 1);
     for (uint32_t done = 0; done < spp; done += frames_per_chunk) {
         P.frame0 = frame0 + done;
@@ -626,14 +603,15 @@ lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* p
         k_init_counters<<<1, 32, 0, st>>>(B.counters, npaths);
         k_camera<<<grid_work, kThreads, 0, st>>>(P, B);
         for (int depth = 0; depth < bounces; depth++) {
-            k_q_trace_closest<<<grid_trace, kThreads, 0, st>>>(S, B.rays, B.hits, B.counters + 0);
+            k_q_trace_closest<<<grid_trace, kThreads, 0, st>>>(S, B.rays, B.hits, B.counters + 0, B.counters + 8);
             k_classify<<<grid_work, kThreads, 0, st>>>(S, P, B);
             k_shade<CLS_DIFFUSE><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
             k_shade<CLS_CONDUCTOR><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
             k_shade<CLS_SPECULAR><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
             k_shade<CLS_PRINCIPLED><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
-            k_q_trace_any<<<grid_trace, kThreads, 0, st>>>(S, B.srays, B.sbits, B.counters + 2);
-            k_q_trace_closest<<<grid_trace, kThreads, 0, st>>>(S, B.mrays, B.mhits, B.counters + 2);
+            LGB_CUDA_TRY(ctx, cudaMemsetAsync(B.sbits, 0, sizeof(uint32_t) * ((cap + 31) / 32), st));
+            k_q_trace_any<<<grid_trace, kThreads, 0, st>>>(S, B.srays, B.sbits, B.counters + 2, B.counters + 9);
+            k_q_trace_closest<<<grid_trace, kThreads, 0, st>>>(S, B.mrays, B.mhits, B.counters + 2, B.counters + 10);
             k_nee_resolve<<<grid_work, kThreads, 0, st>>>(S, B);
             k_rotate<<<1, 32, 0, st>>>(B.counters);
             std::swap(B.rays, B.rays_next);

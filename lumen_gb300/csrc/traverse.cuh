@@ -20,7 +20,7 @@ struct RayQ {
     float Sx, Sy, Sz;
     int kx, ky, kz;
     float ix, iy, iz;  // inverse direction for box tests (zero components replaced by +-1e-20)
-    uint32_t oct;      // bit a set when d_a >= 0
+    uint32_t oct;      // bit a set when the guarded direction component a is positive
 };
 
 __device__ __forceinline__ float comp(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
@@ -46,7 +46,8 @@ __device__ __forceinline__ RayQ make_rayq(float ox, float oy, float oz, float tm
     float gy = ay < tiny ? copysignf(tiny, dy) : dy;
     float gz = az < tiny ? copysignf(tiny, dz) : dz;
     r.ix = 1.0f / gx; r.iy = 1.0f / gy; r.iz = 1.0f / gz;
-    r.oct = (dx >= 0.0f ? 1u : 0u) | (dy >= 0.0f ? 2u : 0u) | (dz >= 0.0f ? 4u : 0u);
+    // The octant follows the sign of the guarded inverse, so near/far plane selection always agrees with it.
+    r.oct = (gx > 0.0f ? 1u : 0u) | (gy > 0.0f ? 2u : 0u) | (gz > 0.0f ? 4u : 0u);
     return r;
 }
 
@@ -92,13 +93,44 @@ __device__ __forceinline__ bool tri_intersect(const RayQ& r, float4 a, float4 b,
 __device__ __forceinline__ uint4 ldg4(const void* p) { return __ldg(reinterpret_cast<const uint4*>(p)); }
 __device__ __forceinline__ float4 ldg4f(const void* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 
-__device__ __forceinline__ float qbyte(uint32_t lo4, uint32_t hi4, int i) {
-    uint32_t w = i < 4 ? lo4 : hi4;
-    return (float)((w >> (8 * (i & 3))) & 0xffu);
+// Byte k of w as an exact float: the byte is placed under the exponent of 2^23 with one PRMT and the
+// bias is subtracted (cheaper than an integer-to-float conversion, which runs on a quarter-rate pipe).
+template <int K> __device__ __forceinline__ float byte_f(uint32_t w) {
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | K)) - 8388608.0f;
+}
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
 }
 
-// Tests the 8 children of a node. Returns the hit mask of internal children placed at bit (slot ^ oct)
-// (bits 0-7) and the triangle hit mask relative to tri_base (bits 0-23).
+template <int I>
+__device__ __forceinline__ void child_test(const RayQ& r, float tlim, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t fx,
+                                           uint32_t fy, uint32_t fz, float sx, float sy, float sz, float ax, float ay,
+                                           float az, uint32_t imask, uint32_t meta, uint32_t& ih, uint32_t& th) {
+    constexpr int K = I & 3;
+    const float tnx = fmaf(byte_f<K>(nx), sx, ax);
+    const float tny = fmaf(byte_f<K>(ny), sy, ay);
+    const float tnz = fmaf(byte_f<K>(nz), sz, az);
+    const float tfx = fmaf(byte_f<K>(fx), sx, ax);
+    const float tfy = fmaf(byte_f<K>(fy), sy, ay);
+    const float tfz = fmaf(byte_f<K>(fz), sz, az);
+    const float tn = fmaxf(fmax3(tnx, tny, tnz), r.tmin);
+    const float tf = fminf(fmin3(tfx, tfy, tfz), tlim);
+    const uint32_t hit = tn <= tf ? 0xffffffffu : 0u;
+    const uint32_t m = (meta >> (8 * K)) & 0xffu;
+    ih |= (((imask >> I) & 1u) & hit) << ((uint32_t)I ^ r.oct);
+    th |= ((((m >> 5) & 7u) << (m & 31u)) & hit);
+}
+
+// Tests the 8 children of a node. Internal-child hits go to bit (slot ^ oct) of int_hits (bits 0-7), leaf
+// hits to tri_hits relative to tri_base (bits 0-23). Empty slots carry inverted boxes and meta 0, so they
+// contribute nothing and need no branch.
 __device__ __forceinline__ void intersect_node(const RayQ& r, const WideNode* __restrict__ node, float tlim,
                                                uint32_t& child_base, uint32_t& imask, uint32_t& int_hits,
                                                uint32_t& tri_base, uint32_t& tri_hits) {
@@ -107,133 +139,170 @@ __device__ __forceinline__ void intersect_node(const RayQ& r, const WideNode* __
     const uint4 c2 = ldg4(reinterpret_cast<const char*>(node) + 32);
     const uint4 c3 = ldg4(reinterpret_cast<const char*>(node) + 48);
     const uint4 c4 = ldg4(reinterpret_cast<const char*>(node) + 64);
-    const float px = __uint_as_float(c0.x), py = __uint_as_float(c0.y), pz = __uint_as_float(c0.z);
     const uint32_t e = c0.w;
     imask = e >> 24;
     child_base = c1.x;
     tri_base = c1.y;
-    const uint32_t meta_lo = c1.z, meta_hi = c1.w;
     const float sx = __uint_as_float((e & 0xffu) << 23) * r.ix;
     const float sy = __uint_as_float(((e >> 8) & 0xffu) << 23) * r.iy;
     const float sz = __uint_as_float(((e >> 16) & 0xffu) << 23) * r.iz;
-    const float ax = (px - r.ox) * r.ix;
-    const float ay = (py - r.oy) * r.iy;
-    const float az = (pz - r.oz) * r.iz;
-    // near/far byte planes per axis
-    const bool fx = r.ix >= 0.0f, fy = r.iy >= 0.0f, fz = r.iz >= 0.0f;
-    const uint32_t nx0 = fx ? c2.x : c3.z, nx1 = fx ? c2.y : c3.w, fx0 = fx ? c3.z : c2.x, fx1 = fx ? c3.w : c2.y;
-    const uint32_t ny0 = fy ? c2.z : c4.x, ny1 = fy ? c2.w : c4.y, fy0 = fy ? c4.x : c2.z, fy1 = fy ? c4.y : c2.w;
-    const uint32_t nz0 = fz ? c3.x : c4.z, nz1 = fz ? c3.y : c4.w, fz0 = fz ? c4.z : c3.x, fz1 = fz ? c4.w : c3.y;
+    const float ax = (__uint_as_float(c0.x) - r.ox) * r.ix;
+    const float ay = (__uint_as_float(c0.y) - r.oy) * r.iy;
+    const float az = (__uint_as_float(c0.z) - r.oz) * r.iz;
+    // near and far byte planes per axis: qlo is near for a non-negative direction component
+    const bool px = r.oct & 1u, py = r.oct & 2u, pz = r.oct & 4u;
+    const uint32_t nx0 = px ? c2.x : c3.z, nx1 = px ? c2.y : c3.w, fx0 = px ? c3.z : c2.x, fx1 = px ? c3.w : c2.y;
+    const uint32_t ny0 = py ? c2.z : c4.x, ny1 = py ? c2.w : c4.y, fy0 = py ? c4.x : c2.z, fy1 = py ? c4.y : c2.w;
+    const uint32_t nz0 = pz ? c3.x : c4.z, nz1 = pz ? c3.y : c4.w, fz0 = pz ? c4.z : c3.x, fz1 = pz ? c4.w : c3.y;
     uint32_t ih = 0, th = 0;
-#pragma unroll
-    for (int i = 0; i < 8; i++) {
-        const uint32_t meta = ((i < 4 ? meta_lo : meta_hi) >> (8 * (i & 3))) & 0xffu;
-        const bool is_int = (imask >> i) & 1u;
-        if (!is_int && meta == 0u) continue;
-        const float tnx = fmaf(qbyte(nx0, nx1, i), sx, ax);
-        const float tny = fmaf(qbyte(ny0, ny1, i), sy, ay);
-        const float tnz = fmaf(qbyte(nz0, nz1, i), sz, az);
-        const float tfx = fmaf(qbyte(fx0, fx1, i), sx, ax);
-        const float tfy = fmaf(qbyte(fy0, fy1, i), sy, ay);
-        const float tfz = fmaf(qbyte(fz0, fz1, i), sz, az);
-        const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
-        const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tlim));
-        if (tn <= tf) {
-            if (is_int) ih |= 1u << (i ^ r.oct);
-            else th |= ((meta >> 5) & 7u) << (meta & 31u);
-        }
-    }
+    child_test<0>(r, tlim, nx0, ny0, nz0, fx0, fy0, fz0, sx, sy, sz, ax, ay, az, imask, c1.z, ih, th);
+    child_test<1>(r, tlim, nx0, ny0, nz0, fx0, fy0, fz0, sx, sy, sz, ax, ay, az, imask, c1.z, ih, th);
+    child_test<2>(r, tlim, nx0, ny0, nz0, fx0, fy0, fz0, sx, sy, sz, ax, ay, az, imask, c1.z, ih, th);
+    child_test<3>(r, tlim, nx0, ny0, nz0, fx0, fy0, fz0, sx, sy, sz, ax, ay, az, imask, c1.z, ih, th);
+    child_test<4>(r, tlim, nx1, ny1, nz1, fx1, fy1, fz1, sx, sy, sz, ax, ay, az, imask, c1.w, ih, th);
+    child_test<5>(r, tlim, nx1, ny1, nz1, fx1, fy1, fz1, sx, sy, sz, ax, ay, az, imask, c1.w, ih, th);
+    child_test<6>(r, tlim, nx1, ny1, nz1, fx1, fy1, fz1, sx, sy, sz, ax, ay, az, imask, c1.w, ih, th);
+    child_test<7>(r, tlim, nx1, ny1, nz1, fx1, fy1, fz1, sx, sy, sz, ax, ay, az, imask, c1.w, ih, th);
     int_hits = ih;
     tri_hits = th;
 }
 
-// Closest-hit traversal. Returns prim (LGB_NO_HIT on a miss). COUNT adds node and triangle fetches.
-template <bool COUNT>
-__device__ __forceinline__ uint32_t trace_closest_dev(const WideNode* __restrict__ nodes, const WideTri* __restrict__ tris,
-                                                       const RayQ& r, float& t_best, float& u_best, float& v_best,
-                                                       uint32_t* status, uint32_t& n_nodes, uint32_t& n_tris) {
+// Persistent ray queries. Every warp loops until the ray list is exhausted: lanes whose ray has finished take
+// a new ray index from a global counter (one atomic per warp per refill), so short rays do not leave lanes
+// idle while the longest ray of a warp finishes. Each loop iteration visits one node of each active lane
+// and tests that node's leaf triangles.
+//   ANY = false: closest hit into hits[id]; ANY = true: occlusion bit id of occ_bits (which must be zeroed).
+//   COUNT adds the nodes and triangles fetched into counters[0..1].
+// The ray count is read from *count_ptr when it is non-null, else n.
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ nodes, const WideTri* __restrict__ tris,
+                                                 const lgb_ray* __restrict__ rays, lgb_hit* __restrict__ hits,
+                                                 uint32_t* __restrict__ occ_bits, uint32_t n, const uint32_t* count_ptr,
+                                                 uint32_t* ray_counter, uint32_t* status,
+                                                 unsigned long long* counters) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const uint32_t lanemask_lt = (1u << lane) - 1u;
+    if (count_ptr) n = *count_ptr;
+    RayQ r;
     uint2 stack[kStackSize];
     int sp = 0;
-    t_best = r.tmax;
-    uint32_t best = LGB_NO_HIT;
-    u_best = 0.0f; v_best = 0.0f;
-    // virtual parent of the root: child_base 0, slot 0 internal
-    uint32_t g_base = 0u, g_hits = 1u << (0u ^ r.oct), g_imask = 1u;
-    uint32_t visits = 0;
+    uint32_t ray_id = 0, g_base = 0, g_hm = 0, best = LGB_NO_HIT, visits = 0;
+    float t_best = 0.0f, u_best = 0.0f, v_best = 0.0f;
+    uint32_t n_nodes = 0, n_tris = 0;
+    bool active = false, exhausted = false;
     while (true) {
-        while (g_hits) {
-            const int pos = 31 - __clz(g_hits);
-            g_hits &= ~(1u << pos);
-            const uint32_t slot = (uint32_t)pos ^ r.oct;
-            const uint32_t node_idx = g_base + __popc(g_imask & ((1u << slot) - 1u));
-            if (++visits > kMaxVisits) { atomicOr(status, STATUS_VISIT_LIMIT); return best; }
-            if (g_hits) {
-                if (sp >= kStackSize) { atomicOr(status, STATUS_STACK_OVERFLOW); return best; }
-                stack[sp++] = make_uint2(g_base, (g_hits << 8) | g_imask);
-            }
-            uint32_t tri_base, tri_hits;
-            intersect_node(r, nodes + node_idx, t_best, g_base, g_imask, g_hits, tri_base, tri_hits);
-            if (COUNT) n_nodes++;
-            while (tri_hits) {
-                const int k = __ffs(tri_hits) - 1;
-                tri_hits &= tri_hits - 1u;
-                const WideTri* tp = tris + tri_base + k;
-                const float4 a = ldg4f(&tp->a), b = ldg4f(&tp->b), c = ldg4f(&tp->c);
-                if (COUNT) n_tris++;
-                float t, u, v;
-                if (tri_intersect(r, a, b, c, t_best, t, u, v)) {
-                    const uint32_t prim = __float_as_uint(a.w);
-                    if (t < t_best || prim < best) {
-                        t_best = t; best = prim; u_best = u; v_best = v;
+        if (!exhausted) {
+            const uint32_t need = __ballot_sync(FULL, !active);
+            if (need) {
+                uint32_t base = 0;
+                if (lane == 0) base = atomicAdd(ray_counter, (uint32_t)__popc(need));
+                base = __shfl_sync(FULL, base, 0);
+                if (base + (uint32_t)__popc(need) >= n) exhausted = true;
+                if (!active) {
+                    const uint32_t id = base + (uint32_t)__popc(need & lanemask_lt);
+                    if (id < n) {
+                        const float4 r0 = ldg4f(&rays[id].ox), r1 = ldg4f(&rays[id].dx);
+                        r = make_rayq(r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w);
+                        ray_id = id;
+                        sp = 0;
+                        g_base = 0u;
+                        // virtual parent of the root: slot 0 internal and hit; an empty interval visits nothing
+                        g_hm = r.tmin <= r.tmax ? (((1u << (0u ^ r.oct)) << 8) | 1u) : 1u;
+                        best = LGB_NO_HIT;
+                        t_best = r.tmax;
+                        u_best = v_best = 0.0f;
+                        visits = 0;
+                        active = true;
                     }
                 }
             }
         }
-        if (sp == 0) break;
-        const uint2 g = stack[--sp];
-        g_base = g.x;
-        g_hits = g.y >> 8;
-        g_imask = g.y & 0xffu;
-    }
-    return best;
-}
-
-// Any-hit traversal: true on the first triangle hit in [tmin, tmax].
-__device__ __forceinline__ bool trace_any_dev(const WideNode* __restrict__ nodes, const WideTri* __restrict__ tris,
-                                              const RayQ& r, uint32_t* status) {
-    uint2 stack[kStackSize];
-    int sp = 0;
-    uint32_t g_base = 0u, g_hits = 1u << (0u ^ r.oct), g_imask = 1u;
-    uint32_t visits = 0;
-    while (true) {
-        while (g_hits) {
-            const int pos = 31 - __clz(g_hits);
-            g_hits &= ~(1u << pos);
-            const uint32_t slot = (uint32_t)pos ^ r.oct;
-            const uint32_t node_idx = g_base + __popc(g_imask & ((1u << slot) - 1u));
-            if (++visits > kMaxVisits) { atomicOr(status, STATUS_VISIT_LIMIT); return false; }
-            if (g_hits) {
-                if (sp >= kStackSize) { atomicOr(status, STATUS_STACK_OVERFLOW); return false; }
-                stack[sp++] = make_uint2(g_base, (g_hits << 8) | g_imask);
+        if (!__any_sync(FULL, active)) break;
+        if (active) {
+            bool done = false, occluded = false;
+            uint32_t hm = g_hm >> 8;
+            if (hm == 0u) {
+                if (sp == 0) {
+                    done = true;
+                } else {
+                    const uint2 g = stack[--sp];
+                    g_base = g.x;
+                    g_hm = g.y;
+                    hm = g_hm >> 8;
+                }
             }
-            uint32_t tri_base, tri_hits;
-            intersect_node(r, nodes + node_idx, r.tmax, g_base, g_imask, g_hits, tri_base, tri_hits);
-            while (tri_hits) {
-                const int k = __ffs(tri_hits) - 1;
-                tri_hits &= tri_hits - 1u;
-                const WideTri* tp = tris + tri_base + k;
-                const float4 a = ldg4f(&tp->a), b = ldg4f(&tp->b), c = ldg4f(&tp->c);
-                float t, u, v;
-                if (tri_intersect(r, a, b, c, r.tmax, t, u, v)) return true;
+            if (!done) {
+                const uint32_t imask = g_hm & 0xffu;
+                const int pos = 31 - __clz(hm);
+                hm &= ~(1u << pos);
+                const uint32_t slot = (uint32_t)pos ^ r.oct;
+                const uint32_t node_idx = g_base + __popc(imask & ((1u << slot) - 1u));
+                if (hm) {
+                    if (sp >= kStackSize) {
+                        atomicOr(status, STATUS_STACK_OVERFLOW);
+                        done = true;
+                    } else {
+                        stack[sp++] = make_uint2(g_base, (hm << 8) | imask);
+                    }
+                }
+                if (++visits > kMaxVisits) {
+                    atomicOr(status, STATUS_VISIT_LIMIT);
+                    done = true;
+                }
+                if (!done) {
+                    uint32_t nb, nimask, nhits, tri_base, tri_hits;
+                    intersect_node(r, nodes + node_idx, ANY ? r.tmax : t_best, nb, nimask, nhits, tri_base, tri_hits);
+                    if (COUNT) n_nodes++;
+                    g_base = nb;
+                    g_hm = (nhits << 8) | nimask;
+                    while (tri_hits) {
+                        const int k = __ffs(tri_hits) - 1;
+                        tri_hits &= tri_hits - 1u;
+                        const WideTri* tp = tris + tri_base + k;
+                        const float4 a = ldg4f(&tp->a), b = ldg4f(&tp->b), c = ldg4f(&tp->c);
+                        if (COUNT) n_tris++;
+                        float t, u, v;
+                        if (tri_intersect(r, a, b, c, ANY ? r.tmax : t_best, t, u, v)) {
+                            if (ANY) {
+                                occluded = true;
+                                done = true;
+                                break;
+                            }
+                            const uint32_t prim = __float_as_uint(a.w);
+                            if (t < t_best || prim < best) {
+                                t_best = t;
+                                best = prim;
+                                u_best = u;
+                                v_best = v;
+                            }
+                        }
+                    }
+                }
+            }
+            if (done) {
+                if (ANY) {
+                    if (occluded) atomicOr(&occ_bits[ray_id >> 5], 1u << (ray_id & 31u));
+                } else {
+                    uint4 out = make_uint4(best, __float_as_uint(best == LGB_NO_HIT ? 0.0f : t_best),
+                                           __float_as_uint(u_best), __float_as_uint(v_best));
+                    reinterpret_cast<uint4*>(hits)[ray_id] = out;
+                }
+                active = false;
             }
         }
-        if (sp == 0) break;
-        const uint2 g = stack[--sp];
-        g_base = g.x;
-        g_hits = g.y >> 8;
-        g_imask = g.y & 0xffu;
     }
-    return false;
+    if (COUNT) {
+        unsigned long long a = n_nodes, b = n_tris;
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(FULL, a, o);
+            b += __shfl_xor_sync(FULL, b, o);
+        }
+        if (lane == 0) {
+            atomicAdd(&counters[0], a);
+            atomicAdd(&counters[1], b);
+        }
+    }
 }
 
 }  // namespace lgb

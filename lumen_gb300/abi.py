@@ -76,7 +76,7 @@ class SceneDesc(C.Structure):
 
 
 class BuildOpts(C.Structure):
-    _fields_ = [("leaf_max", C.c_uint32), ("reserved", C.c_uint32 * 7)]
+    _fields_ = [("leaf_max", C.c_uint32), ("treelet_rounds", C.c_uint32), ("reserved", C.c_uint32 * 6)]
 
 
 class BuildStats(C.Structure):

@@ -9,7 +9,9 @@
 //   2. 63-bit Morton codes of triangle centroids
 //   3. LSD radix sort of (code, triangle) pairs, 8 passes of 8 bits, stable block-local ranking
 //   4. binary radix tree over the sorted codes (Karras, HPG 2012), ties broken by position
-//   5. bottom-up node boxes (first arrival stops, second merges)
+//   5. bottom-up node boxes, SAH costs and triangle counts (first arrival stops, second merges)
+//   5b. treelet restructuring rounds: 7-leaf treelets re-topologised for minimum SAH cost (Karras and
+//       Aila, HPG 2013)
 //   6. top-down collapse to 8-wide nodes, one level per launch: each binary node becomes a wide node
 //      by repeatedly opening its largest-area internal child; children are placed in octant slots, boxes
 //      quantised to 8 bits with outward rounding, and leaf triangles copied into leaf order.
@@ -228,10 +230,19 @@ __global__ void k_radix_tree(const uint64_t* __restrict__ keys, int n, uint32_t*
 }
 
 // Bottom-up boxes. node_box: 6 floats per internal node; leaf boxes come from tri_box via sorted vals.
+// SAH constants of the binary tree the treelet pass optimises: cost of an internal node and of a triangle.
+constexpr float kCostNode = 1.2f;
+constexpr float kCostTri = 1.0f;
+
+__device__ __forceinline__ float box_half_area(const float* b) {
+    const float dx = fmaxf(b[3] - b[0], 0.0f), dy = fmaxf(b[4] - b[1], 0.0f), dz = fmaxf(b[5] - b[2], 0.0f);
+    return dx * dy + dy * dz + dz * dx;
+}
+
 __global__ void k_bottom_up(int n, const uint32_t* __restrict__ vals, const float* __restrict__ tri_box,
                             const uint32_t* __restrict__ left, const uint32_t* __restrict__ right,
                             const uint32_t* __restrict__ parent_int, const uint32_t* __restrict__ parent_leaf,
-                            float* node_box, uint32_t* flags) {
+                            float* node_box, float* node_cost, uint32_t* node_count, uint32_t* flags) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     uint32_t node = parent_leaf[k];
@@ -249,8 +260,163 @@ __global__ void k_bottom_up(int n, const uint32_t* __restrict__ vals, const floa
             b[3 + a] = fmaxf(__ldcg(&A[3 + a]), __ldcg(&B[3 + a]));
         }
         for (int a = 0; a < 6; a++) __stcg(&node_box[6 * (size_t)node + a], b[a]);
+        const float cl_cost = (cl & kLeafFlag) ? kCostTri * box_half_area(A) : __ldcg(&node_cost[cl]);
+        const float cr_cost = (cr & kLeafFlag) ? kCostTri * box_half_area(B) : __ldcg(&node_cost[cr]);
+        const uint32_t cl_cnt = (cl & kLeafFlag) ? 1u : __ldcg(&node_count[cl]);
+        const uint32_t cr_cnt = (cr & kLeafFlag) ? 1u : __ldcg(&node_count[cr]);
+        __stcg(&node_cost[node], kCostNode * box_half_area(b) + cl_cost + cr_cost);
+        __stcg(&node_count[node], cl_cnt + cr_cnt);
         if (node == 0) return;
         node = parent_int[node];
+    }
+}
+
+// ---------------- treelet restructuring (Karras and Aila, HPG 2013) ----------------
+// A bottom-up pass like k_bottom_up. When the second child of a node with at least `gamma` triangles has
+// finished, the arriving thread grows a treelet of up to 7 leaves under it (always splitting the
+// largest-area leaf), finds the binary topology over those leaves with minimum SAH cost by dynamic
+// programming over all 127 leaf subsets, and rebuilds the treelet's internal nodes in place when that
+// lowers the cost. Treelets of different threads are disjoint: a node's descendants are final before the
+// node is processed, and its ancestors are untouched until it is done.
+constexpr int kTreeletLeaves = 7;
+
+struct TreeArgs {
+    uint32_t* left;
+    uint32_t* right;
+    uint32_t* parent_int;
+    uint32_t* parent_leaf;
+    float* node_box;
+    float* node_cost;
+    uint32_t* node_count;
+    const float* tri_box;
+    const uint32_t* vals;
+    uint32_t* flags;
+};
+
+__device__ __forceinline__ void load_ref_box(const TreeArgs& T, uint32_t ref, float* b) {
+    if (ref & kLeafFlag) {
+        const float* src = &T.tri_box[6 * (size_t)T.vals[ref & ~kLeafFlag]];
+        for (int a = 0; a < 6; a++) b[a] = src[a];
+    } else {
+        for (int a = 0; a < 6; a++) b[a] = __ldcg(&T.node_box[6 * (size_t)ref + a]);
+    }
+}
+
+__device__ void optimise_treelet(const TreeArgs& T, uint32_t root) {
+    uint32_t leaves[kTreeletLeaves];
+    uint32_t inner[kTreeletLeaves - 1];
+    float lbox[kTreeletLeaves][6];
+    float larea[kTreeletLeaves];
+    int nl = 2, ni = 1;
+    inner[0] = root;
+    leaves[0] = __ldcg(&T.left[root]);
+    leaves[1] = __ldcg(&T.right[root]);
+    load_ref_box(T, leaves[0], lbox[0]);
+    load_ref_box(T, leaves[1], lbox[1]);
+    larea[0] = box_half_area(lbox[0]);
+    larea[1] = box_half_area(lbox[1]);
+    while (nl < kTreeletLeaves) {
+        int best = -1;
+        float ba = -1.0f;
+        for (int k = 0; k < nl; k++)
+            if (!(leaves[k] & kLeafFlag) && larea[k] > ba) { ba = larea[k]; best = k; }
+        if (best < 0) break;
+        const uint32_t r = leaves[best];
+        inner[ni++] = r;
+        leaves[best] = __ldcg(&T.left[r]);
+        leaves[nl] = __ldcg(&T.right[r]);
+        load_ref_box(T, leaves[best], lbox[best]);
+        load_ref_box(T, leaves[nl], lbox[nl]);
+        larea[best] = box_half_area(lbox[best]);
+        larea[nl] = box_half_area(lbox[nl]);
+        nl++;
+    }
+    if (nl < 3) return;
+    float cost[1 << kTreeletLeaves];
+    uint8_t part[1 << kTreeletLeaves];
+    const uint32_t full = (1u << nl) - 1u;
+    for (uint32_t sset = 1; sset <= full; sset++) {
+        if ((sset & (sset - 1u)) == 0u) {
+            const int k = __ffs(sset) - 1;
+            cost[sset] = (leaves[k] & kLeafFlag) ? kCostTri * larea[k] : __ldcg(&T.node_cost[leaves[k]]);
+            part[sset] = 0;
+            continue;
+        }
+        float b[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+        for (int k = 0; k < nl; k++)
+            if (sset & (1u << k))
+                for (int a = 0; a < 3; a++) { b[a] = fminf(b[a], lbox[k][a]); b[3 + a] = fmaxf(b[3 + a], lbox[k][3 + a]); }
+        const uint32_t low = sset & (0u - sset);
+        float bc = FLT_MAX;
+        uint32_t bp = low;
+        for (uint32_t q = (sset - 1u) & sset; q; q = (q - 1u) & sset) {
+            if (!(q & low)) continue;  // each unordered split once
+            const float c = cost[q] + cost[sset ^ q];
+            if (c < bc) { bc = c; bp = q; }
+        }
+        cost[sset] = kCostNode * box_half_area(b) + bc;
+        part[sset] = (uint8_t)bp;
+    }
+    if (!(cost[full] < __ldcg(&T.node_cost[root]) * 0.9999f)) return;
+    // rebuild top-down, reusing the treelet's internal nodes
+    uint32_t st_set[kTreeletLeaves], st_node[kTreeletLeaves];
+    int sp = 0, next = 1;
+    st_set[sp] = full;
+    st_node[sp] = root;
+    sp++;
+    while (sp > 0) {
+        sp--;
+        const uint32_t sset = st_set[sp], node = st_node[sp];
+        const uint32_t sub[2] = {part[sset], sset ^ part[sset]};
+        uint32_t ref[2];
+        for (int c = 0; c < 2; c++) {
+            if ((sub[c] & (sub[c] - 1u)) == 0u) {
+                ref[c] = leaves[__ffs(sub[c]) - 1];
+            } else {
+                ref[c] = inner[next++];
+                st_set[sp] = sub[c];
+                st_node[sp] = ref[c];
+                sp++;
+            }
+            if (ref[c] & kLeafFlag) __stcg(&T.parent_leaf[ref[c] & ~kLeafFlag], node);
+            else __stcg(&T.parent_int[ref[c]], node);
+        }
+        __stcg(&T.left[node], ref[0]);
+        __stcg(&T.right[node], ref[1]);
+        float b[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+        uint32_t cnt = 0;
+        for (int k = 0; k < nl; k++) {
+            if (!(sset & (1u << k))) continue;
+            for (int a = 0; a < 3; a++) { b[a] = fminf(b[a], lbox[k][a]); b[3 + a] = fmaxf(b[3 + a], lbox[k][3 + a]); }
+            cnt += (leaves[k] & kLeafFlag) ? 1u : __ldcg(&T.node_count[leaves[k]]);
+        }
+        for (int a = 0; a < 6; a++) __stcg(&T.node_box[6 * (size_t)node + a], b[a]);
+        __stcg(&T.node_cost[node], cost[sset]);
+        __stcg(&T.node_count[node], cnt);
+    }
+}
+
+__global__ void k_treelet(TreeArgs T, int n, uint32_t gamma) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t node = __ldcg(&T.parent_leaf[k]);
+    for (int steps = 0; steps < n; steps++) {
+        __threadfence();
+        if (atomicAdd(&T.flags[node], 1u) == 0u) return;
+        __threadfence();
+        // children are final: refresh this node's cost, then try to improve its treelet
+        const uint32_t cl = __ldcg(&T.left[node]), cr = __ldcg(&T.right[node]);
+        float bl[6], br[6];
+        load_ref_box(T, cl, bl);
+        load_ref_box(T, cr, br);
+        const float ccl = (cl & kLeafFlag) ? kCostTri * box_half_area(bl) : __ldcg(&T.node_cost[cl]);
+        const float ccr = (cr & kLeafFlag) ? kCostTri * box_half_area(br) : __ldcg(&T.node_cost[cr]);
+        float nb[6];
+        for (int a = 0; a < 3; a++) { nb[a] = fminf(bl[a], br[a]); nb[3 + a] = fmaxf(bl[3 + a], br[3 + a]); }
+        __stcg(&T.node_cost[node], kCostNode * box_half_area(nb) + ccl + ccr);
+        if (__ldcg(&T.node_count[node]) >= gamma) optimise_treelet(T, node);
+        if (node == 0) return;
+        node = __ldcg(&T.parent_int[node]);
     }
 }
 
@@ -258,8 +424,7 @@ __global__ void k_bottom_up(int n, const uint32_t* __restrict__ vals, const floa
 struct CollapseArgs {
     const uint32_t* left;
     const uint32_t* right;
-    const uint32_t* range_lo;
-    const uint32_t* range_hi;
+    const uint32_t* node_count;
     const float* node_box;
     const float* tri_box;
     const uint32_t* vals;   // sorted position -> original triangle
@@ -278,10 +443,23 @@ __device__ __forceinline__ void ref_box(const CollapseArgs& A, uint32_t ref, flo
     for (int a = 0; a < 6; a++) b[a] = src[a];
 }
 __device__ __forceinline__ uint32_t ref_count(const CollapseArgs& A, uint32_t ref) {
-    return (ref & kLeafFlag) ? 1u : (A.range_hi[ref] - A.range_lo[ref] + 1u);
+    return (ref & kLeafFlag) ? 1u : A.node_count[ref];
 }
-__device__ __forceinline__ uint32_t ref_first(const CollapseArgs& A, uint32_t ref) {
-    return (ref & kLeafFlag) ? (ref & ~kLeafFlag) : A.range_lo[ref];
+// Sorted-order positions of the (at most 3) triangles under a small subtree.
+__device__ __forceinline__ int gather_leaves(const CollapseArgs& A, uint32_t ref, uint32_t* out) {
+    uint32_t st[4];
+    int sp = 0, n = 0;
+    st[sp++] = ref;
+    while (sp > 0 && n < 3) {
+        const uint32_t r = st[--sp];
+        if (r & kLeafFlag) {
+            out[n++] = r & ~kLeafFlag;
+        } else if (sp + 2 <= 4) {
+            st[sp++] = A.right[r];
+            st[sp++] = A.left[r];
+        }
+    }
+    return n;
 }
 __device__ __forceinline__ float half_area(const float* b) {
     float dx = fmaxf(b[3] - b[0], 0.0f), dy = fmaxf(b[4] - b[1], 0.0f), dz = fmaxf(b[5] - b[2], 0.0f);
@@ -407,9 +585,10 @@ __global__ void k_collapse(CollapseArgs A, const uint2* __restrict__ qin, uint32
             int_rank++;
         } else {
             meta[s] = (uint8_t)((((1u << cnt) - 1u) << 5) | tri_off);
-            uint32_t first = ref_first(A, ch[c]);
+            uint32_t pos[3];
+            gather_leaves(A, ch[c], pos);
             for (uint32_t k = 0; k < cnt; k++) {
-                uint32_t prim = A.vals[first + k];
+                uint32_t prim = A.vals[pos[k]];
                 const float* v = A.tri_verts + 9 * (size_t)prim;
                 WideTri t;
                 t.a = make_float4(v[0], v[1], v[2], __uint_as_float(prim));
@@ -439,6 +618,9 @@ lgb_status build_bvh(Scene* s, const lgb_build_opts* opts, lgb_build_stats* stat
     Ctx* ctx = s->ctx;
     const uint32_t n = s->num_tris;
     int leaf_max = (opts && opts->leaf_max) ? (int)opts->leaf_max : 3;
+    int treelet_rounds = 3;
+    if (opts && opts->treelet_rounds)
+        treelet_rounds = opts->treelet_rounds == 0xFFFFFFFFu ? 0 : (int)std::min(opts->treelet_rounds, 16u);
     if (leaf_max < 1 || leaf_max > 3) return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "leaf_max must be 1..3");
     if (n == 0) return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "scene has no triangles");
     cudaStream_t st = 0;
@@ -451,7 +633,8 @@ lgb_status build_bvh(Scene* s, const lgb_build_opts* opts, lgb_build_stats* stat
     uint64_t *keys = nullptr, *keys2 = nullptr;
     uint32_t *vals = nullptr, *vals2 = nullptr, *counts = nullptr, *bounds = nullptr;
     uint32_t *left = nullptr, *right = nullptr, *pint = nullptr, *pleaf = nullptr, *rlo = nullptr, *rhi = nullptr, *flags = nullptr;
-    float *tri_box = nullptr, *node_box = nullptr, *sah = nullptr;
+    float *tri_box = nullptr, *node_box = nullptr, *sah = nullptr, *node_cost = nullptr;
+    uint32_t* node_count = nullptr;
     uint2 *qa = nullptr, *qb = nullptr;
     uint32_t* counters = nullptr;
     WideNode* nodes = nullptr;
@@ -471,6 +654,7 @@ lgb_status build_bvh(Scene* s, const lgb_build_opts* opts, lgb_build_stats* stat
         STEP(dalloc(&left, nint)); STEP(dalloc(&right, nint)); STEP(dalloc(&pint, nint)); STEP(dalloc(&pleaf, n));
         STEP(dalloc(&rlo, nint)); STEP(dalloc(&rhi, nint)); STEP(dalloc(&flags, nint));
         STEP(dalloc(&tri_box, 6 * (size_t)n)); STEP(dalloc(&node_box, 6 * (size_t)nint)); STEP(dalloc(&sah, 1));
+        STEP(dalloc(&node_cost, nint)); STEP(dalloc(&node_count, nint));
         STEP(dalloc(&qa, nint + 1)); STEP(dalloc(&qb, nint + 1)); STEP(dalloc(&counters, 4));
         STEP(dalloc(&nodes, nint)); STEP(dalloc(&tris, n));
 
@@ -493,8 +677,15 @@ lgb_status build_bvh(Scene* s, const lgb_build_opts* opts, lgb_build_stats* stat
         if (n > 1) {
             k_radix_tree<<<(n - 1 + 255) / 256, 256, 0, st>>>(keys, (int)n, left, right, pint, pleaf, rlo, rhi);
             STEP(cudaMemsetAsync(flags, 0, sizeof(uint32_t) * nint, st));
-            k_bottom_up<<<(n + 255) / 256, 256, 0, st>>>((int)n, vals, tri_box, left, right, pint, pleaf, node_box, flags);
+            k_bottom_up<<<(n + 255) / 256, 256, 0, st>>>((int)n, vals, tri_box, left, right, pint, pleaf, node_box,
+                                                         node_cost, node_count, flags);
             STEP(cudaGetLastError());
+            TreeArgs T{left, right, pint, pleaf, node_box, node_cost, node_count, tri_box, vals, flags};
+            for (int round = 0; round < treelet_rounds; round++) {
+                STEP(cudaMemsetAsync(flags, 0, sizeof(uint32_t) * nint, st));
+                k_treelet<<<(n + 127) / 128, 128, 0, st>>>(T, (int)n, (uint32_t)kTreeletLeaves);
+                STEP(cudaGetLastError());
+            }
             root_ref = 0;
         } else {
             root_ref = kLeafFlag;
@@ -511,7 +702,7 @@ lgb_status build_bvh(Scene* s, const lgb_build_opts* opts, lgb_build_stats* stat
                    fmaxf(rb[5] - rb[2], 0.f) * fmaxf(rb[3] - rb[0], 0.f);
 
         CollapseArgs A;
-        A.left = left; A.right = right; A.range_lo = rlo; A.range_hi = rhi; A.node_box = node_box; A.tri_box = tri_box;
+        A.left = left; A.right = right; A.node_count = node_count; A.node_box = node_box; A.tri_box = tri_box;
         A.vals = vals; A.tri_verts = s->d_tri_verts; A.nodes = nodes; A.tris = tris; A.counters = counters; A.sah = sah;
         A.leaf_max = leaf_max;
         A.inv_root_area = ra > 0.0f ? 1.0f / ra : 0.0f;
@@ -586,6 +777,7 @@ cleanup:
     cudaFree(keys); cudaFree(keys2); cudaFree(vals); cudaFree(vals2); cudaFree(counts); cudaFree(bounds);
     cudaFree(left); cudaFree(right); cudaFree(pint); cudaFree(pleaf); cudaFree(rlo); cudaFree(rhi); cudaFree(flags);
     cudaFree(tri_box); cudaFree(node_box); cudaFree(sah); cudaFree(qa); cudaFree(qb); cudaFree(counters);
+    cudaFree(node_cost); cudaFree(node_count);
     if (nodes) cudaFree(nodes);
     if (tris) cudaFree(tris);
     cudaEventDestroy(e0);

@@ -199,9 +199,10 @@ class GpuScene:
         self.handle = h
         self.stats = None
 
-    def build(self, leaf_max: int = 0) -> abi.BuildStats:
+    def build(self, leaf_max: int = 0, treelet_rounds: int = 0) -> abi.BuildStats:
         opts = abi.BuildOpts()
         opts.leaf_max = leaf_max
+        opts.treelet_rounds = treelet_rounds
         stats = abi.BuildStats()
         _check(self.lib, self.ctx.handle, self.lib.lgb_bvh_build(self.handle, C.byref(opts), C.byref(stats)))
         self.stats = stats

@@ -77,11 +77,11 @@ def test_small_scene_matches_oracle(ctx, oracle):
     assert np.array_equal(gpu_any(sc, short), b.any(short))
 
 
-@pytest.mark.parametrize("leaf_max", [1, 2, 3])
-def test_leaf_sizes(ctx, oracle, leaf_max):
+@pytest.mark.parametrize("leaf_max,rounds", [(1, 0), (2, 0), (3, 0), (3, 0xFFFFFFFF), (2, 6)])
+def test_leaf_sizes_and_treelet_rounds(ctx, oracle, leaf_max, rounds):
     arrays = procedural.traversal_scene(sphere_freq=12, n_random=3000, seed=4)
     sc = GpuScene(ctx, arrays)
-    sc.build(leaf_max=leaf_max)
+    sc.build(leaf_max=leaf_max, treelet_rounds=rounds)
     rays = procedural.incoherent_rays(arrays, 20000, seed=9)
     assert_hits_equal(gpu_closest(sc, rays), oracle.bvh(arrays.tri_verts()).closest(rays))
 

@@ -115,22 +115,13 @@ def make_workload(cache=True):
     return arrays, rays
 
 
-def measure_l2_peak(torch):
-    """Read bandwidth of an L2-resident buffer (32 MB, read 64 times per launch with a reduction)."""
-    x = torch.ones(8 * 1024 * 1024, dtype=torch.float32, device="cuda")
-    for _ in range(3):
-        x.sum()
-    torch.cuda.synchronize()
-    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    best = 0.0
-    for _ in range(5):
-        s.record()
-        for _ in range(64):
-            x.sum()
-        e.record()
-        e.synchronize()
-        best = max(best, 64 * x.numel() * 4 / (s.elapsed_time(e) * 1e-3) / 1e9)
-    return best
+def measure_l2_peak(device: int) -> float:
+    """Read bandwidth of a 32 MB L2-resident buffer streamed 64 times by every SM (lgb_measure_l2_read_gbs)."""
+    import ctypes as C
+    from lumen_gb300 import abi
+    out = C.c_double(0.0)
+    st = abi.load().lgb_measure_l2_read_gbs(device, 32 << 20, 64, C.byref(out))
+    return out.value if st == abi.LGB_OK else float("nan")
 
 
 def cpu_oracle_rate(arrays, rays, seconds=12.0, threads=None):
@@ -264,7 +255,7 @@ def run_gpu(args):
         with open(peaks_path) as f:
             hbm_peak = float(json.load(f).get("hbm_gbs", hbm_peak))
         peak_src = "measured"
-    l2_peak = measure_l2_peak(torch)
+    l2_peak = measure_l2_peak(local)
     achieved = bytes_per_ray * n / (step_ms * 1e-3) / 1e9
     traffic = None
     prof = os.path.join(ROOT, "profiles", "trace_closest_incoherent_1M.json")

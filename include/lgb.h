@@ -211,6 +211,10 @@ LGB_API lgb_status lgb_render_path(lgb_scene* scene, const lgb_camera* camera, c
 /* Waits for `stream` and reports any fault a kernel recorded in the scene's device status word. */
 LGB_API lgb_status lgb_sync(lgb_scene* scene, void* stream);
 
+/* Measurement helper with no counterpart in Lumen: best-of-5 read bandwidth (GB/s) of an L2-resident
+ * buffer of `bytes` read `reps` times by all SMs, used as the roofline denominator of L2-bound traversal. */
+LGB_API lgb_status lgb_measure_l2_read_gbs(int device, uint64_t bytes, uint32_t reps, double* out_gbs);
+
 #ifdef __cplusplus
 }
 #endif

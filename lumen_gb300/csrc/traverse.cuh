@@ -109,28 +109,53 @@ __device__ __forceinline__ float fmin3(float a, float b, float c) {
     return d;
 }
 
+// Packed FP32 pairs (Blackwell f32x2 datapath): one instruction handles two children.
+__device__ __forceinline__ unsigned long long pk(float lo, float hi) {
+    return ((unsigned long long)__float_as_uint(hi) << 32) | __float_as_uint(lo);
+}
+__device__ __forceinline__ float lo_f(unsigned long long v) { return __uint_as_float((uint32_t)v); }
+__device__ __forceinline__ float hi_f(unsigned long long v) { return __uint_as_float((uint32_t)(v >> 32)); }
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ unsigned long long add2(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+// Bytes K and K+1 of w as an exact float pair (see byte_f).
+template <int K> __device__ __forceinline__ unsigned long long byte_pair(uint32_t w) {
+    const uint32_t a = __byte_perm(w, 0x4B000000u, 0x7440u | K);
+    const uint32_t b = __byte_perm(w, 0x4B000000u, 0x7440u | (K + 1));
+    return ((unsigned long long)b << 32) | a;
+}
+
+// Children K, K+1 (K even) of one 4-child half: their slab entry/exit distances and hit bits.
 template <int I>
-__device__ __forceinline__ void child_test(const RayQ& r, float tlim, uint32_t nx, uint32_t ny, uint32_t nz, uint32_t fx,
-                                           uint32_t fy, uint32_t fz, float sx, float sy, float sz, float ax, float ay,
-                                           float az, uint32_t imask, uint32_t meta, uint32_t& ih, uint32_t& th) {
+__device__ __forceinline__ uint32_t child_pair(const RayQ& r, float tlim, uint32_t nx, uint32_t ny, uint32_t nz,
+                                               uint32_t fx, uint32_t fy, uint32_t fz, unsigned long long sx,
+                                               unsigned long long sy, unsigned long long sz, unsigned long long ax,
+                                               unsigned long long ay, unsigned long long az) {
     constexpr int K = I & 3;
-    const float tnx = fmaf(byte_f<K>(nx), sx, ax);
-    const float tny = fmaf(byte_f<K>(ny), sy, ay);
-    const float tnz = fmaf(byte_f<K>(nz), sz, az);
-    const float tfx = fmaf(byte_f<K>(fx), sx, ax);
-    const float tfy = fmaf(byte_f<K>(fy), sy, ay);
-    const float tfz = fmaf(byte_f<K>(fz), sz, az);
-    const float tn = fmaxf(fmax3(tnx, tny, tnz), r.tmin);
-    const float tf = fminf(fmin3(tfx, tfy, tfz), tlim);
-    const uint32_t hit = tn <= tf ? 0xffffffffu : 0u;
-    const uint32_t m = (meta >> (8 * K)) & 0xffu;
-    ih |= (((imask >> I) & 1u) & hit) << ((uint32_t)I ^ r.oct);
-    th |= ((((m >> 5) & 7u) << (m & 31u)) & hit);
+    const unsigned long long bias = pk(-8388608.0f, -8388608.0f);
+    const unsigned long long tnx = fma2(add2(byte_pair<K>(nx), bias), sx, ax);
+    const unsigned long long tny = fma2(add2(byte_pair<K>(ny), bias), sy, ay);
+    const unsigned long long tnz = fma2(add2(byte_pair<K>(nz), bias), sz, az);
+    const unsigned long long tfx = fma2(add2(byte_pair<K>(fx), bias), sx, ax);
+    const unsigned long long tfy = fma2(add2(byte_pair<K>(fy), bias), sy, ay);
+    const unsigned long long tfz = fma2(add2(byte_pair<K>(fz), bias), sz, az);
+    const float tn0 = fmaxf(fmax3(lo_f(tnx), lo_f(tny), lo_f(tnz)), r.tmin);
+    const float tf0 = fminf(fmin3(lo_f(tfx), lo_f(tfy), lo_f(tfz)), tlim);
+    const float tn1 = fmaxf(fmax3(hi_f(tnx), hi_f(tny), hi_f(tnz)), r.tmin);
+    const float tf1 = fminf(fmin3(hi_f(tfx), hi_f(tfy), hi_f(tfz)), tlim);
+    return (tn0 <= tf0 ? (1u << I) : 0u) | (tn1 <= tf1 ? (2u << I) : 0u);
 }
 
 // Tests the 8 children of a node. Internal-child hits go to bit (slot ^ oct) of int_hits (bits 0-7), leaf
 // hits to tri_hits relative to tri_base (bits 0-23). Empty slots carry inverted boxes and meta 0, so they
-// contribute nothing and need no branch.
+// never contribute.
 __device__ __forceinline__ void intersect_node(const RayQ& r, const WideNode* __restrict__ node, float tlim,
                                                uint32_t& child_base, uint32_t& imask, uint32_t& int_hits,
                                                uint32_t& tri_base, uint32_t& tri_hits) {
@@ -143,27 +168,38 @@ __device__ __forceinline__ void intersect_node(const RayQ& r, const WideNode* __
     imask = e >> 24;
     child_base = c1.x;
     tri_base = c1.y;
-    const float sx = __uint_as_float((e & 0xffu) << 23) * r.ix;
-    const float sy = __uint_as_float(((e >> 8) & 0xffu) << 23) * r.iy;
-    const float sz = __uint_as_float(((e >> 16) & 0xffu) << 23) * r.iz;
-    const float ax = (__uint_as_float(c0.x) - r.ox) * r.ix;
-    const float ay = (__uint_as_float(c0.y) - r.oy) * r.iy;
-    const float az = (__uint_as_float(c0.z) - r.oz) * r.iz;
-    // near and far byte planes per axis: qlo is near for a non-negative direction component
+    const float fsx = __uint_as_float((e & 0xffu) << 23) * r.ix;
+    const float fsy = __uint_as_float(((e >> 8) & 0xffu) << 23) * r.iy;
+    const float fsz = __uint_as_float(((e >> 16) & 0xffu) << 23) * r.iz;
+    const float fax = (__uint_as_float(c0.x) - r.ox) * r.ix;
+    const float fay = (__uint_as_float(c0.y) - r.oy) * r.iy;
+    const float faz = (__uint_as_float(c0.z) - r.oz) * r.iz;
+    const unsigned long long sx = pk(fsx, fsx), sy = pk(fsy, fsy), sz = pk(fsz, fsz);
+    const unsigned long long ax = pk(fax, fax), ay = pk(fay, fay), az = pk(faz, faz);
+    // near and far byte planes per axis: qlo is near for a positive direction component
     const bool px = r.oct & 1u, py = r.oct & 2u, pz = r.oct & 4u;
     const uint32_t nx0 = px ? c2.x : c3.z, nx1 = px ? c2.y : c3.w, fx0 = px ? c3.z : c2.x, fx1 = px ? c3.w : c2.y;
     const uint32_t ny0 = py ? c2.z : c4.x, ny1 = py ? c2.w : c4.y, fy0 = py ? c4.x : c2.z, fy1 = py ? c4.y : c2.w;
     const uint32_t nz0 = pz ? c3.x : c4.z, nz1 = pz ? c3.y : c4.w, fz0 = pz ? c4.z : c3.x, fz1 = pz ? c4.w : c3.y;
-    uint32_t ih = 0, th = 0;
-    child_test<0>(r, tlim, nx0, ny0, nz0, fx0, fy0, fz0, sx, sy, sz, ax, ay, az, imask, c1.z, ih, th);
-    child_test<1>(r, tlim, nx0, ny0, nz0, fx0, fy0, fz0, sx, sy, sz, ax, ay, az, imask, c1.z, ih, th);
-    child_test<2>(r, tlim, nx0, ny0, nz0, fx0, fy0, fz0, sx, sy, sz, ax, ay, az, imask, c1.z, ih, th);
-    child_test<3>(r, tlim, nx0, ny0, nz0, fx0, fy0, fz0, sx, sy, sz, ax, ay, az, imask, c1.z, ih, th);
-    child_test<4>(r, tlim, nx1, ny1, nz1, fx1, fy1, fz1, sx, sy, sz, ax, ay, az, imask, c1.w, ih, th);
-    child_test<5>(r, tlim, nx1, ny1, nz1, fx1, fy1, fz1, sx, sy, sz, ax, ay, az, imask, c1.w, ih, th);
-    child_test<6>(r, tlim, nx1, ny1, nz1, fx1, fy1, fz1, sx, sy, sz, ax, ay, az, imask, c1.w, ih, th);
-    child_test<7>(r, tlim, nx1, ny1, nz1, fx1, fy1, fz1, sx, sy, sz, ax, ay, az, imask, c1.w, ih, th);
-    int_hits = ih;
+    const uint32_t hits = child_pair<0>(r, tlim, nx0, ny0, nz0, fx0, fy0, fz0, sx, sy, sz, ax, ay, az) |
+                          child_pair<2>(r, tlim, nx0, ny0, nz0, fx0, fy0, fz0, sx, sy, sz, ax, ay, az) |
+                          child_pair<4>(r, tlim, nx1, ny1, nz1, fx1, fy1, fz1, sx, sy, sz, ax, ay, az) |
+                          child_pair<6>(r, tlim, nx1, ny1, nz1, fx1, fy1, fz1, sx, sy, sz, ax, ay, az);
+    // internal hits, bit i moved to bit i ^ oct (front-to-back rank)
+    uint32_t x = hits & imask;
+    if (r.oct & 1u) x = ((x & 0x55u) << 1) | ((x >> 1) & 0x55u);
+    if (r.oct & 2u) x = ((x & 0x33u) << 2) | ((x >> 2) & 0x33u);
+    if (r.oct & 4u) x = ((x & 0x0Fu) << 4) | ((x >> 4) & 0x0Fu);
+    int_hits = x;
+    // leaf hits: unary triangle counts at their offsets
+    uint32_t lh = hits & ~imask, th = 0;
+    const unsigned long long meta = ((unsigned long long)c1.w << 32) | c1.z;
+    while (lh) {
+        const int i = __ffs(lh) - 1;
+        lh &= lh - 1u;
+        const uint32_t m = (uint32_t)(meta >> (8 * i)) & 0xffu;
+        th |= ((m >> 5) & 7u) << (m & 31u);
+    }
     tri_hits = th;
 }
 

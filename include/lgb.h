@@ -208,6 +208,17 @@ LGB_API lgb_status lgb_camera_lookat(const float pos[3], const float dir[3], flo
 LGB_API lgb_status lgb_render_path(lgb_scene* scene, const lgb_camera* camera, const lgb_path_params* params,
                                    uint32_t frame0, uint32_t spp, float* d_film, void* stream);
 
+/* The Path integrator without any device allocation. No counterpart in Lumen: it exists for callers that
+ * cannot let a library call cudaMalloc while they render (a host that budgets all device memory up front,
+ * or one that cannot afford the device-wide synchronisation of cudaFree in its frame loop). Same arguments
+ * and results as lgb_render_path; its work arena is a fixed 6 MiB device array that every GPU loading the
+ * library holds until exit, so images are limited to 16384 pixels (e.g. 128 x 128) and larger ones are
+ * rejected with LGB_ERR_INVALID_ARGUMENT. All calls share that array: calls that overlap on the GPU race,
+ * so order them on one stream. The first call on a device looks the array up; make it before any stream
+ * capture. */
+LGB_API lgb_status lgb_render_path_noalloc(lgb_scene* scene, const lgb_camera* camera, const lgb_path_params* params,
+                                           uint32_t frame0, uint32_t spp, float* d_film, void* stream);
+
 /* Waits for `stream` and reports any fault a kernel recorded in the scene's device status word. */
 LGB_API lgb_status lgb_sync(lgb_scene* scene, void* stream);
 

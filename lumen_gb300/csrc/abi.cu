@@ -88,9 +88,6 @@ void invert4(const double m[16], double out[16]) {
 
 using namespace lgb;
 
-struct lgb_ctx : public lgb::Ctx {};
-struct lgb_scene : public lgb::Scene {};
-
 extern "C" {
 
 LGB_API uint32_t lgb_abi_version(void) { return 1u; }

@@ -129,3 +129,7 @@ lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* p
                        float* film, cudaStream_t st);
 
 }  // namespace lgb
+
+// The opaque handles of include/lgb.h.
+struct lgb_ctx : public lgb::Ctx {};
+struct lgb_scene : public lgb::Scene {};

@@ -16,6 +16,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
+#include <string>
 
 #include "bsdf.cuh"
 #include "lgb_internal.cuh"
@@ -624,3 +626,131 @@ lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* p
 }
 
 }  // namespace lgb
+
+// ---------------------------------------------------------------------------------------------------------
+// lgb_render_path_noalloc: the same path integrator with its work arena in a fixed device array.
+//
+// Who needs it: callers that cannot call cudaMalloc while they render. A real-time host that budgets all
+// device memory up front (its own pool, a fixed VRAM budget) cannot let a library allocate in the middle of
+// a frame, where an allocation can fail or stall; cudaFree also synchronises the whole device, which would
+// stall the caller's other streams. lgb_render_path grows its arena with cudaMalloc on first use; this entry
+// point never allocates and instead uses the static array below.
+//
+// Limit: at most kNoAllocPaths paths in flight, so images of at most 16384 pixels (for example 128 x 128);
+// more samples per pixel are rendered in successive chunks of whole frames.
+// Every GPU that loads the library holds the array (6 MiB) until the process exits. All calls share it, so
+// calls that overlap on the GPU (another stream, another thread) race on it; order them on one stream.
+// The first call on a device takes the array's address there (cudaGetSymbolAddress); make that first call
+// before any stream capture.
+// ---------------------------------------------------------------------------------------------------------
+namespace lgb {
+namespace {
+
+constexpr uint32_t kNoAllocPaths = 16384;
+constexpr size_t kNoAllocBytes = (size_t)6 << 20;
+static __device__ __align__(256) unsigned char g_noalloc_arena[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kMaxDevices] = {};
+
+// Host address of g_noalloc_arena on `device` (current), looked up once per device.
+lgb_status noalloc_arena(Ctx* ctx, int device, char** out) {
+    if (device < 0 || device >= kMaxDevices)
+        return set_error(ctx, LGB_ERR_UNSUPPORTED, "device index too large for the no-alloc arena table");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_arena);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "cudaGetSymbolAddress(g_noalloc_arena)");
+        g_noalloc_ptr[device] = p;
+    }
+    *out = (char*)g_noalloc_ptr[device];
+    return LGB_OK;
+}
+
+lgb_status render_path_noalloc(Scene* s, const lgb_camera* cam, const lgb_path_params* pp, uint32_t frame0,
+                               uint32_t spp, float* film, cudaStream_t st) {
+    Ctx* ctx = s->ctx;
+    const uint64_t npix64 = (uint64_t)cam->width * cam->height;
+    if (npix64 > kNoAllocPaths)
+        return set_error(ctx, LGB_ERR_INVALID_ARGUMENT,
+                         "lgb_render_path_noalloc renders at most 16384 pixels per image (its fixed arena holds "
+                         "16384 paths); use lgb_render_path for larger images");
+    const uint32_t npix = (uint32_t)npix64;
+    const uint32_t frames_per_chunk = std::max(1u, std::min(spp, kNoAllocPaths / npix));
+    const uint32_t cap = npix * frames_per_chunk;
+    Buffers B;
+    if (carve(nullptr, cap, B) > kNoAllocBytes)
+        return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "no-alloc arena too small for this launch");
+    char* arena = nullptr;
+    lgb_status ast = noalloc_arena(ctx, ctx->device, &arena);
+    if (ast != LGB_OK) return ast;
+    carve(arena, cap, B);
+    SceneView S;
+    S.nodes = s->bvh.nodes; S.tris = s->bvh.tris; S.verts = s->d_vertices; S.idx = s->d_indices;
+    S.tri_mesh = s->d_tri_mesh; S.meshes = s->d_meshes; S.mesh_first = s->d_mesh_first_tri; S.mats = s->d_materials;
+    S.lights = s->d_lights; S.texs = s->d_textures; S.status = s->d_status;
+    Params P;
+    for (int i = 0; i < 16; i++) { P.iv[i] = cam->inv_view[i]; P.ip[i] = cam->inv_projection[i]; }
+    P.width = cam->width; P.height = cam->height; P.npix = npix;
+    for (int i = 0; i < 3; i++) P.sky[i] = pp->sky_col[i];
+    P.max_depth = pp->max_depth; P.num_lights = pp->num_lights; P.light_tri_count = pp->light_triangle_count;
+    P.direct_lighting = pp->direct_lighting; P.film_mode = pp->film_mode;
+    P.cap = cap;
+    const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    int trace_blocks = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&trace_blocks, k_q_trace_closest, kThreads, 0);
+    const int grid_work = sms * 8, grid_trace = sms * std::max(trace_blocks, 1);
+    const int bounces = std::max(pp->max_depth, 1);
+    for (uint32_t done = 0; done < spp; done += frames_per_chunk) {
+        P.frame0 = frame0 + done;
+        P.nframes = std::min(frames_per_chunk, spp - done);
+        const uint32_t npaths = npix * P.nframes;
+        // The arena keeps the previous call's contents: the counters are reset here, the occlusion bits
+        // before every shadow query, and every other array is written before it is read.
+        k_init_counters<<<1, 32, 0, st>>>(B.counters, npaths);
+        k_camera<<<grid_work, kThreads, 0, st>>>(P, B);
+        for (int depth = 0; depth < bounces; depth++) {
+            k_q_trace_closest<<<grid_trace, kThreads, 0, st>>>(S, B.rays, B.hits, B.counters + 0, B.counters + 8);
+            k_classify<<<grid_work, kThreads, 0, st>>>(S, P, B);
+            k_shade<CLS_DIFFUSE><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
+            k_shade<CLS_CONDUCTOR><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
+            k_shade<CLS_SPECULAR><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
+            k_shade<CLS_PRINCIPLED><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
+            LGB_CUDA_TRY(ctx, cudaMemsetAsync(B.sbits, 0, sizeof(uint32_t) * ((cap + 31) / 32), st));
+            k_q_trace_any<<<grid_trace, kThreads, 0, st>>>(S, B.srays, B.sbits, B.counters + 2, B.counters + 9);
+            k_q_trace_closest<<<grid_trace, kThreads, 0, st>>>(S, B.mrays, B.mhits, B.counters + 2, B.counters + 10);
+            k_nee_resolve<<<grid_work, kThreads, 0, st>>>(S, B);
+            k_rotate<<<1, 32, 0, st>>>(B.counters);
+            std::swap(B.rays, B.rays_next);
+            std::swap(B.q_cur, B.q_next);
+        }
+        k_film<<<grid_work, kThreads, 0, st>>>(P, B, reinterpret_cast<float4*>(film));
+        LGB_CUDA_TRY(ctx, cudaGetLastError());
+    }
+    return LGB_OK;
+}
+
+}  // namespace
+}  // namespace lgb
+
+extern "C" LGB_API lgb_status lgb_render_path_noalloc(lgb_scene* s, const lgb_camera* cam, const lgb_path_params* p,
+                                                      uint32_t frame0, uint32_t spp, float* d_film, void* stream) {
+    using namespace lgb;
+    if (!s) return LGB_ERR_INVALID_ARGUMENT;
+    if (!cam || !p || !d_film || cam->width == 0 || cam->height == 0)
+        return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "null camera, params or film");
+    if (reinterpret_cast<uintptr_t>(d_film) & 15u)
+        return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "film must be 16-byte aligned");
+    if (!s->bvh.nodes) return set_error(s->ctx, LGB_ERR_NOT_READY, "lgb_bvh_build has not been called");
+    if (p->num_lights < 0 || (uint32_t)p->num_lights > s->num_lights)
+        return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "num_lights exceeds the scene's light count");
+    if (p->num_lights > 0 && p->light_triangle_count <= 0)
+        return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "light_triangle_count must be positive");
+    if (p->dir_light_idx != 0xFFFFFFFFu)
+        return set_error(s->ctx, LGB_ERR_UNSUPPORTED, "atmosphere shading for directional lights is not supported");
+    if (spp == 0) return LGB_OK;
+    if (cudaSetDevice(s->ctx->device) != cudaSuccess) return set_error(s->ctx, LGB_ERR_CUDA, "cudaSetDevice failed");
+    return render_path_noalloc(s, cam, p, frame0, spp, d_film, (cudaStream_t)stream);
+}

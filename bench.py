@@ -142,6 +142,50 @@ def cpu_oracle_rate(arrays, rays, seconds=12.0, threads=None):
     return n / dt, n, threads
 
 
+def cornell_secondary(torch, ctx_cls, scene_cls, local, cpu_leg: bool):
+    """The Cornell-box path tracer (256^2, 16 spp, depth 8): GPU Msamples/s through lgb_render_path, L2 not
+    flushed (the scene is 36 triangles), and the CPU oracle on a bounded sample of the same frames."""
+    from lumen_gb300 import procedural
+    from lumen_gb300.scene import camera_lookat, path_params
+    cb = procedural.cornell_box()
+    ctx = ctx_cls(local)
+    sc = scene_cls(ctx, cb)
+    sc.build()
+    w = h = 256
+    spp = 16
+    cam = camera_lookat(cb.camera_pos, cb.camera_dir, cb.fov, w, h)
+    params = path_params(cb, 8)
+    film = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        sc.render_path(cam, params, 0, spp, film, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        sc.render_path(cam, params, 0, spp, film, stream=stream.cuda_stream)
+        e.record(stream)
+        e.synchronize()
+        times.append(s.elapsed_time(e))
+    sc.sync(stream.cuda_stream)
+    ms = float(np.median(times))
+    out = {"workload": "Cornell box 36 triangles, 256x256, 16 spp, max depth 8, FP32", "ms": ms,
+           "msamples_per_s": w * h * spp / (ms * 1e-3) / 1e6, "mean_radiance": float(film[:, :3].mean())}
+    if cpu_leg:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_lib
+        ora = oracle_lib.Oracle()
+        osc = ora.scene(cb)
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        osc.film(cam, 8, w, h, 0, 2, threads=threads)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": w * h * 2 / dt / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
+                               "sample": "frames 0-1 of the same render"}
+    return out
+
+
 def run_reference(args):
     rank, world, _ = _dist()
     if rank != 0:
@@ -268,6 +312,9 @@ def run_gpu(args):
         rate, sample, threads = cpu_oracle_rate(arrays, rays)
         cpu = {"value": rate / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
                "sample": f"first {sample} of the 4M incoherent rays on the oracle binary SAH BVH (build untimed)"}
+    secondary = {}
+    if not args.no_secondary:
+        secondary["path_tracer"] = cornell_secondary(torch, Context, GpuScene, local, world == 1 and not args.no_cpu_baseline)
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
@@ -288,6 +335,7 @@ def run_gpu(args):
         "cpu_baseline": cpu,
         "clocks": clk,
         "gpu_launches": args.steps,
+        "secondary": secondary,
     }
     print(json.dumps(line))
     if world > 1:
@@ -301,6 +349,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the Cornell-box path-tracer measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -222,6 +222,13 @@ LGB_API lgb_status lgb_render_path_noalloc(lgb_scene* scene, const lgb_camera* c
 /* Waits for `stream` and reports any fault a kernel recorded in the scene's device status word. */
 LGB_API lgb_status lgb_sync(lgb_scene* scene, void* stream);
 
+/* Film error (src/shaders/rmse/*.comp, RayTracer.cpp:215-241): RMSE of d_film against d_reference, both RGBA32F
+ * with npix pixels; alpha is ignored. mode 0 = sqrt(sum of squared RGB errors / (3 npix)); mode 1 = the value
+ * Lumen reports (per 1024-pixel group the minimum of its warps' sums, calc_rmse.comp:37, then
+ * sqrt(sum) / (3 npix), output_rmse.comp:23). Waits for `stream` and writes the result to *out_rmse. */
+LGB_API lgb_status lgb_film_rmse(lgb_ctx* ctx, const float* d_film, const float* d_reference, uint32_t npix,
+                                 uint32_t mode, double* out_rmse, void* stream);
+
 /* Measurement helper with no counterpart in Lumen: best-of-5 read bandwidth (GB/s) of an L2-resident
  * buffer of `bytes` read `reps` times by all SMs, used as the roofline denominator of L2-bound traversal. */
 LGB_API lgb_status lgb_measure_l2_read_gbs(int device, uint64_t bytes, uint32_t reps, double* out_gbs);

@@ -118,6 +118,8 @@ SIGNATURES = {
     "lgb_render_path_noalloc": ([C.c_void_p, C.POINTER(Camera), C.POINTER(PathParams), C.c_uint32, C.c_uint32,
                                  C.c_void_p, C.c_void_p], C.c_int32),
     "lgb_sync": ([C.c_void_p, C.c_void_p], C.c_int32),
+    "lgb_film_rmse": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_double), C.c_void_p],
+                      C.c_int32),
     "lgb_measure_l2_read_gbs": ([C.c_int, C.c_uint64, C.c_uint32, C.POINTER(C.c_double)], C.c_int32),
 }
 

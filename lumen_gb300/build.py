@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
-SOURCES = ["abi.cu", "bvh_build.cu", "traverse.cu", "path.cu", "diag.cu"]
+SOURCES = ["abi.cu", "bvh_build.cu", "traverse.cu", "path.cu", "diag.cu", "film.cu"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
@@ -38,4 +38,25 @@ def build_library(verbose: bool = False) -> str:
                 print(r.stderr)
     lib = os.path.join(OUT, "liblgb.so")
     _run([NVCC, *ARCH, "-shared", "--cudart", "static", "-o", lib, *objs])
+    build_host(lib)
     return lib
+
+
+HOST_SOURCES = ["lumen_scene.cpp", "integrator.cpp", "host_capi.cpp"]
+
+
+def build_host(lib: str) -> str:
+    """liblgb_host.so (scene loading + Integrator mirror, plain C++ over the C ABI) and the lgb_render CLI."""
+    hdir = os.path.join(HERE, "host")
+    inc = ["-I" + os.path.join(ROOT, "include"), "-I" + hdir]
+    objs = [os.path.join(OUT, "host_" + s.replace(".cpp", ".o")) for s in HOST_SOURCES]
+    jobs = [[NVCC, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden", *inc, "-c",
+             os.path.join(hdir, s), "-o", o] for s, o in zip(HOST_SOURCES, objs)]
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        list(ex.map(_run, jobs))
+    host = os.path.join(OUT, "liblgb_host.so")
+    rpath = ["-Xlinker", "-rpath", "-Xlinker", "$ORIGIN"]
+    _run([NVCC, "-shared", "--cudart", "static", "-o", host, *objs, "-L" + OUT, "-llgb", *rpath])
+    _run([NVCC, "-O2", "-std=c++17", *inc, os.path.join(hdir, "lgb_render.cpp"), "-o", os.path.join(OUT, "lgb_render"),
+          "-L" + OUT, "-llgb_host", "-llgb", *rpath])
+    return host

@@ -1,0 +1,62 @@
+#include "integrator.h"
+
+#include <cuda_runtime.h>
+
+#include <stdexcept>
+#include <string>
+
+namespace lgbh {
+
+void Integrator::check(lgb_status st, const char* what) {
+    if (st != LGB_OK) throw std::runtime_error(std::string(what) + ": " + lgb_last_error(ctx));
+}
+
+void Integrator::init() {
+    const lgb_scene_desc d = lumen_scene->desc();
+    check(lgb_scene_create(ctx, &d, &scene), "lgb_scene_create");
+    const size_t bytes = sizeof(float) * 4 * (size_t)width * height;
+    if (cudaMalloc((void**)&output_film, bytes) != cudaSuccess) throw std::runtime_error("film allocation failed");
+    cudaMemset(output_film, 0, bytes);
+    update();
+}
+
+bool Integrator::update() {
+    const CameraSettings& c = lumen_scene->config.cam;
+    check(lgb_camera_lookat(c.pos, c.dir, c.fov, width, height, &cam), "lgb_camera_lookat");
+    return updated;
+}
+
+void Integrator::destroy() {
+    if (output_film) cudaFree(output_film);
+    output_film = nullptr;
+    if (scene) lgb_scene_destroy(scene);
+    scene = nullptr;
+}
+
+void Integrator::create_accel(const lgb_build_opts* opts) { check(lgb_bvh_build(scene, opts, &accel_stats), "lgb_bvh_build"); }
+
+void GpuPath::init() {
+    Integrator::init();
+    frame_num = 0;
+    path_length = (uint32_t)lumen_scene->config.path_length;  // Path::init (Path.cpp:24)
+}
+
+void GpuPath::render() {  // Path::render (Path.cpp:27-59)
+    lgb_path_params p{};
+    for (int i = 0; i < 3; i++) p.sky_col[i] = lumen_scene->config.sky_col[i];
+    p.max_depth = (int32_t)path_length;
+    p.num_lights = (int32_t)lumen_scene->lights.size();
+    p.light_triangle_count = (int32_t)lumen_scene->total_light_triangle_cnt;
+    p.dir_light_idx = lumen_scene->dir_light_idx;
+    p.direct_lighting = direct_lighting ? 1u : 0u;
+    check(lgb_render_path(scene, &cam, &p, frame_num, 1, output_film, stream), "lgb_render_path");
+}
+
+bool GpuPath::update() {  // Path::update (Path.cpp:61-68)
+    frame_num++;
+    const bool changed = Integrator::update();
+    if (changed) frame_num = 0;
+    return changed;
+}
+
+}  // namespace lgbh

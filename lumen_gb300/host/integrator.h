@@ -1,0 +1,55 @@
+// Host-side mirror of Lumen's integrator interface (src/RayTracer/Integrator.h:14-33, Path.h:4-20) over the
+// C ABI, headless: the output is an RGBA32F device film instead of a Vulkan texture.
+#pragma once
+#include <cstdint>
+#include <memory>
+#include <string>
+
+#include "lgb.h"
+#include "lumen_scene.h"
+
+namespace lgbh {
+
+class Integrator {
+  public:
+    Integrator(LumenScene* scene, lgb_ctx* ctx, uint32_t width, uint32_t height)
+        : lumen_scene(scene), ctx(ctx), width(width), height(height) {}
+    virtual ~Integrator() { destroy(); }
+    // Integrator::init (Integrator.cpp:8-50): uploads the scene, allocates the output film, sets the camera.
+    virtual void init();
+    virtual void render() = 0;
+    // Integrator::update (Integrator.cpp:74-125) without input handling: refreshes the camera matrices.
+    virtual bool update();
+    virtual void destroy();
+    // Integrator::create_accel (Integrator.cpp:137-160): one 8-wide BVH over every mesh.
+    virtual void create_accel(const lgb_build_opts* opts = nullptr);
+
+    float* output_film = nullptr;  // device RGBA32F, width * height
+    bool updated = false;
+    uint32_t frame_num = 0;
+    lgb_build_stats accel_stats{};
+    lgb_scene* gpu_scene() const { return scene; }
+    const lgb_camera& camera() const { return cam; }
+
+  protected:
+    void check(lgb_status st, const char* what);
+    LumenScene* lumen_scene = nullptr;
+    lgb_ctx* ctx = nullptr;
+    lgb_scene* scene = nullptr;
+    lgb_camera cam{};
+    uint32_t width = 0, height = 0;
+};
+
+// The Path integrator (Path.cpp): one sample per pixel per render(), progressive mean in the film.
+class GpuPath final : public Integrator {
+  public:
+    using Integrator::Integrator;
+    void init() override;
+    void render() override;
+    bool update() override;
+    uint32_t path_length = 6;
+    bool direct_lighting = true;
+    void* stream = nullptr;
+};
+
+}  // namespace lgbh

@@ -1,0 +1,396 @@
+// Lumen JSON + OBJ scene loading onto the arrays of include/lgb.h. See lumen_scene.h.
+#include "lumen_scene.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <stdexcept>
+
+#include "json.h"
+
+namespace lgbh {
+namespace {
+
+std::string read_file(const std::string& path) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) throw std::runtime_error("cannot open " + path);
+    std::stringstream ss;
+    ss << f.rdbuf();
+    return ss.str();
+}
+
+std::string dir_of(const std::string& path) {
+    const size_t p = path.find_last_of("/\\");
+    return p == std::string::npos ? std::string() : path.substr(0, p + 1);
+}
+
+lgb_material default_material() {
+    lgb_material m;
+    std::memset(&m, 0, sizeof(m));
+    m.texture_id = -1;
+    return m;
+}
+
+void vec3_of(const Json& j, float* out, const float* def) {
+    for (int i = 0; i < 3; i++) out[i] = j.is_null() ? def[i] : (float)j[i].as_number();
+}
+
+// One OBJ face corner: position / texcoord / normal indices (0-based, -1 = absent).
+struct Corner {
+    long v = -1, t = -1, n = -1;
+};
+
+long obj_index(const std::string& tok, size_t count) {
+    if (tok.empty()) return -1;
+    long i = std::strtol(tok.c_str(), nullptr, 10);
+    if (i > 0) return i - 1;
+    if (i < 0) return (long)count + i;
+    return -1;
+}
+
+}  // namespace
+
+// OBJ subset of the files Lumen's scenes reference: v / vt / vn / f (polygons split into fans), with shapes
+// started by 'o' or 'g'. Every face corner becomes its own vertex, as LumenScene.cpp:302-324 lays them out.
+// Files without normals get the triangle's geometric normal (Lumen would read past its normal array) and
+// files without texture coordinates get (0, 0).
+void LumenScene::load_obj(const std::string& path) {
+    std::istringstream in(read_file(path));
+    std::vector<float> v, vt, vn;
+    struct Shape {
+        std::string name;
+        std::vector<Corner> corners;  // 3 per triangle
+    };
+    std::vector<Shape> shapes(1);
+    std::string line;
+    while (std::getline(in, line)) {
+        if (!line.empty() && line.back() == '\r') line.pop_back();
+        std::istringstream ls(line);
+        std::string tag;
+        if (!(ls >> tag)) continue;
+        if (tag == "v") {
+            float x = 0, y = 0, z = 0;
+            ls >> x >> y >> z;
+            v.push_back(x); v.push_back(y); v.push_back(z);
+        } else if (tag == "vt") {
+            float s = 0, t = 0;
+            ls >> s >> t;
+            vt.push_back(s); vt.push_back(t);
+        } else if (tag == "vn") {
+            float x = 0, y = 0, z = 0;
+            ls >> x >> y >> z;
+            vn.push_back(x); vn.push_back(y); vn.push_back(z);
+        } else if (tag == "o" || tag == "g") {
+            std::string name;
+            std::getline(ls, name);
+            name.erase(0, name.find_first_not_of(" \t"));
+            if (!shapes.back().corners.empty() || !shapes.back().name.empty()) shapes.emplace_back();
+            shapes.back().name = name;
+        } else if (tag == "f") {
+            std::vector<Corner> poly;
+            std::string tok;
+            while (ls >> tok) {
+                Corner c;
+                size_t a = tok.find('/');
+                if (a == std::string::npos) {
+                    c.v = obj_index(tok, v.size() / 3);
+                } else {
+                    c.v = obj_index(tok.substr(0, a), v.size() / 3);
+                    size_t b = tok.find('/', a + 1);
+                    if (b == std::string::npos) {
+                        c.t = obj_index(tok.substr(a + 1), vt.size() / 2);
+                    } else {
+                        c.t = obj_index(tok.substr(a + 1, b - a - 1), vt.size() / 2);
+                        c.n = obj_index(tok.substr(b + 1), vn.size() / 3);
+                    }
+                }
+                if (c.v < 0 || (size_t)c.v >= v.size() / 3) throw std::runtime_error("OBJ face index out of range in " + path);
+                poly.push_back(c);
+            }
+            for (size_t k = 2; k < poly.size(); k++) {
+                shapes.back().corners.push_back(poly[0]);
+                shapes.back().corners.push_back(poly[k - 1]);
+                shapes.back().corners.push_back(poly[k]);
+            }
+        }
+    }
+    for (const Shape& sh : shapes) {
+        if (sh.corners.empty()) continue;
+        lgb_mesh m;
+        m.index_offset = (uint32_t)indices.size();
+        m.vertex_offset = (uint32_t)(positions.size() / 3);
+        m.material_index = 0;
+        m.tri_count = (uint32_t)(sh.corners.size() / 3);
+        for (size_t i = 0; i < sh.corners.size(); i += 3) {
+            float fn[3] = {0, 0, 1};
+            {
+                const float* p0 = &v[3 * sh.corners[i].v];
+                const float* p1 = &v[3 * sh.corners[i + 1].v];
+                const float* p2 = &v[3 * sh.corners[i + 2].v];
+                const float e0[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+                const float e1[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+                const float c[3] = {e0[1] * e1[2] - e1[1] * e0[2], e0[2] * e1[0] - e1[2] * e0[0], e0[0] * e1[1] - e1[0] * e0[1]};
+                const float l = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+                if (l > 0) { fn[0] = c[0] / l; fn[1] = c[1] / l; fn[2] = c[2] / l; }
+            }
+            for (int k = 0; k < 3; k++) {
+                const Corner& c = sh.corners[i + k];
+                for (int a = 0; a < 3; a++) positions.push_back(v[3 * c.v + a]);
+                for (int a = 0; a < 3; a++) normals.push_back(c.n >= 0 && (size_t)c.n < vn.size() / 3 ? vn[3 * c.n + a] : fn[a]);
+                for (int a = 0; a < 2; a++) uvs.push_back(c.t >= 0 && (size_t)c.t < vt.size() / 2 ? vt[2 * c.t + a] : 0.0f);
+                indices.push_back((uint32_t)(i + k));  // per-mesh local index (LumenScene.cpp:305)
+            }
+        }
+        meshes.push_back(m);
+        mesh_names.push_back(sh.name);
+    }
+}
+
+void LumenScene::load(const std::string& json_path) {
+    const Json j = parse_json(read_file(json_path));
+    const std::string root = dir_of(json_path);
+    // integrator block (LumenScene.cpp:237-247)
+    const Json& integ = j["integrator"];
+    if (!integ["type"].is_null()) {
+        config.integrator = integ["type"].as_string();
+        std::transform(config.integrator.begin(), config.integrator.end(), config.integrator.begin(), ::tolower);
+    }
+    if (!integ["path_length"].is_null()) config.path_length = (int)integ["path_length"].as_number();
+    if (!integ["sky_col"].is_null()) vec3_of(integ["sky_col"], config.sky_col, config.sky_col);
+    // geometry
+    if (j["mesh_file"].is_null()) throw std::runtime_error("scene has no mesh_file");
+    load_obj(root + j["mesh_file"].as_string());
+    // materials (LumenScene.cpp:347-486)
+    const Json& bsdfs = j["bsdfs"];
+    materials.assign(std::max<size_t>(bsdfs.size(), 1), default_material());
+    for (size_t bi = 0; bi < bsdfs.size(); bi++) {
+        const Json& b = bsdfs[bi];
+        lgb_material& m = materials[bi];
+        const float one[3] = {1, 1, 1}, zero[3] = {0, 0, 0};
+        if (!b["texture"].is_null()) {
+            const std::string tex = root + b["texture"].as_string();
+            if (tex.size() >= 4 && tex.compare(tex.size() - 4, 4, ".pfm") == 0) {
+                textures.push_back(read_pfm(tex));
+                m.texture_id = (int)textures.size() - 1;
+            } else {
+                std::fprintf(stderr, "lgbh: texture %s skipped (only PFM textures are read)\n", tex.c_str());
+            }
+        }
+        vec3_of(b["albedo"], m.albedo, one);
+        vec3_of(b["emissive_factor"], m.emissive_factor, zero);
+        const std::string type = b["type"].is_null() ? std::string() : b["type"].as_string();
+        if (type == "diffuse") {
+            m.bsdf_type = LGB_BSDF_DIFFUSE;
+            m.bsdf_props = LGB_FLAG_DIFFUSE | LGB_FLAG_REFLECTION;
+        } else if (type == "mirror") {
+            m.bsdf_type = LGB_BSDF_MIRROR;
+            m.bsdf_props = LGB_FLAG_SPECULAR | LGB_FLAG_REFLECTION;
+        } else if (type == "glass") {
+            m.bsdf_type = LGB_BSDF_GLASS;
+            m.bsdf_props = LGB_FLAG_SPECULAR | LGB_FLAG_TRANSMISSION;
+            m.ior = b["ior"].f(1.0f);
+        } else if (type == "dielectric") {
+            m.bsdf_type = LGB_BSDF_DIELECTRIC;
+            m.ior = b["ior"].f(1.0f);
+            m.roughness = b["roughness"].f(0.0f);
+            if (b["transmission"].is_null() || b["transmission"].as_number() != 0.0) m.bsdf_props |= LGB_FLAG_TRANSMISSION;
+            if (b["reflection"].is_null() || b["reflection"].as_number() != 0.0) m.bsdf_props |= LGB_FLAG_REFLECTION;
+            m.bsdf_props |= (m.ior != 1.0f && m.roughness > 0.08f) ? LGB_FLAG_GLOSSY : LGB_FLAG_SPECULAR;
+            m.thin = b["thin"].is_null() ? 0u : (uint32_t)b["thin"].as_number();
+        } else if (type == "conductor") {
+            m.bsdf_type = LGB_BSDF_CONDUCTOR;
+            m.roughness = b["roughness"].f(0.0f);
+            if (!b["reflectance"].is_null()) {
+                // reflectance_to_conductor_eta_k (LumenScene.cpp:47-50): eta = 1, k = 2 sqrt(r) / sqrt(max(1 - r, 0.001))
+                for (int a = 0; a < 3; a++) {
+                    const float r = std::min(std::max((float)b["reflectance"][a].as_number(), 0.0f), 0.9999f);
+                    m.albedo[a] = 1.0f;
+                    m.k[a] = 2.0f * std::sqrt(r) / std::sqrt(std::max(1.0f - r, 0.001f));
+                }
+            }
+            if (!b["edge_tint"].is_null()) {
+                // Gulbrandsen's artist-friendly mapping (JCGT 3(4) 2014), as LumenScene.cpp:425-435 applies it
+                for (int a = 0; a < 3; a++) {
+                    const float g = (float)b["edge_tint"][a].as_number();
+                    const float r = (float)b["reflectivity"][a].as_number();
+                    const float sr = std::sqrt(r);
+                    const float n = g * (1.0f - r) / (1.0f + r) + (1.0f - g) * (1.0f + sr) / (1.0f - sr);
+                    const float t1 = r * (n + 1.0f), t2 = n - 1.0f;
+                    m.albedo[a] = n;
+                    m.k[a] = std::sqrt(1.0f / (1.0f - r) * (t1 * t1 - t2 * t2));
+                }
+            }
+            m.bsdf_props = LGB_FLAG_REFLECTION | (m.roughness > 0.08f ? LGB_FLAG_GLOSSY : LGB_FLAG_SPECULAR);
+        } else if (type == "principled") {
+            m.bsdf_type = LGB_BSDF_PRINCIPLED;
+            m.ior = b["ior"].f(1.0f);
+            m.roughness = b["roughness"].f(0.5f);
+            m.diffuse_trans = b["diffuse_transmission"].f(0.0f);
+            m.spec_trans = b["specular_transmission"].f(0.0f);
+            m.metallic = b["metallic"].f(0.0f);
+            m.specular_tint = b["specular_tint"].f(0.0f);
+            m.sheen_tint = b["sheen_tint"].f(0.5f);
+            m.clearcoat = b["clearcoat"].f(0.0f);
+            m.clearcoat_gloss = b["clearcoat_gloss"].f(1.0f);
+            m.subsurface = b["subsurface"].f(0.0f);
+            m.flatness = b["flatness"].f(0.0f);
+            m.sheen = b["sheen"].f(0.0f);
+            m.anisotropy = b["anisotropy"].f(0.0f);
+            m.thin = b["thin"].is_null() ? 0u : (uint32_t)b["thin"].as_number();
+            if (m.roughness < 1.0f) m.bsdf_props |= LGB_FLAG_REFLECTION;
+            if (m.spec_trans > 0.0f) m.bsdf_props |= LGB_FLAG_TRANSMISSION;
+            m.bsdf_props |= m.roughness > 0.08f ? LGB_FLAG_GLOSSY : LGB_FLAG_SPECULAR;
+        } else {
+            throw std::runtime_error("unknown bsdf type '" + type + "'");
+        }
+        const Json& refs = b["refs"];
+        for (size_t r = 0; r < refs.size(); r++)
+            for (size_t s = 0; s < meshes.size(); s++)
+                if (refs[r].as_string() == mesh_names[s]) meshes[s].material_index = (uint32_t)bi;
+    }
+    // camera (LumenScene.cpp:487-491)
+    const Json& cam = j["camera"];
+    config.cam.fov = cam["fov"].f(45.0f);
+    const float zero3[3] = {0, 0, 0}, z3[3] = {0, 0, 1};
+    vec3_of(cam["position"], config.cam.pos, zero3);
+    vec3_of(cam["dir"], config.cam.dir, z3);
+    // scene bounds (LumenScene.cpp:732-751): from the meshes' vertex bounds; a degenerate box becomes [-1, 1]^3
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (size_t i = 0; i < positions.size(); i += 3)
+        for (int a = 0; a < 3; a++) { lo[a] = std::min(lo[a], positions[i + a]); hi[a] = std::max(hi[a], positions[i + a]); }
+    if (!(lo[0] < hi[0] && lo[1] < hi[1] && lo[2] < hi[2])) {
+        for (int a = 0; a < 3; a++) { lo[a] = -1.0f; hi[a] = 1.0f; }
+    }
+    float d2 = 0.0f;
+    for (int a = 0; a < 3; a++) { bbox_min[a] = lo[a]; bbox_max[a] = hi[a]; d2 += (hi[a] - lo[a]) * (hi[a] - lo[a]); }
+    radius = std::sqrt(d2) * 0.5f;
+    // lights (LumenScene.cpp:74-113): emissive meshes become area lights, then the JSON lights
+    total_light_triangle_cnt = 0;
+    for (size_t s = 0; s < meshes.size(); s++) {
+        const lgb_material& mat = materials[meshes[s].material_index];
+        const float* e = mat.emissive_factor;
+        if (e[0] > 0 || e[1] > 0 || e[2] > 0) {
+            lgb_light l;
+            std::memset(&l, 0, sizeof(l));
+            for (int i = 0; i < 4; i++) l.world_matrix[5 * i] = 1.0f;
+            l.num_triangles = meshes[s].tri_count;
+            l.prim_mesh_idx = (uint32_t)s;
+            l.light_flags = LGB_LIGHT_AREA | (1u << 4);
+            for (int a = 0; a < 3; a++) l.L[a] = e[a];
+            lights.push_back(l);
+            total_light_triangle_cnt += l.num_triangles;
+            for (uint32_t t = 0; t < meshes[s].tri_count; t++) {
+                const uint32_t base = meshes[s].index_offset + 3 * t;
+                const float* p0 = &positions[3 * (size_t)(indices[base] + meshes[s].vertex_offset)];
+                const float* p1 = &positions[3 * (size_t)(indices[base + 1] + meshes[s].vertex_offset)];
+                const float* p2 = &positions[3 * (size_t)(indices[base + 2] + meshes[s].vertex_offset)];
+                const float e1[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+                const float e2[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+                const float c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+                total_light_area += 0.5f * std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+            }
+        }
+    }
+    const Json& jl = j["lights"];
+    for (size_t i = 0; i < jl.size(); i++) {
+        const Json& L = jl[i];
+        lgb_light l;
+        std::memset(&l, 0, sizeof(l));
+        for (int k = 0; k < 4; k++) l.world_matrix[5 * k] = 1.0f;
+        vec3_of(L["pos"], l.pos, zero3);
+        vec3_of(L["dir"], l.to, zero3);
+        vec3_of(L["L"], l.L, zero3);
+        const std::string type = L["type"].is_null() ? std::string() : L["type"].as_string();
+        if (type == "spot") l.light_flags = LGB_LIGHT_SPOT | (1u << 4) | (1u << 5);
+        else if (type == "directional") l.light_flags = LGB_LIGHT_DIRECTIONAL | (1u << 5);
+        else throw std::runtime_error("unknown light type '" + type + "'");
+        l.world_radius = radius;
+        for (int a = 0; a < 3; a++) l.world_center[a] = 0.5f * (bbox_max[a] + bbox_min[a]);
+        if ((l.light_flags & 7u) == LGB_LIGHT_DIRECTIONAL) dir_light_idx = (uint32_t)i;
+        total_light_triangle_cnt++;
+        lights.push_back(l);
+    }
+}
+
+std::vector<lgb_texture> LumenScene::texture_views() const {
+    std::vector<lgb_texture> v;
+    for (const TextureData& t : textures) v.push_back({t.width, t.height, t.rgba.data()});
+    return v;
+}
+
+lgb_scene_desc LumenScene::desc() const {
+    tex_views_ = texture_views();
+    lgb_scene_desc d;
+    std::memset(&d, 0, sizeof(d));
+    d.positions = positions.data();
+    d.normals = normals.data();
+    d.uvs = uvs.data();
+    d.num_vertices = (uint32_t)(positions.size() / 3);
+    d.indices = indices.data();
+    d.num_indices = (uint32_t)indices.size();
+    d.meshes = meshes.data();
+    d.num_meshes = (uint32_t)meshes.size();
+    d.materials = materials.data();
+    d.num_materials = (uint32_t)materials.size();
+    d.lights = lights.empty() ? nullptr : lights.data();
+    d.num_lights = (uint32_t)lights.size();
+    d.textures = tex_views_.empty() ? nullptr : tex_views_.data();
+    d.num_textures = (uint32_t)tex_views_.size();
+    return d;
+}
+
+TextureData read_pfm(const std::string& path) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) throw std::runtime_error("cannot open " + path);
+    std::string magic;
+    uint32_t w = 0, h = 0;
+    float scale = 0.0f;
+    f >> magic >> w >> h >> scale;
+    f.get();
+    if ((magic != "PF" && magic != "Pf") || w == 0 || h == 0) throw std::runtime_error("not a PFM file: " + path);
+    const int ch = magic == "PF" ? 3 : 1;
+    std::vector<float> raw((size_t)w * h * ch);
+    f.read(reinterpret_cast<char*>(raw.data()), raw.size() * 4);
+    if (!f) throw std::runtime_error("truncated PFM file: " + path);
+    const bool little = scale < 0.0f;
+    const uint16_t probe = 1;
+    const bool host_little = *reinterpret_cast<const uint8_t*>(&probe) == 1;
+    if (little != host_little)
+        for (float& x : raw) {
+            uint8_t* b = reinterpret_cast<uint8_t*>(&x);
+            std::swap(b[0], b[3]);
+            std::swap(b[1], b[2]);
+        }
+    TextureData t;
+    t.width = w;
+    t.height = h;
+    t.rgba.resize((size_t)w * h * 4);
+    for (uint32_t y = 0; y < h; y++)  // PFM rows run bottom-up
+        for (uint32_t x = 0; x < w; x++) {
+            const float* src = &raw[((size_t)(h - 1 - y) * w + x) * ch];
+            float* dst = &t.rgba[((size_t)y * w + x) * 4];
+            for (int a = 0; a < 3; a++) dst[a] = src[ch == 3 ? a : 0];
+            dst[3] = 1.0f;
+        }
+    return t;
+}
+
+void write_pfm(const std::string& path, const float* rgba, uint32_t width, uint32_t height) {
+    std::ofstream f(path, std::ios::binary);
+    if (!f) throw std::runtime_error("cannot write " + path);
+    const uint16_t probe = 1;
+    const bool host_little = *reinterpret_cast<const uint8_t*>(&probe) == 1;
+    f << "PF\n" << width << " " << height << "\n" << (host_little ? "-1.0" : "1.0") << "\n";
+    std::vector<float> row((size_t)width * 3);
+    for (uint32_t y = 0; y < height; y++) {
+        const uint32_t src_y = height - 1 - y;
+        for (uint32_t x = 0; x < width; x++)
+            for (int a = 0; a < 3; a++) row[(size_t)x * 3 + a] = rgba[((size_t)src_y * width + x) * 4 + a];
+        f.write(reinterpret_cast<const char*>(row.data()), row.size() * 4);
+    }
+}
+
+}  // namespace lgbh

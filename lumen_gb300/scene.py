@@ -186,6 +186,15 @@ class Context:
             pass
 
 
+def film_rmse(ctx: Context, film, reference, mode: int = 0, stream=None) -> float:
+    """lgb_film_rmse on two (N, 4) float32 CUDA tensors; mode 1 gives the value Lumen reports."""
+    out = C.c_double(0.0)
+    _check(ctx.lib, ctx.handle, ctx.lib.lgb_film_rmse(ctx.handle, C.c_void_p(film.data_ptr()),
+                                                        C.c_void_p(reference.data_ptr()), film.shape[0], mode,
+                                                        C.byref(out), C.c_void_p(stream)))
+    return out.value
+
+
 class GpuScene:
     """A scene uploaded with lgb_scene_create; owns its BVH (lgb_bvh_build)."""
 

@@ -171,7 +171,14 @@ def cornell_secondary(torch, ctx_cls, scene_cls, local, cpu_leg: bool):
     sc.sync(stream.cuda_stream)
     ms = float(np.median(times))
     out = {"workload": "Cornell box 36 triangles, 256x256, 16 spp, max depth 8, FP32", "ms": ms,
-           "msamples_per_s": w * h * spp / (ms * 1e-3) / 1e6, "mean_radiance": float(film[:, :3].mean())}
+           "msamples_per_s": w * h * spp / (ms * 1e-3) / 1e6, "mean_radiance": float(film[:, :3].mean()),
+           "graph": "bounce loop captured once as a CUDA graph and replayed"}
+    ref_path = os.path.join(ROOT, "tests", "golden", "cornell_256_fp64_ref.npy")
+    if os.path.exists(ref_path):
+        from lumen_gb300.scene import film_rmse
+        ref = np.load(ref_path).reshape(-1, 3)
+        ref4 = torch.from_numpy(np.concatenate([ref, np.ones((len(ref), 1), np.float32)], 1)).cuda()
+        out["rmse_vs_fp64_2048spp"] = film_rmse(ctx, film, ref4, 0)
     if cpu_leg:
         sys.path.insert(0, os.path.join(ROOT, "tests"))
         import oracle_lib

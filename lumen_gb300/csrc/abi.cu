@@ -40,6 +40,8 @@ void free_scene(Scene* s) {
     cudaFree(s->d_status);
     cudaFree(s->d_ray_counter);
     cudaFree(s->pt_buf);
+    if (s->pt_graph) cudaGraphExecDestroy((cudaGraphExec_t)s->pt_graph);
+    if (s->capture_stream) cudaStreamDestroy((cudaStream_t)s->capture_stream);
 }
 
 template <class T> cudaError_t upload(T** dst, const T* src, size_t count) {

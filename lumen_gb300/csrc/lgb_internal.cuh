@@ -108,6 +108,9 @@ struct Scene {
     // path-tracer work buffers (grown on demand)
     void* pt_buf = nullptr;
     size_t pt_buf_bytes = 0;
+    void* pt_graph = nullptr;        // cudaGraphExec_t of the captured bounce loop
+    uint64_t pt_graph_key[6] = {};   // what the captured graph depends on
+    void* capture_stream = nullptr;  // private stream used only to record graphs
 };
 
 // Error helpers: record a message on the context and return a status.

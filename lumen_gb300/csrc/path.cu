@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 #include <string>
 
@@ -49,6 +50,18 @@ struct __align__(16) NeeRec {
 };
 enum : uint32_t { NEE_AREA = 1u };
 
+struct Params {
+    float iv[16], ip[16];
+    uint32_t width, height, npix;
+    float sky[3];
+    int max_depth, num_lights, light_tri_count;
+    uint32_t direct_lighting, film_mode;
+    uint32_t frame0;   // first frame of this chunk
+    uint32_t nframes;  // frames in this chunk
+    uint32_t cap;      // path capacity of the buffers
+    float4* film;      // RGBA32F output
+};
+
 struct Buffers {
     uint32_t* pix;      // pixel index
     uint32_t* frame;
@@ -68,18 +81,9 @@ struct Buffers {
     lgb_hit* mhits;
     uint32_t* sbits;
     uint32_t* counters; // [0] cur, [1] next, [2] nee, [3..6] class counts, [8..10] trace work counters
+    Params* params;     // per-chunk parameters in device memory, so that a captured graph can be replayed
 };
 
-struct Params {
-    float iv[16], ip[16];
-    uint32_t width, height, npix;
-    float sky[3];
-    int max_depth, num_lights, light_tri_count;
-    uint32_t direct_lighting, film_mode;
-    uint32_t frame0;   // first frame of this chunk
-    uint32_t nframes;  // frames in this chunk
-    uint32_t cap;      // path capacity of the buffers
-};
 
 struct SceneView {
     const WideNode* nodes;
@@ -193,7 +197,8 @@ __device__ __forceinline__ int class_of(uint32_t bsdf_type) {
 // ---------------- kernels ----------------
 
 // path.rgen:22-46: the seed is (x, y, frame, 0); two draws jitter the pixel.
-__global__ void __launch_bounds__(kThreads) k_camera(Params P, Buffers B) {
+__global__ void __launch_bounds__(kThreads) k_camera(const Params* __restrict__ Pp, Buffers B) {
+    const Params& P = *Pp;
     const uint32_t n = P.npix * P.nframes;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t pix = i % P.npix, f = P.frame0 + i / P.npix;
@@ -233,7 +238,8 @@ __global__ void __launch_bounds__(kThreads) k_q_trace_any(SceneView S, const lgb
 
 // path.rgen:49-55: a miss adds the sky colour (shade_atmosphere without a directional light returns
 // sky_col, commons.glsl:157-159) and ends the path; hits are binned by material class.
-__global__ void __launch_bounds__(kThreads) k_classify(SceneView S, Params P, Buffers B) {
+__global__ void __launch_bounds__(kThreads) k_classify(SceneView S, const Params* __restrict__ Pp, Buffers B) {
+    const Params& P = *Pp;
     const uint32_t n = B.counters[0];
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -290,7 +296,8 @@ __device__ __forceinline__ v3 cls_eval(v3 n_s, v3 wo, const Mat& m, bool ff, v3 
 
 // One bounce of path.rgen:56-100 for the hits of one material class.
 template <int CLS>
-__global__ void __launch_bounds__(kThreads) k_shade(SceneView S, Params P, Buffers B, int depth) {
+__global__ void __launch_bounds__(kThreads) k_shade(SceneView S, const Params* __restrict__ Pp, Buffers B, int depth) {
+    const Params& P = *Pp;
     const uint32_t n = B.counters[3 + CLS];
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t* list = B.q_cls + (size_t)CLS * P.cap;
@@ -508,7 +515,9 @@ __global__ void k_rotate(uint32_t* counters) {
 }
 
 // path.rgen:102-112 applied to the chunk's frames in order.
-__global__ void __launch_bounds__(kThreads) k_film(Params P, Buffers B, float4* __restrict__ film) {
+__global__ void __launch_bounds__(kThreads) k_film(const Params* __restrict__ Pp, Buffers B) {
+    const Params& P = *Pp;
+    float4* __restrict__ film = P.film;
     for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < P.npix; pix += gridDim.x * blockDim.x) {
         float4 px = film[pix];
         for (uint32_t k = 0; k < P.nframes; k++) {
@@ -531,8 +540,18 @@ __global__ void __launch_bounds__(kThreads) k_film(Params P, Buffers B, float4* 
     }
 }
 
-__global__ void k_init_counters(uint32_t* counters, uint32_t n) {
-    if (threadIdx.x < 16) counters[threadIdx.x] = threadIdx.x == 0 ? n : 0u;
+// Zeroes the occlusion words of this bounce's shadow queries (device-counted, so it can sit in a graph).
+__global__ void k_clear_bits(uint32_t* bits, const uint32_t* count_ptr) {
+    const uint32_t words = (*count_ptr + 31u) / 32u;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < words; i += gridDim.x * blockDim.x) bits[i] = 0u;
+}
+
+__global__ void k_init_counters(uint32_t* counters, const Params* __restrict__ Pp) {
+    if (threadIdx.x < 16) counters[threadIdx.x] = threadIdx.x == 0 ? Pp->npix * Pp->nframes : 0u;
+}
+
+__global__ void k_set_params(Params P, Params* dst) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *dst = P;
 }
 
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -559,7 +578,65 @@ size_t carve(char* base, uint32_t cap, Buffers& B) {
     B.mhits = (lgb_hit*)take(sizeof(lgb_hit) * (size_t)cap);
     B.sbits = (uint32_t*)take(4ull * ((cap + 31) / 32));
     B.counters = (uint32_t*)take(64);
+    B.params = (Params*)take(sizeof(Params));
     return off;
+}
+
+struct Grids {
+    int work, trace;
+};
+
+Grids path_grids(Ctx* ctx) {
+    int trace_blocks = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&trace_blocks, k_q_trace_closest, kThreads, 0);
+    const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    return Grids{sms * 8, sms * std::max(trace_blocks, 1)};
+}
+
+// One chunk of frames: camera rays, `bounces` bounces, film. Every kernel reads B.params, so this
+// sequence can be captured once and replayed with new parameters.
+cudaError_t launch_chunk(const SceneView& S, Buffers B, int bounces, Grids g, cudaStream_t st) {
+    k_init_counters<<<1, 32, 0, st>>>(B.counters, B.params);
+    k_camera<<<g.work, kThreads, 0, st>>>(B.params, B);
+    for (int depth = 0; depth < bounces; depth++) {
+        k_q_trace_closest<<<g.trace, kThreads, 0, st>>>(S, B.rays, B.hits, B.counters + 0, B.counters + 8);
+        k_classify<<<g.work, kThreads, 0, st>>>(S, B.params, B);
+        k_shade<CLS_DIFFUSE><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        k_shade<CLS_CONDUCTOR><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        k_shade<CLS_SPECULAR><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        k_shade<CLS_PRINCIPLED><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        k_clear_bits<<<g.work, kThreads, 0, st>>>(B.sbits, B.counters + 2);
+        k_q_trace_any<<<g.trace, kThreads, 0, st>>>(S, B.srays, B.sbits, B.counters + 2, B.counters + 9);
+        k_q_trace_closest<<<g.trace, kThreads, 0, st>>>(S, B.mrays, B.mhits, B.counters + 2, B.counters + 10);
+        k_nee_resolve<<<g.work, kThreads, 0, st>>>(S, B);
+        k_rotate<<<1, 32, 0, st>>>(B.counters);
+        std::swap(B.rays, B.rays_next);
+        std::swap(B.q_cur, B.q_next);
+    }
+    k_film<<<g.work, kThreads, 0, st>>>(B.params, B);
+    return cudaGetLastError();
+}
+
+SceneView scene_view(Scene* s) {
+    SceneView S;
+    S.nodes = s->bvh.nodes; S.tris = s->bvh.tris; S.verts = s->d_vertices; S.idx = s->d_indices;
+    S.tri_mesh = s->d_tri_mesh; S.meshes = s->d_meshes; S.mesh_first = s->d_mesh_first_tri; S.mats = s->d_materials;
+    S.lights = s->d_lights; S.texs = s->d_textures; S.status = s->d_status;
+    return S;
+}
+
+Params make_params(const lgb_camera* cam, const lgb_path_params* pp, uint32_t cap, float* film) {
+    Params P;
+    for (int i = 0; i < 16; i++) { P.iv[i] = cam->inv_view[i]; P.ip[i] = cam->inv_projection[i]; }
+    P.width = cam->width; P.height = cam->height; P.npix = cam->width * cam->height;
+    for (int i = 0; i < 3; i++) P.sky[i] = pp->sky_col[i];
+    P.max_depth = pp->max_depth; P.num_lights = pp->num_lights; P.light_tri_count = pp->light_triangle_count;
+    P.direct_lighting = pp->direct_lighting; P.film_mode = pp->film_mode;
+    P.cap = cap;
+    P.film = reinterpret_cast<float4*>(film);
+    P.frame0 = 0;
+    P.nframes = 0;
+    return P;
 }
 
 }  // namespace
@@ -575,6 +652,7 @@ lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* p
     Buffers B;
     const size_t bytes = carve(nullptr, cap, B);
     if (s->pt_buf_bytes < bytes) {
+        if (s->pt_graph) { cudaGraphExecDestroy((cudaGraphExec_t)s->pt_graph); s->pt_graph = nullptr; }
         cudaFree(s->pt_buf);
         s->pt_buf = nullptr;
         s->pt_buf_bytes = 0;
@@ -582,46 +660,46 @@ lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* p
         s->pt_buf_bytes = bytes;
     }
     carve((char*)s->pt_buf, cap, B);
-    SceneView S;
-    S.nodes = s->bvh.nodes; S.tris = s->bvh.tris; S.verts = s->d_vertices; S.idx = s->d_indices;
-    S.tri_mesh = s->d_tri_mesh; S.meshes = s->d_meshes; S.mesh_first = s->d_mesh_first_tri; S.mats = s->d_materials;
-    S.lights = s->d_lights; S.texs = s->d_textures; S.status = s->d_status;
-    Params P;
-    for (int i = 0; i < 16; i++) { P.iv[i] = cam->inv_view[i]; P.ip[i] = cam->inv_projection[i]; }
-    P.width = cam->width; P.height = cam->height; P.npix = npix;
-    for (int i = 0; i < 3; i++) P.sky[i] = pp->sky_col[i];
-    P.max_depth = pp->max_depth; P.num_lights = pp->num_lights; P.light_tri_count = pp->light_triangle_count;
-    P.direct_lighting = pp->direct_lighting; P.film_mode = pp->film_mode;
-    P.cap = cap;
-    const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
-    int trace_blocks = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&trace_blocks, k_q_trace_closest, kThreads, 0);
-    const int grid_work = sms * 8, grid_trace = sms * std::max(trace_blocks, 1);
+    const SceneView S = scene_view(s);
+    Params P = make_params(cam, pp, cap, film);
+    const Grids g = path_grids(ctx);
     const int bounces = std::max(pp->max_depth, 1);
+    // The bounce loop of a chunk is captured once into a CUDA graph and replayed; the graph depends only on the
+    // arena layout, the scene's device arrays and the bounce count, while everything per call travels in
+    // B.params. If the caller is itself capturing this stream, the kernels are issued directly into its capture.
+    cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+    LGB_CUDA_TRY(ctx, cudaStreamIsCapturing(st, &cap_status));
+    const bool use_graph = cap_status == cudaStreamCaptureStatusNone;
+    const uint64_t key[6] = {(uint64_t)(uintptr_t)s->pt_buf, cap, (uint64_t)bounces, (uint64_t)(uintptr_t)S.nodes,
+                             (uint64_t)(uintptr_t)S.tris, ((uint64_t)g.work << 32) | (uint32_t)g.trace};
+    if (use_graph && (!s->pt_graph || std::memcmp(key, s->pt_graph_key, sizeof(key)) != 0)) {
+        if (s->pt_graph) { cudaGraphExecDestroy((cudaGraphExec_t)s->pt_graph); s->pt_graph = nullptr; }
+        if (!s->capture_stream) LGB_CUDA_TRY(ctx, cudaStreamCreateWithFlags((cudaStream_t*)&s->capture_stream, cudaStreamNonBlocking));
+        const cudaStream_t cs = (cudaStream_t)s->capture_stream;
+        cudaGraph_t graph = nullptr;
+        LGB_CUDA_TRY(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        const cudaError_t le = launch_chunk(S, B, bounces, g, cs);
+        const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
+        if (le != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_error(ctx, le, "capturing the bounce loop"); }
+        if (ce != cudaSuccess) return cuda_error(ctx, ce, "cudaStreamEndCapture");
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) return cuda_error(ctx, ie, "cudaGraphInstantiate");
+        s->pt_graph = exec;
+        std::memcpy(s->pt_graph_key, key, sizeof(key));
+    }
     for (uint32_t done = 0; done < spp; done += frames_per_chunk) {
         P.frame0 = frame0 + done;
         P.nframes = std::min(frames_per_chunk, spp - done);
-        const uint32_t npaths = npix * P.nframes;
-        k_init_counters<<<1, 32, 0, st>>>(B.counters, npaths);
-        k_camera<<<grid_work, kThreads, 0, st>>>(P, B);
-        for (int depth = 0; depth < bounces; depth++) {
-            k_q_trace_closest<<<grid_trace, kThreads, 0, st>>>(S, B.rays, B.hits, B.counters + 0, B.counters + 8);
-            k_classify<<<grid_work, kThreads, 0, st>>>(S, P, B);
-            k_shade<CLS_DIFFUSE><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
-            k_shade<CLS_CONDUCTOR><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
-            k_shade<CLS_SPECULAR><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
-            k_shade<CLS_PRINCIPLED><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
-            LGB_CUDA_TRY(ctx, cudaMemsetAsync(B.sbits, 0, sizeof(uint32_t) * ((cap + 31) / 32), st));
-            k_q_trace_any<<<grid_trace, kThreads, 0, st>>>(S, B.srays, B.sbits, B.counters + 2, B.counters + 9);
-            k_q_trace_closest<<<grid_trace, kThreads, 0, st>>>(S, B.mrays, B.mhits, B.counters + 2, B.counters + 10);
-            k_nee_resolve<<<grid_work, kThreads, 0, st>>>(S, B);
-            k_rotate<<<1, 32, 0, st>>>(B.counters);
-            std::swap(B.rays, B.rays_next);
-            std::swap(B.q_cur, B.q_next);
+        k_set_params<<<1, 1, 0, st>>>(P, B.params);
+        if (use_graph) {
+            LGB_CUDA_TRY(ctx, cudaGraphLaunch((cudaGraphExec_t)s->pt_graph, st));
+        } else {
+            LGB_CUDA_TRY(ctx, launch_chunk(S, B, bounces, g, st));
         }
-        k_film<<<grid_work, kThreads, 0, st>>>(P, B, reinterpret_cast<float4*>(film));
-        LGB_CUDA_TRY(ctx, cudaGetLastError());
     }
+    LGB_CUDA_TRY(ctx, cudaGetLastError());
     return LGB_OK;
 }
 
@@ -687,47 +765,17 @@ lgb_status render_path_noalloc(Scene* s, const lgb_camera* cam, const lgb_path_p
     lgb_status ast = noalloc_arena(ctx, ctx->device, &arena);
     if (ast != LGB_OK) return ast;
     carve(arena, cap, B);
-    SceneView S;
-    S.nodes = s->bvh.nodes; S.tris = s->bvh.tris; S.verts = s->d_vertices; S.idx = s->d_indices;
-    S.tri_mesh = s->d_tri_mesh; S.meshes = s->d_meshes; S.mesh_first = s->d_mesh_first_tri; S.mats = s->d_materials;
-    S.lights = s->d_lights; S.texs = s->d_textures; S.status = s->d_status;
-    Params P;
-    for (int i = 0; i < 16; i++) { P.iv[i] = cam->inv_view[i]; P.ip[i] = cam->inv_projection[i]; }
-    P.width = cam->width; P.height = cam->height; P.npix = npix;
-    for (int i = 0; i < 3; i++) P.sky[i] = pp->sky_col[i];
-    P.max_depth = pp->max_depth; P.num_lights = pp->num_lights; P.light_tri_count = pp->light_triangle_count;
-    P.direct_lighting = pp->direct_lighting; P.film_mode = pp->film_mode;
-    P.cap = cap;
-    const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
-    int trace_blocks = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&trace_blocks, k_q_trace_closest, kThreads, 0);
-    const int grid_work = sms * 8, grid_trace = sms * std::max(trace_blocks, 1);
+    const SceneView S = scene_view(s);
+    Params P = make_params(cam, pp, cap, film);
+    const Grids g = path_grids(ctx);
     const int bounces = std::max(pp->max_depth, 1);
     for (uint32_t done = 0; done < spp; done += frames_per_chunk) {
         P.frame0 = frame0 + done;
         P.nframes = std::min(frames_per_chunk, spp - done);
-        const uint32_t npaths = npix * P.nframes;
-        // The arena keeps the previous call's contents: the counters are reset here, the occlusion bits
-        // before every shadow query, and every other array is written before it is read.
-        k_init_counters<<<1, 32, 0, st>>>(B.counters, npaths);
-        k_camera<<<grid_work, kThreads, 0, st>>>(P, B);
-        for (int depth = 0; depth < bounces; depth++) {
-            k_q_trace_closest<<<grid_trace, kThreads, 0, st>>>(S, B.rays, B.hits, B.counters + 0, B.counters + 8);
-            k_classify<<<grid_work, kThreads, 0, st>>>(S, P, B);
-            k_shade<CLS_DIFFUSE><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
-            k_shade<CLS_CONDUCTOR><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
-            k_shade<CLS_SPECULAR><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
-            k_shade<CLS_PRINCIPLED><<<grid_work, kThreads, 0, st>>>(S, P, B, depth);
-            LGB_CUDA_TRY(ctx, cudaMemsetAsync(B.sbits, 0, sizeof(uint32_t) * ((cap + 31) / 32), st));
-            k_q_trace_any<<<grid_trace, kThreads, 0, st>>>(S, B.srays, B.sbits, B.counters + 2, B.counters + 9);
-            k_q_trace_closest<<<grid_trace, kThreads, 0, st>>>(S, B.mrays, B.mhits, B.counters + 2, B.counters + 10);
-            k_nee_resolve<<<grid_work, kThreads, 0, st>>>(S, B);
-            k_rotate<<<1, 32, 0, st>>>(B.counters);
-            std::swap(B.rays, B.rays_next);
-            std::swap(B.q_cur, B.q_next);
-        }
-        k_film<<<grid_work, kThreads, 0, st>>>(P, B, reinterpret_cast<float4*>(film));
-        LGB_CUDA_TRY(ctx, cudaGetLastError());
+        // The arena keeps the previous call's contents: the parameters and counters are rewritten here, the
+        // occlusion bits before every shadow query, and every other array is written before it is read.
+        k_set_params<<<1, 1, 0, st>>>(P, B.params);
+        LGB_CUDA_TRY(ctx, launch_chunk(S, B, bounces, g, st));
     }
     return LGB_OK;
 }

@@ -133,3 +133,23 @@ def test_textured_albedo_matches_oracle(ctx, oracle):
     cam, got = gpu_samples(sc, cb, 48, 48, 0)
     want, _ = oracle.scene(cb).samples(cam, 8, 48, 48, 0)
     assert close_fraction(got, want) >= 0.99
+
+
+def test_converged_rmse_against_fp64_reference(cornell, oracle):
+    """16 spp at 256^2 against the committed 2048-spp FP64 oracle render: the GPU image and the FP32 oracle image
+    of the same samples have the same error against the converged reference."""
+    from lumen_gb300.scene import film_rmse
+    cb, sc, osc = cornell
+    ref = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "cornell_256_fp64_ref.npy"))
+    ref = ref.reshape(-1, 3)
+    w = h = 256
+    cam = camera_lookat(cb.camera_pos, cb.camera_dir, cb.fov, w, h)
+    film = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+    sc.render_path(cam, path_params(cb, 8), 0, 16, film)
+    sc.sync()
+    ref4 = torch.from_numpy(np.concatenate([ref, np.ones((len(ref), 1), np.float32)], 1)).cuda()
+    rmse_gpu = film_rmse(sc.ctx, film, ref4, 0)
+    cpu = osc.film(cam, 8, w, h, 0, 16)
+    rmse_cpu = float(np.sqrt(((cpu[:, :3].astype(np.float64) - ref) ** 2).mean()))
+    assert 0.0 < rmse_gpu < 0.5
+    np.testing.assert_allclose(rmse_gpu, rmse_cpu, rtol=0.02)

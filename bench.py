@@ -193,6 +193,62 @@ def cornell_secondary(torch, ctx_cls, scene_cls, local, cpu_leg: bool):
     return out
 
 
+def adjoint_secondary(torch, ctx_cls, scene_cls, local):
+    """Differentiable rendering (512^2, 32 spp, max depth 6, textured back wall + two GGX conductor boxes):
+    time of the primal (lgb_diff_render keeping the per-sample radiance) and of the adjoint replay
+    (lgb_adjoint_path from those samples) for gradients of an L2 image loss wrt 64x64 texels, roughness and
+    emission; the ratio (primal + adjoint) / primal is the cost of one gradient step."""
+    from lumen_gb300 import procedural
+    from lumen_gb300.scene import camera_lookat, path_params
+    arrays = procedural.cornell_diff()
+    ctx = ctx_cls(local)
+    sc = scene_cls(ctx, arrays)
+    sc.build()
+    w = h = 512
+    spp = 32
+    cam = camera_lookat(arrays.camera_pos, arrays.camera_dir, arrays.fov, w, h)
+    params = path_params(arrays, 6)
+    tex = torch.from_numpy(np.ascontiguousarray(arrays.textures[0])).cuda()
+    rough = torch.from_numpy(arrays.materials["roughness"].astype(np.float32)).cuda()
+    emis = torch.from_numpy(arrays.materials["emissive_factor"].astype(np.float32)).cuda()
+    film = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+    samples = torch.empty((spp * w * h, 4), dtype=torch.float32, device="cuda")
+    target = torch.from_numpy(np.random.default_rng(7).uniform(0.0, 1.0, (w * h, 4)).astype(np.float32)).cuda()
+    gt, gr, ge = torch.zeros_like(tex), torch.zeros_like(rough), torch.zeros_like(emis)
+    stream = torch.cuda.current_stream()
+    cs = stream.cuda_stream
+
+    def primal():
+        sc.diff_render(cam, params, 0, spp, film, 0, tex, rough, emis, samples=samples, stream=cs)
+
+    def backward():
+        dimage = (film - target) * (2.0 / film.numel())
+        sc.adjoint_path(cam, params, 0, spp, dimage, 0, tex, rough, emis, gt, gr, ge, samples=samples, stream=cs)
+
+    for _ in range(2):
+        primal()
+        backward()
+    torch.cuda.synchronize()
+    tp, ta = [], []
+    for _ in range(5):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record(stream)
+        primal()
+        e[1].record(stream)
+        backward()
+        e[2].record(stream)
+        e[2].synchronize()
+        tp.append(e[0].elapsed_time(e[1]))
+        ta.append(e[1].elapsed_time(e[2]))
+    sc.sync(cs)
+    mp, ma = float(np.median(tp)), float(np.median(ta))
+    return {"workload": "differentiable Cornell box, 512x512, 32 spp, max depth 6, 64x64 RGB texels + per-material "
+                        "roughness + emission, L2 image loss", "primal_ms": mp, "adjoint_ms": ma,
+            "primal_plus_adjoint_over_primal": (mp + ma) / mp,
+            "primal_msamples_per_s": w * h * spp / (mp * 1e-3) / 1e6,
+            "grad_norms": {"texels": float(gt.norm()), "roughness": float(gr.norm()), "emission": float(ge.norm())}}
+
+
 def run_reference(args):
     rank, world, _ = _dist()
     if rank != 0:
@@ -322,6 +378,7 @@ def run_gpu(args):
     secondary = {}
     if not args.no_secondary:
         secondary["path_tracer"] = cornell_secondary(torch, Context, GpuScene, local, world == 1 and not args.no_cpu_baseline)
+        secondary["adjoint"] = adjoint_secondary(torch, Context, GpuScene, local)
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",

@@ -219,6 +219,51 @@ LGB_API lgb_status lgb_render_path(lgb_scene* scene, const lgb_camera* camera, c
 LGB_API lgb_status lgb_render_path_noalloc(lgb_scene* scene, const lgb_camera* camera, const lgb_path_params* params,
                                            uint32_t frame0, uint32_t spp, float* d_film, void* stream);
 
+/* ---- differentiable rendering (no counterpart in Lumen) ----
+ * The estimator of lgb_render_path with every sampling decision detached from the parameters: directions,
+ * pdfs, MIS weights and Russian roulette use the scene's materials, while BSDF values and emission use the
+ * parameter buffers below. Parameters: the texels of one texture (albedo multipliers of the materials that use
+ * it), roughness per material (rough GGX conductors), emission per material (RGB). Null pointers keep the
+ * scene's values. With LGB_DIFF_SAMPLE_PARAMS the sampling decisions use the parameter values instead of the
+ * scene's (still detached: the gradient is that of f / p with p held fixed, which is exact when p follows the
+ * current values); an optimiser wants this, since sampling a lobe far from the one evaluated is noisy, while a
+ * finite-difference check with common random numbers wants it off.
+ * The image is the plain mean of the spp samples of each pixel (frames frame0..frame0+spp-1, seeded as
+ * lgb_render_path seeds them); a sample whose radiance is not finite counts as zero and has no gradient
+ * (Lumen's film drops it). Path depth is limited to 16. */
+#define LGB_DIFF_SAMPLE_PARAMS 1u /* sample with the parameter values too (still detached from them) */
+
+typedef struct lgb_diff_params {
+    int32_t texture_id;      /* texture whose texels are parameters */
+    uint32_t flags;          /* LGB_DIFF_* */
+    const float* texels;     /* device, width*height RGBA of that texture (alpha ignored); null = no texel params */
+    const float* roughness;  /* device, one per material */
+    const float* emission;   /* device, three per material */
+} lgb_diff_params;
+
+typedef struct lgb_diff_grads {  /* device gradient accumulators, same layouts; the library adds into them */
+    float* texels;
+    float* roughness;
+    float* emission;
+} lgb_diff_grads;
+
+/* Primal image of the differentiable estimator into d_film (RGBA32F, width*height). If d_samples is not null
+ * it receives the radiance of every sample (RGBA32F, [spp][width*height], 16 bytes each), which
+ * lgb_adjoint_path can replay from; otherwise the samples go to a scene-owned buffer. */
+LGB_API lgb_status lgb_diff_render(lgb_scene* scene, const lgb_camera* camera, const lgb_path_params* params,
+                                   const lgb_diff_params* diff, uint32_t frame0, uint32_t spp, float* d_film,
+                                   float* d_samples, void* stream);
+/* Adjoint path replay: adds d loss / d parameter into grads, given d loss / d image (RGBA32F per pixel, alpha
+ * ignored) for the image lgb_diff_render produces with the same arguments. Each path is re-traced from its
+ * counter-based RNG stream; no path vertex is stored. With d_primal_samples (the d_samples that
+ * lgb_diff_render wrote for the same arguments and parameter values) every path is traced once more;
+ * with null it is traced twice (primal, then replay). Gradients are accumulated with float atomics, so their
+ * low bits depend on the order of the additions. */
+LGB_API lgb_status lgb_adjoint_path(lgb_scene* scene, const lgb_camera* camera, const lgb_path_params* params,
+                                    const lgb_diff_params* diff, uint32_t frame0, uint32_t spp,
+                                    const float* d_dloss_dimage, const float* d_primal_samples, lgb_diff_grads* grads,
+                                    void* stream);
+
 /* Waits for `stream` and reports any fault a kernel recorded in the scene's device status word. */
 LGB_API lgb_status lgb_sync(lgb_scene* scene, void* stream);
 

@@ -99,6 +99,18 @@ class PathParams(C.Structure):
     ]
 
 
+DIFF_SAMPLE_PARAMS = 1
+
+
+class DiffParams(C.Structure):
+    _fields_ = [("texture_id", C.c_int32), ("flags", C.c_uint32), ("texels", C.c_void_p), ("roughness", C.c_void_p),
+                ("emission", C.c_void_p)]
+
+
+class DiffGrads(C.Structure):
+    _fields_ = [("texels", C.c_void_p), ("roughness", C.c_void_p), ("emission", C.c_void_p)]
+
+
 # Every exported symbol with its argument and result types (the declarations of include/lgb.h).
 SIGNATURES = {
     "lgb_abi_version": ([], C.c_uint32),
@@ -117,6 +129,10 @@ SIGNATURES = {
                          C.c_void_p], C.c_int32),
     "lgb_render_path_noalloc": ([C.c_void_p, C.POINTER(Camera), C.POINTER(PathParams), C.c_uint32, C.c_uint32,
                                  C.c_void_p, C.c_void_p], C.c_int32),
+    "lgb_diff_render": ([C.c_void_p, C.POINTER(Camera), C.POINTER(PathParams), C.POINTER(DiffParams), C.c_uint32,
+                         C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int32),
+    "lgb_adjoint_path": ([C.c_void_p, C.POINTER(Camera), C.POINTER(PathParams), C.POINTER(DiffParams), C.c_uint32,
+                          C.c_uint32, C.c_void_p, C.c_void_p, C.POINTER(DiffGrads), C.c_void_p], C.c_int32),
     "lgb_sync": ([C.c_void_p, C.c_void_p], C.c_int32),
     "lgb_film_rmse": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_double), C.c_void_p],
                       C.c_int32),

@@ -1,0 +1,655 @@
+// Differentiable path tracing: primal and adjoint path replay for gradients of an image loss with respect to
+// albedo texels, conductor roughness and emission. No counterpart in Lumen; built on the Path integrator's
+// estimator (src/shaders/integrators/path/path.rgen:22-113, pt_commons.glsl:3-48).
+//
+// Estimator. Every discrete or sampling decision is detached from the parameters: directions, pdfs, MIS
+// weights and Russian roulette come from the scene's own materials, while the BSDF values and emission that
+// multiply the path come from the parameter buffers. With the parameters equal to the scene's values this is
+// the ordinary estimator; for fixed random numbers it is a smooth function of the parameters (visibility held
+// fixed), so its gradient can be checked by central finite differences with common random numbers.
+//
+// Adjoint. Each thread renders one sample of one pixel twice. The primal pass records the radiance collected
+// at each depth; the replay pass re-runs the same path from the same counter-based RNG stream (nothing about
+// the path is stored) and, at every vertex, adds
+//   * for the BSDF value f at the continuation direction:   d loss / d ln f = delta * (radiance collected after it)
+//   * for the BSDF values in the two light-sampling terms:  d loss / d ln f = delta * (that term's contribution)
+//   * for emission: the throughput-weighted factors multiplying it,
+// where delta = d loss / d sample = d loss / d image / spp. These are turned into parameter gradients with
+// d f / d texel (bilinear weights) and d ln f / d roughness (GGX D and Smith G). Texel gradients go straight
+// to global atomics; roughness and emission gradients are kept per thread and reduced per warp before one
+// atomic per parameter.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "path_common.cuh"
+
+namespace lgb {
+namespace {
+
+constexpr int kDiffMaxDepth = 16;
+constexpr int kDiffRegMaterials = 8;  // roughness/emission gradients held in registers for materials 0..7
+#ifndef LGB_DIFF_THREADS
+#define LGB_DIFF_THREADS 128
+#endif
+#ifndef LGB_DIFF_MIN_BLOCKS
+#define LGB_DIFF_MIN_BLOCKS 1
+#endif
+constexpr int kDiffThreads = LGB_DIFF_THREADS;      // threads per block of the path kernels
+constexpr int kDiffMinBlocks = LGB_DIFF_MIN_BLOCKS; // resident blocks per SM the register budget is sized for
+constexpr float kTMinD = 0.001f, kTMaxD = 10000.0f, kEpsD = 0.001f;
+
+#ifndef LGB_DIFF_OUTLINE
+#define LGB_DIFF_OUTLINE 0
+#endif
+// Code size: the path loop calls closest-hit traversal twice, any-hit once and the BSDF sampler twice, and the
+// inlined body stalls on instruction fetch while a warp's paths sit at different bounces. Calling them out of
+// line (1 = traversal, 2 = traversal and BSDF dispatch) keeps one copy of each but measured slower on GB300
+// (call overhead and more registers: 46-55 against 69 Msamples/s at 512^2 x 32 spp), so the default inlines.
+#if LGB_DIFF_OUTLINE >= 1
+#define LGB_DIFF_TRACE_FN __noinline__
+#else
+#define LGB_DIFF_TRACE_FN __forceinline__
+#endif
+#if LGB_DIFF_OUTLINE >= 2
+#define LGB_DIFF_BSDF_FN __noinline__
+#else
+#define LGB_DIFF_BSDF_FN __forceinline__
+#endif
+
+struct DiffHit {
+    uint32_t prim;
+    float t, u, v;
+};
+
+__device__ LGB_DIFF_TRACE_FN DiffHit diff_closest(const WideNode* __restrict__ nodes, const WideTri* __restrict__ tris,
+                                                  RayQ rq, uint32_t* status) {
+    DiffHit h;
+    h.prim = trace_closest_single(nodes, tris, rq, h.t, h.u, h.v, status);
+    return h;
+}
+
+__device__ LGB_DIFF_TRACE_FN bool diff_any(const WideNode* __restrict__ nodes, const WideTri* __restrict__ tris, RayQ rq,
+                                           uint32_t* status) {
+    return trace_any_single(nodes, tris, rq, status);
+}
+
+struct BsdfSample {
+    v3 f, wi;
+    float pdf, cos_t;
+};
+
+template <uint32_t MASK>
+__device__ LGB_DIFF_BSDF_FN BsdfSample diff_sample_bsdf(v3 n_s, v3 wo, Mat m, bool side, v3 r) {
+    BsdfSample b;
+    b.f = sample_bsdf<MASK>(n_s, wo, m, side, b.wi, b.pdf, b.cos_t, r);
+    return b;
+}
+
+template <uint32_t MASK>
+__device__ LGB_DIFF_BSDF_FN float4 diff_eval_bsdf(v3 n_s, v3 wo, Mat m, bool side, v3 wi) {
+    float pdf;
+    const v3 f = eval_bsdf<MASK>(n_s, wo, m, side, wi, pdf);
+    return make_float4(f.x, f.y, f.z, pdf);
+}
+
+struct DiffArgs {
+    float iv[16], ip[16];
+    uint32_t width, height, npix;
+    float sky[3];
+    int max_depth, num_lights, light_tri_count;
+    uint32_t direct_lighting, frame0, spp, num_materials;
+    int tex_id;                 // texture whose texels are parameters (-1 = none)
+    uint32_t sample_params;     // sampling uses the evaluation material too
+    const float4* texels;       // its evaluation texels, tex_w * tex_h
+    uint32_t tex_w, tex_h;
+    const float* rough;         // evaluation roughness per material (null = scene values)
+    const float* emis;          // evaluation emission per material, RGB (null = scene values)
+    float4* samples;            // primal: radiance per sample, [spp][npix]
+    const float4* dimage;       // adjoint: d loss / d image per pixel
+    const float4* primal;       // adjoint: radiance per sample from the primal, [spp][npix] (null = recompute)
+    float4* g_tex;              // adjoint outputs
+    float* g_rough;
+    float* g_emis;
+};
+
+struct EvalMat {
+    Mat m;              // evaluation material
+    bool textured;      // albedo = base * parameter texture
+    v3 base;            // untextured albedo
+    float tex_w[4];     // bilinear weights and texel indices of the lookup
+    uint32_t tex_i[4];
+    v3 texc;            // interpolated texel colour
+};
+
+__device__ __forceinline__ v3 bilinear(const float4* __restrict__ t, uint32_t W, uint32_t H, float u, float v, float* w,
+                                       uint32_t* idx) {
+    if (!isfinite(u) || !isfinite(v)) { u = 0.0f; v = 0.0f; }
+    const float x = u * (float)W - 0.5f, y = v * (float)H - 0.5f;
+    const float x0 = floorf(x), y0 = floorf(y);
+    const float fx = x - x0, fy = y - y0;
+    const long long Wl = W, Hl = H;
+    long long ix = (long long)x0 % Wl; if (ix < 0) ix += Wl;
+    long long iy = (long long)y0 % Hl; if (iy < 0) iy += Hl;
+    const long long ix1 = (ix + 1) % Wl, iy1 = (iy + 1) % Hl;
+    idx[0] = (uint32_t)(iy * Wl + ix); idx[1] = (uint32_t)(iy * Wl + ix1);
+    idx[2] = (uint32_t)(iy1 * Wl + ix); idx[3] = (uint32_t)(iy1 * Wl + ix1);
+    w[0] = (1.0f - fx) * (1.0f - fy); w[1] = fx * (1.0f - fy); w[2] = (1.0f - fx) * fy; w[3] = fx * fy;
+    return f3(t[idx[0]]) * w[0] + f3(t[idx[1]]) * w[1] + f3(t[idx[2]]) * w[2] + f3(t[idx[3]]) * w[3];
+}
+
+__device__ __forceinline__ EvalMat eval_material(const SceneView& S, const DiffArgs& A, const Mat& ms, uint32_t mat_idx,
+                                                 float u, float v) {
+    EvalMat e;
+    e.m = ms;
+    e.textured = false;
+    const lgb_material* src = &S.mats[mat_idx];
+    e.base = V3(src->albedo[0], src->albedo[1], src->albedo[2]);
+    if (A.texels && src->texture_id >= 0 && src->texture_id == A.tex_id) {
+        e.textured = true;
+        e.texc = bilinear(A.texels, A.tex_w, A.tex_h, u, v, e.tex_w, e.tex_i);
+        e.m.albedo = e.base * e.texc;
+    }
+    if (A.rough) e.m.roughness = A.rough[mat_idx];
+    if (A.emis) e.m.emissive = V3(A.emis[3 * mat_idx], A.emis[3 * mat_idx + 1], A.emis[3 * mat_idx + 2]);
+    return e;
+}
+
+// Value of the evaluation BSDF for (wo, wi) in world space. Diffuse and rough conductors depend on the
+// parameters; every other lobe keeps the detached value `fallback`.
+__device__ __forceinline__ v3 eval_value(const EvalMat& e, v3 n_s, v3 wo, v3 wi, v3 fallback, bool from_sample) {
+    v3 T, B;
+    branchless_onb(n_s, T, B);
+    const v3 wol = to_local(wo, T, B, n_s), wil = to_local(wi, T, B, n_s);
+    if (e.m.type == LGB_BSDF_DIFFUSE) {
+        float pdf;
+        const v3 f = eval_diffuse(e.m, wol, wil, pdf);
+        return from_sample && fallback.x == 0.0f && fallback.y == 0.0f && fallback.z == 0.0f ? V3(0.0f) : f;
+    }
+    if (e.m.type == LGB_BSDF_CONDUCTOR && !effectively_delta(e.m.roughness * e.m.roughness)) {
+        float pdf;
+        return eval_conductor(e.m, wol, wil, pdf);
+    }
+    return fallback;
+}
+
+// d ln(D G) / d roughness of the isotropic GGX conductor (D_iso and the height-correlated Smith G of
+// microfacet_commons.glsl, alpha = roughness^2, so alpha^2 = roughness^4).
+__device__ __forceinline__ float conductor_dlog_dr(float r, v3 wol, v3 wil) {
+    const float alpha = r * r, a2 = alpha * alpha;
+    v3 h = normalize(wol + wil);
+    h = h * signf(h.z);
+    const float c2 = h.z * h.z;
+    const float d = c2 * (a2 - 1.0f) + 1.0f;
+    const float dlnD = 1.0f / a2 - 2.0f * c2 / d;
+    auto lam = [&](float c, float& dl) {
+        const float cs = c * c;
+        const float ts = fmaxf(1.0f - cs, 0.0f) / cs;
+        const float q = sqrtf(1.0f + a2 * ts);
+        dl = c == 0.0f ? 0.0f : 0.25f * ts / q;
+        return c == 0.0f ? 0.0f : 0.5f * (q - 1.0f);
+    };
+    float dlo, dli;
+    const float lo = lam(wol.z, dlo), li = lam(wil.z, dli);
+    const float G = 1.0f / (1.0f + lo + li);
+    const float dlnG = -(dlo + dli) * G;
+    return (dlnD + dlnG) * 4.0f * r * r * r;
+}
+
+// Roughness and emission gradients of materials 0..kDiffRegMaterials-1 are summed in shared memory per block
+// and pushed with one global atomic per parameter at the end; other materials go straight to global memory.
+struct GradAcc {
+    float* rough;  // shared, kDiffRegMaterials
+    float* emis;   // shared, 3 * kDiffRegMaterials
+};
+
+__device__ __forceinline__ void add_emis(const DiffArgs& A, GradAcc& g, uint32_t m, v3 v) {
+    if (!(isfinite(v.x) && isfinite(v.y) && isfinite(v.z))) return;
+    if (m < kDiffRegMaterials) {
+        atomicAdd(&g.emis[3 * m], v.x); atomicAdd(&g.emis[3 * m + 1], v.y); atomicAdd(&g.emis[3 * m + 2], v.z);
+    } else {
+        atomicAdd(&A.g_emis[3 * m], v.x); atomicAdd(&A.g_emis[3 * m + 1], v.y); atomicAdd(&A.g_emis[3 * m + 2], v.z);
+    }
+}
+
+// sf = d loss / d ln f per channel for the rough-conductor value f(wo, wi) of evaluation material e.
+__device__ __forceinline__ void add_rough_grad(const DiffArgs& A, GradAcc& g, const EvalMat& e, uint32_t m, v3 sf,
+                                               v3 n_s, v3 wo, v3 wi) {
+    if (e.m.type != LGB_BSDF_CONDUCTOR || !A.rough || effectively_delta(e.m.roughness * e.m.roughness)) return;
+    v3 T, B;
+    branchless_onb(n_s, T, B);
+    const float q = conductor_dlog_dr(e.m.roughness, to_local(wo, T, B, n_s), to_local(wi, T, B, n_s));
+    const float v = (sf.x + sf.y + sf.z) * q;
+    if (!isfinite(v)) return;
+    atomicAdd(m < kDiffRegMaterials ? &g.rough[m] : &A.g_rough[m], v);
+}
+
+// Texel gradients of one vertex. All BSDF values of a textured diffuse vertex share the texture lookup, so
+// their d loss / d ln f add up first: f_c = base_c * tex_c / pi gives d loss / d texel_{i,c} = sf_c * w_i / tex_c,
+// one float4 reduction per bilinear tap.
+__device__ __forceinline__ void flush_texel_grad(const DiffArgs& A, const EvalMat& e, v3 sf) {
+    if (!e.textured || e.m.type != LGB_BSDF_DIFFUSE) return;
+    if (sf.x == 0.0f && sf.y == 0.0f && sf.z == 0.0f) return;
+    const v3 s = V3(e.texc.x > 0.0f ? sf.x / e.texc.x : 0.0f, e.texc.y > 0.0f ? sf.y / e.texc.y : 0.0f,
+                    e.texc.z > 0.0f ? sf.z / e.texc.z : 0.0f);
+    if (!(isfinite(s.x) && isfinite(s.y) && isfinite(s.z))) return;
+    for (int k = 0; k < 4; k++) {
+        const float w = e.tex_w[k];
+        if (w == 0.0f) continue;
+        atomicAdd(&A.g_tex[e.tex_i[k]], make_float4(s.x * w, s.y * w, s.z * w, 0.0f));
+    }
+}
+
+// Replay modes of diff_path.
+enum : int {
+    kPrimal = 0,       // radiance only
+    kReplaySuffix = 1, // contrib holds, per depth, the radiance collected after that depth
+    kReplayTotal = 2,  // total holds the sample's radiance; the radiance after each depth is what remains
+    kRecord = 3,       // radiance, and the radiance collected at each depth written to contrib
+};
+
+// One sample of pixel `pix` at `frame`; returns its radiance. The replay modes accumulate gradients.
+template <int MODE, uint32_t MASK>
+__device__ v3 diff_path(const SceneView& S, const DiffArgs& A, uint32_t pix, uint32_t frame, v3* contrib, v3 total,
+                        v3 delta, GradAcc& g) {
+    constexpr bool ADJ = MODE == kReplaySuffix || MODE == kReplayTotal;
+    const uint32_t x = pix % A.width, y = pix / A.width;
+    uint4 seed = make_uint4(x, y, frame, 0u);
+    const float r0 = rnd(seed) - 0.5f;
+    const float r1 = rnd(seed) - 0.5f;
+    const float pu = ((float)x + 0.5f + r0) / (float)A.width, pv = ((float)y + 0.5f + r1) / (float)A.height;
+    const float dx = pu * 2.0f - 1.0f, dy = pv * 2.0f - 1.0f;
+    const float4 o4 = mat_vec(A.iv, 0.0f, 0.0f, 0.0f, 1.0f);
+    const float4 t4 = mat_vec(A.ip, dx, dy, 1.0f, 1.0f);
+    const v3 tn = normalize(V3(t4.x, t4.y, t4.z));
+    const float4 d4 = mat_vec(A.iv, tn.x, tn.y, tn.z, 0.0f);
+    v3 origin = V3(o4.x, o4.y, o4.z), dir = V3(d4.x, d4.y, d4.z);
+    v3 Tv = V3(1.0f), Tc = V3(1.0f), L = V3(0.0f), rem = total;
+    bool last_spec = false;
+    const v3 sky = V3(A.sky[0], A.sky[1], A.sky[2]);
+    for (int depth = 0; depth < kDiffMaxDepth; depth++) {
+        v3 Cd = V3(0.0f);
+        const RayQ rq = make_rayq(origin.x, origin.y, origin.z, kTMinD, dir.x, dir.y, dir.z, kTMaxD);
+        const DiffHit ph = diff_closest(S.nodes, S.tris, rq, S.status);
+        const uint32_t prim = ph.prim;
+        const float bu = ph.u, bv = ph.v;
+        if (prim == LGB_NO_HIT) {
+            if (depth > 0 || A.direct_lighting == 1u) Cd = Tv * sky;
+            if (MODE == kRecord) contrib[depth] = Cd;
+            L = L + Cd;
+            break;
+        }
+        const HitAttr h = resolve_hit(S, prim, bu, bv);
+        Mat ms = load_material(S, h.mat, h.u, h.v);
+        const EvalMat em = eval_material(S, A, ms, h.mat, h.u, h.v);
+        if (A.sample_params) ms = em.m;  // then every BSDF value below is the sampler's own
+        if ((depth == 0 && A.direct_lighting == 1u) || last_spec) {
+            Cd = Cd + Tv * em.m.emissive;
+            if (ADJ && A.emis) add_emis(A, g, h.mat, delta * Tv);
+        }
+        if (depth >= A.max_depth - 1) {
+            if (MODE == kRecord) contrib[depth] = Cd;
+            L = L + Cd;
+            break;
+        }
+        const v3 wo = -dir;
+        v3 n_s = h.n_s;
+        bool side = true;
+        v3 n_g = h.n_g;
+        if (dot(h.n_g, wo) < 0.0f) n_g = -n_g;
+        if (dot(n_g, h.n_s) < 0.0f) { n_s = -n_s; side = false; }
+        const v3 next_origin = offset_ray(h.pos, n_g);
+        const bool spec = has_prop(ms.props, LGB_FLAG_SPECULAR);
+        v3 sf_tex = V3(0.0f);  // d loss / d ln f summed over this vertex's BSDF values (texel gradients)
+        if (!spec && (depth > 0 || A.direct_lighting == 1u)) {
+            if (A.num_lights <= 0) {
+                for (int k = 0; k < 4; k++) (void)rnd(seed);
+            } else {
+                const float lpp = 1.0f / (float)A.light_tri_count;
+                const float q0 = rnd(seed), q1 = rnd(seed), q2 = rnd(seed), q3 = rnd(seed);
+                const uint32_t li = (uint32_t)(q0 * (float)A.num_lights);
+                const lgb_light* Lt = &S.lights[li];
+                const uint32_t ltype = Lt->light_flags & 7u;
+                v3 Le = V3(0.0f), wi = V3(0.0f);
+                float wi_len = 0.0f, pdf_w = 0.0f, pdf_a = 0.0f;
+                uint32_t lprim = LGB_NO_HIT, lmat = 0xFFFFFFFFu;
+                if (ltype == LGB_LIGHT_AREA) {
+                    const lgb_mesh pm = S.meshes[Lt->prim_mesh_idx];
+                    const uint32_t tri = (uint32_t)(q1 * (float)Lt->num_triangles);
+                    lprim = S.mesh_first[Lt->prim_mesh_idx] + tri;
+                    const uint32_t io = pm.index_offset + 3u * tri;
+                    const DevVertex a = S.verts[S.idx[io] + pm.vertex_offset];
+                    const DevVertex b = S.verts[S.idx[io + 1] + pm.vertex_offset];
+                    const DevVertex c = S.verts[S.idx[io + 2] + pm.vertex_offset];
+                    const float su = 1.0f - sqrtf(q2), sv = q3 * sqrtf(q2);
+                    const float b0 = 1.0f - su - sv;
+                    const v3 v0 = V3(a.px, a.py, a.pz), v1 = V3(b.px, b.py, b.pz), v2 = V3(c.px, c.py, c.pz);
+                    const v3 lpos = v0 * b0 + v1 * su + v2 * sv;
+                    const v3 ln = normalize(normalize(V3(a.nx, a.ny, a.nz) * b0 + V3(b.nx, b.ny, b.nz) * su +
+                                                      V3(c.nx, c.ny, c.nz) * sv));
+                    const float tri_pdf = 2.0f / length(cross(v1 - v0, v2 - v0));
+                    lmat = pm.material_index;
+                    const lgb_material* lm = &S.mats[lmat];
+                    Le = A.emis ? V3(A.emis[3 * lmat], A.emis[3 * lmat + 1], A.emis[3 * lmat + 2])
+                                : V3(lm->emissive_factor[0], lm->emissive_factor[1], lm->emissive_factor[2]);
+                    wi = lpos - h.pos;
+                    const float l2 = dot(wi, wi);
+                    wi_len = sqrtf(l2);
+                    wi = wi / wi_len;
+                    const float cfl = fabsf(dot(ln, -wi));
+                    pdf_a = tri_pdf;
+                    pdf_w = pdf_a * l2 / cfl;
+                } else if (ltype == LGB_LIGHT_SPOT) {
+                    const v3 lp = V3(Lt->pos[0], Lt->pos[1], Lt->pos[2]);
+                    wi = lp - h.pos;
+                    const float l2 = dot(wi, wi);
+                    wi_len = sqrtf(l2);
+                    wi = wi / wi_len;
+                    const v3 ldir = normalize(V3(Lt->to[0], Lt->to[1], Lt->to[2]) - lp);
+                    const float cfl = dot(-wi, ldir);
+                    const float cw = cosf(LGB_PI / 6.0f), cf = cosf(25.0f * LGB_PI / 180.0f);
+                    float fall;
+                    if (cfl < cw) fall = 0.0f;
+                    else if (cfl >= cf) fall = 1.0f;
+                    else { const float dd = (cfl - cw) / (cf - cw); fall = (dd * dd) * (dd * dd); }
+                    pdf_a = 1.0f;
+                    pdf_w = l2;
+                    Le = V3(Lt->L[0], Lt->L[1], Lt->L[2]) * fall;
+                } else {
+                    const v3 ddir = normalize(V3(Lt->pos[0], Lt->pos[1], Lt->pos[2]) - V3(Lt->to[0], Lt->to[1], Lt->to[2]));
+                    const v3 lp = h.pos + ddir * (2.0f * Lt->world_radius);
+                    wi = lp - h.pos;
+                    wi_len = length(wi);
+                    wi = wi / wi_len;
+                    pdf_a = 1.0f;
+                    pdf_w = 1.0f;
+                    Le = V3(Lt->L[0], Lt->L[1], Lt->L[2]);
+                }
+                const v3 sp = offset_ray2(h.pos, n_s);
+                const float cos_x = dot(n_s, wi);
+                const float4 fp1 = diff_eval_bsdf<MASK>(n_s, wo, ms, side, wi);
+                const v3 fs1 = V3(fp1.x, fp1.y, fp1.z);
+                const float bsdf_pdf = fp1.w;
+                const v3 fe1 = A.sample_params ? fs1 : eval_value(em, n_s, wo, wi, fs1, false);
+                v3 term1 = V3(0.0f), k1 = V3(0.0f);
+                if (pdf_w > 0.0f) {
+                    const RayQ sq = make_rayq(sp.x, sp.y, sp.z, 0.0f, wi.x, wi.y, wi.z, wi_len - kEpsD);
+                    if (!diff_any(S.nodes, S.tris, sq, S.status)) {
+                        const float mis = ((Lt->light_flags >> 5) & 1u) ? 1.0f : 1.0f / (1.0f + bsdf_pdf / pdf_w);
+                        k1 = mis * fe1 * fabsf(cos_x) / pdf_w;  // term1 = k1 * Le
+                        term1 = k1 * Le;
+                    }
+                }
+                v3 term2 = V3(0.0f), k2 = V3(0.0f), wi2 = V3(0.0f);
+                if (ltype == LGB_LIGHT_AREA) {
+                    const float b0r = rnd(seed), b1r = rnd(seed), b2r = rnd(seed);
+                    const BsdfSample bs2 = diff_sample_bsdf<MASK>(n_s, wo, ms, side, V3(b0r, b1r, b2r));
+                    const v3 fs2 = bs2.f;
+                    const float pdf2 = bs2.pdf, cos2 = bs2.cos_t;
+                    wi2 = bs2.wi;
+                    if (pdf2 != 0.0f) {
+                        const RayQ mq = make_rayq(sp.x, sp.y, sp.z, kTMinD, wi2.x, wi2.y, wi2.z, kTMaxD);
+                        const DiffHit mhit = diff_closest(S.nodes, S.tris, mq, S.status);
+                        const uint32_t mprim = mhit.prim;
+                        const float mu = mhit.u, mv = mhit.v;
+                        // a missed MIS ray leaves the previous payload (ray.rmiss:13): compare the shading triangle
+                        const uint32_t pl_prim = mprim == LGB_NO_HIT ? prim : mprim;
+                        if (pl_prim == lprim) {
+                            v3 pl_pos = h.pos, pl_ns = h.n_s;
+                            if (mprim != LGB_NO_HIT) {
+                                const HitAttr mh = resolve_hit(S, mprim, mu, mv);
+                                pl_pos = mh.pos;
+                                pl_ns = mh.n_s;
+                            }
+                            const float wl = length(pl_pos - h.pos);
+                            const float gg = fabsf(dot(pl_ns, -wi2)) / (wl * wl);
+                            const float mis = 1.0f / (1.0f + pdf_a / (gg * pdf2));
+                            const v3 fe2 = A.sample_params ? fs2 : eval_value(em, n_s, wo, wi2, fs2, true);
+                            k2 = fe2 * mis * fabsf(cos2) / pdf2;
+                            term2 = k2 * Le;
+                        }
+                    }
+                }
+                const v3 res = term1 + term2;
+                Cd = Cd + Tv * res / lpp;
+                if (ADJ) {
+                    if (A.emis && lmat != 0xFFFFFFFFu) add_emis(A, g, lmat, delta * Tv * (k1 + k2) / lpp);
+                    const v3 sf1 = delta * (Tv * term1 / lpp), sf2 = delta * (Tv * term2 / lpp);
+                    sf_tex = sf1 + sf2;
+                    add_rough_grad(A, g, em, h.mat, sf1, n_s, wo, wi);
+                    if (ltype == LGB_LIGHT_AREA) add_rough_grad(A, g, em, h.mat, sf2, n_s, wo, wi2);
+                }
+            }
+        }
+        const float c0 = rnd(seed), c1 = rnd(seed), c2 = rnd(seed);
+        const BsdfSample bs = diff_sample_bsdf<MASK>(n_s, wo, ms, side, V3(c0, c1, c2));
+        const v3 fs = bs.f, dnext = bs.wi;
+        const float pdf = bs.pdf, cos_t = bs.cos_t;
+        if (MODE == kRecord) contrib[depth] = Cd;
+        L = L + Cd;
+        v3 after = V3(0.0f);  // radiance collected after this depth
+        if (MODE == kReplaySuffix) after = contrib[depth];
+        if (MODE == kReplayTotal) { rem = rem - Cd; after = rem; }
+        if (pdf == 0.0f) {
+            if (ADJ) flush_texel_grad(A, em, sf_tex);
+            break;
+        }
+        const v3 fe = A.sample_params ? fs : eval_value(em, n_s, wo, dnext, fs, true);
+        if (ADJ) {
+            const v3 sf3 = delta * after;
+            add_rough_grad(A, g, em, h.mat, sf3, n_s, wo, dnext);
+            flush_texel_grad(A, em, sf_tex + sf3);
+        }
+        Tv = Tv * (fe * fabsf(cos_t) / pdf);
+        Tc = Tc * (fs * fabsf(cos_t) / pdf);
+        float rr_scale = 1.0f;
+        if (has_prop(ms.props, LGB_FLAG_TRANSMISSION)) rr_scale *= side ? 1.0f / ms.ior : ms.ior;
+        if (depth > 3) {
+            const float rr = fminf(0.95f, luminance(Tc) * rr_scale);
+            if (rr == 0.0f || rr < rnd(seed)) break;
+            Tv = Tv / rr;
+            Tc = Tc / rr;
+        }
+        origin = next_origin;
+        dir = dnext;
+        last_spec = spec;
+    }
+    return L;
+}
+
+// MODE kPrimal writes each sample's radiance; kReplaySuffix re-runs the primal in the thread (kRecord, keeping
+// the per-depth radiance in local memory) and then replays; kReplayTotal replays once from the stored radiance
+// of each sample.
+template <int MODE, uint32_t MASK>
+__global__ void __launch_bounds__(kDiffThreads, kDiffMinBlocks) k_diff(SceneView S, DiffArgs A) {
+    __shared__ float sh_grad[4 * kDiffRegMaterials];
+    constexpr bool ADJ = MODE != kPrimal;
+    GradAcc g{sh_grad, sh_grad + kDiffRegMaterials};
+    if (ADJ) {
+        for (int i = threadIdx.x; i < 4 * kDiffRegMaterials; i += blockDim.x) sh_grad[i] = 0.0f;
+        __syncthreads();
+    }
+    const uint32_t n = A.npix * A.spp;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const float inv = 1.0f / (float)A.spp;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t pix = i % A.npix, k = i / A.npix;
+        if (MODE == kPrimal) {
+            // a sample whose radiance is not finite counts as zero and is marked (w = 0) so the replay skips it;
+            // Lumen's film drops such samples (path.rgen:102-104)
+            const v3 L = diff_path<kPrimal, MASK>(S, A, pix, A.frame0 + k, nullptr, V3(0.0f), V3(0.0f), g);
+            const bool ok = isfinite(L.x) && isfinite(L.y) && isfinite(L.z);
+            A.samples[(size_t)k * A.npix + pix] = ok ? make_float4(L.x, L.y, L.z, 1.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        } else {
+            const float4 di = A.dimage[pix];
+            const v3 delta = V3(di.x * inv, di.y * inv, di.z * inv);
+            if (delta.x == 0.0f && delta.y == 0.0f && delta.z == 0.0f) continue;
+            if (MODE == kReplayTotal) {
+                const float4 tot = A.primal[(size_t)k * A.npix + pix];
+                if (tot.w == 0.0f) continue;
+                (void)diff_path<kReplayTotal, MASK>(S, A, pix, A.frame0 + k, nullptr, V3(tot.x, tot.y, tot.z), delta, g);
+            } else {
+                v3 contrib[kDiffMaxDepth];
+                for (int d = 0; d < kDiffMaxDepth; d++) contrib[d] = V3(0.0f);
+                const v3 L = diff_path<kRecord, MASK>(S, A, pix, A.frame0 + k, contrib, V3(0.0f), V3(0.0f), g);
+                if (!(isfinite(L.x) && isfinite(L.y) && isfinite(L.z))) continue;
+                v3 acc = V3(0.0f);  // per-depth radiance into suffix sums, summed back to front
+                for (int d = kDiffMaxDepth - 1; d >= 0; d--) {
+                    const v3 c = contrib[d];
+                    contrib[d] = acc;
+                    acc = acc + c;
+                }
+                (void)diff_path<kReplaySuffix, MASK>(S, A, pix, A.frame0 + k, contrib, V3(0.0f), delta, g);
+            }
+        }
+    }
+    if (ADJ) {
+        __syncthreads();
+        const uint32_t nm = min(A.num_materials, (uint32_t)kDiffRegMaterials);
+        for (uint32_t j = threadIdx.x; j < nm; j += blockDim.x) {
+            if (A.rough && sh_grad[j] != 0.0f) atomicAdd(&A.g_rough[j], sh_grad[j]);
+            if (A.emis) {
+                for (int c = 0; c < 3; c++) {
+                    const float e = sh_grad[kDiffRegMaterials + 3 * j + c];
+                    if (e != 0.0f) atomicAdd(&A.g_emis[3 * j + c], e);
+                }
+            }
+        }
+    }
+}
+
+// Kernel instantiation for a scene's BSDF types: diffuse + conductor scenes get a kernel without the
+// dielectric and principled lobes.
+template <int MODE>
+void launch_diff(Scene* s, const DiffArgs& A, int grid, cudaStream_t cs) {
+    constexpr uint32_t kDC = LGB_BSDF_DIFFUSE | LGB_BSDF_CONDUCTOR;
+    if ((s->bsdf_mask & ~kDC) == 0) k_diff<MODE, kDC><<<grid, kDiffThreads, 0, cs>>>(scene_view(s), A);
+    else k_diff<MODE, sh::kAllBsdfs><<<grid, kDiffThreads, 0, cs>>>(scene_view(s), A);
+}
+
+// Film = mean of the spp samples of each pixel, summed in frame order.
+__global__ void k_mean(const float4* __restrict__ samples, uint32_t npix, uint32_t spp, float4* __restrict__ film) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
+        float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+        for (uint32_t k = 0; k < spp; k++) {
+            const float4 v = samples[(size_t)k * npix + p];
+            sx += v.x; sy += v.y; sz += v.z;
+        }
+        const float inv = 1.0f / (float)spp;
+        film[p] = make_float4(sx * inv, sy * inv, sz * inv, 1.0f);
+    }
+}
+
+}  // namespace
+}  // namespace lgb
+
+using namespace lgb;
+
+namespace {
+
+lgb_status make_diff_args(lgb_scene* s, const lgb_camera* cam, const lgb_path_params* p, const lgb_diff_params* dp,
+                          uint32_t frame0, uint32_t spp, DiffArgs& A) {
+    if (!cam || !p || !dp || cam->width == 0 || cam->height == 0 || spp == 0)
+        return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "null camera/params/diff params or zero spp");
+    if (!s->bvh.nodes) return set_error(s->ctx, LGB_ERR_NOT_READY, "lgb_bvh_build has not been called");
+    if (p->max_depth > kDiffMaxDepth) return set_error(s->ctx, LGB_ERR_UNSUPPORTED, "differentiable path depth is limited to 16");
+    if (p->num_lights < 0 || (uint32_t)p->num_lights > s->num_lights || (p->num_lights > 0 && p->light_triangle_count <= 0))
+        return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "bad light counts");
+    if (p->dir_light_idx != 0xFFFFFFFFu) return set_error(s->ctx, LGB_ERR_UNSUPPORTED, "directional-light atmosphere unsupported");
+    if ((uint64_t)cam->width * cam->height * spp >= 0x80000000ull)
+        return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "width * height * spp must stay below 2^31");
+    if (dp->texels) {
+        if (dp->texture_id < 0 || (uint32_t)dp->texture_id >= s->num_textures)
+            return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "texture_id of the texel parameters is out of range");
+        if (reinterpret_cast<uintptr_t>(dp->texels) & 15u)
+            return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "texel parameters must be 16-byte aligned");
+    }
+    if ((reinterpret_cast<uintptr_t>(dp->roughness) & 3u) || (reinterpret_cast<uintptr_t>(dp->emission) & 3u))
+        return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "roughness/emission parameters must be 4-byte aligned");
+    std::memset(&A, 0, sizeof(A));
+    for (int i = 0; i < 16; i++) { A.iv[i] = cam->inv_view[i]; A.ip[i] = cam->inv_projection[i]; }
+    A.width = cam->width; A.height = cam->height; A.npix = cam->width * cam->height;
+    for (int i = 0; i < 3; i++) A.sky[i] = p->sky_col[i];
+    A.max_depth = p->max_depth; A.num_lights = p->num_lights; A.light_tri_count = p->light_triangle_count;
+    A.direct_lighting = p->direct_lighting; A.frame0 = frame0; A.spp = spp; A.num_materials = s->num_materials;
+    A.tex_id = dp->texels ? dp->texture_id : -1;
+    A.sample_params = (dp->flags & LGB_DIFF_SAMPLE_PARAMS) ? 1u : 0u;
+    A.texels = reinterpret_cast<const float4*>(dp->texels);
+    if (dp->texels) {
+        DevTexture t;
+        LGB_CUDA_TRY(s->ctx, cudaMemcpy(&t, s->d_textures + dp->texture_id, sizeof(t), cudaMemcpyDeviceToHost));
+        A.tex_w = t.width; A.tex_h = t.height;
+    }
+    A.rough = dp->roughness;
+    A.emis = dp->emission;
+    return LGB_OK;
+}
+
+int diff_grid(Ctx* ctx, uint32_t n) {
+    const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    return (int)std::min<uint32_t>((n + kDiffThreads - 1) / kDiffThreads, (uint32_t)sms * 16u);
+}
+
+}  // namespace
+
+extern "C" LGB_API lgb_status lgb_diff_render(lgb_scene* s, const lgb_camera* cam, const lgb_path_params* p,
+                                              const lgb_diff_params* dp, uint32_t frame0, uint32_t spp, float* d_film,
+                                              float* d_samples, void* stream) {
+    if (!s) return LGB_ERR_INVALID_ARGUMENT;
+    if (!d_film || (reinterpret_cast<uintptr_t>(d_film) & 15u) || (reinterpret_cast<uintptr_t>(d_samples) & 15u))
+        return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "film and samples must be 16-byte aligned device pointers");
+    cudaSetDevice(s->ctx->device);
+    DiffArgs A;
+    lgb_status st = make_diff_args(s, cam, p, dp, frame0, spp, A);
+    if (st != LGB_OK) return st;
+    if (d_samples) {
+        A.samples = reinterpret_cast<float4*>(d_samples);
+    } else {
+        const size_t bytes = sizeof(float4) * (size_t)A.npix * spp;
+        if (s->diff_buf_bytes < bytes) {
+            cudaFree(s->diff_buf);
+            s->diff_buf = nullptr;
+            s->diff_buf_bytes = 0;
+            LGB_CUDA_TRY(s->ctx, cudaMalloc(&s->diff_buf, bytes));
+            s->diff_buf_bytes = bytes;
+        }
+        A.samples = reinterpret_cast<float4*>(s->diff_buf);
+    }
+    const cudaStream_t cs = (cudaStream_t)stream;
+    launch_diff<kPrimal>(s, A, diff_grid(s->ctx, A.npix * spp), cs);
+    k_mean<<<diff_grid(s->ctx, A.npix), kDiffThreads, 0, cs>>>(A.samples, A.npix, spp, reinterpret_cast<float4*>(d_film));
+    LGB_CUDA_TRY(s->ctx, cudaGetLastError());
+    return LGB_OK;
+}
+
+extern "C" LGB_API lgb_status lgb_adjoint_path(lgb_scene* s, const lgb_camera* cam, const lgb_path_params* p,
+                                               const lgb_diff_params* dp, uint32_t frame0, uint32_t spp,
+                                               const float* d_dloss_dimage, const float* d_primal_samples,
+                                               lgb_diff_grads* grads, void* stream) {
+    if (!s) return LGB_ERR_INVALID_ARGUMENT;
+    if (!d_dloss_dimage || !grads || (reinterpret_cast<uintptr_t>(d_dloss_dimage) & 15u) ||
+        (reinterpret_cast<uintptr_t>(d_primal_samples) & 15u))
+        return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "null or misaligned d_dloss_dimage / samples / grads");
+    if ((dp && dp->texels && !grads->texels) || (dp && dp->roughness && !grads->roughness) ||
+        (dp && dp->emission && !grads->emission))
+        return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "a gradient buffer is missing for a parameter set");
+    if ((reinterpret_cast<uintptr_t>(grads->texels) & 15u) || (reinterpret_cast<uintptr_t>(grads->roughness) & 3u) ||
+        (reinterpret_cast<uintptr_t>(grads->emission) & 3u))
+        return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "misaligned gradient buffer");
+    cudaSetDevice(s->ctx->device);
+    DiffArgs A;
+    lgb_status st = make_diff_args(s, cam, p, dp, frame0, spp, A);
+    if (st != LGB_OK) return st;
+    A.dimage = reinterpret_cast<const float4*>(d_dloss_dimage);
+    A.primal = reinterpret_cast<const float4*>(d_primal_samples);
+    A.g_tex = reinterpret_cast<float4*>(grads->texels);
+    A.g_rough = grads->roughness;
+    A.g_emis = grads->emission;
+    const cudaStream_t cs = (cudaStream_t)stream;
+    const int grid = diff_grid(s->ctx, A.npix * spp);
+    if (A.primal) launch_diff<kReplayTotal>(s, A, grid, cs);
+    else launch_diff<kReplaySuffix>(s, A, grid, cs);
+    LGB_CUDA_TRY(s->ctx, cudaGetLastError());
+    return LGB_OK;
+}

@@ -385,6 +385,11 @@ __device__ __forceinline__ v3 eval_principled(const Mat& m, v3 wo, v3 wi, float&
 }
 
 // ---- bsdf_commons.glsl dispatch (radiance transport, mode 1) ----
+// MASK (LGB_BSDF_* bits) limits the lobes compiled into a caller; a type outside it evaluates to zero, so a
+// kernel instantiated for a scene's own type set gives the same results with fewer registers.
+constexpr uint32_t kAllBsdfs = 0x3Fu;
+
+template <uint32_t MASK = kAllBsdfs>
 __device__ __forceinline__ v3 sample_bsdf(v3 n_s, v3 wo, const Mat& m, bool ff, v3& wi, float& pdf, float& cos_t, v3 r) {
     v3 f = V3(0.0f);
     pdf = 0.0f; cos_t = 0.0f; wi = V3(0.0f);
@@ -392,31 +397,53 @@ __device__ __forceinline__ v3 sample_bsdf(v3 n_s, v3 wo, const Mat& m, bool ff, 
     branchless_onb(n_s, T, B);
     wo = to_local(wo, T, B, n_s);
     const v2 xy = V2(r.x, r.y);
-    switch (m.type) {
-        case LGB_BSDF_DIFFUSE: f = sample_diffuse(m, wo, wi, pdf, cos_t, xy); break;
-        case LGB_BSDF_MIRROR: f = sample_mirror(wo, wi, pdf, cos_t); break;
-        case LGB_BSDF_GLASS: f = sample_glass(m, wo, wi, pdf, cos_t, 1u, ff); break;
-        case LGB_BSDF_DIELECTRIC: f = sample_dielectric(m, wo, wi, 1u, ff, pdf, cos_t, xy); break;
-        case LGB_BSDF_CONDUCTOR: f = sample_conductor(m, wo, wi, pdf, cos_t, xy); break;
-        case LGB_BSDF_PRINCIPLED: f = sample_principled(m, wo, wi, 1u, ff, pdf, cos_t, r); break;
+    switch (m.type & MASK) {
+        case LGB_BSDF_DIFFUSE:
+            if constexpr ((MASK & LGB_BSDF_DIFFUSE) != 0) f = sample_diffuse(m, wo, wi, pdf, cos_t, xy);
+            break;
+        case LGB_BSDF_MIRROR:
+            if constexpr ((MASK & LGB_BSDF_MIRROR) != 0) f = sample_mirror(wo, wi, pdf, cos_t);
+            break;
+        case LGB_BSDF_GLASS:
+            if constexpr ((MASK & LGB_BSDF_GLASS) != 0) f = sample_glass(m, wo, wi, pdf, cos_t, 1u, ff);
+            break;
+        case LGB_BSDF_DIELECTRIC:
+            if constexpr ((MASK & LGB_BSDF_DIELECTRIC) != 0) f = sample_dielectric(m, wo, wi, 1u, ff, pdf, cos_t, xy);
+            break;
+        case LGB_BSDF_CONDUCTOR:
+            if constexpr ((MASK & LGB_BSDF_CONDUCTOR) != 0) f = sample_conductor(m, wo, wi, pdf, cos_t, xy);
+            break;
+        case LGB_BSDF_PRINCIPLED:
+            if constexpr ((MASK & LGB_BSDF_PRINCIPLED) != 0) f = sample_principled(m, wo, wi, 1u, ff, pdf, cos_t, r);
+            break;
         default: break;
     }
     wi = to_world(wi, T, B, n_s);
     return f;
 }
+template <uint32_t MASK = kAllBsdfs>
 __device__ __forceinline__ v3 eval_bsdf(v3 n_s, v3 wo, const Mat& m, bool ff, v3 wi, float& pdf) {
     pdf = 0.0f;
     v3 T, B;
     branchless_onb(n_s, T, B);
     wo = to_local(wo, T, B, n_s);
     wi = to_local(wi, T, B, n_s);
-    switch (m.type) {
-        case LGB_BSDF_DIFFUSE: return eval_diffuse(m, wo, wi, pdf);
-        case LGB_BSDF_DIELECTRIC: return eval_dielectric(m, wo, wi, pdf, ff);
-        case LGB_BSDF_CONDUCTOR: return eval_conductor(m, wo, wi, pdf);
-        case LGB_BSDF_PRINCIPLED: return eval_principled(m, wo, wi, pdf, ff);
-        default: return V3(0.0f);
+    switch (m.type & MASK) {
+        case LGB_BSDF_DIFFUSE:
+            if constexpr ((MASK & LGB_BSDF_DIFFUSE) != 0) return eval_diffuse(m, wo, wi, pdf);
+            break;
+        case LGB_BSDF_DIELECTRIC:
+            if constexpr ((MASK & LGB_BSDF_DIELECTRIC) != 0) return eval_dielectric(m, wo, wi, pdf, ff);
+            break;
+        case LGB_BSDF_CONDUCTOR:
+            if constexpr ((MASK & LGB_BSDF_CONDUCTOR) != 0) return eval_conductor(m, wo, wi, pdf);
+            break;
+        case LGB_BSDF_PRINCIPLED:
+            if constexpr ((MASK & LGB_BSDF_PRINCIPLED) != 0) return eval_principled(m, wo, wi, pdf, ff);
+            break;
+        default: break;
     }
+    return V3(0.0f);
 }
 
 }  // namespace sh

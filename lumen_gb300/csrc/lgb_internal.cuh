@@ -100,6 +100,7 @@ struct Scene {
     DevTexture* d_textures = nullptr;
     std::vector<void*> texture_buffers;
     uint32_t num_meshes = 0, num_materials = 0, num_lights = 0, num_textures = 0;
+    uint32_t bsdf_mask = 0;  // union of the materials' LGB_BSDF_* types
     std::vector<uint32_t> h_mesh_first_tri;
     std::vector<lgb_mesh> h_meshes;
     BvhDevice bvh;
@@ -111,6 +112,8 @@ struct Scene {
     void* pt_graph = nullptr;        // cudaGraphExec_t of the captured bounce loop
     uint64_t pt_graph_key[6] = {};   // what the captured graph depends on
     void* capture_stream = nullptr;  // private stream used only to record graphs
+    void* diff_buf = nullptr;        // per-sample radiance of the differentiable renderer
+    size_t diff_buf_bytes = 0;
 };
 
 // Error helpers: record a message on the context and return a status.

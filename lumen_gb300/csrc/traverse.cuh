@@ -341,4 +341,95 @@ __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ no
     }
 }
 
+// Single-ray queries for kernels that trace one ray per thread inside a larger loop (path-per-thread
+// megakernels). Same node and triangle tests and the same closest/any contract as trace_persistent.
+__device__ __forceinline__ uint32_t trace_closest_single(const WideNode* __restrict__ nodes, const WideTri* __restrict__ tris,
+                                                         const RayQ& r, float& t_best, float& u_best, float& v_best,
+                                                         uint32_t* status) {
+    uint2 stack[kStackSize];
+    int sp = 0;
+    uint32_t best = LGB_NO_HIT, visits = 0;
+    t_best = r.tmax;
+    u_best = v_best = 0.0f;
+    uint32_t g_base = 0u, g_hm = r.tmin <= r.tmax ? (((1u << (0u ^ r.oct)) << 8) | 1u) : 1u;
+    while (true) {
+        uint32_t hm = g_hm >> 8;
+        if (hm == 0u) {
+            if (sp == 0) break;
+            const uint2 g = stack[--sp];
+            g_base = g.x;
+            g_hm = g.y;
+            hm = g_hm >> 8;
+        }
+        const uint32_t imask = g_hm & 0xffu;
+        const int pos = 31 - __clz(hm);
+        hm &= ~(1u << pos);
+        const uint32_t slot = (uint32_t)pos ^ r.oct;
+        const uint32_t node_idx = g_base + __popc(imask & ((1u << slot) - 1u));
+        if (hm) {
+            if (sp >= kStackSize) { atomicOr(status, STATUS_STACK_OVERFLOW); break; }
+            stack[sp++] = make_uint2(g_base, (hm << 8) | imask);
+        } else {
+            g_hm = imask;  // this group is exhausted
+        }
+        if (++visits > kMaxVisits) { atomicOr(status, STATUS_VISIT_LIMIT); break; }
+        uint32_t nb, nimask, nhits, tri_base, tri_hits;
+        intersect_node(r, nodes + node_idx, t_best, nb, nimask, nhits, tri_base, tri_hits);
+        g_base = nb;
+        g_hm = (nhits << 8) | nimask;
+        while (tri_hits) {
+            const int k = __ffs(tri_hits) - 1;
+            tri_hits &= tri_hits - 1u;
+            const WideTri* tp = tris + tri_base + k;
+            const float4 a = ldg4f(&tp->a), b = ldg4f(&tp->b), c = ldg4f(&tp->c);
+            float t, u, v;
+            if (tri_intersect(r, a, b, c, t_best, t, u, v)) {
+                const uint32_t prim = __float_as_uint(a.w);
+                if (t < t_best || prim < best) { t_best = t; best = prim; u_best = u; v_best = v; }
+            }
+        }
+    }
+    return best;
+}
+
+__device__ __forceinline__ bool trace_any_single(const WideNode* __restrict__ nodes, const WideTri* __restrict__ tris,
+                                                 const RayQ& r, uint32_t* status) {
+    uint2 stack[kStackSize];
+    int sp = 0;
+    uint32_t visits = 0;
+    uint32_t g_base = 0u, g_hm = r.tmin <= r.tmax ? (((1u << (0u ^ r.oct)) << 8) | 1u) : 1u;
+    while (true) {
+        uint32_t hm = g_hm >> 8;
+        if (hm == 0u) {
+            if (sp == 0) return false;
+            const uint2 g = stack[--sp];
+            g_base = g.x;
+            g_hm = g.y;
+            hm = g_hm >> 8;
+        }
+        const uint32_t imask = g_hm & 0xffu;
+        const int pos = 31 - __clz(hm);
+        hm &= ~(1u << pos);
+        const uint32_t slot = (uint32_t)pos ^ r.oct;
+        const uint32_t node_idx = g_base + __popc(imask & ((1u << slot) - 1u));
+        if (hm) {
+            if (sp >= kStackSize) { atomicOr(status, STATUS_STACK_OVERFLOW); return false; }
+            stack[sp++] = make_uint2(g_base, (hm << 8) | imask);
+        }
+        if (++visits > kMaxVisits) { atomicOr(status, STATUS_VISIT_LIMIT); return false; }
+        uint32_t nb, nimask, nhits, tri_base, tri_hits;
+        intersect_node(r, nodes + node_idx, r.tmax, nb, nimask, nhits, tri_base, tri_hits);
+        g_base = nb;
+        g_hm = (nhits << 8) | nimask;
+        while (tri_hits) {
+            const int k = __ffs(tri_hits) - 1;
+            tri_hits &= tri_hits - 1u;
+            const WideTri* tp = tris + tri_base + k;
+            const float4 a = ldg4f(&tp->a), b = ldg4f(&tp->b), c = ldg4f(&tp->c);
+            float t, u, v;
+            if (tri_intersect(r, a, b, c, r.tmax, t, u, v)) return true;
+        }
+    }
+}
+
 }  // namespace lgb

@@ -6,6 +6,8 @@ fixes the arrays; tests that need bit-identical inputs on every host read them f
   cornell_box()        36 triangles: 5 walls (white 0.73 / red / green), two boxes rotated +-18 deg about y,
                        a 0.5 x 0.5 emitter (L = 17) just below the ceiling; camera on the +z axis
                        viewing the box along -z.
+  cornell_diff()       the same box with a textured back wall and two GGX conductor boxes (differentiable
+                       rendering).
   traversal_scene()    icosphere of frequency 200 (800 000 triangles) displaced by 3-octave value noise of
                        amplitude 0.1, plus 200 000 random small triangles in [-2, 2]^3.
   primary_rays()       one ray per pixel centre of a pinhole camera.
@@ -18,7 +20,7 @@ import math
 import numpy as np
 
 from . import abi
-from .scene import MESH_DTYPE, LIGHT_DTYPE, SceneArrays, diffuse
+from .scene import MESH_DTYPE, LIGHT_DTYPE, SceneArrays, conductor, diffuse
 
 WHITE = (0.73, 0.73, 0.73)
 RED = (0.63, 0.065, 0.05)
@@ -146,6 +148,54 @@ def cornell_box() -> SceneArrays:
     # Lumen's camera "dir" is the look-at direction of a left-handed view combined with a right-handed
     # projection (Camera.h:74,111-115), so the rendered view looks along -dir: here towards -z.
     return b.arrays(mats, lights, 2, (0.0, 0.0, 3.5), (0.0, 0.0, 1.0), 45.0)
+
+
+def albedo_texture(seed: int, size: int = 64) -> np.ndarray:
+    """(size, size, 4) float32 RGBA texture with RGB uniform in [0.1, 0.9] from PCG64(seed), alpha 1."""
+    rng = np.random.default_rng(seed)
+    tex = np.ones((size, size, 4), np.float32)
+    tex[..., :3] = rng.uniform(0.1, 0.9, (size, size, 3))
+    return tex
+
+
+def cornell_diff(texture_seed: int = 5, roughness=(0.35, 0.2)) -> SceneArrays:
+    """The Cornell box of the differentiable-rendering configuration: the back wall has its own white material
+    (albedo 1) modulated by a 64 x 64 RGB texture (albedo_texture(texture_seed)), mapped once over the wall
+    (u along +x, v along +y); the short and tall boxes are GGX conductors (reflectance 0.9, 0.6, 0.3 and
+    0.8, 0.8, 0.8) with one roughness per box. Materials: 0 white, 1 red, 2 green, 3 emitter, 4 back wall,
+    5 short box, 6 tall box."""
+    b = _Builder()
+    mats = [diffuse(WHITE), diffuse(RED), diffuse(GREEN), diffuse((1.0, 1.0, 1.0), emissive=(17.0, 17.0, 17.0)),
+            diffuse((1.0, 1.0, 1.0)), conductor((0.9, 0.6, 0.3), roughness[0]), conductor((0.8, 0.8, 0.8), roughness[1])]
+    mats[4]["texture_id"] = 0
+    W, R, G, E, BACK, SHORT, TALL = range(7)
+    t, n = _quad((-1, -1, -1), (1, -1, -1), (1, -1, 1), (-1, -1, 1), inward=(0, 1, 0))
+    b.add(t, n, W)
+    t, n = _quad((-1, 1, -1), (1, 1, -1), (1, 1, 1), (-1, 1, 1), inward=(0, -1, 0))
+    b.add(t, n, W)
+    t, n = _quad((-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1), inward=(0, 0, 1))
+    uv = (t[..., :2] + 1.0) * 0.5  # back wall at z = -1: (x, y) in [-1, 1]^2 -> [0, 1]^2
+    b.add(t, n, BACK, uv)
+    t, n = _quad((-1, -1, -1), (-1, -1, 1), (-1, 1, 1), (-1, 1, -1), inward=(1, 0, 0))
+    b.add(t, n, R)
+    t, n = _quad((1, -1, -1), (1, -1, 1), (1, 1, 1), (1, 1, -1), inward=(-1, 0, 0))
+    b.add(t, n, G)
+    t, n = _box((0.35, -0.7, -0.25), (0.6, 0.6, 0.6), -18.0)
+    b.add(t, n, SHORT)
+    t, n = _box((-0.33, -0.4, -0.45), (0.6, 1.2, 0.6), 18.0)
+    b.add(t, n, TALL)
+    y = 0.999
+    t, n = _quad((-0.25, y, -0.25), (0.25, y, -0.25), (0.25, y, 0.25), (-0.25, y, 0.25), inward=(0, -1, 0))
+    light_mesh = b.add(t, n, E)
+    lights = np.zeros(1, LIGHT_DTYPE)
+    lights["world_matrix"] = np.eye(4, dtype=np.float32).reshape(16)
+    lights["prim_mesh_idx"] = light_mesh
+    lights["num_triangles"] = 2
+    lights["L"] = 17.0
+    lights["light_flags"] = abi.LIGHT_AREA | abi.LIGHT_FINITE
+    arrays = b.arrays(mats, lights, 2, (0.0, 0.0, 3.5), (0.0, 0.0, 1.0), 45.0)
+    arrays.textures = [albedo_texture(texture_seed)]
+    return arrays
 
 
 # ---------------------------------------------------------------------------------------------------

@@ -243,6 +243,45 @@ class GpuScene:
     def sync(self, stream=None):
         _check(self.lib, self.ctx.handle, self.lib.lgb_sync(self.handle, C.c_void_p(stream)))
 
+    @staticmethod
+    def _diff_params(texture_id, texels, roughness, emission, flags=0) -> abi.DiffParams:
+        dp = abi.DiffParams()
+        dp.texture_id = texture_id
+        dp.flags = flags
+        dp.texels = texels.data_ptr() if texels is not None else None
+        dp.roughness = roughness.data_ptr() if roughness is not None else None
+        dp.emission = emission.data_ptr() if emission is not None else None
+        return dp
+
+    def diff_render(self, cam: abi.Camera, params: abi.PathParams, frame0: int, spp: int, film, texture_id=-1,
+                    texels=None, roughness=None, emission=None, samples=None, flags=0, stream=None):
+        """lgb_diff_render: mean image of the differentiable estimator into film ((npix, 4) float32 CUDA).
+        texels (H, W, 4), roughness (num_materials,) and emission (num_materials, 3) are float32 CUDA tensors
+        or None (scene values); samples ((spp * npix, 4) float32 CUDA) optionally receives every sample;
+        flags = abi.DIFF_SAMPLE_PARAMS samples with the parameter values."""
+        dp = self._diff_params(texture_id, texels, roughness, emission, flags)
+        sp = C.c_void_p(samples.data_ptr()) if samples is not None else None
+        _check(self.lib, self.ctx.handle,
+               self.lib.lgb_diff_render(self.handle, C.byref(cam), C.byref(params), C.byref(dp), frame0, spp,
+                                        C.c_void_p(film.data_ptr()), sp, C.c_void_p(stream)))
+
+    def adjoint_path(self, cam: abi.Camera, params: abi.PathParams, frame0: int, spp: int, dimage, texture_id=-1,
+                     texels=None, roughness=None, emission=None, g_texels=None, g_roughness=None, g_emission=None,
+                     samples=None, flags=0, stream=None):
+        """lgb_adjoint_path: adds d loss / d parameter into the g_* tensors given dimage = d loss / d image
+        ((npix, 4) float32 CUDA) for the image diff_render makes with the same arguments; samples are the
+        per-sample radiance diff_render wrote (one replay) or None (primal and replay)."""
+        dp = self._diff_params(texture_id, texels, roughness, emission, flags)
+        g = abi.DiffGrads()
+        g.texels = g_texels.data_ptr() if g_texels is not None else None
+        g.roughness = g_roughness.data_ptr() if g_roughness is not None else None
+        g.emission = g_emission.data_ptr() if g_emission is not None else None
+        _check(self.lib, self.ctx.handle,
+               self.lib.lgb_adjoint_path(self.handle, C.byref(cam), C.byref(params), C.byref(dp), frame0, spp,
+                                         C.c_void_p(dimage.data_ptr()),
+                                         C.c_void_p(samples.data_ptr()) if samples is not None else None,
+                                         C.byref(g), C.c_void_p(stream)))
+
     def close(self):
         if getattr(self, "handle", None):
             self.lib.lgb_scene_destroy(self.handle)

@@ -124,6 +124,11 @@ void orc_render_samples(void* scene, const float inv_view[16], const float inv_p
 void orc_render_film(void* scene, const float inv_view[16], const float inv_proj[16],
                      const orc_path_params* params, uint32_t frame0, uint32_t spp, float* film, int fp64,
                      int nthreads);
+// Mean image of the detached differentiable estimator (sampling from the scene's materials, values from
+// the parameter arrays; see path.cpp). Used for finite-difference checks of the adjoint kernels.
+void orc_render_diff(void* scene, const float inv_view[16], const float inv_proj[16], const orc_path_params* params,
+                     int tex_id, const float* texels, const float* rough, const float* emis, uint32_t frame0,
+                     uint32_t spp, double* film_rgb, int fp64, int nthreads);
 // PCG4D (utils.glsl:121-133) applied to n state vectors; for known-answer tests.
 void orc_pcg4d(const uint32_t* in, uint32_t* out, uint32_t n);
 // offset_ray (utils.glsl:73-84) applied to n (p, n) pairs.

@@ -78,6 +78,9 @@ class Oracle:
                                          C.POINTER(C.c_uint8), C.c_int, C.c_int]
         L.orc_render_film.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(_Params),
                                       C.c_uint32, C.c_uint32, C.POINTER(C.c_float), C.c_int, C.c_int]
+        L.orc_render_diff.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(_Params),
+                                      C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                      C.POINTER(C.c_double), C.c_int, C.c_int]
         L.orc_pcg4d.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint32]
         L.orc_offset_ray.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32]
 
@@ -231,3 +234,26 @@ class OracleScene:
         self.ora.lib.orc_render_film(self.h, _p(iv), _p(ip), C.byref(p), frame0, spp, _p(film), int(fp64),
                                      threads or (os.cpu_count() or 1))
         return film
+
+    def diff(self, cam, max_depth, width, height, frame0, spp, tex_id=-1, texels=None, rough=None, emis=None,
+             fp64=True, threads=0):
+        """Mean image (npix, 3) float64 of the detached differentiable estimator over frames [frame0, frame0+spp).
+        texels (H, W, 4) replace texture tex_id, rough (per material) and emis (per material, RGB) replace the
+        scene values in every BSDF value and emission, while sampling keeps the scene's materials."""
+        iv = np.ascontiguousarray(np.array(cam.inv_view[:], np.float32))
+        ip = np.ascontiguousarray(np.array(cam.inv_projection[:], np.float32))
+        out = np.zeros((width * height, 3), np.float64)
+        keep = []
+
+        def ptr(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, np.float32)
+            keep.append(a)
+            return a.ctypes.data
+
+        p = self._params(max_depth, width, height, frame0)
+        self.ora.lib.orc_render_diff(self.h, _p(iv), _p(ip), C.byref(p), int(tex_id), ptr(texels), ptr(rough),
+                                     ptr(emis), frame0, spp, _p(out, C.c_double), int(fp64),
+                                     threads or (os.cpu_count() or 1))
+        return out

@@ -185,3 +185,53 @@ def test_camera_center_ray_looks_along_minus_dir(oracle):
     d = IV @ np.array([*(t[:3] / np.linalg.norm(t[:3])), 0.0])
     np.testing.assert_allclose(d[:3], [0, 0, -1], atol=1e-6)
     np.testing.assert_allclose((IV @ np.array([0, 0, 0, 1.0]))[:3], cb.camera_pos, atol=1e-6)
+
+
+def test_diff_estimator_equals_path_at_scene_values(oracle):
+    """With the parameters equal to the scene's values the detached estimator is the path estimator."""
+    a = procedural.cornell_diff()
+    sc = oracle.scene(a)
+    cam = _camera(oracle, a, 32, 32)
+    film = sc.film(cam, 6, 32, 32, 0, 4)
+    em = np.zeros((len(a.materials), 3), np.float32)
+    em[3] = 17.0
+    d = sc.diff(cam, 6, 32, 32, 0, 4, tex_id=0, texels=a.textures[0], rough=a.materials["roughness"], emis=em,
+                fp64=False)
+    # the film is Lumen's running FP32 mean, the diff image a double mean of the same FP32 samples
+    np.testing.assert_allclose(d, film[:, :3], rtol=1e-3, atol=1e-6)
+    assert np.array_equal(d, sc.diff(cam, 6, 32, 32, 0, 4, fp64=False))
+
+
+def test_diff_estimator_is_linear_in_emission_and_smooth_in_parameters(oracle):
+    """FP64, common random numbers: the image is exactly linear in the emission, and central differences of a
+    texel and of a roughness are stable under halving h (no path changes with the parameters)."""
+    a = procedural.cornell_diff()
+    sc = oracle.scene(a)
+    w = h = 24
+    cam = _camera(oracle, a, w, h)
+    em = np.zeros((len(a.materials), 3), np.float32)
+    em[3] = 17.0
+    base = sc.diff(cam, 6, w, h, 0, 2, emis=em)
+    np.testing.assert_allclose(sc.diff(cam, 6, w, h, 0, 2, emis=2 * em), 2 * base, rtol=1e-13, atol=0)
+    wts = np.random.default_rng(1).uniform(-1, 1, base.shape)
+
+    def fd(make, step):
+        return ((sc.diff(cam, 6, w, h, 0, 2, **make(step)) - sc.diff(cam, 6, w, h, 0, 2, **make(-step))) * wts).sum()
+
+    tex = a.textures[0]
+
+    def texel(step):
+        t = tex.copy()
+        t[:, :, :3] += np.float32(step)  # every texel at once: a directional derivative
+        return {"tex_id": 0, "texels": t}
+
+    def rough(step):
+        r = a.materials["roughness"].copy()
+        r[6] += np.float32(step)
+        return {"rough": r}
+
+    for make in (texel, rough):
+        g1 = fd(make, 1e-3) / 2e-3
+        g2 = fd(make, 5e-4) / 1e-3
+        assert abs(g1) > 1e-3
+        np.testing.assert_allclose(g1, g2, rtol=2e-3)

@@ -267,6 +267,46 @@ LGB_API lgb_status lgb_adjoint_path(lgb_scene* scene, const lgb_camera* camera, 
 /* Waits for `stream` and reports any fault a kernel recorded in the scene's device status word. */
 LGB_API lgb_status lgb_sync(lgb_scene* scene, void* stream);
 
+/* ---- batched rendering (no counterpart in Lumen) ----
+ * Many scenes and camera views of uneven size rendered by one wavefront: the paths of every job share the
+ * queues, the traversal and shading launches and one captured bounce loop, instead of each image issuing its
+ * own sequence. Every path is seeded and computed exactly as lgb_render_path computes it, so each job's film
+ * is the one lgb_render_path would produce. */
+typedef struct lgb_batch lgb_batch;
+
+typedef struct lgb_batch_job {
+    uint32_t scene;          /* index into the scene list given to lgb_batch_create */
+    uint32_t frame0;         /* first frame (progressive film, as lgb_render_path) */
+    uint32_t spp;            /* frames to add; 0 = nothing for this job */
+    uint32_t reserved;
+    lgb_camera camera;
+    lgb_path_params params;
+    float* d_film;           /* RGBA32F, width * height, 16-byte aligned; the films of one call must not overlap */
+} lgb_batch_job;
+
+typedef struct lgb_batch_opts {
+    uint32_t path_capacity;        /* paths in flight per chunk (the queue size); 0 = 2^21 */
+    uint32_t work_blocks_per_sm;   /* grid of the camera, shading and film kernels; 0 = 8 */
+    uint32_t trace_blocks_per_sm;  /* grid of the persistent traversal kernels; 0 = as many as fit */
+    uint32_t reserved[5];
+} lgb_batch_opts;
+
+/* Copies the BVHs of `scenes` (each built with lgb_bvh_build) into one forest. The scenes must outlive the
+ * batch; rebuilding a scene's BVH afterwards makes lgb_batch_render refuse the batch (LGB_ERR_NOT_READY). */
+LGB_API lgb_status lgb_batch_create(lgb_ctx* ctx, lgb_scene* const* scenes, uint32_t num_scenes, lgb_batch** out);
+LGB_API void lgb_batch_destroy(lgb_batch* batch);
+/* Renders up to 128 jobs. opts null = the options lgb_batch_tune chose, else the defaults. Jobs are cut into
+ * chunks of whole frames; a chunk holds frames of several jobs. */
+LGB_API lgb_status lgb_batch_render(lgb_batch* batch, const lgb_batch_job* jobs, uint32_t num_jobs,
+                                    const lgb_batch_opts* opts, void* stream);
+/* Autotuner: times lgb_batch_render over candidate queue sizes and grids on a reduced copy of `jobs` (a
+ * quarter of each job's frames, films untouched), keeps the fastest for later renders and writes it to *best.
+ * Waits for `stream`. */
+LGB_API lgb_status lgb_batch_tune(lgb_batch* batch, const lgb_batch_job* jobs, uint32_t num_jobs,
+                                  lgb_batch_opts* best, void* stream);
+/* Waits for `stream` and reports faults recorded by the batch's traversal or by any of its scenes. */
+LGB_API lgb_status lgb_batch_sync(lgb_batch* batch, void* stream);
+
 /* Film error (src/shaders/rmse/*.comp, RayTracer.cpp:215-241): RMSE of d_film against d_reference, both RGBA32F
  * with npix pixels; alpha is ignored. mode 0 = sqrt(sum of squared RGB errors / (3 npix)); mode 1 = the value
  * Lumen reports (per 1024-pixel group the minimum of its warps' sums, calc_rmse.comp:37, then

@@ -111,6 +111,16 @@ class DiffGrads(C.Structure):
     _fields_ = [("texels", C.c_void_p), ("roughness", C.c_void_p), ("emission", C.c_void_p)]
 
 
+class BatchJob(C.Structure):
+    _fields_ = [("scene", C.c_uint32), ("frame0", C.c_uint32), ("spp", C.c_uint32), ("reserved", C.c_uint32),
+                ("camera", Camera), ("params", PathParams), ("d_film", C.c_void_p)]
+
+
+class BatchOpts(C.Structure):
+    _fields_ = [("path_capacity", C.c_uint32), ("work_blocks_per_sm", C.c_uint32),
+                ("trace_blocks_per_sm", C.c_uint32), ("reserved", C.c_uint32 * 5)]
+
+
 # Every exported symbol with its argument and result types (the declarations of include/lgb.h).
 SIGNATURES = {
     "lgb_abi_version": ([], C.c_uint32),
@@ -134,6 +144,11 @@ SIGNATURES = {
     "lgb_adjoint_path": ([C.c_void_p, C.POINTER(Camera), C.POINTER(PathParams), C.POINTER(DiffParams), C.c_uint32,
                           C.c_uint32, C.c_void_p, C.c_void_p, C.POINTER(DiffGrads), C.c_void_p], C.c_int32),
     "lgb_sync": ([C.c_void_p, C.c_void_p], C.c_int32),
+    "lgb_batch_create": ([C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, C.POINTER(C.c_void_p)], C.c_int32),
+    "lgb_batch_destroy": ([C.c_void_p], None),
+    "lgb_batch_render": ([C.c_void_p, C.POINTER(BatchJob), C.c_uint32, C.POINTER(BatchOpts), C.c_void_p], C.c_int32),
+    "lgb_batch_tune": ([C.c_void_p, C.POINTER(BatchJob), C.c_uint32, C.POINTER(BatchOpts), C.c_void_p], C.c_int32),
+    "lgb_batch_sync": ([C.c_void_p, C.c_void_p], C.c_int32),
     "lgb_film_rmse": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_double), C.c_void_p],
                       C.c_int32),
     "lgb_measure_l2_read_gbs": ([C.c_int, C.c_uint64, C.c_uint32, C.POINTER(C.c_double)], C.c_int32),

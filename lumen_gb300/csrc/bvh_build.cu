@@ -761,6 +761,7 @@ lgb_status build_bvh(Scene* s, const lgb_build_opts* opts, lgb_build_stats* stat
         s->bvh.num_nodes = hc[0];
         s->bvh.num_tris = n;
         s->bvh.max_depth = depth;
+        s->bvh.generation++;
         if (stats) {
             std::memset(stats, 0, sizeof(*stats));
             stats->build_ms = ms;

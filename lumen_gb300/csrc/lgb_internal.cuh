@@ -82,6 +82,7 @@ struct BvhDevice {
     uint32_t num_nodes = 0;
     uint32_t num_tris = 0;
     uint32_t max_depth = 0;
+    uint32_t generation = 0;  // incremented by every build
 };
 
 struct Scene {
@@ -116,6 +117,28 @@ struct Scene {
     size_t diff_buf_bytes = 0;
 };
 
+// Several scenes rendered as one wavefront: their BVHs copied into one forest (node and triangle indices
+// relocated, each scene rooted at its first node), plus the batch's own work arena and captured graph.
+struct Batch {
+    Ctx* ctx = nullptr;
+    std::vector<Scene*> scenes;
+    std::vector<uint32_t> roots;            // root node of every scene in the forest
+    std::vector<uint32_t> bvh_generation;   // each scene's BVH build at creation, to detect a rebuild
+    WideNode* nodes = nullptr;
+    WideTri* tris = nullptr;
+    uint32_t num_nodes = 0, num_tris = 0;
+    uint32_t* d_status = nullptr;
+    void* buf = nullptr;
+    size_t buf_bytes = 0;
+    void* graph = nullptr;
+    uint64_t graph_key[6] = {};
+    void* capture_stream = nullptr;
+    void* staging = nullptr;        // pinned host copy of the job table
+    void* staging_event = nullptr;  // recorded after the table's upload, before the staging is reused
+    bool tuned = false;
+    lgb_batch_opts tuned_opts{};
+};
+
 // Error helpers: record a message on the context and return a status.
 lgb_status set_error(Ctx* ctx, lgb_status st, const std::string& msg);
 lgb_status cuda_error(Ctx* ctx, cudaError_t e, const char* what);
@@ -138,4 +161,5 @@ lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* p
 
 // The opaque handles of include/lgb.h.
 struct lgb_ctx : public lgb::Ctx {};
+struct lgb_batch : public lgb::Batch {};
 struct lgb_scene : public lgb::Scene {};

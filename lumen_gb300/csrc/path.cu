@@ -60,6 +60,9 @@ struct Params {
     float4* film;      // RGBA32F output
 };
 
+struct JobRec;
+struct BatchChunk;
+
 struct Buffers {
     uint32_t* pix;      // pixel index
     uint32_t* frame;
@@ -80,7 +83,49 @@ struct Buffers {
     uint32_t* sbits;
     uint32_t* counters; // [0] cur, [1] next, [2] nee, [3..6] class counts, [8..10] trace work counters
     Params* params;     // per-chunk parameters in device memory, so that a captured graph can be replayed
+    uint32_t cap;       // path capacity of the arena
+    // batched rendering only (null otherwise)
+    uint32_t* job;       // job of each path
+    uint32_t* root;      // BVH root node of each ray of the current queue
+    uint32_t* root_next; // ... of the continuation rays being enqueued
+    uint32_t* nroot;     // ... of the shadow and BSDF-MIS rays
+    const JobRec* jobs;
+    const BatchChunk* chunk;
 };
+
+// Batched rendering: several scenes and cameras share one wavefront. Every job (a scene, a camera, path
+// parameters, a film and a frame range) has a record in device memory; a chunk of paths is a list of segments,
+// each holding whole frames of one job, so that the film of every job still receives its frames in order.
+constexpr uint32_t kMaxBatchJobs = 128;
+
+struct JobRec {
+    Params P;       // camera, image and path parameters, film (frame0, nframes and cap unused)
+    SceneView S;    // the job's scene arrays (traversal uses the batch's BVH forest instead)
+    uint32_t root;  // root node of the job's BVH in the forest
+    uint32_t pad[3];
+};
+
+struct Segment {
+    uint32_t job, frame0, nframes, path_off, pix_off, npix;
+};
+
+struct BatchChunk {
+    uint32_t nseg, npaths, npix_total, write_film;
+    Segment seg[kMaxBatchJobs];
+};
+
+// Segment holding element `i` of a prefix-offset field (path_off or pix_off): binary search, nseg <= 128.
+template <bool PIX>
+__device__ __forceinline__ uint32_t find_segment(const BatchChunk& C, uint32_t i) {
+    uint32_t lo = 0, hi = C.nseg - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        const uint32_t off = PIX ? C.seg[mid].pix_off : C.seg[mid].path_off;
+        if (off <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
 
 
 __device__ __forceinline__ int class_of(uint32_t bsdf_type) {
@@ -96,11 +141,21 @@ __device__ __forceinline__ int class_of(uint32_t bsdf_type) {
 // ---------------- kernels ----------------
 
 // path.rgen:22-46: the seed is (x, y, frame, 0); two draws jitter the pixel.
+template <bool BATCH>
 __global__ void __launch_bounds__(kThreads) k_camera(const Params* __restrict__ Pp, Buffers B) {
-    const Params& P = *Pp;
-    const uint32_t n = P.npix * P.nframes;
+    const uint32_t n = BATCH ? B.chunk->npaths : Pp->npix * Pp->nframes;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t pix = i % P.npix, f = P.frame0 + i / P.npix;
+        uint32_t local = i, frame0 = 0u, job = 0u;
+        if (BATCH) {
+            const Segment& sg = B.chunk->seg[find_segment<false>(*B.chunk, i)];
+            local = i - sg.path_off;
+            frame0 = sg.frame0;
+            job = sg.job;
+        } else {
+            frame0 = Pp->frame0;
+        }
+        const Params& P = BATCH ? B.jobs[job].P : *Pp;
+        const uint32_t pix = local % P.npix, f = frame0 + local / P.npix;
         const uint32_t x = pix % P.width, y = pix / P.width;
         uint4 seed = make_uint4(x, y, f, 0u);
         const float px = (float)x + 0.5f, py = (float)y + 0.5f;
@@ -119,26 +174,33 @@ __global__ void __launch_bounds__(kThreads) k_camera(const Params* __restrict__ 
         B.T[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
         B.col[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         B.q_cur[i] = i;
+        if (BATCH) {
+            B.job[i] = job;
+            B.root[i] = B.jobs[job].root;
+        }
         store_ray(&B.rays[i], make_ray(V3(origin.x, origin.y, origin.z), kTMin, V3(dir.x, dir.y, dir.z), kTMax));
     }
 }
 
-// Closest-hit / any-hit over a device-counted queue of rays, persistent with dynamic fetch.
+// Closest-hit / any-hit over a device-counted queue of rays, persistent with dynamic fetch; `roots` gives each
+// ray's BVH root in a batch forest (null: one BVH rooted at node 0).
 __global__ void __launch_bounds__(kThreads) k_q_trace_closest(SceneView S, const lgb_ray* __restrict__ rays,
                                                               lgb_hit* __restrict__ hits, const uint32_t* count_ptr,
-                                                              uint32_t* ray_counter) {
-    trace_persistent<false, false>(S.nodes, S.tris, rays, hits, nullptr, 0u, count_ptr, ray_counter, S.status, nullptr);
+                                                              uint32_t* ray_counter, const uint32_t* __restrict__ roots) {
+    trace_persistent<false, false>(S.nodes, S.tris, rays, hits, nullptr, 0u, count_ptr, ray_counter, S.status, nullptr,
+                                   roots);
 }
 __global__ void __launch_bounds__(kThreads) k_q_trace_any(SceneView S, const lgb_ray* __restrict__ rays,
                                                           uint32_t* __restrict__ bits, const uint32_t* count_ptr,
-                                                          uint32_t* ray_counter) {
-    trace_persistent<true, false>(S.nodes, S.tris, rays, nullptr, bits, 0u, count_ptr, ray_counter, S.status, nullptr);
+                                                          uint32_t* ray_counter, const uint32_t* __restrict__ roots) {
+    trace_persistent<true, false>(S.nodes, S.tris, rays, nullptr, bits, 0u, count_ptr, ray_counter, S.status, nullptr,
+                                  roots);
 }
 
 // path.rgen:49-55: a miss adds the sky colour (shade_atmosphere without a directional light returns
 // sky_col, commons.glsl:157-159) and ends the path; hits are binned by material class.
-__global__ void __launch_bounds__(kThreads) k_classify(SceneView S, const Params* __restrict__ Pp, Buffers B) {
-    const Params& P = *Pp;
+template <bool BATCH>
+__global__ void __launch_bounds__(kThreads) k_classify(SceneView S0, const Params* __restrict__ Pp, Buffers B) {
     const uint32_t n = B.counters[0];
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -146,8 +208,10 @@ __global__ void __launch_bounds__(kThreads) k_classify(SceneView S, const Params
         int cls = -1;
         if (i < n) {
             const uint32_t prim = B.hits[i].prim;
+            const uint32_t p = B.q_cur[i];
+            const uint32_t job = BATCH ? B.job[p] : 0u;
             if (prim == LGB_NO_HIT) {
-                const uint32_t p = B.q_cur[i];
+                const Params& P = BATCH ? B.jobs[job].P : *Pp;
                 const uint32_t depth = B.flags[p] & 0xffffu;
                 if (depth > 0 || P.direct_lighting == 1u) {
                     const float4 T = B.T[p];
@@ -158,13 +222,14 @@ __global__ void __launch_bounds__(kThreads) k_classify(SceneView S, const Params
                     B.col[p] = c;
                 }
             } else {
+                const SceneView S = BATCH ? B.jobs[job].S : S0;
                 cls = class_of(S.mats[S.meshes[S.tri_mesh[prim]].material_index].bsdf_type);
             }
         }
 #pragma unroll
         for (int c = 0; c < NUM_CLS; c++) {
             const uint32_t slot = agg_slot(&B.counters[3 + c], cls == c);
-            if (cls == c) B.q_cls[(size_t)c * P.cap + slot] = i;
+            if (cls == c) B.q_cls[(size_t)c * B.cap + slot] = i;
         }
     }
 }
@@ -194,21 +259,24 @@ __device__ __forceinline__ v3 cls_eval(v3 n_s, v3 wo, const Mat& m, bool ff, v3 
 }
 
 // One bounce of path.rgen:56-100 for the hits of one material class.
-template <int CLS>
-__global__ void __launch_bounds__(kThreads) k_shade(SceneView S, const Params* __restrict__ Pp, Buffers B, int depth) {
-    const Params& P = *Pp;
+template <int CLS, bool BATCH>
+__global__ void __launch_bounds__(kThreads) k_shade(SceneView S0, const Params* __restrict__ Pp, Buffers B, int depth) {
     const uint32_t n = B.counters[3 + CLS];
     const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t* list = B.q_cls + (size_t)CLS * P.cap;
+    const uint32_t* list = B.q_cls + (size_t)CLS * B.cap;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t k = base + threadIdx.x;
         bool cont = false, nee = false;
-        uint32_t p = 0;
+        uint32_t p = 0, root = 0;
         lgb_ray next_ray, sray, mray;
         NeeRec rec;
         if (k < n) {
             const uint32_t qi = list[k];
             p = B.q_cur[qi];
+            const uint32_t job = BATCH ? B.job[p] : 0u;
+            const Params& P = BATCH ? B.jobs[job].P : *Pp;
+            const SceneView S = BATCH ? B.jobs[job].S : S0;
+            if (BATCH) root = B.jobs[job].root;
             const lgb_hit hit = B.hits[qi];
             const lgb_ray ray = B.rays[qi];
             const uint32_t pix = B.pix[p], frame = B.frame[p];
@@ -350,12 +418,14 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneView S, const Params* _
         if (cont) {
             B.q_next[cslot] = p;
             store_ray(&B.rays_next[cslot], next_ray);
+            if (BATCH) B.root_next[cslot] = root;
         }
         const uint32_t nslot = agg_slot(&B.counters[2], nee);
         if (nee) {
             B.nee[nslot] = rec;
             store_ray(&B.srays[nslot], sray);
             store_ray(&B.mrays[nslot], mray);
+            if (BATCH) B.nroot[nslot] = root;
         }
     }
 }
@@ -364,11 +434,13 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneView S, const Params* _
 // sample (if it hit the sampled light triangle), then col += T * res / light_pick_pdf (path.rgen:78).
 // A missed MIS ray leaves the previous closest-hit payload in place (ray.rmiss:13 only marks the
 // material), so the comparison then uses the shading point's own triangle, position and normal.
-__global__ void __launch_bounds__(kThreads) k_nee_resolve(SceneView S, Buffers B) {
+template <bool BATCH>
+__global__ void __launch_bounds__(kThreads) k_nee_resolve(SceneView S0, Buffers B) {
     const uint32_t n = B.counters[2];
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         const NeeRec rec = B.nee[r];
         const uint32_t p = __float_as_uint(rec.Le.w);
+        const SceneView S = BATCH ? B.jobs[B.job[p]].S : S0;
         const bool occluded = (B.sbits[r >> 5] >> (r & 31)) & 1u;
         v3 res = V3(0.0f);
         if (!occluded && rec.term1.w > 0.0f) res = res + f3(rec.term1);
@@ -414,28 +486,42 @@ __global__ void k_rotate(uint32_t* counters) {
 }
 
 // path.rgen:102-112 applied to the chunk's frames in order.
-__global__ void __launch_bounds__(kThreads) k_film(const Params* __restrict__ Pp, Buffers B) {
-    const Params& P = *Pp;
-    float4* __restrict__ film = P.film;
-    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < P.npix; pix += gridDim.x * blockDim.x) {
-        float4 px = film[pix];
-        for (uint32_t k = 0; k < P.nframes; k++) {
-            const uint32_t f = P.frame0 + k;
-            const float4 c4 = B.col[(size_t)k * P.npix + pix];
-            const v3 col = f3(c4);
-            if (P.film_mode == 1u) {
-                px = make_float4(col.x, col.y, col.z, 1.0f);
-                continue;
-            }
-            if (isnan(luminance(col))) continue;
-            if (f > 0u) {
-                const float w = 1.0f / (float)(f + 1u);
-                px = make_float4(mixf(px.x, col.x, w), mixf(px.y, col.y, w), mixf(px.z, col.z, w), 1.0f);
-            } else {
-                px = make_float4(col.x, col.y, col.z, 1.0f);
-            }
+__device__ __forceinline__ void film_frames(const Params& P, const Buffers& B, float4* __restrict__ film, uint32_t pix,
+                                            uint32_t frame0, uint32_t nframes, uint32_t path_off) {
+    float4 px = film[pix];
+    for (uint32_t k = 0; k < nframes; k++) {
+        const uint32_t f = frame0 + k;
+        const float4 c4 = B.col[path_off + (size_t)k * P.npix + pix];
+        const v3 col = f3(c4);
+        if (P.film_mode == 1u) {
+            px = make_float4(col.x, col.y, col.z, 1.0f);
+            continue;
         }
-        film[pix] = px;
+        if (isnan(luminance(col))) continue;
+        if (f > 0u) {
+            const float w = 1.0f / (float)(f + 1u);
+            px = make_float4(mixf(px.x, col.x, w), mixf(px.y, col.y, w), mixf(px.z, col.z, w), 1.0f);
+        } else {
+            px = make_float4(col.x, col.y, col.z, 1.0f);
+        }
+    }
+    film[pix] = px;
+}
+
+template <bool BATCH>
+__global__ void __launch_bounds__(kThreads) k_film(const Params* __restrict__ Pp, Buffers B) {
+    if (BATCH) {
+        const BatchChunk& C = *B.chunk;
+        if (!C.write_film) return;
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < C.npix_total; i += gridDim.x * blockDim.x) {
+            const Segment& sg = C.seg[find_segment<true>(C, i)];
+            const Params& P = B.jobs[sg.job].P;
+            film_frames(P, B, P.film, i - sg.pix_off, sg.frame0, sg.nframes, sg.path_off);
+        }
+    } else {
+        const Params& P = *Pp;
+        for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < P.npix; pix += gridDim.x * blockDim.x)
+            film_frames(P, B, P.film, pix, P.frame0, P.nframes, 0u);
     }
 }
 
@@ -445,8 +531,10 @@ __global__ void k_clear_bits(uint32_t* bits, const uint32_t* count_ptr) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < words; i += gridDim.x * blockDim.x) bits[i] = 0u;
 }
 
-__global__ void k_init_counters(uint32_t* counters, const Params* __restrict__ Pp) {
-    if (threadIdx.x < 16) counters[threadIdx.x] = threadIdx.x == 0 ? Pp->npix * Pp->nframes : 0u;
+template <bool BATCH>
+__global__ void k_init_counters(Buffers B, const Params* __restrict__ Pp) {
+    if (threadIdx.x < 16)
+        B.counters[threadIdx.x] = threadIdx.x == 0 ? (BATCH ? B.chunk->npaths : Pp->npix * Pp->nframes) : 0u;
 }
 
 __global__ void k_set_params(Params P, Params* dst) {
@@ -455,8 +543,9 @@ __global__ void k_set_params(Params P, Params* dst) {
 
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
-// Carves the work arena for `cap` paths; returns the byte size when base is null.
-size_t carve(char* base, uint32_t cap, Buffers& B) {
+// Carves the work arena for `cap` paths (with the per-path job and per-ray root arrays when `batch`); returns
+// the byte size when base is null.
+size_t carve(char* base, uint32_t cap, Buffers& B, bool batch = false) {
     size_t off = 0;
     auto take = [&](size_t bytes) { char* p = base ? base + off : nullptr; off += align_up(bytes); return p; };
     B.pix = (uint32_t*)take(4ull * cap);
@@ -478,6 +567,18 @@ size_t carve(char* base, uint32_t cap, Buffers& B) {
     B.sbits = (uint32_t*)take(4ull * ((cap + 31) / 32));
     B.counters = (uint32_t*)take(64);
     B.params = (Params*)take(sizeof(Params));
+    B.cap = cap;
+    B.job = B.root = B.root_next = B.nroot = nullptr;
+    B.jobs = nullptr;
+    B.chunk = nullptr;
+    if (batch) {
+        B.job = (uint32_t*)take(4ull * cap);
+        B.root = (uint32_t*)take(4ull * cap);
+        B.root_next = (uint32_t*)take(4ull * cap);
+        B.nroot = (uint32_t*)take(4ull * cap);
+        B.jobs = (const JobRec*)take(sizeof(JobRec) * kMaxBatchJobs);
+        B.chunk = (const BatchChunk*)take(sizeof(BatchChunk));
+    }
     return off;
 }
 
@@ -492,27 +593,30 @@ Grids path_grids(Ctx* ctx) {
     return Grids{sms * 8, sms * std::max(trace_blocks, 1)};
 }
 
-// One chunk of frames: camera rays, `bounces` bounces, film. Every kernel reads B.params, so this
-// sequence can be captured once and replayed with new parameters.
+// One chunk of frames: camera rays, `bounces` bounces, film. Every kernel reads its parameters from device
+// memory (B.params, or the job table and chunk record when batched), so this sequence can be captured once and
+// replayed with new parameters.
+template <bool BATCH>
 cudaError_t launch_chunk(const SceneView& S, Buffers B, int bounces, Grids g, cudaStream_t st) {
-    k_init_counters<<<1, 32, 0, st>>>(B.counters, B.params);
-    k_camera<<<g.work, kThreads, 0, st>>>(B.params, B);
+    k_init_counters<BATCH><<<1, 32, 0, st>>>(B, B.params);
+    k_camera<BATCH><<<g.work, kThreads, 0, st>>>(B.params, B);
     for (int depth = 0; depth < bounces; depth++) {
-        k_q_trace_closest<<<g.trace, kThreads, 0, st>>>(S, B.rays, B.hits, B.counters + 0, B.counters + 8);
-        k_classify<<<g.work, kThreads, 0, st>>>(S, B.params, B);
-        k_shade<CLS_DIFFUSE><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
-        k_shade<CLS_CONDUCTOR><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
-        k_shade<CLS_SPECULAR><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
-        k_shade<CLS_PRINCIPLED><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        k_q_trace_closest<<<g.trace, kThreads, 0, st>>>(S, B.rays, B.hits, B.counters + 0, B.counters + 8, B.root);
+        k_classify<BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B);
+        k_shade<CLS_DIFFUSE, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        k_shade<CLS_CONDUCTOR, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        k_shade<CLS_SPECULAR, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        k_shade<CLS_PRINCIPLED, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
         k_clear_bits<<<g.work, kThreads, 0, st>>>(B.sbits, B.counters + 2);
-        k_q_trace_any<<<g.trace, kThreads, 0, st>>>(S, B.srays, B.sbits, B.counters + 2, B.counters + 9);
-        k_q_trace_closest<<<g.trace, kThreads, 0, st>>>(S, B.mrays, B.mhits, B.counters + 2, B.counters + 10);
-        k_nee_resolve<<<g.work, kThreads, 0, st>>>(S, B);
+        k_q_trace_any<<<g.trace, kThreads, 0, st>>>(S, B.srays, B.sbits, B.counters + 2, B.counters + 9, B.nroot);
+        k_q_trace_closest<<<g.trace, kThreads, 0, st>>>(S, B.mrays, B.mhits, B.counters + 2, B.counters + 10, B.nroot);
+        k_nee_resolve<BATCH><<<g.work, kThreads, 0, st>>>(S, B);
         k_rotate<<<1, 32, 0, st>>>(B.counters);
         std::swap(B.rays, B.rays_next);
         std::swap(B.q_cur, B.q_next);
+        std::swap(B.root, B.root_next);
     }
-    k_film<<<g.work, kThreads, 0, st>>>(B.params, B);
+    k_film<BATCH><<<g.work, kThreads, 0, st>>>(B.params, B);
     return cudaGetLastError();
 }
 
@@ -570,7 +674,7 @@ lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* p
         const cudaStream_t cs = (cudaStream_t)s->capture_stream;
         cudaGraph_t graph = nullptr;
         LGB_CUDA_TRY(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-        const cudaError_t le = launch_chunk(S, B, bounces, g, cs);
+        const cudaError_t le = launch_chunk<false>(S, B, bounces, g, cs);
         const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
         if (le != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_error(ctx, le, "capturing the bounce loop"); }
         if (ce != cudaSuccess) return cuda_error(ctx, ce, "cudaStreamEndCapture");
@@ -588,7 +692,7 @@ lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* p
         if (use_graph) {
             LGB_CUDA_TRY(ctx, cudaGraphLaunch((cudaGraphExec_t)s->pt_graph, st));
         } else {
-            LGB_CUDA_TRY(ctx, launch_chunk(S, B, bounces, g, st));
+            LGB_CUDA_TRY(ctx, launch_chunk<false>(S, B, bounces, g, st));
         }
     }
     LGB_CUDA_TRY(ctx, cudaGetLastError());
@@ -667,7 +771,7 @@ lgb_status render_path_noalloc(Scene* s, const lgb_camera* cam, const lgb_path_p
         // The arena keeps the previous call's contents: the parameters and counters are rewritten here, the
         // occlusion bits before every shadow query, and every other array is written before it is read.
         k_set_params<<<1, 1, 0, st>>>(P, B.params);
-        LGB_CUDA_TRY(ctx, launch_chunk(S, B, bounces, g, st));
+        LGB_CUDA_TRY(ctx, launch_chunk<false>(S, B, bounces, g, st));
     }
     return LGB_OK;
 }
@@ -694,3 +798,341 @@ extern "C" LGB_API lgb_status lgb_render_path_noalloc(lgb_scene* s, const lgb_ca
     if (cudaSetDevice(s->ctx->device) != cudaSuccess) return set_error(s->ctx, LGB_ERR_CUDA, "cudaSetDevice failed");
     return render_path_noalloc(s, cam, p, frame0, spp, d_film, (cudaStream_t)stream);
 }
+
+// ---------------------------------------------------------------------------------------------------------
+// Batched rendering (lgb_batch_*): the path integrator above over many jobs at once. The BVHs of the batch's
+// scenes are copied into one forest with relocated node and triangle indices, so the traversal kernels keep
+// one node array and one triangle array and each ray carries only its root node; the shading kernels find
+// their scene, camera and film through the job of the path.
+// ---------------------------------------------------------------------------------------------------------
+namespace lgb {
+namespace {
+
+constexpr uint32_t kBatchDefaultCap = 1u << 21;
+constexpr uint32_t kBatchMaxCap = 1u << 24;
+
+__global__ void k_relocate(const WideNode* __restrict__ src, uint32_t n, uint32_t node_off, uint32_t tri_off,
+                           WideNode* __restrict__ dst) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        WideNode w = src[i];
+        w.child_base += node_off;
+        w.tri_base += tri_off;
+        dst[i] = w;
+    }
+}
+
+__global__ void k_set_chunk(BatchChunk C, BatchChunk* dst) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *dst = C;
+}
+
+void free_batch(Batch* b) {
+    cudaSetDevice(b->ctx->device);
+    if (b->graph) cudaGraphExecDestroy((cudaGraphExec_t)b->graph);
+    if (b->capture_stream) cudaStreamDestroy((cudaStream_t)b->capture_stream);
+    if (b->staging_event) {
+        cudaEventSynchronize((cudaEvent_t)b->staging_event);
+        cudaEventDestroy((cudaEvent_t)b->staging_event);
+    }
+    if (b->staging) cudaFreeHost(b->staging);
+    cudaFree(b->buf);
+    cudaFree(b->nodes);
+    cudaFree(b->tris);
+    cudaFree(b->d_status);
+}
+
+lgb_status batch_create(Ctx* ctx, Scene* const* scenes, uint32_t n, Batch* b) {
+    b->ctx = ctx;
+    uint64_t nodes = 0, tris = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        Scene* s = scenes[i];
+        if (!s || s->ctx != ctx) return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "scene " + std::to_string(i) + " is null or of another context");
+        if (!s->bvh.nodes || s->bvh.num_nodes == 0)
+            return set_error(ctx, LGB_ERR_NOT_READY, "scene " + std::to_string(i) + " has no BVH (lgb_bvh_build)");
+        b->scenes.push_back(s);
+        b->roots.push_back((uint32_t)nodes);
+        b->bvh_generation.push_back(s->bvh.generation);
+        nodes += s->bvh.num_nodes;
+        tris += s->bvh.num_tris;
+    }
+    if (nodes >= 0x7fffffffull || tris >= 0x7fffffffull)
+        return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "the batch's BVHs exceed 2^31 nodes or triangles");
+    b->num_nodes = (uint32_t)nodes;
+    b->num_tris = (uint32_t)tris;
+    LGB_CUDA_TRY(ctx, cudaMalloc(&b->nodes, sizeof(WideNode) * std::max<uint64_t>(nodes, 1)));
+    LGB_CUDA_TRY(ctx, cudaMalloc(&b->tris, sizeof(WideTri) * std::max<uint64_t>(tris, 1)));
+    LGB_CUDA_TRY(ctx, cudaMalloc(&b->d_status, sizeof(uint32_t)));
+    LGB_CUDA_TRY(ctx, cudaMemset(b->d_status, 0, sizeof(uint32_t)));
+    uint32_t tri_off = 0;
+    const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    for (uint32_t i = 0; i < n; i++) {
+        const Scene* s = b->scenes[i];
+        const uint32_t nn = s->bvh.num_nodes, nt = s->bvh.num_tris;
+        if (nn) k_relocate<<<std::min<uint32_t>((nn + 255) / 256, sms * 8), 256>>>(s->bvh.nodes, nn, b->roots[i], tri_off,
+                                                                             b->nodes + b->roots[i]);
+        if (nt) LGB_CUDA_TRY(ctx, cudaMemcpy(b->tris + tri_off, s->bvh.tris, sizeof(WideTri) * nt, cudaMemcpyDeviceToDevice));
+        tri_off += nt;
+    }
+    LGB_CUDA_TRY(ctx, cudaGetLastError());
+    LGB_CUDA_TRY(ctx, cudaDeviceSynchronize());
+    LGB_CUDA_TRY(ctx, cudaMallocHost(&b->staging, sizeof(JobRec) * kMaxBatchJobs));
+    cudaEvent_t ev;
+    LGB_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    b->staging_event = ev;
+    LGB_CUDA_TRY(ctx, cudaEventRecord(ev, 0));
+    return LGB_OK;
+}
+
+lgb_status check_jobs(Batch* b, const lgb_batch_job* jobs, uint32_t n) {
+    Ctx* ctx = b->ctx;
+    if (!jobs || n == 0 || n > kMaxBatchJobs)
+        return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "between 1 and 128 jobs per batch call");
+    for (size_t i = 0; i < b->scenes.size(); i++)
+        if (b->scenes[i]->bvh.generation != b->bvh_generation[i])
+            return set_error(ctx, LGB_ERR_NOT_READY, "scene " + std::to_string(i) + " was rebuilt after lgb_batch_create");
+    for (uint32_t i = 0; i < n; i++) {
+        const lgb_batch_job& j = jobs[i];
+        const std::string id = "job " + std::to_string(i) + ": ";
+        if (j.scene >= b->scenes.size()) return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, id + "scene index out of range");
+        const Scene* s = b->scenes[j.scene];
+        const lgb_path_params& p = j.params;
+        if (!j.d_film || (reinterpret_cast<uintptr_t>(j.d_film) & 15u) || j.camera.width == 0 || j.camera.height == 0)
+            return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, id + "null or misaligned film, or empty image");
+        if ((uint64_t)j.camera.width * j.camera.height > kBatchMaxCap)
+            return set_error(ctx, LGB_ERR_UNSUPPORTED, id + "image larger than 2^24 pixels");
+        if (p.num_lights < 0 || (uint32_t)p.num_lights > s->num_lights)
+            return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, id + "num_lights exceeds the scene's light count");
+        if (p.num_lights > 0 && p.light_triangle_count <= 0)
+            return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, id + "light_triangle_count must be positive");
+        if (p.dir_light_idx != 0xFFFFFFFFu)
+            return set_error(ctx, LGB_ERR_UNSUPPORTED, id + "atmosphere shading for directional lights is not supported");
+    }
+    return LGB_OK;
+}
+
+// Cuts the jobs into chunks of at most `cap` paths, each a list of whole-frame segments. A job's frames are
+// taken in order, as many as fit; a chunk that cannot take one more frame of the current job is closed, so
+// a job appears at most once per chunk and its chunks run in frame order.
+void plan_chunks(const lgb_batch_job* jobs, uint32_t n, uint32_t cap, bool write_film, std::vector<BatchChunk>& out) {
+    BatchChunk C;
+    std::memset(&C, 0, sizeof(C));
+    C.write_film = write_film ? 1u : 0u;
+    auto flush = [&]() {
+        if (C.nseg) out.push_back(C);
+        std::memset(&C, 0, sizeof(C));
+        C.write_film = write_film ? 1u : 0u;
+    };
+    for (uint32_t j = 0; j < n; j++) {
+        const uint32_t npix = jobs[j].camera.width * jobs[j].camera.height;
+        uint32_t f = jobs[j].frame0, left = jobs[j].spp;
+        while (left > 0) {
+            const uint32_t k = std::min(left, (cap - C.npaths) / npix);
+            if (k == 0) { flush(); continue; }
+            Segment& sg = C.seg[C.nseg++];
+            sg.job = j; sg.frame0 = f; sg.nframes = k; sg.path_off = C.npaths; sg.pix_off = C.npix_total; sg.npix = npix;
+            C.npaths += k * npix;
+            C.npix_total += npix;
+            f += k;
+            left -= k;
+            if (C.nseg == kMaxBatchJobs) flush();
+        }
+    }
+    flush();
+}
+
+lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const lgb_batch_opts& o, bool write_film,
+                        cudaStream_t st) {
+    Ctx* ctx = b->ctx;
+    uint32_t max_npix = 1;
+    int bounces = 1;
+    for (uint32_t j = 0; j < n; j++) {
+        max_npix = std::max(max_npix, jobs[j].camera.width * jobs[j].camera.height);
+        bounces = std::max(bounces, jobs[j].params.max_depth);
+    }
+    uint32_t cap = o.path_capacity ? o.path_capacity : kBatchDefaultCap;
+    cap = std::min(std::max(cap, max_npix), kBatchMaxCap);
+    Buffers B;
+    const size_t bytes = carve(nullptr, cap, B, true);
+    if (b->buf_bytes < bytes) {
+        if (b->graph) { cudaGraphExecDestroy((cudaGraphExec_t)b->graph); b->graph = nullptr; }
+        cudaFree(b->buf);
+        b->buf = nullptr;
+        b->buf_bytes = 0;
+        LGB_CUDA_TRY(ctx, cudaMalloc(&b->buf, bytes));
+        b->buf_bytes = bytes;
+    }
+    carve((char*)b->buf, cap, B, true);
+    const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    Grids g = path_grids(ctx);
+    if (o.work_blocks_per_sm) g.work = sms * (int)std::min(o.work_blocks_per_sm, 64u);
+    if (o.trace_blocks_per_sm) g.trace = std::min(g.trace, sms * (int)o.trace_blocks_per_sm);
+
+    // Job table: staged in pinned memory (after the previous upload has left it) and copied on the stream.
+    LGB_CUDA_TRY(ctx, cudaEventSynchronize((cudaEvent_t)b->staging_event));
+    JobRec* stage = reinterpret_cast<JobRec*>(b->staging);
+    for (uint32_t j = 0; j < n; j++) {
+        std::memset(&stage[j], 0, sizeof(JobRec));
+        stage[j].P = make_params(&jobs[j].camera, &jobs[j].params, cap, jobs[j].d_film);
+        stage[j].S = scene_view(b->scenes[jobs[j].scene]);
+        stage[j].root = b->roots[jobs[j].scene];
+    }
+    LGB_CUDA_TRY(ctx, cudaMemcpyAsync(const_cast<JobRec*>(B.jobs), stage, sizeof(JobRec) * n, cudaMemcpyHostToDevice, st));
+    LGB_CUDA_TRY(ctx, cudaEventRecord((cudaEvent_t)b->staging_event, st));
+
+    SceneView F;
+    std::memset(&F, 0, sizeof(F));
+    F.nodes = b->nodes;
+    F.tris = b->tris;
+    F.status = b->d_status;
+    cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+    LGB_CUDA_TRY(ctx, cudaStreamIsCapturing(st, &cap_status));
+    const bool use_graph = cap_status == cudaStreamCaptureStatusNone;
+    const uint64_t key[6] = {(uint64_t)(uintptr_t)b->buf, cap, (uint64_t)bounces, (uint64_t)(uintptr_t)b->nodes,
+                             (uint64_t)(uintptr_t)b->tris, ((uint64_t)g.work << 32) | (uint32_t)g.trace};
+    if (use_graph && (!b->graph || std::memcmp(key, b->graph_key, sizeof(key)) != 0)) {
+        if (b->graph) { cudaGraphExecDestroy((cudaGraphExec_t)b->graph); b->graph = nullptr; }
+        if (!b->capture_stream) LGB_CUDA_TRY(ctx, cudaStreamCreateWithFlags((cudaStream_t*)&b->capture_stream, cudaStreamNonBlocking));
+        const cudaStream_t cs = (cudaStream_t)b->capture_stream;
+        cudaGraph_t graph = nullptr;
+        LGB_CUDA_TRY(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        const cudaError_t le = launch_chunk<true>(F, B, bounces, g, cs);
+        const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
+        if (le != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_error(ctx, le, "capturing the batch bounce loop"); }
+        if (ce != cudaSuccess) return cuda_error(ctx, ce, "cudaStreamEndCapture");
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) return cuda_error(ctx, ie, "cudaGraphInstantiate");
+        b->graph = exec;
+        std::memcpy(b->graph_key, key, sizeof(key));
+    }
+    std::vector<BatchChunk> chunks;
+    plan_chunks(jobs, n, cap, write_film, chunks);
+    for (const BatchChunk& C : chunks) {
+        k_set_chunk<<<1, 1, 0, st>>>(C, const_cast<BatchChunk*>(B.chunk));
+        if (use_graph) LGB_CUDA_TRY(ctx, cudaGraphLaunch((cudaGraphExec_t)b->graph, st));
+        else LGB_CUDA_TRY(ctx, launch_chunk<true>(F, B, bounces, g, st));
+    }
+    LGB_CUDA_TRY(ctx, cudaGetLastError());
+    return LGB_OK;
+}
+
+// Times every candidate (queue size x shading grid) on a quarter of each job's frames, films untouched; the
+// first run of a candidate records its graph, the second is timed.
+lgb_status batch_tune(Batch* b, const lgb_batch_job* jobs, uint32_t n, lgb_batch_opts* best, cudaStream_t st) {
+    Ctx* ctx = b->ctx;
+    std::vector<lgb_batch_job> reduced(jobs, jobs + n);
+    uint32_t max_npix = 1;
+    for (auto& j : reduced) {
+        if (j.spp) j.spp = std::max(1u, (j.spp + 3u) / 4u);
+        max_npix = std::max(max_npix, j.camera.width * j.camera.height);
+    }
+    const uint32_t caps[] = {1u << 20, 1u << 21, 1u << 22};
+    const uint32_t works[] = {4u, 8u, 16u};
+    cudaEvent_t e0, e1;
+    LGB_CUDA_TRY(ctx, cudaEventCreate(&e0));
+    LGB_CUDA_TRY(ctx, cudaEventCreate(&e1));
+    float best_ms = 0.0f;
+    lgb_batch_opts best_o{};
+    bool have = false;
+    lgb_status result = LGB_OK;
+    for (uint32_t c : caps) {
+        if (c < max_npix && c != caps[2]) continue;  // smaller than one frame: the larger candidates cover it
+        for (uint32_t w : works) {
+            lgb_batch_opts o{};
+            o.path_capacity = c;
+            o.work_blocks_per_sm = w;
+            float ms = 0.0f;
+            for (int rep = 0; rep < 2 && result == LGB_OK; rep++) {
+                cudaEventRecord(e0, st);
+                result = batch_render(b, reduced.data(), n, o, false, st);
+                cudaEventRecord(e1, st);
+                if (result == LGB_OK && cudaEventSynchronize(e1) != cudaSuccess) result = cuda_error(ctx, cudaGetLastError(), "batch tuning");
+                if (result == LGB_OK) cudaEventElapsedTime(&ms, e0, e1);
+            }
+            if (result != LGB_OK) break;
+            if (!have || ms < best_ms) { best_ms = ms; best_o = o; have = true; }
+        }
+        if (result != LGB_OK) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (result != LGB_OK) return result;
+    b->tuned = true;
+    b->tuned_opts = best_o;
+    if (best) *best = best_o;
+    return LGB_OK;
+}
+
+}  // namespace
+}  // namespace lgb
+
+extern "C" {
+
+LGB_API lgb_status lgb_batch_create(lgb_ctx* ctx, lgb_scene* const* scenes, uint32_t num_scenes, lgb_batch** out) {
+    using namespace lgb;
+    if (!ctx) return LGB_ERR_INVALID_ARGUMENT;
+    if (!out || !scenes || num_scenes == 0) return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "null output or empty scene list");
+    *out = nullptr;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return set_error(ctx, LGB_ERR_CUDA, "cudaSetDevice failed");
+    lgb_batch* b = new (std::nothrow) lgb_batch();
+    if (!b) return set_error(ctx, LGB_ERR_OUT_OF_MEMORY, "host allocation failed");
+    std::vector<Scene*> list(scenes, scenes + num_scenes);
+    const lgb_status st = batch_create(ctx, list.data(), num_scenes, b);
+    if (st != LGB_OK) {
+        free_batch(b);
+        delete b;
+        return st;
+    }
+    *out = b;
+    return LGB_OK;
+}
+
+LGB_API void lgb_batch_destroy(lgb_batch* b) {
+    if (!b) return;
+    lgb::free_batch(b);
+    delete b;
+}
+
+LGB_API lgb_status lgb_batch_render(lgb_batch* b, const lgb_batch_job* jobs, uint32_t num_jobs, const lgb_batch_opts* opts,
+                                    void* stream) {
+    using namespace lgb;
+    if (!b) return LGB_ERR_INVALID_ARGUMENT;
+    lgb_status st = check_jobs(b, jobs, num_jobs);
+    if (st != LGB_OK) return st;
+    if (cudaSetDevice(b->ctx->device) != cudaSuccess) return set_error(b->ctx, LGB_ERR_CUDA, "cudaSetDevice failed");
+    const lgb_batch_opts o = opts ? *opts : (b->tuned ? b->tuned_opts : lgb_batch_opts{});
+    return batch_render(b, jobs, num_jobs, o, true, (cudaStream_t)stream);
+}
+
+LGB_API lgb_status lgb_batch_tune(lgb_batch* b, const lgb_batch_job* jobs, uint32_t num_jobs, lgb_batch_opts* best,
+                                  void* stream) {
+    using namespace lgb;
+    if (!b) return LGB_ERR_INVALID_ARGUMENT;
+    lgb_status st = check_jobs(b, jobs, num_jobs);
+    if (st != LGB_OK) return st;
+    if (cudaSetDevice(b->ctx->device) != cudaSuccess) return set_error(b->ctx, LGB_ERR_CUDA, "cudaSetDevice failed");
+    return batch_tune(b, jobs, num_jobs, best, (cudaStream_t)stream);
+}
+
+LGB_API lgb_status lgb_batch_sync(lgb_batch* b, void* stream) {
+    using namespace lgb;
+    if (!b) return LGB_ERR_INVALID_ARGUMENT;
+    LGB_CUDA_TRY(b->ctx, cudaStreamSynchronize((cudaStream_t)stream));
+    uint32_t status = 0;
+    LGB_CUDA_TRY(b->ctx, cudaMemcpy(&status, b->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    for (Scene* s : b->scenes) {
+        uint32_t v = 0;
+        LGB_CUDA_TRY(b->ctx, cudaMemcpy(&v, s->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        status |= v;
+    }
+    if (status) {
+        const uint32_t zero = 0;
+        cudaMemcpy(b->d_status, &zero, sizeof(uint32_t), cudaMemcpyHostToDevice);
+        for (Scene* s : b->scenes) cudaMemcpy(s->d_status, &zero, sizeof(uint32_t), cudaMemcpyHostToDevice);
+        return set_error(b->ctx, LGB_ERR_DEVICE_STATUS,
+                         "device status word 0x" + std::to_string(status) + " (bit 0: traversal stack overflow, bit 1: bad index, bit 2: visit limit)");
+    }
+    return LGB_OK;
+}
+
+}  // extern "C"

@@ -215,7 +215,8 @@ __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ no
                                                  const lgb_ray* __restrict__ rays, lgb_hit* __restrict__ hits,
                                                  uint32_t* __restrict__ occ_bits, uint32_t n, const uint32_t* count_ptr,
                                                  uint32_t* ray_counter, uint32_t* status,
-                                                 unsigned long long* counters) {
+                                                 unsigned long long* counters,
+                                                 const uint32_t* __restrict__ roots = nullptr) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const uint32_t lanemask_lt = (1u << lane) - 1u;
@@ -242,7 +243,7 @@ __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ no
                         r = make_rayq(r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w);
                         ray_id = id;
                         sp = 0;
-                        g_base = 0u;
+                        g_base = roots ? roots[id] : 0u;  // per-ray root node when several BVHs share the arrays
                         // virtual parent of the root: slot 0 internal and hit; an empty interval visits nothing
                         g_hm = r.tmin <= r.tmax ? (((1u << (0u ^ r.oct)) << 8) | 1u) : 1u;
                         best = LGB_NO_HIT;

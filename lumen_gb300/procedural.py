@@ -10,6 +10,8 @@ fixes the arrays; tests that need bit-identical inputs on every host read them f
                        rendering).
   traversal_scene()    icosphere of frequency 200 (800 000 triangles) displaced by 3-octave value noise of
                        amplitude 0.1, plus 200 000 random small triangles in [-2, 2]^3.
+  batch_scene()        displaced sphere + floor + boxes + 1-8 quad lights with principled / dielectric
+                       materials (batched rendering); batch_config() draws the 32 scenes' sizes.
   primary_rays()       one ray per pixel centre of a pinhole camera.
   incoherent_rays()    origins area-uniform on the surfaces, cosine-distributed about a random side.
 """
@@ -311,6 +313,67 @@ def traversal_scene(sphere_freq: int = 200, n_random: int = 200_000, seed: int =
     if n_random:
         b.add(random_triangles(n_random, seed + 1), None, 0)
     return b.arrays([diffuse(WHITE)], np.zeros(0, LIGHT_DTYPE), 0, (0.0, 0.0, -4.0), (0.0, 0.0, 1.0), 45.0)
+
+
+def batch_scene(seed: int, n_tris: int) -> SceneArrays:
+    """One scene of the batched-rendering configuration: a displaced icosphere of about n_tris triangles
+    (frequency round(sqrt(n_tris / 20))) on a floor, three boxes and 1-8 quad lights (L = 12) overhead. Every
+    surface material is drawn from PCG64(seed): with probability 0.2 a smooth dielectric of IOR 1.5, else
+    Disney principled with baseColor U[0,1]^3, roughness U[0.05,1], metallic Bernoulli(0.3) and specular 0.5
+    (IOR 1.5, F0 = 0.04). Camera on +z looking at the sphere."""
+    rng = np.random.default_rng(seed)
+    from .scene import dielectric, principled
+
+    def material():
+        if rng.uniform() < 0.2:
+            return dielectric(1.5, 0.0)
+        return principled(tuple(rng.uniform(0.0, 1.0, 3)), roughness=float(rng.uniform(0.05, 1.0)),
+                          metallic=float(rng.uniform() < 0.3), ior=1.5)
+
+    b = _Builder()
+    mats = []
+    freq = max(2, int(round(math.sqrt(n_tris / 20.0))))
+    mats.append(material())
+    b.add(displaced_icosphere(freq, 0.1, seed * 7 + 1), None, len(mats) - 1)
+    mats.append(material())
+    t, n = _quad((-4, -1.2, -4), (4, -1.2, -4), (4, -1.2, 4), (-4, -1.2, 4), inward=(0, 1, 0))
+    b.add(t, n, len(mats) - 1)
+    for k in range(3):
+        mats.append(material())
+        c = (float(rng.uniform(-2.5, 2.5)), -1.2 + 0.3, float(rng.uniform(-2.5, 0.5)))
+        t, n = _box(c, (0.6, 0.6, 0.6), float(rng.uniform(-45, 45)))
+        b.add(t, n, len(mats) - 1)
+    n_lights = int(rng.integers(1, 9))
+    emitter = diffuse((1.0, 1.0, 1.0), emissive=(12.0, 12.0, 12.0))
+    mats.append(emitter)
+    lights = np.zeros(n_lights, LIGHT_DTYPE)
+    for k in range(n_lights):
+        cx, cz = (float(v) for v in rng.uniform(-2.0, 2.0, 2))
+        y = 2.5
+        t, n = _quad((cx - 0.25, y, cz - 0.25), (cx + 0.25, y, cz - 0.25), (cx + 0.25, y, cz + 0.25),
+                     (cx - 0.25, y, cz + 0.25), inward=(0, -1, 0))
+        mesh = b.add(t, n, len(mats) - 1)
+        lights[k]["world_matrix"] = np.eye(4, dtype=np.float32).reshape(16)
+        lights[k]["prim_mesh_idx"] = mesh
+        lights[k]["num_triangles"] = 2
+        lights[k]["L"] = 12.0
+        lights[k]["light_flags"] = abi.LIGHT_AREA | abi.LIGHT_FINITE
+    return b.arrays(mats, lights, 2 * n_lights, (0.0, 0.5, 4.5), (0.0, 0.5 / 4.5, 1.0), 45.0)
+
+
+def batch_config(seed: int = 0, n_scenes: int = 32, min_tris: int = 10_000, max_tris: int = 2_000_000,
+                 min_res: int = 128, max_res: int = 1024, min_spp: int = 8, max_spp: int = 64):
+    """The batched-rendering configuration: n_scenes (seed, triangles, width, height, spp) with triangle counts,
+    square resolutions (multiples of 32) and spp log-uniform in their ranges, drawn from PCG64(seed)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_scenes):
+        tris = int(round(math.exp(rng.uniform(math.log(min_tris), math.log(max_tris)))))
+        res = int(round(math.exp(rng.uniform(math.log(min_res), math.log(max_res))) / 32.0)) * 32
+        res = min(max(res, min_res), max_res)
+        spp = int(round(math.exp(rng.uniform(math.log(min_spp), math.log(max_spp)))))
+        out.append((1000 + i, tris, res, res, spp))
+    return out
 
 
 def primary_rays(width: int, height: int, pos=(0.0, 0.0, -4.0), fov: float = 45.0, tmax: float = 10000.0) -> np.ndarray:

@@ -294,6 +294,61 @@ class GpuScene:
             pass
 
 
+class Batch:
+    """lgb_batch_*: several GpuScenes (BVHs built) rendered as one wavefront. The scenes are kept alive by the
+    batch."""
+
+    def __init__(self, ctx: Context, scenes):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.scenes = list(scenes)
+        arr = (C.c_void_p * len(self.scenes))(*[sc.handle.value for sc in self.scenes])
+        h = C.c_void_p()
+        _check(self.lib, ctx.handle, self.lib.lgb_batch_create(ctx.handle, arr, len(self.scenes), C.byref(h)))
+        self.handle = h
+
+    @staticmethod
+    def job(scene_index: int, cam: abi.Camera, params: abi.PathParams, frame0: int, spp: int, film) -> abi.BatchJob:
+        j = abi.BatchJob()
+        j.scene = scene_index
+        j.frame0 = frame0
+        j.spp = spp
+        j.camera = cam
+        j.params = params
+        j.d_film = film.data_ptr()
+        return j
+
+    @staticmethod
+    def _array(jobs):
+        return (abi.BatchJob * len(jobs))(*jobs)
+
+    def render(self, jobs, opts: abi.BatchOpts | None = None, stream=None):
+        arr = self._array(jobs)
+        _check(self.lib, self.ctx.handle,
+               self.lib.lgb_batch_render(self.handle, arr, len(jobs), C.byref(opts) if opts is not None else None,
+                                         C.c_void_p(stream)))
+
+    def tune(self, jobs, stream=None) -> abi.BatchOpts:
+        best = abi.BatchOpts()
+        _check(self.lib, self.ctx.handle,
+               self.lib.lgb_batch_tune(self.handle, self._array(jobs), len(jobs), C.byref(best), C.c_void_p(stream)))
+        return best
+
+    def sync(self, stream=None):
+        _check(self.lib, self.ctx.handle, self.lib.lgb_batch_sync(self.handle, C.c_void_p(stream)))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.lgb_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def path_params(arrays: SceneArrays, max_depth: int, sky=(0.0, 0.0, 0.0), direct_lighting: int = 1,
                 film_mode: int = 0) -> abi.PathParams:
     """PCPath as Path::render fills it (src/RayTracer/Path.cpp:28-38)."""

@@ -43,6 +43,10 @@ def test_struct_layouts():
     assert C.sizeof(abi.Camera) == 136
     assert C.sizeof(abi.PathParams) == 48
     assert C.sizeof(abi.BuildStats) == 56
+    assert C.sizeof(abi.DiffParams) == 32
+    assert C.sizeof(abi.DiffGrads) == 24
+    assert C.sizeof(abi.BatchJob) == 208
+    assert C.sizeof(abi.BatchOpts) == 32
 
 
 def test_camera_lookat_matches_oracle(lib, oracle):
@@ -69,3 +73,33 @@ def test_null_handles_are_rejected(lib):
     assert lib.lgb_trace_closest(None, None, None, 0, None) == 1
     assert lib.lgb_sync(None, None) == 1
     assert lib.lgb_last_error(None) == b"null context"
+
+
+def test_ctypes_layouts_match_the_header(tmp_path):
+    """Every ctypes mirror has the size and field offsets the C compiler gives the header's struct."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    mirrors = {"lgb_ray": abi.Ray, "lgb_hit": abi.Hit, "lgb_material": abi.Material, "lgb_light": abi.Light,
+               "lgb_mesh": abi.Mesh, "lgb_camera": abi.Camera, "lgb_path_params": abi.PathParams,
+               "lgb_build_opts": abi.BuildOpts, "lgb_build_stats": abi.BuildStats, "lgb_diff_params": abi.DiffParams,
+               "lgb_diff_grads": abi.DiffGrads, "lgb_batch_job": abi.BatchJob, "lgb_batch_opts": abi.BatchOpts}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "lgb.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for fname, *_ in py._fields_:
+            lines.append(f'printf("{cname}.{fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-std=c11", "-I" + inc, str(src), "-o", str(exe)], check=True)
+    out = dict(l.rsplit(" ", 1) for l in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                          text=True).stdout.splitlines())
+    for cname, py in mirrors.items():
+        assert int(out[cname]) == C.sizeof(py), cname
+        for fname, *_ in py._fields_:
+            assert int(out[f"{cname}.{fname}"]) == getattr(py, fname).offset, f"{cname}.{fname}"

@@ -1,0 +1,171 @@
+"""GPU tests of batched rendering (lgb_batch_*): several scenes and views in one wavefront.
+
+Every path of a batch is seeded and computed as lgb_render_path computes it, so each job's film must be
+bit-identical to the film of the same job rendered alone, whatever the chunking (small path capacities force
+chunks that mix segments of several jobs and split jobs across chunks)."""
+import os
+
+import numpy as np
+import pytest
+
+from lumen_gb300 import abi, build, procedural
+from lumen_gb300.scene import Batch, Context, GpuScene, camera_lookat, path_params
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+DEPTH = 12
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    if not os.path.exists(abi.LIB_PATH):
+        build.build_library()
+    return Context(0)
+
+
+@pytest.fixture(scope="module")
+def scenes(ctx):
+    out = []
+    for seed, tris in ((7, 2000), (8, 12000), (9, 5000)):
+        arrays = procedural.batch_scene(seed, tris)
+        sc = GpuScene(ctx, arrays)
+        sc.build()
+        out.append((arrays, sc))
+    cb = procedural.cornell_box()
+    sc = GpuScene(ctx, cb)
+    sc.build()
+    out.append((cb, sc))
+    return out
+
+
+# (scene, width, height, frame0, spp): uneven sizes, two views of scene 0, a continuation from frame 3
+JOBS = [(0, 48, 40, 0, 3), (1, 64, 64, 0, 5), (2, 32, 32, 0, 2), (3, 56, 48, 0, 4), (0, 40, 40, 0, 6),
+        (3, 32, 32, 3, 2)]
+
+
+def _camera(arrays, w, h, view=0):
+    pos = np.array(arrays.camera_pos, np.float64)
+    if view:
+        pos = pos + np.array([0.6, 0.3, 0.0])
+    return camera_lookat(tuple(pos), arrays.camera_dir, arrays.fov, w, h)
+
+
+def _films(jobs, seed_film=None):
+    films = []
+    for k, (_, w, h, frame0, _) in enumerate(jobs):
+        f = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+        if frame0 and seed_film is not None:
+            f.copy_(seed_film[k])
+        films.append(f)
+    return films
+
+
+def _alone(scenes, jobs, films):
+    for k, (si, w, h, frame0, spp) in enumerate(jobs):
+        arrays, sc = scenes[si]
+        cam = _camera(arrays, w, h, view=k == 4)
+        sc.render_path(cam, path_params(arrays, DEPTH), frame0, spp, films[k])
+        sc.sync()
+
+
+def _batched(ctx, scenes, jobs, films, opts=None, tune=False):
+    batch = Batch(ctx, [sc for _, sc in scenes])
+    js = []
+    for k, (si, w, h, frame0, spp) in enumerate(jobs):
+        arrays, _ = scenes[si]
+        js.append(Batch.job(si, _camera(arrays, w, h, view=k == 4), path_params(arrays, DEPTH), frame0, spp, films[k]))
+    best = batch.tune(js) if tune else None
+    batch.render(js, opts)
+    batch.sync()
+    return batch, best
+
+
+def _start_films(scenes):
+    """Films for the jobs that continue from frame 3: the first three frames rendered alone."""
+    pre = {}
+    for k, (si, w, h, frame0, _) in enumerate(JOBS):
+        if frame0:
+            arrays, sc = scenes[si]
+            f = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+            sc.render_path(_camera(arrays, w, h), path_params(arrays, DEPTH), 0, frame0, f)
+            sc.sync()
+            pre[k] = f
+    return [pre.get(k) for k in range(len(JOBS))]
+
+
+@pytest.mark.parametrize("capacity", [0, 4096, 6000])
+def test_batched_films_equal_films_rendered_alone(ctx, scenes, capacity):
+    start = _start_films(scenes)
+    want = _films(JOBS, start)
+    _alone(scenes, JOBS, want)
+    got = _films(JOBS, start)
+    opts = None
+    if capacity:
+        opts = abi.BatchOpts()
+        opts.path_capacity = capacity  # below some images: raised to the largest image
+        opts.work_blocks_per_sm = 4
+    _batched(ctx, scenes, JOBS, got, opts)
+    for k in range(len(JOBS)):
+        a, b = got[k].cpu().numpy(), want[k].cpu().numpy()
+        assert np.array_equal(a, b), f"job {k}: max diff {np.abs(a - b).max()}"
+        assert (a[:, 3] == 1.0).all() and a[:, :3].mean() > 0.0
+
+
+def test_tuner_picks_options_and_leaves_films(ctx, scenes):
+    films = _films(JOBS)
+    for f in films:
+        f.fill_(-1.0)
+    batch = Batch(ctx, [sc for _, sc in scenes])
+    js = []
+    for k, (si, w, h, frame0, spp) in enumerate(JOBS):
+        arrays, _ = scenes[si]
+        js.append(Batch.job(si, _camera(arrays, w, h, view=k == 4), path_params(arrays, DEPTH), 0, spp, films[k]))
+    best = batch.tune(js)
+    batch.sync()
+    assert best.path_capacity in (1 << 20, 1 << 21, 1 << 22)
+    assert best.work_blocks_per_sm in (4, 8, 16)
+    assert all(bool((f == -1.0).all()) for f in films)
+    for f in films:
+        f.zero_()
+    batch.render(js)  # tuned options
+    batch.sync()
+    want = _films(JOBS)
+    for k, (si, w, h, _, spp) in enumerate(JOBS):
+        arrays, sc = scenes[si]
+        sc.render_path(_camera(arrays, w, h, view=k == 4), path_params(arrays, DEPTH), 0, spp, want[k])
+        sc.sync()
+        assert np.array_equal(films[k].cpu().numpy(), want[k].cpu().numpy())
+
+
+def test_batch_error_paths(ctx, scenes):
+    arrays, sc = scenes[0]
+    batch = Batch(ctx, [sc])
+    film = torch.zeros((32 * 32, 4), dtype=torch.float32, device="cuda")
+    cam = _camera(arrays, 32, 32)
+    with pytest.raises(abi.LgbError):
+        batch.render([Batch.job(1, cam, path_params(arrays, DEPTH), 0, 1, film)])  # no scene 1
+    with pytest.raises(abi.LgbError):
+        batch.render([Batch.job(0, cam, path_params(arrays, DEPTH), 0, 1, film)] * 129)  # too many jobs
+    bad = path_params(arrays, DEPTH)
+    bad.num_lights = 99
+    with pytest.raises(abi.LgbError):
+        batch.render([Batch.job(0, cam, bad, 0, 1, film)])
+    misaligned = torch.zeros(32 * 32 * 4 + 4, dtype=torch.float32, device="cuda")[1:]  # 4-byte offset
+    with pytest.raises(abi.LgbError):
+        batch.render([Batch.job(0, cam, path_params(arrays, DEPTH), 0, 1, misaligned)])
+    # a scene rebuilt after the batch was made is refused
+    other = GpuScene(ctx, procedural.batch_scene(3, 500))
+    other.build()
+    b2 = Batch(ctx, [other])
+    other.build()
+    with pytest.raises(abi.LgbError):
+        b2.render([Batch.job(0, _camera(other.arrays, 32, 32), path_params(other.arrays, DEPTH), 0, 1, film)])
+    b2.close()
+    # a scene without a BVH cannot join a batch
+    fresh = GpuScene(ctx, procedural.batch_scene(4, 500))
+    with pytest.raises(abi.LgbError):
+        Batch(ctx, [fresh])
+    batch.render([Batch.job(0, cam, path_params(arrays, DEPTH), 0, 2, film)])
+    batch.sync()
+    assert film[:, :3].mean().item() > 0.0

@@ -249,6 +249,79 @@ def adjoint_secondary(torch, ctx_cls, scene_cls, local):
             "grad_norms": {"texels": float(gt.norm()), "roughness": float(gr.norm()), "emission": float(ge.norm())}}
 
 
+def batch_secondary(torch, ctx_cls, scene_cls, local):
+    """Batched rendering: the 32-scene configuration (10k-2M triangles, 128^2-1024^2, 8-64 spp, depth 12,
+    principled / dielectric materials) rendered (a) scene after scene through lgb_render_path and (b) as one
+    tuned lgb_batch_render. Both give the same per-path computation, so the films are compared for equality
+    (equal RMSE against any reference) and the Msamples/s of the two are reported."""
+    import multiprocessing as mp
+    from lumen_gb300 import procedural
+    from lumen_gb300.scene import Batch, camera_lookat, path_params
+    cfg = procedural.batch_config()
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        arrays = pool.starmap(procedural.batch_scene, [(seed, tris) for seed, tris, _, _, _ in cfg])
+    gen_s = time.perf_counter() - t0
+    ctx = ctx_cls(local)
+    scenes = []
+    for a in arrays:
+        sc = scene_cls(ctx, a)
+        sc.build()
+        scenes.append(sc)
+    stream = torch.cuda.current_stream()
+    cs = stream.cuda_stream
+    jobs, films_a, films_b = [], [], []
+    for i, (a, (_, _, w, h, spp)) in enumerate(zip(arrays, cfg)):
+        cam = camera_lookat(a.camera_pos, a.camera_dir, a.fov, w, h)
+        films_a.append(torch.zeros((w * h, 4), dtype=torch.float32, device="cuda"))
+        films_b.append(torch.zeros((w * h, 4), dtype=torch.float32, device="cuda"))
+        jobs.append((i, cam, path_params(a, 12), spp))
+    samples = sum(w * h * spp for _, _, w, h, spp in cfg)
+
+    def alone():
+        for i, cam, params, spp in jobs:
+            scenes[i].render_path(cam, params, 0, spp, films_a[i], stream=cs)
+
+    batch = Batch(ctx, scenes)
+    bjobs = [Batch.job(i, cam, params, 0, spp, films_b[i]) for i, cam, params, spp in jobs]
+    t0 = time.perf_counter()
+    best = batch.tune(bjobs, stream=cs)
+    tune_s = time.perf_counter() - t0
+
+    def batched():
+        batch.render(bjobs, stream=cs)
+
+    def timed(fn, reps=2):
+        fn()
+        torch.cuda.synchronize()
+        out = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            out.append(e0.elapsed_time(e1))
+        return min(out)
+
+    ms_alone = timed(alone)
+    ms_batch = timed(batched)
+    batch.sync(cs)
+    max_diff = max(float((fa - fb).abs().max()) for fa, fb in zip(films_a, films_b))
+    res = {"workload": "32 scenes, 10k-2M triangles (log-uniform, 14.3M total), 128^2-1024^2, 8-64 spp, depth 12, "
+                       "principled (80 %) and dielectric (20 %) materials, 1-8 quad lights",
+           "samples": samples, "per_scene_ms": ms_alone, "batched_ms": ms_batch,
+           "per_scene_msamples_per_s": samples / (ms_alone * 1e-3) / 1e6,
+           "batched_msamples_per_s": samples / (ms_batch * 1e-3) / 1e6,
+           "speedup": ms_alone / ms_batch, "films_max_abs_diff": max_diff,
+           "tuned": {"path_capacity": best.path_capacity, "work_blocks_per_sm": best.work_blocks_per_sm},
+           "tune_s": tune_s, "scene_generation_s": gen_s}
+    batch.close()
+    for sc in scenes:
+        sc.close()
+    return res
+
+
 def run_reference(args):
     rank, world, _ = _dist()
     if rank != 0:
@@ -379,6 +452,7 @@ def run_gpu(args):
     if not args.no_secondary:
         secondary["path_tracer"] = cornell_secondary(torch, Context, GpuScene, local, world == 1 and not args.no_cpu_baseline)
         secondary["adjoint"] = adjoint_secondary(torch, Context, GpuScene, local)
+        secondary["batched"] = batch_secondary(torch, Context, GpuScene, local)
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",

@@ -267,6 +267,48 @@ LGB_API lgb_status lgb_adjoint_path(lgb_scene* scene, const lgb_camera* camera, 
 /* Waits for `stream` and reports any fault a kernel recorded in the scene's device status word. */
 LGB_API lgb_status lgb_sync(lgb_scene* scene, void* stream);
 
+/* ---- VCM: vertex connection and merging (src/RayTracer/VCM.cpp, src/shaders/integrators/vcm*) ---- */
+#define LGB_VCM_ACCUMULATE 1u /* sum every light-vertex connection and merge (the reference keeps the last) */
+
+typedef struct lgb_vcm_params {
+    float sky_col[3];
+    int32_t max_depth;             /* path_length */
+    int32_t num_lights;
+    int32_t light_triangle_count;  /* LumenScene::total_light_triangle_cnt: a non-area light counts as one */
+    uint32_t dir_light_idx;        /* must be 0xFFFFFFFF */
+    float radius;                  /* merge radius of this iteration, see lgb_vcm_radius */
+    float scene_min[3];            /* photon grid bounds: the scene's bounding box (LumenScene::m_dimensions) */
+    float scene_max[3];
+    int32_t use_vm, use_vc;        /* vertex merging / vertex connection (VCM.cpp uses VC always) */
+    uint32_t light_seed, eye_seed; /* per-iteration seeds; the reference draws them with host rand() */
+    uint32_t frame_num;            /* progressive film frame: 0 overwrites, k mixes with weight 1/(k+1) */
+    uint32_t flags;                /* LGB_VCM_* */
+    uint32_t reserved[2];
+} lgb_vcm_params;
+
+/* Merge radius of iteration `iteration` (VCM.cpp:137-138): scene_radius * radius_factor / 100 shrunk by
+ * (iteration + 1)^(0.5 (1 - alpha)); the reference fixes alpha = 2/3. */
+LGB_API float lgb_vcm_radius(float scene_radius, float radius_factor, uint32_t iteration, float alpha);
+
+/* One VCM iteration into d_film (RGBA32F, width*height): light subpaths with camera splats, the photon table,
+ * eye subpaths. Light vertices, per-path counts and the splat image live in the scene between iterations, as
+ * the reference's buffers do (reallocated and zeroed when the image size or max_depth changes). Area and spot
+ * lights only. */
+LGB_API lgb_status lgb_vcm_iteration(lgb_scene* scene, const lgb_camera* camera, const lgb_vcm_params* params,
+                                     float* d_film, void* stream);
+
+/* The photon table alone (vcm_commons.glsl:455-469, made deterministic): for n positions (float4, w < 0 marks
+ * an unused entry) the slot hash(cell(p)) mod 10 * screen_size over the grid of (scene_min, scene_max, radius)
+ * (VCM.cpp:144-147); writes, per slot, the number of positions and the index of the last one. Built by radix
+ * sort and scan; waits for `stream`. */
+LGB_API lgb_status lgb_vcm_grid(lgb_ctx* ctx, const float* d_pos4, uint32_t n, const float scene_min[3],
+                                const float scene_max[3], float radius, uint32_t screen_size, uint32_t* d_count,
+                                uint32_t* d_rep, void* stream);
+
+/* The forward matrices of a camera (view and projection, column-major), inverted in double from the camera's
+ * inverse matrices and rounded to float: what lgb_vcm_iteration projects light vertices with. */
+LGB_API lgb_status lgb_camera_forward(const lgb_camera* camera, float view[16], float projection[16]);
+
 /* ---- batched rendering (no counterpart in Lumen) ----
  * Many scenes and camera views of uneven size rendered by one wavefront: the paths of every job share the
  * queues, the traversal and shading launches and one captured bounce loop, instead of each image issuing its

@@ -121,6 +121,17 @@ class BatchOpts(C.Structure):
                 ("trace_blocks_per_sm", C.c_uint32), ("reserved", C.c_uint32 * 5)]
 
 
+VCM_ACCUMULATE = 1
+
+
+class VcmParams(C.Structure):
+    _fields_ = [("sky_col", C.c_float * 3), ("max_depth", C.c_int32), ("num_lights", C.c_int32),
+                ("light_triangle_count", C.c_int32), ("dir_light_idx", C.c_uint32), ("radius", C.c_float),
+                ("scene_min", C.c_float * 3), ("scene_max", C.c_float * 3), ("use_vm", C.c_int32),
+                ("use_vc", C.c_int32), ("light_seed", C.c_uint32), ("eye_seed", C.c_uint32),
+                ("frame_num", C.c_uint32), ("flags", C.c_uint32), ("reserved", C.c_uint32 * 2)]
+
+
 # Every exported symbol with its argument and result types (the declarations of include/lgb.h).
 SIGNATURES = {
     "lgb_abi_version": ([], C.c_uint32),
@@ -144,6 +155,11 @@ SIGNATURES = {
     "lgb_adjoint_path": ([C.c_void_p, C.POINTER(Camera), C.POINTER(PathParams), C.POINTER(DiffParams), C.c_uint32,
                           C.c_uint32, C.c_void_p, C.c_void_p, C.POINTER(DiffGrads), C.c_void_p], C.c_int32),
     "lgb_sync": ([C.c_void_p, C.c_void_p], C.c_int32),
+    "lgb_vcm_radius": ([C.c_float, C.c_float, C.c_uint32, C.c_float], C.c_float),
+    "lgb_vcm_iteration": ([C.c_void_p, C.POINTER(Camera), C.POINTER(VcmParams), C.c_void_p, C.c_void_p], C.c_int32),
+    "lgb_vcm_grid": ([C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float,
+                      C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int32),
+    "lgb_camera_forward": ([C.POINTER(Camera), C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int32),
     "lgb_batch_create": ([C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, C.POINTER(C.c_void_p)], C.c_int32),
     "lgb_batch_destroy": ([C.c_void_p], None),
     "lgb_batch_render": ([C.c_void_p, C.POINTER(BatchJob), C.c_uint32, C.POINTER(BatchOpts), C.c_void_p], C.c_int32),

@@ -41,6 +41,7 @@ void free_scene(Scene* s) {
     cudaFree(s->d_ray_counter);
     cudaFree(s->pt_buf);
     cudaFree(s->diff_buf);
+    cudaFree(s->vcm_buf);
     if (s->pt_graph) cudaGraphExecDestroy((cudaGraphExec_t)s->pt_graph);
     if (s->capture_stream) cudaStreamDestroy((cudaStream_t)s->capture_stream);
 }
@@ -186,6 +187,8 @@ LGB_API lgb_status lgb_scene_create(lgb_ctx* ctx, const lgb_scene_desc* d, lgb_s
     s->num_materials = d->num_materials;
     for (uint32_t i = 0; i < d->num_materials; i++) s->bsdf_mask |= d->materials[i].bsdf_type;
     s->num_lights = d->num_lights;
+    for (uint32_t i = 0; i < d->num_lights; i++)
+        if ((d->lights[i].light_flags & 7u) == LGB_LIGHT_DIRECTIONAL) s->num_directional++;
     s->num_textures = d->num_textures;
     s->bmin = make_float3(bmin[0], bmin[1], bmin[2]);
     s->bmax = make_float3(bmax[0], bmax[1], bmax[2]);

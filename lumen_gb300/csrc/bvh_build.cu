@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "lgb_internal.cuh"
+#include "radix_sort.cuh"
 
 namespace lgb {
 namespace {
@@ -96,99 +97,6 @@ __global__ void k_morton(const float* __restrict__ tv, uint32_t n, const uint32_
     }
     keys[i] = (split3(q[0]) << 2) | (split3(q[1]) << 1) | split3(q[2]);
     vals[i] = i;
-}
-
-// ---------------- LSD radix sort (64-bit keys, 32-bit values) ----------------
-constexpr int RS_THREADS = 256;
-constexpr int RS_ITEMS = 8;
-constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
-
-__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint64_t* __restrict__ keys, uint32_t n, int shift,
-                                                        uint32_t* counts, uint32_t nblocks) {
-    __shared__ uint32_t h[256];
-    h[threadIdx.x] = 0;
-    __syncthreads();
-    size_t base = (size_t)blockIdx.x * RS_TILE;
-    for (int k = 0; k < RS_ITEMS; k++) {
-        size_t idx = base + (size_t)k * RS_THREADS + threadIdx.x;
-        if (idx < n) atomicAdd(&h[(uint32_t)(keys[idx] >> shift) & 0xffu], 1u);
-    }
-    __syncthreads();
-    counts[(size_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
-}
-
-// Exclusive scan of m counts in place, one block of 1024 threads.
-__global__ void __launch_bounds__(1024) k_scan_single(uint32_t* data, uint32_t m) {
-    __shared__ uint32_t warp_sums[32];
-    const uint32_t per = (m + 1023) / 1024;
-    const uint32_t b = threadIdx.x * per, e = min(m, b + per);
-    uint32_t sum = 0;
-    for (uint32_t i = b; i < e; i++) sum += data[i];
-    // block exclusive scan of sum
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t x = sum;
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) warp_sums[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t w = warp_sums[lane];
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w += y;
-        }
-        warp_sums[lane] = w;
-    }
-    __syncthreads();
-    uint32_t excl = x - sum + (warp > 0 ? warp_sums[warp - 1] : 0u);
-    for (uint32_t i = b; i < e; i++) {
-        uint32_t c = data[i];
-        data[i] = excl;
-        excl += c;
-    }
-}
-
-__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
-                                                           uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
-                                                           uint32_t n, int shift, const uint32_t* __restrict__ offsets,
-                                                           uint32_t nblocks) {
-    __shared__ uint32_t base_off[256];
-    __shared__ uint32_t warp_cnt[RS_THREADS / 32][256];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    base_off[tid] = offsets[(size_t)tid * nblocks + blockIdx.x];
-    const uint32_t lanemask_lt = (1u << lane) - 1u;
-    const size_t tile = (size_t)blockIdx.x * RS_TILE;
-    for (int r = 0; r < RS_ITEMS; r++) {
-        for (int w = 0; w < RS_THREADS / 32; w++) warp_cnt[w][tid] = 0;
-        __syncthreads();
-        const size_t idx = tile + (size_t)r * RS_THREADS + tid;
-        const bool valid = idx < n;
-        uint64_t key = valid ? kin[idx] : 0ull;
-        uint32_t val = valid ? vin[idx] : 0u;
-        uint32_t digit = valid ? ((uint32_t)(key >> shift) & 0xffu) : (256u + lane);
-        uint32_t peers = __match_any_sync(0xffffffffu, digit);
-        uint32_t rank = __popc(peers & lanemask_lt);
-        int leader = __ffs(peers) - 1;
-        if (valid && lane == leader) warp_cnt[warp][digit] = __popc(peers);
-        __syncthreads();
-        uint32_t running = 0;
-        for (int w = 0; w < RS_THREADS / 32; w++) {
-            uint32_t c = warp_cnt[w][tid];
-            warp_cnt[w][tid] = running;
-            running += c;
-        }
-        __syncthreads();
-        if (valid) {
-            uint32_t pos = base_off[digit] + warp_cnt[warp][digit] + rank;
-            kout[pos] = key;
-            vout[pos] = val;
-        }
-        __syncthreads();
-        base_off[tid] += running;
-        __syncthreads();
-    }
 }
 
 // ---------------- binary radix tree (Karras 2012) ----------------

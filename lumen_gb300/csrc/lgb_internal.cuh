@@ -115,6 +115,10 @@ struct Scene {
     void* capture_stream = nullptr;  // private stream used only to record graphs
     void* diff_buf = nullptr;        // per-sample radiance of the differentiable renderer
     size_t diff_buf_bytes = 0;
+    void* vcm_buf = nullptr;         // VCM state kept between iterations (light vertices, counts, splats, table)
+    size_t vcm_buf_bytes = 0;
+    uint32_t vcm_w = 0, vcm_h = 0, vcm_per = 0;
+    uint32_t num_directional = 0;    // directional lights (not supported by VCM)
 };
 
 // Several scenes rendered as one wavefront: their BVHs copied into one forest (node and triangle indices

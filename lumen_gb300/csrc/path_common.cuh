@@ -79,6 +79,7 @@ struct HitAttr {
     v3 n_g, n_s, pos;
     float u, v;
     uint32_t mat;
+    float area;  // world-space triangle area (ray.rchit:81)
 };
 __device__ __forceinline__ HitAttr resolve_hit(const SceneView& S, uint32_t prim, float bu, float bv) {
     HitAttr h;
@@ -96,7 +97,9 @@ __device__ __forceinline__ HitAttr resolve_hit(const SceneView& S, uint32_t prim
     h.n_s = normalize(normalize(n0 * b0 + n1 * b1 + n2 * b2));
     h.u = a.u * b0 + b.u * b1 + c.u * b2;
     h.v = a.v * b0 + b.v * b1 + c.v * b2;
-    h.n_g = normalize(cross(v2 - v0, v1 - v0));
+    const v3 cr = cross(v2 - v0, v1 - v0);
+    h.n_g = normalize(cr);
+    h.area = 0.5f * length(cr);
     h.mat = pm.material_index;
     return h;
 }

@@ -1,0 +1,851 @@
+// VCM: vertex connection and merging, Lumen's VCM integrator (src/RayTracer/VCM.cpp:131-265 without the
+// reservoir passes, which Lumen disables: RAY_GUIDE = 0 in vcm_light.rgen:34).
+//
+//   k_vcm_light    vcm_light.rgen:123-166, vcm_generate_light_sample and vcm_fill_light
+//                  (vcm_commons.glsl:77-130, 302-454): one light subpath per launch point, its non-specular
+//                  vertices stored, each connected to the camera and splatted (atomics into the splat image)
+//   photon table   vcm_commons.glsl:455-469 built by sort and scan: a slot key per stored vertex, a stable LSD
+//                  radix sort of (slot, vertex id), then per slot the count and the last vertex in id order,
+//                  which is the photon the reference's last writer leaves (deterministic here)
+//   k_vcm_eye      vcm_eye.rgen:42-97 and vcm_trace_eye (vcm_commons.glsl:477-631): eye subpath with emission
+//                  MIS, light connection, connections to one random light subpath, merging, progressive film
+//
+// Kept from the reference: the connection and merge loops assign rather than accumulate (`res =`), unless
+// LGB_VCM_ACCUMULATE is set; splat and light-path indices are column-major (x * height + y). Deviations: the
+// seeds are parameters (the reference draws them with host rand()); a light subpath whose emission sample has
+// a zero direction pdf stores no vertex (the reference keeps the previous iteration's count); an eye vertex
+// whose merge range exceeds 16 cells per axis does not merge; the uninitialised pdf_rev of the last eye
+// bounce is zero; the random light subpath index is clamped to the last subpath.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "bsdf_vcm.cuh"
+#include "path_common.cuh"
+#include "radix_sort.cuh"
+
+namespace lgb {
+namespace {
+
+constexpr int kVcmThreads = 128;
+constexpr int kMaxMergeCells = 16;
+constexpr float kTMinV = 0.001f, kTMaxV = 10000.0f, kEpsV = 0.001f;
+constexpr int kVertexF4 = 6;  // light vertex = 6 x float4 (96 bytes)
+
+struct VcmArgs {
+    float iv[16], ip[16], view[16], proj[16];
+    uint32_t W, H, screen;
+    float sky[3];
+    int max_depth, num_lights, light_tri_count;
+    int use_vm, use_vc;
+    uint32_t light_seed, eye_seed, frame_num, accumulate;
+    float radius;
+    float mn[3], mx[3];
+    int res[3];
+    float4* verts;           // screen * (max_depth + 1) vertices
+    uint32_t* counts;        // stored vertices per light subpath
+    float* splat;            // screen * 3, pixel x * H + y
+    const uint32_t* g_count; // 10 * screen slots
+    const uint32_t* g_rep;
+    float4* film;            // RGBA32F, row-major
+};
+
+struct CamV {
+    v3 pos, nrm;
+    float area;
+};
+__device__ __forceinline__ CamV cam_setup(const VcmArgs& A) {
+    CamV c;
+    const float4 o = mat_vec(A.iv, 0.0f, 0.0f, 0.0f, 1.0f);
+    const float4 f = mat_vec(A.iv, 0.0f, 0.0f, 1.0f, 0.0f);
+    c.pos = V3(o.x, o.y, o.z);
+    c.nrm = V3(-f.x, -f.y, -f.z);
+    const float4 a = mat_vec(A.ip, 2.0f / (float)A.W, 2.0f / (float)A.H, 0.0f, 1.0f);
+    c.area = fabsf((a.x / a.w) * (a.y / a.w));
+    return c;
+}
+
+struct Etas { float vcm, vc, vm; };
+__device__ __forceinline__ Etas etas(const VcmArgs& A) {
+    const float r2 = A.radius * A.radius;
+    Etas e;
+    e.vcm = LGB_PI * r2 * (float)A.screen;
+    e.vc = A.use_vc == 1 ? 1.0f / e.vcm : 0.0f;
+    e.vm = A.use_vm == 1 ? LGB_PI * r2 * (float)A.screen : 0.0f;
+    return e;
+}
+
+__device__ __forceinline__ int3 grid_idx(v3 p, const float* mn, const float* mx, const int* res) {
+    const float nx = (p.x - mn[0]) / (mx[0] - mn[0]), ny = (p.y - mn[1]) / (mx[1] - mn[1]), nz = (p.z - mn[2]) / (mx[2] - mn[2]);
+    return make_int3(__float2int_rz(nx * (float)res[0]), __float2int_rz(ny * (float)res[1]), __float2int_rz(nz * (float)res[2]));
+}
+// utils.glsl:62-65 with the products wrapping as 32-bit integers
+__device__ __forceinline__ uint32_t grid_hash(int3 p, uint32_t screen) {
+    const uint32_t h = ((uint32_t)p.x * 73856093u) ^ ((uint32_t)p.y * 19349663u) ^ ((uint32_t)p.z * 83492791u);
+    return h % (10u * screen);
+}
+
+// Light vertex: (pos, area) (wi, d_vcm) (wo, d_vc) (n_s, d_vm) (throughput, u) (v, material, path_len, side)
+struct LVert {
+    v3 pos, wi, wo, n_s, thr;
+    float area, d_vcm, d_vc, d_vm, u, v;
+    uint32_t mat, path_len, side;
+};
+__device__ __forceinline__ void store_lvert(float4* p, const LVert& v) {
+    p[0] = f4(v.pos, v.area);
+    p[1] = f4(v.wi, v.d_vcm);
+    p[2] = f4(v.wo, v.d_vc);
+    p[3] = f4(v.n_s, v.d_vm);
+    p[4] = f4(v.thr, v.u);
+    p[5] = make_float4(v.v, __uint_as_float(v.mat), __uint_as_float(v.path_len), __uint_as_float(v.side));
+}
+__device__ __forceinline__ LVert load_lvert(const float4* p) {
+    LVert v;
+    const float4 a = p[0], b = p[1], c = p[2], d = p[3], e = p[4], g = p[5];
+    v.pos = V3(a.x, a.y, a.z); v.area = a.w;
+    v.wi = V3(b.x, b.y, b.z); v.d_vcm = b.w;
+    v.wo = V3(c.x, c.y, c.z); v.d_vc = c.w;
+    v.n_s = V3(d.x, d.y, d.z); v.d_vm = d.w;
+    v.thr = V3(e.x, e.y, e.z); v.u = e.w;
+    v.v = g.x; v.mat = __float_as_uint(g.y); v.path_len = __float_as_uint(g.z); v.side = __float_as_uint(g.w);
+    return v;
+}
+
+__device__ __forceinline__ bool is_zero3(v3 a) { return a.x == 0.0f && a.y == 0.0f && a.z == 0.0f; }
+__device__ __forceinline__ bool light_finite(uint32_t f) { return ((f >> 4) & 1u) != 0u; }
+__device__ __forceinline__ bool light_delta(uint32_t f) { return ((f >> 5) & 1u) != 0u; }
+
+// commons.glsl:112-149 with an identity world matrix
+__device__ __forceinline__ void sample_tri(const SceneView& S, const lgb_mesh& pm, uint32_t tri, float rx, float ry, v3& pos,
+                                           v3& n, float& tri_pdf) {
+    const uint32_t io = pm.index_offset + 3u * tri;
+    const DevVertex a = S.verts[S.idx[io] + pm.vertex_offset];
+    const DevVertex b = S.verts[S.idx[io + 1] + pm.vertex_offset];
+    const DevVertex c = S.verts[S.idx[io + 2] + pm.vertex_offset];
+    const float su = 1.0f - sqrtf(rx), sv = ry * sqrtf(rx);
+    const float b0 = 1.0f - su - sv;
+    const v3 v0 = V3(a.px, a.py, a.pz), v1 = V3(b.px, b.py, b.pz), v2 = V3(c.px, c.py, c.pz);
+    pos = v0 * b0 + v1 * su + v2 * sv;
+    n = normalize(normalize(V3(a.nx, a.ny, a.nz) * b0 + V3(b.nx, b.ny, b.nz) * su + V3(c.nx, c.ny, c.nz) * sv));
+    tri_pdf = 2.0f / length(cross(v1 - v0, v2 - v0));
+}
+
+struct Emission {
+    v3 L, pos, wi;
+    float cos_from_light, pdf_pos_a, pdf_dir_w;
+    uint32_t flags;
+};
+
+// sample_light_Le (commons.glsl:335-406), area and spot lights
+__device__ Emission sample_light_Le(const SceneView& S, const VcmArgs& A, float r0, float r1, float r2, float r3, float d0, float d1) {
+    Emission e;
+    const uint32_t li = (uint32_t)(r0 * (float)A.num_lights);
+    const lgb_light* L = &S.lights[li];
+    e.L = V3(0.0f); e.pos = V3(0.0f); e.wi = V3(0.0f);
+    e.cos_from_light = 0.0f; e.pdf_pos_a = 0.0f; e.pdf_dir_w = 0.0f;
+    e.flags = L->light_flags;
+    const uint32_t type = L->light_flags & 7u;
+    if (type == LGB_LIGHT_AREA) {
+        const lgb_mesh pm = S.meshes[L->prim_mesh_idx];
+        const uint32_t tri = (uint32_t)(r1 * (float)L->num_triangles);
+        v3 n;
+        float tri_pdf;
+        sample_tri(S, pm, tri, r2, r3, e.pos, n, tri_pdf);
+        const lgb_material* lm = &S.mats[pm.material_index];
+        v3 T, B;
+        branchless_onb(n, T, B);
+        e.wi = to_world(sample_hemisphere(V2(d0, d1)), T, B, n);
+        e.L = V3(lm->emissive_factor[0], lm->emissive_factor[1], lm->emissive_factor[2]);
+        e.cos_from_light = fmaxf(dot(n, e.wi), 0.0f);
+        e.pdf_pos_a = tri_pdf;
+        e.pdf_dir_w = dot(e.wi, n) / LGB_PI;
+    } else if (type == LGB_LIGHT_SPOT) {
+        const float cos_width = cosf(30.0f * LGB_PI / 180.0f);
+        const float cos_faloff = cosf(25.0f * LGB_PI / 180.0f);
+        const v3 lp = V3(L->pos[0], L->pos[1], L->pos[2]);
+        const v3 ldir = normalize(V3(L->to[0], L->to[1], L->to[2]) - lp);
+        // to_local_quat (utils.glsl:157-160), then invert_quat and rot_quat (utils.glsl:167-172)
+        float qx = 1.0f, qy = 0.0f, qz = 0.0f, qw = 0.0f;
+        if (!(ldir.z < -0.99999f)) {
+            qx = ldir.y; qy = -ldir.x; qz = 0.0f; qw = 1.0f + ldir.z;
+            const float len = sqrtf(qx * qx + qy * qy + qz * qz + qw * qw);
+            qx = qx / len; qy = qy / len; qz = qz / len; qw = qw / len;
+        }
+        const v3 a = V3(-qx, -qy, -qz);
+        const float ct = (1.0f - d0) + d0 * cos_width;
+        const float st = sqrtf(1.0f - ct * ct);
+        const float phi = d1 * LGB_TWO_PI;
+        const v3 cone = V3(cosf(phi) * st, sinf(phi) * st, ct);
+        e.wi = 2.0f * dot(a, cone) * a + (qw * qw - dot(a, a)) * cone + 2.0f * qw * cross(a, cone);
+        e.pos = lp;
+        e.cos_from_light = dot(e.wi, ldir);
+        float fall;
+        if (e.cos_from_light < cos_width) fall = 0.0f;
+        else if (e.cos_from_light >= cos_faloff) fall = 1.0f;
+        else { const float d = (e.cos_from_light - cos_width) / (cos_faloff - cos_width); fall = (d * d) * (d * d); }
+        e.L = V3(L->L[0], L->L[1], L->L[2]) * fall;
+        e.pdf_pos_a = 1.0f;
+        e.pdf_dir_w = 1.0f / (LGB_TWO_PI * (1.0f - cos_width));
+    }
+    e.pdf_pos_a = e.pdf_pos_a / (float)A.light_tri_count;
+    return e;
+}
+
+struct Incidence {
+    v3 L, wi;
+    float wi_len, pdf_pos_w, pdf_pos_dir_w, cos_y;
+    uint32_t flags;
+};
+
+// sample_light_Li with the positional-directional pdf (commons.glsl:224-300), area and spot lights
+__device__ Incidence sample_light_Li_vcm(const SceneView& S, const VcmArgs& A, float r0, float r1, float r2, float r3, v3 p) {
+    Incidence r;
+    const uint32_t li = (uint32_t)(r0 * (float)A.num_lights);
+    const lgb_light* L = &S.lights[li];
+    r.L = V3(0.0f); r.wi = V3(0.0f); r.wi_len = 0.0f; r.pdf_pos_w = 0.0f; r.pdf_pos_dir_w = 0.0f; r.cos_y = 0.0f;
+    r.flags = L->light_flags;
+    const uint32_t type = L->light_flags & 7u;
+    if (type == LGB_LIGHT_AREA) {
+        const lgb_mesh pm = S.meshes[L->prim_mesh_idx];
+        const uint32_t tri = (uint32_t)(r1 * (float)L->num_triangles);
+        v3 pos, n;
+        float tri_pdf;
+        sample_tri(S, pm, tri, r2, r3, pos, n, tri_pdf);
+        const lgb_material* lm = &S.mats[pm.material_index];
+        v3 wi = pos - p;
+        const float l2 = dot(wi, wi);
+        r.wi_len = sqrtf(l2);
+        wi = wi / r.wi_len;
+        r.wi = wi;
+        r.cos_y = fabsf(dot(n, -wi));
+        r.L = V3(lm->emissive_factor[0], lm->emissive_factor[1], lm->emissive_factor[2]);
+        r.pdf_pos_w = tri_pdf * l2 / r.cos_y;
+        r.pdf_pos_dir_w = r.cos_y * LGB_INV_PI * tri_pdf;
+    } else if (type == LGB_LIGHT_SPOT) {
+        const v3 lp = V3(L->pos[0], L->pos[1], L->pos[2]);
+        v3 wi = lp - p;
+        const float l2 = dot(wi, wi);
+        r.wi_len = sqrtf(l2);
+        wi = wi / r.wi_len;
+        r.wi = wi;
+        const v3 ldir = normalize(V3(L->to[0], L->to[1], L->to[2]) - lp);
+        r.cos_y = dot(-wi, ldir);
+        const float cos_width = cosf(LGB_PI / 6.0f), cos_faloff = cosf(25.0f * LGB_PI / 180.0f);
+        float fall;
+        if (r.cos_y < cos_width) fall = 0.0f;
+        else if (r.cos_y >= cos_faloff) fall = 1.0f;
+        else { const float d = (r.cos_y - cos_width) / (cos_faloff - cos_width); fall = (d * d) * (d * d); }
+        r.pdf_pos_w = l2;
+        r.pdf_pos_dir_w = 1.0f / (LGB_TWO_PI * (1.0f - cos_width));
+        r.L = V3(L->L[0], L->L[1], L->L[2]) * fall;
+    }
+    return r;
+}
+
+struct VState {
+    v3 pos, wi, thr;
+    float d_vcm, d_vc, d_vm;
+};
+
+// vcm_connect_cam (vcm_commons.glsl:24-75): the splat of a light vertex and its pixel (have = false: none).
+__device__ v3 connect_cam(const SceneView& S, const VcmArgs& A, const CamV& c, v3 n_s, v3 payload_ns, v3 pos,
+                          const VState& st, float eta_vm, v3 wo, const Mat& mat, uint32_t& pidx, bool& have) {
+    have = false;
+    v3 L = V3(0.0f);
+    v3 dir = c.pos - pos;
+    const float len = length(dir);
+    dir = dir / len;
+    const float cos_y = dot(dir, n_s);
+    const float cos_theta = dot(c.nrm, -dir);
+    if (cos_theta <= 0.0f) return L;
+    const float cos3 = cos_theta * cos_theta * cos_theta;
+    const float screen = (float)A.screen;
+    const float ratio = fabsf(cos_y) / (c.area * cos3 * len * len);
+    const v3 origin = offset_ray2(pos, n_s);
+    float pdf_fwd, pdf_rev;
+    const v3 f = eval_bsdf_rev(n_s, wo, mat, dot(payload_ns, wo) > 0.0f, dir, pdf_fwd, pdf_rev, true);
+    if (is_zero3(f)) return L;
+    if (ratio > 0.0f) {
+        const RayQ q = make_rayq(origin.x, origin.y, origin.z, 0.0f, dir.x, dir.y, dir.z, len - kEpsV);
+        if (!trace_any_single(S.nodes, S.tris, q, S.status)) {
+            const float w_light = (ratio / screen) * (eta_vm + st.d_vcm + pdf_rev * st.d_vc);
+            const float mis = 1.0f / (1.0f + w_light);
+            L = mis * st.thr * ratio * f / screen;
+        }
+    }
+    dir = -dir;
+    float4 t = mat_vec(A.view, dir.x, dir.y, dir.z, 0.0f);
+    t = make_float4(t.x / t.z, t.y / t.z, t.z / t.z, t.w / t.z);
+    t = mat_vec(A.proj, t.x, t.y, t.z, t.w);
+    t = make_float4(-t.x, -t.y, -t.z, -t.w);
+    const int cx = __float2int_rz(0.5f * (1.0f + t.x) * (float)A.W - 0.5f);
+    const int cy = __float2int_rz(0.5f * (1.0f + t.y) * (float)A.H - 0.5f);
+    if (cx < 0 || cx >= (int)A.W || cy < 0 || cy >= (int)A.H || dot(dir, c.nrm) < 0.0f) return V3(0.0f);
+    have = true;
+    pidx = (uint32_t)cx * A.H + (uint32_t)cy;
+    return L;
+}
+
+// vcm_light.rgen main: one light subpath per launch point (x, y), stored at x * H + y.
+__global__ void __launch_bounds__(kVcmThreads) k_vcm_light(SceneView S, VcmArgs A) {
+    const CamV cam = cam_setup(A);
+    const Etas eta = etas(A);
+    const uint32_t per = (uint32_t)(A.max_depth + 1);
+    for (uint32_t li = blockIdx.x * blockDim.x + threadIdx.x; li < A.screen; li += gridDim.x * blockDim.x) {
+        const uint32_t x = li / A.H, y = li % A.H;
+        float4* lv = A.verts + (size_t)li * per * kVertexF4;
+        uint4 seed = make_uint4(x, y, A.light_seed, 0u);
+        const float r0 = rnd(seed), r1 = rnd(seed), r2 = rnd(seed), r3 = rnd(seed);
+        const float d0 = rnd(seed), d1 = rnd(seed);
+        const Emission e = sample_light_Le(S, A, r0, r1, r2, r3, d0, d1);
+        if (e.pdf_dir_w <= 0.0f) {
+            A.counts[li] = 0u;
+            continue;
+        }
+        VState st;
+        const float pdf_emit = e.pdf_pos_a * e.pdf_dir_w;
+        st.pos = e.pos;
+        st.wi = e.wi;
+        st.thr = e.L * e.cos_from_light / (e.pdf_dir_w * e.pdf_pos_a);
+        st.d_vcm = e.pdf_pos_a / pdf_emit;
+        const bool finite = light_finite(e.flags);
+        st.d_vc = light_delta(e.flags) ? 0.0f : (finite ? e.cos_from_light : 1.0f) / (e.pdf_dir_w * e.pdf_pos_a);
+        st.d_vm = st.d_vc * eta.vc;
+        uint32_t path_idx = 0;
+        for (int depth = 1; depth <= A.max_depth; depth++) {
+            float t, bu, bv;
+            const RayQ q = make_rayq(st.pos.x, st.pos.y, st.pos.z, kTMinV, st.wi.x, st.wi.y, st.wi.z, kTMaxV);
+            const uint32_t prim = trace_closest_single(S.nodes, S.tris, q, t, bu, bv, S.status);
+            if (prim == LGB_NO_HIT) break;
+            const HitAttr h = resolve_hit(S, prim, bu, bv);
+            v3 wo = st.pos - h.pos;
+            v3 n_s = h.n_s, n_g = h.n_g;
+            bool side = true;
+            if (dot(h.n_g, wo) <= 0.0f) n_g = -n_g;
+            if (dot(n_g, n_s) < 0.0f) { n_s = -n_s; side = false; }
+            const float dist = length(h.pos - st.pos);
+            const float dist_sqr = dist * dist;
+            wo = wo / dist;
+            const Mat mat = load_material(S, h.mat, h.u, h.v);
+            const bool spec = (mat.props & LGB_FLAG_SPECULAR) == LGB_FLAG_SPECULAR;
+            const float cos_wo = fabsf(dot(wo, n_s));
+            if (depth > 1 || finite) st.d_vcm *= dist_sqr;
+            st.d_vcm /= cos_wo;
+            st.d_vc /= cos_wo;
+            st.d_vm /= cos_wo;
+            if (!spec && (A.use_vc == 1 || A.use_vm == 1)) {
+                LVert v;
+                v.pos = h.pos; v.area = h.area; v.wi = st.wi; v.d_vcm = st.d_vcm; v.wo = wo; v.d_vc = st.d_vc;
+                v.n_s = n_s; v.d_vm = st.d_vm; v.thr = st.thr; v.u = h.u; v.v = h.v; v.mat = h.mat;
+                v.path_len = (uint32_t)depth + 1u; v.side = side ? 1u : 0u;
+                store_lvert(lv + (size_t)path_idx * kVertexF4, v);
+                path_idx++;
+            }
+            if (depth >= A.max_depth) break;
+            if (!spec && A.use_vc == 1) {
+                uint32_t pidx = 0;
+                bool have = false;
+                const v3 L = connect_cam(S, A, cam, n_s, h.n_s, h.pos, st, eta.vm, wo, mat, pidx, have);
+                if (luminance(L) > 0.0f && have) {
+                    atomicAdd(&A.splat[3 * pidx], L.x);
+                    atomicAdd(&A.splat[3 * pidx + 1], L.y);
+                    atomicAdd(&A.splat[3 * pidx + 2], L.z);
+                }
+            }
+            const float c0 = rnd(seed), c1 = rnd(seed), c2 = rnd(seed);
+            float pdf_dir, cos_t;
+            v3 wi;
+            const v3 f = sample_bsdf_mode(n_s, wo, mat, 0u, side, wi, pdf_dir, cos_t, V3(c0, c1, c2));
+            st.wi = wi;
+            const bool same = dot(st.wi, n_s) > 0.0f && dot(wo, n_s) > 0.0f;
+            const bool trans = (mat.props & LGB_FLAG_TRANSMISSION) == LGB_FLAG_TRANSMISSION;
+            if (is_zero3(f) || pdf_dir == 0.0f || (!same && !trans)) break;
+            float pdf_rev = pdf_dir;
+            if (!spec) pdf_rev = bsdf_pdf(mat, n_s, st.wi, wo, side);
+            const float ac = fabsf(cos_t);
+            st.pos = offset_ray(h.pos, n_g);
+            if (!spec) {
+                st.d_vc = (ac / pdf_dir) * (eta.vm + st.d_vcm + pdf_rev * st.d_vc);
+                st.d_vm = (ac / pdf_dir) * (1.0f + st.d_vcm * eta.vc + pdf_rev * st.d_vm);
+                st.d_vcm = 1.0f / pdf_dir;
+            } else {
+                st.d_vcm = 0.0f;
+                st.d_vc *= ac;
+                st.d_vm *= ac;
+            }
+            st.thr = st.thr * (f * ac / pdf_dir);
+        }
+        A.counts[li] = path_idx;
+    }
+}
+
+struct EyeHit {
+    v3 pos, ns_payload;
+    float area;
+};
+
+// vcm_connect_light (vcm_commons.glsl:146-204)
+__device__ v3 connect_light(const SceneView& S, const VcmArgs& A, uint4& seed, const EyeHit& h, v3 n_s, v3 wo, const Mat& mat,
+                            bool side, float eta_vm, const VState& cs, float& pdf_rev) {
+    v3 res = V3(0.0f);
+    const float q0 = rnd(seed), q1 = rnd(seed), q2 = rnd(seed), q3 = rnd(seed);
+    const Incidence li = sample_light_Li_vcm(S, A, q0, q1, q2, q3, h.pos);
+    const float cos_x = dot(li.wi, n_s);
+    const v3 origin = offset_ray2(h.pos, n_s);
+    float pdf_fwd;
+    const v3 f = eval_bsdf_rev(n_s, wo, mat, side, li.wi, pdf_fwd, pdf_rev, true);
+    if (!is_zero3(f)) {
+        const RayQ q = make_rayq(origin.x, origin.y, origin.z, 0.0f, li.wi.x, li.wi.y, li.wi.z, li.wi_len - kEpsV);
+        if (!trace_any_single(S.nodes, S.tris, q, S.status)) {
+            if (light_delta(li.flags)) pdf_fwd = 0.0f;
+            const float ltc = (float)A.light_tri_count;
+            const float w_light = pdf_fwd / (li.pdf_pos_w / ltc);
+            const float w_cam = li.pdf_pos_dir_w * fabsf(cos_x) / (li.pdf_pos_w * li.cos_y) *
+                                (eta_vm + cs.d_vcm + cs.d_vc * pdf_rev);
+            const float mis = 1.0f / (1.0f + w_light + w_cam);
+            if (mis > 0.0f) res = mis * fabsf(cos_x) * f * cs.thr * li.L / (li.pdf_pos_w / ltc);
+        }
+    }
+    return res;
+}
+
+// vcm_connect_light_vertices (vcm_commons.glsl:206-251)
+__device__ v3 connect_light_vertices(const SceneView& S, const VcmArgs& A, const float4* lv, uint32_t len_path, int depth,
+                                     const EyeHit& h, v3 n_s, v3 wo, const Mat& mat, bool side, float eta_vm,
+                                     const VState& cs, float pdf_rev) {
+    v3 res = V3(0.0f);
+    for (uint32_t i = 0; i < len_path; i++) {
+        const LVert v = load_lvert(lv + (size_t)i * kVertexF4);
+        if (v.path_len + (uint32_t)depth - 1u >= (uint32_t)A.max_depth) break;
+        v3 dir = v.pos - h.pos;
+        const float len = length(dir);
+        const float len_sqr = len * len;
+        dir = dir / len;
+        const float cos_cam = dot(n_s, dir);
+        const float cos_light = dot(v.n_s, -dir);
+        const float G = cos_light * cos_cam / len_sqr;
+        if (!(G > 0.0f)) continue;
+        float cam_pdf_fwd, unused, light_pdf_fwd, light_pdf_rev;
+        const v3 f_cam = eval_bsdf_rev(n_s, wo, mat, side, dir, cam_pdf_fwd, unused, false);
+        const Mat lm = load_material(S, v.mat, v.u, v.v);
+        const v3 f_light = eval_bsdf_rev(v.n_s, v.wo, lm, v.side == 1u, -dir, light_pdf_fwd, light_pdf_rev, true);
+        if (is_zero3(f_light) || is_zero3(f_cam)) continue;
+        cam_pdf_fwd *= fabsf(cos_light) / len_sqr;
+        light_pdf_fwd *= fabsf(cos_cam) / len_sqr;
+        const float w_light = cam_pdf_fwd * (eta_vm + v.d_vcm + light_pdf_rev * v.d_vc);
+        const float w_camera = light_pdf_fwd * (eta_vm + cs.d_vcm + pdf_rev * cs.d_vc);
+        const float mis = 1.0f / (1.0f + w_camera + w_light);
+        const v3 origin = offset_ray2(h.pos, n_s);
+        const RayQ q = make_rayq(origin.x, origin.y, origin.z, 0.0f, dir.x, dir.y, dir.z, len - kEpsV);
+        if (!trace_any_single(S.nodes, S.tris, q, S.status)) {
+            const v3 c = mis * G * cs.thr * v.thr * f_cam * f_light;
+            res = A.accumulate ? res + c : c;
+        }
+    }
+    return res;
+}
+
+// vcm_merge_light_vertices (vcm_commons.glsl:254-296) over the slot table (count, representative photon)
+__device__ v3 merge(const VcmArgs& A, int depth, const EyeHit& h, v3 n_s, v3 wo, const Mat& mat, bool side, float eta_vc,
+                    const VState& cs, float norm) {
+    const float radius = A.radius;
+    const float r_sqr = radius * radius;
+    v3 res = V3(0.0f);
+    const int3 lo = grid_idx(h.pos - V3(radius), A.mn, A.mx, A.res);
+    const int3 hi = grid_idx(h.pos + V3(radius), A.mn, A.mx, A.res);
+    if ((long long)hi.x - lo.x >= kMaxMergeCells || (long long)hi.y - lo.y >= kMaxMergeCells ||
+        (long long)hi.z - lo.z >= kMaxMergeCells)
+        return res;
+    for (int x = lo.x; x <= hi.x; x++)
+        for (int y = lo.y; y <= hi.y; y++)
+            for (int z = lo.z; z <= hi.z; z++) {
+                const uint32_t slot = grid_hash(make_int3(x, y, z), A.screen);
+                const uint32_t count = A.g_count[slot];
+                if (count == 0u) continue;
+                const LVert ph = load_lvert(A.verts + (size_t)A.g_rep[slot] * kVertexF4);
+                const v3 pp = h.pos - ph.pos;
+                const float dist_sqr = dot(pp, pp);
+                if (dist_sqr > r_sqr) continue;
+                if (ph.path_len + (uint32_t)depth - 1u > (uint32_t)A.max_depth) continue;
+                const v3 pwi = -ph.wi;
+                float cam_pdf_fwd, cam_pdf_rev;
+                const v3 f = eval_bsdf_rev(n_s, wo, mat, side, pwi, cam_pdf_fwd, cam_pdf_rev, true);
+                if (is_zero3(f)) continue;
+                const float w_light = ph.d_vcm * eta_vc + ph.d_vm * cam_pdf_fwd;
+                const float w_cam = cs.d_vcm * eta_vc + cs.d_vm * cam_pdf_rev;
+                const float mis = 1.0f / (1.0f + w_light + w_cam);
+                if (dot(ph.n_s, n_s) > kEpsV) {
+                    const float w = 1.0f - sqrtf(dist_sqr) / radius;
+                    const v3 c = w * mis * (float)(int)count * ph.thr * f * cs.thr * norm * 3.0f;
+                    res = A.accumulate ? res + c : c;
+                }
+            }
+    return res;
+}
+
+// vcm_eye.rgen main + vcm_trace_eye for pixel (x, y): film[y * W + x], consumes the pixel's splat.
+__global__ void __launch_bounds__(kVcmThreads) k_vcm_eye(SceneView S, VcmArgs A) {
+    const CamV cam = cam_setup(A);
+    const Etas eta = etas(A);
+    const float norm = 1.0f / (LGB_PI * A.radius * A.radius * (float)A.screen);
+    const uint32_t per = (uint32_t)(A.max_depth + 1);
+    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < A.screen; pix += gridDim.x * blockDim.x) {
+        const uint32_t x = pix % A.W, y = pix / A.W;
+        uint4 seed = make_uint4(x, y, A.eye_seed, 0u);
+        const float j0 = rnd(seed), j1 = rnd(seed);
+        const float u = ((float)x + 0.5f + (j0 - 0.5f)) / (float)A.W, v = ((float)y + 0.5f + (j1 - 0.5f)) / (float)A.H;
+        const float dx = u * 2.0f - 1.0f, dy = v * 2.0f - 1.0f;
+        const float4 t4 = mat_vec(A.ip, dx, dy, 1.0f, 1.0f);
+        const v3 tn = normalize(V3(t4.x, t4.y, t4.z));
+        const float4 d4 = mat_vec(A.iv, tn.x, tn.y, tn.z, 0.0f);
+        VState cs;
+        cs.wi = V3(d4.x, d4.y, d4.z);
+        cs.pos = cam.pos;
+        cs.thr = V3(1.0f);
+        const float ct0 = fabsf(dot(cam.nrm, cs.wi));
+        cs.d_vcm = cam.area * (float)A.screen * ct0 * ct0 * ct0;
+        cs.d_vc = 0.0f;
+        cs.d_vm = 0.0f;
+        // uint(rand * screen) (vcm_commons.glsl:518) can round up to screen for large images: clamped
+        const uint32_t lp = min((uint32_t)(rnd(seed) * (float)A.screen), A.screen - 1u);
+        const uint32_t lp_len = A.counts[lp];
+        const float4* lv = A.verts + (size_t)lp * per * kVertexF4;
+        v3 col = V3(0.0f);
+        for (int depth = 1; depth <= A.max_depth; depth++) {
+            float t, bu, bv;
+            const RayQ q = make_rayq(cs.pos.x, cs.pos.y, cs.pos.z, kTMinV, cs.wi.x, cs.wi.y, cs.wi.z, kTMaxV);
+            const uint32_t prim = trace_closest_single(S.nodes, S.tris, q, t, bu, bv, S.status);
+            if (prim == LGB_NO_HIT) {
+                col = col + cs.thr * V3(A.sky[0], A.sky[1], A.sky[2]);
+                break;
+            }
+            const HitAttr h = resolve_hit(S, prim, bu, bv);
+            v3 wo = cs.pos - h.pos;
+            const float dist = length(h.pos - cs.pos);
+            const float dist_sqr = dist * dist;
+            wo = wo / dist;
+            v3 n_s = h.n_s, n_g = h.n_g;
+            bool side = true;
+            if (dot(h.n_g, wo) < 0.0f) n_g = -n_g;
+            if (dot(n_g, n_s) < 0.0f) { n_s = -n_s; side = false; }
+            const float cos_wo = fabsf(dot(wo, n_s));
+            const Mat mat = load_material(S, h.mat, h.u, h.v);
+            const bool spec = (mat.props & LGB_FLAG_SPECULAR) == LGB_FLAG_SPECULAR;
+            cs.d_vcm *= dist_sqr;
+            cs.d_vcm /= cos_wo;
+            cs.d_vc /= cos_wo;
+            cs.d_vm /= cos_wo;
+            const EyeHit eh{h.pos, h.n_s, h.area};
+            if (luminance(mat.emissive) > 0.0f) {  // vcm_get_light_radiance (vcm_commons.glsl:132-144)
+                v3 Le = mat.emissive;
+                if (depth != 1) {
+                    const float pdf_light_pos = 1.0f / (eh.area * (float)A.light_tri_count);
+                    const float pdf_light_dir = fabsf(dot(eh.ns_payload, -cs.wi)) / LGB_PI;
+                    const float w_camera = pdf_light_pos * cs.d_vcm +
+                                           ((A.use_vc == 1 || A.use_vm == 1) ? (pdf_light_pos * pdf_light_dir) * cs.d_vc : 0.0f);
+                    Le = (1.0f / (1.0f + w_camera)) * mat.emissive;
+                }
+                col = col + cs.thr * Le;
+            }
+            float pdf_rev = 0.0f;
+            if (!spec && depth < A.max_depth) col = col + connect_light(S, A, seed, eh, n_s, wo, mat, side, eta.vm, cs, pdf_rev);
+            if (!spec) col = col + connect_light_vertices(S, A, lv, lp_len, depth, eh, n_s, wo, mat, side, eta.vm, cs, pdf_rev);
+            if (!spec && A.use_vm == 1) col = col + merge(A, depth, eh, n_s, wo, mat, side, eta.vc, cs, norm);
+            if (depth >= A.max_depth) break;
+            const float c0 = rnd(seed), c1 = rnd(seed), c2 = rnd(seed);
+            float pdf_dir, cos_t;
+            v3 wi;
+            const v3 f = sample_bsdf_mode(n_s, wo, mat, 1u, side, wi, pdf_dir, cos_t, V3(c0, c1, c2));
+            cs.wi = wi;
+            const bool trans = (mat.props & LGB_FLAG_TRANSMISSION) == LGB_FLAG_TRANSMISSION;
+            const bool same = dot(cs.wi, n_s) > 0.0f && dot(wo, n_s) > 0.0f;
+            if (is_zero3(f) || pdf_dir == 0.0f || (!same && !trans)) break;
+            pdf_rev = pdf_dir;
+            if (!spec) pdf_rev = bsdf_pdf(mat, n_s, cs.wi, wo, side);
+            const float ac = fabsf(cos_t);
+            cs.pos = offset_ray(h.pos, n_g);
+            if (!spec) {
+                cs.d_vc = (ac / pdf_dir) * (eta.vm + cs.d_vcm + pdf_rev * cs.d_vc);
+                cs.d_vm = (ac / pdf_dir) * (1.0f + cs.d_vcm * eta.vc + pdf_rev * cs.d_vm);
+                cs.d_vcm = 1.0f / pdf_dir;
+            } else {
+                cs.d_vcm = 0.0f;
+                cs.d_vc *= ac;
+                cs.d_vm *= ac;
+            }
+            cs.thr = cs.thr * (f * ac / pdf_dir);
+        }
+        if (isnan(luminance(col))) continue;  // vcm_eye.rgen:80-83: no film write, the splat stays
+        const uint32_t sidx = x * A.H + y;
+        col = col + V3(A.splat[3 * sidx], A.splat[3 * sidx + 1], A.splat[3 * sidx + 2]);
+        A.splat[3 * sidx] = 0.0f;
+        A.splat[3 * sidx + 1] = 0.0f;
+        A.splat[3 * sidx + 2] = 0.0f;
+        float4 px = A.film[pix];
+        if (A.frame_num > 0u) {
+            const float w = 1.0f / (float)(A.frame_num + 1u);
+            px = make_float4(mixf(px.x, col.x, w), mixf(px.y, col.y, w), mixf(px.z, col.z, w), 1.0f);
+        } else {
+            px = make_float4(col.x, col.y, col.z, 1.0f);
+        }
+        A.film[pix] = px;
+    }
+}
+
+// Photon table by sort and scan. Keys: the slot of every stored light vertex; unused vertex slots get the
+// table size and sort after every real slot. Values: the vertex id, so the stable sort keeps id order inside
+// a slot and the run's last element is the highest id (the sequential last writer).
+__global__ void k_vcm_keys(VcmArgs A, uint32_t table, uint64_t* keys, uint32_t* vals) {
+    const uint32_t per = (uint32_t)(A.max_depth + 1);
+    const uint32_t n = A.screen * per;
+    for (uint32_t vid = blockIdx.x * blockDim.x + threadIdx.x; vid < n; vid += gridDim.x * blockDim.x) {
+        const uint32_t li = vid / per, k = vid % per;
+        uint32_t key = table;
+        if (k < A.counts[li]) {
+            const float4 p = A.verts[(size_t)vid * kVertexF4];
+            key = grid_hash(grid_idx(V3(p.x, p.y, p.z), A.mn, A.mx, A.res), A.screen);
+        }
+        keys[vid] = key;
+        vals[vid] = vid;
+    }
+}
+
+// Keys of n photon positions (w < 0: unused), for the stand-alone table builder.
+__global__ void k_vcm_keys_pos(const float4* __restrict__ pos, uint32_t n, float mn0, float mn1, float mn2, float mx0,
+                               float mx1, float mx2, int r0, int r1, int r2, uint32_t screen, uint64_t* keys, uint32_t* vals) {
+    const float mn[3] = {mn0, mn1, mn2}, mx[3] = {mx0, mx1, mx2};
+    const int res[3] = {r0, r1, r2};
+    const uint32_t table = 10u * screen;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 p = pos[i];
+        keys[i] = p.w < 0.0f ? table : grid_hash(grid_idx(V3(p.x, p.y, p.z), mn, mx, res), screen);
+        vals[i] = i;
+    }
+}
+
+// Run starts: rep[slot] = first sorted position (temporarily).
+__global__ void k_vcm_run_first(const uint64_t* __restrict__ keys, uint32_t n, uint32_t table, uint32_t* rep) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint64_t k = keys[i];
+        if (k >= table) continue;
+        if (i == 0 || keys[i - 1] != k) rep[k] = i;
+    }
+}
+// Run ends: count = length of the run, rep = its last vertex id.
+__global__ void k_vcm_run_last(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t n,
+                               uint32_t table, uint32_t* count, uint32_t* rep) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint64_t k = keys[i];
+        if (k >= table) continue;
+        if (i == n - 1 || keys[i + 1] != k) {
+            count[k] = i - rep[k] + 1u;
+            rep[k] = vals[i];
+        }
+    }
+}
+
+int to_int_rz_host(float x) {
+    if (x != x) return 0;
+    if (x >= 2147483648.0f) return INT32_MAX;
+    if (x <= -2147483648.0f) return INT32_MIN;
+    return (int)x;
+}
+
+// VCM.cpp:144-147
+void grid_resolution(const float* mn, const float* mx, float radius, int* res) {
+    const float d[3] = {mx[0] - mn[0], mx[1] - mn[1], mx[2] - mn[2]};
+    const float max_comp = std::max(d[0], std::max(d[1], d[2]));
+    const int base = to_int_rz_host(max_comp / radius);
+    for (int k = 0; k < 3; k++) res[k] = std::max(to_int_rz_host(d[k] * (float)base / max_comp), 1);
+}
+
+int sort_passes(uint32_t table) {
+    int bits = 0;
+    while (bits < 32 && (uint64_t)table >= (1ull << bits)) bits++;
+    return (bits + 7) / 8;
+}
+
+int vcm_grid_blocks(Ctx* ctx, uint64_t n) {
+    const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, (uint64_t)sms * 16));
+}
+
+// Sorts (keys, vals) in place (k0/v0 end up holding the result) and writes the table (count and rep zeroed first).
+lgb_status build_table(Ctx* ctx, uint64_t*& k0, uint32_t*& v0, uint64_t*& k1, uint32_t*& v1, uint32_t* sort_counts, uint32_t n,
+                       uint32_t table, uint32_t* count, uint32_t* rep, cudaStream_t st) {
+    LGB_CUDA_TRY(ctx, cudaMemsetAsync(count, 0, sizeof(uint32_t) * table, st));
+    LGB_CUDA_TRY(ctx, cudaMemsetAsync(rep, 0, sizeof(uint32_t) * table, st));
+    LGB_CUDA_TRY(ctx, radix_sort_pairs(k0, v0, k1, v1, sort_counts, n, sort_passes(table), st));
+    const int g = vcm_grid_blocks(ctx, n);
+    k_vcm_run_first<<<g, 256, 0, st>>>(k0, n, table, rep);
+    k_vcm_run_last<<<g, 256, 0, st>>>(k0, v0, n, table, count, rep);
+    LGB_CUDA_TRY(ctx, cudaGetLastError());
+    return LGB_OK;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Inverts a column-major 4x4 matrix in double (Gauss-Jordan with partial pivoting); false if singular.
+bool invert4(const float* in, double* out) {
+    double a[4][8];
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++) { a[r][c] = in[4 * c + r]; a[r][4 + c] = r == c ? 1.0 : 0.0; }
+    for (int c = 0; c < 4; c++) {
+        int piv = c;
+        for (int r = c + 1; r < 4; r++) if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+        if (a[piv][c] == 0.0) return false;
+        if (piv != c) for (int k = 0; k < 8; k++) std::swap(a[c][k], a[piv][k]);
+        const double inv = 1.0 / a[c][c];
+        for (int k = 0; k < 8; k++) a[c][k] *= inv;
+        for (int r = 0; r < 4; r++) {
+            if (r == c) continue;
+            const double f = a[r][c];
+            for (int k = 0; k < 8; k++) a[r][k] -= f * a[c][k];
+        }
+    }
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++) out[4 * c + r] = a[r][4 + c];
+    return true;
+}
+
+}  // namespace
+}  // namespace lgb
+
+using namespace lgb;
+
+extern "C" {
+
+LGB_API float lgb_vcm_radius(float scene_radius, float radius_factor, uint32_t iteration, float alpha) {
+    float r = scene_radius * radius_factor / 100.0f;
+    r /= (float)std::pow((double)iteration + 1.0, 0.5 * (1.0 - (double)alpha));
+    return r;
+}
+
+LGB_API lgb_status lgb_camera_forward(const lgb_camera* cam, float view[16], float projection[16]) {
+    if (!cam || !view || !projection) return LGB_ERR_INVALID_ARGUMENT;
+    double v[16], p[16];
+    if (!invert4(cam->inv_view, v) || !invert4(cam->inv_projection, p)) return LGB_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < 16; i++) { view[i] = (float)v[i]; projection[i] = (float)p[i]; }
+    return LGB_OK;
+}
+
+LGB_API lgb_status lgb_vcm_grid(lgb_ctx* ctx, const float* d_pos4, uint32_t n, const float scene_min[3],
+                                const float scene_max[3], float radius, uint32_t screen_size, uint32_t* d_count,
+                                uint32_t* d_rep, void* stream) {
+    if (!ctx) return LGB_ERR_INVALID_ARGUMENT;
+    if (!scene_min || !scene_max || !d_count || !d_rep || (n > 0 && !d_pos4) || (reinterpret_cast<uintptr_t>(d_pos4) & 15u))
+        return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "null or misaligned argument");
+    if (screen_size == 0 || screen_size > 0x0CCCCCCCu || !(radius > 0.0f) || !std::isfinite(radius))
+        return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "screen_size must be in [1, 2^32 / 20) and radius positive");
+    for (int k = 0; k < 3; k++)
+        if (!(scene_max[k] > scene_min[k])) return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "scene bounds are not a volume");
+    cudaSetDevice(ctx->device);
+    const cudaStream_t st = (cudaStream_t)stream;
+    const uint32_t table = 10u * screen_size;
+    int res[3];
+    grid_resolution(scene_min, scene_max, radius, res);
+    uint64_t *k0 = nullptr, *k1 = nullptr;
+    uint32_t *v0 = nullptr, *v1 = nullptr, *cnt = nullptr;
+    const uint32_t nb = std::max<uint32_t>(1u, (n + RS_TILE - 1) / RS_TILE);
+    lgb_status result = LGB_OK;
+    const size_t m = std::max<uint32_t>(n, 1u);
+    if (cudaMalloc(&k0, 8 * m) != cudaSuccess || cudaMalloc(&k1, 8 * m) != cudaSuccess || cudaMalloc(&v0, 4 * m) != cudaSuccess ||
+        cudaMalloc(&v1, 4 * m) != cudaSuccess || cudaMalloc(&cnt, sizeof(uint32_t) * 256 * nb) != cudaSuccess) {
+        result = set_error(ctx, LGB_ERR_OUT_OF_MEMORY, "photon table scratch");
+    } else {
+        if (n > 0)
+            k_vcm_keys_pos<<<vcm_grid_blocks(ctx, n), 256, 0, st>>>(reinterpret_cast<const float4*>(d_pos4), n, scene_min[0],
+                                                                 scene_min[1], scene_min[2], scene_max[0], scene_max[1],
+                                                                 scene_max[2], res[0], res[1], res[2], screen_size, k0, v0);
+        result = build_table(ctx, k0, v0, k1, v1, cnt, n, table, d_count, d_rep, st);
+        if (result == LGB_OK && cudaStreamSynchronize(st) != cudaSuccess)
+            result = cuda_error(ctx, cudaGetLastError(), "lgb_vcm_grid");
+    }
+    cudaFree(k0); cudaFree(k1); cudaFree(v0); cudaFree(v1); cudaFree(cnt);
+    return result;
+}
+
+LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const lgb_vcm_params* p, float* d_film,
+                                     void* stream) {
+    if (!s) return LGB_ERR_INVALID_ARGUMENT;
+    Ctx* ctx = s->ctx;
+    if (!cam || !p || !d_film || (reinterpret_cast<uintptr_t>(d_film) & 15u) || cam->width == 0 || cam->height == 0)
+        return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "null camera / params, empty image or misaligned film");
+    if (!s->bvh.nodes) return set_error(ctx, LGB_ERR_NOT_READY, "lgb_bvh_build has not been called");
+    if (p->max_depth < 1 || p->max_depth > 64) return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "max_depth must be in [1, 64]");
+    if (p->num_lights < 1 || (uint32_t)p->num_lights > s->num_lights || p->light_triangle_count <= 0)
+        return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "VCM needs 1..num_lights lights and a positive light_triangle_count");
+    if (p->dir_light_idx != 0xFFFFFFFFu || s->num_directional > 0)
+        return set_error(ctx, LGB_ERR_UNSUPPORTED, "VCM supports area and spot lights only");
+    if (!(p->radius > 0.0f) || !std::isfinite(p->radius)) return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "radius must be positive");
+    for (int k = 0; k < 3; k++)
+        if (!(p->scene_max[k] > p->scene_min[k])) return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "scene bounds are not a volume");
+    const uint64_t screen64 = (uint64_t)cam->width * cam->height;
+    const uint32_t per = (uint32_t)p->max_depth + 1u;
+    if (screen64 * per >= 0x80000000ull || screen64 * 10u >= 0x80000000ull)
+        return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "width * height * (max_depth + 1) must stay below 2^31");
+    const uint32_t screen = (uint32_t)screen64, nv = screen * per, table = 10u * screen;
+    cudaSetDevice(ctx->device);
+    const cudaStream_t st = (cudaStream_t)stream;
+    // state: vertices, counts, splats, table, sort scratch
+    const uint32_t nb = std::max<uint32_t>(1u, (nv + RS_TILE - 1) / RS_TILE);
+    size_t off = 0;
+    auto take = [&](size_t bytes) { const size_t o = off; off += align256(bytes); return o; };
+    const size_t o_verts = take(sizeof(float4) * kVertexF4 * (size_t)nv), o_counts = take(4ull * screen),
+                 o_splat = take(12ull * screen), o_gc = take(4ull * table), o_gr = take(4ull * table), o_k0 = take(8ull * nv),
+                 o_k1 = take(8ull * nv), o_v0 = take(4ull * nv), o_v1 = take(4ull * nv), o_sc = take(4ull * 256 * nb);
+    if (!s->vcm_buf || s->vcm_w != cam->width || s->vcm_h != cam->height || s->vcm_per != per || s->vcm_buf_bytes < off) {
+        cudaFree(s->vcm_buf);
+        s->vcm_buf = nullptr;
+        s->vcm_buf_bytes = 0;
+        LGB_CUDA_TRY(ctx, cudaMalloc(&s->vcm_buf, off));
+        LGB_CUDA_TRY(ctx, cudaMemsetAsync(s->vcm_buf, 0, off, st));
+        s->vcm_buf_bytes = off;
+        s->vcm_w = cam->width; s->vcm_h = cam->height; s->vcm_per = per;
+    }
+    char* base = (char*)s->vcm_buf;
+    VcmArgs A;
+    std::memset(&A, 0, sizeof(A));
+    for (int i = 0; i < 16; i++) { A.iv[i] = cam->inv_view[i]; A.ip[i] = cam->inv_projection[i]; }
+    LGB_CUDA_TRY(ctx, lgb_camera_forward(cam, A.view, A.proj) == LGB_OK ? cudaSuccess : cudaErrorInvalidValue);
+    A.W = cam->width; A.H = cam->height; A.screen = screen;
+    for (int k = 0; k < 3; k++) { A.sky[k] = p->sky_col[k]; A.mn[k] = p->scene_min[k]; A.mx[k] = p->scene_max[k]; }
+    A.max_depth = p->max_depth; A.num_lights = p->num_lights; A.light_tri_count = p->light_triangle_count;
+    A.use_vm = p->use_vm; A.use_vc = p->use_vc;
+    A.light_seed = p->light_seed; A.eye_seed = p->eye_seed; A.frame_num = p->frame_num;
+    A.accumulate = (p->flags & LGB_VCM_ACCUMULATE) ? 1u : 0u;
+    A.radius = p->radius;
+    grid_resolution(A.mn, A.mx, A.radius, A.res);
+    A.verts = reinterpret_cast<float4*>(base + o_verts);
+    A.counts = reinterpret_cast<uint32_t*>(base + o_counts);
+    A.splat = reinterpret_cast<float*>(base + o_splat);
+    uint32_t* gc = reinterpret_cast<uint32_t*>(base + o_gc);
+    uint32_t* gr = reinterpret_cast<uint32_t*>(base + o_gr);
+    A.g_count = gc;
+    A.g_rep = gr;
+    A.film = reinterpret_cast<float4*>(d_film);
+    const SceneView S = scene_view(s);
+    const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    const int grid = (int)std::min<uint32_t>((screen + kVcmThreads - 1) / kVcmThreads, (uint32_t)sms * 16u);
+    k_vcm_light<<<grid, kVcmThreads, 0, st>>>(S, A);
+    LGB_CUDA_TRY(ctx, cudaGetLastError());
+    if (p->use_vm == 1) {
+        uint64_t* k0 = reinterpret_cast<uint64_t*>(base + o_k0);
+        uint64_t* k1 = reinterpret_cast<uint64_t*>(base + o_k1);
+        uint32_t* v0 = reinterpret_cast<uint32_t*>(base + o_v0);
+        uint32_t* v1 = reinterpret_cast<uint32_t*>(base + o_v1);
+        k_vcm_keys<<<vcm_grid_blocks(ctx, nv), 256, 0, st>>>(A, table, k0, v0);
+        LGB_CUDA_TRY(ctx, cudaGetLastError());
+        const lgb_status ts = build_table(ctx, k0, v0, k1, v1, reinterpret_cast<uint32_t*>(base + o_sc), nv, table, gc, gr, st);
+        if (ts != LGB_OK) return ts;
+    } else {
+        LGB_CUDA_TRY(ctx, cudaMemsetAsync(gc, 0, 4ull * table, st));
+    }
+    k_vcm_eye<<<grid, kVcmThreads, 0, st>>>(S, A);
+    LGB_CUDA_TRY(ctx, cudaGetLastError());
+    return LGB_OK;
+}
+
+}  // extern "C"

@@ -12,6 +12,7 @@ fixes the arrays; tests that need bit-identical inputs on every host read them f
                        amplitude 0.1, plus 200 000 random small triangles in [-2, 2]^3.
   batch_scene()        displaced sphere + floor + boxes + 1-8 quad lights with principled / dielectric
                        materials (batched rendering); batch_config() draws the 32 scenes' sizes.
+  vcm_scene()          dielectric torus on a diffuse plane lit by a spot light (VCM caustics).
   primary_rays()       one ray per pixel centre of a pinhole camera.
   incoherent_rays()    origins area-uniform on the surfaces, cosine-distributed about a random side.
 """
@@ -374,6 +375,49 @@ def batch_config(seed: int = 0, n_scenes: int = 32, min_tris: int = 10_000, max_
         spp = int(round(math.exp(rng.uniform(math.log(min_spp), math.log(max_spp)))))
         out.append((1000 + i, tris, res, res, spp))
     return out
+
+
+def torus(R: float = 1.0, r: float = 0.35, n_major: int = 500, n_minor: int = 200, center=(0.0, 0.35, 0.0)):
+    """Torus around the y axis with smooth analytic normals: 2 * n_major * n_minor triangles, (T, 3, 3) vertices
+    and normals."""
+    u = np.arange(n_major + 1) * (2.0 * math.pi / n_major)
+    v = np.arange(n_minor + 1) * (2.0 * math.pi / n_minor)
+    U, V = np.meshgrid(u, v, indexing="ij")
+    cu, su, cv, sv = np.cos(U), np.sin(U), np.cos(V), np.sin(V)
+    pos = np.stack([(R + r * cv) * cu, r * sv, (R + r * cv) * su], -1) + np.asarray(center)
+    nrm = np.stack([cv * cu, sv, cv * su], -1)
+    i, j = np.meshgrid(np.arange(n_major), np.arange(n_minor), indexing="ij")
+    i, j = i.ravel(), j.ravel()
+    a, b, c, d = (i, j), (i + 1, j), (i + 1, j + 1), (i, j + 1)
+    tri_idx = [(a, c, b), (a, d, c)]
+    tris = np.concatenate([np.stack([pos[p0], pos[p1], pos[p2]], 1) for p0, p1, p2 in tri_idx])
+    nrms = np.concatenate([np.stack([nrm[p0], nrm[p1], nrm[p2]], 1) for p0, p1, p2 in tri_idx])
+    return tris, nrms
+
+
+def vcm_scene(n_major: int = 500, n_minor: int = 200) -> SceneArrays:
+    """The VCM caustics configuration: a smooth dielectric torus (IOR 1.5, R = 1, r = 0.35, 2 * n_major * n_minor
+    triangles, 200 000 by default) resting on a 10 x 10 diffuse plane (albedo 0.8), lit by a spot light of
+    intensity 100 at (0, 4, 1) aimed at the torus. Lumen's spot light has a fixed 30 degree cone with a 25 degree
+    falloff start (commons.glsl:264-265, 344-345): its Light record has no cone angle. Camera at (0, 3, 5)."""
+    from .scene import dielectric
+    b = _Builder()
+    mats = [diffuse((0.8, 0.8, 0.8)), dielectric(1.5, 0.0)]
+    t, n = _quad((-5, 0, -5), (5, 0, -5), (5, 0, 5), (-5, 0, 5), inward=(0, 1, 0))
+    b.add(t, n, 0)
+    t, n = torus(1.0, 0.35, n_major, n_minor)
+    b.add(t, n, 1)
+    lights = np.zeros(1, LIGHT_DTYPE)
+    lights["world_matrix"] = np.eye(4, dtype=np.float32).reshape(16)
+    lights["pos"] = (0.0, 4.0, 1.0)
+    lights["to"] = (0.0, 0.0, 0.0)
+    lights["L"] = 100.0
+    lights["light_flags"] = abi.LIGHT_SPOT | abi.LIGHT_FINITE | abi.LIGHT_DELTA
+    cam_pos = np.array([0.0, 3.0, 5.0])
+    cam_dir = cam_pos - np.array([0.0, 0.2, 0.0])  # Lumen's view looks along -dir
+    cam_dir /= np.linalg.norm(cam_dir)
+    # a non-area light counts as one light triangle (LumenScene.cpp:106)
+    return b.arrays(mats, lights, 1, tuple(cam_pos), tuple(cam_dir), 45.0)
 
 
 def primary_rays(width: int, height: int, pos=(0.0, 0.0, -4.0), fov: float = 45.0, tmax: float = 10000.0) -> np.ndarray:

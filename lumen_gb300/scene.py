@@ -186,6 +186,29 @@ class Context:
             pass
 
 
+def camera_forward(cam: abi.Camera):
+    """lgb_camera_forward: (view, projection) as two 16-float column-major numpy arrays."""
+    lib = abi.load()
+    view, proj = (C.c_float * 16)(), (C.c_float * 16)()
+    st = lib.lgb_camera_forward(C.byref(cam), view, proj)
+    if st != abi.LGB_OK:
+        raise abi.LgbError(st, "lgb_camera_forward")
+    return np.array(view[:], np.float32), np.array(proj[:], np.float32)
+
+
+def vcm_radius(scene_radius: float, radius_factor: float, iteration: int, alpha: float = 2.0 / 3.0) -> float:
+    return float(abi.load().lgb_vcm_radius(scene_radius, radius_factor, iteration, alpha))
+
+
+def vcm_grid(ctx: Context, pos4, scene_min, scene_max, radius: float, screen_size: int, count, rep, stream=None):
+    """lgb_vcm_grid on CUDA tensors: pos4 (n, 4) float32; count / rep (10 * screen_size,) int32."""
+    mn = (C.c_float * 3)(*[float(v) for v in scene_min])
+    mx = (C.c_float * 3)(*[float(v) for v in scene_max])
+    _check(ctx.lib, ctx.handle,
+           ctx.lib.lgb_vcm_grid(ctx.handle, C.c_void_p(pos4.data_ptr()), pos4.shape[0], mn, mx, radius, screen_size,
+                                C.c_void_p(count.data_ptr()), C.c_void_p(rep.data_ptr()), C.c_void_p(stream)))
+
+
 def film_rmse(ctx: Context, film, reference, mode: int = 0, stream=None) -> float:
     """lgb_film_rmse on two (N, 4) float32 CUDA tensors; mode 1 gives the value Lumen reports."""
     out = C.c_double(0.0)
@@ -242,6 +265,12 @@ class GpuScene:
 
     def sync(self, stream=None):
         _check(self.lib, self.ctx.handle, self.lib.lgb_sync(self.handle, C.c_void_p(stream)))
+
+    def vcm_iteration(self, cam: abi.Camera, params: abi.VcmParams, film, stream=None):
+        """lgb_vcm_iteration into film ((npix, 4) float32 CUDA)."""
+        _check(self.lib, self.ctx.handle,
+               self.lib.lgb_vcm_iteration(self.handle, C.byref(cam), C.byref(params), C.c_void_p(film.data_ptr()),
+                                          C.c_void_p(stream)))
 
     @staticmethod
     def _diff_params(texture_id, texels, roughness, emission, flags=0) -> abi.DiffParams:
@@ -347,6 +376,35 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def vcm_params(arrays: SceneArrays, max_depth: int, radius: float, light_seed: int, eye_seed: int, frame_num: int,
+               use_vm: int = 1, use_vc: int = 1, sky=(0.0, 0.0, 0.0), flags: int = 0) -> abi.VcmParams:
+    """PCVCM as VCM::render fills it (src/RayTracer/VCM.cpp:131-147) with explicit seeds; the grid bounds are the
+    scene's bounding box."""
+    p = abi.VcmParams()
+    p.sky_col[:] = list(sky)
+    p.max_depth = max_depth
+    p.num_lights = len(arrays.lights)
+    p.light_triangle_count = arrays.light_triangle_count
+    p.dir_light_idx = 0xFFFFFFFF
+    p.radius = radius
+    mn, mx = arrays.positions.min(0), arrays.positions.max(0)
+    p.scene_min[:] = [float(v) for v in mn]
+    p.scene_max[:] = [float(v) for v in mx]
+    p.use_vm = use_vm
+    p.use_vc = use_vc
+    p.light_seed = light_seed
+    p.eye_seed = eye_seed
+    p.frame_num = frame_num
+    p.flags = flags
+    return p
+
+
+def scene_radius(arrays: SceneArrays) -> float:
+    """Half the diagonal of the scene's bounding box (LumenScene::m_dimensions.radius)."""
+    mn, mx = arrays.positions.min(0).astype(np.float64), arrays.positions.max(0).astype(np.float64)
+    return float(np.linalg.norm(mx - mn) / 2.0)
 
 
 def path_params(arrays: SceneArrays, max_depth: int, sky=(0.0, 0.0, 0.0), direct_lighting: int = 1,

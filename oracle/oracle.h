@@ -129,6 +129,33 @@ void orc_render_film(void* scene, const float inv_view[16], const float inv_proj
 void orc_render_diff(void* scene, const float inv_view[16], const float inv_proj[16], const orc_path_params* params,
                      int tex_id, const float* texels, const float* rough, const float* emis, uint32_t frame0,
                      uint32_t spp, double* film_rgb, int fp64, int nthreads);
+// ---- VCM (vcm_commons.glsl, vcm_light.rgen, vcm_eye.rgen, VCM.cpp) ----
+struct orc_vcm_params {
+    float sky_col[3];
+    int32_t max_depth;
+    int32_t num_lights;
+    int32_t light_triangle_count;
+    float radius;             // merge radius of this iteration
+    int32_t use_vm, use_vc;
+    uint32_t light_seed, eye_seed;  // the reference's host rand() values
+    uint32_t frame_num;
+    float scene_min[3], scene_max[3];
+    uint32_t flags;  // bit 0: accumulate every connection and merge instead of keeping the last (`res =`)
+};
+// VCMVertex, vcm_commons.h:89-104 (104 bytes).
+struct orc_vcm_vertex {
+    float wi[3], wo[3], n_s[3], pos[3], uv[2], throughput[3];
+    uint32_t material_idx, path_len;
+    float area, d_vcm, d_vc, d_vm;
+    uint32_t side, coords;
+};
+void orc_vcm_grid_res(const float scene_min[3], const float scene_max[3], float radius, int32_t res[3]);
+void orc_vcm_grid(const float* pos4, uint32_t n, const float scene_min[3], const float scene_max[3], float radius,
+                  uint32_t screen_size, uint32_t* count, uint32_t* rep);
+void orc_vcm_iteration(void* scene, const float inv_view[16], const float inv_proj[16], const float view[16],
+                       const float proj[16], uint32_t width, uint32_t height, const orc_vcm_params* p,
+                       orc_vcm_vertex* verts, uint32_t* counts, float* splat, uint32_t* grid_count, uint32_t* grid_rep,
+                       float* film, int nthreads);
 // PCG4D (utils.glsl:121-133) applied to n state vectors; for known-answer tests.
 void orc_pcg4d(const uint32_t* in, uint32_t* out, uint32_t n);
 // offset_ray (utils.glsl:73-84) applied to n (p, n) pairs.

@@ -759,4 +759,44 @@ inline V3<T> eval_bsdf(V3<T> n_s, V3<T> wo, const Mat<T>& mat, uint32_t mode, bo
     return f;
 }
 
+// bsdf_pdf (bsdf_commons.glsl:26-66) with the per-lobe pdf functions it calls: conductor.glsl:74-90,
+// principled.glsl:338-359 (the others are above).
+template <class T> inline T eval_conductor_pdf(const Mat<T>& mat, V3<T> wo, V3<T> wi) {
+    T alpha = mat.roughness * mat.roughness;
+    if (bsdf_is_effectively_delta(alpha)) return T(0);
+    if (wo.z * wi.z < T(0)) return T(0);
+    if (wo.z == T(0) || wi.z == T(0)) return T(0);
+    V3<T> h = normalize(wo + wi);
+    h *= T(sign(h.z));
+    return eval_vndf_pdf_isotropic(alpha, wo, h) / (T(4) * dot(wo, h));
+}
+template <class T> inline T eval_principled_pdf(const Mat<T>& mat, V3<T> wo, V3<T> wi, bool ff) {
+    T pdf = T(0);
+    T p_spec, p_diff, p_clearcoat, p_spec_trans;
+    T F = fresnel_dielectric(wo.z, mat.ior, ff);
+    initialize_sampling_probs(mat, F, ff, p_spec, p_diff, p_clearcoat, p_spec_trans);
+    if (p_spec > T(0)) pdf += p_spec * eval_principled_brdf_pdf(mat, wo, wi);
+    if (gmin(wi.z, wo.z) > T(0)) {
+        if (p_diff > T(0)) pdf += p_diff * eval_diffuse_pdf(wo, wi);
+        if (p_clearcoat > T(0)) pdf += p_clearcoat * eval_clearcoat_pdf(mat, wo, wi);
+    }
+    if (p_spec_trans > T(0)) pdf += p_spec_trans * eval_dielectric_pdf(mat, wo, wi, ff);
+    return pdf;
+}
+template <class T> inline T bsdf_pdf(const Mat<T>& mat, V3<T> n_s, V3<T> wo, V3<T> wi, bool ff) {
+    V3<T> Tt, B;
+    branchless_onb(n_s, Tt, B);
+    wo = to_local(wo, Tt, B, n_s);
+    wi = to_local(wi, Tt, B, n_s);
+    switch (mat.bsdf_type) {
+        case BSDF_TYPE_DIFFUSE: return eval_diffuse_pdf(wo, wi);
+        case BSDF_TYPE_MIRROR: return T(0);
+        case BSDF_TYPE_GLASS: return T(0);
+        case BSDF_TYPE_DIELECTRIC: return eval_dielectric_pdf(mat, wo, wi, ff);
+        case BSDF_TYPE_CONDUCTOR: return eval_conductor_pdf(mat, wo, wi);
+        case BSDF_TYPE_PRINCIPLED: return eval_principled_pdf(mat, wo, wi, ff);
+        default: return T(0);
+    }
+}
+
 }  // namespace orc

@@ -43,6 +43,17 @@ class _Params(C.Structure):
                 ("light_triangle_count", C.c_int32), ("dir_light_idx", C.c_uint32), ("direct_lighting", C.c_uint32)]
 
 
+class VcmParams(C.Structure):
+    _fields_ = [("sky_col", C.c_float * 3), ("max_depth", C.c_int32), ("num_lights", C.c_int32),
+                ("light_triangle_count", C.c_int32), ("radius", C.c_float), ("use_vm", C.c_int32),
+                ("use_vc", C.c_int32), ("light_seed", C.c_uint32), ("eye_seed", C.c_uint32),
+                ("frame_num", C.c_uint32), ("scene_min", C.c_float * 3), ("scene_max", C.c_float * 3),
+                ("flags", C.c_uint32)]
+
+
+VCM_VERTEX_BYTES = 104
+
+
 def ensure_built() -> str:
     if not os.path.exists(LIB):
         subprocess.run(["make", "-s", "-C", ORACLE_DIR], check=True)
@@ -81,6 +92,12 @@ class Oracle:
         L.orc_render_diff.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(_Params),
                                       C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
                                       C.POINTER(C.c_double), C.c_int, C.c_int]
+        L.orc_vcm_grid_res.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float, C.POINTER(C.c_int32)]
+        L.orc_vcm_grid.argtypes = [C.POINTER(C.c_float), C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                   C.c_float, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+        L.orc_vcm_iteration.argtypes = [C.c_void_p] + [C.POINTER(C.c_float)] * 4 + [
+            C.c_uint32, C.c_uint32, C.POINTER(VcmParams), C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_float),
+            C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_float), C.c_int]
         L.orc_pcg4d.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint32]
         L.orc_offset_ray.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32]
 
@@ -257,3 +274,35 @@ class OracleScene:
                                      ptr(emis), frame0, spp, _p(out, C.c_double), int(fp64),
                                      threads or (os.cpu_count() or 1))
         return out
+
+    def vcm_state(self, width, height, max_depth):
+        """Buffers that persist across VCM iterations (as the reference's do), zero-initialised."""
+        screen = width * height
+        return {"verts": np.zeros(screen * (max_depth + 1) * VCM_VERTEX_BYTES, np.uint8),
+                "counts": np.zeros(screen, np.uint32), "splat": np.zeros(screen * 3, np.float32),
+                "grid_count": np.zeros(10 * screen, np.uint32), "grid_rep": np.zeros(10 * screen, np.uint32),
+                "film": np.zeros((screen, 4), np.float32), "width": width, "height": height}
+
+    def vcm_iteration(self, cam, view, proj, params: "VcmParams", state, threads=0):
+        """One VCM iteration into state['film'] (RGBA32F, row-major); view / proj are the camera's forward
+        matrices (column-major 4x4 float32)."""
+        f32 = lambda a: np.ascontiguousarray(np.array(a, np.float32).reshape(16))
+        iv, ip, vw, pj = f32(cam.inv_view[:]), f32(cam.inv_projection[:]), f32(view), f32(proj)
+        self.ora.lib.orc_vcm_iteration(self.h, _p(iv), _p(ip), _p(vw), _p(pj), state["width"], state["height"],
+                                       C.byref(params), state["verts"].ctypes.data, _p(state["counts"], C.c_uint32),
+                                       _p(state["splat"]), _p(state["grid_count"], C.c_uint32),
+                                       _p(state["grid_rep"], C.c_uint32), _p(state["film"]),
+                                       threads or (os.cpu_count() or 1))
+        return state["film"]
+
+
+def vcm_grid(ora: Oracle, pos4, scene_min, scene_max, radius, screen_size):
+    """The sequential photon table: (count, representative) per slot, 10 * screen_size slots."""
+    pos4 = np.ascontiguousarray(pos4, np.float32)
+    count = np.zeros(10 * screen_size, np.uint32)
+    rep = np.zeros(10 * screen_size, np.uint32)
+    mn = np.ascontiguousarray(scene_min, np.float32)
+    mx = np.ascontiguousarray(scene_max, np.float32)
+    ora.lib.orc_vcm_grid(_p(pos4), len(pos4), _p(mn), _p(mx), radius, screen_size, _p(count, C.c_uint32),
+                         _p(rep, C.c_uint32))
+    return count, rep

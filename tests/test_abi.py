@@ -85,7 +85,8 @@ def test_ctypes_layouts_match_the_header(tmp_path):
     mirrors = {"lgb_ray": abi.Ray, "lgb_hit": abi.Hit, "lgb_material": abi.Material, "lgb_light": abi.Light,
                "lgb_mesh": abi.Mesh, "lgb_camera": abi.Camera, "lgb_path_params": abi.PathParams,
                "lgb_build_opts": abi.BuildOpts, "lgb_build_stats": abi.BuildStats, "lgb_diff_params": abi.DiffParams,
-               "lgb_diff_grads": abi.DiffGrads, "lgb_batch_job": abi.BatchJob, "lgb_batch_opts": abi.BatchOpts}
+               "lgb_diff_grads": abi.DiffGrads, "lgb_batch_job": abi.BatchJob, "lgb_batch_opts": abi.BatchOpts,
+               "lgb_vcm_params": abi.VcmParams}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "lgb.h"', "int main(void) {"]
     for cname, py in mirrors.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')

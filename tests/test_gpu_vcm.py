@@ -1,0 +1,130 @@
+"""GPU tests of VCM (lgb_vcm_iteration, lgb_vcm_grid) against the CPU oracle's restatement.
+
+  * the photon table built by radix sort and scan equals the oracle's sequentially written table bit for bit
+    (same positions in, same counts and representatives out);
+  * VCM iterations equal the oracle's pixel by pixel (same seeds); the light subpaths' camera splats are summed
+    with float atomics on the GPU and in path order on the CPU, so pixels agree to rounding, and a rare branch
+    flip (CUDA's and glibc's sinf/cosf differ by an ULP) changes a few pixels;
+  * the caustics configuration (dielectric torus, spot light) with merging; the accumulate option; error paths.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from lumen_gb300 import abi, build, procedural
+from lumen_gb300.scene import (Context, GpuScene, camera_forward, camera_lookat, scene_radius, vcm_grid, vcm_params,
+                               vcm_radius)
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    if not os.path.exists(abi.LIB_PATH):
+        build.build_library()
+    return Context(0)
+
+
+def close_fraction(a, b, rtol=1e-3, atol=1e-5):
+    ok = np.abs(a - b) <= rtol * np.maximum(np.abs(b), 1e-6) + atol
+    return ok.all(axis=1).mean()
+
+
+def test_photon_table_is_bit_exact(ctx, oracle):
+    from oracle_lib import vcm_grid as oracle_grid
+    rng = np.random.default_rng(8)
+    n, screen = 200_000, 128 * 128
+    pos4 = np.concatenate([rng.uniform(-2.1, 2.1, (n, 3)), np.where(rng.uniform(size=(n, 1)) < 0.2, -1.0, 1.0)], 1)
+    pos4[:1000, :3] = pos4[1000:2000, :3]
+    pos4 = pos4.astype(np.float32)
+    mn, mx, radius = (-2.0, -2.0, -2.0), (2.0, 2.0, 2.0), 0.03
+    count = torch.zeros(10 * screen, dtype=torch.int32, device="cuda")
+    rep = torch.zeros(10 * screen, dtype=torch.int32, device="cuda")
+    vcm_grid(ctx, torch.from_numpy(pos4).cuda(), mn, mx, radius, screen, count, rep)
+    want_c, want_r = oracle_grid(oracle, pos4, mn, mx, radius, screen)
+    assert np.array_equal(count.cpu().numpy().view(np.uint32), want_c)
+    assert np.array_equal(rep.cpu().numpy().view(np.uint32), want_r)
+    assert (want_c > 1).sum() > 1000
+    # an empty input gives an empty table
+    vcm_grid(ctx, torch.zeros((0, 4), device="cuda"), mn, mx, radius, screen, count, rep)
+    assert int(count.abs().sum()) == 0
+
+
+def _run_both(ctx, oracle, arrays, w, h, iters, depth, flags=0, use_vm=1, alpha=2.0 / 3.0, factor=1.0):
+    from oracle_lib import VcmParams
+    sc = GpuScene(ctx, arrays)
+    sc.build()
+    osc = oracle.scene(arrays)
+    cam = camera_lookat(arrays.camera_pos, arrays.camera_dir, arrays.fov, w, h)
+    view, proj = camera_forward(cam)
+    film = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+    st = osc.vcm_state(w, h, depth)
+    R = scene_radius(arrays)
+    for it in range(iters):
+        r = vcm_radius(R, factor, it, alpha)
+        p = vcm_params(arrays, depth, r, 1000 + it, 5000 + it, it, use_vm=use_vm, flags=flags)
+        sc.vcm_iteration(cam, p, film)
+        op = VcmParams()
+        for name in ("max_depth", "num_lights", "light_triangle_count", "radius", "use_vm", "use_vc", "light_seed",
+                     "eye_seed", "frame_num", "flags"):
+            setattr(op, name, getattr(p, name))
+        op.sky_col[:] = list(p.sky_col)
+        op.scene_min[:] = list(p.scene_min)
+        op.scene_max[:] = list(p.scene_max)
+        osc.vcm_iteration(cam, view, proj, op, st)
+    sc.sync()
+    got = film.cpu().numpy()
+    sc.close()
+    return got, st["film"]
+
+
+def test_iteration_matches_oracle_cornell(ctx, oracle):
+    cb = procedural.cornell_box()
+    got, want = _run_both(ctx, oracle, cb, 48, 48, 1, 8)
+    frac = close_fraction(got[:, :3], want[:, :3])
+    assert frac >= 0.97, f"only {frac:.4f} of pixels agree"
+    assert (got[:, 3] == 1.0).all()
+    got8, want8 = _run_both(ctx, oracle, cb, 48, 48, 8, 8)
+    np.testing.assert_allclose(got8[:, :3].mean(0), want8[:, :3].mean(0), rtol=0.01)
+    assert close_fraction(got8[:, :3], want8[:, :3]) >= 0.9
+
+
+def test_caustics_scene_with_merging_matches_oracle(ctx, oracle):
+    arrays = procedural.vcm_scene(100, 40)
+    got, want = _run_both(ctx, oracle, arrays, 64, 64, 4, 10, alpha=0.75)
+    assert not np.isnan(got).any()
+    frac = close_fraction(got[:, :3], want[:, :3])
+    assert frac >= 0.95, f"only {frac:.4f} of pixels agree"
+    np.testing.assert_allclose(got[:, :3].mean(0), want[:, :3].mean(0), rtol=0.02)
+    assert got[:, :3].mean() > 0.0
+
+
+def test_accumulate_option_matches_oracle(ctx, oracle):
+    cb = procedural.cornell_box()
+    got, want = _run_both(ctx, oracle, cb, 32, 32, 2, 8, flags=abi.VCM_ACCUMULATE)
+    assert close_fraction(got[:, :3], want[:, :3]) >= 0.95
+    base, _ = _run_both(ctx, oracle, cb, 32, 32, 2, 8)
+    assert got[:, :3].mean() >= base[:, :3].mean()
+
+
+def test_vcm_error_paths(ctx):
+    cb = procedural.cornell_box()
+    sc = GpuScene(ctx, cb)
+    sc.build()
+    cam = camera_lookat(cb.camera_pos, cb.camera_dir, cb.fov, 16, 16)
+    film = torch.zeros((256, 4), dtype=torch.float32, device="cuda")
+    for bad in (dict(max_depth=0), dict(radius=0.0), dict(num_lights=0)):
+        p = vcm_params(cb, 8, 0.01, 1, 2, 0)
+        for k, v in bad.items():
+            setattr(p, k, v)
+        with pytest.raises(abi.LgbError):
+            sc.vcm_iteration(cam, p, film)
+    p = vcm_params(cb, 8, 0.01, 1, 2, 0)
+    p.scene_max[1] = p.scene_min[1]
+    with pytest.raises(abi.LgbError):
+        sc.vcm_iteration(cam, p, film)
+    sc.vcm_iteration(cam, vcm_params(cb, 8, 0.01, 1, 2, 0), film)
+    sc.sync()
+    sc.close()

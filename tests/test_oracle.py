@@ -235,3 +235,74 @@ def test_diff_estimator_is_linear_in_emission_and_smooth_in_parameters(oracle):
         g2 = fd(make, 5e-4) / 1e-3
         assert abs(g1) > 1e-3
         np.testing.assert_allclose(g1, g2, rtol=2e-3)
+
+
+def _np_vcm_table(pos4, mn, mx, radius, screen):
+    """utils.glsl:62-65 hash of vcm_commons.glsl:17-23 cells over the VCM.cpp:144-147 grid, written sequentially."""
+    f32 = np.float32
+    mn, mx = np.asarray(mn, f32), np.asarray(mx, f32)
+    d = mx - mn
+    max_comp = d.max()
+    base = int(f32(max_comp / f32(radius)))
+    res = [max(int(f32(d[k] * f32(base) / max_comp)), 1) for k in range(3)]
+    p = pos4[:, :3].astype(f32)
+    cell = ((p - mn) / d * np.asarray(res, f32)).astype(np.int32)
+    with np.errstate(over="ignore"):
+        h = ((cell[:, 0].astype(np.uint32) * np.uint32(73856093)) ^ (cell[:, 1].astype(np.uint32) * np.uint32(19349663)) ^
+             (cell[:, 2].astype(np.uint32) * np.uint32(83492791))) % np.uint32(10 * screen)
+    count = np.zeros(10 * screen, np.uint32)
+    rep = np.zeros(10 * screen, np.uint32)
+    for i in np.nonzero(pos4[:, 3] >= 0)[0]:
+        count[h[i]] += 1
+        rep[h[i]] = i
+    return count, rep
+
+
+def test_vcm_photon_table_matches_independent_restatement(oracle):
+    from oracle_lib import vcm_grid
+    rng = np.random.default_rng(4)
+    n, screen = 5000, 700
+    pos4 = np.concatenate([rng.uniform(-1.2, 1.2, (n, 3)), np.where(rng.uniform(size=(n, 1)) < 0.1, -1.0, 1.0)], 1)
+    pos4[:50, :3] = pos4[50:100, :3]  # coincident photons share a slot
+    mn, mx, radius = (-1.0, -1.0, -1.0), (1.0, 1.0, 1.0), 0.05
+    count, rep = vcm_grid(oracle, pos4.astype(np.float32), mn, mx, radius, screen)
+    want_c, want_r = _np_vcm_table(pos4.astype(np.float32), mn, mx, radius, screen)
+    assert np.array_equal(count, want_c) and np.array_equal(rep, want_r)
+    assert count.sum() == (pos4[:, 3] >= 0).sum() and (count > 1).any()
+
+
+def _vcm_oracle_run(oracle, arrays, w, h, iters, depth, flags, use_vm=1):
+    from oracle_lib import VcmParams
+    from lumen_gb300.scene import camera_lookat, camera_forward, scene_radius, vcm_radius
+    sc = oracle.scene(arrays)
+    cam = camera_lookat(arrays.camera_pos, arrays.camera_dir, arrays.fov, w, h)
+    view, proj = camera_forward(cam)
+    st = sc.vcm_state(w, h, depth)
+    R = scene_radius(arrays)
+    for it in range(iters):
+        p = VcmParams()
+        p.max_depth, p.num_lights, p.light_triangle_count = depth, len(arrays.lights), arrays.light_triangle_count
+        p.scene_min[:] = [float(v) for v in arrays.positions.min(0)]
+        p.scene_max[:] = [float(v) for v in arrays.positions.max(0)]
+        p.radius = vcm_radius(R, 1.0, it, 2.0 / 3.0)
+        p.use_vm, p.use_vc = use_vm, 1
+        p.light_seed, p.eye_seed, p.frame_num, p.flags = 1000 + it, 5000 + it, it, flags
+        sc.vcm_iteration(cam, view, proj, p, st)
+    return sc, cam, st
+
+
+def test_vcm_oracle_is_deterministic_and_energy_consistent(oracle):
+    """With every connection accumulated (LGB_VCM_ACCUMULATE) and a non-reflecting emitter, VCM converges to the
+    path tracer's image. (With the white emitter of the Cornell box the path tracer itself gains energy from its
+    stale-payload quirk on BSDF-MIS rays that start on the emitter and miss, pt_commons.glsl:32-33.)"""
+    cb = procedural.cornell_box()
+    m = cb.materials.copy()
+    m["albedo"][3] = 0.0
+    cb.materials = m
+    sc, cam, st = _vcm_oracle_run(oracle, cb, 32, 32, 48, 8, 1)
+    _, _, st2 = _vcm_oracle_run(oracle, cb, 32, 32, 48, 8, 1)
+    assert np.array_equal(st["film"], st2["film"])
+    pt = sc.film(cam, 8, 32, 32, 0, 256)
+    vcm_mean, pt_mean = st["film"][:, :3].mean(), pt[:, :3].mean()
+    assert abs(vcm_mean - pt_mean) < 0.03 * pt_mean, (vcm_mean, pt_mean)
+    assert not np.isnan(st["film"]).any()

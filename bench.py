@@ -322,6 +322,44 @@ def batch_secondary(torch, ctx_cls, scene_cls, local):
     return res
 
 
+def vcm_secondary(torch, ctx_cls, scene_cls, local, iters=4):
+    """VCM caustics configuration: dielectric torus (200k triangles) on a diffuse plane, spot light, 1024^2,
+    one light subpath per pixel per iteration (1M), max depth 10, merge radius 0.01 x scene extent shrinking
+    with alpha = 0.75. Times `iters` iterations after one warm-up (device time per lgb_vcm_iteration)."""
+    from lumen_gb300 import procedural
+    from lumen_gb300.scene import camera_lookat, scene_radius, vcm_params, vcm_radius
+    arrays = procedural.vcm_scene()
+    ctx = ctx_cls(local)
+    sc = scene_cls(ctx, arrays)
+    sc.build()
+    w = h = 1024
+    cam = camera_lookat(arrays.camera_pos, arrays.camera_dir, arrays.fov, w, h)
+    film = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+    R = scene_radius(arrays)
+    stream = torch.cuda.current_stream()
+    cs = stream.cuda_stream
+
+    def it(i):
+        sc.vcm_iteration(cam, vcm_params(arrays, 10, vcm_radius(R, 1.0, i, 0.75), 1000 + i, 5000 + i, i), film, stream=cs)
+
+    it(0)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(1, iters + 1):
+        it(i)
+    e1.record(stream)
+    e1.synchronize()
+    sc.sync(cs)
+    ms = e0.elapsed_time(e1) / iters
+    out = {"workload": "VCM: dielectric torus (200k triangles, IOR 1.5) on a diffuse plane, spot light L = 100, "
+                       "1024x1024, 1M light subpaths per iteration, max depth 10, radius 0.01 x extent, alpha 0.75",
+           "ms_per_iteration": ms, "light_plus_eye_paths_per_s": 2 * w * h / (ms * 1e-3),
+           "mean_radiance": float(film[:, :3].mean()), "iterations_timed": iters}
+    sc.close()
+    return out
+
+
 def run_reference(args):
     rank, world, _ = _dist()
     if rank != 0:
@@ -453,6 +491,7 @@ def run_gpu(args):
         secondary["path_tracer"] = cornell_secondary(torch, Context, GpuScene, local, world == 1 and not args.no_cpu_baseline)
         secondary["adjoint"] = adjoint_secondary(torch, Context, GpuScene, local)
         secondary["batched"] = batch_secondary(torch, Context, GpuScene, local)
+        secondary["vcm"] = vcm_secondary(torch, Context, GpuScene, local)
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",

@@ -36,7 +36,8 @@ LGB_API void lgbh_scene_free(lgbh_scene* s);
 /* The loaded arrays as an lgb_scene_desc (pointers stay valid until lgbh_scene_free). */
 LGB_API lgb_status lgbh_scene_desc(lgbh_scene* s, lgb_scene_desc* out);
 LGB_API lgb_status lgbh_scene_get_info(lgbh_scene* s, lgbh_scene_info* out);
-/* Headless render with the Path integrator: init, create_accel, then `spp` frames of render/update, film
+/* Headless render with the scene's integrator (Path, or VCM with seeds from the deterministic sequence of
+ * GpuVCM, light_seed / eye_seed = vcm_seeds(0, frame)): init, create_accel, then `spp` frames of render/update, film
  * written to out_pfm (RGB PFM; skipped when null) and copied to host_rgba (width*height*4 floats; skipped when
  * null). */
 LGB_API lgb_status lgbh_render_path(const char* json_path, int device, uint32_t width, uint32_t height, uint32_t spp,

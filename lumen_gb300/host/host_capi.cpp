@@ -7,6 +7,8 @@
 #include <string>
 #include <vector>
 
+#include <memory>
+
 #include "integrator.h"
 #include "lgb_host.h"
 #include "lumen_scene.h"
@@ -80,17 +82,21 @@ LGB_API lgb_status lgbh_render_path(const char* json_path, int device, uint32_t 
     try {
         lgbh::LumenScene scene;
         scene.load(json_path);
-        lgbh::GpuPath path(&scene, ctx, width, height);
-        path.init();            // RayTracer::init -> integrator->init (RayTracer.cpp:61-65)
-        path.create_accel();    // integrator->create_accel
+        // RayTracer::init picks the integrator named in the scene (RayTracer.cpp:45-60): Path or VCM here
+        std::unique_ptr<lgbh::Integrator> integrator;
+        if (scene.config.integrator == "vcm") integrator.reset(new lgbh::GpuVCM(&scene, ctx, width, height));
+        else if (scene.config.integrator == "path") integrator.reset(new lgbh::GpuPath(&scene, ctx, width, height));
+        else throw std::runtime_error("integrator \"" + scene.config.integrator + "\" is not supported (path, vcm)");
+        integrator->init();           // RayTracer::init -> integrator->init (RayTracer.cpp:61-65)
+        integrator->create_accel();   // integrator->create_accel
         for (uint32_t f = 0; f < spp; f++) {  // the frame loop: render, then update (RayTracer.cpp:167-197)
-            path.render();
-            path.update();
+            integrator->render();
+            integrator->update();
         }
-        st = lgb_sync(path.gpu_scene(), nullptr);
+        st = lgb_sync(integrator->gpu_scene(), nullptr);
         if (st != LGB_OK) throw std::runtime_error(lgb_last_error(ctx));
         std::vector<float> film((size_t)width * height * 4);
-        if (cudaMemcpy(film.data(), path.output_film, film.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+        if (cudaMemcpy(film.data(), integrator->output_film, film.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
             throw std::runtime_error("film read-back failed");
         if (out_pfm) lgbh::write_pfm(out_pfm, film.data(), width, height);
         if (host_rgba) std::memcpy(host_rgba, film.data(), film.size() * 4);

@@ -59,4 +59,50 @@ bool GpuPath::update() {  // Path::update (Path.cpp:61-68)
     return changed;
 }
 
+static uint32_t hash32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+void vcm_seeds(uint32_t seed, uint32_t frame, uint32_t* light_seed, uint32_t* eye_seed) {
+    *light_seed = hash32(seed * 0x9e3779b9u + 2u * frame + 1u);
+    *eye_seed = hash32(seed * 0x9e3779b9u + 2u * frame + 2u);
+}
+
+void GpuVCM::init() {
+    Integrator::init();
+    frame_num = 0;
+    path_length = (uint32_t)lumen_scene->config.path_length;
+}
+
+void GpuVCM::render() {  // VCM::render (VCM.cpp:131-265)
+    lgb_vcm_params p{};
+    for (int i = 0; i < 3; i++) {
+        p.sky_col[i] = lumen_scene->config.sky_col[i];
+        p.scene_min[i] = lumen_scene->bbox_min[i];
+        p.scene_max[i] = lumen_scene->bbox_max[i];
+    }
+    p.max_depth = (int32_t)path_length;
+    p.num_lights = (int32_t)lumen_scene->lights.size();
+    p.light_triangle_count = (int32_t)lumen_scene->total_light_triangle_cnt;
+    p.dir_light_idx = lumen_scene->dir_light_idx;
+    p.radius = lgb_vcm_radius(lumen_scene->radius, lumen_scene->config.radius_factor, frame_num, 2.0f / 3.0f);
+    p.use_vm = lumen_scene->config.enable_vm ? 1 : 0;
+    p.use_vc = 1;
+    vcm_seeds(seed, frame_num, &p.light_seed, &p.eye_seed);
+    p.frame_num = frame_num;
+    check(lgb_vcm_iteration(scene, &cam, &p, output_film, stream), "lgb_vcm_iteration");
+}
+
+bool GpuVCM::update() {  // VCM::update (VCM.cpp:267-274)
+    frame_num++;
+    const bool changed = Integrator::update();
+    if (changed) frame_num = 0;
+    return changed;
+}
+
 }  // namespace lgbh

@@ -52,4 +52,21 @@ class GpuPath final : public Integrator {
     void* stream = nullptr;
 };
 
+// The VCM integrator (VCM.cpp:131-275): one iteration per render(); the merge radius shrinks with the frame
+// (VCM.cpp:137-138) and VC is always on (VCM.cpp:8). Lumen seeds each iteration with host rand(); here the
+// seeds are the deterministic sequence vcm_seeds(seed, frame_num).
+class GpuVCM final : public Integrator {
+  public:
+    using Integrator::Integrator;
+    void init() override;
+    void render() override;
+    bool update() override;
+    uint32_t path_length = 6;
+    uint32_t seed = 0;
+    void* stream = nullptr;
+};
+
+// Light and eye seeds of VCM iteration `frame` (PCG-style integer hash of (seed, frame, stream)).
+void vcm_seeds(uint32_t seed, uint32_t frame, uint32_t* light_seed, uint32_t* eye_seed);
+
 }  // namespace lgbh

@@ -159,6 +159,10 @@ void LumenScene::load(const std::string& json_path) {
         std::transform(config.integrator.begin(), config.integrator.end(), config.integrator.begin(), ::tolower);
     }
     if (!integ["path_length"].is_null()) config.path_length = (int)integ["path_length"].as_number();
+    if (config.integrator == "vcm") {  // LumenScene.cpp:248-253
+        if (!integ["enable_vm"].is_null()) config.enable_vm = integ["enable_vm"].as_number() == 1;
+        if (!integ["radius_factor"].is_null()) config.radius_factor = (float)integ["radius_factor"].as_number();
+    }
     if (!integ["sky_col"].is_null()) vec3_of(integ["sky_col"], config.sky_col, config.sky_col);
     // geometry
     if (j["mesh_file"].is_null()) throw std::runtime_error("scene has no mesh_file");

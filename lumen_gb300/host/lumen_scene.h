@@ -21,9 +21,11 @@ struct CameraSettings {  // SceneConfig.h:6-11
     float dir[3] = {0, 0, 1};
 };
 
-struct SceneConfig {  // SceneConfig.h:15-24 (the fields the Path integrator reads)
+struct SceneConfig {  // SceneConfig.h:15-63 (the fields the Path and VCM integrators read)
     std::string integrator = "path";
     int path_length = 6;
+    bool enable_vm = false;        // VCMConfig
+    float radius_factor = 0.025f;  // VCMConfig
     float sky_col[3] = {0, 0, 0};
     CameraSettings cam;
 };

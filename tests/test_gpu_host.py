@@ -65,3 +65,41 @@ def test_cli_writes_the_same_film(host, tmp_path):
     np.testing.assert_array_equal(img, film[:, :3])
     bad = subprocess.run([exe, str(tmp_path / "none.json"), "8", "8", "1", str(out)], capture_output=True, text=True)
     assert bad.returncode == 1 and "cannot open" in bad.stderr
+
+
+def _hash32(x):
+    x &= 0xFFFFFFFF
+    x ^= x >> 16
+    x = (x * 0x7FEB352D) & 0xFFFFFFFF
+    x ^= x >> 15
+    x = (x * 0x846CA68B) & 0xFFFFFFFF
+    x ^= x >> 16
+    return x
+
+
+def test_headless_vcm_matches_direct_iterations(host):
+    """A scene whose integrator is "vcm" renders through the GpuVCM mirror (radius schedule, bounds, seeds) exactly
+    as direct lgb_vcm_iteration calls with the same parameters; splats are float atomics, so pixels agree to
+    rounding."""
+    from lumen_gb300.scene import Context, GpuScene, camera_lookat, vcm_params, vcm_radius
+    scene = os.path.join(HERE, "golden", "scenes", "mixed_vcm.json")
+    w, h, n = 40, 30, 4
+    film = host.render_path(scene, w, h, n)
+    arrays, info = host.load_scene(scene)
+    ctx = Context(0)
+    sc = GpuScene(ctx, arrays)
+    sc.build()
+    cam = camera_lookat(arrays.camera_pos, arrays.camera_dir, arrays.fov, w, h)
+    direct = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+    for f in range(n):
+        ls, es = _hash32(2 * f + 1), _hash32(2 * f + 2)
+        p = vcm_params(arrays, int(info.path_length), vcm_radius(float(info.radius), 1.0, f), ls, es, f,
+                       sky=tuple(info.sky_col))
+        p.scene_min[:] = list(info.bbox_min)
+        p.scene_max[:] = list(info.bbox_max)
+        sc.vcm_iteration(cam, p, direct)
+    sc.sync()
+    got = direct.cpu().numpy()
+    ok = np.abs(film[:, :3] - got[:, :3]) <= 1e-4 * np.maximum(np.abs(got[:, :3]), 1e-6) + 1e-6
+    assert ok.all(axis=1).mean() >= 0.99
+    assert film[:, :3].mean() > 0.01

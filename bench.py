@@ -360,6 +360,20 @@ def vcm_secondary(torch, ctx_cls, scene_cls, local, iters=4):
     return out
 
 
+def replica_throughput(step_ms, e2e_ms, units_per_rank, world, device="cuda"):
+    """Replicas only: every rank processes its own copy of the workload; the job's step time is the maximum
+    over ranks (all_reduce MAX on `device`: NCCL on GPUs, gloo on CPU), and the whole-job throughput is
+    world * units_per_rank per step. Returns (step_ms, e2e_ms, value, e2e) with value and e2e in M units/s."""
+    import torch
+    if world > 1:
+        t = torch.tensor([step_ms, e2e_ms], device=device, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        step_ms, e2e_ms = t.tolist()
+    value = world * units_per_rank / (step_ms * 1e-3) / 1e6
+    e2e = world * units_per_rank / (e2e_ms * 1e-3) / 1e6
+    return step_ms, e2e_ms, value, e2e
+
+
 def run_reference(args):
     rank, world, _ = _dist()
     if rank != 0:
@@ -457,16 +471,9 @@ def run_gpu(args):
             e2e_ms.append(s.elapsed_time(e))
     clk = clocks.stop()
     sc.sync(sptr)
-    step_ms = float(np.mean(ms))
-    e2e_step = float(np.mean(e2e_ms))
-    if world > 1:
-        t = torch.tensor([step_ms, e2e_step], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        step_ms, e2e_step = t.tolist()
+    step_ms, e2e_step, value, e2e = replica_throughput(float(np.mean(ms)), float(np.mean(e2e_ms)), n, world)
     if rank != 0:
         return
-    value = world * n / (step_ms * 1e-3) / 1e6
-    e2e = world * n / (e2e_step * 1e-3) / 1e6
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     hbm_peak, peak_src = 6800.0, "fallback"
     if os.path.exists(peaks_path):

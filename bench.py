@@ -19,6 +19,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import re
 import statistics
 import subprocess
 import sys
@@ -482,12 +483,15 @@ def run_gpu(args):
         peak_src = "measured"
     l2_peak = measure_l2_peak(local)
     achieved = bytes_per_ray * n / (step_ms * 1e-3) / 1e9
+    # DRAM bytes per ray of one ncu capture of this launch (dram__bytes_read.sum + dram__bytes_write.sum over the
+    # rays of the launch), kept in the kernel's profile summary as `traffic_bytes_per_ray: X`.
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "trace_closest_incoherent_1M.json")
+    prof = os.path.join(ROOT, "profiles", "trace_closest_incoherent_1M.md")
     if os.path.exists(prof):
         with open(prof) as f:
-            p = json.load(f)
-        traffic = p.get("dram_bytes_per_ray") and p["dram_bytes_per_ray"] * n
+            m = re.search(r"traffic_bytes_per_ray:\s*([0-9.]+)", f.read())
+        if m:
+            traffic = float(m.group(1)) * n
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         rate, sample, threads = cpu_oracle_rate(arrays, rays)

@@ -205,12 +205,14 @@ __device__ __forceinline__ void intersect_node(const RayQ& r, const WideNode* __
 
 // Persistent ray queries. Every warp loops until the ray list is exhausted: lanes whose ray has finished take
 // a new ray index from a global counter (one atomic per warp per refill), so short rays do not leave lanes
-// idle while the longest ray of a warp finishes. Each loop iteration either tests one leaf triangle left by
-// the previous node or visits one node.
+// idle while the longest ray of a warp finishes. POSTPONE = true: each loop iteration either tests one leaf
+// triangle left by the previous node or visits one node, so lanes in different phases stay converged (incoherent
+// rays). POSTPONE = false: a node's leaf triangles are tested in the iteration that visits it (short coherent
+// rays, fewer loop trips). Both give the same hits.
 //   ANY = false: closest hit into hits[id]; ANY = true: occlusion bit id of occ_bits (which must be zeroed).
 //   COUNT adds the nodes and triangles fetched into counters[0..1].
 // The ray count is read from *count_ptr when it is non-null, else n.
-template <bool ANY, bool COUNT>
+template <bool ANY, bool COUNT, bool POSTPONE = true>
 __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ nodes, const WideTri* __restrict__ tris,
                                                  const lgb_ray* __restrict__ rays, lgb_hit* __restrict__ hits,
                                                  uint32_t* __restrict__ occ_bits, uint32_t n, const uint32_t* count_ptr,
@@ -260,7 +262,7 @@ __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ no
         if (!__any_sync(FULL, active)) break;
         if (active) {
             bool done = false, occluded = false;
-            if (p_hits) {
+            if (POSTPONE && p_hits) {
                 // One postponed leaf triangle per iteration: a lane whose node hit many leaf triangles no longer
                 // holds its warp for all of them in one iteration (+9 % closest-hit on GB300). The triangles are
                 // tested before the next node, in the same order as an inner loop would, so hits are identical.
@@ -320,6 +322,30 @@ __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ no
                         if (COUNT) n_nodes++;
                         g_base = nb;
                         g_hm = (nhits << 8) | nimask;
+                        if (!POSTPONE) {  // all of the node's leaf triangles in this iteration
+                            while (p_hits) {
+                                const int k = __ffs(p_hits) - 1;
+                                p_hits &= p_hits - 1u;
+                                const WideTri* tp = tris + p_base + k;
+                                const float4 a = ldg4f(&tp->a), b = ldg4f(&tp->b), c = ldg4f(&tp->c);
+                                if (COUNT) n_tris++;
+                                float t, u, v;
+                                if (tri_intersect(r, a, b, c, ANY ? r.tmax : t_best, t, u, v)) {
+                                    if (ANY) {
+                                        occluded = true;
+                                        done = true;
+                                        break;
+                                    }
+                                    const uint32_t prim = __float_as_uint(a.w);
+                                    if (t < t_best || prim < best) {
+                                        t_best = t;
+                                        best = prim;
+                                        u_best = u;
+                                        v_best = v;
+                                    }
+                                }
+                            }
+                        }
                     }
                 }
             }

@@ -323,10 +323,56 @@ def batch_secondary(torch, ctx_cls, scene_cls, local):
     return res
 
 
-def vcm_secondary(torch, ctx_cls, scene_cls, local, iters=4):
-    """VCM caustics configuration: dielectric torus (200k triangles) on a diffuse plane, spot light, 1024^2,
-    one light subpath per pixel per iteration (1M), max depth 10, merge radius 0.01 x scene extent shrinking
-    with alpha = 0.75. Times `iters` iterations after one warm-up (device time per lgb_vcm_iteration)."""
+def traversal_secondary(torch, sc, rays, flush, stream, reps=10, warmup=3):
+    """The other two traversal figures of the 1M-triangle configuration, on the same BVH: 1M coherent primary
+    rays (1024^2 pinhole at (0, 0, -4) looking at the origin, fov 45 degrees, pixel centres) closest-hit, and
+    any-hit for the 4M incoherent origins with tmax = 0.5. Median of `reps` launches, L2 flushed before each."""
+    from lumen_gb300 import procedural
+    sptr = stream.cuda_stream
+    prim = torch.from_numpy(procedural.primary_rays(1024, 1024)).cuda()
+    hits = torch.empty((prim.shape[0], 4), dtype=torch.int32, device="cuda")
+    short = torch.from_numpy(rays).cuda()
+    short[:, 7] = 0.5
+    bits = torch.zeros((len(rays) + 31) // 32, dtype=torch.int32, device="cuda")
+
+    def timed(fn, prep):
+        for _ in range(warmup):
+            prep()
+            fn()
+        ts = []
+        for _ in range(reps):
+            prep()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            fn()
+            e.record(stream)
+            e.synchronize()
+            ts.append(s.elapsed_time(e))
+        return statistics.median(ts)
+
+    def prep_bits():
+        flush.fill_(1.0)
+        bits.zero_()
+
+    t_c = timed(lambda: sc.trace_closest(prim, hits, stream=sptr), lambda: flush.fill_(1.0))
+    t_a = timed(lambda: sc.trace_any(short, bits, stream=sptr), prep_bits)
+    counters = torch.zeros(2, dtype=torch.int64, device="cuda")
+    sc.trace_closest_counted(prim, hits, counters, stream=sptr)
+    sc.sync(sptr)
+    n_nodes, n_tris = (counters.cpu().numpy() / prim.shape[0]).tolist()
+    return {"coherent_closest_mrays_per_s": prim.shape[0] / (t_c * 1e-3) / 1e6,
+            "coherent_rays": int(prim.shape[0]), "coherent_nodes_per_ray": n_nodes, "coherent_tris_per_ray": n_tris,
+            "coherent_hit_fraction": float((hits[:, 0] != -1).float().mean()),
+            "incoherent_any_tmax_0.5_mrays_per_s": len(rays) / (t_a * 1e-3) / 1e6,
+            "any_occluded_fraction": float(np.unpackbits(bits.cpu().numpy().view(np.uint8)).sum()) / len(rays),
+            "l2": "flushed with a 256 MB write before every launch"}
+
+
+def vcm_secondary(torch, ctx_cls, scene_cls, local, iters=63):
+    """VCM caustics configuration: dielectric torus (200k triangles) on a diffuse plane, spot light (cone
+    half-angle 20 degrees, falloff from 25/30 of it), 1024^2, one light subpath and one eye subpath per pixel per
+    iteration (1M each), max depth 10, merge radius 0.01 x scene radius shrinking with alpha = 0.75, 64
+    iterations: the first is the warm-up, the other 63 are timed (device time per lgb_vcm_iteration)."""
     from lumen_gb300 import procedural
     from lumen_gb300.scene import camera_lookat, scene_radius, vcm_params, vcm_radius
     arrays = procedural.vcm_scene()
@@ -341,7 +387,8 @@ def vcm_secondary(torch, ctx_cls, scene_cls, local, iters=4):
     cs = stream.cuda_stream
 
     def it(i):
-        sc.vcm_iteration(cam, vcm_params(arrays, 10, vcm_radius(R, 1.0, i, 0.75), 1000 + i, 5000 + i, i), film, stream=cs)
+        sc.vcm_iteration(cam, vcm_params(arrays, 10, vcm_radius(R, 1.0, i, 0.75), 1000 + i, 5000 + i, i,
+                                         spot_angle=20.0), film, stream=cs)
 
     it(0)
     torch.cuda.synchronize()
@@ -353,9 +400,11 @@ def vcm_secondary(torch, ctx_cls, scene_cls, local, iters=4):
     e1.synchronize()
     sc.sync(cs)
     ms = e0.elapsed_time(e1) / iters
-    out = {"workload": "VCM: dielectric torus (200k triangles, IOR 1.5) on a diffuse plane, spot light L = 100, "
-                       "1024x1024, 1M light subpaths per iteration, max depth 10, radius 0.01 x extent, alpha 0.75",
-           "ms_per_iteration": ms, "light_plus_eye_paths_per_s": 2 * w * h / (ms * 1e-3),
+    out = {"workload": "VCM: dielectric torus (200k triangles, IOR 1.5) on a diffuse plane, spot light L = 100 "
+                       "with a 20 degree cone, 1024x1024, 1M light subpaths per iteration, max depth 10, radius "
+                       "0.01 x scene radius, alpha 0.75, 64 iterations",
+           "ms_per_iteration": ms, "msamples_per_s": w * h / (ms * 1e-3) / 1e6,
+           "light_plus_eye_paths_per_s": 2 * w * h / (ms * 1e-3),
            "mean_radiance": float(film[:, :3].mean()), "iterations_timed": iters}
     sc.close()
     return out
@@ -499,6 +548,7 @@ def run_gpu(args):
                "sample": f"first {sample} of the 4M incoherent rays on the oracle binary SAH BVH (build untimed)"}
     secondary = {}
     if not args.no_secondary:
+        secondary["traversal"] = traversal_secondary(torch, sc, rays, flush, stream)
         secondary["path_tracer"] = cornell_secondary(torch, Context, GpuScene, local, world == 1 and not args.no_cpu_baseline)
         secondary["adjoint"] = adjoint_secondary(torch, Context, GpuScene, local)
         secondary["batched"] = batch_secondary(torch, Context, GpuScene, local)

@@ -283,7 +283,9 @@ typedef struct lgb_vcm_params {
     uint32_t light_seed, eye_seed; /* per-iteration seeds; the reference draws them with host rand() */
     uint32_t frame_num;            /* progressive film frame: 0 overwrites, k mixes with weight 1/(k+1) */
     uint32_t flags;                /* LGB_VCM_* */
-    uint32_t reserved[2];
+    float spot_angle;              /* spot cone half-angle in degrees, (0, 90); the falloff starts at 25/30 of it.
+                                      0 keeps the reference's fixed 30 and 25 degrees (commons.glsl:264-265) */
+    uint32_t reserved;
 } lgb_vcm_params;
 
 /* Merge radius of iteration `iteration` (VCM.cpp:137-138): scene_radius * radius_factor / 100 shrunk by

@@ -129,7 +129,8 @@ class VcmParams(C.Structure):
                 ("light_triangle_count", C.c_int32), ("dir_light_idx", C.c_uint32), ("radius", C.c_float),
                 ("scene_min", C.c_float * 3), ("scene_max", C.c_float * 3), ("use_vm", C.c_int32),
                 ("use_vc", C.c_int32), ("light_seed", C.c_uint32), ("eye_seed", C.c_uint32),
-                ("frame_num", C.c_uint32), ("flags", C.c_uint32), ("reserved", C.c_uint32 * 2)]
+                ("frame_num", C.c_uint32), ("flags", C.c_uint32), ("spot_angle", C.c_float),
+                ("reserved", C.c_uint32)]
 
 
 # Every exported symbol with its argument and result types (the declarations of include/lgb.h).

@@ -93,11 +93,6 @@ __device__ __forceinline__ bool tri_intersect(const RayQ& r, float4 a, float4 b,
 __device__ __forceinline__ uint4 ldg4(const void* p) { return __ldg(reinterpret_cast<const uint4*>(p)); }
 __device__ __forceinline__ float4 ldg4f(const void* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 
-// Byte k of w as an exact float: the byte is placed under the exponent of 2^23 with one PRMT and the
-// bias is subtracted (cheaper than an integer-to-float conversion, which runs on a quarter-rate pipe).
-template <int K> __device__ __forceinline__ float byte_f(uint32_t w) {
-    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | K)) - 8388608.0f;
-}
 __device__ __forceinline__ float fmax3(float a, float b, float c) {
     float d;
     asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
@@ -120,12 +115,8 @@ __device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigne
     asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
     return d;
 }
-__device__ __forceinline__ unsigned long long add2(unsigned long long a, unsigned long long b) {
-    unsigned long long d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-// Bytes K and K+1 of w as an exact float pair (see byte_f).
+// Bytes K and K+1 of w as the float pair (2^23 + byte): each byte goes under the exponent of 2^23 with one PRMT
+// (cheaper than an integer-to-float conversion, which runs on a quarter-rate pipe).
 template <int K> __device__ __forceinline__ unsigned long long byte_pair(uint32_t w) {
     const uint32_t a = __byte_perm(w, 0x4B000000u, 0x7440u | K);
     const uint32_t b = __byte_perm(w, 0x4B000000u, 0x7440u | (K + 1));
@@ -139,13 +130,13 @@ __device__ __forceinline__ uint32_t child_pair(const RayQ& r, float tlim, uint32
                                                unsigned long long sy, unsigned long long sz, unsigned long long ax,
                                                unsigned long long ay, unsigned long long az) {
     constexpr int K = I & 3;
-    const unsigned long long bias = pk(-8388608.0f, -8388608.0f);
-    const unsigned long long tnx = fma2(add2(byte_pair<K>(nx), bias), sx, ax);
-    const unsigned long long tny = fma2(add2(byte_pair<K>(ny), bias), sy, ay);
-    const unsigned long long tnz = fma2(add2(byte_pair<K>(nz), bias), sz, az);
-    const unsigned long long tfx = fma2(add2(byte_pair<K>(fx), bias), sx, ax);
-    const unsigned long long tfy = fma2(add2(byte_pair<K>(fy), bias), sy, ay);
-    const unsigned long long tfz = fma2(add2(byte_pair<K>(fz), bias), sz, az);
+    // The byte pairs are 2^23 + q; the node offsets ax/ay/az already subtract 2^23 steps (see intersect_node).
+    const unsigned long long tnx = fma2(byte_pair<K>(nx), sx, ax);
+    const unsigned long long tny = fma2(byte_pair<K>(ny), sy, ay);
+    const unsigned long long tnz = fma2(byte_pair<K>(nz), sz, az);
+    const unsigned long long tfx = fma2(byte_pair<K>(fx), sx, ax);
+    const unsigned long long tfy = fma2(byte_pair<K>(fy), sy, ay);
+    const unsigned long long tfz = fma2(byte_pair<K>(fz), sz, az);
     const float tn0 = fmaxf(fmax3(lo_f(tnx), lo_f(tny), lo_f(tnz)), r.tmin);
     const float tf0 = fminf(fmin3(lo_f(tfx), lo_f(tfy), lo_f(tfz)), tlim);
     const float tn1 = fmaxf(fmax3(hi_f(tnx), hi_f(tny), hi_f(tnz)), r.tmin);
@@ -171,9 +162,13 @@ __device__ __forceinline__ void intersect_node(const RayQ& r, const WideNode* __
     const float fsx = __uint_as_float((e & 0xffu) << 23) * r.ix;
     const float fsy = __uint_as_float(((e >> 8) & 0xffu) << 23) * r.iy;
     const float fsz = __uint_as_float(((e >> 16) & 0xffu) << 23) * r.iz;
-    const float fax = (__uint_as_float(c0.x) - r.ox) * r.ix;
-    const float fay = (__uint_as_float(c0.y) - r.oy) * r.iy;
-    const float faz = (__uint_as_float(c0.z) - r.oz) * r.iz;
+    // Plane distance of byte q: (origin + q * step - o) * inv_dir = (2^23 + q) * fs + (fa - 2^23 * fs), so the
+    // byte decode needs no bias subtraction. Rounding fa - 2^23 * fs once costs at most half a quantisation
+    // step, inside the one step of outward margin every quantised box carries (+1.3 % closest-hit on GB300,
+    // identical hits).
+    const float fax = fmaf(-8388608.0f, fsx, (__uint_as_float(c0.x) - r.ox) * r.ix);
+    const float fay = fmaf(-8388608.0f, fsy, (__uint_as_float(c0.y) - r.oy) * r.iy);
+    const float faz = fmaf(-8388608.0f, fsz, (__uint_as_float(c0.z) - r.oz) * r.iz);
     const unsigned long long sx = pk(fsx, fsx), sy = pk(fsy, fsy), sz = pk(fsz, fsz);
     const unsigned long long ax = pk(fax, fax), ay = pk(fay, fay), az = pk(faz, faz);
     // near and far byte planes per axis: qlo is near for a positive direction component
@@ -211,20 +206,26 @@ __device__ __forceinline__ void intersect_node(const RayQ& r, const WideNode* __
 // rays, fewer loop trips). Both give the same hits.
 //   ANY = false: closest hit into hits[id]; ANY = true: occlusion bit id of occ_bits (which must be zeroed).
 //   COUNT adds the nodes and triangles fetched into counters[0..1].
+//   SK > 0: the bottom SK stack entries of each thread live in shared memory (`sstack`, SK x THREADS entries,
+//   slot-major so that a warp's lanes at different depths hit different banks); deeper entries stay in the
+//   per-thread local array.
 // The ray count is read from *count_ptr when it is non-null, else n.
-template <bool ANY, bool COUNT, bool POSTPONE = true>
+template <bool ANY, bool COUNT, bool POSTPONE = true, int SK = 0, int THREADS = 128>
 __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ nodes, const WideTri* __restrict__ tris,
                                                  const lgb_ray* __restrict__ rays, lgb_hit* __restrict__ hits,
                                                  uint32_t* __restrict__ occ_bits, uint32_t n, const uint32_t* count_ptr,
                                                  uint32_t* ray_counter, uint32_t* status,
                                                  unsigned long long* counters,
-                                                 const uint32_t* __restrict__ roots = nullptr) {
+                                                 const uint32_t* __restrict__ roots = nullptr,
+                                                 uint2* sstack = nullptr) {
+    static_assert(SK >= 0 && SK < kStackSize, "shared stack entries");
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const uint32_t lanemask_lt = (1u << lane) - 1u;
     if (count_ptr) n = *count_ptr;
     RayQ r;
-    uint2 stack[kStackSize];
+    uint2 stack[kStackSize - SK];
+    uint2* const my_stack = SK > 0 ? sstack + threadIdx.x : nullptr;
     int sp = 0;
     uint32_t ray_id = 0, g_base = 0, g_hm = 0, best = LGB_NO_HIT, visits = 0;
     float t_best = 0.0f, u_best = 0.0f, v_best = 0.0f;
@@ -292,7 +293,13 @@ __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ no
                     if (sp == 0) {
                         done = true;
                     } else {
-                        const uint2 g = stack[--sp];
+                        --sp;
+                        uint2 g;
+                        if (SK > 0 && sp < SK) {
+                            g = my_stack[sp * THREADS];
+                        } else {
+                            g = stack[sp - SK];
+                        }
                         g_base = g.x;
                         g_hm = g.y;
                         hm = g_hm >> 8;
@@ -309,7 +316,13 @@ __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ no
                             atomicOr(status, STATUS_STACK_OVERFLOW);
                             done = true;
                         } else {
-                            stack[sp++] = make_uint2(g_base, (hm << 8) | imask);
+                            const uint2 g = make_uint2(g_base, (hm << 8) | imask);
+                            if (SK > 0 && sp < SK) {
+                                my_stack[sp * THREADS] = g;
+                            } else {
+                                stack[sp - SK] = g;
+                            }
+                            ++sp;
                         }
                     }
                     if (++visits > kMaxVisits) {

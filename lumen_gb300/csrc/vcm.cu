@@ -41,6 +41,7 @@ struct VcmArgs {
     int max_depth, num_lights, light_tri_count;
     int use_vm, use_vc;
     uint32_t light_seed, eye_seed, frame_num, accumulate;
+    float spot_cos_width, spot_cos_falloff;  // cosines of the spot cone and of its falloff start
     float radius;
     float mn[3], mx[3];
     int res[3];
@@ -162,8 +163,7 @@ __device__ Emission sample_light_Le(const SceneView& S, const VcmArgs& A, float 
         e.pdf_pos_a = tri_pdf;
         e.pdf_dir_w = dot(e.wi, n) / LGB_PI;
     } else if (type == LGB_LIGHT_SPOT) {
-        const float cos_width = cosf(30.0f * LGB_PI / 180.0f);
-        const float cos_faloff = cosf(25.0f * LGB_PI / 180.0f);
+        const float cos_width = A.spot_cos_width, cos_faloff = A.spot_cos_falloff;
         const v3 lp = V3(L->pos[0], L->pos[1], L->pos[2]);
         const v3 ldir = normalize(V3(L->to[0], L->to[1], L->to[2]) - lp);
         // to_local_quat (utils.glsl:157-160), then invert_quat and rot_quat (utils.glsl:167-172)
@@ -232,7 +232,7 @@ __device__ Incidence sample_light_Li_vcm(const SceneView& S, const VcmArgs& A, f
         r.wi = wi;
         const v3 ldir = normalize(V3(L->to[0], L->to[1], L->to[2]) - lp);
         r.cos_y = dot(-wi, ldir);
-        const float cos_width = cosf(LGB_PI / 6.0f), cos_faloff = cosf(25.0f * LGB_PI / 180.0f);
+        const float cos_width = A.spot_cos_width, cos_faloff = A.spot_cos_falloff;
         float fall;
         if (r.cos_y < cos_width) fall = 0.0f;
         else if (r.cos_y >= cos_faloff) fall = 1.0f;
@@ -653,6 +653,16 @@ int to_int_rz_host(float x) {
     return (int)x;
 }
 
+// Spot cone of sample_light_Le / sample_light_Li (commons.glsl:264-265 fixes the half-angle at 30 degrees and
+// the falloff start at 25): half-angle `angle` degrees with the falloff from 25/30 of it, 0 for the fixed cone.
+// Evaluated in double on the host so the oracle gets the same two floats.
+void spot_cone(float angle, float& cos_width, float& cos_falloff) {
+    const double a = angle > 0.0f ? (double)angle : 30.0;
+    const double deg = 3.14159265358979323846 / 180.0;
+    cos_width = (float)std::cos(a * deg);
+    cos_falloff = (float)std::cos(a * (25.0 / 30.0) * deg);
+}
+
 // VCM.cpp:144-147
 void grid_resolution(const float* mn, const float* mx, float radius, int* res) {
     const float d[3] = {mx[0] - mn[0], mx[1] - mn[1], mx[2] - mn[2]};
@@ -782,6 +792,8 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
     if (!(p->radius > 0.0f) || !std::isfinite(p->radius)) return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "radius must be positive");
     for (int k = 0; k < 3; k++)
         if (!(p->scene_max[k] > p->scene_min[k])) return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "scene bounds are not a volume");
+    if (!(p->spot_angle >= 0.0f && p->spot_angle < 90.0f))
+        return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "spot_angle must be in [0, 90) degrees");
     const uint64_t screen64 = (uint64_t)cam->width * cam->height;
     const uint32_t per = (uint32_t)p->max_depth + 1u;
     if (screen64 * per >= 0x80000000ull || screen64 * 10u >= 0x80000000ull)
@@ -816,6 +828,7 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
     A.use_vm = p->use_vm; A.use_vc = p->use_vc;
     A.light_seed = p->light_seed; A.eye_seed = p->eye_seed; A.frame_num = p->frame_num;
     A.accumulate = (p->flags & LGB_VCM_ACCUMULATE) ? 1u : 0u;
+    spot_cone(p->spot_angle, A.spot_cos_width, A.spot_cos_falloff);
     A.radius = p->radius;
     grid_resolution(A.mn, A.mx, A.radius, A.res);
     A.verts = reinterpret_cast<float4*>(base + o_verts);

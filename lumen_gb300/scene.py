@@ -379,9 +379,10 @@ class Batch:
 
 
 def vcm_params(arrays: SceneArrays, max_depth: int, radius: float, light_seed: int, eye_seed: int, frame_num: int,
-               use_vm: int = 1, use_vc: int = 1, sky=(0.0, 0.0, 0.0), flags: int = 0) -> abi.VcmParams:
+               use_vm: int = 1, use_vc: int = 1, sky=(0.0, 0.0, 0.0), flags: int = 0,
+               spot_angle: float = 0.0) -> abi.VcmParams:
     """PCVCM as VCM::render fills it (src/RayTracer/VCM.cpp:131-147) with explicit seeds; the grid bounds are the
-    scene's bounding box."""
+    scene's bounding box. spot_angle: spot cone half-angle in degrees (0: the reference's fixed 30)."""
     p = abi.VcmParams()
     p.sky_col[:] = list(sky)
     p.max_depth = max_depth
@@ -398,6 +399,7 @@ def vcm_params(arrays: SceneArrays, max_depth: int, radius: float, light_seed: i
     p.eye_seed = eye_seed
     p.frame_num = frame_num
     p.flags = flags
+    p.spot_angle = spot_angle
     return p
 
 

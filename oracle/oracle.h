@@ -141,6 +141,7 @@ struct orc_vcm_params {
     uint32_t frame_num;
     float scene_min[3], scene_max[3];
     uint32_t flags;  // bit 0: accumulate every connection and merge instead of keeping the last (`res =`)
+    float spot_angle;  // spot cone half-angle in degrees (falloff from 25/30 of it); 0: fixed 30 and 25 degrees
 };
 // VCMVertex, vcm_commons.h:89-104 (104 bytes).
 struct orc_vcm_vertex {

@@ -86,7 +86,17 @@ template <class T> struct Emission {
     T cos_from_light, pdf_pos_a, pdf_dir_w;
     uint32_t flags;
 };
-template <class T> Emission<T> sample_light_Le(const Scene& s, V4<T> rp, V2<T> rd, int num_lights, int total_light) {
+// Spot cone: half-angle `angle` degrees, falloff from 25/30 of it; 0 gives commons.glsl:264-265's fixed 30 and
+// 25 degrees. Computed in double and rounded once, as the library's host code does.
+struct Cone { float cos_width, cos_falloff; };
+Cone spot_cone(float angle) {
+    const double a = angle > 0.0f ? (double)angle : 30.0;
+    const double deg = 3.14159265358979323846 / 180.0;
+    return Cone{(float)std::cos(a * deg), (float)std::cos(a * (25.0 / 30.0) * deg)};
+}
+
+template <class T> Emission<T> sample_light_Le(const Scene& s, V4<T> rp, V2<T> rd, int num_lights, int total_light,
+                                              Cone cone) {
     Emission<T> e;
     const uint32_t light_idx = (uint32_t)(rp.x * T(num_lights));
     const orc_light& light = s.lights[light_idx];
@@ -110,8 +120,7 @@ template <class T> Emission<T> sample_light_Le(const Scene& s, V4<T> rp, V2<T> r
         e.pdf_dir_w = dot(e.wi, n) / K<T>::PI();
         e.n = n;
     } else if (type == LIGHT_SPOT) {
-        const T cos_width = std::cos(T(30) * K<T>::PI() / T(180));
-        const T cos_faloff = std::cos(T(25) * K<T>::PI() / T(180));
+        const T cos_width = T(cone.cos_width), cos_faloff = T(cone.cos_falloff);
         const V3<T> lp(light.pos[0], light.pos[1], light.pos[2]), to(light.to[0], light.to[1], light.to[2]);
         const V3<T> light_dir = normalize(to - lp);
         V4q<T> q = to_local_quat(light_dir);
@@ -138,7 +147,7 @@ template <class T> struct Incidence {
     T wi_len, pdf_pos_w, pdf_pos_dir_w, cos_y;
     uint32_t flags;
 };
-template <class T> Incidence<T> sample_light_Li_vcm(const Scene& s, V4<T> rp, V3<T> p, int num_lights) {
+template <class T> Incidence<T> sample_light_Li_vcm(const Scene& s, V4<T> rp, V3<T> p, int num_lights, Cone cone) {
     Incidence<T> r;
     const uint32_t light_idx = (uint32_t)(rp.x * T(num_lights));
     const orc_light& light = s.lights[light_idx];
@@ -169,8 +178,7 @@ template <class T> Incidence<T> sample_light_Li_vcm(const Scene& s, V4<T> rp, V3
         r.wi = wi;
         const V3<T> light_dir = normalize(to - lp);
         r.cos_y = dot(-wi, light_dir);
-        const T cos_width = std::cos(K<T>::PI() / T(6));
-        const T cos_faloff = std::cos(T(25) * K<T>::PI() / T(180));
+        const T cos_width = T(cone.cos_width), cos_faloff = T(cone.cos_falloff);
         T faloff;
         if (r.cos_y < cos_width) faloff = T(0);
         else if (r.cos_y >= cos_faloff) faloff = T(1);
@@ -285,7 +293,7 @@ void light_path(const Scene& s, const Cam& c, const orc_vcm_params* p, const Eta
     const float r0 = rand(seed), r1 = rand(seed), r2 = rand(seed), r3 = rand(seed);
     const float r4 = rand(seed), r5 = rand(seed);
     const Emission<float> e = sample_light_Le<float>(s, V4<float>(r0, r1, r2, r3), V2<float>(r4, r5), p->num_lights,
-                                                     p->light_triangle_count);
+                                                     p->light_triangle_count, spot_cone(p->spot_angle));
     if (e.pdf_dir_w <= 0.0f) {  // the reference returns here and leaves the previous iteration's count
         counts[li] = 0;
         return;
@@ -373,7 +381,8 @@ V3<float> connect_light(const Scene& s, const orc_vcm_params* p, U4& seed, const
                         const Mat<float>& mat, bool side, float eta_vm, const VState& cs, float& pdf_rev) {
     V3<float> res(0.0f);
     const float q0 = rand(seed), q1 = rand(seed), q2 = rand(seed), q3 = rand(seed);
-    const Incidence<float> li = sample_light_Li_vcm<float>(s, V4<float>(q0, q1, q2, q3), h.pos, p->num_lights);
+    const Incidence<float> li = sample_light_Li_vcm<float>(s, V4<float>(q0, q1, q2, q3), h.pos, p->num_lights,
+                                                              spot_cone(p->spot_angle));
     const float cos_x = dot(li.wi, n_s);
     const V3<float> origin = offset_ray2(h.pos, n_s);
     float pdf_fwd;

@@ -48,7 +48,7 @@ class VcmParams(C.Structure):
                 ("light_triangle_count", C.c_int32), ("radius", C.c_float), ("use_vm", C.c_int32),
                 ("use_vc", C.c_int32), ("light_seed", C.c_uint32), ("eye_seed", C.c_uint32),
                 ("frame_num", C.c_uint32), ("scene_min", C.c_float * 3), ("scene_max", C.c_float * 3),
-                ("flags", C.c_uint32)]
+                ("flags", C.c_uint32), ("spot_angle", C.c_float)]
 
 
 VCM_VERTEX_BYTES = 104

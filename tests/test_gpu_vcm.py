@@ -52,7 +52,7 @@ def test_photon_table_is_bit_exact(ctx, oracle):
     assert int(count.abs().sum()) == 0
 
 
-def _run_both(ctx, oracle, arrays, w, h, iters, depth, flags=0, use_vm=1, alpha=2.0 / 3.0, factor=1.0):
+def _run_both(ctx, oracle, arrays, w, h, iters, depth, flags=0, use_vm=1, alpha=2.0 / 3.0, factor=1.0, spot_angle=0.0):
     from oracle_lib import VcmParams
     sc = GpuScene(ctx, arrays)
     sc.build()
@@ -64,11 +64,11 @@ def _run_both(ctx, oracle, arrays, w, h, iters, depth, flags=0, use_vm=1, alpha=
     R = scene_radius(arrays)
     for it in range(iters):
         r = vcm_radius(R, factor, it, alpha)
-        p = vcm_params(arrays, depth, r, 1000 + it, 5000 + it, it, use_vm=use_vm, flags=flags)
+        p = vcm_params(arrays, depth, r, 1000 + it, 5000 + it, it, use_vm=use_vm, flags=flags, spot_angle=spot_angle)
         sc.vcm_iteration(cam, p, film)
         op = VcmParams()
         for name in ("max_depth", "num_lights", "light_triangle_count", "radius", "use_vm", "use_vc", "light_seed",
-                     "eye_seed", "frame_num", "flags"):
+                     "eye_seed", "frame_num", "flags", "spot_angle"):
             setattr(op, name, getattr(p, name))
         op.sky_col[:] = list(p.sky_col)
         op.scene_min[:] = list(p.scene_min)
@@ -91,14 +91,24 @@ def test_iteration_matches_oracle_cornell(ctx, oracle):
     assert close_fraction(got8[:, :3], want8[:, :3]) >= 0.9
 
 
-def test_caustics_scene_with_merging_matches_oracle(ctx, oracle):
+@pytest.mark.parametrize("spot_angle", [0.0, 20.0])
+def test_caustics_scene_with_merging_matches_oracle(ctx, oracle, spot_angle):
     arrays = procedural.vcm_scene(100, 40)
-    got, want = _run_both(ctx, oracle, arrays, 64, 64, 4, 10, alpha=0.75)
+    got, want = _run_both(ctx, oracle, arrays, 64, 64, 4, 10, alpha=0.75, spot_angle=spot_angle)
     assert not np.isnan(got).any()
     frac = close_fraction(got[:, :3], want[:, :3])
     assert frac >= 0.95, f"only {frac:.4f} of pixels agree"
     np.testing.assert_allclose(got[:, :3].mean(0), want[:, :3].mean(0), rtol=0.02)
     assert got[:, :3].mean() > 0.0
+
+
+def test_spot_cone_narrows_the_lit_area(ctx, oracle):
+    arrays = procedural.vcm_scene(100, 40)
+    wide, _ = _run_both(ctx, oracle, arrays, 48, 48, 1, 4, alpha=0.75)
+    narrow, want = _run_both(ctx, oracle, arrays, 48, 48, 1, 4, alpha=0.75, spot_angle=10.0)
+    assert close_fraction(narrow[:, :3], want[:, :3]) >= 0.95
+    lit = lambda img: int((img[:, :3].sum(1) > 1e-4).sum())
+    assert 0 < lit(narrow) < lit(wide)
 
 
 def test_accumulate_option_matches_oracle(ctx, oracle):
@@ -115,7 +125,8 @@ def test_vcm_error_paths(ctx):
     sc.build()
     cam = camera_lookat(cb.camera_pos, cb.camera_dir, cb.fov, 16, 16)
     film = torch.zeros((256, 4), dtype=torch.float32, device="cuda")
-    for bad in (dict(max_depth=0), dict(radius=0.0), dict(num_lights=0)):
+    for bad in (dict(max_depth=0), dict(radius=0.0), dict(num_lights=0), dict(spot_angle=90.0),
+                dict(spot_angle=-1.0), dict(spot_angle=float("nan"))):
         p = vcm_params(cb, 8, 0.01, 1, 2, 0)
         for k, v in bad.items():
             setattr(p, k, v)

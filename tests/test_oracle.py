@@ -271,7 +271,7 @@ def test_vcm_photon_table_matches_independent_restatement(oracle):
     assert count.sum() == (pos4[:, 3] >= 0).sum() and (count > 1).any()
 
 
-def _vcm_oracle_run(oracle, arrays, w, h, iters, depth, flags, use_vm=1):
+def _vcm_oracle_run(oracle, arrays, w, h, iters, depth, flags, use_vm=1, spot_angle=0.0, alpha=2.0 / 3.0):
     from oracle_lib import VcmParams
     from lumen_gb300.scene import camera_lookat, camera_forward, scene_radius, vcm_radius
     sc = oracle.scene(arrays)
@@ -284,7 +284,8 @@ def _vcm_oracle_run(oracle, arrays, w, h, iters, depth, flags, use_vm=1):
         p.max_depth, p.num_lights, p.light_triangle_count = depth, len(arrays.lights), arrays.light_triangle_count
         p.scene_min[:] = [float(v) for v in arrays.positions.min(0)]
         p.scene_max[:] = [float(v) for v in arrays.positions.max(0)]
-        p.radius = vcm_radius(R, 1.0, it, 2.0 / 3.0)
+        p.radius = vcm_radius(R, 1.0, it, alpha)
+        p.spot_angle = spot_angle
         p.use_vm, p.use_vc = use_vm, 1
         p.light_seed, p.eye_seed, p.frame_num, p.flags = 1000 + it, 5000 + it, it, flags
         sc.vcm_iteration(cam, view, proj, p, st)
@@ -306,3 +307,14 @@ def test_vcm_oracle_is_deterministic_and_energy_consistent(oracle):
     vcm_mean, pt_mean = st["film"][:, :3].mean(), pt[:, :3].mean()
     assert abs(vcm_mean - pt_mean) < 0.03 * pt_mean, (vcm_mean, pt_mean)
     assert not np.isnan(st["film"]).any()
+
+
+def test_vcm_oracle_spot_cone(oracle):
+    """The spot cone parameter: 30 degrees equals the reference's fixed cone exactly; a 10 degree cone lights
+    fewer pixels of the caustics scene than the fixed one, and a 20 degree one sits between them."""
+    arrays = procedural.vcm_scene(60, 24)
+    films = {a: _vcm_oracle_run(oracle, arrays, 32, 32, 1, 4, 0, spot_angle=a, alpha=0.75)[2]["film"]
+             for a in (0.0, 30.0, 20.0, 10.0)}
+    assert np.array_equal(films[0.0], films[30.0])
+    lit = {a: int((f[:, :3].sum(1) > 1e-4).sum()) for a, f in films.items()}
+    assert 0 < lit[10.0] < lit[20.0] < lit[0.0], lit

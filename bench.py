@@ -174,12 +174,7 @@ def cornell_secondary(torch, ctx_cls, scene_cls, local, cpu_leg: bool):
     out = {"workload": "Cornell box 36 triangles, 256x256, 16 spp, max depth 8, FP32", "ms": ms,
            "msamples_per_s": w * h * spp / (ms * 1e-3) / 1e6, "mean_radiance": float(film[:, :3].mean()),
            "graph": "bounce loop captured once as a CUDA graph and replayed"}
-    ref_path = os.path.join(ROOT, "tests", "golden", "cornell_256_fp64_ref.npy")
-    if os.path.exists(ref_path):
-        from lumen_gb300.scene import film_rmse
-        ref = np.load(ref_path).reshape(-1, 3)
-        ref4 = torch.from_numpy(np.concatenate([ref, np.ones((len(ref), 1), np.float32)], 1)).cuda()
-        out["rmse_vs_fp64_2048spp"] = film_rmse(ctx, film, ref4, 0)
+    out["rmse_vs_fp64_2048spp"] = reference_rmse(torch, ctx, film, "cornell_256_fp64_ref.npy")
     if cpu_leg:
         sys.path.insert(0, os.path.join(ROOT, "tests"))
         import oracle_lib
@@ -192,6 +187,18 @@ def cornell_secondary(torch, ctx_cls, scene_cls, local, cpu_leg: bool):
         out["cpu_baseline"] = {"value": w * h * 2 / dt / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
                                "sample": "frames 0-1 of the same render"}
     return out
+
+
+def reference_rmse(torch, ctx, film, name):
+    """RMSE (lgb_film_rmse, RGB) of an (N, 4) CUDA film against a committed converged render in tests/golden, or
+    None when the file is absent."""
+    from lumen_gb300.scene import film_rmse
+    path = os.path.join(ROOT, "tests", "golden", name)
+    if not os.path.exists(path):
+        return None
+    ref = np.load(path).reshape(-1, 3)
+    ref4 = torch.from_numpy(np.concatenate([ref, np.ones((len(ref), 1), np.float32)], 1)).cuda()
+    return film_rmse(ctx, film, ref4, 0)
 
 
 def adjoint_secondary(torch, ctx_cls, scene_cls, local):
@@ -243,10 +250,12 @@ def adjoint_secondary(torch, ctx_cls, scene_cls, local):
         ta.append(e[1].elapsed_time(e[2]))
     sc.sync(cs)
     mp, ma = float(np.median(tp)), float(np.median(ta))
+    rmse = reference_rmse(torch, ctx, film, "diff_512_fp64_ref.npy")
     return {"workload": "differentiable Cornell box, 512x512, 32 spp, max depth 6, 64x64 RGB texels + per-material "
                         "roughness + emission, L2 image loss", "primal_ms": mp, "adjoint_ms": ma,
             "primal_plus_adjoint_over_primal": (mp + ma) / mp,
             "primal_msamples_per_s": w * h * spp / (mp * 1e-3) / 1e6,
+            "primal_rmse_vs_fp64_512spp": rmse,
             "grad_norms": {"texels": float(gt.norm()), "roughness": float(gr.norm()), "emission": float(ge.norm())}}
 
 
@@ -315,7 +324,8 @@ def batch_secondary(torch, ctx_cls, scene_cls, local):
            "per_scene_msamples_per_s": samples / (ms_alone * 1e-3) / 1e6,
            "batched_msamples_per_s": samples / (ms_batch * 1e-3) / 1e6,
            "speedup": ms_alone / ms_batch, "films_max_abs_diff": max_diff,
-           "tuned": {"path_capacity": best.path_capacity, "work_blocks_per_sm": best.work_blocks_per_sm},
+           "tuned": {"path_capacity": best.path_capacity, "work_blocks_per_sm": best.work_blocks_per_sm,
+                     "stack": "shared" if best.stack_placement == 1 else "local"},
            "tune_s": tune_s, "scene_generation_s": gen_s}
     batch.close()
     for sc in scenes:
@@ -400,12 +410,22 @@ def vcm_secondary(torch, ctx_cls, scene_cls, local, iters=63):
     e1.synchronize()
     sc.sync(cs)
     ms = e0.elapsed_time(e1) / iters
+    # convergence: the same 64 iterations at 256^2 against the committed 1024-iteration oracle render
+    w2 = h2 = 256
+    cam2 = camera_lookat(arrays.camera_pos, arrays.camera_dir, arrays.fov, w2, h2)
+    film2 = torch.zeros((w2 * h2, 4), dtype=torch.float32, device="cuda")
+    for i in range(64):
+        sc.vcm_iteration(cam2, vcm_params(arrays, 10, vcm_radius(R, 1.0, i, 0.75), 1000 + i, 5000 + i, i,
+                                          spot_angle=20.0), film2, stream=cs)
+    sc.sync(cs)
+    rmse = reference_rmse(torch, ctx, film2, "vcm_torus_256_ref.npy")
     out = {"workload": "VCM: dielectric torus (200k triangles, IOR 1.5) on a diffuse plane, spot light L = 100 "
                        "with a 20 degree cone, 1024x1024, 1M light subpaths per iteration, max depth 10, radius "
                        "0.01 x scene radius, alpha 0.75, 64 iterations",
            "ms_per_iteration": ms, "msamples_per_s": w * h / (ms * 1e-3) / 1e6,
            "light_plus_eye_paths_per_s": 2 * w * h / (ms * 1e-3),
-           "mean_radiance": float(film[:, :3].mean()), "iterations_timed": iters}
+           "mean_radiance": float(film[:, :3].mean()), "iterations_timed": iters,
+           "rmse_256_64it_vs_oracle_1024it": rmse}
     sc.close()
     return out
 
@@ -580,6 +600,25 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+LEGS = ("path_tracer", "adjoint", "batched", "vcm")
+
+
+def run_leg(name):
+    import torch
+    from lumen_gb300.scene import Context, GpuScene
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if name == "path_tracer":
+        out = cornell_secondary(torch, Context, GpuScene, local, False)
+    elif name == "adjoint":
+        out = adjoint_secondary(torch, Context, GpuScene, local)
+    elif name == "batched":
+        out = batch_secondary(torch, Context, GpuScene, local)
+    else:
+        out = vcm_secondary(torch, Context, GpuScene, local)
+    print(json.dumps({"leg": name, **out}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -587,11 +626,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-secondary", action="store_true", help="skip the Cornell-box path-tracer measurement")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the secondary measurements (other traversal figures, path tracer, adjoint, batched, VCM)")
+    ap.add_argument("--leg", choices=sorted(LEGS),
+                    help="run one secondary measurement alone and print its JSON (for profiling that workload)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.leg:
+        run_leg(args.leg)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

@@ -332,8 +332,12 @@ typedef struct lgb_batch_opts {
     uint32_t path_capacity;        /* paths in flight per chunk (the queue size); 0 = 2^21 */
     uint32_t work_blocks_per_sm;   /* grid of the camera, shading and film kernels; 0 = 8 */
     uint32_t trace_blocks_per_sm;  /* grid of the persistent traversal kernels; 0 = as many as fit */
-    uint32_t reserved[5];
+    uint32_t stack_placement;      /* traversal stack: LGB_STACK_LOCAL (0) per-thread local memory, or
+                                      LGB_STACK_SHARED: its bottom 8 entries in shared memory */
+    uint32_t reserved[4];
 } lgb_batch_opts;
+#define LGB_STACK_LOCAL 0u
+#define LGB_STACK_SHARED 1u
 
 /* Copies the BVHs of `scenes` (each built with lgb_bvh_build) into one forest. The scenes must outlive the
  * batch; rebuilding a scene's BVH afterwards makes lgb_batch_render refuse the batch (LGB_ERR_NOT_READY). */

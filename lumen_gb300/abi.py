@@ -118,9 +118,11 @@ class BatchJob(C.Structure):
 
 class BatchOpts(C.Structure):
     _fields_ = [("path_capacity", C.c_uint32), ("work_blocks_per_sm", C.c_uint32),
-                ("trace_blocks_per_sm", C.c_uint32), ("reserved", C.c_uint32 * 5)]
+                ("trace_blocks_per_sm", C.c_uint32), ("stack_placement", C.c_uint32),
+                ("reserved", C.c_uint32 * 4)]
 
 
+STACK_LOCAL, STACK_SHARED = 0, 1  # lgb_batch_opts.stack_placement
 VCM_ACCUMULATE = 1
 
 

@@ -191,20 +191,29 @@ __global__ void __launch_bounds__(kThreads) k_camera(const Params* __restrict__ 
 //   leaf triangles in one iteration, 1 block   414 / 277
 //   one postponed triangle per iteration, 9    392 / 294
 //   one postponed triangle per iteration, 1    336 / 280
-// The stack stays in local memory here: 8 bottom entries in shared memory cost 1 % (465 / 296).
+// SK: bottom stack entries per thread in shared memory (0: the whole stack in local memory, the default here:
+// 8 shared entries cost 1 % on the two scenes above, 465 / 296). The batch autotuner tries both placements.
 constexpr bool kQueuePostpone = false;
 constexpr int kQueueTraceMinBlocks = 9;
+constexpr int kQueueSharedStack = 8;  // entries when the stack placement is LGB_STACK_SHARED
+// Idle lanes a warp waits for before fetching new rays. Cornell / batch scene, Msamples/s, with the MIS
+// pre-test of k_shade: refill at 8 idle lanes 542 / 356, at 16: 550 / 354, at 32: 566 / 329.
+constexpr int kQueueRefill = 16;
+template <int SK>
 __global__ void __launch_bounds__(kThreads, kQueueTraceMinBlocks)
     k_q_trace_closest(SceneView S, const lgb_ray* __restrict__ rays, lgb_hit* __restrict__ hits,
                       const uint32_t* count_ptr, uint32_t* ray_counter, const uint32_t* __restrict__ roots) {
-    trace_persistent<false, false, kQueuePostpone>(
-        S.nodes, S.tris, rays, hits, nullptr, 0u, count_ptr, ray_counter, S.status, nullptr, roots);
+    __shared__ uint2 s_stack[SK > 0 ? SK * kThreads : 1];
+    trace_persistent<false, false, kQueuePostpone, SK, kThreads, kQueueRefill>(
+        S.nodes, S.tris, rays, hits, nullptr, 0u, count_ptr, ray_counter, S.status, nullptr, roots, s_stack);
 }
+template <int SK>
 __global__ void __launch_bounds__(kThreads, kQueueTraceMinBlocks)
     k_q_trace_any(SceneView S, const lgb_ray* __restrict__ rays, uint32_t* __restrict__ bits,
                   const uint32_t* count_ptr, uint32_t* ray_counter, const uint32_t* __restrict__ roots) {
-    trace_persistent<true, false, kQueuePostpone>(
-        S.nodes, S.tris, rays, nullptr, bits, 0u, count_ptr, ray_counter, S.status, nullptr, roots);
+    __shared__ uint2 s_stack[SK > 0 ? SK * kThreads : 1];
+    trace_persistent<true, false, kQueuePostpone, SK, kThreads, kQueueRefill>(
+        S.nodes, S.tris, rays, nullptr, bits, 0u, count_ptr, ray_counter, S.status, nullptr, roots, s_stack);
 }
 
 // path.rgen:49-55: a miss adds the sky colour (shade_atmosphere without a directional light returns
@@ -269,8 +278,11 @@ __device__ __forceinline__ v3 cls_eval(v3 n_s, v3 wo, const Mat& m, bool ff, v3 
 }
 
 // One bounce of path.rgen:56-100 for the hits of one material class.
+// Registers capped for 4 blocks per SM (128): the diffuse kernel reads and writes ~400 B of path state per path
+// and wants occupancy (Cornell / batch scene 550 / 354 Msamples/s against 549 / 349 uncapped at 140 registers).
+constexpr int kShadeMinBlocks = 4;
 template <int CLS, bool BATCH>
-__global__ void __launch_bounds__(kThreads) k_shade(SceneView S0, const Params* __restrict__ Pp, Buffers B, int depth) {
+__global__ void __launch_bounds__(kThreads, kShadeMinBlocks) k_shade(SceneView S0, const Params* __restrict__ Pp, Buffers B, int depth) {
     const uint32_t n = B.counters[3 + CLS];
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t* list = B.q_cls + (size_t)CLS * B.cap;
@@ -322,12 +334,14 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneView S0, const Params* 
                     const uint32_t lflags = L->light_flags, ltype = lflags & 7u;
                     v3 Le = V3(0.0f), wi = V3(0.0f);
                     float wi_len = 0.0f, pdf_w = 0.0f, pdf_a = 0.0f;
-                    uint32_t lprim = LGB_NO_HIT;
+                    uint32_t lprim = LGB_NO_HIT, lio = 0u, lvo = 0u;
                     if (ltype == LGB_LIGHT_AREA) {
                         const lgb_mesh pm = S.meshes[L->prim_mesh_idx];
                         const uint32_t tri = (uint32_t)(q1 * (float)L->num_triangles);
                         lprim = S.mesh_first[L->prim_mesh_idx] + tri;
                         const uint32_t io = pm.index_offset + 3u * tri;
+                        lio = io;
+                        lvo = pm.vertex_offset;
                         const DevVertex a = S.verts[S.idx[io] + pm.vertex_offset];
                         const DevVertex b = S.verts[S.idx[io + 1] + pm.vertex_offset];
                         const DevVertex c = S.verts[S.idx[io + 2] + pm.vertex_offset];
@@ -392,6 +406,22 @@ __global__ void __launch_bounds__(kThreads) k_shade(SceneView S0, const Params* 
                         f2 = cls_sample<CLS>(n_s, wo, m, side, wi2, pdf2, cos2, V3(b0r, b1r, b2r));
                     }
                     mray = make_ray(sp, kTMin, wi2, pdf2 != 0.0f ? kTMax : -1.0f);
+                    // The MIS ray only counts when its closest hit is the sampled light triangle. Unless the
+                    // shading point is on that triangle (a miss then reuses the shading point's own payload), a
+                    // ray that fails the traversal's watertight test against it (same ray, same vertices) cannot
+                    // count: it gets an empty interval, which the trace kernel ends at once as a miss, and a miss
+                    // resolves to no contribution exactly as the traced ray would have.
+                    if (pdf2 != 0.0f && lprim != hit.prim) {
+                        const DevVertex a = S.verts[S.idx[lio] + lvo];
+                        const DevVertex b = S.verts[S.idx[lio + 1] + lvo];
+                        const DevVertex c = S.verts[S.idx[lio + 2] + lvo];
+                        const RayQ rq = make_rayq(mray.ox, mray.oy, mray.oz, mray.tmin, mray.dx, mray.dy, mray.dz,
+                                                  mray.tmax);
+                        float tt, tu, tv;
+                        if (!tri_intersect(rq, make_float4(a.px, a.py, a.pz, 0.0f), make_float4(b.px, b.py, b.pz, 0.0f),
+                                           make_float4(c.px, c.py, c.pz, 0.0f), rq.tmax, tt, tu, tv))
+                            mray.tmax = -1.0f;
+                    }
                     rec.term1 = f4(term1, pdf_w);
                     rec.T = f4(T, lpp);
                     rec.f2 = f4(f2, pdf2);
@@ -594,13 +624,32 @@ size_t carve(char* base, uint32_t cap, Buffers& B, bool batch = false) {
 
 struct Grids {
     int work, trace;
+    bool shared_stack;  // the traversal kernels keep the bottom of their stack in shared memory
 };
 
-Grids path_grids(Ctx* ctx) {
+Grids path_grids(Ctx* ctx, bool shared_stack = false) {
     int trace_blocks = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&trace_blocks, k_q_trace_closest, kThreads, 0);
+    if (shared_stack)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&trace_blocks, k_q_trace_closest<kQueueSharedStack>, kThreads, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&trace_blocks, k_q_trace_closest<0>, kThreads, 0);
     const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
-    return Grids{sms * 8, sms * std::max(trace_blocks, 1)};
+    return Grids{sms * 8, sms * std::max(trace_blocks, 1), shared_stack};
+}
+
+template <int SK> void launch_queue_traces(const SceneView& S, const Buffers& B, Grids g, cudaStream_t st, bool first) {
+    if (first) {
+        k_q_trace_closest<SK><<<g.trace, kThreads, 0, st>>>(S, B.rays, B.hits, B.counters + 0, B.counters + 8, B.root);
+    } else {
+        k_q_trace_any<SK><<<g.trace, kThreads, 0, st>>>(S, B.srays, B.sbits, B.counters + 2, B.counters + 9, B.nroot);
+        k_q_trace_closest<SK><<<g.trace, kThreads, 0, st>>>(S, B.mrays, B.mhits, B.counters + 2, B.counters + 10,
+                                                            B.nroot);
+    }
+}
+// first: the continuation rays' closest hits; else the shadow rays and the BSDF-MIS rays of the bounce.
+void queue_traces(const SceneView& S, const Buffers& B, Grids g, cudaStream_t st, bool first) {
+    if (g.shared_stack) launch_queue_traces<kQueueSharedStack>(S, B, g, st, first);
+    else launch_queue_traces<0>(S, B, g, st, first);
 }
 
 // One chunk of frames: camera rays, `bounces` bounces, film. Every kernel reads its parameters from device
@@ -611,15 +660,14 @@ cudaError_t launch_chunk(const SceneView& S, Buffers B, int bounces, Grids g, cu
     k_init_counters<BATCH><<<1, 32, 0, st>>>(B, B.params);
     k_camera<BATCH><<<g.work, kThreads, 0, st>>>(B.params, B);
     for (int depth = 0; depth < bounces; depth++) {
-        k_q_trace_closest<<<g.trace, kThreads, 0, st>>>(S, B.rays, B.hits, B.counters + 0, B.counters + 8, B.root);
+        queue_traces(S, B, g, st, true);
         k_classify<BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B);
         k_shade<CLS_DIFFUSE, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
         k_shade<CLS_CONDUCTOR, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
         k_shade<CLS_SPECULAR, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
         k_shade<CLS_PRINCIPLED, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
         k_clear_bits<<<g.work, kThreads, 0, st>>>(B.sbits, B.counters + 2);
-        k_q_trace_any<<<g.trace, kThreads, 0, st>>>(S, B.srays, B.sbits, B.counters + 2, B.counters + 9, B.nroot);
-        k_q_trace_closest<<<g.trace, kThreads, 0, st>>>(S, B.mrays, B.mhits, B.counters + 2, B.counters + 10, B.nroot);
+        queue_traces(S, B, g, st, false);
         k_nee_resolve<BATCH><<<g.work, kThreads, 0, st>>>(S, B);
         k_rotate<<<1, 32, 0, st>>>(B.counters);
         std::swap(B.rays, B.rays_next);
@@ -972,7 +1020,9 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
     }
     carve((char*)b->buf, cap, B, true);
     const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
-    Grids g = path_grids(ctx);
+    if (o.stack_placement > LGB_STACK_SHARED)
+        return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "stack_placement must be LGB_STACK_LOCAL or LGB_STACK_SHARED");
+    Grids g = path_grids(ctx, o.stack_placement == LGB_STACK_SHARED);
     if (o.work_blocks_per_sm) g.work = sms * (int)std::min(o.work_blocks_per_sm, 64u);
     if (o.trace_blocks_per_sm) g.trace = std::min(g.trace, sms * (int)o.trace_blocks_per_sm);
 
@@ -996,8 +1046,9 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
     cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
     LGB_CUDA_TRY(ctx, cudaStreamIsCapturing(st, &cap_status));
     const bool use_graph = cap_status == cudaStreamCaptureStatusNone;
-    const uint64_t key[6] = {(uint64_t)(uintptr_t)b->buf, cap, (uint64_t)bounces, (uint64_t)(uintptr_t)b->nodes,
-                             (uint64_t)(uintptr_t)b->tris, ((uint64_t)g.work << 32) | (uint32_t)g.trace};
+    const uint64_t key[6] = {(uint64_t)(uintptr_t)b->buf, cap, (uint64_t)bounces | ((uint64_t)g.shared_stack << 32),
+                             (uint64_t)(uintptr_t)b->nodes, (uint64_t)(uintptr_t)b->tris,
+                             ((uint64_t)g.work << 32) | (uint32_t)g.trace};
     if (use_graph && (!b->graph || std::memcmp(key, b->graph_key, sizeof(key)) != 0)) {
         if (b->graph) { cudaGraphExecDestroy((cudaGraphExec_t)b->graph); b->graph = nullptr; }
         if (!b->capture_stream) LGB_CUDA_TRY(ctx, cudaStreamCreateWithFlags((cudaStream_t*)&b->capture_stream, cudaStreamNonBlocking));
@@ -1026,8 +1077,9 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
     return LGB_OK;
 }
 
-// Times every candidate (queue size x shading grid) on a quarter of each job's frames, films untouched; the
-// first run of a candidate records its graph, the second is timed.
+// Times every candidate (queue size x shading grid, stack in local memory) on a quarter of each job's frames,
+// films untouched, then the best of them with the stack bottom in shared memory; the first run of a candidate
+// records its graph, the second is timed.
 lgb_status batch_tune(Batch* b, const lgb_batch_job* jobs, uint32_t n, lgb_batch_opts* best, cudaStream_t st) {
     Ctx* ctx = b->ctx;
     std::vector<lgb_batch_job> reduced(jobs, jobs + n);
@@ -1045,24 +1097,33 @@ lgb_status batch_tune(Batch* b, const lgb_batch_job* jobs, uint32_t n, lgb_batch
     lgb_batch_opts best_o{};
     bool have = false;
     lgb_status result = LGB_OK;
+    auto trial = [&](const lgb_batch_opts& o) {
+        float ms = 0.0f;
+        for (int rep = 0; rep < 2 && result == LGB_OK; rep++) {
+            cudaEventRecord(e0, st);
+            result = batch_render(b, reduced.data(), n, o, false, st);
+            cudaEventRecord(e1, st);
+            if (result == LGB_OK && cudaEventSynchronize(e1) != cudaSuccess) result = cuda_error(ctx, cudaGetLastError(), "batch tuning");
+            if (result == LGB_OK) cudaEventElapsedTime(&ms, e0, e1);
+        }
+        if (result == LGB_OK && (!have || ms < best_ms)) { best_ms = ms; best_o = o; have = true; }
+    };
     for (uint32_t c : caps) {
         if (c < max_npix && c != caps[2]) continue;  // smaller than one frame: the larger candidates cover it
         for (uint32_t w : works) {
             lgb_batch_opts o{};
             o.path_capacity = c;
             o.work_blocks_per_sm = w;
-            float ms = 0.0f;
-            for (int rep = 0; rep < 2 && result == LGB_OK; rep++) {
-                cudaEventRecord(e0, st);
-                result = batch_render(b, reduced.data(), n, o, false, st);
-                cudaEventRecord(e1, st);
-                if (result == LGB_OK && cudaEventSynchronize(e1) != cudaSuccess) result = cuda_error(ctx, cudaGetLastError(), "batch tuning");
-                if (result == LGB_OK) cudaEventElapsedTime(&ms, e0, e1);
-            }
+            o.stack_placement = LGB_STACK_LOCAL;
+            trial(o);
             if (result != LGB_OK) break;
-            if (!have || ms < best_ms) { best_ms = ms; best_o = o; have = true; }
         }
         if (result != LGB_OK) break;
+    }
+    if (result == LGB_OK && have) {
+        lgb_batch_opts o = best_o;
+        o.stack_placement = LGB_STACK_SHARED;
+        trial(o);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -19,7 +19,7 @@ struct RayQ {
     float ox, oy, oz, tmin, tmax;
     float Sx, Sy, Sz;
     int kx, ky, kz;
-    float ix, iy, iz;  // inverse direction for box tests (zero components replaced by +-1e-20)
+    float ix, iy, iz;  // inverse direction for box tests (zero components replaced by +-1e-20), approximate
     uint32_t oct;      // bit a set when the guarded direction component a is positive
 };
 
@@ -45,7 +45,11 @@ __device__ __forceinline__ RayQ make_rayq(float ox, float oy, float oz, float tm
     float gx = ax < tiny ? copysignf(tiny, dx) : dx;
     float gy = ay < tiny ? copysignf(tiny, dy) : dy;
     float gz = az < tiny ? copysignf(tiny, dz) : dz;
-    r.ix = 1.0f / gx; r.iy = 1.0f / gy; r.iz = 1.0f / gz;
+    // Box tests only: rcp.approx is within a few ulps, far inside the one quantisation step of outward margin of
+    // every box (the triangle test above keeps IEEE divisions). |g| >= 1e-20, so no result is denormal.
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r.ix) : "f"(gx));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r.iy) : "f"(gy));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r.iz) : "f"(gz));
     // The octant follows the sign of the guarded inverse, so near/far plane selection always agrees with it.
     r.oct = (gx > 0.0f ? 1u : 0u) | (gy > 0.0f ? 2u : 0u) | (gz > 0.0f ? 4u : 0u);
     return r;
@@ -209,8 +213,10 @@ __device__ __forceinline__ void intersect_node(const RayQ& r, const WideNode* __
 //   SK > 0: the bottom SK stack entries of each thread live in shared memory (`sstack`, SK x THREADS entries,
 //   slot-major so that a warp's lanes at different depths hit different banks); deeper entries stay in the
 //   per-thread local array.
+//   REFILL: a warp fetches new rays once at least REFILL of its lanes are idle (a warp whose lanes are all idle
+//   always refills, so every ray is fetched and the loop ends); fewer, fuller refills cost fewer atomics.
 // The ray count is read from *count_ptr when it is non-null, else n.
-template <bool ANY, bool COUNT, bool POSTPONE = true, int SK = 0, int THREADS = 128>
+template <bool ANY, bool COUNT, bool POSTPONE = true, int SK = 0, int THREADS = 128, int REFILL = 1>
 __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ nodes, const WideTri* __restrict__ tris,
                                                  const lgb_ray* __restrict__ rays, lgb_hit* __restrict__ hits,
                                                  uint32_t* __restrict__ occ_bits, uint32_t n, const uint32_t* count_ptr,
@@ -219,6 +225,7 @@ __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ no
                                                  const uint32_t* __restrict__ roots = nullptr,
                                                  uint2* sstack = nullptr) {
     static_assert(SK >= 0 && SK < kStackSize, "shared stack entries");
+    static_assert(REFILL >= 1 && REFILL <= 32, "refill threshold");
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const uint32_t lanemask_lt = (1u << lane) - 1u;
@@ -235,7 +242,7 @@ __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ no
     while (true) {
         if (!exhausted) {
             const uint32_t need = __ballot_sync(FULL, !active);
-            if (need) {
+            if (__popc(need) >= REFILL) {
                 uint32_t base = 0;
                 if (lane == 0) base = atomicAdd(ray_counter, (uint32_t)__popc(need));
                 base = __shfl_sync(FULL, base, 0);

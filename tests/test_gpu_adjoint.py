@@ -296,3 +296,22 @@ def test_autograd_adam_recovers_target(diff_scene):
     assert e1[1] < 0.5 * e0[1]
     assert e1[2] < 0.1 * e0[2]
     assert l1 < 0.25 * l0
+
+
+def test_primal_converged_rmse_against_fp64_reference(diff_scene):
+    """32 spp of the differentiable configuration (512^2) against the committed 512-spp FP64 oracle render: the GPU
+    primal and the FP32 oracle estimator of the same samples have the same error against the converged image."""
+    from lumen_gb300.scene import film_rmse
+    arrays, sc, osc = diff_scene
+    ref = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "diff_512_fp64_ref.npy"))
+    ref = ref.reshape(-1, 3)
+    w = h = 512
+    tex, rough, emis = scene_params(arrays)
+    cam, film = render(sc, arrays, w, h, 0, 32, tex, rough, emis)
+    sc.sync()
+    ref4 = torch.from_numpy(np.concatenate([ref, np.ones((len(ref), 1), np.float32)], 1)).cuda()
+    rmse_gpu = film_rmse(sc.ctx, film, ref4, 0)
+    cpu = osc.diff(cam, DEPTH, w, h, 0, 32, fp64=False)
+    rmse_cpu = float(np.sqrt(((cpu - ref) ** 2).mean()))
+    assert 0.0 < rmse_gpu < 0.5
+    np.testing.assert_allclose(rmse_gpu, rmse_cpu, rtol=0.02)

@@ -94,17 +94,18 @@ def _start_films(scenes):
     return [pre.get(k) for k in range(len(JOBS))]
 
 
-@pytest.mark.parametrize("capacity", [0, 4096, 6000])
-def test_batched_films_equal_films_rendered_alone(ctx, scenes, capacity):
+@pytest.mark.parametrize("capacity,stack", [(0, 0), (4096, 0), (6000, 0), (0, 1), (6000, 1)])
+def test_batched_films_equal_films_rendered_alone(ctx, scenes, capacity, stack):
     start = _start_films(scenes)
     want = _films(JOBS, start)
     _alone(scenes, JOBS, want)
     got = _films(JOBS, start)
     opts = None
-    if capacity:
+    if capacity or stack:
         opts = abi.BatchOpts()
         opts.path_capacity = capacity  # below some images: raised to the largest image
         opts.work_blocks_per_sm = 4
+        opts.stack_placement = stack  # the stack's bottom in shared memory gives the same hits
     _batched(ctx, scenes, JOBS, got, opts)
     for k in range(len(JOBS)):
         a, b = got[k].cpu().numpy(), want[k].cpu().numpy()
@@ -125,6 +126,7 @@ def test_tuner_picks_options_and_leaves_films(ctx, scenes):
     batch.sync()
     assert best.path_capacity in (1 << 20, 1 << 21, 1 << 22)
     assert best.work_blocks_per_sm in (4, 8, 16)
+    assert best.stack_placement in (abi.STACK_LOCAL, abi.STACK_SHARED)
     assert all(bool((f == -1.0).all()) for f in films)
     for f in films:
         f.zero_()
@@ -151,6 +153,10 @@ def test_batch_error_paths(ctx, scenes):
     bad.num_lights = 99
     with pytest.raises(abi.LgbError):
         batch.render([Batch.job(0, cam, bad, 0, 1, film)])
+    bad_opts = abi.BatchOpts()
+    bad_opts.stack_placement = 2
+    with pytest.raises(abi.LgbError):
+        batch.render([Batch.job(0, cam, path_params(arrays, DEPTH), 0, 1, film)], bad_opts)
     misaligned = torch.zeros(32 * 32 * 4 + 4, dtype=torch.float32, device="cuda")[1:]  # 4-byte offset
     with pytest.raises(abi.LgbError):
         batch.render([Batch.job(0, cam, path_params(arrays, DEPTH), 0, 1, misaligned)])

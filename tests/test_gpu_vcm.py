@@ -139,3 +139,18 @@ def test_vcm_error_paths(ctx):
     sc.vcm_iteration(cam, vcm_params(cb, 8, 0.01, 1, 2, 0), film)
     sc.sync()
     sc.close()
+
+
+def test_converged_rmse_against_oracle_reference(ctx, oracle):
+    """64 iterations of the caustics configuration at 256^2 against the committed 1024-iteration oracle render:
+    the GPU image and the oracle's own 64 iterations have the same error against it."""
+    from lumen_gb300.scene import film_rmse
+    ref = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "vcm_torus_256_ref.npy"))
+    ref = ref.reshape(-1, 3)
+    arrays = procedural.vcm_scene()
+    got, want = _run_both(ctx, oracle, arrays, 256, 256, 64, 10, alpha=0.75, spot_angle=20.0)
+    ref4 = torch.from_numpy(np.concatenate([ref, np.ones((len(ref), 1), np.float32)], 1)).cuda()
+    rmse_gpu = film_rmse(ctx, torch.from_numpy(got).cuda(), ref4, 0)
+    rmse_cpu = float(np.sqrt(((want[:, :3].astype(np.float64) - ref) ** 2).mean()))
+    assert 0.0 < rmse_gpu < 1.0
+    np.testing.assert_allclose(rmse_gpu, rmse_cpu, rtol=0.05)

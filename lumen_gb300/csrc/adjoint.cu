@@ -313,12 +313,14 @@ __device__ v3 diff_path(const SceneView& S, const DiffArgs& A, uint32_t pix, uin
                 const uint32_t ltype = Lt->light_flags & 7u;
                 v3 Le = V3(0.0f), wi = V3(0.0f);
                 float wi_len = 0.0f, pdf_w = 0.0f, pdf_a = 0.0f;
-                uint32_t lprim = LGB_NO_HIT, lmat = 0xFFFFFFFFu;
+                uint32_t lprim = LGB_NO_HIT, lmat = 0xFFFFFFFFu, lio = 0u, lvo = 0u;
                 if (ltype == LGB_LIGHT_AREA) {
                     const lgb_mesh pm = S.meshes[Lt->prim_mesh_idx];
                     const uint32_t tri = (uint32_t)(q1 * (float)Lt->num_triangles);
                     lprim = S.mesh_first[Lt->prim_mesh_idx] + tri;
                     const uint32_t io = pm.index_offset + 3u * tri;
+                    lio = io;
+                    lvo = pm.vertex_offset;
                     const DevVertex a = S.verts[S.idx[io] + pm.vertex_offset];
                     const DevVertex b = S.verts[S.idx[io + 1] + pm.vertex_offset];
                     const DevVertex c = S.verts[S.idx[io + 2] + pm.vertex_offset];
@@ -388,8 +390,21 @@ __device__ v3 diff_path(const SceneView& S, const DiffArgs& A, uint32_t pix, uin
                     const v3 fs2 = bs2.f;
                     const float pdf2 = bs2.pdf, cos2 = bs2.cos_t;
                     wi2 = bs2.wi;
-                    if (pdf2 != 0.0f) {
-                        const RayQ mq = make_rayq(sp.x, sp.y, sp.z, kTMinD, wi2.x, wi2.y, wi2.z, kTMaxD);
+                    const RayQ mq = make_rayq(sp.x, sp.y, sp.z, kTMinD, wi2.x, wi2.y, wi2.z, kTMaxD);
+                    bool may_count = pdf2 != 0.0f;
+                    if (may_count && lprim != prim) {
+                        // Only a closest hit on the sampled light triangle counts (a miss reuses the shading
+                        // triangle, which differs here): a ray that fails the traversal's own watertight test
+                        // against that triangle cannot count, so it is not traced.
+                        const DevVertex a = S.verts[S.idx[lio] + lvo];
+                        const DevVertex b = S.verts[S.idx[lio + 1] + lvo];
+                        const DevVertex c = S.verts[S.idx[lio + 2] + lvo];
+                        float tt, tu, tv;
+                        may_count = tri_intersect(mq, make_float4(a.px, a.py, a.pz, 0.0f),
+                                                  make_float4(b.px, b.py, b.pz, 0.0f),
+                                                  make_float4(c.px, c.py, c.pz, 0.0f), mq.tmax, tt, tu, tv);
+                    }
+                    if (may_count) {
                         const DiffHit mhit = diff_closest(S.nodes, S.tris, mq, S.status);
                         const uint32_t mprim = mhit.prim;
                         const float mu = mhit.u, mv = mhit.v;

@@ -547,7 +547,6 @@ lgb_status build_bvh(Scene* s, const lgb_build_opts* opts, lgb_build_stats* stat
     uint32_t* counters = nullptr;
     WideNode* nodes = nullptr;
     WideTri* tris = nullptr;
-    const uint32_t nblocks = (n + RS_TILE - 1) / RS_TILE;
     const uint32_t nint = n > 1 ? n - 1 : 1;
     lgb_status status = LGB_OK;
     auto fail = [&](cudaError_t e, const char* what) { status = cuda_error(ctx, e, what); };
@@ -558,7 +557,7 @@ lgb_status build_bvh(Scene* s, const lgb_build_opts* opts, lgb_build_stats* stat
     } while (0)
     {
         STEP(dalloc(&keys, n)); STEP(dalloc(&keys2, n)); STEP(dalloc(&vals, n)); STEP(dalloc(&vals2, n));
-        STEP(dalloc(&counts, (size_t)256 * nblocks)); STEP(dalloc(&bounds, 6));
+        STEP(dalloc(&counts, radix_sort_scratch_words(n))); STEP(dalloc(&bounds, 6));
         STEP(dalloc(&left, nint)); STEP(dalloc(&right, nint)); STEP(dalloc(&pint, nint)); STEP(dalloc(&pleaf, n));
         STEP(dalloc(&rlo, nint)); STEP(dalloc(&rhi, nint)); STEP(dalloc(&flags, nint));
         STEP(dalloc(&tri_box, 6 * (size_t)n)); STEP(dalloc(&node_box, 6 * (size_t)nint)); STEP(dalloc(&sah, 1));
@@ -572,15 +571,7 @@ lgb_status build_bvh(Scene* s, const lgb_build_opts* opts, lgb_build_stats* stat
         k_centroid_bounds<<<grid, 256, 0, st>>>(s->d_tri_verts, n, bounds);
         k_morton<<<(n + 255) / 256, 256, 0, st>>>(s->d_tri_verts, n, bounds, keys, vals, tri_box);
         STEP(cudaGetLastError());
-        for (int pass = 0; pass < 8; pass++) {
-            int shift = pass * 8;
-            k_rs_hist<<<nblocks, RS_THREADS, 0, st>>>(keys, n, shift, counts, nblocks);
-            k_scan_single<<<1, 1024, 0, st>>>(counts, 256 * nblocks);
-            k_rs_scatter<<<nblocks, RS_THREADS, 0, st>>>(keys, vals, keys2, vals2, n, shift, counts, nblocks);
-            std::swap(keys, keys2);
-            std::swap(vals, vals2);
-        }
-        STEP(cudaGetLastError());
+        STEP(radix_sort_pairs(keys, vals, keys2, vals2, counts, n, 8, st));
         uint32_t root_ref;
         if (n > 1) {
             k_radix_tree<<<(n - 1 + 255) / 256, 256, 0, st>>>(keys, (int)n, left, right, pint, pleaf, rlo, rhi);

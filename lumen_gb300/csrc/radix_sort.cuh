@@ -1,7 +1,8 @@
 // LSD radix sort of (64-bit key, 32-bit value) pairs, 8 bits per pass, stable: per-block digit histograms,
 // one exclusive scan over all (digit, block) counts, and a scatter that ranks equal digits within each warp
 // with __match_any_sync so that equal keys keep their input order. Shared by the BVH builder (Morton codes)
-// and the photon grid (hash slots).
+// and the photon grid (hash slots). The scan runs in three steps over tiles of 4096 counts (tile sums, a scan of
+// the sums, each tile scanned in shared memory from its offset), all with coalesced loads and stores.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -14,6 +15,15 @@ namespace {
 constexpr int RS_THREADS = 256;
 constexpr int RS_ITEMS = 8;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+constexpr int SCAN_THREADS = 512;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+// Words of scratch radix_sort_pairs needs for n pairs: the (digit, block) counts and one sum per scan tile.
+inline size_t radix_sort_scratch_words(uint32_t n) {
+    const size_t m = 256 * (size_t)((n + RS_TILE - 1) / RS_TILE);
+    return m + (m + SCAN_TILE - 1) / SCAN_TILE;
+}
 
 __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint64_t* __restrict__ keys, uint32_t n, int shift,
                                                         uint32_t* counts, uint32_t nblocks) {
@@ -62,6 +72,87 @@ __global__ void __launch_bounds__(1024) k_scan_single(uint32_t* data, uint32_t m
     }
 }
 
+// Sum of each SCAN_TILE-count tile of data[0, m) into sums[tile].
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile_sums(const uint32_t* __restrict__ data, uint32_t m,
+                                                                 uint32_t* __restrict__ sums) {
+    __shared__ uint32_t ws[SCAN_THREADS / 32];
+    const size_t base = (size_t)blockIdx.x * SCAN_TILE;
+    uint32_t s = 0;
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        const size_t i = base + (size_t)k * SCAN_THREADS + threadIdx.x;
+        if (i < m) s += data[i];
+    }
+    s = __reduce_add_sync(0xffffffffu, s);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint32_t v = threadIdx.x < SCAN_THREADS / 32 ? ws[threadIdx.x] : 0u;
+        v = __reduce_add_sync(0xffffffffu, v);
+        if (threadIdx.x == 0) sums[blockIdx.x] = v;
+    }
+}
+
+// Exclusive scan of one tile of data[0, m) in place, starting from sums[tile] (0 when sums is null): the tile is
+// staged in shared memory, each thread scans SCAN_ITEMS consecutive counts, and the thread totals are scanned
+// across the block.
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile_apply(uint32_t* __restrict__ data, uint32_t m,
+                                                                  const uint32_t* __restrict__ sums) {
+    __shared__ uint32_t tile[SCAN_TILE];
+    __shared__ uint32_t ws[SCAN_THREADS / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const size_t base = (size_t)blockIdx.x * SCAN_TILE;
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        const int i = k * SCAN_THREADS + tid;
+        tile[i] = base + i < m ? data[base + i] : 0u;
+    }
+    __syncthreads();
+    uint32_t v[SCAN_ITEMS];
+    uint32_t sum = 0;
+    for (int j = 0; j < SCAN_ITEMS; j++) {
+        v[j] = tile[tid * SCAN_ITEMS + j];
+        sum += v[j];
+    }
+    uint32_t x = sum;  // inclusive scan of the thread totals within the warp
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < SCAN_THREADS / 32 ? ws[lane] : 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < SCAN_THREADS / 32) ws[lane] = w;
+    }
+    __syncthreads();
+    uint32_t excl = x - sum + (warp > 0 ? ws[warp - 1] : 0u) + (sums ? sums[blockIdx.x] : 0u);
+    for (int j = 0; j < SCAN_ITEMS; j++) {
+        tile[tid * SCAN_ITEMS + j] = excl;
+        excl += v[j];
+    }
+    __syncthreads();
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        const int i = k * SCAN_THREADS + tid;
+        if (base + i < m) data[base + i] = tile[i];
+    }
+}
+
+// Exclusive scan of data[0, m) in place; data must have room for the tile sums after the m counts.
+inline void scan_exclusive(uint32_t* data, uint32_t m, cudaStream_t st) {
+    const uint32_t nt = (m + SCAN_TILE - 1) / SCAN_TILE;
+    if (nt <= 1) {
+        k_scan_tile_apply<<<1, SCAN_THREADS, 0, st>>>(data, m, nullptr);
+        return;
+    }
+    uint32_t* sums = data + m;
+    k_scan_tile_sums<<<nt, SCAN_THREADS, 0, st>>>(data, m, sums);
+    k_scan_single<<<1, 1024, 0, st>>>(sums, nt);
+    k_scan_tile_apply<<<nt, SCAN_THREADS, 0, st>>>(data, m, sums);
+}
+
 __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                            uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                                            uint32_t n, int shift, const uint32_t* __restrict__ offsets,
@@ -103,7 +194,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t* __res
     }
 }
 
-// Sorts n pairs by the low 8 * passes bits of the keys; counts must hold 256 * ceil(n / RS_TILE) words. The
+// Sorts n pairs by the low 8 * passes bits of the keys; counts must hold radix_sort_scratch_words(n) words. The
 // result ends in (k0, v0) or (k1, v1): the function swaps the pointers so that k0 / v0 name the sorted arrays.
 inline cudaError_t radix_sort_pairs(uint64_t*& k0, uint32_t*& v0, uint64_t*& k1, uint32_t*& v1, uint32_t* counts,
                                     uint32_t n, int passes, cudaStream_t st) {
@@ -112,7 +203,7 @@ inline cudaError_t radix_sort_pairs(uint64_t*& k0, uint32_t*& v0, uint64_t*& k1,
     for (int pass = 0; pass < passes; pass++) {
         const int shift = pass * 8;
         k_rs_hist<<<nblocks, RS_THREADS, 0, st>>>(k0, n, shift, counts, nblocks);
-        k_scan_single<<<1, 1024, 0, st>>>(counts, 256 * nblocks);
+        scan_exclusive(counts, 256 * nblocks, st);
         k_rs_scatter<<<nblocks, RS_THREADS, 0, st>>>(k0, v0, k1, v1, n, shift, counts, nblocks);
         std::swap(k0, k1);
         std::swap(v0, v1);

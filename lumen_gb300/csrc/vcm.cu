@@ -762,7 +762,7 @@ LGB_API lgb_status lgb_vcm_grid(lgb_ctx* ctx, const float* d_pos4, uint32_t n, c
     lgb_status result = LGB_OK;
     const size_t m = std::max<uint32_t>(n, 1u);
     if (cudaMalloc(&k0, 8 * m) != cudaSuccess || cudaMalloc(&k1, 8 * m) != cudaSuccess || cudaMalloc(&v0, 4 * m) != cudaSuccess ||
-        cudaMalloc(&v1, 4 * m) != cudaSuccess || cudaMalloc(&cnt, sizeof(uint32_t) * 256 * nb) != cudaSuccess) {
+        cudaMalloc(&v1, 4 * m) != cudaSuccess || cudaMalloc(&cnt, sizeof(uint32_t) * radix_sort_scratch_words(n)) != cudaSuccess) {
         result = set_error(ctx, LGB_ERR_OUT_OF_MEMORY, "photon table scratch");
     } else {
         if (n > 0)
@@ -807,7 +807,7 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
     auto take = [&](size_t bytes) { const size_t o = off; off += align256(bytes); return o; };
     const size_t o_verts = take(sizeof(float4) * kVertexF4 * (size_t)nv), o_counts = take(4ull * screen),
                  o_splat = take(12ull * screen), o_gc = take(4ull * table), o_gr = take(4ull * table), o_k0 = take(8ull * nv),
-                 o_k1 = take(8ull * nv), o_v0 = take(4ull * nv), o_v1 = take(4ull * nv), o_sc = take(4ull * 256 * nb);
+                 o_k1 = take(8ull * nv), o_v0 = take(4ull * nv), o_v1 = take(4ull * nv), o_sc = take(4ull * radix_sort_scratch_words(nv));
     if (!s->vcm_buf || s->vcm_w != cam->width || s->vcm_h != cam->height || s->vcm_per != per || s->vcm_buf_bytes < off) {
         cudaFree(s->vcm_buf);
         s->vcm_buf = nullptr;

@@ -210,7 +210,20 @@ __device__ __forceinline__ void load_ref_box(const TreeArgs& T, uint32_t ref, fl
     }
 }
 
-__device__ void optimise_treelet(const TreeArgs& T, uint32_t root) {
+// Shared-memory DP tables of one warp.
+struct TreeletSmem {
+    float cost[1 << kTreeletLeaves];
+    float area[1 << kTreeletLeaves];
+    uint8_t part[1 << kTreeletLeaves];
+};
+
+// Optimises the treelet under `root` with the whole warp (all 32 lanes call it with the same root). Every lane
+// grows the same treelet from the same loads; the subsets' box areas and then their optimal partitions are
+// computed one subset per lane, subset sizes in increasing order; lane 0 rewrites the nodes. Each subset's
+// partitions are tried in the order of a sequential search with the same arithmetic, so the tree is the one a
+// single-thread search would build.
+__device__ void optimise_treelet_warp(const TreeArgs& T, uint32_t root, TreeletSmem& sm) {
+    const int lane = threadIdx.x & 31;
     uint32_t leaves[kTreeletLeaves];
     uint32_t inner[kTreeletLeaves - 1];
     float lbox[kTreeletLeaves][6];
@@ -239,92 +252,127 @@ __device__ void optimise_treelet(const TreeArgs& T, uint32_t root) {
         larea[nl] = box_half_area(lbox[nl]);
         nl++;
     }
-    if (nl < 3) return;
-    float cost[1 << kTreeletLeaves];
-    uint8_t part[1 << kTreeletLeaves];
+    if (nl < 3) return;  // the same on every lane
     const uint32_t full = (1u << nl) - 1u;
-    for (uint32_t sset = 1; sset <= full; sset++) {
+    // singletons and the union areas of the larger subsets
+    for (uint32_t sset = 1u + (uint32_t)lane; sset <= full; sset += 32u) {
         if ((sset & (sset - 1u)) == 0u) {
             const int k = __ffs(sset) - 1;
-            cost[sset] = (leaves[k] & kLeafFlag) ? kCostTri * larea[k] : __ldcg(&T.node_cost[leaves[k]]);
-            part[sset] = 0;
+            sm.cost[sset] = (leaves[k] & kLeafFlag) ? kCostTri * larea[k] : __ldcg(&T.node_cost[leaves[k]]);
+            sm.part[sset] = 0;
             continue;
         }
         float b[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
         for (int k = 0; k < nl; k++)
             if (sset & (1u << k))
                 for (int a = 0; a < 3; a++) { b[a] = fminf(b[a], lbox[k][a]); b[3 + a] = fmaxf(b[3 + a], lbox[k][3 + a]); }
-        const uint32_t low = sset & (0u - sset);
-        float bc = FLT_MAX;
-        uint32_t bp = low;
-        for (uint32_t q = (sset - 1u) & sset; q; q = (q - 1u) & sset) {
-            if (!(q & low)) continue;  // each unordered split once
-            const float c = cost[q] + cost[sset ^ q];
-            if (c < bc) { bc = c; bp = q; }
-        }
-        cost[sset] = kCostNode * box_half_area(b) + bc;
-        part[sset] = (uint8_t)bp;
+        sm.area[sset] = box_half_area(b);
     }
-    if (!(cost[full] < __ldcg(&T.node_cost[root]) * 0.9999f)) return;
-    // rebuild top-down, reusing the treelet's internal nodes
-    uint32_t st_set[kTreeletLeaves], st_node[kTreeletLeaves];
-    int sp = 0, next = 1;
-    st_set[sp] = full;
-    st_node[sp] = root;
-    sp++;
-    while (sp > 0) {
-        sp--;
-        const uint32_t sset = st_set[sp], node = st_node[sp];
-        const uint32_t sub[2] = {part[sset], sset ^ part[sset]};
-        uint32_t ref[2];
-        for (int c = 0; c < 2; c++) {
-            if ((sub[c] & (sub[c] - 1u)) == 0u) {
-                ref[c] = leaves[__ffs(sub[c]) - 1];
-            } else {
-                ref[c] = inner[next++];
-                st_set[sp] = sub[c];
-                st_node[sp] = ref[c];
-                sp++;
+    __syncwarp();
+    for (int size = 2; size <= nl; size++) {
+        for (uint32_t sset = 1u + (uint32_t)lane; sset <= full; sset += 32u) {
+            if (__popc(sset) != size) continue;
+            const uint32_t low = sset & (0u - sset);
+            float bc = FLT_MAX;
+            uint32_t bp = low;
+            for (uint32_t q = (sset - 1u) & sset; q; q = (q - 1u) & sset) {
+                if (!(q & low)) continue;  // each unordered split once
+                const float c = sm.cost[q] + sm.cost[sset ^ q];
+                if (c < bc) { bc = c; bp = q; }
             }
-            if (ref[c] & kLeafFlag) __stcg(&T.parent_leaf[ref[c] & ~kLeafFlag], node);
-            else __stcg(&T.parent_int[ref[c]], node);
+            sm.cost[sset] = kCostNode * sm.area[sset] + bc;
+            sm.part[sset] = (uint8_t)bp;
         }
-        __stcg(&T.left[node], ref[0]);
-        __stcg(&T.right[node], ref[1]);
-        float b[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
-        uint32_t cnt = 0;
-        for (int k = 0; k < nl; k++) {
-            if (!(sset & (1u << k))) continue;
-            for (int a = 0; a < 3; a++) { b[a] = fminf(b[a], lbox[k][a]); b[3 + a] = fmaxf(b[3 + a], lbox[k][3 + a]); }
-            cnt += (leaves[k] & kLeafFlag) ? 1u : __ldcg(&T.node_count[leaves[k]]);
-        }
-        for (int a = 0; a < 6; a++) __stcg(&T.node_box[6 * (size_t)node + a], b[a]);
-        __stcg(&T.node_cost[node], cost[sset]);
-        __stcg(&T.node_count[node], cnt);
+        __syncwarp();
     }
+    const bool better = sm.cost[full] < __ldcg(&T.node_cost[root]) * 0.9999f;
+    if (better && lane == 0) {
+        // rebuild top-down, reusing the treelet's internal nodes
+        uint32_t st_set[kTreeletLeaves], st_node[kTreeletLeaves];
+        int sp = 0, next = 1;
+        st_set[sp] = full;
+        st_node[sp] = root;
+        sp++;
+        while (sp > 0) {
+            sp--;
+            const uint32_t sset = st_set[sp], node = st_node[sp];
+            const uint32_t sub[2] = {sm.part[sset], sset ^ sm.part[sset]};
+            uint32_t ref[2];
+            for (int c = 0; c < 2; c++) {
+                if ((sub[c] & (sub[c] - 1u)) == 0u) {
+                    ref[c] = leaves[__ffs(sub[c]) - 1];
+                } else {
+                    ref[c] = inner[next++];
+                    st_set[sp] = sub[c];
+                    st_node[sp] = ref[c];
+                    sp++;
+                }
+                if (ref[c] & kLeafFlag) __stcg(&T.parent_leaf[ref[c] & ~kLeafFlag], node);
+                else __stcg(&T.parent_int[ref[c]], node);
+            }
+            __stcg(&T.left[node], ref[0]);
+            __stcg(&T.right[node], ref[1]);
+            float b[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+            uint32_t cnt = 0;
+            for (int k = 0; k < nl; k++) {
+                if (!(sset & (1u << k))) continue;
+                for (int a = 0; a < 3; a++) { b[a] = fminf(b[a], lbox[k][a]); b[3 + a] = fmaxf(b[3 + a], lbox[k][3 + a]); }
+                cnt += (leaves[k] & kLeafFlag) ? 1u : __ldcg(&T.node_count[leaves[k]]);
+            }
+            for (int a = 0; a < 6; a++) __stcg(&T.node_box[6 * (size_t)node + a], b[a]);
+            __stcg(&T.node_cost[node], sm.cost[sset]);
+            __stcg(&T.node_count[node], cnt);
+        }
+        __threadfence();  // the rewrite is visible before any lane of the warp signals the parent
+    }
+    __syncwarp();
 }
 
-__global__ void k_treelet(TreeArgs T, int n, uint32_t gamma) {
+constexpr int kTreeletThreads = 128;
+
+// Bottom-up pass, warp-synchronous: in each step every lane still climbing takes the next node on its path
+// (the first of the two children to finish stops there), refreshes that node's cost from its children, and
+// the warp then optimises, one after another, the treelets of the lanes whose node has at least `gamma`
+// triangles. The step count is bounded by the number of triangles (a path from a leaf to the root is shorter).
+__global__ void __launch_bounds__(kTreeletThreads) k_treelet(TreeArgs T, int n, uint32_t gamma) {
+    __shared__ TreeletSmem smem[kTreeletThreads / 32];
+    TreeletSmem& sm = smem[threadIdx.x >> 5];
+    const unsigned FULL = 0xffffffffu;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    uint32_t node = __ldcg(&T.parent_leaf[k]);
-    for (int steps = 0; steps < n; steps++) {
-        __threadfence();
-        if (atomicAdd(&T.flags[node], 1u) == 0u) return;
-        __threadfence();
-        // children are final: refresh this node's cost, then try to improve its treelet
-        const uint32_t cl = __ldcg(&T.left[node]), cr = __ldcg(&T.right[node]);
-        float bl[6], br[6];
-        load_ref_box(T, cl, bl);
-        load_ref_box(T, cr, br);
-        const float ccl = (cl & kLeafFlag) ? kCostTri * box_half_area(bl) : __ldcg(&T.node_cost[cl]);
-        const float ccr = (cr & kLeafFlag) ? kCostTri * box_half_area(br) : __ldcg(&T.node_cost[cr]);
-        float nb[6];
-        for (int a = 0; a < 3; a++) { nb[a] = fminf(bl[a], br[a]); nb[3 + a] = fmaxf(bl[3 + a], br[3 + a]); }
-        __stcg(&T.node_cost[node], kCostNode * box_half_area(nb) + ccl + ccr);
-        if (__ldcg(&T.node_count[node]) >= gamma) optimise_treelet(T, node);
-        if (node == 0) return;
-        node = __ldcg(&T.parent_int[node]);
+    bool climbing = k < n;
+    uint32_t node = climbing ? __ldcg(&T.parent_leaf[k]) : 0u;
+    for (int steps = 0; steps <= n && __any_sync(FULL, climbing); steps++) {
+        bool ready = false;
+        if (climbing) {
+            __threadfence();
+            if (atomicAdd(&T.flags[node], 1u) == 0u) {
+                climbing = false;
+            } else {
+                __threadfence();
+                ready = true;
+                // children are final: refresh this node's cost
+                const uint32_t cl = __ldcg(&T.left[node]), cr = __ldcg(&T.right[node]);
+                float bl[6], br[6];
+                load_ref_box(T, cl, bl);
+                load_ref_box(T, cr, br);
+                const float ccl = (cl & kLeafFlag) ? kCostTri * box_half_area(bl) : __ldcg(&T.node_cost[cl]);
+                const float ccr = (cr & kLeafFlag) ? kCostTri * box_half_area(br) : __ldcg(&T.node_cost[cr]);
+                float nb[6];
+                for (int a = 0; a < 3; a++) { nb[a] = fminf(bl[a], br[a]); nb[3 + a] = fmaxf(bl[3 + a], br[3 + a]); }
+                __stcg(&T.node_cost[node], kCostNode * box_half_area(nb) + ccl + ccr);
+            }
+        }
+        uint32_t todo = __ballot_sync(FULL, ready && __ldcg(&T.node_count[node]) >= gamma);
+        while (todo) {
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1u;
+            optimise_treelet_warp(T, __shfl_sync(FULL, node, src), sm);
+        }
+        if (ready) {
+            __threadfence();
+            if (node == 0) climbing = false;
+            else node = __ldcg(&T.parent_int[node]);
+        }
     }
 }
 
@@ -582,7 +630,7 @@ lgb_status build_bvh(Scene* s, const lgb_build_opts* opts, lgb_build_stats* stat
             TreeArgs T{left, right, pint, pleaf, node_box, node_cost, node_count, tri_box, vals, flags};
             for (int round = 0; round < treelet_rounds; round++) {
                 STEP(cudaMemsetAsync(flags, 0, sizeof(uint32_t) * nint, st));
-                k_treelet<<<(n + 127) / 128, 128, 0, st>>>(T, (int)n, (uint32_t)kTreeletLeaves);
+                k_treelet<<<(n + kTreeletThreads - 1) / kTreeletThreads, kTreeletThreads, 0, st>>>(T, (int)n, (uint32_t)kTreeletLeaves);
                 STEP(cudaGetLastError());
             }
             root_ref = 0;

@@ -198,6 +198,15 @@ LGB_API lgb_status lgb_trace_any(lgb_scene* scene, const lgb_ray* d_rays, uint32
  * d_counters[0] and d_counters[1] (device uint64). For bytes-per-ray accounting. */
 LGB_API lgb_status lgb_trace_closest_counted(lgb_scene* scene, const lgb_ray* d_rays, lgb_hit* d_hits, uint32_t n,
                                              uint64_t* d_counters, void* stream);
+/* The same two queries on HOST buffers (a caller whose rays live in host memory). Pinned buffers (cudaHostAlloc
+ * or cudaHostRegister, 16-byte aligned) are read and written by the traversal kernel itself over the CPU-GPU
+ * link, each ray and hit crossing it once; pageable buffers are copied in and out in up to eight chunks that
+ * overlap the traversal. Stream-ordered: the results are in h_hits / h_occluded_bits once `stream` has
+ * finished. */
+LGB_API lgb_status lgb_trace_closest_host(lgb_scene* scene, const lgb_ray* h_rays, lgb_hit* h_hits, uint32_t n,
+                                          void* stream);
+LGB_API lgb_status lgb_trace_any_host(lgb_scene* scene, const lgb_ray* h_rays, uint32_t* h_occluded_bits, uint32_t n,
+                                      void* stream);
 
 /* ---- camera helper (Camera.h:67-123, Integrator.cpp:60-72): fills out->inv_view/inv_projection ---- */
 LGB_API lgb_status lgb_camera_lookat(const float pos[3], const float dir[3], float fov_deg, uint32_t width,

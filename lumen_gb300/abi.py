@@ -147,6 +147,8 @@ SIGNATURES = {
     "lgb_trace_closest": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p], C.c_int32),
     "lgb_trace_any": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p], C.c_int32),
     "lgb_trace_closest_counted": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p], C.c_int32),
+    "lgb_trace_closest_host": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p], C.c_int32),
+    "lgb_trace_any_host": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p], C.c_int32),
     "lgb_camera_lookat": ([C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float, C.c_uint32, C.c_uint32,
                            C.POINTER(Camera)], C.c_int32),
     "lgb_render_path": ([C.c_void_p, C.POINTER(Camera), C.POINTER(PathParams), C.c_uint32, C.c_uint32, C.c_void_p,

@@ -44,6 +44,10 @@ void free_scene(Scene* s) {
     cudaFree(s->vcm_buf);
     if (s->pt_graph) cudaGraphExecDestroy((cudaGraphExec_t)s->pt_graph);
     if (s->capture_stream) cudaStreamDestroy((cudaStream_t)s->capture_stream);
+    cudaFree(s->stage_buf);
+    if (s->stream_h2d) cudaStreamDestroy((cudaStream_t)s->stream_h2d);
+    if (s->stream_d2h) cudaStreamDestroy((cudaStream_t)s->stream_d2h);
+    for (void* e : s->stage_events) cudaEventDestroy((cudaEvent_t)e);
 }
 
 template <class T> cudaError_t upload(T** dst, const T* src, size_t count) {
@@ -288,6 +292,31 @@ LGB_API lgb_status lgb_trace_any(lgb_scene* s, const lgb_ray* rays, uint32_t* bi
     lgb_status st = check_trace(s, rays, bits, n);
     if (st != LGB_OK || n == 0) return st;
     return launch_trace_any(s, rays, bits, n, (cudaStream_t)stream);
+}
+
+static lgb_status check_trace_host(lgb_scene* s, const void* rays, const void* out, uint32_t n) {
+    if (!s) return LGB_ERR_INVALID_ARGUMENT;
+    if (n == 0) return LGB_OK;
+    if (!rays || !out) return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "null ray or result buffer");
+    if (n >= 0x80000000u) return set_error(s->ctx, LGB_ERR_INVALID_ARGUMENT, "at most 2^31 - 1 rays per call");
+    if (!s->bvh.nodes) return set_error(s->ctx, LGB_ERR_NOT_READY, "lgb_bvh_build has not been called");
+    return LGB_OK;
+}
+
+LGB_API lgb_status lgb_trace_closest_host(lgb_scene* s, const lgb_ray* h_rays, lgb_hit* h_hits, uint32_t n,
+                                          void* stream) {
+    lgb_status st = check_trace_host(s, h_rays, h_hits, n);
+    if (st != LGB_OK || n == 0) return st;
+    cudaSetDevice(s->ctx->device);
+    return trace_host(s, h_rays, h_hits, n, false, (cudaStream_t)stream);
+}
+
+LGB_API lgb_status lgb_trace_any_host(lgb_scene* s, const lgb_ray* h_rays, uint32_t* h_occluded_bits, uint32_t n,
+                                      void* stream) {
+    lgb_status st = check_trace_host(s, h_rays, h_occluded_bits, n);
+    if (st != LGB_OK || n == 0) return st;
+    cudaSetDevice(s->ctx->device);
+    return trace_host(s, h_rays, h_occluded_bits, n, true, (cudaStream_t)stream);
 }
 
 LGB_API lgb_status lgb_sync(lgb_scene* s, void* stream) {

@@ -119,6 +119,12 @@ struct Scene {
     size_t vcm_buf_bytes = 0;
     uint32_t vcm_w = 0, vcm_h = 0, vcm_per = 0;
     uint32_t num_directional = 0;    // directional lights (not supported by VCM)
+    // queries on host buffers: device copies of the rays and results, two copy streams and chunk events
+    void* stage_buf = nullptr;
+    size_t stage_bytes = 0;
+    void* stream_h2d = nullptr;
+    void* stream_d2h = nullptr;
+    std::vector<void*> stage_events;
 };
 
 // Several scenes rendered as one wavefront: their BVHs copied into one forest (node and triangle indices
@@ -158,6 +164,8 @@ lgb_status build_bvh(Scene* s, const lgb_build_opts* opts, lgb_build_stats* stat
 lgb_status launch_trace_closest(Scene* s, const lgb_ray* rays, lgb_hit* hits, uint32_t n, cudaStream_t st,
                                 uint64_t* counters);
 lgb_status launch_trace_any(Scene* s, const lgb_ray* rays, uint32_t* bits, uint32_t n, cudaStream_t st);
+// Queries on host buffers (out = lgb_hit[n] or occlusion bits), copies and traversal pipelined in chunks.
+lgb_status trace_host(Scene* s, const lgb_ray* h_rays, void* h_out, uint32_t n, bool any, cudaStream_t st);
 lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* p, uint32_t frame0, uint32_t spp,
                        float* film, cudaStream_t st);
 

@@ -60,6 +60,111 @@ lgb_status launch_trace_closest(Scene* s, const lgb_ray* rays, lgb_hit* hits, ui
     return LGB_OK;
 }
 
+namespace {
+constexpr uint32_t kHostChunks = 8;           // chunks of one host-buffer query
+constexpr uint32_t kHostChunkMin = 1u << 18;  // rays in a chunk, at least
+}  // namespace
+
+// Device address of a pinned (page-locked, mapped) host buffer, or null for pageable memory.
+static const void* mapped_host(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Pinned host buffers: the persistent kernel loads each ray (32 B, once) from host memory and, for closest hits,
+// stores each hit (16 B) there, over the CPU-GPU link; the link latency is hidden among the rays in flight and
+// nothing else crosses it. Any-hit sets its bits with atomics, so they are gathered in device memory and copied
+// out once (n / 8 bytes). Pageable buffers: the rays are cut into up to kHostChunks chunks (multiples of 32 rays,
+// so any-hit bit words never straddle two chunks); chunk c is copied in on the library's upload stream, traced on
+// the caller's stream once it has arrived, and its results are copied out on the download stream once traced.
+// Either way the caller's stream ends after the results are in host memory, so the call is stream-ordered like
+// the device-buffer queries.
+lgb_status trace_host(Scene* s, const lgb_ray* h_rays, void* h_out, uint32_t n, bool any, cudaStream_t st) {
+    Ctx* ctx = s->ctx;
+    const lgb_ray* m_rays = reinterpret_cast<const lgb_ray*>(mapped_host(h_rays));
+    void* m_out = any ? nullptr : const_cast<void*>(mapped_host(h_out));
+    if (m_rays && (any || m_out) && !(reinterpret_cast<uintptr_t>(m_rays) & 15u) &&
+        !(reinterpret_cast<uintptr_t>(m_out) & 15u)) {
+        if (!any) return launch_trace_closest(s, m_rays, reinterpret_cast<lgb_hit*>(m_out), n, st, nullptr);
+        const size_t words = (n + 31) / 32;
+        if (s->stage_bytes < sizeof(uint32_t) * words) {
+            cudaFree(s->stage_buf);  // waits for any query still using it
+            s->stage_buf = nullptr;
+            s->stage_bytes = 0;
+            LGB_CUDA_TRY(ctx, cudaMalloc(&s->stage_buf, sizeof(uint32_t) * words));
+            s->stage_bytes = sizeof(uint32_t) * words;
+        }
+        uint32_t* bits = reinterpret_cast<uint32_t*>(s->stage_buf);
+        const lgb_status ls = launch_trace_any(s, m_rays, bits, n, st);
+        if (ls != LGB_OK) return ls;
+        LGB_CUDA_TRY(ctx, cudaMemcpyAsync(h_out, bits, sizeof(uint32_t) * words, cudaMemcpyDeviceToHost, st));
+        return LGB_OK;
+    }
+    const size_t ray_bytes = sizeof(lgb_ray) * (size_t)n;
+    const size_t out_bytes = any ? sizeof(uint32_t) * (size_t)((n + 31) / 32) : sizeof(lgb_hit) * (size_t)n;
+    const size_t out_off = (ray_bytes + 255) & ~(size_t)255;
+    if (s->stage_bytes < out_off + out_bytes) {
+        cudaFree(s->stage_buf);  // waits for any query still using it
+        s->stage_buf = nullptr;
+        s->stage_bytes = 0;
+        LGB_CUDA_TRY(ctx, cudaMalloc(&s->stage_buf, out_off + out_bytes));
+        s->stage_bytes = out_off + out_bytes;
+    }
+    if (!s->stream_h2d) LGB_CUDA_TRY(ctx, cudaStreamCreateWithFlags((cudaStream_t*)&s->stream_h2d, cudaStreamNonBlocking));
+    if (!s->stream_d2h) LGB_CUDA_TRY(ctx, cudaStreamCreateWithFlags((cudaStream_t*)&s->stream_d2h, cudaStreamNonBlocking));
+    while (s->stage_events.size() < 2 * kHostChunks + 2) {
+        cudaEvent_t e;
+        LGB_CUDA_TRY(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        s->stage_events.push_back(e);
+    }
+    const cudaStream_t up = (cudaStream_t)s->stream_h2d, down = (cudaStream_t)s->stream_d2h;
+    cudaEvent_t* ev = reinterpret_cast<cudaEvent_t*>(s->stage_events.data());
+    lgb_ray* d_rays = reinterpret_cast<lgb_ray*>(s->stage_buf);
+    char* d_out = reinterpret_cast<char*>(s->stage_buf) + out_off;
+    uint32_t chunk = (n + kHostChunks - 1) / kHostChunks;
+    chunk = std::max(chunk, kHostChunkMin);
+    chunk = (chunk + 31u) & ~31u;
+    // the staging buffer is free once the caller's stream reaches this point (earlier queries joined it)
+    LGB_CUDA_TRY(ctx, cudaEventRecord(ev[0], st));
+    LGB_CUDA_TRY(ctx, cudaStreamWaitEvent(up, ev[0], 0));
+    LGB_CUDA_TRY(ctx, cudaStreamWaitEvent(down, ev[0], 0));
+    uint32_t c = 0;
+    for (uint32_t off = 0; off < n; off += chunk, c++) {
+        const uint32_t cnt = std::min(chunk, n - off);
+        cudaEvent_t arrived = ev[1 + 2 * c], traced = ev[2 + 2 * c];
+        LGB_CUDA_TRY(ctx, cudaMemcpyAsync(d_rays + off, h_rays + off, sizeof(lgb_ray) * (size_t)cnt,
+                                          cudaMemcpyHostToDevice, up));
+        LGB_CUDA_TRY(ctx, cudaEventRecord(arrived, up));
+        LGB_CUDA_TRY(ctx, cudaStreamWaitEvent(st, arrived, 0));
+        size_t o_off, o_len;
+        if (any) {
+            uint32_t* bits = reinterpret_cast<uint32_t*>(d_out);
+            const lgb_status ls = launch_trace_any(s, d_rays + off, bits + off / 32, cnt, st);
+            if (ls != LGB_OK) return ls;
+            o_off = sizeof(uint32_t) * (size_t)(off / 32);
+            o_len = sizeof(uint32_t) * (size_t)((cnt + 31) / 32);
+        } else {
+            lgb_hit* hits = reinterpret_cast<lgb_hit*>(d_out);
+            const lgb_status ls = launch_trace_closest(s, d_rays + off, hits + off, cnt, st, nullptr);
+            if (ls != LGB_OK) return ls;
+            o_off = sizeof(lgb_hit) * (size_t)off;
+            o_len = sizeof(lgb_hit) * (size_t)cnt;
+        }
+        LGB_CUDA_TRY(ctx, cudaEventRecord(traced, st));
+        LGB_CUDA_TRY(ctx, cudaStreamWaitEvent(down, traced, 0));
+        LGB_CUDA_TRY(ctx, cudaMemcpyAsync(reinterpret_cast<char*>(h_out) + o_off, d_out + o_off, o_len,
+                                          cudaMemcpyDeviceToHost, down));
+    }
+    cudaEvent_t done = ev[2 * kHostChunks + 1];
+    LGB_CUDA_TRY(ctx, cudaEventRecord(done, down));
+    LGB_CUDA_TRY(ctx, cudaStreamWaitEvent(st, done, 0));
+    return LGB_OK;
+}
+
 lgb_status launch_trace_any(Scene* s, const lgb_ray* rays, uint32_t* bits, uint32_t n, cudaStream_t st) {
     if (n == 0) return LGB_OK;
     LGB_CUDA_TRY(s->ctx, cudaMemsetAsync(s->d_ray_counter, 0, sizeof(uint32_t), st));

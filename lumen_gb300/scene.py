@@ -252,6 +252,20 @@ class GpuScene:
                                                   C.c_void_p(hits.data_ptr()), rays.shape[0],
                                                   C.c_void_p(counters.data_ptr()), C.c_void_p(stream)))
 
+    def trace_closest_host(self, rays, hits, stream=None):
+        """lgb_trace_closest_host on CPU tensors ((n, 8) float32 rays, (n, 4) int32 hits; pinned for overlap)."""
+        assert rays.device.type == "cpu" and hits.device.type == "cpu"
+        _check(self.lib, self.ctx.handle,
+               self.lib.lgb_trace_closest_host(self.handle, C.c_void_p(rays.data_ptr()), C.c_void_p(hits.data_ptr()),
+                                               rays.shape[0], C.c_void_p(stream)))
+
+    def trace_any_host(self, rays, bits, stream=None):
+        """lgb_trace_any_host on CPU tensors ((n, 8) float32 rays, ((n + 31) // 32,) int32 occlusion bits)."""
+        assert rays.device.type == "cpu" and bits.device.type == "cpu"
+        _check(self.lib, self.ctx.handle,
+               self.lib.lgb_trace_any_host(self.handle, C.c_void_p(rays.data_ptr()), C.c_void_p(bits.data_ptr()),
+                                           rays.shape[0], C.c_void_p(stream)))
+
     def trace_any(self, rays, bits, n=None, stream=None):
         n = rays.shape[0] if n is None else n
         _check(self.lib, self.ctx.handle,

@@ -175,3 +175,49 @@ def test_full_size_traversal_config(ctx, oracle):
     sample = rng.choice(len(rays), 65536, replace=False)
     b = oracle.bvh(arrays.tri_verts())
     assert_hits_equal(got[sample], b.closest(rays[sample]))
+
+
+@pytest.mark.parametrize("n", [1, 31, 33, 70_000, 1_300_001])
+def test_host_buffer_queries_equal_device_queries(ctx, n):
+    """lgb_trace_closest_host / lgb_trace_any_host (chunked copies overlapped with traversal) give exactly the
+    device-buffer results, for one chunk, ragged sizes and several chunks (the last one partial)."""
+    arrays = procedural.traversal_scene(sphere_freq=40, n_random=20000, seed=7)
+    sc = GpuScene(ctx, arrays)
+    sc.build()
+    rays = procedural.incoherent_rays(arrays, n, seed=11)
+    rays[:, 7] = np.where(np.arange(n) % 2 == 0, 0.5, rays[:, 7])  # half short rays: mixed occlusion
+    want = gpu_closest(sc, rays)
+    want_occ = gpu_any(sc, rays)
+    h_rays = torch.from_numpy(rays).pin_memory()
+    h_hits = torch.full((n, 4), -7, dtype=torch.int32).pin_memory()
+    h_bits = torch.full(((n + 31) // 32,), -1, dtype=torch.int32).pin_memory()
+    sc.trace_closest_host(h_rays, h_hits)
+    sc.trace_any_host(h_rays, h_bits)
+    sc.sync()
+    got = h_hits.numpy().view(np.uint32).reshape(-1).view(oracle_lib.HIT_DTYPE)
+    assert np.array_equal(got, want)
+    bits = h_bits.numpy().view(np.uint32)
+    occ = ((bits[np.arange(n) >> 5] >> (np.arange(n) & 31).astype(np.uint32)) & 1).astype(np.uint8)
+    assert np.array_equal(occ, want_occ)
+    assert 0 < occ.sum() < n or n < 100
+    # pageable host memory works too (the copies are then synchronous)
+    h2 = torch.zeros((n, 4), dtype=torch.int32)
+    sc.trace_closest_host(torch.from_numpy(rays), h2)
+    sc.sync()
+    assert np.array_equal(h2.numpy().view(np.uint32).reshape(-1).view(oracle_lib.HIT_DTYPE), want)
+
+
+def test_host_buffer_query_errors(ctx):
+    arrays = procedural.traversal_scene(sphere_freq=8, n_random=100, seed=2)
+    sc = GpuScene(ctx, arrays)
+    rays = torch.zeros((4, 8), dtype=torch.float32)
+    hits = torch.zeros((4, 4), dtype=torch.int32)
+    with pytest.raises(abi.LgbError):
+        sc.trace_closest_host(rays, hits)  # no BVH yet
+    sc.build()
+    import ctypes as C
+    with pytest.raises(abi.LgbError):
+        from lumen_gb300.scene import _check
+        _check(sc.lib, sc.ctx.handle, sc.lib.lgb_trace_closest_host(sc.handle, None, C.c_void_p(hits.data_ptr()), 4, None))
+    sc.trace_closest_host(rays[:0], hits[:0])  # zero rays: nothing to do
+    sc.sync()

@@ -70,6 +70,18 @@ LGB_API lgb_status lgbh_scene_get_info(lgbh_scene* s, lgbh_scene_info* out) {
     return LGB_OK;
 }
 
+LGB_API lgb_status lgbh_write_image(const char* path, const float* rgba, uint32_t width, uint32_t height, char* err,
+                                    size_t errlen) {
+    if (!path || !rgba || width == 0 || height == 0) return LGB_ERR_INVALID_ARGUMENT;
+    try {
+        lgbh::write_image(path, rgba, width, height);
+    } catch (const std::exception& e) {
+        put_err(e.what(), err, errlen);
+        return LGB_ERR_INVALID_ARGUMENT;
+    }
+    return LGB_OK;
+}
+
 LGB_API lgb_status lgbh_render_path(const char* json_path, int device, uint32_t width, uint32_t height, uint32_t spp,
                                     const char* out_pfm, float* host_rgba, char* err, size_t errlen) {
     if (!json_path || width == 0 || height == 0) return LGB_ERR_INVALID_ARGUMENT;
@@ -98,7 +110,7 @@ LGB_API lgb_status lgbh_render_path(const char* json_path, int device, uint32_t 
         std::vector<float> film((size_t)width * height * 4);
         if (cudaMemcpy(film.data(), integrator->output_film, film.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess)
             throw std::runtime_error("film read-back failed");
-        if (out_pfm) lgbh::write_pfm(out_pfm, film.data(), width, height);
+        if (out_pfm) lgbh::write_image(out_pfm, film.data(), width, height);
         if (host_rgba) std::memcpy(host_rgba, film.data(), film.size() * 4);
     } catch (const std::exception& e) {
         put_err(e.what(), err, errlen);

@@ -248,7 +248,13 @@ void LumenScene::load(const std::string& json_path) {
             if (m.spec_trans > 0.0f) m.bsdf_props |= LGB_FLAG_TRANSMISSION;
             m.bsdf_props |= m.roughness > 0.08f ? LGB_FLAG_GLOSSY : LGB_FLAG_SPECULAR;
         } else {
-            throw std::runtime_error("unknown bsdf type '" + type + "'");
+            // LumenScene.cpp:371-475 sets nothing for an unrecognised type ("disney" in
+            // scenes/cornell_box/cornell_box_disney.json): the material keeps type 0 and no lobes, so it reflects
+            // nothing and only its emission counts. The same here, with a warning.
+            std::fprintf(stderr, "lgbh: bsdf type '%s' is not one Lumen's loader knows; the material reflects nothing\n",
+                         type.c_str());
+            m.bsdf_type = 0;
+            m.bsdf_props = 0;
         }
         const Json& refs = b["refs"];
         for (size_t r = 0; r < refs.size(); r++)
@@ -395,6 +401,92 @@ void write_pfm(const std::string& path, const float* rgba, uint32_t width, uint3
             for (int a = 0; a < 3; a++) row[(size_t)x * 3 + a] = rgba[((size_t)src_y * width + x) * 4 + a];
         f.write(reinterpret_cast<const char*>(row.data()), row.size() * 4);
     }
+}
+
+namespace {
+// Little-endian byte writers for the OpenEXR header and scanline blocks.
+void put_u32(std::string& b, uint32_t v) { for (int k = 0; k < 4; k++) b.push_back((char)((v >> (8 * k)) & 0xffu)); }
+void put_u64(std::string& b, uint64_t v) { for (int k = 0; k < 8; k++) b.push_back((char)((v >> (8 * k)) & 0xffu)); }
+void put_f32(std::string& b, float f) {
+    uint32_t v;
+    std::memcpy(&v, &f, 4);
+    put_u32(b, v);
+}
+void put_attr(std::string& b, const char* name, const char* type, const std::string& value) {
+    b.append(name);
+    b.push_back('\0');
+    b.append(type);
+    b.push_back('\0');
+    put_u32(b, (uint32_t)value.size());
+    b.append(value);
+}
+}  // namespace
+
+// OpenEXR 2.0, single-part scanline image, no compression, channels B, G, R as 32-bit floats (channel records
+// in alphabetical order, as the format requires), one scanline per block, the offset table after the header.
+// Rows run top-down, as in the film. Written from the published file layout; stands in for the tinyexr call of
+// ImageUtils.cpp:22-89.
+void write_exr(const std::string& path, const float* rgba, uint32_t width, uint32_t height) {
+    if (width == 0 || height == 0 || width > 0x7fffffffu || height > 0x7fffffffu)
+        throw std::runtime_error("bad image size for " + path);
+    std::string b;
+    put_u32(b, 20000630u);  // magic 0x762f3101
+    put_u32(b, 2u);         // version 2, single-part scanline
+    std::string ch;
+    for (const char* c : {"B", "G", "R"}) {
+        ch.append(c);
+        ch.push_back('\0');
+        put_u32(ch, 2u);            // pixel type FLOAT
+        ch.append(4, '\0');         // pLinear = 0, three reserved bytes
+        put_u32(ch, 1u);            // x sampling
+        put_u32(ch, 1u);            // y sampling
+    }
+    ch.push_back('\0');
+    put_attr(b, "channels", "chlist", ch);
+    put_attr(b, "compression", "compression", std::string(1, '\0'));
+    std::string box;
+    put_u32(box, 0u);
+    put_u32(box, 0u);
+    put_u32(box, width - 1u);
+    put_u32(box, height - 1u);
+    put_attr(b, "dataWindow", "box2i", box);
+    put_attr(b, "displayWindow", "box2i", box);
+    put_attr(b, "lineOrder", "lineOrder", std::string(1, '\0'));  // increasing y
+    std::string one;
+    put_f32(one, 1.0f);
+    put_attr(b, "pixelAspectRatio", "float", one);
+    std::string center;
+    put_f32(center, 0.0f);
+    put_f32(center, 0.0f);
+    put_attr(b, "screenWindowCenter", "v2f", center);
+    put_attr(b, "screenWindowWidth", "float", one);
+    b.push_back('\0');  // end of header
+    const uint64_t row_bytes = 3ull * 4ull * width;
+    const uint64_t block_bytes = 8ull + row_bytes;
+    const uint64_t first = b.size() + 8ull * height;
+    for (uint32_t y = 0; y < height; y++) put_u64(b, first + (uint64_t)y * block_bytes);
+    std::ofstream f(path, std::ios::binary);
+    if (!f) throw std::runtime_error("cannot write " + path);
+    f.write(b.data(), (std::streamsize)b.size());
+    std::string row;
+    row.reserve((size_t)block_bytes);
+    for (uint32_t y = 0; y < height; y++) {
+        row.clear();
+        put_u32(row, y);
+        put_u32(row, (uint32_t)row_bytes);
+        for (int c : {2, 1, 0})  // B, G, R planes of the row
+            for (uint32_t x = 0; x < width; x++) put_f32(row, rgba[((size_t)y * width + x) * 4 + c]);
+        f.write(row.data(), (std::streamsize)row.size());
+    }
+    if (!f) throw std::runtime_error("write failed: " + path);
+}
+
+// ".exr" writes OpenEXR, anything else PFM.
+void write_image(const std::string& path, const float* rgba, uint32_t width, uint32_t height) {
+    const bool exr = path.size() >= 4 && (path.compare(path.size() - 4, 4, ".exr") == 0 ||
+                                          path.compare(path.size() - 4, 4, ".EXR") == 0);
+    if (exr) write_exr(path, rgba, width, height);
+    else write_pfm(path, rgba, width, height);
 }
 
 }  // namespace lgbh

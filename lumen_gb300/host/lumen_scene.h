@@ -61,5 +61,9 @@ class LumenScene {
 TextureData read_pfm(const std::string& path);
 // Writes RGB of an RGBA32F host film as a little-endian colour PFM (rows bottom-up as PFM stores them).
 void write_pfm(const std::string& path, const float* rgba, uint32_t width, uint32_t height);
+// OpenEXR (uncompressed FLOAT B, G, R scanlines), the format Lumen saves its film in (ImageUtils.cpp:22-89).
+void write_exr(const std::string& path, const float* rgba, uint32_t width, uint32_t height);
+// By extension: ".exr" -> write_exr, otherwise write_pfm.
+void write_image(const std::string& path, const float* rgba, uint32_t width, uint32_t height);
 
 }  // namespace lgbh

@@ -38,6 +38,8 @@ def load():
         lib.lgbh_render_path.argtypes = [C.c_char_p, C.c_int, C.c_uint32, C.c_uint32, C.c_uint32, C.c_char_p,
                                          C.c_void_p, C.c_char_p, C.c_size_t]
         lib.lgbh_render_path.restype = C.c_int32
+        lib.lgbh_write_image.argtypes = [C.c_char_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_char_p, C.c_size_t]
+        lib.lgbh_write_image.restype = C.c_int32
         _lib = lib
     return _lib
 
@@ -77,6 +79,17 @@ def load_scene(json_path: str):
         return arrays, info
     finally:
         lib.lgbh_scene_free(h)
+
+
+def write_image(path: str, film: np.ndarray, width: int, height: int):
+    """lgbh_write_image: an (H*W, 4) float32 film as OpenEXR (path ending in .exr) or PFM."""
+    lib = load()
+    film = np.ascontiguousarray(film, np.float32)
+    assert film.size == width * height * 4
+    err = C.create_string_buffer(512)
+    st = lib.lgbh_write_image(path.encode(), film.ctypes.data, width, height, err, 512)
+    if st != abi.LGB_OK:
+        raise abi.LgbError(st, err.value.decode())
 
 
 def render_path(json_path: str, width: int, height: int, spp: int, out_pfm: str | None = None, device: int = 0):

@@ -100,12 +100,71 @@ def test_load_errors(tmp_path):
     from lumen_gb300 import host_scene
     with pytest.raises(abi.LgbError, match="cannot open"):
         host_scene.load_scene(str(tmp_path / "missing.json"))
-    bad = tmp_path / "bad.json"
-    bad.write_text('{"bsdfs": [{"type": "velvet", "refs": []}], "mesh_file": "x.obj"}')
+    unknown = tmp_path / "unknown.json"
+    unknown.write_text('{"bsdfs": [{"type": "velvet", "albedo": [0.5, 0.5, 0.5], "emissive_factor": [1, 2, 3], '
+                       '"refs": ["a"]}], "mesh_file": "x.obj", "camera": {"fov": 40, "position": [0, 0, 5], '
+                       '"dir": [0, 0, -1]}, "lights": []}')
     (tmp_path / "x.obj").write_text("o a\nv 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3\n")
-    with pytest.raises(abi.LgbError, match="unknown bsdf type"):
-        host_scene.load_scene(str(bad))
+    arrays, _ = host_scene.load_scene(str(unknown))  # as Lumen's loader: no lobes, emission kept
+    assert arrays.materials[0]["bsdf_type"] == 0 and arrays.materials[0]["bsdf_props"] == 0
+    np.testing.assert_allclose(arrays.materials[0]["emissive_factor"], [1, 2, 3])
     broken = tmp_path / "broken.json"
     broken.write_text('{"mesh_file": "x.obj", ')
     with pytest.raises(abi.LgbError, match="JSON parse error"):
         host_scene.load_scene(str(broken))
+
+
+def _read_exr(path):
+    """Reader for single-part, uncompressed scanline OpenEXR with FLOAT channels (the subset the host layer
+    writes), from the published file layout: returns {channel: (H, W) float32}."""
+    import struct
+    data = open(path, "rb").read()
+    assert data[:4] == b"\x76\x2f\x31\x01" and struct.unpack_from("<I", data, 4)[0] & 0xff == 2
+    pos, attrs = 8, {}
+    while data[pos] != 0:
+        end = data.index(b"\0", pos)
+        name = data[pos:end].decode()
+        tend = data.index(b"\0", end + 1)
+        size = struct.unpack_from("<I", data, tend + 1)[0]
+        attrs[name] = data[tend + 5:tend + 5 + size]
+        pos = tend + 5 + size
+    pos += 1
+    chans, p = [], 0
+    cl = attrs["channels"]
+    while cl[p] != 0:
+        e = cl.index(b"\0", p)
+        chans.append((cl[p:e].decode(), struct.unpack_from("<i", cl, e + 1)[0]))
+        p = e + 1 + 16
+    assert attrs["compression"] == b"\0" and all(t == 2 for _, t in chans)
+    x0, y0, x1, y1 = struct.unpack("<4i", attrs["dataWindow"])
+    w, h = x1 - x0 + 1, y1 - y0 + 1
+    offsets = struct.unpack_from(f"<{h}Q", data, pos)
+    out = {c: np.zeros((h, w), np.float32) for c, _ in chans}
+    for off in offsets:
+        y, size = struct.unpack_from("<iI", data, off)
+        assert size == 4 * w * len(chans)
+        row = np.frombuffer(data, np.float32, w * len(chans), off + 8).reshape(len(chans), w)
+        for k, (c, _) in enumerate(chans):
+            out[c][y - y0] = row[k]
+    return out
+
+
+def test_film_writers_exr_and_pfm(tmp_path):
+    from lumen_gb300 import host_scene
+    rng = np.random.default_rng(3)
+    w, h = 37, 23
+    film = rng.uniform(0, 5, (w * h, 4)).astype(np.float32)
+    film[5, :3] = [np.inf, 0.0, 1e-30]
+    host_scene.write_image(str(tmp_path / "f.exr"), film, w, h)
+    img = _read_exr(str(tmp_path / "f.exr"))
+    assert sorted(img) == ["B", "G", "R"]
+    for k, c in enumerate("RGB"):
+        np.testing.assert_array_equal(img[c], film[:, k].reshape(h, w))
+    host_scene.write_image(str(tmp_path / "f.pfm"), film, w, h)
+    raw = open(tmp_path / "f.pfm", "rb").read()
+    header_end = [i for i, b in enumerate(raw) if b == 0x0a][2] + 1
+    assert raw[:3] == b"PF\n"
+    pfm = np.frombuffer(raw[header_end:], "<f4").reshape(h, w, 3)[::-1]  # PFM rows run bottom-up
+    np.testing.assert_array_equal(pfm, film[:, :3].reshape(h, w, 3))
+    with pytest.raises(abi.LgbError):
+        host_scene.write_image(str(tmp_path / "no" / "such" / "dir.exr"), film, w, h)

@@ -431,6 +431,39 @@ def vcm_secondary(torch, ctx_cls, scene_cls, local, iters=63):
     return out
 
 
+def sppm_secondary(torch, ctx_cls, scene_cls, local, frames=64):
+    """SPPM on the Cornell box (256^2, max depth 6, base radius 0.03 as the shipped cornell_box_sppm.json):
+    device time per lgb_sppm_iteration over `frames` frames after one warm-up frame (one eye path and one light
+    path per pixel per frame)."""
+    from lumen_gb300 import procedural
+    from lumen_gb300.scene import camera_lookat, sppm_params
+    cb = procedural.cornell_box()
+    ctx = ctx_cls(local)
+    sc = scene_cls(ctx, cb)
+    sc.build()
+    w = h = 256
+    cam = camera_lookat(cb.camera_pos, cb.camera_dir, cb.fov, w, h)
+    film = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    cs = stream.cuda_stream
+    sc.sppm_iteration(cam, sppm_params(cb, 6, 0.03, 77, 0), film, stream=cs)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for f in range(1, frames + 1):
+        sc.sppm_iteration(cam, sppm_params(cb, 6, 0.03, 77, f), film, stream=cs)
+    e1.record(stream)
+    e1.synchronize()
+    sc.sync(cs)
+    ms = e0.elapsed_time(e1) / frames
+    out = {"workload": "SPPM: Cornell box 36 triangles, 256x256, max depth 6, base radius 0.03, one eye and one "
+                       "light path per pixel per frame", "ms_per_frame": ms,
+           "msamples_per_s": w * h / (ms * 1e-3) / 1e6, "frames_timed": frames,
+           "mean_radiance": float(film[:, :3].mean())}
+    sc.close()
+    return out
+
+
 def replica_throughput(step_ms, e2e_ms, units_per_rank, world, device="cuda"):
     """Replicas only: every rank processes its own copy of the workload; the job's step time is the maximum
     over ranks (all_reduce MAX on `device`: NCCL on GPUs, gloo on CPU), and the whole-job throughput is
@@ -575,6 +608,7 @@ def run_gpu(args):
         secondary["adjoint"] = adjoint_secondary(torch, Context, GpuScene, local)
         secondary["batched"] = batch_secondary(torch, Context, GpuScene, local)
         secondary["vcm"] = vcm_secondary(torch, Context, GpuScene, local)
+        secondary["sppm"] = sppm_secondary(torch, Context, GpuScene, local)
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
@@ -603,7 +637,7 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
-LEGS = ("path_tracer", "adjoint", "batched", "vcm")
+LEGS = ("path_tracer", "adjoint", "batched", "vcm", "sppm")
 
 
 def run_leg(name):
@@ -617,6 +651,8 @@ def run_leg(name):
         out = adjoint_secondary(torch, Context, GpuScene, local)
     elif name == "batched":
         out = batch_secondary(torch, Context, GpuScene, local)
+    elif name == "sppm":
+        out = sppm_secondary(torch, Context, GpuScene, local)
     else:
         out = vcm_secondary(torch, Context, GpuScene, local)
     print(json.dumps({"leg": name, **out}))

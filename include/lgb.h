@@ -320,6 +320,29 @@ LGB_API lgb_status lgb_vcm_grid(lgb_ctx* ctx, const float* d_pos4, uint32_t n, c
  * inverse matrices and rounded to float: what lgb_vcm_iteration projects light vertices with. */
 LGB_API lgb_status lgb_camera_forward(const lgb_camera* camera, float view[16], float projection[16]);
 
+/* ---- SPPM: stochastic progressive photon mapping (src/RayTracer/SPPM.cpp:78-184,
+ *      src/shaders/integrators/sppm/{sppm_eye.rgen, sppm_light.rgen, gather.comp, composite.comp, min/max/
+ *      calc_bounds.comp}) on the same traversal and the same sort-and-scan photon table as VCM. ---- */
+typedef struct lgb_sppm_params {
+    float sky_col[3];
+    int32_t max_depth;             /* path_length */
+    int32_t num_lights;
+    int32_t light_triangle_count;  /* LumenScene::total_light_triangle_cnt */
+    uint32_t dir_light_idx;        /* must be 0xFFFFFFFF */
+    float base_radius;             /* SPPMConfig::base_radius (default 0.03): every pixel's radius at frame 0 */
+    uint32_t seed;                 /* the RNG's frame value is frame_num ^ seed (the reference draws seed with rand()) */
+    uint32_t frame_num;            /* 0 restarts (per-pixel state cleared); k mixes the film with weight 1/(k+1) */
+    float spot_angle;              /* spot cone half-angle as lgb_vcm_params; 0 = Lumen's fixed 30 / 25 degrees */
+    uint32_t reserved[5];
+} lgb_sppm_params;
+
+/* One SPPM frame into d_film (RGBA32F, width*height): eye pass (visible points at the first diffuse hit, direct
+ * light by the path tracer's light sampling), grid bounds from the visible points, light pass (photons from the
+ * second bounce on), photon table, gather and progressive radius / flux update, film. The per-pixel state and the
+ * photons live in the scene between frames. Area and spot lights only. */
+LGB_API lgb_status lgb_sppm_iteration(lgb_scene* scene, const lgb_camera* camera, const lgb_sppm_params* params,
+                                      float* d_film, void* stream);
+
 /* ---- batched rendering (no counterpart in Lumen) ----
  * Many scenes and camera views of uneven size rendered by one wavefront: the paths of every job share the
  * queues, the traversal and shading launches and one captured bounce loop, instead of each image issuing its

@@ -135,6 +135,13 @@ class VcmParams(C.Structure):
                 ("reserved", C.c_uint32)]
 
 
+class SppmParams(C.Structure):
+    _fields_ = [("sky_col", C.c_float * 3), ("max_depth", C.c_int32), ("num_lights", C.c_int32),
+                ("light_triangle_count", C.c_int32), ("dir_light_idx", C.c_uint32), ("base_radius", C.c_float),
+                ("seed", C.c_uint32), ("frame_num", C.c_uint32), ("spot_angle", C.c_float),
+                ("reserved", C.c_uint32 * 5)]
+
+
 # Every exported symbol with its argument and result types (the declarations of include/lgb.h).
 SIGNATURES = {
     "lgb_abi_version": ([], C.c_uint32),
@@ -162,6 +169,7 @@ SIGNATURES = {
     "lgb_sync": ([C.c_void_p, C.c_void_p], C.c_int32),
     "lgb_vcm_radius": ([C.c_float, C.c_float, C.c_uint32, C.c_float], C.c_float),
     "lgb_vcm_iteration": ([C.c_void_p, C.POINTER(Camera), C.POINTER(VcmParams), C.c_void_p, C.c_void_p], C.c_int32),
+    "lgb_sppm_iteration": ([C.c_void_p, C.POINTER(Camera), C.POINTER(SppmParams), C.c_void_p, C.c_void_p], C.c_int32),
     "lgb_vcm_grid": ([C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float,
                       C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int32),
     "lgb_camera_forward": ([C.POINTER(Camera), C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int32),

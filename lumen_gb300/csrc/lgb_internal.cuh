@@ -118,6 +118,9 @@ struct Scene {
     void* vcm_buf = nullptr;         // VCM state kept between iterations (light vertices, counts, splats, table)
     size_t vcm_buf_bytes = 0;
     uint32_t vcm_w = 0, vcm_h = 0, vcm_per = 0;
+    void* sppm_buf = nullptr;        // SPPM state kept between frames (visible points, photons, table, bounds)
+    size_t sppm_buf_bytes = 0;
+    uint32_t sppm_w = 0, sppm_h = 0, sppm_depth = 0;
     uint32_t num_directional = 0;    // directional lights (not supported by VCM)
     // queries on host buffers: device copies of the rays and results, two copy streams and chunk events
     void* stage_buf = nullptr;

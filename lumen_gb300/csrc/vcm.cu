@@ -23,7 +23,9 @@
 #include <cstring>
 
 #include "bsdf_vcm.cuh"
+#include "light_sample.cuh"
 #include "path_common.cuh"
+#include "photon_table.cuh"
 #include "radix_sort.cuh"
 
 namespace lgb {
@@ -53,6 +55,10 @@ struct VcmArgs {
     float4* film;            // RGBA32F, row-major
 };
 
+__device__ __forceinline__ LightSet lights_of(const VcmArgs& A) {
+    return LightSet{A.num_lights, A.light_tri_count, A.spot_cos_width, A.spot_cos_falloff};
+}
+
 struct CamV {
     v3 pos, nrm;
     float area;
@@ -78,15 +84,6 @@ __device__ __forceinline__ Etas etas(const VcmArgs& A) {
     return e;
 }
 
-__device__ __forceinline__ int3 grid_idx(v3 p, const float* mn, const float* mx, const int* res) {
-    const float nx = (p.x - mn[0]) / (mx[0] - mn[0]), ny = (p.y - mn[1]) / (mx[1] - mn[1]), nz = (p.z - mn[2]) / (mx[2] - mn[2]);
-    return make_int3(__float2int_rz(nx * (float)res[0]), __float2int_rz(ny * (float)res[1]), __float2int_rz(nz * (float)res[2]));
-}
-// utils.glsl:62-65 with the products wrapping as 32-bit integers
-__device__ __forceinline__ uint32_t grid_hash(int3 p, uint32_t screen) {
-    const uint32_t h = ((uint32_t)p.x * 73856093u) ^ ((uint32_t)p.y * 19349663u) ^ ((uint32_t)p.z * 83492791u);
-    return h % (10u * screen);
-}
 
 // Light vertex: (pos, area) (wi, d_vcm) (wo, d_vc) (n_s, d_vm) (throughput, u) (v, material, path_len, side)
 struct LVert {
@@ -118,131 +115,6 @@ __device__ __forceinline__ bool is_zero3(v3 a) { return a.x == 0.0f && a.y == 0.
 __device__ __forceinline__ bool light_finite(uint32_t f) { return ((f >> 4) & 1u) != 0u; }
 __device__ __forceinline__ bool light_delta(uint32_t f) { return ((f >> 5) & 1u) != 0u; }
 
-// commons.glsl:112-149 with an identity world matrix
-__device__ __forceinline__ void sample_tri(const SceneView& S, const lgb_mesh& pm, uint32_t tri, float rx, float ry, v3& pos,
-                                           v3& n, float& tri_pdf) {
-    const uint32_t io = pm.index_offset + 3u * tri;
-    const DevVertex a = S.verts[S.idx[io] + pm.vertex_offset];
-    const DevVertex b = S.verts[S.idx[io + 1] + pm.vertex_offset];
-    const DevVertex c = S.verts[S.idx[io + 2] + pm.vertex_offset];
-    const float su = 1.0f - sqrtf(rx), sv = ry * sqrtf(rx);
-    const float b0 = 1.0f - su - sv;
-    const v3 v0 = V3(a.px, a.py, a.pz), v1 = V3(b.px, b.py, b.pz), v2 = V3(c.px, c.py, c.pz);
-    pos = v0 * b0 + v1 * su + v2 * sv;
-    n = normalize(normalize(V3(a.nx, a.ny, a.nz) * b0 + V3(b.nx, b.ny, b.nz) * su + V3(c.nx, c.ny, c.nz) * sv));
-    tri_pdf = 2.0f / length(cross(v1 - v0, v2 - v0));
-}
-
-struct Emission {
-    v3 L, pos, wi;
-    float cos_from_light, pdf_pos_a, pdf_dir_w;
-    uint32_t flags;
-};
-
-// sample_light_Le (commons.glsl:335-406), area and spot lights
-__device__ Emission sample_light_Le(const SceneView& S, const VcmArgs& A, float r0, float r1, float r2, float r3, float d0, float d1) {
-    Emission e;
-    const uint32_t li = (uint32_t)(r0 * (float)A.num_lights);
-    const lgb_light* L = &S.lights[li];
-    e.L = V3(0.0f); e.pos = V3(0.0f); e.wi = V3(0.0f);
-    e.cos_from_light = 0.0f; e.pdf_pos_a = 0.0f; e.pdf_dir_w = 0.0f;
-    e.flags = L->light_flags;
-    const uint32_t type = L->light_flags & 7u;
-    if (type == LGB_LIGHT_AREA) {
-        const lgb_mesh pm = S.meshes[L->prim_mesh_idx];
-        const uint32_t tri = (uint32_t)(r1 * (float)L->num_triangles);
-        v3 n;
-        float tri_pdf;
-        sample_tri(S, pm, tri, r2, r3, e.pos, n, tri_pdf);
-        const lgb_material* lm = &S.mats[pm.material_index];
-        v3 T, B;
-        branchless_onb(n, T, B);
-        e.wi = to_world(sample_hemisphere(V2(d0, d1)), T, B, n);
-        e.L = V3(lm->emissive_factor[0], lm->emissive_factor[1], lm->emissive_factor[2]);
-        e.cos_from_light = fmaxf(dot(n, e.wi), 0.0f);
-        e.pdf_pos_a = tri_pdf;
-        e.pdf_dir_w = dot(e.wi, n) / LGB_PI;
-    } else if (type == LGB_LIGHT_SPOT) {
-        const float cos_width = A.spot_cos_width, cos_faloff = A.spot_cos_falloff;
-        const v3 lp = V3(L->pos[0], L->pos[1], L->pos[2]);
-        const v3 ldir = normalize(V3(L->to[0], L->to[1], L->to[2]) - lp);
-        // to_local_quat (utils.glsl:157-160), then invert_quat and rot_quat (utils.glsl:167-172)
-        float qx = 1.0f, qy = 0.0f, qz = 0.0f, qw = 0.0f;
-        if (!(ldir.z < -0.99999f)) {
-            qx = ldir.y; qy = -ldir.x; qz = 0.0f; qw = 1.0f + ldir.z;
-            const float len = sqrtf(qx * qx + qy * qy + qz * qz + qw * qw);
-            qx = qx / len; qy = qy / len; qz = qz / len; qw = qw / len;
-        }
-        const v3 a = V3(-qx, -qy, -qz);
-        const float ct = (1.0f - d0) + d0 * cos_width;
-        const float st = sqrtf(1.0f - ct * ct);
-        const float phi = d1 * LGB_TWO_PI;
-        const v3 cone = V3(cosf(phi) * st, sinf(phi) * st, ct);
-        e.wi = 2.0f * dot(a, cone) * a + (qw * qw - dot(a, a)) * cone + 2.0f * qw * cross(a, cone);
-        e.pos = lp;
-        e.cos_from_light = dot(e.wi, ldir);
-        float fall;
-        if (e.cos_from_light < cos_width) fall = 0.0f;
-        else if (e.cos_from_light >= cos_faloff) fall = 1.0f;
-        else { const float d = (e.cos_from_light - cos_width) / (cos_faloff - cos_width); fall = (d * d) * (d * d); }
-        e.L = V3(L->L[0], L->L[1], L->L[2]) * fall;
-        e.pdf_pos_a = 1.0f;
-        e.pdf_dir_w = 1.0f / (LGB_TWO_PI * (1.0f - cos_width));
-    }
-    e.pdf_pos_a = e.pdf_pos_a / (float)A.light_tri_count;
-    return e;
-}
-
-struct Incidence {
-    v3 L, wi;
-    float wi_len, pdf_pos_w, pdf_pos_dir_w, cos_y;
-    uint32_t flags;
-};
-
-// sample_light_Li with the positional-directional pdf (commons.glsl:224-300), area and spot lights
-__device__ Incidence sample_light_Li_vcm(const SceneView& S, const VcmArgs& A, float r0, float r1, float r2, float r3, v3 p) {
-    Incidence r;
-    const uint32_t li = (uint32_t)(r0 * (float)A.num_lights);
-    const lgb_light* L = &S.lights[li];
-    r.L = V3(0.0f); r.wi = V3(0.0f); r.wi_len = 0.0f; r.pdf_pos_w = 0.0f; r.pdf_pos_dir_w = 0.0f; r.cos_y = 0.0f;
-    r.flags = L->light_flags;
-    const uint32_t type = L->light_flags & 7u;
-    if (type == LGB_LIGHT_AREA) {
-        const lgb_mesh pm = S.meshes[L->prim_mesh_idx];
-        const uint32_t tri = (uint32_t)(r1 * (float)L->num_triangles);
-        v3 pos, n;
-        float tri_pdf;
-        sample_tri(S, pm, tri, r2, r3, pos, n, tri_pdf);
-        const lgb_material* lm = &S.mats[pm.material_index];
-        v3 wi = pos - p;
-        const float l2 = dot(wi, wi);
-        r.wi_len = sqrtf(l2);
-        wi = wi / r.wi_len;
-        r.wi = wi;
-        r.cos_y = fabsf(dot(n, -wi));
-        r.L = V3(lm->emissive_factor[0], lm->emissive_factor[1], lm->emissive_factor[2]);
-        r.pdf_pos_w = tri_pdf * l2 / r.cos_y;
-        r.pdf_pos_dir_w = r.cos_y * LGB_INV_PI * tri_pdf;
-    } else if (type == LGB_LIGHT_SPOT) {
-        const v3 lp = V3(L->pos[0], L->pos[1], L->pos[2]);
-        v3 wi = lp - p;
-        const float l2 = dot(wi, wi);
-        r.wi_len = sqrtf(l2);
-        wi = wi / r.wi_len;
-        r.wi = wi;
-        const v3 ldir = normalize(V3(L->to[0], L->to[1], L->to[2]) - lp);
-        r.cos_y = dot(-wi, ldir);
-        const float cos_width = A.spot_cos_width, cos_faloff = A.spot_cos_falloff;
-        float fall;
-        if (r.cos_y < cos_width) fall = 0.0f;
-        else if (r.cos_y >= cos_faloff) fall = 1.0f;
-        else { const float d = (r.cos_y - cos_width) / (cos_faloff - cos_width); fall = (d * d) * (d * d); }
-        r.pdf_pos_w = l2;
-        r.pdf_pos_dir_w = 1.0f / (LGB_TWO_PI * (1.0f - cos_width));
-        r.L = V3(L->L[0], L->L[1], L->L[2]) * fall;
-    }
-    return r;
-}
 
 struct VState {
     v3 pos, wi, thr;
@@ -299,7 +171,7 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_light(SceneView S, VcmArgs 
         uint4 seed = make_uint4(x, y, A.light_seed, 0u);
         const float r0 = rnd(seed), r1 = rnd(seed), r2 = rnd(seed), r3 = rnd(seed);
         const float d0 = rnd(seed), d1 = rnd(seed);
-        const Emission e = sample_light_Le(S, A, r0, r1, r2, r3, d0, d1);
+        const Emission e = sample_light_Le(S, lights_of(A), r0, r1, r2, r3, d0, d1);
         if (e.pdf_dir_w <= 0.0f) {
             A.counts[li] = 0u;
             continue;
@@ -391,7 +263,7 @@ __device__ v3 connect_light(const SceneView& S, const VcmArgs& A, uint4& seed, c
                             bool side, float eta_vm, const VState& cs, float& pdf_rev) {
     v3 res = V3(0.0f);
     const float q0 = rnd(seed), q1 = rnd(seed), q2 = rnd(seed), q3 = rnd(seed);
-    const Incidence li = sample_light_Li_vcm(S, A, q0, q1, q2, q3, h.pos);
+    const Incidence li = sample_light_Li_pos(S, lights_of(A), q0, q1, q2, q3, h.pos);
     const float cos_x = dot(li.wi, n_s);
     const v3 origin = offset_ray2(h.pos, n_s);
     float pdf_fwd;
@@ -625,75 +497,7 @@ __global__ void k_vcm_keys_pos(const float4* __restrict__ pos, uint32_t n, float
     }
 }
 
-// Run starts: rep[slot] = first sorted position (temporarily).
-__global__ void k_vcm_run_first(const uint64_t* __restrict__ keys, uint32_t n, uint32_t table, uint32_t* rep) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint64_t k = keys[i];
-        if (k >= table) continue;
-        if (i == 0 || keys[i - 1] != k) rep[k] = i;
-    }
-}
-// Run ends: count = length of the run, rep = its last vertex id.
-__global__ void k_vcm_run_last(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t n,
-                               uint32_t table, uint32_t* count, uint32_t* rep) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint64_t k = keys[i];
-        if (k >= table) continue;
-        if (i == n - 1 || keys[i + 1] != k) {
-            count[k] = i - rep[k] + 1u;
-            rep[k] = vals[i];
-        }
-    }
-}
 
-int to_int_rz_host(float x) {
-    if (x != x) return 0;
-    if (x >= 2147483648.0f) return INT32_MAX;
-    if (x <= -2147483648.0f) return INT32_MIN;
-    return (int)x;
-}
-
-// Spot cone of sample_light_Le / sample_light_Li (commons.glsl:264-265 fixes the half-angle at 30 degrees and
-// the falloff start at 25): half-angle `angle` degrees with the falloff from 25/30 of it, 0 for the fixed cone.
-// Evaluated in double on the host so the oracle gets the same two floats.
-void spot_cone(float angle, float& cos_width, float& cos_falloff) {
-    const double a = angle > 0.0f ? (double)angle : 30.0;
-    const double deg = 3.14159265358979323846 / 180.0;
-    cos_width = (float)std::cos(a * deg);
-    cos_falloff = (float)std::cos(a * (25.0 / 30.0) * deg);
-}
-
-// VCM.cpp:144-147
-void grid_resolution(const float* mn, const float* mx, float radius, int* res) {
-    const float d[3] = {mx[0] - mn[0], mx[1] - mn[1], mx[2] - mn[2]};
-    const float max_comp = std::max(d[0], std::max(d[1], d[2]));
-    const int base = to_int_rz_host(max_comp / radius);
-    for (int k = 0; k < 3; k++) res[k] = std::max(to_int_rz_host(d[k] * (float)base / max_comp), 1);
-}
-
-int sort_passes(uint32_t table) {
-    int bits = 0;
-    while (bits < 32 && (uint64_t)table >= (1ull << bits)) bits++;
-    return (bits + 7) / 8;
-}
-
-int vcm_grid_blocks(Ctx* ctx, uint64_t n) {
-    const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
-    return (int)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, (uint64_t)sms * 16));
-}
-
-// Sorts (keys, vals) in place (k0/v0 end up holding the result) and writes the table (count and rep zeroed first).
-lgb_status build_table(Ctx* ctx, uint64_t*& k0, uint32_t*& v0, uint64_t*& k1, uint32_t*& v1, uint32_t* sort_counts, uint32_t n,
-                       uint32_t table, uint32_t* count, uint32_t* rep, cudaStream_t st) {
-    LGB_CUDA_TRY(ctx, cudaMemsetAsync(count, 0, sizeof(uint32_t) * table, st));
-    LGB_CUDA_TRY(ctx, cudaMemsetAsync(rep, 0, sizeof(uint32_t) * table, st));
-    LGB_CUDA_TRY(ctx, radix_sort_pairs(k0, v0, k1, v1, sort_counts, n, sort_passes(table), st));
-    const int g = vcm_grid_blocks(ctx, n);
-    k_vcm_run_first<<<g, 256, 0, st>>>(k0, n, table, rep);
-    k_vcm_run_last<<<g, 256, 0, st>>>(k0, v0, n, table, count, rep);
-    LGB_CUDA_TRY(ctx, cudaGetLastError());
-    return LGB_OK;
-}
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -766,7 +570,7 @@ LGB_API lgb_status lgb_vcm_grid(lgb_ctx* ctx, const float* d_pos4, uint32_t n, c
         result = set_error(ctx, LGB_ERR_OUT_OF_MEMORY, "photon table scratch");
     } else {
         if (n > 0)
-            k_vcm_keys_pos<<<vcm_grid_blocks(ctx, n), 256, 0, st>>>(reinterpret_cast<const float4*>(d_pos4), n, scene_min[0],
+            k_vcm_keys_pos<<<table_grid_blocks(ctx, n), 256, 0, st>>>(reinterpret_cast<const float4*>(d_pos4), n, scene_min[0],
                                                                  scene_min[1], scene_min[2], scene_max[0], scene_max[1],
                                                                  scene_max[2], res[0], res[1], res[2], screen_size, k0, v0);
         result = build_table(ctx, k0, v0, k1, v1, cnt, n, table, d_count, d_rep, st);
@@ -849,7 +653,7 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
         uint64_t* k1 = reinterpret_cast<uint64_t*>(base + o_k1);
         uint32_t* v0 = reinterpret_cast<uint32_t*>(base + o_v0);
         uint32_t* v1 = reinterpret_cast<uint32_t*>(base + o_v1);
-        k_vcm_keys<<<vcm_grid_blocks(ctx, nv), 256, 0, st>>>(A, table, k0, v0);
+        k_vcm_keys<<<table_grid_blocks(ctx, nv), 256, 0, st>>>(A, table, k0, v0);
         LGB_CUDA_TRY(ctx, cudaGetLastError());
         const lgb_status ts = build_table(ctx, k0, v0, k1, v1, reinterpret_cast<uint32_t*>(base + o_sc), nv, table, gc, gr, st);
         if (ts != LGB_OK) return ts;

@@ -286,6 +286,12 @@ class GpuScene:
                self.lib.lgb_vcm_iteration(self.handle, C.byref(cam), C.byref(params), C.c_void_p(film.data_ptr()),
                                           C.c_void_p(stream)))
 
+    def sppm_iteration(self, cam: abi.Camera, params: abi.SppmParams, film, stream=None):
+        """lgb_sppm_iteration: one SPPM frame into film ((npix, 4) float32 CUDA)."""
+        _check(self.lib, self.ctx.handle,
+               self.lib.lgb_sppm_iteration(self.handle, C.byref(cam), C.byref(params), C.c_void_p(film.data_ptr()),
+                                           C.c_void_p(stream)))
+
     @staticmethod
     def _diff_params(texture_id, texels, roughness, emission, flags=0) -> abi.DiffParams:
         dp = abi.DiffParams()
@@ -413,6 +419,22 @@ def vcm_params(arrays: SceneArrays, max_depth: int, radius: float, light_seed: i
     p.eye_seed = eye_seed
     p.frame_num = frame_num
     p.flags = flags
+    p.spot_angle = spot_angle
+    return p
+
+
+def sppm_params(arrays: SceneArrays, max_depth: int, base_radius: float, seed: int, frame_num: int,
+                sky=(0.0, 0.0, 0.0), spot_angle: float = 0.0) -> abi.SppmParams:
+    """PCSPPM as SPPM::render fills it (src/RayTracer/SPPM.cpp:78-96) with an explicit seed."""
+    p = abi.SppmParams()
+    p.sky_col[:] = list(sky)
+    p.max_depth = max_depth
+    p.num_lights = len(arrays.lights)
+    p.light_triangle_count = arrays.light_triangle_count
+    p.dir_light_idx = 0xFFFFFFFF
+    p.base_radius = base_radius
+    p.seed = seed
+    p.frame_num = frame_num
     p.spot_angle = spot_angle
     return p
 

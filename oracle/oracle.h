@@ -157,6 +157,22 @@ void orc_vcm_iteration(void* scene, const float inv_view[16], const float inv_pr
                        const float proj[16], uint32_t width, uint32_t height, const orc_vcm_params* p,
                        orc_vcm_vertex* verts, uint32_t* counts, float* splat, uint32_t* grid_count, uint32_t* grid_rep,
                        float* film, int nthreads);
+// SPPM (SPPM.cpp:78-184): one frame. vp (W*H*32 floats), photons (W*H*max_depth*16 floats), grid_count and
+// grid_rep (10*W*H) and film (W*H*4, row-major) persist across frames; vp must be zero before frame 0. The
+// visible-point and photon layouts are the library's (8 and 4 float4, integer fields stored as their bits).
+struct orc_sppm_params {
+    float sky_col[3];
+    int32_t max_depth;
+    int32_t num_lights;
+    int32_t light_triangle_count;
+    float base_radius;
+    uint32_t seed;       // RNG frame value = frame_num ^ seed
+    uint32_t frame_num;
+    float spot_angle;    // degrees, 0 = the fixed 30 / 25 degree cone
+};
+void orc_sppm_iteration(void* scene, const float inv_view[16], const float inv_proj[16], uint32_t width,
+                        uint32_t height, const orc_sppm_params* p, float* vp, float* photons, uint32_t* grid_count,
+                        uint32_t* grid_rep, float* film, int nthreads);
 // PCG4D (utils.glsl:121-133) applied to n state vectors; for known-answer tests.
 void orc_pcg4d(const uint32_t* in, uint32_t* out, uint32_t n);
 // offset_ray (utils.glsl:73-84) applied to n (p, n) pairs.

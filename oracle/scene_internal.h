@@ -137,8 +137,10 @@ template <class T> struct LightSample {
     uint32_t flags, triangle_idx, instance_idx;
 };
 
-// commons.glsl:224-300
-template <class T> LightSample<T> sample_light_Li(const Scene& s, V4<T> rands, V3<T> p, int num_lights) {
+// commons.glsl:224-300. A spot cone given by its two cosines replaces the fixed 30 / 25 degrees of
+// commons.glsl:264-265 when cone_cos_width >= -1.
+template <class T> LightSample<T> sample_light_Li(const Scene& s, V4<T> rands, V3<T> p, int num_lights,
+                                                 T cone_cos_width = T(-2), T cone_cos_falloff = T(-2)) {
     LightSample<T> r;
     uint32_t light_idx = (uint32_t)(rands.x * T(num_lights));
     const orc_light& light = s.lights[light_idx];
@@ -172,8 +174,8 @@ template <class T> LightSample<T> sample_light_Li(const Scene& s, V4<T> rands, V
         V3<T> to(light.to[0], light.to[1], light.to[2]);
         const V3<T> light_dir = normalize(to - lp);
         r.cos_from_light = dot(-wi, light_dir);
-        const T cos_width = std::cos(K<T>::PI() / T(6));
-        const T cos_faloff = std::cos(T(25) * K<T>::PI() / T(180));
+        const T cos_width = cone_cos_width >= T(-1) ? cone_cos_width : std::cos(K<T>::PI() / T(6));
+        const T cos_faloff = cone_cos_width >= T(-1) ? cone_cos_falloff : std::cos(T(25) * K<T>::PI() / T(180));
         T faloff;
         if (r.cos_from_light < cos_width) faloff = T(0);
         else if (r.cos_from_light >= cos_faloff) faloff = T(1);

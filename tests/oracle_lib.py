@@ -51,6 +51,12 @@ class VcmParams(C.Structure):
                 ("flags", C.c_uint32), ("spot_angle", C.c_float)]
 
 
+class SppmParams(C.Structure):
+    _fields_ = [("sky_col", C.c_float * 3), ("max_depth", C.c_int32), ("num_lights", C.c_int32),
+                ("light_triangle_count", C.c_int32), ("base_radius", C.c_float), ("seed", C.c_uint32),
+                ("frame_num", C.c_uint32), ("spot_angle", C.c_float)]
+
+
 VCM_VERTEX_BYTES = 104
 
 
@@ -98,6 +104,10 @@ class Oracle:
         L.orc_vcm_iteration.argtypes = [C.c_void_p] + [C.POINTER(C.c_float)] * 4 + [
             C.c_uint32, C.c_uint32, C.POINTER(VcmParams), C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_float),
             C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_float), C.c_int]
+        L.orc_sppm_iteration.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32,
+                                         C.c_uint32, C.POINTER(SppmParams), C.POINTER(C.c_float),
+                                         C.POINTER(C.c_float), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                         C.POINTER(C.c_float), C.c_int]
         L.orc_pcg4d.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint32]
         L.orc_offset_ray.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32]
 
@@ -294,6 +304,25 @@ class OracleScene:
                                        _p(state["grid_rep"], C.c_uint32), _p(state["film"]),
                                        threads or (os.cpu_count() or 1))
         return state["film"]
+
+
+def sppm_state(width, height, max_depth):
+    """Buffers that persist across SPPM frames, zero-initialised (the reference clears them at frame 0)."""
+    screen = width * height
+    return {"vp": np.zeros(screen * 32, np.float32), "photons": np.zeros(screen * max_depth * 16, np.float32),
+            "grid_count": np.zeros(10 * screen, np.uint32), "grid_rep": np.zeros(10 * screen, np.uint32),
+            "film": np.zeros((screen, 4), np.float32), "width": width, "height": height}
+
+
+def sppm_iteration(scene: "OracleScene", cam, params: SppmParams, state, threads=0):
+    """One SPPM frame of the oracle into state['film']."""
+    f32 = lambda a: np.ascontiguousarray(np.array(a, np.float32).reshape(16))
+    iv, ip = f32(cam.inv_view[:]), f32(cam.inv_projection[:])
+    scene.ora.lib.orc_sppm_iteration(scene.h, _p(iv), _p(ip), state["width"], state["height"], C.byref(params),
+                                     _p(state["vp"]), _p(state["photons"]), _p(state["grid_count"], C.c_uint32),
+                                     _p(state["grid_rep"], C.c_uint32), _p(state["film"]),
+                                     threads or (os.cpu_count() or 1))
+    return state["film"]
 
 
 def vcm_grid(ora: Oracle, pos4, scene_min, scene_max, radius, screen_size):

@@ -318,3 +318,28 @@ def test_vcm_oracle_spot_cone(oracle):
     assert np.array_equal(films[0.0], films[30.0])
     lit = {a: int((f[:, :3].sum(1) > 1e-4).sum()) for a, f in films.items()}
     assert 0 < lit[10.0] < lit[20.0] < lit[0.0], lit
+
+
+def test_sppm_oracle_is_deterministic_and_plausible(oracle):
+    """The oracle's SPPM: the same seed gives the same film; radii shrink as photons are gathered; the image is
+    within 25 % of the path tracer's mean (the two estimators share the eye pass's direct lighting but differ in
+    the reference's quirks: the path tracer's stale BSDF-MIS payload brightens the white emitter's surround)."""
+    import oracle_lib
+    from lumen_gb300.scene import camera_lookat
+    cb = procedural.cornell_box()
+    sc = oracle.scene(cb)
+    cam = camera_lookat(cb.camera_pos, cb.camera_dir, cb.fov, 32, 32)
+    films = []
+    for _ in range(2):
+        st = oracle_lib.sppm_state(32, 32, 6)
+        for f in range(8):
+            p = oracle_lib.SppmParams()
+            p.max_depth, p.num_lights, p.light_triangle_count = 6, len(cb.lights), cb.light_triangle_count
+            p.base_radius, p.seed, p.frame_num = 0.03, 5, f
+            oracle_lib.sppm_iteration(sc, cam, p, st)
+        films.append(st["film"].copy())
+    assert np.array_equal(films[0], films[1]) and not np.isnan(films[0]).any()
+    vp = st["vp"].reshape(-1, 32)
+    assert vp[:, 3].min() < 0.03 and vp[:, 3].max() <= 0.03
+    pt = sc.film(cam, 6, 32, 32, 0, 32)
+    assert abs(films[0][:, :3].mean() - pt[:, :3].mean()) < 0.25 * pt[:, :3].mean()

@@ -105,4 +105,32 @@ bool GpuVCM::update() {  // VCM::update (VCM.cpp:267-274)
     return changed;
 }
 
+void GpuSPPM::init() {
+    Integrator::init();
+    frame_num = 0;
+    path_length = (uint32_t)lumen_scene->config.path_length;
+    base_radius = lumen_scene->config.base_radius;
+}
+
+void GpuSPPM::render() {  // SPPM::render (SPPM.cpp:78-184)
+    lgb_sppm_params p{};
+    for (int i = 0; i < 3; i++) p.sky_col[i] = lumen_scene->config.sky_col[i];
+    p.max_depth = (int32_t)path_length;
+    p.num_lights = (int32_t)lumen_scene->lights.size();
+    p.light_triangle_count = (int32_t)lumen_scene->total_light_triangle_cnt;
+    p.dir_light_idx = lumen_scene->dir_light_idx;
+    p.base_radius = base_radius;
+    uint32_t unused;
+    vcm_seeds(seed, frame_num, &p.seed, &unused);
+    p.frame_num = frame_num;
+    check(lgb_sppm_iteration(scene, &cam, &p, output_film, stream), "lgb_sppm_iteration");
+}
+
+bool GpuSPPM::update() {  // SPPM::update (SPPM.cpp:186-192)
+    frame_num++;
+    const bool changed = Integrator::update();
+    if (changed) frame_num = 0;
+    return changed;
+}
+
 }  // namespace lgbh

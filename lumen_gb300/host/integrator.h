@@ -66,6 +66,21 @@ class GpuVCM final : public Integrator {
     void* stream = nullptr;
 };
 
+// The SPPM integrator (SPPM.cpp:78-192): one frame per render(); the per-pixel state restarts at frame 0, which
+// update() returns to when the camera changed. Lumen draws each frame's RNG offset with host rand(); here it is
+// the light seed of vcm_seeds(seed, frame_num).
+class GpuSPPM final : public Integrator {
+  public:
+    using Integrator::Integrator;
+    void init() override;
+    void render() override;
+    bool update() override;
+    uint32_t path_length = 6;
+    float base_radius = 0.03f;
+    uint32_t seed = 0;
+    void* stream = nullptr;
+};
+
 // Light and eye seeds of VCM iteration `frame` (PCG-style integer hash of (seed, frame, stream)).
 void vcm_seeds(uint32_t seed, uint32_t frame, uint32_t* light_seed, uint32_t* eye_seed);
 

@@ -162,6 +162,7 @@ void LumenScene::load(const std::string& json_path) {
     if (config.integrator == "vcm") {  // LumenScene.cpp:248-253
         if (!integ["enable_vm"].is_null()) config.enable_vm = integ["enable_vm"].as_number() == 1;
         if (!integ["radius_factor"].is_null()) config.radius_factor = (float)integ["radius_factor"].as_number();
+        if (!integ["base_radius"].is_null()) config.base_radius = (float)integ["base_radius"].as_number();
     }
     if (!integ["sky_col"].is_null()) vec3_of(integ["sky_col"], config.sky_col, config.sky_col);
     // geometry

@@ -26,6 +26,7 @@ struct SceneConfig {  // SceneConfig.h:15-63 (the fields the Path and VCM integr
     int path_length = 6;
     bool enable_vm = false;        // VCMConfig
     float radius_factor = 0.025f;  // VCMConfig
+    float base_radius = 0.03f;     // SPPMConfig (SceneConfig.h:34)
     float sky_col[3] = {0, 0, 0};
     CameraSettings cam;
 };

@@ -343,6 +343,35 @@ typedef struct lgb_sppm_params {
 LGB_API lgb_status lgb_sppm_iteration(lgb_scene* scene, const lgb_camera* camera, const lgb_sppm_params* params,
                                       float* d_film, void* stream);
 
+/* ---- ReSTIR DI (src/RayTracer/ReSTIR.cpp:74-157, src/shaders/integrators/restir/di/*): resampled direct
+ *      lighting with temporal and spatial reuse, on the library's traversal and light sampling. ---- */
+typedef struct lgb_restir_params {
+    float sky_col[3];              /* PCReSTIR fields of the temporal pass's path-traced colour, which the output */
+    int32_t max_depth;             /* pass never reads (output.rgen:12): kept for the layout, not used */
+    int32_t num_lights;
+    int32_t light_triangle_count;  /* LumenScene::total_light_triangle_cnt */
+    uint32_t dir_light_idx;        /* must be 0xFFFFFFFF */
+    uint32_t seed;                 /* the RNG's frame value is frame_num ^ seed (the reference draws seed with rand()) */
+    uint32_t frame_num;
+    uint32_t do_spatiotemporal;    /* 0 on the first frame (the temporal reservoirs are cleared), then 1 */
+    uint32_t enable_accumulation;  /* 1: progressive mean over frames, 0: each frame alone */
+    float spot_angle;              /* spot cone half-angle as lgb_vcm_params; 0 = Lumen's fixed 30 / 25 degrees */
+    uint32_t flags;                /* LGB_RESTIR_* */
+    uint32_t reserved[3];
+} lgb_restir_params;
+/* The spatial pass of the reference counts the pixel's own reservoir as one sample (spatial_pass.rgen:16-17, the
+ * count is read after one combine), so W is too large by (m + neighbours) / (1 + neighbours), and the temporal
+ * reuse feeds that back: the image brightens frame after frame. With this flag the count starts at the
+ * reservoir's own m, and the estimate stays put. */
+#define LGB_RESTIR_SPATIAL_COUNT_FIX 1u
+
+/* One ReSTIR DI frame into d_film (RGBA32F, width*height): temporal pass (G-buffer, up to 32 light candidates,
+ * visibility, merge with the previous frame's reservoir), spatial pass (5 neighbours), output. prev_camera is the
+ * previous frame's camera for the temporal reprojection test (null: the same camera). The G-buffer and the
+ * reservoirs live in the scene between frames. Area and spot lights only. */
+LGB_API lgb_status lgb_restir_di_iteration(lgb_scene* scene, const lgb_camera* camera, const lgb_camera* prev_camera,
+                                           const lgb_restir_params* params, float* d_film, void* stream);
+
 /* ---- batched rendering (no counterpart in Lumen) ----
  * Many scenes and camera views of uneven size rendered by one wavefront: the paths of every job share the
  * queues, the traversal and shading launches and one captured bounce loop, instead of each image issuing its

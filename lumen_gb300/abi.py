@@ -124,6 +124,7 @@ class BatchOpts(C.Structure):
 
 STACK_LOCAL, STACK_SHARED = 0, 1  # lgb_batch_opts.stack_placement
 VCM_ACCUMULATE = 1
+RESTIR_SPATIAL_COUNT_FIX = 1
 
 
 class VcmParams(C.Structure):
@@ -140,6 +141,13 @@ class SppmParams(C.Structure):
                 ("light_triangle_count", C.c_int32), ("dir_light_idx", C.c_uint32), ("base_radius", C.c_float),
                 ("seed", C.c_uint32), ("frame_num", C.c_uint32), ("spot_angle", C.c_float),
                 ("reserved", C.c_uint32 * 5)]
+
+
+class RestirParams(C.Structure):
+    _fields_ = [("sky_col", C.c_float * 3), ("max_depth", C.c_int32), ("num_lights", C.c_int32),
+                ("light_triangle_count", C.c_int32), ("dir_light_idx", C.c_uint32), ("seed", C.c_uint32),
+                ("frame_num", C.c_uint32), ("do_spatiotemporal", C.c_uint32), ("enable_accumulation", C.c_uint32),
+                ("spot_angle", C.c_float), ("flags", C.c_uint32), ("reserved", C.c_uint32 * 3)]
 
 
 # Every exported symbol with its argument and result types (the declarations of include/lgb.h).
@@ -170,6 +178,8 @@ SIGNATURES = {
     "lgb_vcm_radius": ([C.c_float, C.c_float, C.c_uint32, C.c_float], C.c_float),
     "lgb_vcm_iteration": ([C.c_void_p, C.POINTER(Camera), C.POINTER(VcmParams), C.c_void_p, C.c_void_p], C.c_int32),
     "lgb_sppm_iteration": ([C.c_void_p, C.POINTER(Camera), C.POINTER(SppmParams), C.c_void_p, C.c_void_p], C.c_int32),
+    "lgb_restir_di_iteration": ([C.c_void_p, C.POINTER(Camera), C.POINTER(Camera), C.POINTER(RestirParams),
+                                 C.c_void_p, C.c_void_p], C.c_int32),
     "lgb_vcm_grid": ([C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float,
                       C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int32),
     "lgb_camera_forward": ([C.POINTER(Camera), C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int32),

@@ -121,6 +121,9 @@ struct Scene {
     void* sppm_buf = nullptr;        // SPPM state kept between frames (visible points, photons, table, bounds)
     size_t sppm_buf_bytes = 0;
     uint32_t sppm_w = 0, sppm_h = 0, sppm_depth = 0;
+    void* restir_buf = nullptr;      // ReSTIR DI state kept between frames (G-buffer, reservoirs)
+    size_t restir_buf_bytes = 0;
+    uint32_t restir_w = 0, restir_h = 0;
     uint32_t num_directional = 0;    // directional lights (not supported by VCM)
     // queries on host buffers: device copies of the rays and results, two copy streams and chunk events
     void* stage_buf = nullptr;

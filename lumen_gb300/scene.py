@@ -286,6 +286,14 @@ class GpuScene:
                self.lib.lgb_vcm_iteration(self.handle, C.byref(cam), C.byref(params), C.c_void_p(film.data_ptr()),
                                           C.c_void_p(stream)))
 
+    def restir_di_iteration(self, cam: abi.Camera, params: abi.RestirParams, film, prev_cam: abi.Camera = None,
+                            stream=None):
+        """lgb_restir_di_iteration: one ReSTIR DI frame into film ((npix, 4) float32 CUDA)."""
+        _check(self.lib, self.ctx.handle,
+               self.lib.lgb_restir_di_iteration(self.handle, C.byref(cam),
+                                                C.byref(prev_cam) if prev_cam is not None else None,
+                                                C.byref(params), C.c_void_p(film.data_ptr()), C.c_void_p(stream)))
+
     def sppm_iteration(self, cam: abi.Camera, params: abi.SppmParams, film, stream=None):
         """lgb_sppm_iteration: one SPPM frame into film ((npix, 4) float32 CUDA)."""
         _check(self.lib, self.ctx.handle,
@@ -436,6 +444,23 @@ def sppm_params(arrays: SceneArrays, max_depth: int, base_radius: float, seed: i
     p.seed = seed
     p.frame_num = frame_num
     p.spot_angle = spot_angle
+    return p
+
+
+def restir_params(arrays: SceneArrays, seed: int, frame_num: int, do_spatiotemporal: int = 1,
+                  enable_accumulation: int = 1, spot_angle: float = 0.0, flags: int = 0) -> abi.RestirParams:
+    """PCReSTIR as ReSTIR::render fills it (src/RayTracer/ReSTIR.cpp:74-86) with an explicit seed."""
+    p = abi.RestirParams()
+    p.max_depth = 6
+    p.num_lights = len(arrays.lights)
+    p.light_triangle_count = arrays.light_triangle_count
+    p.dir_light_idx = 0xFFFFFFFF
+    p.seed = seed
+    p.frame_num = frame_num
+    p.do_spatiotemporal = do_spatiotemporal
+    p.enable_accumulation = enable_accumulation
+    p.spot_angle = spot_angle
+    p.flags = flags
     return p
 
 

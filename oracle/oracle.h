@@ -173,6 +173,23 @@ struct orc_sppm_params {
 void orc_sppm_iteration(void* scene, const float inv_view[16], const float inv_proj[16], uint32_t width,
                         uint32_t height, const orc_sppm_params* p, float* vp, float* photons, uint32_t* grid_count,
                         uint32_t* grid_rep, float* film, int nthreads);
+// ReSTIR DI (ReSTIR.cpp:74-151): one frame. gbuf, passthrough, temporal_res and spatial_res (W*H*12 floats each)
+// and film (W*H*4, row-major) persist across frames; prev_view / prev_proj are the previous camera's forward
+// matrices (column-major). Layouts are the library's.
+struct orc_restir_params {
+    int32_t num_lights;
+    int32_t light_triangle_count;
+    uint32_t seed;                 // RNG frame value = frame_num ^ seed
+    uint32_t frame_num;
+    uint32_t do_spatiotemporal;
+    uint32_t enable_accumulation;
+    float spot_angle;
+    uint32_t flags;  // bit 0: the spatial pass counts the pixel's reservoir with its m (LGB_RESTIR_SPATIAL_COUNT_FIX)
+};
+void orc_restir_di_iteration(void* scene, const float inv_view[16], const float inv_proj[16], const float prev_view[16],
+                             const float prev_proj[16], uint32_t width, uint32_t height, const orc_restir_params* p,
+                             float* gbuf, float* passthrough, float* temporal_res, float* spatial_res, float* film,
+                             int nthreads);
 // PCG4D (utils.glsl:121-133) applied to n state vectors; for known-answer tests.
 void orc_pcg4d(const uint32_t* in, uint32_t* out, uint32_t n);
 // offset_ray (utils.glsl:73-84) applied to n (p, n) pairs.

@@ -57,6 +57,12 @@ class SppmParams(C.Structure):
                 ("frame_num", C.c_uint32), ("spot_angle", C.c_float)]
 
 
+class RestirParams(C.Structure):
+    _fields_ = [("num_lights", C.c_int32), ("light_triangle_count", C.c_int32), ("seed", C.c_uint32),
+                ("frame_num", C.c_uint32), ("do_spatiotemporal", C.c_uint32), ("enable_accumulation", C.c_uint32),
+                ("spot_angle", C.c_float), ("flags", C.c_uint32)]
+
+
 VCM_VERTEX_BYTES = 104
 
 
@@ -108,6 +114,8 @@ class Oracle:
                                          C.c_uint32, C.POINTER(SppmParams), C.POINTER(C.c_float),
                                          C.POINTER(C.c_float), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                          C.POINTER(C.c_float), C.c_int]
+        L.orc_restir_di_iteration.argtypes = [C.c_void_p] + [C.POINTER(C.c_float)] * 4 + [
+            C.c_uint32, C.c_uint32, C.POINTER(RestirParams)] + [C.POINTER(C.c_float)] * 5 + [C.c_int]
         L.orc_pcg4d.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint32]
         L.orc_offset_ray.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32]
 
@@ -322,6 +330,25 @@ def sppm_iteration(scene: "OracleScene", cam, params: SppmParams, state, threads
                                      _p(state["vp"]), _p(state["photons"]), _p(state["grid_count"], C.c_uint32),
                                      _p(state["grid_rep"], C.c_uint32), _p(state["film"]),
                                      threads or (os.cpu_count() or 1))
+    return state["film"]
+
+
+def restir_state(width, height):
+    """G-buffer, reservoirs and film that persist across ReSTIR frames, zero-initialised."""
+    screen = width * height
+    return {"gbuf": np.zeros(screen * 12, np.float32), "pass": np.zeros(screen * 12, np.float32),
+            "temporal": np.zeros(screen * 12, np.float32), "spatial": np.zeros(screen * 12, np.float32),
+            "film": np.zeros((screen, 4), np.float32), "width": width, "height": height}
+
+
+def restir_iteration(scene: "OracleScene", cam, prev_view, prev_proj, params: RestirParams, state, threads=0):
+    """One ReSTIR DI frame of the oracle into state['film']."""
+    f32 = lambda a: np.ascontiguousarray(np.array(a, np.float32).reshape(16))
+    iv, ip, pv, pp = f32(cam.inv_view[:]), f32(cam.inv_projection[:]), f32(prev_view), f32(prev_proj)
+    scene.ora.lib.orc_restir_di_iteration(scene.h, _p(iv), _p(ip), _p(pv), _p(pp), state["width"], state["height"],
+                                          C.byref(params), _p(state["gbuf"]), _p(state["pass"]),
+                                          _p(state["temporal"]), _p(state["spatial"]), _p(state["film"]),
+                                          threads or (os.cpu_count() or 1))
     return state["film"]
 
 

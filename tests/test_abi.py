@@ -48,6 +48,7 @@ def test_struct_layouts():
     assert C.sizeof(abi.BatchJob) == 208
     assert C.sizeof(abi.BatchOpts) == 32
     assert C.sizeof(abi.SppmParams) == 64
+    assert C.sizeof(abi.RestirParams) == 64
 
 
 def test_camera_lookat_matches_oracle(lib, oracle):
@@ -87,7 +88,8 @@ def test_ctypes_layouts_match_the_header(tmp_path):
                "lgb_mesh": abi.Mesh, "lgb_camera": abi.Camera, "lgb_path_params": abi.PathParams,
                "lgb_build_opts": abi.BuildOpts, "lgb_build_stats": abi.BuildStats, "lgb_diff_params": abi.DiffParams,
                "lgb_diff_grads": abi.DiffGrads, "lgb_batch_job": abi.BatchJob, "lgb_batch_opts": abi.BatchOpts,
-               "lgb_vcm_params": abi.VcmParams, "lgb_sppm_params": abi.SppmParams}
+               "lgb_vcm_params": abi.VcmParams, "lgb_sppm_params": abi.SppmParams,
+               "lgb_restir_params": abi.RestirParams}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "lgb.h"', "int main(void) {"]
     for cname, py in mirrors.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')

@@ -343,3 +343,43 @@ def test_sppm_oracle_is_deterministic_and_plausible(oracle):
     assert vp[:, 3].min() < 0.03 and vp[:, 3].max() <= 0.03
     pt = sc.film(cam, 6, 32, 32, 0, 32)
     assert abs(films[0][:, :3].mean() - pt[:, :3].mean()) < 0.25 * pt[:, :3].mean()
+
+
+def _restir_frames(oracle, arrays, w, h, frames, seed=11, flags=0, accumulate=1):
+    import oracle_lib
+    from lumen_gb300.scene import camera_forward, camera_lookat
+    sc = oracle.scene(arrays)
+    cam = camera_lookat(arrays.camera_pos, arrays.camera_dir, arrays.fov, w, h)
+    view, proj = camera_forward(cam)
+    st = oracle_lib.restir_state(w, h)
+    means = []
+    for f in range(frames):
+        p = oracle_lib.RestirParams()
+        p.num_lights, p.light_triangle_count = len(arrays.lights), arrays.light_triangle_count
+        p.seed, p.frame_num, p.do_spatiotemporal, p.enable_accumulation = seed, f, 1 if f > 0 else 0, accumulate
+        p.flags = flags
+        oracle_lib.restir_iteration(sc, cam, view, proj, p, st)
+        means.append(st["film"][:, :3].copy())
+    return sc, cam, st, means
+
+
+def test_restir_oracle_is_deterministic_and_matches_direct_light(oracle):
+    """The oracle's ReSTIR DI on the Cornell box. The same seed gives the same film. Frame 0 (no reuse over time)
+    is close to the path tracer's direct light (depth-2 minus depth-1 images) on the pixels that do not see the
+    emitter (there the path tracer's stale BSDF-MIS payload adds light ReSTIR does not have). With Lumen's spatial
+    sample count the per-frame image brightens frame after frame; with LGB_RESTIR_SPATIAL_COUNT_FIX it holds a
+    steady level, somewhat below the direct light (reused samples are not tested for visibility where they are
+    reused, and a pixel whose own sample was occluded does not reuse: ReSTIR's usual darkening)."""
+    cb = procedural.cornell_box()
+    sc, cam, st, quirk = _restir_frames(oracle, cb, 32, 32, 10, accumulate=0)
+    _, _, st2, _ = _restir_frames(oracle, cb, 32, 32, 10, accumulate=0)
+    assert np.array_equal(st["film"], st2["film"]) and not np.isnan(st["film"]).any()
+    emitter = sc.film(cam, 1, 32, 32, 0, 64)[:, :3].sum(1) > 0
+    direct = (sc.film(cam, 2, 32, 32, 0, 256)[:, :3] - sc.film(cam, 1, 32, 32, 0, 256)[:, :3])[~emitter].mean()
+    f0 = quirk[0][~emitter].mean()
+    assert abs(f0 - direct) < 0.15 * direct, (f0, direct)
+    assert quirk[-1][~emitter].mean() > 2.0 * f0  # the reference's estimate grows with the frames
+    _, _, _, fixed = _restir_frames(oracle, cb, 32, 32, 10, flags=1, accumulate=0)
+    levels = [m[~emitter].mean() for m in fixed[1:]]
+    assert max(levels) < 1.2 * min(levels), levels
+    assert 0.6 * direct < min(levels) and max(levels) < 1.1 * direct, (levels, direct)

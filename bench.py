@@ -464,6 +464,40 @@ def sppm_secondary(torch, ctx_cls, scene_cls, local, frames=64):
     return out
 
 
+def restir_secondary(torch, ctx_cls, scene_cls, local, frames=64):
+    """ReSTIR DI on the Cornell box (256^2: 2 light candidates per pixel, temporal and 5-neighbour spatial reuse,
+    with the spatial sample count fixed): device time per lgb_restir_di_iteration over `frames` frames after one
+    warm-up frame."""
+    from lumen_gb300 import abi, procedural
+    from lumen_gb300.scene import camera_lookat, restir_params
+    cb = procedural.cornell_box()
+    ctx = ctx_cls(local)
+    sc = scene_cls(ctx, cb)
+    sc.build()
+    w = h = 256
+    cam = camera_lookat(cb.camera_pos, cb.camera_dir, cb.fov, w, h)
+    film = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    cs = stream.cuda_stream
+    fix = abi.RESTIR_SPATIAL_COUNT_FIX
+    sc.restir_di_iteration(cam, restir_params(cb, 91, 0, 0, flags=fix), film, stream=cs)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for f in range(1, frames + 1):
+        sc.restir_di_iteration(cam, restir_params(cb, 91, f, 1, flags=fix), film, stream=cs)
+    e1.record(stream)
+    e1.synchronize()
+    sc.sync(cs)
+    ms = e0.elapsed_time(e1) / frames
+    out = {"workload": "ReSTIR DI: Cornell box 36 triangles, 256x256, light candidates min(light triangles, 32) = 2, "
+                       "temporal + 5-neighbour spatial reuse, spatial sample count fixed", "ms_per_frame": ms,
+           "msamples_per_s": w * h / (ms * 1e-3) / 1e6, "frames_timed": frames,
+           "mean_radiance": float(film[:, :3].mean())}
+    sc.close()
+    return out
+
+
 def replica_throughput(step_ms, e2e_ms, units_per_rank, world, device="cuda"):
     """Replicas only: every rank processes its own copy of the workload; the job's step time is the maximum
     over ranks (all_reduce MAX on `device`: NCCL on GPUs, gloo on CPU), and the whole-job throughput is
@@ -609,6 +643,7 @@ def run_gpu(args):
         secondary["batched"] = batch_secondary(torch, Context, GpuScene, local)
         secondary["vcm"] = vcm_secondary(torch, Context, GpuScene, local)
         secondary["sppm"] = sppm_secondary(torch, Context, GpuScene, local)
+        secondary["restir_di"] = restir_secondary(torch, Context, GpuScene, local)
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
@@ -637,7 +672,7 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
-LEGS = ("path_tracer", "adjoint", "batched", "vcm", "sppm")
+LEGS = ("path_tracer", "adjoint", "batched", "vcm", "sppm", "restir_di")
 
 
 def run_leg(name):
@@ -653,6 +688,8 @@ def run_leg(name):
         out = batch_secondary(torch, Context, GpuScene, local)
     elif name == "sppm":
         out = sppm_secondary(torch, Context, GpuScene, local)
+    elif name == "restir_di":
+        out = restir_secondary(torch, Context, GpuScene, local)
     else:
         out = vcm_secondary(torch, Context, GpuScene, local)
     print(json.dumps({"leg": name, **out}))

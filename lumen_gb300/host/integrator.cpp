@@ -133,4 +133,36 @@ bool GpuSPPM::update() {  // SPPM::update (SPPM.cpp:186-192)
     return changed;
 }
 
+void GpuReSTIR::init() {
+    Integrator::init();
+    frame_num = 0;
+    do_spatiotemporal = false;
+    prev_cam_ = cam;
+}
+
+void GpuReSTIR::render() {  // ReSTIR::render (ReSTIR.cpp:74-157)
+    lgb_restir_params p{};
+    for (int i = 0; i < 3; i++) p.sky_col[i] = lumen_scene->config.sky_col[i];
+    p.max_depth = lumen_scene->config.path_length;
+    p.num_lights = (int32_t)lumen_scene->lights.size();
+    p.light_triangle_count = (int32_t)lumen_scene->total_light_triangle_cnt;
+    p.dir_light_idx = lumen_scene->dir_light_idx;
+    uint32_t unused;
+    vcm_seeds(seed, frame_num, &p.seed, &unused);
+    p.frame_num = frame_num;
+    p.do_spatiotemporal = do_spatiotemporal ? 1u : 0u;
+    p.enable_accumulation = enable_accumulation ? 1u : 0u;
+    p.flags = flags;
+    check(lgb_restir_di_iteration(scene, &cam, &prev_cam_, &p, output_film, stream), "lgb_restir_di_iteration");
+    do_spatiotemporal = true;
+    prev_cam_ = cam;
+}
+
+bool GpuReSTIR::update() {  // ReSTIR::update (ReSTIR.cpp:159-165)
+    frame_num++;
+    const bool changed = Integrator::update();
+    if (changed) frame_num = 0;
+    return changed;
+}
+
 }  // namespace lgbh

@@ -81,6 +81,24 @@ class GpuSPPM final : public Integrator {
     void* stream = nullptr;
 };
 
+// The ReSTIR DI integrator (ReSTIR.cpp:74-165): one frame per render(); spatiotemporal reuse is off for the
+// first frame and on afterwards (ReSTIR.cpp:154-156); the previous camera feeds the temporal reprojection test.
+class GpuReSTIR final : public Integrator {
+  public:
+    using Integrator::Integrator;
+    void init() override;
+    void render() override;
+    bool update() override;
+    bool do_spatiotemporal = false;
+    bool enable_accumulation = true;
+    uint32_t flags = 0;  // LGB_RESTIR_*
+    uint32_t seed = 0;
+    void* stream = nullptr;
+
+  private:
+    lgb_camera prev_cam_{};
+};
+
 // Light and eye seeds of VCM iteration `frame` (PCG-style integer hash of (seed, frame, stream)).
 void vcm_seeds(uint32_t seed, uint32_t frame, uint32_t* light_seed, uint32_t* eye_seed);
 

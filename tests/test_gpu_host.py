@@ -128,3 +128,27 @@ def test_headless_sppm_matches_direct_iterations(host):
     assert ok.all(axis=1).mean() >= 0.99, (ok.all(axis=1).mean(), np.abs(film - got).max())
     np.testing.assert_allclose(film[:, :3].mean(0), got[:, :3].mean(0), rtol=1e-3)
     assert film[:, :3].mean() > 0.01
+
+
+def test_headless_restir_matches_direct_iterations(host):
+    """A scene whose integrator is "restir" renders through the GpuReSTIR mirror (reuse off for the first frame, on
+    afterwards, the previous camera, seeds) as direct lgb_restir_di_iteration calls with the same parameters."""
+    from lumen_gb300.scene import Context, GpuScene, camera_lookat, restir_params
+    scene = os.path.join(HERE, "golden", "scenes", "mixed_restir.json")
+    w, h, n = 40, 30, 4
+    film = host.render_path(scene, w, h, n)
+    arrays, info = host.load_scene(scene)
+    assert len(arrays.lights) == 1
+    ctx = Context(0)
+    sc = GpuScene(ctx, arrays)
+    sc.build()
+    cam = camera_lookat(arrays.camera_pos, arrays.camera_dir, arrays.fov, w, h)
+    direct = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+    for f in range(n):
+        sc.restir_di_iteration(cam, restir_params(arrays, _hash32(2 * f + 1), f, 1 if f > 0 else 0), direct,
+                               prev_cam=cam)
+    sc.sync()
+    got = direct.cpu().numpy()
+    ok = np.abs(film[:, :3] - got[:, :3]) <= 1e-4 * np.maximum(np.abs(got[:, :3]), 1e-6) + 1e-6
+    assert ok.all(axis=1).mean() >= 0.97, (ok.all(axis=1).mean(), np.abs(film - got).max())
+    assert film[:, :3].mean() > 0.0

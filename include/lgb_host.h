@@ -27,6 +27,9 @@ typedef struct lgbh_scene_info {
     float bbox_min[3];
     float bbox_max[3];
     float radius;
+    float base_radius;    /* SPPM integrator block (SPPMConfig::base_radius) */
+    float radius_factor;  /* VCM integrator block (VCMConfig::radius_factor) */
+    int32_t enable_vm;    /* VCM integrator block (VCMConfig::enable_vm) */
 } lgbh_scene_info;
 
 /* Loads a Lumen JSON scene and its OBJ (LumenScene::load_lumen_scene, LumenScene.cpp:231-513). On failure

@@ -22,6 +22,12 @@ lgb_status cuda_error(Ctx* ctx, cudaError_t e, const char* what) {
     return set_error(ctx, e == cudaErrorMemoryAllocation ? LGB_ERR_OUT_OF_MEMORY : LGB_ERR_CUDA, m);
 }
 
+void ctx_retain(Ctx* c) { c->users++; }
+void ctx_release(Ctx* c) {
+    if (c->users > 0) c->users--;
+    if (c->users == 0 && c->released) delete static_cast<lgb_ctx*>(c);
+}
+
 namespace {
 
 void free_scene(Scene* s) {
@@ -117,7 +123,11 @@ LGB_API lgb_status lgb_create(lgb_ctx** out, int device) {
     return LGB_OK;
 }
 
-LGB_API void lgb_destroy(lgb_ctx* ctx) { delete ctx; }
+LGB_API void lgb_destroy(lgb_ctx* ctx) {
+    if (!ctx) return;
+    if (ctx->users == 0) delete ctx;
+    else ctx->released = true;
+}
 
 LGB_API const char* lgb_last_error(const lgb_ctx* ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
 
@@ -243,14 +253,17 @@ LGB_API lgb_status lgb_scene_create(lgb_ctx* ctx, const lgb_scene_desc* d, lgb_s
         return st;
     }
     *out = s;
+    ctx_retain(ctx);
     return LGB_OK;
 }
 
 LGB_API void lgb_scene_destroy(lgb_scene* s) {
     if (!s) return;
-    cudaSetDevice(s->ctx->device);
+    Ctx* c = s->ctx;
+    cudaSetDevice(c->device);
     free_scene(s);
     delete s;
+    ctx_release(c);
 }
 
 LGB_API lgb_status lgb_bvh_build(lgb_scene* s, const lgb_build_opts* opts, lgb_build_stats* stats) {

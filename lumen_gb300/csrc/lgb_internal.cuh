@@ -74,7 +74,13 @@ struct Ctx {
     int device = 0;
     std::string last_error;
     int sm_count = 0;
+    uint32_t users = 0;     // scenes and batches made with this context and not destroyed yet
+    bool released = false;  // lgb_destroy was called while users > 0: freed with the last user
 };
+// A scene or batch holds its context: lgb_destroy of a context still in use only marks it, and the last
+// lgb_scene_destroy / lgb_batch_destroy frees it, so the order of the destroy calls does not matter.
+void ctx_retain(Ctx* c);
+void ctx_release(Ctx* c);
 
 struct BvhDevice {
     WideNode* nodes = nullptr;

@@ -1155,13 +1155,16 @@ LGB_API lgb_status lgb_batch_create(lgb_ctx* ctx, lgb_scene* const* scenes, uint
         return st;
     }
     *out = b;
+    ctx_retain(ctx);
     return LGB_OK;
 }
 
 LGB_API void lgb_batch_destroy(lgb_batch* b) {
     if (!b) return;
+    lgb::Ctx* c = b->ctx;
     lgb::free_batch(b);
     delete b;
+    lgb::ctx_release(c);
 }
 
 LGB_API lgb_status lgb_batch_render(lgb_batch* b, const lgb_batch_job* jobs, uint32_t num_jobs, const lgb_batch_opts* opts,

@@ -67,6 +67,9 @@ LGB_API lgb_status lgbh_scene_get_info(lgbh_scene* s, lgbh_scene_info* out) {
     out->dir_light_idx = sc.dir_light_idx;
     out->total_light_area = sc.total_light_area;
     out->radius = sc.radius;
+    out->base_radius = sc.config.base_radius;
+    out->radius_factor = sc.config.radius_factor;
+    out->enable_vm = sc.config.enable_vm ? 1 : 0;
     return LGB_OK;
 }
 

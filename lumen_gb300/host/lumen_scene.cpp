@@ -159,10 +159,11 @@ void LumenScene::load(const std::string& json_path) {
         std::transform(config.integrator.begin(), config.integrator.end(), config.integrator.begin(), ::tolower);
     }
     if (!integ["path_length"].is_null()) config.path_length = (int)integ["path_length"].as_number();
-    if (config.integrator == "vcm") {  // LumenScene.cpp:248-253
+    if (config.integrator == "sppm") {  // LumenScene.cpp:248-249
+        if (!integ["base_radius"].is_null()) config.base_radius = (float)integ["base_radius"].as_number();
+    } else if (config.integrator == "vcm") {  // LumenScene.cpp:250-253
         if (!integ["enable_vm"].is_null()) config.enable_vm = integ["enable_vm"].as_number() == 1;
         if (!integ["radius_factor"].is_null()) config.radius_factor = (float)integ["radius_factor"].as_number();
-        if (!integ["base_radius"].is_null()) config.base_radius = (float)integ["base_radius"].as_number();
     }
     if (!integ["sky_col"].is_null()) vec3_of(integ["sky_col"], config.sky_col, config.sky_col);
     // geometry

@@ -16,7 +16,8 @@ class SceneInfo(C.Structure):
     _fields_ = [("cam_pos", C.c_float * 3), ("cam_dir", C.c_float * 3), ("fov", C.c_float),
                 ("path_length", C.c_int32), ("sky_col", C.c_float * 3), ("light_triangle_count", C.c_uint32),
                 ("dir_light_idx", C.c_uint32), ("total_light_area", C.c_float), ("bbox_min", C.c_float * 3),
-                ("bbox_max", C.c_float * 3), ("radius", C.c_float)]
+                ("bbox_max", C.c_float * 3), ("radius", C.c_float), ("base_radius", C.c_float),
+                ("radius_factor", C.c_float), ("enable_vm", C.c_int32)]
 
 
 _lib = None

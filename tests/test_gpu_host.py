@@ -120,8 +120,8 @@ def test_headless_sppm_matches_direct_iterations(host):
     cam = camera_lookat(arrays.camera_pos, arrays.camera_dir, arrays.fov, w, h)
     direct = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
     for f in range(n):
-        sc.sppm_iteration(cam, sppm_params(arrays, int(info.path_length), 0.05, _hash32(2 * f + 1), f,
-                                           sky=tuple(info.sky_col)), direct)
+        sc.sppm_iteration(cam, sppm_params(arrays, int(info.path_length), float(info.base_radius),
+                                           _hash32(2 * f + 1), f, sky=tuple(info.sky_col)), direct)
     sc.sync()
     got = direct.cpu().numpy()
     ok = np.abs(film[:, :3] - got[:, :3]) <= 1e-4 * np.maximum(np.abs(got[:, :3]), 1e-6) + 1e-6

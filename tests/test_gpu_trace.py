@@ -221,3 +221,26 @@ def test_host_buffer_query_errors(ctx):
         _check(sc.lib, sc.ctx.handle, sc.lib.lgb_trace_closest_host(sc.handle, None, C.c_void_p(hits.data_ptr()), 4, None))
     sc.trace_closest_host(rays[:0], hits[:0])  # zero rays: nothing to do
     sc.sync()
+
+
+def test_context_outlives_its_scenes_whatever_the_destroy_order(ctx):
+    """lgb_destroy of a context that scenes and batches still use only marks it; the last lgb_scene_destroy /
+    lgb_batch_destroy frees it (a garbage collector may finalise the context first). No CUDA error is left behind."""
+    import ctypes as C
+    from lumen_gb300.scene import Batch
+    lib = abi.load()
+    own = Context(0)
+    arrays = procedural.traversal_scene(sphere_freq=8, n_random=200, seed=5)
+    sc = GpuScene(own, arrays)
+    sc.build()
+    batch = Batch(own, [sc])
+    lib.lgb_destroy(own.handle)  # the context goes first
+    own.handle = None
+    batch.close()
+    sc.close()
+    rays = procedural.incoherent_rays(arrays, 1000, seed=2)
+    other = GpuScene(ctx, arrays)  # another context keeps working, with no stale error
+    other.build()
+    hits = gpu_closest(other, rays)
+    assert (hits["prim"] != 0xFFFFFFFF).any()
+    other.close()

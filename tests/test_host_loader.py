@@ -168,3 +168,14 @@ def test_film_writers_exr_and_pfm(tmp_path):
     np.testing.assert_array_equal(pfm, film[:, :3].reshape(h, w, 3))
     with pytest.raises(abi.LgbError):
         host_scene.write_image(str(tmp_path / "no" / "such" / "dir.exr"), film, w, h)
+
+
+def test_integrator_blocks():
+    """The integrator block's own fields (LumenScene.cpp:237-253): base_radius for SPPM; radius_factor and
+    enable_vm for VCM; each read only for its own integrator type."""
+    from lumen_gb300 import host_scene
+    scenes = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "scenes")
+    _, sppm = host_scene.load_scene(os.path.join(scenes, "mixed_sppm.json"))
+    assert sppm.path_length == 5 and abs(sppm.base_radius - 0.05) < 1e-7
+    _, vcm = host_scene.load_scene(os.path.join(scenes, "mixed_vcm.json"))
+    assert vcm.enable_vm == 1 and abs(vcm.radius_factor - 1.0) < 1e-7 and abs(vcm.base_radius - 0.03) < 1e-7

@@ -125,24 +125,35 @@ __device__ __forceinline__ v3 eval_principled_rev(const Mat& m, v3 wo, v3 wi, fl
 }
 
 // eval_bsdf(n_s, wo, mat, mode, ff, wi, pdf_w, pdf_rev_w, eval_reverse): the mode only changes the unused
-// inner transmission value, so it is not a parameter here.
+// inner transmission value, so it is not a parameter here. MASK (LGB_BSDF_* bits) limits the lobes compiled in,
+// as in bsdf.cuh: a type outside it evaluates to zero.
+template <uint32_t MASK = kAllBsdfs>
 __device__ __forceinline__ v3 eval_bsdf_rev(v3 n_s, v3 wo, const Mat& m, bool ff, v3 wi, float& pdf, float& pdf_rev, bool rev) {
     pdf = 0.0f; pdf_rev = 0.0f;
     v3 T, B;
     branchless_onb(n_s, T, B);
     wo = to_local(wo, T, B, n_s);
     wi = to_local(wi, T, B, n_s);
-    switch (m.type) {
-        case LGB_BSDF_DIFFUSE: {
-            const v3 f = eval_diffuse(m, wo, wi, pdf);
-            pdf_rev = pdf;
-            return f;
-        }
-        case LGB_BSDF_DIELECTRIC: return eval_dielectric_rev(m, wo, wi, pdf, pdf_rev, ff, rev);
-        case LGB_BSDF_CONDUCTOR: return eval_conductor_rev(m, wo, wi, pdf, pdf_rev, rev);
-        case LGB_BSDF_PRINCIPLED: return eval_principled_rev(m, wo, wi, pdf, pdf_rev, ff, rev);
-        default: return V3(0.0f);
+    switch (m.type & MASK) {
+        case LGB_BSDF_DIFFUSE:
+            if constexpr ((MASK & LGB_BSDF_DIFFUSE) != 0) {
+                const v3 f = eval_diffuse(m, wo, wi, pdf);
+                pdf_rev = pdf;
+                return f;
+            }
+            break;
+        case LGB_BSDF_DIELECTRIC:
+            if constexpr ((MASK & LGB_BSDF_DIELECTRIC) != 0) return eval_dielectric_rev(m, wo, wi, pdf, pdf_rev, ff, rev);
+            break;
+        case LGB_BSDF_CONDUCTOR:
+            if constexpr ((MASK & LGB_BSDF_CONDUCTOR) != 0) return eval_conductor_rev(m, wo, wi, pdf, pdf_rev, rev);
+            break;
+        case LGB_BSDF_PRINCIPLED:
+            if constexpr ((MASK & LGB_BSDF_PRINCIPLED) != 0) return eval_principled_rev(m, wo, wi, pdf, pdf_rev, ff, rev);
+            break;
+        default: break;
     }
+    return V3(0.0f);
 }
 
 __device__ __forceinline__ float conductor_pdf(const Mat& m, v3 wo, v3 wi) {
@@ -198,16 +209,24 @@ __device__ __forceinline__ float clearcoat_pdf(const Mat& m, v3 wo, v3 wi) {
     return D / (4.0f * dot(wo, h));
 }
 
+template <uint32_t MASK = kAllBsdfs>
 __device__ __forceinline__ float bsdf_pdf(const Mat& m, v3 n_s, v3 wo, v3 wi, bool ff) {
     v3 T, B;
     branchless_onb(n_s, T, B);
     wo = to_local(wo, T, B, n_s);
     wi = to_local(wi, T, B, n_s);
-    switch (m.type) {
-        case LGB_BSDF_DIFFUSE: return diffuse_pdf(wo, wi);
-        case LGB_BSDF_DIELECTRIC: return dielectric_pdf_only(m, wo, wi, ff);
-        case LGB_BSDF_CONDUCTOR: return conductor_pdf(m, wo, wi);
-        case LGB_BSDF_PRINCIPLED: {
+    switch (m.type & MASK) {
+        case LGB_BSDF_DIFFUSE:
+            if constexpr ((MASK & LGB_BSDF_DIFFUSE) != 0) return diffuse_pdf(wo, wi);
+            break;
+        case LGB_BSDF_DIELECTRIC:
+            if constexpr ((MASK & LGB_BSDF_DIELECTRIC) != 0) return dielectric_pdf_only(m, wo, wi, ff);
+            break;
+        case LGB_BSDF_CONDUCTOR:
+            if constexpr ((MASK & LGB_BSDF_CONDUCTOR) != 0) return conductor_pdf(m, wo, wi);
+            break;
+        case LGB_BSDF_PRINCIPLED:
+            if constexpr ((MASK & LGB_BSDF_PRINCIPLED) != 0) {
             float pdf = 0.0f, ps, pd, pc, pt;
             const float F = fresnel_dielectric(wo.z, m.ior, ff);
             sampling_probs(m, F, ff, ps, pd, pc, pt);
@@ -218,12 +237,15 @@ __device__ __forceinline__ float bsdf_pdf(const Mat& m, v3 n_s, v3 wo, v3 wi, bo
             }
             if (pt > 0.0f) pdf += pt * dielectric_pdf_only(m, wo, wi, ff);
             return pdf;
-        }
-        default: return 0.0f;
+            }
+            break;
+        default: break;
     }
+    return 0.0f;
 }
 
 // sample_bsdf with an explicit transport mode (0 = importance, light subpaths; 1 = radiance).
+template <uint32_t MASK = kAllBsdfs>
 __device__ __forceinline__ v3 sample_bsdf_mode(v3 n_s, v3 wo, const Mat& m, uint32_t mode, bool ff, v3& wi, float& pdf,
                                                float& cos_t, v3 r) {
     v3 f = V3(0.0f);
@@ -232,13 +254,25 @@ __device__ __forceinline__ v3 sample_bsdf_mode(v3 n_s, v3 wo, const Mat& m, uint
     branchless_onb(n_s, T, B);
     wo = to_local(wo, T, B, n_s);
     const v2 xy = V2(r.x, r.y);
-    switch (m.type) {
-        case LGB_BSDF_DIFFUSE: f = sample_diffuse(m, wo, wi, pdf, cos_t, xy); break;
-        case LGB_BSDF_MIRROR: f = sample_mirror(wo, wi, pdf, cos_t); break;
-        case LGB_BSDF_GLASS: f = sample_glass(m, wo, wi, pdf, cos_t, mode, ff); break;
-        case LGB_BSDF_DIELECTRIC: f = sample_dielectric(m, wo, wi, mode, ff, pdf, cos_t, xy); break;
-        case LGB_BSDF_CONDUCTOR: f = sample_conductor(m, wo, wi, pdf, cos_t, xy); break;
-        case LGB_BSDF_PRINCIPLED: f = sample_principled(m, wo, wi, mode, ff, pdf, cos_t, r); break;
+    switch (m.type & MASK) {
+        case LGB_BSDF_DIFFUSE:
+            if constexpr ((MASK & LGB_BSDF_DIFFUSE) != 0) f = sample_diffuse(m, wo, wi, pdf, cos_t, xy);
+            break;
+        case LGB_BSDF_MIRROR:
+            if constexpr ((MASK & LGB_BSDF_MIRROR) != 0) f = sample_mirror(wo, wi, pdf, cos_t);
+            break;
+        case LGB_BSDF_GLASS:
+            if constexpr ((MASK & LGB_BSDF_GLASS) != 0) f = sample_glass(m, wo, wi, pdf, cos_t, mode, ff);
+            break;
+        case LGB_BSDF_DIELECTRIC:
+            if constexpr ((MASK & LGB_BSDF_DIELECTRIC) != 0) f = sample_dielectric(m, wo, wi, mode, ff, pdf, cos_t, xy);
+            break;
+        case LGB_BSDF_CONDUCTOR:
+            if constexpr ((MASK & LGB_BSDF_CONDUCTOR) != 0) f = sample_conductor(m, wo, wi, pdf, cos_t, xy);
+            break;
+        case LGB_BSDF_PRINCIPLED:
+            if constexpr ((MASK & LGB_BSDF_PRINCIPLED) != 0) f = sample_principled(m, wo, wi, mode, ff, pdf, cos_t, r);
+            break;
         default: break;
     }
     wi = to_world(wi, T, B, n_s);

@@ -35,6 +35,9 @@ constexpr int kVcmThreads = 128;
 constexpr int kMaxMergeCells = 16;
 constexpr float kTMinV = 0.001f, kTMaxV = 10000.0f, kEpsV = 0.001f;
 constexpr int kVertexF4 = 6;  // light vertex = 6 x float4 (96 bytes)
+// BSDF type sets the subpath kernels are compiled for: diffuse, mirror, glass and dielectric; those and conductor.
+constexpr uint32_t kVcmLobesDG = LGB_BSDF_DIFFUSE | LGB_BSDF_MIRROR | LGB_BSDF_GLASS | LGB_BSDF_DIELECTRIC;
+constexpr uint32_t kVcmLobesDGC = kVcmLobesDG | LGB_BSDF_CONDUCTOR;
 
 struct VcmArgs {
     float iv[16], ip[16], view[16], proj[16];
@@ -122,6 +125,7 @@ struct VState {
 };
 
 // vcm_connect_cam (vcm_commons.glsl:24-75): the splat of a light vertex and its pixel (have = false: none).
+template <uint32_t MASK>
 __device__ v3 connect_cam(const SceneView& S, const VcmArgs& A, const CamV& c, v3 n_s, v3 payload_ns, v3 pos,
                           const VState& st, float eta_vm, v3 wo, const Mat& mat, uint32_t& pidx, bool& have) {
     have = false;
@@ -137,7 +141,7 @@ __device__ v3 connect_cam(const SceneView& S, const VcmArgs& A, const CamV& c, v
     const float ratio = fabsf(cos_y) / (c.area * cos3 * len * len);
     const v3 origin = offset_ray2(pos, n_s);
     float pdf_fwd, pdf_rev;
-    const v3 f = eval_bsdf_rev(n_s, wo, mat, dot(payload_ns, wo) > 0.0f, dir, pdf_fwd, pdf_rev, true);
+    const v3 f = eval_bsdf_rev<MASK>(n_s, wo, mat, dot(payload_ns, wo) > 0.0f, dir, pdf_fwd, pdf_rev, true);
     if (is_zero3(f)) return L;
     if (ratio > 0.0f) {
         const RayQ q = make_rayq(origin.x, origin.y, origin.z, 0.0f, dir.x, dir.y, dir.z, len - kEpsV);
@@ -161,6 +165,7 @@ __device__ v3 connect_cam(const SceneView& S, const VcmArgs& A, const CamV& c, v
 }
 
 // vcm_light.rgen main: one light subpath per launch point (x, y), stored at x * H + y.
+template <uint32_t MASK>
 __global__ void __launch_bounds__(kVcmThreads) k_vcm_light(SceneView S, VcmArgs A) {
     const CamV cam = cam_setup(A);
     const Etas eta = etas(A);
@@ -219,7 +224,7 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_light(SceneView S, VcmArgs 
             if (!spec && A.use_vc == 1) {
                 uint32_t pidx = 0;
                 bool have = false;
-                const v3 L = connect_cam(S, A, cam, n_s, h.n_s, h.pos, st, eta.vm, wo, mat, pidx, have);
+                const v3 L = connect_cam<MASK>(S, A, cam, n_s, h.n_s, h.pos, st, eta.vm, wo, mat, pidx, have);
                 if (luminance(L) > 0.0f && have) {
                     atomicAdd(&A.splat[3 * pidx], L.x);
                     atomicAdd(&A.splat[3 * pidx + 1], L.y);
@@ -229,13 +234,13 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_light(SceneView S, VcmArgs 
             const float c0 = rnd(seed), c1 = rnd(seed), c2 = rnd(seed);
             float pdf_dir, cos_t;
             v3 wi;
-            const v3 f = sample_bsdf_mode(n_s, wo, mat, 0u, side, wi, pdf_dir, cos_t, V3(c0, c1, c2));
+            const v3 f = sample_bsdf_mode<MASK>(n_s, wo, mat, 0u, side, wi, pdf_dir, cos_t, V3(c0, c1, c2));
             st.wi = wi;
             const bool same = dot(st.wi, n_s) > 0.0f && dot(wo, n_s) > 0.0f;
             const bool trans = (mat.props & LGB_FLAG_TRANSMISSION) == LGB_FLAG_TRANSMISSION;
             if (is_zero3(f) || pdf_dir == 0.0f || (!same && !trans)) break;
             float pdf_rev = pdf_dir;
-            if (!spec) pdf_rev = bsdf_pdf(mat, n_s, st.wi, wo, side);
+            if (!spec) pdf_rev = bsdf_pdf<MASK>(mat, n_s, st.wi, wo, side);
             const float ac = fabsf(cos_t);
             st.pos = offset_ray(h.pos, n_g);
             if (!spec) {
@@ -259,6 +264,7 @@ struct EyeHit {
 };
 
 // vcm_connect_light (vcm_commons.glsl:146-204)
+template <uint32_t MASK>
 __device__ v3 connect_light(const SceneView& S, const VcmArgs& A, uint4& seed, const EyeHit& h, v3 n_s, v3 wo, const Mat& mat,
                             bool side, float eta_vm, const VState& cs, float& pdf_rev) {
     v3 res = V3(0.0f);
@@ -267,7 +273,7 @@ __device__ v3 connect_light(const SceneView& S, const VcmArgs& A, uint4& seed, c
     const float cos_x = dot(li.wi, n_s);
     const v3 origin = offset_ray2(h.pos, n_s);
     float pdf_fwd;
-    const v3 f = eval_bsdf_rev(n_s, wo, mat, side, li.wi, pdf_fwd, pdf_rev, true);
+    const v3 f = eval_bsdf_rev<MASK>(n_s, wo, mat, side, li.wi, pdf_fwd, pdf_rev, true);
     if (!is_zero3(f)) {
         const RayQ q = make_rayq(origin.x, origin.y, origin.z, 0.0f, li.wi.x, li.wi.y, li.wi.z, li.wi_len - kEpsV);
         if (!trace_any_single(S.nodes, S.tris, q, S.status)) {
@@ -284,6 +290,7 @@ __device__ v3 connect_light(const SceneView& S, const VcmArgs& A, uint4& seed, c
 }
 
 // vcm_connect_light_vertices (vcm_commons.glsl:206-251)
+template <uint32_t MASK>
 __device__ v3 connect_light_vertices(const SceneView& S, const VcmArgs& A, const float4* lv, uint32_t len_path, int depth,
                                      const EyeHit& h, v3 n_s, v3 wo, const Mat& mat, bool side, float eta_vm,
                                      const VState& cs, float pdf_rev) {
@@ -300,9 +307,9 @@ __device__ v3 connect_light_vertices(const SceneView& S, const VcmArgs& A, const
         const float G = cos_light * cos_cam / len_sqr;
         if (!(G > 0.0f)) continue;
         float cam_pdf_fwd, unused, light_pdf_fwd, light_pdf_rev;
-        const v3 f_cam = eval_bsdf_rev(n_s, wo, mat, side, dir, cam_pdf_fwd, unused, false);
+        const v3 f_cam = eval_bsdf_rev<MASK>(n_s, wo, mat, side, dir, cam_pdf_fwd, unused, false);
         const Mat lm = load_material(S, v.mat, v.u, v.v);
-        const v3 f_light = eval_bsdf_rev(v.n_s, v.wo, lm, v.side == 1u, -dir, light_pdf_fwd, light_pdf_rev, true);
+        const v3 f_light = eval_bsdf_rev<MASK>(v.n_s, v.wo, lm, v.side == 1u, -dir, light_pdf_fwd, light_pdf_rev, true);
         if (is_zero3(f_light) || is_zero3(f_cam)) continue;
         cam_pdf_fwd *= fabsf(cos_light) / len_sqr;
         light_pdf_fwd *= fabsf(cos_cam) / len_sqr;
@@ -320,6 +327,7 @@ __device__ v3 connect_light_vertices(const SceneView& S, const VcmArgs& A, const
 }
 
 // vcm_merge_light_vertices (vcm_commons.glsl:254-296) over the slot table (count, representative photon)
+template <uint32_t MASK>
 __device__ v3 merge(const VcmArgs& A, int depth, const EyeHit& h, v3 n_s, v3 wo, const Mat& mat, bool side, float eta_vc,
                     const VState& cs, float norm) {
     const float radius = A.radius;
@@ -343,7 +351,7 @@ __device__ v3 merge(const VcmArgs& A, int depth, const EyeHit& h, v3 n_s, v3 wo,
                 if (ph.path_len + (uint32_t)depth - 1u > (uint32_t)A.max_depth) continue;
                 const v3 pwi = -ph.wi;
                 float cam_pdf_fwd, cam_pdf_rev;
-                const v3 f = eval_bsdf_rev(n_s, wo, mat, side, pwi, cam_pdf_fwd, cam_pdf_rev, true);
+                const v3 f = eval_bsdf_rev<MASK>(n_s, wo, mat, side, pwi, cam_pdf_fwd, cam_pdf_rev, true);
                 if (is_zero3(f)) continue;
                 const float w_light = ph.d_vcm * eta_vc + ph.d_vm * cam_pdf_fwd;
                 const float w_cam = cs.d_vcm * eta_vc + cs.d_vm * cam_pdf_rev;
@@ -358,6 +366,7 @@ __device__ v3 merge(const VcmArgs& A, int depth, const EyeHit& h, v3 n_s, v3 wo,
 }
 
 // vcm_eye.rgen main + vcm_trace_eye for pixel (x, y): film[y * W + x], consumes the pixel's splat.
+template <uint32_t MASK>
 __global__ void __launch_bounds__(kVcmThreads) k_vcm_eye(SceneView S, VcmArgs A) {
     const CamV cam = cam_setup(A);
     const Etas eta = etas(A);
@@ -422,20 +431,20 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_eye(SceneView S, VcmArgs A)
                 col = col + cs.thr * Le;
             }
             float pdf_rev = 0.0f;
-            if (!spec && depth < A.max_depth) col = col + connect_light(S, A, seed, eh, n_s, wo, mat, side, eta.vm, cs, pdf_rev);
-            if (!spec) col = col + connect_light_vertices(S, A, lv, lp_len, depth, eh, n_s, wo, mat, side, eta.vm, cs, pdf_rev);
-            if (!spec && A.use_vm == 1) col = col + merge(A, depth, eh, n_s, wo, mat, side, eta.vc, cs, norm);
+            if (!spec && depth < A.max_depth) col = col + connect_light<MASK>(S, A, seed, eh, n_s, wo, mat, side, eta.vm, cs, pdf_rev);
+            if (!spec) col = col + connect_light_vertices<MASK>(S, A, lv, lp_len, depth, eh, n_s, wo, mat, side, eta.vm, cs, pdf_rev);
+            if (!spec && A.use_vm == 1) col = col + merge<MASK>(A, depth, eh, n_s, wo, mat, side, eta.vc, cs, norm);
             if (depth >= A.max_depth) break;
             const float c0 = rnd(seed), c1 = rnd(seed), c2 = rnd(seed);
             float pdf_dir, cos_t;
             v3 wi;
-            const v3 f = sample_bsdf_mode(n_s, wo, mat, 1u, side, wi, pdf_dir, cos_t, V3(c0, c1, c2));
+            const v3 f = sample_bsdf_mode<MASK>(n_s, wo, mat, 1u, side, wi, pdf_dir, cos_t, V3(c0, c1, c2));
             cs.wi = wi;
             const bool trans = (mat.props & LGB_FLAG_TRANSMISSION) == LGB_FLAG_TRANSMISSION;
             const bool same = dot(cs.wi, n_s) > 0.0f && dot(wo, n_s) > 0.0f;
             if (is_zero3(f) || pdf_dir == 0.0f || (!same && !trans)) break;
             pdf_rev = pdf_dir;
-            if (!spec) pdf_rev = bsdf_pdf(mat, n_s, cs.wi, wo, side);
+            if (!spec) pdf_rev = bsdf_pdf<MASK>(mat, n_s, cs.wi, wo, side);
             const float ac = fabsf(cos_t);
             cs.pos = offset_ray(h.pos, n_g);
             if (!spec) {
@@ -646,7 +655,13 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
     const SceneView S = scene_view(s);
     const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
     const int grid = (int)std::min<uint32_t>((screen + kVcmThreads - 1) / kVcmThreads, (uint32_t)sms * 16u);
-    k_vcm_light<<<grid, kVcmThreads, 0, st>>>(S, A);
+    // The subpath kernels are instantiated per set of BSDF types (the caustics scene needs only diffuse and
+    // dielectric lobes): fewer inlined lobes keep their loops inside the instruction cache.
+    const uint32_t used = s->bsdf_mask;
+    const uint32_t lobes = (used & ~kVcmLobesDG) == 0u ? kVcmLobesDG : ((used & ~kVcmLobesDGC) == 0u ? kVcmLobesDGC : kAllBsdfs);
+    if (lobes == kVcmLobesDG) k_vcm_light<kVcmLobesDG><<<grid, kVcmThreads, 0, st>>>(S, A);
+    else if (lobes == kVcmLobesDGC) k_vcm_light<kVcmLobesDGC><<<grid, kVcmThreads, 0, st>>>(S, A);
+    else k_vcm_light<kAllBsdfs><<<grid, kVcmThreads, 0, st>>>(S, A);
     LGB_CUDA_TRY(ctx, cudaGetLastError());
     if (p->use_vm == 1) {
         uint64_t* k0 = reinterpret_cast<uint64_t*>(base + o_k0);
@@ -660,7 +675,9 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
     } else {
         LGB_CUDA_TRY(ctx, cudaMemsetAsync(gc, 0, 4ull * table, st));
     }
-    k_vcm_eye<<<grid, kVcmThreads, 0, st>>>(S, A);
+    if (lobes == kVcmLobesDG) k_vcm_eye<kVcmLobesDG><<<grid, kVcmThreads, 0, st>>>(S, A);
+    else if (lobes == kVcmLobesDGC) k_vcm_eye<kVcmLobesDGC><<<grid, kVcmThreads, 0, st>>>(S, A);
+    else k_vcm_eye<kAllBsdfs><<<grid, kVcmThreads, 0, st>>>(S, A);
     LGB_CUDA_TRY(ctx, cudaGetLastError());
     return LGB_OK;
 }

@@ -343,6 +343,29 @@ typedef struct lgb_sppm_params {
 LGB_API lgb_status lgb_sppm_iteration(lgb_scene* scene, const lgb_camera* camera, const lgb_sppm_params* params,
                                       float* d_film, void* stream);
 
+/* ---- BDPT: bidirectional path tracing (src/RayTracer/BDPT.cpp:55-88, src/shaders/integrators/bdpt/bdpt.rgen,
+ *      src/shaders/integrators/bdpt_commons.glsl) on the library's traversal, BSDFs and light sampling. ---- */
+typedef struct lgb_bdpt_params {
+    float sky_col[3];              /* PCBDPT::sky_col: set by the reference, never read by bdpt.rgen; kept for the layout */
+    int32_t max_depth;             /* path_length: subpaths of up to max_depth + 1 vertices, strategies s + t <= max_depth + 1 */
+    int32_t num_lights;
+    int32_t light_triangle_count;  /* LumenScene::total_light_triangle_cnt */
+    uint32_t dir_light_idx;        /* must be 0xFFFFFFFF */
+    uint32_t seed;                 /* the RNG's frame value is frame_num ^ seed (the reference draws seed with rand()) */
+    uint32_t frame_num;            /* 0 writes the frame; k mixes the film with weight 1/(k+1) */
+    float spot_angle;              /* spot cone half-angle as lgb_vcm_params; 0 = Lumen's fixed 30 / 25 degrees */
+    uint32_t reserved[6];
+} lgb_bdpt_params;
+
+/* One BDPT frame into d_film (RGBA32F, width*height, row-major): per pixel a light subpath and a camera subpath
+ * through the pixel centre, every connection strategy (s light vertices, t camera vertices) with the reference's
+ * MIS weight, the light-tracing (t = 1) strategies splatted into the frame's image, the progressive film. The
+ * reference's per-frame path buffers live in the scene (reused between frames). A frame's splats all land in that
+ * frame (the reference's unsynchronised splat image leaves the order undefined). max_depth in [1, 32]; area and
+ * spot lights only. */
+LGB_API lgb_status lgb_bdpt_iteration(lgb_scene* scene, const lgb_camera* camera, const lgb_bdpt_params* params,
+                                      float* d_film, void* stream);
+
 /* ---- ReSTIR DI (src/RayTracer/ReSTIR.cpp:74-157, src/shaders/integrators/restir/di/*): resampled direct
  *      lighting with temporal and spatial reuse, on the library's traversal and light sampling. ---- */
 typedef struct lgb_restir_params {

@@ -143,6 +143,12 @@ class SppmParams(C.Structure):
                 ("reserved", C.c_uint32 * 5)]
 
 
+class BdptParams(C.Structure):
+    _fields_ = [("sky_col", C.c_float * 3), ("max_depth", C.c_int32), ("num_lights", C.c_int32),
+                ("light_triangle_count", C.c_int32), ("dir_light_idx", C.c_uint32), ("seed", C.c_uint32),
+                ("frame_num", C.c_uint32), ("spot_angle", C.c_float), ("reserved", C.c_uint32 * 6)]
+
+
 class RestirParams(C.Structure):
     _fields_ = [("sky_col", C.c_float * 3), ("max_depth", C.c_int32), ("num_lights", C.c_int32),
                 ("light_triangle_count", C.c_int32), ("dir_light_idx", C.c_uint32), ("seed", C.c_uint32),
@@ -178,6 +184,7 @@ SIGNATURES = {
     "lgb_vcm_radius": ([C.c_float, C.c_float, C.c_uint32, C.c_float], C.c_float),
     "lgb_vcm_iteration": ([C.c_void_p, C.POINTER(Camera), C.POINTER(VcmParams), C.c_void_p, C.c_void_p], C.c_int32),
     "lgb_sppm_iteration": ([C.c_void_p, C.POINTER(Camera), C.POINTER(SppmParams), C.c_void_p, C.c_void_p], C.c_int32),
+    "lgb_bdpt_iteration": ([C.c_void_p, C.POINTER(Camera), C.POINTER(BdptParams), C.c_void_p, C.c_void_p], C.c_int32),
     "lgb_restir_di_iteration": ([C.c_void_p, C.POINTER(Camera), C.POINTER(Camera), C.POINTER(RestirParams),
                                  C.c_void_p, C.c_void_p], C.c_int32),
     "lgb_vcm_grid": ([C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float,

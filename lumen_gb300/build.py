@@ -15,7 +15,7 @@ ROOT = os.path.dirname(HERE)
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 SOURCES = ["abi.cu", "bvh_build.cu", "traverse.cu", "path.cu", "diag.cu", "film.cu", "adjoint.cu", "vcm.cu", "sppm.cu",
-           "restir.cu"]
+           "restir.cu", "bdpt.cu"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",

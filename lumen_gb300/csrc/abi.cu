@@ -49,6 +49,7 @@ void free_scene(Scene* s) {
     cudaFree(s->diff_buf);
     cudaFree(s->vcm_buf);
     cudaFree(s->sppm_buf);
+    cudaFree(s->bdpt_buf);
     cudaFree(s->restir_buf);
     if (s->pt_graph) cudaGraphExecDestroy((cudaGraphExec_t)s->pt_graph);
     if (s->capture_stream) cudaStreamDestroy((cudaStream_t)s->capture_stream);

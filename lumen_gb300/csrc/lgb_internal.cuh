@@ -124,6 +124,8 @@ struct Scene {
     void* vcm_buf = nullptr;         // VCM state kept between iterations (light vertices, counts, splats, table)
     size_t vcm_buf_bytes = 0;
     uint32_t vcm_w = 0, vcm_h = 0, vcm_per = 0;
+    void* bdpt_buf = nullptr;        // BDPT path buffers, strategy contributions and splat image (per frame)
+    size_t bdpt_buf_bytes = 0;
     void* sppm_buf = nullptr;        // SPPM state kept between frames (visible points, photons, table, bounds)
     size_t sppm_buf_bytes = 0;
     uint32_t sppm_w = 0, sppm_h = 0, sppm_depth = 0;

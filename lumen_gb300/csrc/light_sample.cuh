@@ -94,8 +94,8 @@ __device__ Emission sample_light_Le(const SceneView& S, const LightSet& A, float
 }
 
 struct Incidence {
-    v3 L, wi;
-    float wi_len, pdf_pos_w, pdf_pos_dir_w, cos_y;
+    v3 L, wi, pos, n;  // pos, n: the light point and its normal (-wi for a spot light)
+    float wi_len, pdf_pos_w, pdf_pos_dir_w, cos_y, pdf_pos_a;
     uint32_t flags;
 };
 
@@ -105,6 +105,7 @@ __device__ Incidence sample_light_Li_pos(const SceneView& S, const LightSet& A, 
     const uint32_t li = (uint32_t)(r0 * (float)A.num_lights);
     const lgb_light* L = &S.lights[li];
     r.L = V3(0.0f); r.wi = V3(0.0f); r.wi_len = 0.0f; r.pdf_pos_w = 0.0f; r.pdf_pos_dir_w = 0.0f; r.cos_y = 0.0f;
+    r.pos = V3(0.0f); r.n = V3(0.0f); r.pdf_pos_a = 0.0f;
     r.flags = L->light_flags;
     const uint32_t type = L->light_flags & 7u;
     if (type == LGB_LIGHT_AREA) {
@@ -123,6 +124,9 @@ __device__ Incidence sample_light_Li_pos(const SceneView& S, const LightSet& A, 
         r.L = V3(lm->emissive_factor[0], lm->emissive_factor[1], lm->emissive_factor[2]);
         r.pdf_pos_w = tri_pdf * l2 / r.cos_y;
         r.pdf_pos_dir_w = r.cos_y * LGB_INV_PI * tri_pdf;
+        r.pdf_pos_a = tri_pdf;
+        r.n = n;
+        r.pos = pos;
     } else if (type == LGB_LIGHT_SPOT) {
         const v3 lp = V3(L->pos[0], L->pos[1], L->pos[2]);
         v3 wi = lp - p;
@@ -140,6 +144,9 @@ __device__ Incidence sample_light_Li_pos(const SceneView& S, const LightSet& A, 
         r.pdf_pos_w = l2;
         r.pdf_pos_dir_w = 1.0f / (LGB_TWO_PI * (1.0f - cos_width));
         r.L = V3(L->L[0], L->L[1], L->L[2]) * fall;
+        r.pdf_pos_a = 1.0f;
+        r.n = -wi;
+        r.pos = lp;
     }
     return r;
 }

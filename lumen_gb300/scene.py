@@ -300,6 +300,12 @@ class GpuScene:
                self.lib.lgb_sppm_iteration(self.handle, C.byref(cam), C.byref(params), C.c_void_p(film.data_ptr()),
                                            C.c_void_p(stream)))
 
+    def bdpt_iteration(self, cam: abi.Camera, params: abi.BdptParams, film, stream=None):
+        """lgb_bdpt_iteration: one BDPT frame into film ((npix, 4) float32 CUDA)."""
+        _check(self.lib, self.ctx.handle,
+               self.lib.lgb_bdpt_iteration(self.handle, C.byref(cam), C.byref(params), C.c_void_p(film.data_ptr()),
+                                           C.c_void_p(stream)))
+
     @staticmethod
     def _diff_params(texture_id, texels, roughness, emission, flags=0) -> abi.DiffParams:
         dp = abi.DiffParams()
@@ -441,6 +447,21 @@ def sppm_params(arrays: SceneArrays, max_depth: int, base_radius: float, seed: i
     p.light_triangle_count = arrays.light_triangle_count
     p.dir_light_idx = 0xFFFFFFFF
     p.base_radius = base_radius
+    p.seed = seed
+    p.frame_num = frame_num
+    p.spot_angle = spot_angle
+    return p
+
+
+def bdpt_params(arrays: SceneArrays, max_depth: int, seed: int, frame_num: int, sky=(0.0, 0.0, 0.0),
+                spot_angle: float = 0.0) -> abi.BdptParams:
+    """PCBDPT as BDPT::render fills it (src/RayTracer/BDPT.cpp:55-64) with an explicit seed."""
+    p = abi.BdptParams()
+    p.sky_col[:] = list(sky)
+    p.max_depth = max_depth
+    p.num_lights = len(arrays.lights)
+    p.light_triangle_count = arrays.light_triangle_count
+    p.dir_light_idx = 0xFFFFFFFF
     p.seed = seed
     p.frame_num = frame_num
     p.spot_angle = spot_angle

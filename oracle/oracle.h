@@ -190,6 +190,20 @@ void orc_restir_di_iteration(void* scene, const float inv_view[16], const float 
                              const float prev_proj[16], uint32_t width, uint32_t height, const orc_restir_params* p,
                              float* gbuf, float* passthrough, float* temporal_res, float* spatial_res, float* film,
                              int nthreads);
+// BDPT (BDPT.cpp:55-88, bdpt.rgen, bdpt_commons.glsl): one frame. Light and camera subpaths per pixel, every
+// connection strategy with its MIS weight, the light-tracing splats of the frame and the progressive film
+// (W*H*4, row-major). splat (W*H*3, row-major) receives the frame's splats (diagnostic). Area and spot lights.
+struct orc_bdpt_params {
+    int32_t max_depth;             // path_length
+    int32_t num_lights;
+    int32_t light_triangle_count;
+    uint32_t seed;                 // RNG frame value = frame_num ^ seed
+    uint32_t frame_num;
+    float spot_angle;              // degrees, 0 = the fixed 30 / 25 degree cone
+};
+void orc_bdpt_iteration(void* scene, const float inv_view[16], const float inv_proj[16], const float view[16],
+                        const float proj[16], uint32_t width, uint32_t height, const orc_bdpt_params* p, float* film,
+                        float* splat, int nthreads);
 // PCG4D (utils.glsl:121-133) applied to n state vectors; for known-answer tests.
 void orc_pcg4d(const uint32_t* in, uint32_t* out, uint32_t n);
 // offset_ray (utils.glsl:73-84) applied to n (p, n) pairs.

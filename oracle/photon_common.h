@@ -128,8 +128,8 @@ template <class T> Emission<T> sample_light_Le(const Scene& s, V4<T> rp, V2<T> r
 
 // sample_light_Li with the positional-directional pdf (commons.glsl:224-300, area and spot lights).
 template <class T> struct Incidence {
-    V3<T> L, wi;
-    T wi_len, pdf_pos_w, pdf_pos_dir_w, cos_y;
+    V3<T> L, wi, pos, n;  // pos, n: the light point and its normal (-wi for a spot light)
+    T wi_len, pdf_pos_w, pdf_pos_dir_w, cos_y, pdf_pos_a;
     uint32_t flags;
 };
 template <class T> Incidence<T> sample_light_Li_pos(const Scene& s, V4<T> rp, V3<T> p, int num_lights, Cone cone) {
@@ -137,6 +137,7 @@ template <class T> Incidence<T> sample_light_Li_pos(const Scene& s, V4<T> rp, V3
     const uint32_t light_idx = (uint32_t)(rp.x * T(num_lights));
     const orc_light& light = s.lights[light_idx];
     r.L = V3<T>(0); r.wi = V3<T>(0); r.wi_len = T(0); r.pdf_pos_w = T(0); r.pdf_pos_dir_w = T(0); r.cos_y = T(0);
+    r.pos = V3<T>(0); r.n = V3<T>(0); r.pdf_pos_a = T(0);
     r.flags = light.light_flags;
     const uint32_t type = light.light_flags & 0x7u;
     if (type == LIGHT_AREA) {
@@ -154,6 +155,9 @@ template <class T> Incidence<T> sample_light_Li_pos(const Scene& s, V4<T> rp, V3
         r.L = lm.emissive_factor;
         r.pdf_pos_w = tri_pdf * l2 / r.cos_y;
         r.pdf_pos_dir_w = r.cos_y * K<T>::INV_PI() * tri_pdf;
+        r.pdf_pos_a = tri_pdf;
+        r.n = n;
+        r.pos = pos;
     } else if (type == LIGHT_SPOT) {
         const V3<T> lp(light.pos[0], light.pos[1], light.pos[2]), to(light.to[0], light.to[1], light.to[2]);
         V3<T> wi = lp - p;
@@ -171,6 +175,9 @@ template <class T> Incidence<T> sample_light_Li_pos(const Scene& s, V4<T> rp, V3
         r.pdf_pos_w = l2;
         r.pdf_pos_dir_w = uniform_cone_pdf(cos_width);
         r.L = V3<T>(light.L[0], light.L[1], light.L[2]) * faloff;
+        r.pdf_pos_a = T(1);
+        r.n = -wi;
+        r.pos = lp;
     }
     return r;
 }

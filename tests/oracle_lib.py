@@ -63,6 +63,11 @@ class RestirParams(C.Structure):
                 ("spot_angle", C.c_float), ("flags", C.c_uint32)]
 
 
+class BdptParams(C.Structure):
+    _fields_ = [("max_depth", C.c_int32), ("num_lights", C.c_int32), ("light_triangle_count", C.c_int32),
+                ("seed", C.c_uint32), ("frame_num", C.c_uint32), ("spot_angle", C.c_float)]
+
+
 VCM_VERTEX_BYTES = 104
 
 
@@ -116,6 +121,8 @@ class Oracle:
                                          C.POINTER(C.c_float), C.c_int]
         L.orc_restir_di_iteration.argtypes = [C.c_void_p] + [C.POINTER(C.c_float)] * 4 + [
             C.c_uint32, C.c_uint32, C.POINTER(RestirParams)] + [C.POINTER(C.c_float)] * 5 + [C.c_int]
+        L.orc_bdpt_iteration.argtypes = [C.c_void_p] + [C.POINTER(C.c_float)] * 4 + [
+            C.c_uint32, C.c_uint32, C.POINTER(BdptParams)] + [C.POINTER(C.c_float)] * 2 + [C.c_int]
         L.orc_pcg4d.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.c_uint32]
         L.orc_offset_ray.argtypes = [C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32]
 
@@ -349,6 +356,23 @@ def restir_iteration(scene: "OracleScene", cam, prev_view, prev_proj, params: Re
                                           C.byref(params), _p(state["gbuf"]), _p(state["pass"]),
                                           _p(state["temporal"]), _p(state["spatial"]), _p(state["film"]),
                                           threads or (os.cpu_count() or 1))
+    return state["film"]
+
+
+def bdpt_state(width, height):
+    """The progressive film (persists across BDPT frames) and the last frame's splat image, row-major."""
+    screen = width * height
+    return {"film": np.zeros((screen, 4), np.float32), "splat": np.zeros(screen * 3, np.float32),
+            "width": width, "height": height}
+
+
+def bdpt_iteration(scene: "OracleScene", cam, view, proj, params: BdptParams, state, threads=0):
+    """One BDPT frame of the oracle into state['film']; view / proj are the camera's forward matrices."""
+    f32 = lambda a: np.ascontiguousarray(np.array(a, np.float32).reshape(16))
+    iv, ip, vw, pj = f32(cam.inv_view[:]), f32(cam.inv_projection[:]), f32(view), f32(proj)
+    scene.ora.lib.orc_bdpt_iteration(scene.h, _p(iv), _p(ip), _p(vw), _p(pj), state["width"], state["height"],
+                                     C.byref(params), _p(state["film"]), _p(state["splat"]),
+                                     threads or (os.cpu_count() or 1))
     return state["film"]
 
 

@@ -49,6 +49,7 @@ def test_struct_layouts():
     assert C.sizeof(abi.BatchOpts) == 32
     assert C.sizeof(abi.SppmParams) == 64
     assert C.sizeof(abi.RestirParams) == 64
+    assert C.sizeof(abi.BdptParams) == 64
 
 
 def test_camera_lookat_matches_oracle(lib, oracle):
@@ -89,7 +90,7 @@ def test_ctypes_layouts_match_the_header(tmp_path):
                "lgb_build_opts": abi.BuildOpts, "lgb_build_stats": abi.BuildStats, "lgb_diff_params": abi.DiffParams,
                "lgb_diff_grads": abi.DiffGrads, "lgb_batch_job": abi.BatchJob, "lgb_batch_opts": abi.BatchOpts,
                "lgb_vcm_params": abi.VcmParams, "lgb_sppm_params": abi.SppmParams,
-               "lgb_restir_params": abi.RestirParams}
+               "lgb_restir_params": abi.RestirParams, "lgb_bdpt_params": abi.BdptParams}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "lgb.h"', "int main(void) {"]
     for cname, py in mirrors.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')

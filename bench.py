@@ -464,6 +464,42 @@ def sppm_secondary(torch, ctx_cls, scene_cls, local, frames=64):
     return out
 
 
+def bdpt_secondary(torch, ctx_cls, scene_cls, local, frames=64):
+    """BDPT on the Cornell box (256^2, path length 6 as the shipped cornell_box_bdpt.json): device time per
+    lgb_bdpt_iteration over `frames` frames after one warm-up frame (per pixel one light and one camera subpath of
+    up to 7 vertices and 26 connection strategies)."""
+    from lumen_gb300 import procedural
+    from lumen_gb300.scene import bdpt_params, camera_lookat
+    cb = procedural.cornell_box()
+    ctx = ctx_cls(local)
+    sc = scene_cls(ctx, cb)
+    sc.build()
+    w = h = 256
+    depth = 6
+    cam = camera_lookat(cb.camera_pos, cb.camera_dir, cb.fov, w, h)
+    film = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    cs = stream.cuda_stream
+    sc.bdpt_iteration(cam, bdpt_params(cb, depth, 53, 0), film, stream=cs)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for f in range(1, frames + 1):
+        sc.bdpt_iteration(cam, bdpt_params(cb, depth, 53, f), film, stream=cs)
+    e1.record(stream)
+    e1.synchronize()
+    sc.sync(cs)
+    ms = e0.elapsed_time(e1) / frames
+    strategies = (depth - 1) + depth * (depth + 1) // 2
+    out = {"workload": "BDPT: Cornell box 36 triangles, 256x256, path length 6, one light and one camera subpath "
+                       "per pixel per frame, 26 connection strategies per pixel", "ms_per_frame": ms,
+           "msamples_per_s": w * h / (ms * 1e-3) / 1e6,
+           "strategies_per_s": w * h * strategies / (ms * 1e-3), "frames_timed": frames,
+           "mean_radiance": float(film[:, :3].mean())}
+    sc.close()
+    return out
+
+
 def restir_secondary(torch, ctx_cls, scene_cls, local, frames=64):
     """ReSTIR DI on the Cornell box (256^2: 2 light candidates per pixel, temporal and 5-neighbour spatial reuse,
     with the spatial sample count fixed): device time per lgb_restir_di_iteration over `frames` frames after one
@@ -644,6 +680,7 @@ def run_gpu(args):
         secondary["vcm"] = vcm_secondary(torch, Context, GpuScene, local)
         secondary["sppm"] = sppm_secondary(torch, Context, GpuScene, local)
         secondary["restir_di"] = restir_secondary(torch, Context, GpuScene, local)
+        secondary["bdpt"] = bdpt_secondary(torch, Context, GpuScene, local)
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
@@ -672,7 +709,7 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
-LEGS = ("path_tracer", "adjoint", "batched", "vcm", "sppm", "restir_di")
+LEGS = ("path_tracer", "adjoint", "batched", "vcm", "sppm", "restir_di", "bdpt")
 
 
 def run_leg(name):
@@ -690,6 +727,8 @@ def run_leg(name):
         out = sppm_secondary(torch, Context, GpuScene, local)
     elif name == "restir_di":
         out = restir_secondary(torch, Context, GpuScene, local)
+    elif name == "bdpt":
+        out = bdpt_secondary(torch, Context, GpuScene, local)
     else:
         out = vcm_secondary(torch, Context, GpuScene, local)
     print(json.dumps({"leg": name, **out}))

@@ -44,7 +44,8 @@ LGB_API lgb_status lgbh_scene_get_info(lgbh_scene* s, lgbh_scene_info* out);
 LGB_API lgb_status lgbh_write_image(const char* path, const float* rgba, uint32_t width, uint32_t height, char* err,
                                     size_t errlen);
 /* Headless render with the scene's integrator (Path; VCM with seeds from the deterministic sequence of GpuVCM,
- * light_seed / eye_seed = vcm_seeds(0, frame); SPPM and ReSTIR DI with seed = the light seed of vcm_seeds(0, frame)): init, create_accel, then `spp` frames of render/update, film
+ * light_seed / eye_seed = vcm_seeds(0, frame); SPPM, BDPT and ReSTIR DI with seed = the light seed of
+ * vcm_seeds(0, frame)): init, create_accel, then `spp` frames of render/update, film
  * written to out_pfm (OpenEXR if it ends in ".exr", else RGB PFM; skipped when null) and copied to host_rgba (width*height*4 floats; skipped when
  * null). */
 LGB_API lgb_status lgbh_render_path(const char* json_path, int device, uint32_t width, uint32_t height, uint32_t spp,

@@ -97,13 +97,14 @@ LGB_API lgb_status lgbh_render_path(const char* json_path, int device, uint32_t 
     try {
         lgbh::LumenScene scene;
         scene.load(json_path);
-        // RayTracer::init picks the integrator named in the scene (RayTracer.cpp:45-60): Path or VCM here
+        // RayTracer::init picks the integrator named in the scene (RayTracer.cpp:45-60)
         std::unique_ptr<lgbh::Integrator> integrator;
         if (scene.config.integrator == "vcm") integrator.reset(new lgbh::GpuVCM(&scene, ctx, width, height));
         else if (scene.config.integrator == "sppm") integrator.reset(new lgbh::GpuSPPM(&scene, ctx, width, height));
         else if (scene.config.integrator == "restir") integrator.reset(new lgbh::GpuReSTIR(&scene, ctx, width, height));
+        else if (scene.config.integrator == "bdpt") integrator.reset(new lgbh::GpuBDPT(&scene, ctx, width, height));
         else if (scene.config.integrator == "path") integrator.reset(new lgbh::GpuPath(&scene, ctx, width, height));
-        else throw std::runtime_error("integrator \"" + scene.config.integrator + "\" is not supported (path, vcm, sppm, restir)");
+        else throw std::runtime_error("integrator \"" + scene.config.integrator + "\" is not supported (path, vcm, sppm, restir, bdpt)");
         integrator->init();           // RayTracer::init -> integrator->init (RayTracer.cpp:61-65)
         integrator->create_accel();   // integrator->create_accel
         for (uint32_t f = 0; f < spp; f++) {  // the frame loop: render, then update (RayTracer.cpp:167-197)

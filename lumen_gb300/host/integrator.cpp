@@ -133,6 +133,32 @@ bool GpuSPPM::update() {  // SPPM::update (SPPM.cpp:186-192)
     return changed;
 }
 
+void GpuBDPT::init() {
+    Integrator::init();
+    frame_num = 0;
+    path_length = (uint32_t)lumen_scene->config.path_length;
+}
+
+void GpuBDPT::render() {  // BDPT::render (BDPT.cpp:55-88)
+    lgb_bdpt_params p{};
+    for (int i = 0; i < 3; i++) p.sky_col[i] = lumen_scene->config.sky_col[i];
+    p.max_depth = (int32_t)path_length;
+    p.num_lights = (int32_t)lumen_scene->lights.size();
+    p.light_triangle_count = (int32_t)lumen_scene->total_light_triangle_cnt;
+    p.dir_light_idx = lumen_scene->dir_light_idx;
+    uint32_t unused;
+    vcm_seeds(seed, frame_num, &p.seed, &unused);
+    p.frame_num = frame_num;
+    check(lgb_bdpt_iteration(scene, &cam, &p, output_film, stream), "lgb_bdpt_iteration");
+}
+
+bool GpuBDPT::update() {  // BDPT::update (BDPT.cpp:90-97)
+    frame_num++;
+    const bool changed = Integrator::update();
+    if (changed) frame_num = 0;
+    return changed;
+}
+
 void GpuReSTIR::init() {
     Integrator::init();
     frame_num = 0;

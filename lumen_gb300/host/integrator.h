@@ -81,6 +81,19 @@ class GpuSPPM final : public Integrator {
     void* stream = nullptr;
 };
 
+// The BDPT integrator (BDPT.cpp:55-99): one frame per render(); frame 0 again after a camera change. Lumen draws
+// each frame's RNG offset with host rand(); here it is the light seed of vcm_seeds(seed, frame_num).
+class GpuBDPT final : public Integrator {
+  public:
+    using Integrator::Integrator;
+    void init() override;
+    void render() override;
+    bool update() override;
+    uint32_t path_length = 6;
+    uint32_t seed = 0;
+    void* stream = nullptr;
+};
+
 // The ReSTIR DI integrator (ReSTIR.cpp:74-165): one frame per render(); spatiotemporal reuse is off for the
 // first frame and on afterwards (ReSTIR.cpp:154-156); the previous camera feeds the temporal reprojection test.
 class GpuReSTIR final : public Integrator {

@@ -144,6 +144,57 @@ def cpu_oracle_rate(arrays, rays, seconds=12.0, threads=None):
     return n / dt, n, threads
 
 
+def cpu_integrator_rate(kind, arrays, w, h, frames, depth, **kw):
+    """The CPU oracle's integrator `kind` ("vcm", "sppm", "restir_di", "bdpt") on `frames` frames at w x h, all
+    host cores: the cpu_baseline entry of a secondary line (pixels per second as Msamples/s)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_lib
+    from lumen_gb300.scene import camera_forward, camera_lookat, scene_radius, vcm_params, vcm_radius
+    ora = oracle_lib.Oracle()
+    osc = ora.scene(arrays)
+    cam = camera_lookat(arrays.camera_pos, arrays.camera_dir, arrays.fov, w, h)
+    view, proj = camera_forward(cam)
+    threads = os.cpu_count() or 1
+    nl, ltc, spot = len(arrays.lights), arrays.light_triangle_count, kw.get("spot_angle", 0.0)
+    if kind == "vcm":
+        st = osc.vcm_state(w, h, depth)
+        R = scene_radius(arrays)
+    elif kind == "sppm":
+        st = oracle_lib.sppm_state(w, h, depth)
+    elif kind == "restir_di":
+        st = oracle_lib.restir_state(w, h)
+    else:
+        st = oracle_lib.bdpt_state(w, h)
+    t0 = time.perf_counter()
+    for f in range(frames):
+        if kind == "vcm":
+            g = vcm_params(arrays, depth, vcm_radius(R, 1.0, f, 0.75), 1000 + f, 5000 + f, f, spot_angle=spot)
+            p = oracle_lib.VcmParams()
+            for name in ("max_depth", "num_lights", "light_triangle_count", "radius", "use_vm", "use_vc",
+                         "light_seed", "eye_seed", "frame_num", "flags", "spot_angle"):
+                setattr(p, name, getattr(g, name))
+            p.scene_min[:] = list(g.scene_min)
+            p.scene_max[:] = list(g.scene_max)
+            osc.vcm_iteration(cam, view, proj, p, st, threads)
+        elif kind == "sppm":
+            p = oracle_lib.SppmParams()
+            p.max_depth, p.num_lights, p.light_triangle_count, p.base_radius = depth, nl, ltc, kw.get("base_radius", 0.03)
+            p.seed, p.frame_num, p.spot_angle = 77, f, spot
+            oracle_lib.sppm_iteration(osc, cam, p, st, threads)
+        elif kind == "restir_di":
+            p = oracle_lib.RestirParams()
+            p.num_lights, p.light_triangle_count, p.seed, p.frame_num = nl, ltc, 91, f
+            p.do_spatiotemporal, p.enable_accumulation, p.spot_angle, p.flags = 1 if f else 0, 1, spot, kw.get("flags", 0)
+            oracle_lib.restir_iteration(osc, cam, view, proj, p, st, threads)
+        else:
+            p = oracle_lib.BdptParams()
+            p.max_depth, p.num_lights, p.light_triangle_count, p.seed, p.frame_num, p.spot_angle = depth, nl, ltc, 53, f, spot
+            oracle_lib.bdpt_iteration(osc, cam, view, proj, p, st, threads)
+    dt = time.perf_counter() - t0
+    return {"value": w * h * frames / dt / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
+            "sample": f"{frames} frames of the same scene at {w}x{h} on the CPU oracle"}
+
+
 def cornell_secondary(torch, ctx_cls, scene_cls, local, cpu_leg: bool):
     """The Cornell-box path tracer (256^2, 16 spp, depth 8): GPU Msamples/s through lgb_render_path, L2 not
     flushed (the scene is 36 triangles), and the CPU oracle on a bounded sample of the same frames."""
@@ -379,7 +430,7 @@ def traversal_secondary(torch, sc, rays, flush, stream, reps=10, warmup=3):
             "l2": "flushed with a 256 MB write before every launch"}
 
 
-def vcm_secondary(torch, ctx_cls, scene_cls, local, iters=63):
+def vcm_secondary(torch, ctx_cls, scene_cls, local, cpu_leg=False, iters=63):
     """VCM caustics configuration: dielectric torus (200k triangles) on a diffuse plane, spot light (cone
     half-angle 20 degrees, falloff from 25/30 of it), 1024^2, one light subpath and one eye subpath per pixel per
     iteration (1M each), max depth 10, merge radius 0.01 x scene radius shrinking with alpha = 0.75, 64
@@ -428,10 +479,12 @@ def vcm_secondary(torch, ctx_cls, scene_cls, local, iters=63):
            "mean_radiance": float(film[:, :3].mean()), "iterations_timed": iters,
            "rmse_256_64it_vs_oracle_1024it": rmse}
     sc.close()
+    if cpu_leg:
+        out["cpu_baseline"] = cpu_integrator_rate("vcm", arrays, 256, 256, 8, 10, spot_angle=20.0)
     return out
 
 
-def sppm_secondary(torch, ctx_cls, scene_cls, local, frames=64):
+def sppm_secondary(torch, ctx_cls, scene_cls, local, cpu_leg=False, frames=64):
     """SPPM on the Cornell box (256^2, max depth 6, base radius 0.03 as the shipped cornell_box_sppm.json):
     device time per lgb_sppm_iteration over `frames` frames after one warm-up frame (one eye path and one light
     path per pixel per frame)."""
@@ -461,10 +514,12 @@ def sppm_secondary(torch, ctx_cls, scene_cls, local, frames=64):
            "msamples_per_s": w * h / (ms * 1e-3) / 1e6, "frames_timed": frames,
            "mean_radiance": float(film[:, :3].mean())}
     sc.close()
+    if cpu_leg:
+        out["cpu_baseline"] = cpu_integrator_rate("sppm", cb, w, h, 16, 6, base_radius=0.03)
     return out
 
 
-def bdpt_secondary(torch, ctx_cls, scene_cls, local, frames=64):
+def bdpt_secondary(torch, ctx_cls, scene_cls, local, cpu_leg=False, frames=64):
     """BDPT on the Cornell box (256^2, path length 6 as the shipped cornell_box_bdpt.json): device time per
     lgb_bdpt_iteration over `frames` frames after one warm-up frame (per pixel one light and one camera subpath of
     up to 7 vertices and 26 connection strategies)."""
@@ -497,10 +552,12 @@ def bdpt_secondary(torch, ctx_cls, scene_cls, local, frames=64):
            "strategies_per_s": w * h * strategies / (ms * 1e-3), "frames_timed": frames,
            "mean_radiance": float(film[:, :3].mean())}
     sc.close()
+    if cpu_leg:
+        out["cpu_baseline"] = cpu_integrator_rate("bdpt", cb, w, h, 16, depth)
     return out
 
 
-def restir_secondary(torch, ctx_cls, scene_cls, local, frames=64):
+def restir_secondary(torch, ctx_cls, scene_cls, local, cpu_leg=False, frames=64):
     """ReSTIR DI on the Cornell box (256^2: 2 light candidates per pixel, temporal and 5-neighbour spatial reuse,
     with the spatial sample count fixed): device time per lgb_restir_di_iteration over `frames` frames after one
     warm-up frame."""
@@ -531,6 +588,8 @@ def restir_secondary(torch, ctx_cls, scene_cls, local, frames=64):
            "msamples_per_s": w * h / (ms * 1e-3) / 1e6, "frames_timed": frames,
            "mean_radiance": float(film[:, :3].mean())}
     sc.close()
+    if cpu_leg:
+        out["cpu_baseline"] = cpu_integrator_rate("restir_di", cb, w, h, 64, 6, flags=fix)
     return out
 
 
@@ -677,10 +736,11 @@ def run_gpu(args):
         secondary["path_tracer"] = cornell_secondary(torch, Context, GpuScene, local, world == 1 and not args.no_cpu_baseline)
         secondary["adjoint"] = adjoint_secondary(torch, Context, GpuScene, local)
         secondary["batched"] = batch_secondary(torch, Context, GpuScene, local)
-        secondary["vcm"] = vcm_secondary(torch, Context, GpuScene, local)
-        secondary["sppm"] = sppm_secondary(torch, Context, GpuScene, local)
-        secondary["restir_di"] = restir_secondary(torch, Context, GpuScene, local)
-        secondary["bdpt"] = bdpt_secondary(torch, Context, GpuScene, local)
+        cpu_legs = world == 1 and not args.no_cpu_baseline
+        secondary["vcm"] = vcm_secondary(torch, Context, GpuScene, local, cpu_legs)
+        secondary["sppm"] = sppm_secondary(torch, Context, GpuScene, local, cpu_legs)
+        secondary["restir_di"] = restir_secondary(torch, Context, GpuScene, local, cpu_legs)
+        secondary["bdpt"] = bdpt_secondary(torch, Context, GpuScene, local, cpu_legs)
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",

@@ -56,6 +56,7 @@ struct VcmArgs {
     const uint32_t* g_count; // 10 * screen slots
     const uint32_t* g_rep;
     float4* film;            // RGBA32F, row-major
+    uint32_t* work;          // subpath counters of the light and eye kernels (zeroed before the light kernel)
 };
 
 __device__ __forceinline__ LightSet lights_of(const VcmArgs& A) {
@@ -164,38 +165,65 @@ __device__ v3 connect_cam(const SceneView& S, const VcmArgs& A, const CamV& c, v
     return L;
 }
 
-// vcm_light.rgen main: one light subpath per launch point (x, y), stored at x * H + y.
+// Next unstarted subpath for each calling lane: one atomic per group of converged lanes.
+__device__ __forceinline__ uint32_t fetch_path(uint32_t* counter) {
+    const uint32_t mask = __activemask();
+    const int leader = __ffs(mask) - 1;
+    const int lane = (int)(threadIdx.x & 31u);
+    uint32_t first = 0;
+    if (lane == leader) first = atomicAdd(counter, (uint32_t)__popc(mask));
+    first = __shfl_sync(mask, first, leader);
+    return first + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+constexpr uint32_t kNoPath = 0xffffffffu;
+
+// vcm_light.rgen main: one light subpath per launch point (x, y), stored at x * H + y. Path regeneration: a
+// lane whose subpath ends takes the next unstarted one (work[0]), so the lanes of a warp keep tracing while
+// subpaths of very different lengths finish. A subpath's arithmetic, RNG stream and stores do not depend on
+// the lane that runs it.
 template <uint32_t MASK>
 __global__ void __launch_bounds__(kVcmThreads) k_vcm_light(SceneView S, VcmArgs A) {
     const CamV cam = cam_setup(A);
     const Etas eta = etas(A);
     const uint32_t per = (uint32_t)(A.max_depth + 1);
-    for (uint32_t li = blockIdx.x * blockDim.x + threadIdx.x; li < A.screen; li += gridDim.x * blockDim.x) {
-        const uint32_t x = li / A.H, y = li % A.H;
-        float4* lv = A.verts + (size_t)li * per * kVertexF4;
-        uint4 seed = make_uint4(x, y, A.light_seed, 0u);
-        const float r0 = rnd(seed), r1 = rnd(seed), r2 = rnd(seed), r3 = rnd(seed);
-        const float d0 = rnd(seed), d1 = rnd(seed);
-        const Emission e = sample_light_Le(S, lights_of(A), r0, r1, r2, r3, d0, d1);
-        if (e.pdf_dir_w <= 0.0f) {
-            A.counts[li] = 0u;
-            continue;
+    uint32_t li = kNoPath, path_idx = 0;
+    int depth = 0;
+    bool finite = false;
+    uint4 seed = make_uint4(0u, 0u, 0u, 0u);
+    VState st;
+    float4* lv = nullptr;
+    while (true) {
+        if (li == kNoPath) {
+            li = fetch_path(A.work);
+            if (li >= A.screen) break;
+            const uint32_t x = li / A.H, y = li % A.H;
+            lv = A.verts + (size_t)li * per * kVertexF4;
+            seed = make_uint4(x, y, A.light_seed, 0u);
+            const float r0 = rnd(seed), r1 = rnd(seed), r2 = rnd(seed), r3 = rnd(seed);
+            const float d0 = rnd(seed), d1 = rnd(seed);
+            const Emission e = sample_light_Le(S, lights_of(A), r0, r1, r2, r3, d0, d1);
+            if (e.pdf_dir_w <= 0.0f) {
+                A.counts[li] = 0u;
+                li = kNoPath;
+                continue;
+            }
+            const float pdf_emit = e.pdf_pos_a * e.pdf_dir_w;
+            st.pos = e.pos;
+            st.wi = e.wi;
+            st.thr = e.L * e.cos_from_light / (e.pdf_dir_w * e.pdf_pos_a);
+            st.d_vcm = e.pdf_pos_a / pdf_emit;
+            finite = light_finite(e.flags);
+            st.d_vc = light_delta(e.flags) ? 0.0f : (finite ? e.cos_from_light : 1.0f) / (e.pdf_dir_w * e.pdf_pos_a);
+            st.d_vm = st.d_vc * eta.vc;
+            path_idx = 0;
+            depth = 0;
         }
-        VState st;
-        const float pdf_emit = e.pdf_pos_a * e.pdf_dir_w;
-        st.pos = e.pos;
-        st.wi = e.wi;
-        st.thr = e.L * e.cos_from_light / (e.pdf_dir_w * e.pdf_pos_a);
-        st.d_vcm = e.pdf_pos_a / pdf_emit;
-        const bool finite = light_finite(e.flags);
-        st.d_vc = light_delta(e.flags) ? 0.0f : (finite ? e.cos_from_light : 1.0f) / (e.pdf_dir_w * e.pdf_pos_a);
-        st.d_vm = st.d_vc * eta.vc;
-        uint32_t path_idx = 0;
-        for (int depth = 1; depth <= A.max_depth; depth++) {
-            float t, bu, bv;
-            const RayQ q = make_rayq(st.pos.x, st.pos.y, st.pos.z, kTMinV, st.wi.x, st.wi.y, st.wi.z, kTMaxV);
-            const uint32_t prim = trace_closest_single(S.nodes, S.tris, q, t, bu, bv, S.status);
-            if (prim == LGB_NO_HIT) break;
+        depth++;
+        bool done = true;
+        float t, bu, bv;
+        const RayQ q = make_rayq(st.pos.x, st.pos.y, st.pos.z, kTMinV, st.wi.x, st.wi.y, st.wi.z, kTMaxV);
+        const uint32_t prim = trace_closest_single(S.nodes, S.tris, q, t, bu, bv, S.status);
+        if (prim != LGB_NO_HIT) {
             const HitAttr h = resolve_hit(S, prim, bu, bv);
             v3 wo = st.pos - h.pos;
             v3 n_s = h.n_s, n_g = h.n_g;
@@ -220,41 +248,47 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_light(SceneView S, VcmArgs 
                 store_lvert(lv + (size_t)path_idx * kVertexF4, v);
                 path_idx++;
             }
-            if (depth >= A.max_depth) break;
-            if (!spec && A.use_vc == 1) {
-                uint32_t pidx = 0;
-                bool have = false;
-                const v3 L = connect_cam<MASK>(S, A, cam, n_s, h.n_s, h.pos, st, eta.vm, wo, mat, pidx, have);
-                if (luminance(L) > 0.0f && have) {
-                    atomicAdd(&A.splat[3 * pidx], L.x);
-                    atomicAdd(&A.splat[3 * pidx + 1], L.y);
-                    atomicAdd(&A.splat[3 * pidx + 2], L.z);
+            if (depth < A.max_depth) {
+                if (!spec && A.use_vc == 1) {
+                    uint32_t pidx = 0;
+                    bool have = false;
+                    const v3 L = connect_cam<MASK>(S, A, cam, n_s, h.n_s, h.pos, st, eta.vm, wo, mat, pidx, have);
+                    if (luminance(L) > 0.0f && have) {
+                        atomicAdd(&A.splat[3 * pidx], L.x);
+                        atomicAdd(&A.splat[3 * pidx + 1], L.y);
+                        atomicAdd(&A.splat[3 * pidx + 2], L.z);
+                    }
+                }
+                const float c0 = rnd(seed), c1 = rnd(seed), c2 = rnd(seed);
+                float pdf_dir, cos_t;
+                v3 wi;
+                const v3 f = sample_bsdf_mode<MASK>(n_s, wo, mat, 0u, side, wi, pdf_dir, cos_t, V3(c0, c1, c2));
+                st.wi = wi;
+                const bool same = dot(st.wi, n_s) > 0.0f && dot(wo, n_s) > 0.0f;
+                const bool trans = (mat.props & LGB_FLAG_TRANSMISSION) == LGB_FLAG_TRANSMISSION;
+                if (!(is_zero3(f) || pdf_dir == 0.0f || (!same && !trans))) {
+                    float pdf_rev = pdf_dir;
+                    if (!spec) pdf_rev = bsdf_pdf<MASK>(mat, n_s, st.wi, wo, side);
+                    const float ac = fabsf(cos_t);
+                    st.pos = offset_ray(h.pos, n_g);
+                    if (!spec) {
+                        st.d_vc = (ac / pdf_dir) * (eta.vm + st.d_vcm + pdf_rev * st.d_vc);
+                        st.d_vm = (ac / pdf_dir) * (1.0f + st.d_vcm * eta.vc + pdf_rev * st.d_vm);
+                        st.d_vcm = 1.0f / pdf_dir;
+                    } else {
+                        st.d_vcm = 0.0f;
+                        st.d_vc *= ac;
+                        st.d_vm *= ac;
+                    }
+                    st.thr = st.thr * (f * ac / pdf_dir);
+                    done = false;
                 }
             }
-            const float c0 = rnd(seed), c1 = rnd(seed), c2 = rnd(seed);
-            float pdf_dir, cos_t;
-            v3 wi;
-            const v3 f = sample_bsdf_mode<MASK>(n_s, wo, mat, 0u, side, wi, pdf_dir, cos_t, V3(c0, c1, c2));
-            st.wi = wi;
-            const bool same = dot(st.wi, n_s) > 0.0f && dot(wo, n_s) > 0.0f;
-            const bool trans = (mat.props & LGB_FLAG_TRANSMISSION) == LGB_FLAG_TRANSMISSION;
-            if (is_zero3(f) || pdf_dir == 0.0f || (!same && !trans)) break;
-            float pdf_rev = pdf_dir;
-            if (!spec) pdf_rev = bsdf_pdf<MASK>(mat, n_s, st.wi, wo, side);
-            const float ac = fabsf(cos_t);
-            st.pos = offset_ray(h.pos, n_g);
-            if (!spec) {
-                st.d_vc = (ac / pdf_dir) * (eta.vm + st.d_vcm + pdf_rev * st.d_vc);
-                st.d_vm = (ac / pdf_dir) * (1.0f + st.d_vcm * eta.vc + pdf_rev * st.d_vm);
-                st.d_vcm = 1.0f / pdf_dir;
-            } else {
-                st.d_vcm = 0.0f;
-                st.d_vc *= ac;
-                st.d_vm *= ac;
-            }
-            st.thr = st.thr * (f * ac / pdf_dir);
         }
-        A.counts[li] = path_idx;
+        if (done) {
+            A.counts[li] = path_idx;
+            li = kNoPath;
+        }
     }
 }
 
@@ -365,43 +399,54 @@ __device__ v3 merge(const VcmArgs& A, int depth, const EyeHit& h, v3 n_s, v3 wo,
     return res;
 }
 
-// vcm_eye.rgen main + vcm_trace_eye for pixel (x, y): film[y * W + x], consumes the pixel's splat.
+// vcm_eye.rgen main + vcm_trace_eye for pixel (x, y): film[y * W + x], consumes the pixel's splat. Path
+// regeneration as in k_vcm_light (work[1]): a lane whose eye subpath ends writes its pixel and takes the next.
 template <uint32_t MASK>
 __global__ void __launch_bounds__(kVcmThreads) k_vcm_eye(SceneView S, VcmArgs A) {
     const CamV cam = cam_setup(A);
     const Etas eta = etas(A);
     const float norm = 1.0f / (LGB_PI * A.radius * A.radius * (float)A.screen);
     const uint32_t per = (uint32_t)(A.max_depth + 1);
-    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < A.screen; pix += gridDim.x * blockDim.x) {
-        const uint32_t x = pix % A.W, y = pix / A.W;
-        uint4 seed = make_uint4(x, y, A.eye_seed, 0u);
-        const float j0 = rnd(seed), j1 = rnd(seed);
-        const float u = ((float)x + 0.5f + (j0 - 0.5f)) / (float)A.W, v = ((float)y + 0.5f + (j1 - 0.5f)) / (float)A.H;
-        const float dx = u * 2.0f - 1.0f, dy = v * 2.0f - 1.0f;
-        const float4 t4 = mat_vec(A.ip, dx, dy, 1.0f, 1.0f);
-        const v3 tn = normalize(V3(t4.x, t4.y, t4.z));
-        const float4 d4 = mat_vec(A.iv, tn.x, tn.y, tn.z, 0.0f);
-        VState cs;
-        cs.wi = V3(d4.x, d4.y, d4.z);
-        cs.pos = cam.pos;
-        cs.thr = V3(1.0f);
-        const float ct0 = fabsf(dot(cam.nrm, cs.wi));
-        cs.d_vcm = cam.area * (float)A.screen * ct0 * ct0 * ct0;
-        cs.d_vc = 0.0f;
-        cs.d_vm = 0.0f;
-        // uint(rand * screen) (vcm_commons.glsl:518) can round up to screen for large images: clamped
-        const uint32_t lp = min((uint32_t)(rnd(seed) * (float)A.screen), A.screen - 1u);
-        const uint32_t lp_len = A.counts[lp];
-        const float4* lv = A.verts + (size_t)lp * per * kVertexF4;
-        v3 col = V3(0.0f);
-        for (int depth = 1; depth <= A.max_depth; depth++) {
-            float t, bu, bv;
-            const RayQ q = make_rayq(cs.pos.x, cs.pos.y, cs.pos.z, kTMinV, cs.wi.x, cs.wi.y, cs.wi.z, kTMaxV);
-            const uint32_t prim = trace_closest_single(S.nodes, S.tris, q, t, bu, bv, S.status);
-            if (prim == LGB_NO_HIT) {
-                col = col + cs.thr * V3(A.sky[0], A.sky[1], A.sky[2]);
-                break;
-            }
+    uint32_t pix = kNoPath, lp_len = 0;
+    int depth = 0;
+    uint4 seed = make_uint4(0u, 0u, 0u, 0u);
+    VState cs;
+    v3 col = V3(0.0f);
+    const float4* lv = nullptr;
+    while (true) {
+        if (pix == kNoPath) {
+            pix = fetch_path(A.work + 1);
+            if (pix >= A.screen) break;
+            const uint32_t x = pix % A.W, y = pix / A.W;
+            seed = make_uint4(x, y, A.eye_seed, 0u);
+            const float j0 = rnd(seed), j1 = rnd(seed);
+            const float u = ((float)x + 0.5f + (j0 - 0.5f)) / (float)A.W, v = ((float)y + 0.5f + (j1 - 0.5f)) / (float)A.H;
+            const float dx = u * 2.0f - 1.0f, dy = v * 2.0f - 1.0f;
+            const float4 t4 = mat_vec(A.ip, dx, dy, 1.0f, 1.0f);
+            const v3 tn = normalize(V3(t4.x, t4.y, t4.z));
+            const float4 d4 = mat_vec(A.iv, tn.x, tn.y, tn.z, 0.0f);
+            cs.wi = V3(d4.x, d4.y, d4.z);
+            cs.pos = cam.pos;
+            cs.thr = V3(1.0f);
+            const float ct0 = fabsf(dot(cam.nrm, cs.wi));
+            cs.d_vcm = cam.area * (float)A.screen * ct0 * ct0 * ct0;
+            cs.d_vc = 0.0f;
+            cs.d_vm = 0.0f;
+            // uint(rand * screen) (vcm_commons.glsl:518) can round up to screen for large images: clamped
+            const uint32_t lp = min((uint32_t)(rnd(seed) * (float)A.screen), A.screen - 1u);
+            lp_len = A.counts[lp];
+            lv = A.verts + (size_t)lp * per * kVertexF4;
+            col = V3(0.0f);
+            depth = 0;
+        }
+        depth++;
+        bool done = true;
+        float t, bu, bv;
+        const RayQ q = make_rayq(cs.pos.x, cs.pos.y, cs.pos.z, kTMinV, cs.wi.x, cs.wi.y, cs.wi.z, kTMaxV);
+        const uint32_t prim = trace_closest_single(S.nodes, S.tris, q, t, bu, bv, S.status);
+        if (prim == LGB_NO_HIT) {
+            col = col + cs.thr * V3(A.sky[0], A.sky[1], A.sky[2]);
+        } else {
             const HitAttr h = resolve_hit(S, prim, bu, bv);
             v3 wo = cs.pos - h.pos;
             const float dist = length(h.pos - cs.pos);
@@ -434,44 +479,50 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_eye(SceneView S, VcmArgs A)
             if (!spec && depth < A.max_depth) col = col + connect_light<MASK>(S, A, seed, eh, n_s, wo, mat, side, eta.vm, cs, pdf_rev);
             if (!spec) col = col + connect_light_vertices<MASK>(S, A, lv, lp_len, depth, eh, n_s, wo, mat, side, eta.vm, cs, pdf_rev);
             if (!spec && A.use_vm == 1) col = col + merge<MASK>(A, depth, eh, n_s, wo, mat, side, eta.vc, cs, norm);
-            if (depth >= A.max_depth) break;
-            const float c0 = rnd(seed), c1 = rnd(seed), c2 = rnd(seed);
-            float pdf_dir, cos_t;
-            v3 wi;
-            const v3 f = sample_bsdf_mode<MASK>(n_s, wo, mat, 1u, side, wi, pdf_dir, cos_t, V3(c0, c1, c2));
-            cs.wi = wi;
-            const bool trans = (mat.props & LGB_FLAG_TRANSMISSION) == LGB_FLAG_TRANSMISSION;
-            const bool same = dot(cs.wi, n_s) > 0.0f && dot(wo, n_s) > 0.0f;
-            if (is_zero3(f) || pdf_dir == 0.0f || (!same && !trans)) break;
-            pdf_rev = pdf_dir;
-            if (!spec) pdf_rev = bsdf_pdf<MASK>(mat, n_s, cs.wi, wo, side);
-            const float ac = fabsf(cos_t);
-            cs.pos = offset_ray(h.pos, n_g);
-            if (!spec) {
-                cs.d_vc = (ac / pdf_dir) * (eta.vm + cs.d_vcm + pdf_rev * cs.d_vc);
-                cs.d_vm = (ac / pdf_dir) * (1.0f + cs.d_vcm * eta.vc + pdf_rev * cs.d_vm);
-                cs.d_vcm = 1.0f / pdf_dir;
-            } else {
-                cs.d_vcm = 0.0f;
-                cs.d_vc *= ac;
-                cs.d_vm *= ac;
+            if (depth < A.max_depth) {
+                const float c0 = rnd(seed), c1 = rnd(seed), c2 = rnd(seed);
+                float pdf_dir, cos_t;
+                v3 wi;
+                const v3 f = sample_bsdf_mode<MASK>(n_s, wo, mat, 1u, side, wi, pdf_dir, cos_t, V3(c0, c1, c2));
+                cs.wi = wi;
+                const bool trans = (mat.props & LGB_FLAG_TRANSMISSION) == LGB_FLAG_TRANSMISSION;
+                const bool same = dot(cs.wi, n_s) > 0.0f && dot(wo, n_s) > 0.0f;
+                if (!(is_zero3(f) || pdf_dir == 0.0f || (!same && !trans))) {
+                    pdf_rev = pdf_dir;
+                    if (!spec) pdf_rev = bsdf_pdf<MASK>(mat, n_s, cs.wi, wo, side);
+                    const float ac = fabsf(cos_t);
+                    cs.pos = offset_ray(h.pos, n_g);
+                    if (!spec) {
+                        cs.d_vc = (ac / pdf_dir) * (eta.vm + cs.d_vcm + pdf_rev * cs.d_vc);
+                        cs.d_vm = (ac / pdf_dir) * (1.0f + cs.d_vcm * eta.vc + pdf_rev * cs.d_vm);
+                        cs.d_vcm = 1.0f / pdf_dir;
+                    } else {
+                        cs.d_vcm = 0.0f;
+                        cs.d_vc *= ac;
+                        cs.d_vm *= ac;
+                    }
+                    cs.thr = cs.thr * (f * ac / pdf_dir);
+                    done = false;
+                }
             }
-            cs.thr = cs.thr * (f * ac / pdf_dir);
         }
+        if (!done) continue;
+        const uint32_t x = pix % A.W, y = pix / A.W, fp = pix;
+        pix = kNoPath;
         if (isnan(luminance(col))) continue;  // vcm_eye.rgen:80-83: no film write, the splat stays
         const uint32_t sidx = x * A.H + y;
         col = col + V3(A.splat[3 * sidx], A.splat[3 * sidx + 1], A.splat[3 * sidx + 2]);
         A.splat[3 * sidx] = 0.0f;
         A.splat[3 * sidx + 1] = 0.0f;
         A.splat[3 * sidx + 2] = 0.0f;
-        float4 px = A.film[pix];
+        float4 px = A.film[fp];
         if (A.frame_num > 0u) {
             const float w = 1.0f / (float)(A.frame_num + 1u);
             px = make_float4(mixf(px.x, col.x, w), mixf(px.y, col.y, w), mixf(px.z, col.z, w), 1.0f);
         } else {
             px = make_float4(col.x, col.y, col.z, 1.0f);
         }
-        A.film[pix] = px;
+        A.film[fp] = px;
     }
 }
 
@@ -620,7 +671,8 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
     auto take = [&](size_t bytes) { const size_t o = off; off += align256(bytes); return o; };
     const size_t o_verts = take(sizeof(float4) * kVertexF4 * (size_t)nv), o_counts = take(4ull * screen),
                  o_splat = take(12ull * screen), o_gc = take(4ull * table), o_gr = take(4ull * table), o_k0 = take(8ull * nv),
-                 o_k1 = take(8ull * nv), o_v0 = take(4ull * nv), o_v1 = take(4ull * nv), o_sc = take(4ull * radix_sort_scratch_words(nv));
+                 o_k1 = take(8ull * nv), o_v0 = take(4ull * nv), o_v1 = take(4ull * nv), o_sc = take(4ull * radix_sort_scratch_words(nv)),
+                 o_work = take(8);
     if (!s->vcm_buf || s->vcm_w != cam->width || s->vcm_h != cam->height || s->vcm_per != per || s->vcm_buf_bytes < off) {
         cudaFree(s->vcm_buf);
         s->vcm_buf = nullptr;
@@ -652,16 +704,27 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
     A.g_count = gc;
     A.g_rep = gr;
     A.film = reinterpret_cast<float4*>(d_film);
+    A.work = reinterpret_cast<uint32_t*>(base + o_work);
+    LGB_CUDA_TRY(ctx, cudaMemsetAsync(A.work, 0, 8, st));
     const SceneView S = scene_view(s);
     const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
-    const int grid = (int)std::min<uint32_t>((screen + kVcmThreads - 1) / kVcmThreads, (uint32_t)sms * 16u);
-    // The subpath kernels are instantiated per set of BSDF types (the caustics scene needs only diffuse and
+    // The subpath kernels regenerate paths, so their grids are what the SMs hold at once (at most one block per
+    // 128 subpaths). They are instantiated per set of BSDF types (the caustics scene needs only diffuse and
     // dielectric lobes): fewer inlined lobes keep their loops inside the instruction cache.
+    const uint32_t blocks_needed = (screen + kVcmThreads - 1) / kVcmThreads;
+    auto resident = [&](const void* kernel) {
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kVcmThreads, 0) != cudaSuccess || nb < 1) nb = 1;
+        return (int)std::min<uint32_t>(blocks_needed, (uint32_t)nb * (uint32_t)sms);
+    };
     const uint32_t used = s->bsdf_mask;
     const uint32_t lobes = (used & ~kVcmLobesDG) == 0u ? kVcmLobesDG : ((used & ~kVcmLobesDGC) == 0u ? kVcmLobesDGC : kAllBsdfs);
-    if (lobes == kVcmLobesDG) k_vcm_light<kVcmLobesDG><<<grid, kVcmThreads, 0, st>>>(S, A);
-    else if (lobes == kVcmLobesDGC) k_vcm_light<kVcmLobesDGC><<<grid, kVcmThreads, 0, st>>>(S, A);
-    else k_vcm_light<kAllBsdfs><<<grid, kVcmThreads, 0, st>>>(S, A);
+    if (lobes == kVcmLobesDG)
+        k_vcm_light<kVcmLobesDG><<<resident((const void*)k_vcm_light<kVcmLobesDG>), kVcmThreads, 0, st>>>(S, A);
+    else if (lobes == kVcmLobesDGC)
+        k_vcm_light<kVcmLobesDGC><<<resident((const void*)k_vcm_light<kVcmLobesDGC>), kVcmThreads, 0, st>>>(S, A);
+    else
+        k_vcm_light<kAllBsdfs><<<resident((const void*)k_vcm_light<kAllBsdfs>), kVcmThreads, 0, st>>>(S, A);
     LGB_CUDA_TRY(ctx, cudaGetLastError());
     if (p->use_vm == 1) {
         uint64_t* k0 = reinterpret_cast<uint64_t*>(base + o_k0);
@@ -675,9 +738,12 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
     } else {
         LGB_CUDA_TRY(ctx, cudaMemsetAsync(gc, 0, 4ull * table, st));
     }
-    if (lobes == kVcmLobesDG) k_vcm_eye<kVcmLobesDG><<<grid, kVcmThreads, 0, st>>>(S, A);
-    else if (lobes == kVcmLobesDGC) k_vcm_eye<kVcmLobesDGC><<<grid, kVcmThreads, 0, st>>>(S, A);
-    else k_vcm_eye<kAllBsdfs><<<grid, kVcmThreads, 0, st>>>(S, A);
+    if (lobes == kVcmLobesDG)
+        k_vcm_eye<kVcmLobesDG><<<resident((const void*)k_vcm_eye<kVcmLobesDG>), kVcmThreads, 0, st>>>(S, A);
+    else if (lobes == kVcmLobesDGC)
+        k_vcm_eye<kVcmLobesDGC><<<resident((const void*)k_vcm_eye<kVcmLobesDGC>), kVcmThreads, 0, st>>>(S, A);
+    else
+        k_vcm_eye<kAllBsdfs><<<resident((const void*)k_vcm_eye<kAllBsdfs>), kVcmThreads, 0, st>>>(S, A);
     LGB_CUDA_TRY(ctx, cudaGetLastError());
     return LGB_OK;
 }

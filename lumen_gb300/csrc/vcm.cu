@@ -56,7 +56,6 @@ struct VcmArgs {
     const uint32_t* g_count; // 10 * screen slots
     const uint32_t* g_rep;
     float4* film;            // RGBA32F, row-major
-    uint32_t* work;          // subpath counters of the light and eye kernels (zeroed before the light kernel)
 };
 
 __device__ __forceinline__ LightSet lights_of(const VcmArgs& A) {
@@ -165,8 +164,24 @@ __device__ v3 connect_cam(const SceneView& S, const VcmArgs& A, const CamV& c, v
     return L;
 }
 
-// Next unstarted subpath for each calling lane: one atomic per group of converged lanes.
-__device__ __forceinline__ uint32_t fetch_path(uint32_t* counter) {
+// Wavefront form of the subpath loops: per bounce, the closest hits of a queue of rays come from the persistent
+// traversal kernel (lanes whose ray is done fetch the next one), then a step kernel runs one iteration of the
+// reference's loop body per queued path and appends the paths that continue, with their next rays, to the next
+// queue. Path state lives in path-indexed SoA buffers, with the RNG counter, so a path's arithmetic and random
+// numbers are the loop's; only the order of the camera splats' atomics changes.
+struct Wave {
+    float4* ls;        // light path state, 4 float4 per path: (pos, d_vcm) (wi, d_vc) (thr, d_vm) (rng, stored, finite, -)
+    float4* es;        // eye path state, 5 float4 per pixel: the same three, (col, rng), (lp, lp_len, -, -)
+    lgb_ray* rays[2];  // ray queues of consecutive bounces
+    uint32_t* qidx[2]; // path of each queued ray
+    lgb_hit* hits;
+    uint32_t* qcount;  // [2 * (max_depth + 1)]: queue lengths per bounce, light pass then eye pass
+    uint32_t* tcount;  // [2 * (max_depth + 1)]: fetch counters of the traversal launches
+};
+__device__ __forceinline__ float4* sq(float4* b, int c, uint32_t screen, uint32_t i) { return b + ((size_t)c * screen + i); }
+
+// One slot of a queue for each calling lane: one atomic per group of converged lanes.
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter) {
     const uint32_t mask = __activemask();
     const int leader = __ffs(mask) - 1;
     const int lane = (int)(threadIdx.x & 31u);
@@ -175,56 +190,77 @@ __device__ __forceinline__ uint32_t fetch_path(uint32_t* counter) {
     first = __shfl_sync(mask, first, leader);
     return first + (uint32_t)__popc(mask & ((1u << lane) - 1u));
 }
-constexpr uint32_t kNoPath = 0xffffffffu;
+__device__ __forceinline__ void push_ray(const Wave& W, int q, uint32_t* counter, uint32_t path, v3 o, float tmin, v3 d,
+                                         float tmax) {
+    const uint32_t j = warp_append(counter);
+    W.qidx[q][j] = path;
+    float4* r = reinterpret_cast<float4*>(&W.rays[q][j]);
+    r[0] = make_float4(o.x, o.y, o.z, tmin);
+    r[1] = make_float4(d.x, d.y, d.z, tmax);
+}
 
-// vcm_light.rgen main: one light subpath per launch point (x, y), stored at x * H + y. Path regeneration: a
-// lane whose subpath ends takes the next unstarted one (work[0]), so the lanes of a warp keep tracing while
-// subpaths of very different lengths finish. A subpath's arithmetic, RNG stream and stores do not depend on
-// the lane that runs it.
+constexpr int kWaveTraceMinBlocks = 9;
+constexpr int kWaveRefill = 16;
+__global__ void __launch_bounds__(kVcmThreads, kWaveTraceMinBlocks)
+    k_vcm_trace(SceneView S, const lgb_ray* __restrict__ rays, lgb_hit* __restrict__ hits, const uint32_t* count,
+                uint32_t* fetch) {
+    trace_persistent<false, false, false, 0, kVcmThreads, kWaveRefill>(S.nodes, S.tris, rays, hits, nullptr, 0u, count,
+                                                                     fetch, S.status, nullptr, nullptr, nullptr);
+}
+
+// vcm_light.rgen main and vcm_generate_light_sample: one light subpath per launch point (x, y), path x * H + y;
+// its first ray goes to queue 0.
+__global__ void __launch_bounds__(kVcmThreads) k_vcm_light_init(SceneView S, VcmArgs A, Wave W) {
+    const Etas eta = etas(A);
+    for (uint32_t li = blockIdx.x * blockDim.x + threadIdx.x; li < A.screen; li += gridDim.x * blockDim.x) {
+        const uint32_t x = li / A.H, y = li % A.H;
+        uint4 seed = make_uint4(x, y, A.light_seed, 0u);
+        const float r0 = rnd(seed), r1 = rnd(seed), r2 = rnd(seed), r3 = rnd(seed);
+        const float d0 = rnd(seed), d1 = rnd(seed);
+        const Emission e = sample_light_Le(S, lights_of(A), r0, r1, r2, r3, d0, d1);
+        if (e.pdf_dir_w <= 0.0f) {
+            A.counts[li] = 0u;
+            continue;
+        }
+        const float pdf_emit = e.pdf_pos_a * e.pdf_dir_w;
+        const v3 thr = e.L * e.cos_from_light / (e.pdf_dir_w * e.pdf_pos_a);
+        const float d_vcm = e.pdf_pos_a / pdf_emit;
+        const bool finite = light_finite(e.flags);
+        const float d_vc = light_delta(e.flags) ? 0.0f : (finite ? e.cos_from_light : 1.0f) / (e.pdf_dir_w * e.pdf_pos_a);
+        const float d_vm = d_vc * eta.vc;
+        *sq(W.ls, 0, A.screen, li) = f4(e.pos, d_vcm);
+        *sq(W.ls, 1, A.screen, li) = f4(e.wi, d_vc);
+        *sq(W.ls, 2, A.screen, li) = f4(thr, d_vm);
+        *sq(W.ls, 3, A.screen, li) = make_float4(__uint_as_float(seed.w), __uint_as_float(0u), __uint_as_float(finite ? 1u : 0u), 0.0f);
+        push_ray(W, 0, W.qcount, li, e.pos, kTMinV, e.wi, kTMaxV);
+    }
+}
+
+// vcm_fill_light, one bounce (depth) of the queued light subpaths: vertex store, camera connection, the next
+// direction; a subpath that ends writes its vertex count.
 template <uint32_t MASK>
-__global__ void __launch_bounds__(kVcmThreads) k_vcm_light(SceneView S, VcmArgs A) {
+__global__ void __launch_bounds__(kVcmThreads) k_vcm_light_step(SceneView S, VcmArgs A, Wave W, int depth) {
     const CamV cam = cam_setup(A);
     const Etas eta = etas(A);
     const uint32_t per = (uint32_t)(A.max_depth + 1);
-    uint32_t li = kNoPath, path_idx = 0;
-    int depth = 0;
-    bool finite = false;
-    uint4 seed = make_uint4(0u, 0u, 0u, 0u);
-    VState st;
-    float4* lv = nullptr;
-    while (true) {
-        if (li == kNoPath) {
-            li = fetch_path(A.work);
-            if (li >= A.screen) break;
-            const uint32_t x = li / A.H, y = li % A.H;
-            lv = A.verts + (size_t)li * per * kVertexF4;
-            seed = make_uint4(x, y, A.light_seed, 0u);
-            const float r0 = rnd(seed), r1 = rnd(seed), r2 = rnd(seed), r3 = rnd(seed);
-            const float d0 = rnd(seed), d1 = rnd(seed);
-            const Emission e = sample_light_Le(S, lights_of(A), r0, r1, r2, r3, d0, d1);
-            if (e.pdf_dir_w <= 0.0f) {
-                A.counts[li] = 0u;
-                li = kNoPath;
-                continue;
-            }
-            const float pdf_emit = e.pdf_pos_a * e.pdf_dir_w;
-            st.pos = e.pos;
-            st.wi = e.wi;
-            st.thr = e.L * e.cos_from_light / (e.pdf_dir_w * e.pdf_pos_a);
-            st.d_vcm = e.pdf_pos_a / pdf_emit;
-            finite = light_finite(e.flags);
-            st.d_vc = light_delta(e.flags) ? 0.0f : (finite ? e.cos_from_light : 1.0f) / (e.pdf_dir_w * e.pdf_pos_a);
-            st.d_vm = st.d_vc * eta.vc;
-            path_idx = 0;
-            depth = 0;
-        }
-        depth++;
+    const int cur = (depth - 1) & 1;
+    const uint32_t n = W.qcount[depth - 1];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t li = W.qidx[cur][i];
+        const lgb_hit hit = W.hits[i];
+        const float4 s0 = *sq(W.ls, 0, A.screen, li), s1 = *sq(W.ls, 1, A.screen, li), s2 = *sq(W.ls, 2, A.screen, li),
+                     s3 = *sq(W.ls, 3, A.screen, li);
+        VState st;
+        st.pos = V3(s0.x, s0.y, s0.z); st.d_vcm = s0.w;
+        st.wi = V3(s1.x, s1.y, s1.z); st.d_vc = s1.w;
+        st.thr = V3(s2.x, s2.y, s2.z); st.d_vm = s2.w;
+        uint4 seed = make_uint4(li / A.H, li % A.H, A.light_seed, __float_as_uint(s3.x));
+        uint32_t path_idx = __float_as_uint(s3.y);
+        const bool finite = __float_as_uint(s3.z) != 0u;
+        float4* lv = A.verts + (size_t)li * per * kVertexF4;
         bool done = true;
-        float t, bu, bv;
-        const RayQ q = make_rayq(st.pos.x, st.pos.y, st.pos.z, kTMinV, st.wi.x, st.wi.y, st.wi.z, kTMaxV);
-        const uint32_t prim = trace_closest_single(S.nodes, S.tris, q, t, bu, bv, S.status);
-        if (prim != LGB_NO_HIT) {
-            const HitAttr h = resolve_hit(S, prim, bu, bv);
+        if (hit.prim != LGB_NO_HIT) {
+            const HitAttr h = resolve_hit(S, hit.prim, hit.u, hit.v);
             v3 wo = st.pos - h.pos;
             v3 n_s = h.n_s, n_g = h.n_g;
             bool side = true;
@@ -287,7 +323,12 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_light(SceneView S, VcmArgs 
         }
         if (done) {
             A.counts[li] = path_idx;
-            li = kNoPath;
+        } else {
+            *sq(W.ls, 0, A.screen, li) = f4(st.pos, st.d_vcm);
+            *sq(W.ls, 1, A.screen, li) = f4(st.wi, st.d_vc);
+            *sq(W.ls, 2, A.screen, li) = f4(st.thr, st.d_vm);
+            *sq(W.ls, 3, A.screen, li) = make_float4(__uint_as_float(seed.w), __uint_as_float(path_idx), s3.z, 0.0f);
+            push_ray(W, depth & 1, W.qcount + depth, li, st.pos, kTMinV, st.wi, kTMaxV);
         }
     }
 }
@@ -399,55 +440,63 @@ __device__ v3 merge(const VcmArgs& A, int depth, const EyeHit& h, v3 n_s, v3 wo,
     return res;
 }
 
-// vcm_eye.rgen main + vcm_trace_eye for pixel (x, y): film[y * W + x], consumes the pixel's splat. Path
-// regeneration as in k_vcm_light (work[1]): a lane whose eye subpath ends writes its pixel and takes the next.
-template <uint32_t MASK>
-__global__ void __launch_bounds__(kVcmThreads) k_vcm_eye(SceneView S, VcmArgs A) {
+// vcm_eye.rgen main: the camera ray of pixel (x, y) (path y * W + x), the random light subpath it connects to
+// (vcm_commons.glsl:518) and its first ray in queue 0 of the eye pass.
+__global__ void __launch_bounds__(kVcmThreads) k_vcm_eye_init(VcmArgs A, Wave W) {
     const CamV cam = cam_setup(A);
+    uint32_t* const qc = W.qcount + (A.max_depth + 1);
+    for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < A.screen; pix += gridDim.x * blockDim.x) {
+        const uint32_t x = pix % A.W, y = pix / A.W;
+        uint4 seed = make_uint4(x, y, A.eye_seed, 0u);
+        const float j0 = rnd(seed), j1 = rnd(seed);
+        const float u = ((float)x + 0.5f + (j0 - 0.5f)) / (float)A.W, v = ((float)y + 0.5f + (j1 - 0.5f)) / (float)A.H;
+        const float dx = u * 2.0f - 1.0f, dy = v * 2.0f - 1.0f;
+        const float4 t4 = mat_vec(A.ip, dx, dy, 1.0f, 1.0f);
+        const v3 tn = normalize(V3(t4.x, t4.y, t4.z));
+        const float4 d4 = mat_vec(A.iv, tn.x, tn.y, tn.z, 0.0f);
+        const v3 wi = V3(d4.x, d4.y, d4.z);
+        const float ct0 = fabsf(dot(cam.nrm, wi));
+        const float d_vcm = cam.area * (float)A.screen * ct0 * ct0 * ct0;
+        // uint(rand * screen) can round up to screen for large images: clamped
+        const uint32_t lp = min((uint32_t)(rnd(seed) * (float)A.screen), A.screen - 1u);
+        *sq(W.es, 0, A.screen, pix) = f4(cam.pos, d_vcm);
+        *sq(W.es, 1, A.screen, pix) = f4(wi, 0.0f);
+        *sq(W.es, 2, A.screen, pix) = f4(V3(1.0f), 0.0f);
+        *sq(W.es, 3, A.screen, pix) = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(seed.w));
+        *sq(W.es, 4, A.screen, pix) = make_float4(__uint_as_float(lp), __uint_as_float(A.counts[lp]), 0.0f, 0.0f);
+        push_ray(W, 0, qc, pix, cam.pos, kTMinV, wi, kTMaxV);
+    }
+}
+
+// vcm_trace_eye, one bounce (depth) of the queued eye subpaths: emission, light connection, connections to the
+// light subpath's vertices, merging, the next direction; a subpath that ends writes its pixel (vcm_eye.rgen:80-97).
+template <uint32_t MASK>
+__global__ void __launch_bounds__(kVcmThreads) k_vcm_eye_step(SceneView S, VcmArgs A, Wave W, int depth) {
     const Etas eta = etas(A);
     const float norm = 1.0f / (LGB_PI * A.radius * A.radius * (float)A.screen);
     const uint32_t per = (uint32_t)(A.max_depth + 1);
-    uint32_t pix = kNoPath, lp_len = 0;
-    int depth = 0;
-    uint4 seed = make_uint4(0u, 0u, 0u, 0u);
-    VState cs;
-    v3 col = V3(0.0f);
-    const float4* lv = nullptr;
-    while (true) {
-        if (pix == kNoPath) {
-            pix = fetch_path(A.work + 1);
-            if (pix >= A.screen) break;
-            const uint32_t x = pix % A.W, y = pix / A.W;
-            seed = make_uint4(x, y, A.eye_seed, 0u);
-            const float j0 = rnd(seed), j1 = rnd(seed);
-            const float u = ((float)x + 0.5f + (j0 - 0.5f)) / (float)A.W, v = ((float)y + 0.5f + (j1 - 0.5f)) / (float)A.H;
-            const float dx = u * 2.0f - 1.0f, dy = v * 2.0f - 1.0f;
-            const float4 t4 = mat_vec(A.ip, dx, dy, 1.0f, 1.0f);
-            const v3 tn = normalize(V3(t4.x, t4.y, t4.z));
-            const float4 d4 = mat_vec(A.iv, tn.x, tn.y, tn.z, 0.0f);
-            cs.wi = V3(d4.x, d4.y, d4.z);
-            cs.pos = cam.pos;
-            cs.thr = V3(1.0f);
-            const float ct0 = fabsf(dot(cam.nrm, cs.wi));
-            cs.d_vcm = cam.area * (float)A.screen * ct0 * ct0 * ct0;
-            cs.d_vc = 0.0f;
-            cs.d_vm = 0.0f;
-            // uint(rand * screen) (vcm_commons.glsl:518) can round up to screen for large images: clamped
-            const uint32_t lp = min((uint32_t)(rnd(seed) * (float)A.screen), A.screen - 1u);
-            lp_len = A.counts[lp];
-            lv = A.verts + (size_t)lp * per * kVertexF4;
-            col = V3(0.0f);
-            depth = 0;
-        }
-        depth++;
+    const int cur = (depth - 1) & 1;
+    uint32_t* const qc = W.qcount + (A.max_depth + 1);
+    const uint32_t n = qc[depth - 1];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t pix = W.qidx[cur][i];
+        const lgb_hit hit = W.hits[i];
+        const float4 s0 = *sq(W.es, 0, A.screen, pix), s1 = *sq(W.es, 1, A.screen, pix), s2 = *sq(W.es, 2, A.screen, pix),
+                     s3 = *sq(W.es, 3, A.screen, pix), s4 = *sq(W.es, 4, A.screen, pix);
+        VState cs;
+        cs.pos = V3(s0.x, s0.y, s0.z); cs.d_vcm = s0.w;
+        cs.wi = V3(s1.x, s1.y, s1.z); cs.d_vc = s1.w;
+        cs.thr = V3(s2.x, s2.y, s2.z); cs.d_vm = s2.w;
+        v3 col = V3(s3.x, s3.y, s3.z);
+        const uint32_t x = pix % A.W, y = pix / A.W;
+        uint4 seed = make_uint4(x, y, A.eye_seed, __float_as_uint(s3.w));
+        const uint32_t lp = __float_as_uint(s4.x), lp_len = __float_as_uint(s4.y);
+        const float4* lv = A.verts + (size_t)lp * per * kVertexF4;
         bool done = true;
-        float t, bu, bv;
-        const RayQ q = make_rayq(cs.pos.x, cs.pos.y, cs.pos.z, kTMinV, cs.wi.x, cs.wi.y, cs.wi.z, kTMaxV);
-        const uint32_t prim = trace_closest_single(S.nodes, S.tris, q, t, bu, bv, S.status);
-        if (prim == LGB_NO_HIT) {
+        if (hit.prim == LGB_NO_HIT) {
             col = col + cs.thr * V3(A.sky[0], A.sky[1], A.sky[2]);
         } else {
-            const HitAttr h = resolve_hit(S, prim, bu, bv);
+            const HitAttr h = resolve_hit(S, hit.prim, hit.u, hit.v);
             v3 wo = cs.pos - h.pos;
             const float dist = length(h.pos - cs.pos);
             const float dist_sqr = dist * dist;
@@ -506,23 +555,28 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_eye(SceneView S, VcmArgs A)
                 }
             }
         }
-        if (!done) continue;
-        const uint32_t x = pix % A.W, y = pix / A.W, fp = pix;
-        pix = kNoPath;
+        if (!done) {
+            *sq(W.es, 0, A.screen, pix) = f4(cs.pos, cs.d_vcm);
+            *sq(W.es, 1, A.screen, pix) = f4(cs.wi, cs.d_vc);
+            *sq(W.es, 2, A.screen, pix) = f4(cs.thr, cs.d_vm);
+            *sq(W.es, 3, A.screen, pix) = make_float4(col.x, col.y, col.z, __uint_as_float(seed.w));
+            push_ray(W, depth & 1, qc + depth, pix, cs.pos, kTMinV, cs.wi, kTMaxV);
+            continue;
+        }
         if (isnan(luminance(col))) continue;  // vcm_eye.rgen:80-83: no film write, the splat stays
         const uint32_t sidx = x * A.H + y;
         col = col + V3(A.splat[3 * sidx], A.splat[3 * sidx + 1], A.splat[3 * sidx + 2]);
         A.splat[3 * sidx] = 0.0f;
         A.splat[3 * sidx + 1] = 0.0f;
         A.splat[3 * sidx + 2] = 0.0f;
-        float4 px = A.film[fp];
+        float4 px = A.film[pix];
         if (A.frame_num > 0u) {
             const float w = 1.0f / (float)(A.frame_num + 1u);
             px = make_float4(mixf(px.x, col.x, w), mixf(px.y, col.y, w), mixf(px.z, col.z, w), 1.0f);
         } else {
             px = make_float4(col.x, col.y, col.z, 1.0f);
         }
-        A.film[fp] = px;
+        A.film[pix] = px;
     }
 }
 
@@ -671,8 +725,12 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
     auto take = [&](size_t bytes) { const size_t o = off; off += align256(bytes); return o; };
     const size_t o_verts = take(sizeof(float4) * kVertexF4 * (size_t)nv), o_counts = take(4ull * screen),
                  o_splat = take(12ull * screen), o_gc = take(4ull * table), o_gr = take(4ull * table), o_k0 = take(8ull * nv),
-                 o_k1 = take(8ull * nv), o_v0 = take(4ull * nv), o_v1 = take(4ull * nv), o_sc = take(4ull * radix_sort_scratch_words(nv)),
-                 o_work = take(8);
+                 o_k1 = take(8ull * nv), o_v0 = take(4ull * nv), o_v1 = take(4ull * nv), o_sc = take(4ull * radix_sort_scratch_words(nv));
+    // wavefront: path states, two ray queues with their path indices, hits, queue and fetch counters
+    const size_t o_ls = take(sizeof(float4) * 4 * (size_t)screen), o_es = take(sizeof(float4) * 5 * (size_t)screen),
+                 o_r0 = take(sizeof(lgb_ray) * (size_t)screen), o_r1 = take(sizeof(lgb_ray) * (size_t)screen),
+                 o_q0 = take(4ull * screen), o_q1 = take(4ull * screen), o_hits = take(sizeof(lgb_hit) * (size_t)screen),
+                 o_cnt = take(4ull * 4 * per);
     if (!s->vcm_buf || s->vcm_w != cam->width || s->vcm_h != cam->height || s->vcm_per != per || s->vcm_buf_bytes < off) {
         cudaFree(s->vcm_buf);
         s->vcm_buf = nullptr;
@@ -704,27 +762,46 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
     A.g_count = gc;
     A.g_rep = gr;
     A.film = reinterpret_cast<float4*>(d_film);
-    A.work = reinterpret_cast<uint32_t*>(base + o_work);
-    LGB_CUDA_TRY(ctx, cudaMemsetAsync(A.work, 0, 8, st));
+    Wave W;
+    W.ls = reinterpret_cast<float4*>(base + o_ls);
+    W.es = reinterpret_cast<float4*>(base + o_es);
+    W.rays[0] = reinterpret_cast<lgb_ray*>(base + o_r0);
+    W.rays[1] = reinterpret_cast<lgb_ray*>(base + o_r1);
+    W.qidx[0] = reinterpret_cast<uint32_t*>(base + o_q0);
+    W.qidx[1] = reinterpret_cast<uint32_t*>(base + o_q1);
+    W.hits = reinterpret_cast<lgb_hit*>(base + o_hits);
+    W.qcount = reinterpret_cast<uint32_t*>(base + o_cnt);
+    W.tcount = W.qcount + 2 * per;
+    LGB_CUDA_TRY(ctx, cudaMemsetAsync(W.qcount, 0, 4ull * 4 * per, st));
     const SceneView S = scene_view(s);
     const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
-    // The subpath kernels regenerate paths, so their grids are what the SMs hold at once (at most one block per
-    // 128 subpaths). They are instantiated per set of BSDF types (the caustics scene needs only diffuse and
-    // dielectric lobes): fewer inlined lobes keep their loops inside the instruction cache.
     const uint32_t blocks_needed = (screen + kVcmThreads - 1) / kVcmThreads;
-    auto resident = [&](const void* kernel) {
-        int nb = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kVcmThreads, 0) != cudaSuccess || nb < 1) nb = 1;
-        return (int)std::min<uint32_t>(blocks_needed, (uint32_t)nb * (uint32_t)sms);
-    };
+    const int grid = (int)std::min<uint32_t>(blocks_needed, (uint32_t)sms * 16u);
+    int trace_bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&trace_bps, k_vcm_trace, kVcmThreads, 0) != cudaSuccess || trace_bps < 1)
+        trace_bps = 1;
+    const int trace_grid = (int)std::min<uint32_t>(blocks_needed, (uint32_t)trace_bps * (uint32_t)sms);
+    // The step kernels are instantiated per set of BSDF types (the caustics scene needs only diffuse and
+    // dielectric lobes): fewer inlined lobes keep them inside the instruction cache.
     const uint32_t used = s->bsdf_mask;
     const uint32_t lobes = (used & ~kVcmLobesDG) == 0u ? kVcmLobesDG : ((used & ~kVcmLobesDGC) == 0u ? kVcmLobesDGC : kAllBsdfs);
-    if (lobes == kVcmLobesDG)
-        k_vcm_light<kVcmLobesDG><<<resident((const void*)k_vcm_light<kVcmLobesDG>), kVcmThreads, 0, st>>>(S, A);
-    else if (lobes == kVcmLobesDGC)
-        k_vcm_light<kVcmLobesDGC><<<resident((const void*)k_vcm_light<kVcmLobesDGC>), kVcmThreads, 0, st>>>(S, A);
-    else
-        k_vcm_light<kAllBsdfs><<<resident((const void*)k_vcm_light<kAllBsdfs>), kVcmThreads, 0, st>>>(S, A);
+    // bounce d of a pass: queue d - 1 traced, then stepped into queue d
+    auto bounce = [&](int pass, int d) {
+        const int q = (d - 1) & 1;
+        k_vcm_trace<<<trace_grid, kVcmThreads, 0, st>>>(S, W.rays[q], W.hits, W.qcount + pass * per + (d - 1),
+                                                         W.tcount + pass * per + (d - 1));
+        if (pass == 0) {
+            if (lobes == kVcmLobesDG) k_vcm_light_step<kVcmLobesDG><<<grid, kVcmThreads, 0, st>>>(S, A, W, d);
+            else if (lobes == kVcmLobesDGC) k_vcm_light_step<kVcmLobesDGC><<<grid, kVcmThreads, 0, st>>>(S, A, W, d);
+            else k_vcm_light_step<kAllBsdfs><<<grid, kVcmThreads, 0, st>>>(S, A, W, d);
+        } else {
+            if (lobes == kVcmLobesDG) k_vcm_eye_step<kVcmLobesDG><<<grid, kVcmThreads, 0, st>>>(S, A, W, d);
+            else if (lobes == kVcmLobesDGC) k_vcm_eye_step<kVcmLobesDGC><<<grid, kVcmThreads, 0, st>>>(S, A, W, d);
+            else k_vcm_eye_step<kAllBsdfs><<<grid, kVcmThreads, 0, st>>>(S, A, W, d);
+        }
+    };
+    k_vcm_light_init<<<grid, kVcmThreads, 0, st>>>(S, A, W);
+    for (int d = 1; d <= A.max_depth; d++) bounce(0, d);
     LGB_CUDA_TRY(ctx, cudaGetLastError());
     if (p->use_vm == 1) {
         uint64_t* k0 = reinterpret_cast<uint64_t*>(base + o_k0);
@@ -738,12 +815,8 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
     } else {
         LGB_CUDA_TRY(ctx, cudaMemsetAsync(gc, 0, 4ull * table, st));
     }
-    if (lobes == kVcmLobesDG)
-        k_vcm_eye<kVcmLobesDG><<<resident((const void*)k_vcm_eye<kVcmLobesDG>), kVcmThreads, 0, st>>>(S, A);
-    else if (lobes == kVcmLobesDGC)
-        k_vcm_eye<kVcmLobesDGC><<<resident((const void*)k_vcm_eye<kVcmLobesDGC>), kVcmThreads, 0, st>>>(S, A);
-    else
-        k_vcm_eye<kAllBsdfs><<<resident((const void*)k_vcm_eye<kAllBsdfs>), kVcmThreads, 0, st>>>(S, A);
+    k_vcm_eye_init<<<grid, kVcmThreads, 0, st>>>(A, W);
+    for (int d = 1; d <= A.max_depth; d++) bounce(1, d);
     LGB_CUDA_TRY(ctx, cudaGetLastError());
     return LGB_OK;
 }

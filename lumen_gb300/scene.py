@@ -98,6 +98,17 @@ class SceneArrays:
     def num_tris(self) -> int:
         return int(self.meshes["tri_count"].sum())
 
+    def bounds(self):
+        """(min, max) of the vertex positions as float32 arrays, computed once per positions array (a reduction
+        over every vertex takes milliseconds on the host, longer than a frame's kernels; assign a new positions
+        array rather than editing it in place to change the geometry)."""
+        key = (id(self.positions), self.positions.shape)
+        cached = self.__dict__.get("_bounds")
+        if cached is None or cached[0] != key:
+            cached = (key, self.positions.min(0), self.positions.max(0))
+            self.__dict__["_bounds"] = cached
+        return cached[1], cached[2]
+
     def tri_verts(self) -> np.ndarray:
         """(T, 9) world-space vertices of every global triangle, meshes in order."""
         out = []
@@ -424,7 +435,7 @@ def vcm_params(arrays: SceneArrays, max_depth: int, radius: float, light_seed: i
     p.light_triangle_count = arrays.light_triangle_count
     p.dir_light_idx = 0xFFFFFFFF
     p.radius = radius
-    mn, mx = arrays.positions.min(0), arrays.positions.max(0)
+    mn, mx = arrays.bounds()
     p.scene_min[:] = [float(v) for v in mn]
     p.scene_max[:] = [float(v) for v in mx]
     p.use_vm = use_vm
@@ -487,8 +498,8 @@ def restir_params(arrays: SceneArrays, seed: int, frame_num: int, do_spatiotempo
 
 def scene_radius(arrays: SceneArrays) -> float:
     """Half the diagonal of the scene's bounding box (LumenScene::m_dimensions.radius)."""
-    mn, mx = arrays.positions.min(0).astype(np.float64), arrays.positions.max(0).astype(np.float64)
-    return float(np.linalg.norm(mx - mn) / 2.0)
+    mn, mx = arrays.bounds()
+    return float(np.linalg.norm(mx.astype(np.float64) - mn.astype(np.float64)) / 2.0)
 
 
 def path_params(arrays: SceneArrays, max_depth: int, sky=(0.0, 0.0, 0.0), direct_lighting: int = 1,

@@ -124,33 +124,30 @@ struct VState {
     float d_vcm, d_vc, d_vm;
 };
 
-// vcm_connect_cam (vcm_commons.glsl:24-75): the splat of a light vertex and its pixel (have = false: none).
+// vcm_connect_cam (vcm_commons.glsl:24-75) with its visibility test deferred: the shadow ray towards the camera
+// and the splat it adds to pixel pidx (x * H + y) when not occluded; false when the vertex adds nothing (the
+// camera behind it, a zero BSDF value, a zero pdf ratio, a pixel outside the image, a zero contribution).
 template <uint32_t MASK>
-__device__ v3 connect_cam(const SceneView& S, const VcmArgs& A, const CamV& c, v3 n_s, v3 payload_ns, v3 pos,
-                          const VState& st, float eta_vm, v3 wo, const Mat& mat, uint32_t& pidx, bool& have) {
-    have = false;
-    v3 L = V3(0.0f);
+__device__ bool connect_cam(const VcmArgs& A, const CamV& c, v3 n_s, v3 payload_ns, v3 pos, const VState& st, float eta_vm,
+                            v3 wo, const Mat& mat, float4 (&ray)[2], v3& L, uint32_t& pidx) {
     v3 dir = c.pos - pos;
     const float len = length(dir);
     dir = dir / len;
     const float cos_y = dot(dir, n_s);
     const float cos_theta = dot(c.nrm, -dir);
-    if (cos_theta <= 0.0f) return L;
+    if (cos_theta <= 0.0f) return false;
     const float cos3 = cos_theta * cos_theta * cos_theta;
     const float screen = (float)A.screen;
     const float ratio = fabsf(cos_y) / (c.area * cos3 * len * len);
     const v3 origin = offset_ray2(pos, n_s);
     float pdf_fwd, pdf_rev;
     const v3 f = eval_bsdf_rev<MASK>(n_s, wo, mat, dot(payload_ns, wo) > 0.0f, dir, pdf_fwd, pdf_rev, true);
-    if (is_zero3(f)) return L;
-    if (ratio > 0.0f) {
-        const RayQ q = make_rayq(origin.x, origin.y, origin.z, 0.0f, dir.x, dir.y, dir.z, len - kEpsV);
-        if (!trace_any_single(S.nodes, S.tris, q, S.status)) {
-            const float w_light = (ratio / screen) * (eta_vm + st.d_vcm + pdf_rev * st.d_vc);
-            const float mis = 1.0f / (1.0f + w_light);
-            L = mis * st.thr * ratio * f / screen;
-        }
-    }
+    if (is_zero3(f) || !(ratio > 0.0f)) return false;
+    const float w_light = (ratio / screen) * (eta_vm + st.d_vcm + pdf_rev * st.d_vc);
+    const float mis = 1.0f / (1.0f + w_light);
+    L = mis * st.thr * ratio * f / screen;
+    ray[0] = make_float4(origin.x, origin.y, origin.z, 0.0f);
+    ray[1] = make_float4(dir.x, dir.y, dir.z, len - kEpsV);
     dir = -dir;
     float4 t = mat_vec(A.view, dir.x, dir.y, dir.z, 0.0f);
     t = make_float4(t.x / t.z, t.y / t.z, t.z / t.z, t.w / t.z);
@@ -158,10 +155,9 @@ __device__ v3 connect_cam(const SceneView& S, const VcmArgs& A, const CamV& c, v
     t = make_float4(-t.x, -t.y, -t.z, -t.w);
     const int cx = __float2int_rz(0.5f * (1.0f + t.x) * (float)A.W - 0.5f);
     const int cy = __float2int_rz(0.5f * (1.0f + t.y) * (float)A.H - 0.5f);
-    if (cx < 0 || cx >= (int)A.W || cy < 0 || cy >= (int)A.H || dot(dir, c.nrm) < 0.0f) return V3(0.0f);
-    have = true;
+    if (cx < 0 || cx >= (int)A.W || cy < 0 || cy >= (int)A.H || dot(dir, c.nrm) < 0.0f) return false;
     pidx = (uint32_t)cx * A.H + (uint32_t)cy;
-    return L;
+    return luminance(L) > 0.0f;
 }
 
 // Wavefront form of the subpath loops: per bounce, the closest hits of a queue of rays come from the persistent
@@ -176,7 +172,11 @@ struct Wave {
     uint32_t* qidx[2]; // path of each queued ray
     lgb_hit* hits;
     uint32_t* qcount;  // [2 * (max_depth + 1)]: queue lengths per bounce, light pass then eye pass
-    uint32_t* tcount;  // [2 * (max_depth + 1)]: fetch counters of the traversal launches
+    uint32_t* tcount;  // [2 * (max_depth + 1)]: fetch counters of the traversal launches, then the shadow queue's
+    lgb_ray* srays;    // camera connections of the light pass: shadow rays,
+    float4* spay;      // their splats (value, pixel) and
+    uint32_t* sbits;   // occlusion bits
+    uint32_t* scount;  // [2]: shadow queue length and fetch counter
 };
 __device__ __forceinline__ float4* sq(float4* b, int c, uint32_t screen, uint32_t i) { return b + ((size_t)c * screen + i); }
 
@@ -206,6 +206,25 @@ __global__ void __launch_bounds__(kVcmThreads, kWaveTraceMinBlocks)
                 uint32_t* fetch) {
     trace_persistent<false, false, false, 0, kVcmThreads, kWaveRefill>(S.nodes, S.tris, rays, hits, nullptr, 0u, count,
                                                                      fetch, S.status, nullptr, nullptr, nullptr);
+}
+__global__ void __launch_bounds__(kVcmThreads, kWaveTraceMinBlocks)
+    k_vcm_trace_any(SceneView S, const lgb_ray* __restrict__ rays, uint32_t* __restrict__ bits, const uint32_t* count,
+                    uint32_t* fetch) {
+    trace_persistent<true, false, false, 0, kVcmThreads, kWaveRefill>(S.nodes, S.tris, rays, nullptr, bits, 0u, count,
+                                                                    fetch, S.status, nullptr, nullptr, nullptr);
+}
+
+// The camera splats of the light pass whose shadow rays are not occluded.
+__global__ void __launch_bounds__(256) k_vcm_splat(VcmArgs A, Wave W) {
+    const uint32_t n = W.scount[0];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if ((W.sbits[i >> 5] >> (i & 31u)) & 1u) continue;
+        const float4 c = W.spay[i];
+        const uint32_t pidx = __float_as_uint(c.w);
+        atomicAdd(&A.splat[3 * pidx], c.x);
+        atomicAdd(&A.splat[3 * pidx + 1], c.y);
+        atomicAdd(&A.splat[3 * pidx + 2], c.z);
+    }
 }
 
 // vcm_light.rgen main and vcm_generate_light_sample: one light subpath per launch point (x, y), path x * H + y;
@@ -286,13 +305,15 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_light_step(SceneView S, Vcm
             }
             if (depth < A.max_depth) {
                 if (!spec && A.use_vc == 1) {
-                    uint32_t pidx = 0;
-                    bool have = false;
-                    const v3 L = connect_cam<MASK>(S, A, cam, n_s, h.n_s, h.pos, st, eta.vm, wo, mat, pidx, have);
-                    if (luminance(L) > 0.0f && have) {
-                        atomicAdd(&A.splat[3 * pidx], L.x);
-                        atomicAdd(&A.splat[3 * pidx + 1], L.y);
-                        atomicAdd(&A.splat[3 * pidx + 2], L.z);
+                    float4 ray[2];
+                    v3 L;
+                    uint32_t pidx;
+                    if (connect_cam<MASK>(A, cam, n_s, h.n_s, h.pos, st, eta.vm, wo, mat, ray, L, pidx)) {
+                        const uint32_t j = warp_append(W.scount);
+                        float4* r = reinterpret_cast<float4*>(&W.srays[j]);
+                        r[0] = ray[0];
+                        r[1] = ray[1];
+                        W.spay[j] = make_float4(L.x, L.y, L.z, __uint_as_float(pidx));
                     }
                 }
                 const float c0 = rnd(seed), c1 = rnd(seed), c2 = rnd(seed);
@@ -730,7 +751,8 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
     const size_t o_ls = take(sizeof(float4) * 4 * (size_t)screen), o_es = take(sizeof(float4) * 5 * (size_t)screen),
                  o_r0 = take(sizeof(lgb_ray) * (size_t)screen), o_r1 = take(sizeof(lgb_ray) * (size_t)screen),
                  o_q0 = take(4ull * screen), o_q1 = take(4ull * screen), o_hits = take(sizeof(lgb_hit) * (size_t)screen),
-                 o_cnt = take(4ull * 4 * per);
+                 o_cnt = take(4ull * (4 * per + 2)), o_sr = take(sizeof(lgb_ray) * (size_t)nv),
+                 o_sp = take(sizeof(float4) * (size_t)nv), o_sb = take(4ull * ((nv + 31) / 32));
     if (!s->vcm_buf || s->vcm_w != cam->width || s->vcm_h != cam->height || s->vcm_per != per || s->vcm_buf_bytes < off) {
         cudaFree(s->vcm_buf);
         s->vcm_buf = nullptr;
@@ -772,7 +794,12 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
     W.hits = reinterpret_cast<lgb_hit*>(base + o_hits);
     W.qcount = reinterpret_cast<uint32_t*>(base + o_cnt);
     W.tcount = W.qcount + 2 * per;
-    LGB_CUDA_TRY(ctx, cudaMemsetAsync(W.qcount, 0, 4ull * 4 * per, st));
+    W.scount = W.qcount + 4 * per;
+    W.srays = reinterpret_cast<lgb_ray*>(base + o_sr);
+    W.spay = reinterpret_cast<float4*>(base + o_sp);
+    W.sbits = reinterpret_cast<uint32_t*>(base + o_sb);
+    LGB_CUDA_TRY(ctx, cudaMemsetAsync(W.qcount, 0, 4ull * (4 * per + 2), st));
+    LGB_CUDA_TRY(ctx, cudaMemsetAsync(W.sbits, 0, 4ull * ((nv + 31) / 32), st));
     const SceneView S = scene_view(s);
     const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
     const uint32_t blocks_needed = (screen + kVcmThreads - 1) / kVcmThreads;
@@ -802,6 +829,9 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
     };
     k_vcm_light_init<<<grid, kVcmThreads, 0, st>>>(S, A, W);
     for (int d = 1; d <= A.max_depth; d++) bounce(0, d);
+    // the light pass's camera connections: one any-hit launch over all of them, then the visible splats
+    k_vcm_trace_any<<<trace_grid, kVcmThreads, 0, st>>>(S, W.srays, W.sbits, W.scount, W.scount + 1);
+    k_vcm_splat<<<(int)std::min<uint32_t>((nv + 255) / 256, (uint32_t)sms * 8u), 256, 0, st>>>(A, W);
     LGB_CUDA_TRY(ctx, cudaGetLastError());
     if (p->use_vm == 1) {
         uint64_t* k0 = reinterpret_cast<uint64_t*>(base + o_k0);

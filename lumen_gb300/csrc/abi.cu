@@ -47,6 +47,7 @@ void free_scene(Scene* s) {
     cudaFree(s->d_ray_counter);
     cudaFree(s->pt_buf);
     cudaFree(s->diff_buf);
+    cudaFree(s->diffw_buf);
     cudaFree(s->vcm_buf);
     cudaFree(s->sppm_buf);
     cudaFree(s->bdpt_buf);

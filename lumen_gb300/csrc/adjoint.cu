@@ -249,228 +249,291 @@ enum : int {
     kRecord = 3,       // radiance, and the radiance collected at each depth written to contrib
 };
 
-// One sample of pixel `pix` at `frame`; returns its radiance. The replay modes accumulate gradients.
-template <int MODE, uint32_t MASK>
-__device__ v3 diff_path(const SceneView& S, const DiffArgs& A, uint32_t pix, uint32_t frame, v3* contrib, v3 total,
-                        v3 delta, GradAcc& g) {
-    constexpr bool ADJ = MODE == kReplaySuffix || MODE == kReplayTotal;
+// State of one sample's path between bounces.
+struct DPath {
+    uint4 seed;
+    v3 origin, dir;
+    v3 Tv, Tc;       // throughput with the evaluation values / with the sampler's values (Russian roulette)
+    v3 L, rem;       // radiance so far; radiance still to come (kReplayTotal)
+    bool last_spec;
+};
+
+// The camera ray of one sample of pixel `pix` at `frame` (path.rgen:23-38).
+__device__ __forceinline__ DPath diff_begin(const DiffArgs& A, uint32_t pix, uint32_t frame, v3 total) {
+    DPath P;
     const uint32_t x = pix % A.width, y = pix / A.width;
-    uint4 seed = make_uint4(x, y, frame, 0u);
-    const float r0 = rnd(seed) - 0.5f;
-    const float r1 = rnd(seed) - 0.5f;
+    P.seed = make_uint4(x, y, frame, 0u);
+    const float r0 = rnd(P.seed) - 0.5f;
+    const float r1 = rnd(P.seed) - 0.5f;
     const float pu = ((float)x + 0.5f + r0) / (float)A.width, pv = ((float)y + 0.5f + r1) / (float)A.height;
     const float dx = pu * 2.0f - 1.0f, dy = pv * 2.0f - 1.0f;
     const float4 o4 = mat_vec(A.iv, 0.0f, 0.0f, 0.0f, 1.0f);
     const float4 t4 = mat_vec(A.ip, dx, dy, 1.0f, 1.0f);
     const v3 tn = normalize(V3(t4.x, t4.y, t4.z));
     const float4 d4 = mat_vec(A.iv, tn.x, tn.y, tn.z, 0.0f);
-    v3 origin = V3(o4.x, o4.y, o4.z), dir = V3(d4.x, d4.y, d4.z);
-    v3 Tv = V3(1.0f), Tc = V3(1.0f), L = V3(0.0f), rem = total;
-    bool last_spec = false;
+    P.origin = V3(o4.x, o4.y, o4.z);
+    P.dir = V3(d4.x, d4.y, d4.z);
+    P.Tv = V3(1.0f); P.Tc = V3(1.0f); P.L = V3(0.0f); P.rem = total;
+    P.last_spec = false;
+    return P;
+}
+
+// How a vertex gets its two secondary traversals: inline (the loop below), or in a wavefront as two passes over
+// the same code, the first recording the NEE shadow ray and the BSDF-MIS ray, the second taking their results.
+enum : int { kPhaseInline = 0, kPhaseRays = 1, kPhaseResults = 2 };
+struct VertexIO {
+    float4 sray[2], mray[2];  // kPhaseRays: the rays to trace as (origin, tmin) (direction, tmax); tmin > tmax: none
+    bool occluded;      // kPhaseResults: the shadow ray's result
+    DiffHit mhit;       // kPhaseResults: the BSDF-MIS ray's closest hit
+};
+enum : int { kStepContinue = 0, kStepEnd = 1 };
+
+// One bounce (depth) of the path at the closest hit ph of its current ray (the body of path.rgen's loop):
+// emission, next-event estimation with both MIS strategies, the continuation sample and Russian roulette, and in
+// the replay modes the gradients of the vertex. Returns kStepEnd when the path ends here.
+template <int MODE, uint32_t MASK, int PHASE>
+__device__ int diff_vertex(const SceneView& S, const DiffArgs& A, DPath& P, int depth, const DiffHit& ph, v3* contrib,
+                           v3 delta, GradAcc& g, VertexIO& io) {
+    constexpr bool ADJ = MODE == kReplaySuffix || MODE == kReplayTotal;
+    uint4& seed = P.seed;
+    v3& origin = P.origin;
+    v3& dir = P.dir;
+    v3& Tv = P.Tv;
+    v3& Tc = P.Tc;
+    v3& L = P.L;
+    v3& rem = P.rem;
+    bool& last_spec = P.last_spec;
     const v3 sky = V3(A.sky[0], A.sky[1], A.sky[2]);
-    for (int depth = 0; depth < kDiffMaxDepth; depth++) {
-        v3 Cd = V3(0.0f);
-        const RayQ rq = make_rayq(origin.x, origin.y, origin.z, kTMinD, dir.x, dir.y, dir.z, kTMaxD);
-        const DiffHit ph = diff_closest(S.nodes, S.tris, rq, S.status);
-        const uint32_t prim = ph.prim;
-        const float bu = ph.u, bv = ph.v;
-        if (prim == LGB_NO_HIT) {
-            if (depth > 0 || A.direct_lighting == 1u) Cd = Tv * sky;
-            if (MODE == kRecord) contrib[depth] = Cd;
-            L = L + Cd;
-            break;
-        }
-        const HitAttr h = resolve_hit(S, prim, bu, bv);
-        Mat ms = load_material(S, h.mat, h.u, h.v);
-        const EvalMat em = eval_material(S, A, ms, h.mat, h.u, h.v);
-        if (A.sample_params) ms = em.m;  // then every BSDF value below is the sampler's own
-        if ((depth == 0 && A.direct_lighting == 1u) || last_spec) {
-            Cd = Cd + Tv * em.m.emissive;
-            if (ADJ && A.emis) add_emis(A, g, h.mat, delta * Tv);
-        }
-        if (depth >= A.max_depth - 1) {
-            if (MODE == kRecord) contrib[depth] = Cd;
-            L = L + Cd;
-            break;
-        }
-        const v3 wo = -dir;
-        v3 n_s = h.n_s;
-        bool side = true;
-        v3 n_g = h.n_g;
-        if (dot(h.n_g, wo) < 0.0f) n_g = -n_g;
-        if (dot(n_g, h.n_s) < 0.0f) { n_s = -n_s; side = false; }
-        const v3 next_origin = offset_ray(h.pos, n_g);
-        const bool spec = has_prop(ms.props, LGB_FLAG_SPECULAR);
-        v3 sf_tex = V3(0.0f);  // d loss / d ln f summed over this vertex's BSDF values (texel gradients)
-        if (!spec && (depth > 0 || A.direct_lighting == 1u)) {
-            if (A.num_lights <= 0) {
-                for (int k = 0; k < 4; k++) (void)rnd(seed);
-            } else {
-                const float lpp = 1.0f / (float)A.light_tri_count;
-                const float q0 = rnd(seed), q1 = rnd(seed), q2 = rnd(seed), q3 = rnd(seed);
-                const uint32_t li = (uint32_t)(q0 * (float)A.num_lights);
-                const lgb_light* Lt = &S.lights[li];
-                const uint32_t ltype = Lt->light_flags & 7u;
-                v3 Le = V3(0.0f), wi = V3(0.0f);
-                float wi_len = 0.0f, pdf_w = 0.0f, pdf_a = 0.0f;
-                uint32_t lprim = LGB_NO_HIT, lmat = 0xFFFFFFFFu, lio = 0u, lvo = 0u;
-                if (ltype == LGB_LIGHT_AREA) {
-                    const lgb_mesh pm = S.meshes[Lt->prim_mesh_idx];
-                    const uint32_t tri = (uint32_t)(q1 * (float)Lt->num_triangles);
-                    lprim = S.mesh_first[Lt->prim_mesh_idx] + tri;
-                    const uint32_t io = pm.index_offset + 3u * tri;
-                    lio = io;
-                    lvo = pm.vertex_offset;
-                    const DevVertex a = S.verts[S.idx[io] + pm.vertex_offset];
-                    const DevVertex b = S.verts[S.idx[io + 1] + pm.vertex_offset];
-                    const DevVertex c = S.verts[S.idx[io + 2] + pm.vertex_offset];
-                    const float su = 1.0f - sqrtf(q2), sv = q3 * sqrtf(q2);
-                    const float b0 = 1.0f - su - sv;
-                    const v3 v0 = V3(a.px, a.py, a.pz), v1 = V3(b.px, b.py, b.pz), v2 = V3(c.px, c.py, c.pz);
-                    const v3 lpos = v0 * b0 + v1 * su + v2 * sv;
-                    const v3 ln = normalize(normalize(V3(a.nx, a.ny, a.nz) * b0 + V3(b.nx, b.ny, b.nz) * su +
-                                                      V3(c.nx, c.ny, c.nz) * sv));
-                    const float tri_pdf = 2.0f / length(cross(v1 - v0, v2 - v0));
-                    lmat = pm.material_index;
-                    const lgb_material* lm = &S.mats[lmat];
-                    Le = A.emis ? V3(A.emis[3 * lmat], A.emis[3 * lmat + 1], A.emis[3 * lmat + 2])
-                                : V3(lm->emissive_factor[0], lm->emissive_factor[1], lm->emissive_factor[2]);
-                    wi = lpos - h.pos;
-                    const float l2 = dot(wi, wi);
-                    wi_len = sqrtf(l2);
-                    wi = wi / wi_len;
-                    const float cfl = fabsf(dot(ln, -wi));
-                    pdf_a = tri_pdf;
-                    pdf_w = pdf_a * l2 / cfl;
-                } else if (ltype == LGB_LIGHT_SPOT) {
-                    const v3 lp = V3(Lt->pos[0], Lt->pos[1], Lt->pos[2]);
-                    wi = lp - h.pos;
-                    const float l2 = dot(wi, wi);
-                    wi_len = sqrtf(l2);
-                    wi = wi / wi_len;
-                    const v3 ldir = normalize(V3(Lt->to[0], Lt->to[1], Lt->to[2]) - lp);
-                    const float cfl = dot(-wi, ldir);
-                    const float cw = cosf(LGB_PI / 6.0f), cf = cosf(25.0f * LGB_PI / 180.0f);
-                    float fall;
-                    if (cfl < cw) fall = 0.0f;
-                    else if (cfl >= cf) fall = 1.0f;
-                    else { const float dd = (cfl - cw) / (cf - cw); fall = (dd * dd) * (dd * dd); }
-                    pdf_a = 1.0f;
-                    pdf_w = l2;
-                    Le = V3(Lt->L[0], Lt->L[1], Lt->L[2]) * fall;
-                } else {
-                    const v3 ddir = normalize(V3(Lt->pos[0], Lt->pos[1], Lt->pos[2]) - V3(Lt->to[0], Lt->to[1], Lt->to[2]));
-                    const v3 lp = h.pos + ddir * (2.0f * Lt->world_radius);
-                    wi = lp - h.pos;
-                    wi_len = length(wi);
-                    wi = wi / wi_len;
-                    pdf_a = 1.0f;
-                    pdf_w = 1.0f;
-                    Le = V3(Lt->L[0], Lt->L[1], Lt->L[2]);
-                }
-                const v3 sp = offset_ray2(h.pos, n_s);
-                const float cos_x = dot(n_s, wi);
-                const float4 fp1 = diff_eval_bsdf<MASK>(n_s, wo, ms, side, wi);
-                const v3 fs1 = V3(fp1.x, fp1.y, fp1.z);
-                const float bsdf_pdf = fp1.w;
-                const v3 fe1 = A.sample_params ? fs1 : eval_value(em, n_s, wo, wi, fs1, false);
-                v3 term1 = V3(0.0f), k1 = V3(0.0f);
-                if (pdf_w > 0.0f) {
-                    const RayQ sq = make_rayq(sp.x, sp.y, sp.z, 0.0f, wi.x, wi.y, wi.z, wi_len - kEpsD);
-                    if (!diff_any(S.nodes, S.tris, sq, S.status)) {
-                        const float mis = ((Lt->light_flags >> 5) & 1u) ? 1.0f : 1.0f / (1.0f + bsdf_pdf / pdf_w);
-                        k1 = mis * fe1 * fabsf(cos_x) / pdf_w;  // term1 = k1 * Le
-                        term1 = k1 * Le;
-                    }
-                }
-                v3 term2 = V3(0.0f), k2 = V3(0.0f), wi2 = V3(0.0f);
-                if (ltype == LGB_LIGHT_AREA) {
-                    const float b0r = rnd(seed), b1r = rnd(seed), b2r = rnd(seed);
-                    const BsdfSample bs2 = diff_sample_bsdf<MASK>(n_s, wo, ms, side, V3(b0r, b1r, b2r));
-                    const v3 fs2 = bs2.f;
-                    const float pdf2 = bs2.pdf, cos2 = bs2.cos_t;
-                    wi2 = bs2.wi;
-                    const RayQ mq = make_rayq(sp.x, sp.y, sp.z, kTMinD, wi2.x, wi2.y, wi2.z, kTMaxD);
-                    bool may_count = pdf2 != 0.0f;
-                    if (may_count && lprim != prim) {
-                        // Only a closest hit on the sampled light triangle counts (a miss reuses the shading
-                        // triangle, which differs here): a ray that fails the traversal's own watertight test
-                        // against that triangle cannot count, so it is not traced.
-                        const DevVertex a = S.verts[S.idx[lio] + lvo];
-                        const DevVertex b = S.verts[S.idx[lio + 1] + lvo];
-                        const DevVertex c = S.verts[S.idx[lio + 2] + lvo];
-                        float tt, tu, tv;
-                        may_count = tri_intersect(mq, make_float4(a.px, a.py, a.pz, 0.0f),
-                                                  make_float4(b.px, b.py, b.pz, 0.0f),
-                                                  make_float4(c.px, c.py, c.pz, 0.0f), mq.tmax, tt, tu, tv);
-                    }
-                    if (may_count) {
-                        const DiffHit mhit = diff_closest(S.nodes, S.tris, mq, S.status);
-                        const uint32_t mprim = mhit.prim;
-                        const float mu = mhit.u, mv = mhit.v;
-                        // a missed MIS ray leaves the previous payload (ray.rmiss:13): compare the shading triangle
-                        const uint32_t pl_prim = mprim == LGB_NO_HIT ? prim : mprim;
-                        if (pl_prim == lprim) {
-                            v3 pl_pos = h.pos, pl_ns = h.n_s;
-                            if (mprim != LGB_NO_HIT) {
-                                const HitAttr mh = resolve_hit(S, mprim, mu, mv);
-                                pl_pos = mh.pos;
-                                pl_ns = mh.n_s;
-                            }
-                            const float wl = length(pl_pos - h.pos);
-                            const float gg = fabsf(dot(pl_ns, -wi2)) / (wl * wl);
-                            const float mis = 1.0f / (1.0f + pdf_a / (gg * pdf2));
-                            const v3 fe2 = A.sample_params ? fs2 : eval_value(em, n_s, wo, wi2, fs2, true);
-                            k2 = fe2 * mis * fabsf(cos2) / pdf2;
-                            term2 = k2 * Le;
-                        }
-                    }
-                }
-                const v3 res = term1 + term2;
-                Cd = Cd + Tv * res / lpp;
-                if (ADJ) {
-                    if (A.emis && lmat != 0xFFFFFFFFu) add_emis(A, g, lmat, delta * Tv * (k1 + k2) / lpp);
-                    const v3 sf1 = delta * (Tv * term1 / lpp), sf2 = delta * (Tv * term2 / lpp);
-                    sf_tex = sf1 + sf2;
-                    add_rough_grad(A, g, em, h.mat, sf1, n_s, wo, wi);
-                    if (ltype == LGB_LIGHT_AREA) add_rough_grad(A, g, em, h.mat, sf2, n_s, wo, wi2);
-                }
-            }
-        }
-        const float c0 = rnd(seed), c1 = rnd(seed), c2 = rnd(seed);
-        const BsdfSample bs = diff_sample_bsdf<MASK>(n_s, wo, ms, side, V3(c0, c1, c2));
-        const v3 fs = bs.f, dnext = bs.wi;
-        const float pdf = bs.pdf, cos_t = bs.cos_t;
+    v3 Cd = V3(0.0f);
+    const uint32_t prim = ph.prim;
+    const float bu = ph.u, bv = ph.v;
+    if (prim == LGB_NO_HIT) {
+        if (depth > 0 || A.direct_lighting == 1u) Cd = Tv * sky;
         if (MODE == kRecord) contrib[depth] = Cd;
         L = L + Cd;
-        v3 after = V3(0.0f);  // radiance collected after this depth
-        if (MODE == kReplaySuffix) after = contrib[depth];
-        if (MODE == kReplayTotal) { rem = rem - Cd; after = rem; }
-        if (pdf == 0.0f) {
-            if (ADJ) flush_texel_grad(A, em, sf_tex);
-            break;
-        }
-        const v3 fe = A.sample_params ? fs : eval_value(em, n_s, wo, dnext, fs, true);
-        if (ADJ) {
-            const v3 sf3 = delta * after;
-            add_rough_grad(A, g, em, h.mat, sf3, n_s, wo, dnext);
-            flush_texel_grad(A, em, sf_tex + sf3);
-        }
-        Tv = Tv * (fe * fabsf(cos_t) / pdf);
-        Tc = Tc * (fs * fabsf(cos_t) / pdf);
-        float rr_scale = 1.0f;
-        if (has_prop(ms.props, LGB_FLAG_TRANSMISSION)) rr_scale *= side ? 1.0f / ms.ior : ms.ior;
-        if (depth > 3) {
-            const float rr = fminf(0.95f, luminance(Tc) * rr_scale);
-            if (rr == 0.0f || rr < rnd(seed)) break;
-            Tv = Tv / rr;
-            Tc = Tc / rr;
-        }
-        origin = next_origin;
-        dir = dnext;
-        last_spec = spec;
+        return kStepEnd;
     }
-    return L;
+    const HitAttr h = resolve_hit(S, prim, bu, bv);
+    Mat ms = load_material(S, h.mat, h.u, h.v);
+    const EvalMat em = eval_material(S, A, ms, h.mat, h.u, h.v);
+    if (A.sample_params) ms = em.m;  // then every BSDF value below is the sampler's own
+    if ((depth == 0 && A.direct_lighting == 1u) || last_spec) {
+        Cd = Cd + Tv * em.m.emissive;
+        if (ADJ && PHASE != kPhaseRays && A.emis) add_emis(A, g, h.mat, delta * Tv);
+    }
+    if (depth >= A.max_depth - 1) {
+        if (MODE == kRecord) contrib[depth] = Cd;
+        L = L + Cd;
+        return kStepEnd;
+    }
+    const v3 wo = -dir;
+    v3 n_s = h.n_s;
+    bool side = true;
+    v3 n_g = h.n_g;
+    if (dot(h.n_g, wo) < 0.0f) n_g = -n_g;
+    if (dot(n_g, h.n_s) < 0.0f) { n_s = -n_s; side = false; }
+    const v3 next_origin = offset_ray(h.pos, n_g);
+    const bool spec = has_prop(ms.props, LGB_FLAG_SPECULAR);
+    v3 sf_tex = V3(0.0f);  // d loss / d ln f summed over this vertex's BSDF values (texel gradients)
+    if (!spec && (depth > 0 || A.direct_lighting == 1u)) {
+        if (A.num_lights <= 0) {
+            for (int k = 0; k < 4; k++) (void)rnd(seed);
+        } else {
+            const float lpp = 1.0f / (float)A.light_tri_count;
+            const float q0 = rnd(seed), q1 = rnd(seed), q2 = rnd(seed), q3 = rnd(seed);
+            const uint32_t li = (uint32_t)(q0 * (float)A.num_lights);
+            const lgb_light* Lt = &S.lights[li];
+            const uint32_t ltype = Lt->light_flags & 7u;
+            v3 Le = V3(0.0f), wi = V3(0.0f);
+            float wi_len = 0.0f, pdf_w = 0.0f, pdf_a = 0.0f;
+            uint32_t lprim = LGB_NO_HIT, lmat = 0xFFFFFFFFu, lio = 0u, lvo = 0u;
+            if (ltype == LGB_LIGHT_AREA) {
+                const lgb_mesh pm = S.meshes[Lt->prim_mesh_idx];
+                const uint32_t tri = (uint32_t)(q1 * (float)Lt->num_triangles);
+                lprim = S.mesh_first[Lt->prim_mesh_idx] + tri;
+                const uint32_t io = pm.index_offset + 3u * tri;
+                lio = io;
+                lvo = pm.vertex_offset;
+                const DevVertex a = S.verts[S.idx[io] + pm.vertex_offset];
+                const DevVertex b = S.verts[S.idx[io + 1] + pm.vertex_offset];
+                const DevVertex c = S.verts[S.idx[io + 2] + pm.vertex_offset];
+                const float su = 1.0f - sqrtf(q2), sv = q3 * sqrtf(q2);
+                const float b0 = 1.0f - su - sv;
+                const v3 v0 = V3(a.px, a.py, a.pz), v1 = V3(b.px, b.py, b.pz), v2 = V3(c.px, c.py, c.pz);
+                const v3 lpos = v0 * b0 + v1 * su + v2 * sv;
+                const v3 ln = normalize(normalize(V3(a.nx, a.ny, a.nz) * b0 + V3(b.nx, b.ny, b.nz) * su +
+                                                  V3(c.nx, c.ny, c.nz) * sv));
+                const float tri_pdf = 2.0f / length(cross(v1 - v0, v2 - v0));
+                lmat = pm.material_index;
+                const lgb_material* lm = &S.mats[lmat];
+                Le = A.emis ? V3(A.emis[3 * lmat], A.emis[3 * lmat + 1], A.emis[3 * lmat + 2])
+                            : V3(lm->emissive_factor[0], lm->emissive_factor[1], lm->emissive_factor[2]);
+                wi = lpos - h.pos;
+                const float l2 = dot(wi, wi);
+                wi_len = sqrtf(l2);
+                wi = wi / wi_len;
+                const float cfl = fabsf(dot(ln, -wi));
+                pdf_a = tri_pdf;
+                pdf_w = pdf_a * l2 / cfl;
+            } else if (ltype == LGB_LIGHT_SPOT) {
+                const v3 lp = V3(Lt->pos[0], Lt->pos[1], Lt->pos[2]);
+                wi = lp - h.pos;
+                const float l2 = dot(wi, wi);
+                wi_len = sqrtf(l2);
+                wi = wi / wi_len;
+                const v3 ldir = normalize(V3(Lt->to[0], Lt->to[1], Lt->to[2]) - lp);
+                const float cfl = dot(-wi, ldir);
+                const float cw = cosf(LGB_PI / 6.0f), cf = cosf(25.0f * LGB_PI / 180.0f);
+                float fall;
+                if (cfl < cw) fall = 0.0f;
+                else if (cfl >= cf) fall = 1.0f;
+                else { const float dd = (cfl - cw) / (cf - cw); fall = (dd * dd) * (dd * dd); }
+                pdf_a = 1.0f;
+                pdf_w = l2;
+                Le = V3(Lt->L[0], Lt->L[1], Lt->L[2]) * fall;
+            } else {
+                const v3 ddir = normalize(V3(Lt->pos[0], Lt->pos[1], Lt->pos[2]) - V3(Lt->to[0], Lt->to[1], Lt->to[2]));
+                const v3 lp = h.pos + ddir * (2.0f * Lt->world_radius);
+                wi = lp - h.pos;
+                wi_len = length(wi);
+                wi = wi / wi_len;
+                pdf_a = 1.0f;
+                pdf_w = 1.0f;
+                Le = V3(Lt->L[0], Lt->L[1], Lt->L[2]);
+            }
+            const v3 sp = offset_ray2(h.pos, n_s);
+            const float cos_x = dot(n_s, wi);
+            const float4 fp1 = diff_eval_bsdf<MASK>(n_s, wo, ms, side, wi);
+            const v3 fs1 = V3(fp1.x, fp1.y, fp1.z);
+            const float bsdf_pdf = fp1.w;
+            const v3 fe1 = A.sample_params ? fs1 : eval_value(em, n_s, wo, wi, fs1, false);
+            v3 term1 = V3(0.0f), k1 = V3(0.0f);
+            if (pdf_w > 0.0f) {
+                const RayQ sq = make_rayq(sp.x, sp.y, sp.z, 0.0f, wi.x, wi.y, wi.z, wi_len - kEpsD);
+                bool visible = false;
+                if constexpr (PHASE == kPhaseInline) visible = !diff_any(S.nodes, S.tris, sq, S.status);
+                else if constexpr (PHASE == kPhaseRays) {
+                    io.sray[0] = make_float4(sp.x, sp.y, sp.z, 0.0f);
+                    io.sray[1] = make_float4(wi.x, wi.y, wi.z, wi_len - kEpsD);
+                }
+                else visible = !io.occluded;
+                if (visible) {
+                    const float mis = ((Lt->light_flags >> 5) & 1u) ? 1.0f : 1.0f / (1.0f + bsdf_pdf / pdf_w);
+                    k1 = mis * fe1 * fabsf(cos_x) / pdf_w;  // term1 = k1 * Le
+                    term1 = k1 * Le;
+                }
+            }
+            v3 term2 = V3(0.0f), k2 = V3(0.0f), wi2 = V3(0.0f);
+            if (ltype == LGB_LIGHT_AREA) {
+                const float b0r = rnd(seed), b1r = rnd(seed), b2r = rnd(seed);
+                const BsdfSample bs2 = diff_sample_bsdf<MASK>(n_s, wo, ms, side, V3(b0r, b1r, b2r));
+                const v3 fs2 = bs2.f;
+                const float pdf2 = bs2.pdf, cos2 = bs2.cos_t;
+                wi2 = bs2.wi;
+                const RayQ mq = make_rayq(sp.x, sp.y, sp.z, kTMinD, wi2.x, wi2.y, wi2.z, kTMaxD);
+                bool may_count = pdf2 != 0.0f;
+                if (may_count && lprim != prim) {
+                    // Only a closest hit on the sampled light triangle counts (a miss reuses the shading
+                    // triangle, which differs here): a ray that fails the traversal's own watertight test
+                    // against that triangle cannot count, so it is not traced.
+                    const DevVertex a = S.verts[S.idx[lio] + lvo];
+                    const DevVertex b = S.verts[S.idx[lio + 1] + lvo];
+                    const DevVertex c = S.verts[S.idx[lio + 2] + lvo];
+                    float tt, tu, tv;
+                    may_count = tri_intersect(mq, make_float4(a.px, a.py, a.pz, 0.0f),
+                                              make_float4(b.px, b.py, b.pz, 0.0f),
+                                              make_float4(c.px, c.py, c.pz, 0.0f), mq.tmax, tt, tu, tv);
+                }
+                if constexpr (PHASE == kPhaseRays) {
+                    if (may_count) {
+                        io.mray[0] = make_float4(sp.x, sp.y, sp.z, kTMinD);
+                        io.mray[1] = make_float4(wi2.x, wi2.y, wi2.z, kTMaxD);
+                    }
+                    may_count = false;
+                }
+                if (may_count) {
+                    DiffHit mhit;
+                    if constexpr (PHASE == kPhaseInline) mhit = diff_closest(S.nodes, S.tris, mq, S.status);
+                    else mhit = io.mhit;
+                    const uint32_t mprim = mhit.prim;
+                    const float mu = mhit.u, mv = mhit.v;
+                    // a missed MIS ray leaves the previous payload (ray.rmiss:13): compare the shading triangle
+                    const uint32_t pl_prim = mprim == LGB_NO_HIT ? prim : mprim;
+                    if (pl_prim == lprim) {
+                        v3 pl_pos = h.pos, pl_ns = h.n_s;
+                        if (mprim != LGB_NO_HIT) {
+                            const HitAttr mh = resolve_hit(S, mprim, mu, mv);
+                            pl_pos = mh.pos;
+                            pl_ns = mh.n_s;
+                        }
+                        const float wl = length(pl_pos - h.pos);
+                        const float gg = fabsf(dot(pl_ns, -wi2)) / (wl * wl);
+                        const float mis = 1.0f / (1.0f + pdf_a / (gg * pdf2));
+                        const v3 fe2 = A.sample_params ? fs2 : eval_value(em, n_s, wo, wi2, fs2, true);
+                        k2 = fe2 * mis * fabsf(cos2) / pdf2;
+                        term2 = k2 * Le;
+                    }
+                }
+            }
+            const v3 res = term1 + term2;
+            Cd = Cd + Tv * res / lpp;
+            if (ADJ && PHASE != kPhaseRays) {
+                if (A.emis && lmat != 0xFFFFFFFFu) add_emis(A, g, lmat, delta * Tv * (k1 + k2) / lpp);
+                const v3 sf1 = delta * (Tv * term1 / lpp), sf2 = delta * (Tv * term2 / lpp);
+                sf_tex = sf1 + sf2;
+                add_rough_grad(A, g, em, h.mat, sf1, n_s, wo, wi);
+                if (ltype == LGB_LIGHT_AREA) add_rough_grad(A, g, em, h.mat, sf2, n_s, wo, wi2);
+            }
+        }
+    }
+    if constexpr (PHASE == kPhaseRays) return kStepContinue;  // the vertex's rays are recorded
+    const float c0 = rnd(seed), c1 = rnd(seed), c2 = rnd(seed);
+    const BsdfSample bs = diff_sample_bsdf<MASK>(n_s, wo, ms, side, V3(c0, c1, c2));
+    const v3 fs = bs.f, dnext = bs.wi;
+    const float pdf = bs.pdf, cos_t = bs.cos_t;
+    if (MODE == kRecord) contrib[depth] = Cd;
+    L = L + Cd;
+    v3 after = V3(0.0f);  // radiance collected after this depth
+    if (MODE == kReplaySuffix) after = contrib[depth];
+    if (MODE == kReplayTotal) { rem = rem - Cd; after = rem; }
+    if (pdf == 0.0f) {
+        if (ADJ) flush_texel_grad(A, em, sf_tex);
+        return kStepEnd;
+    }
+    const v3 fe = A.sample_params ? fs : eval_value(em, n_s, wo, dnext, fs, true);
+    if (ADJ) {
+        const v3 sf3 = delta * after;
+        add_rough_grad(A, g, em, h.mat, sf3, n_s, wo, dnext);
+        flush_texel_grad(A, em, sf_tex + sf3);
+    }
+    Tv = Tv * (fe * fabsf(cos_t) / pdf);
+    Tc = Tc * (fs * fabsf(cos_t) / pdf);
+    float rr_scale = 1.0f;
+    if (has_prop(ms.props, LGB_FLAG_TRANSMISSION)) rr_scale *= side ? 1.0f / ms.ior : ms.ior;
+    if (depth > 3) {
+        const float rr = fminf(0.95f, luminance(Tc) * rr_scale);
+        if (rr == 0.0f || rr < rnd(seed)) return kStepEnd;
+        Tv = Tv / rr;
+        Tc = Tc / rr;
+    }
+    origin = next_origin;
+    dir = dnext;
+    last_spec = spec;
+    return kStepContinue;
+}
+
+// One sample of pixel `pix` at `frame`; returns its radiance. The replay modes accumulate gradients.
+template <int MODE, uint32_t MASK>
+__device__ v3 diff_path(const SceneView& S, const DiffArgs& A, uint32_t pix, uint32_t frame, v3* contrib, v3 total,
+                        v3 delta, GradAcc& g) {
+    DPath P = diff_begin(A, pix, frame, total);
+    VertexIO io;
+    for (int depth = 0; depth < kDiffMaxDepth; depth++) {
+        const RayQ rq = make_rayq(P.origin.x, P.origin.y, P.origin.z, kTMinD, P.dir.x, P.dir.y, P.dir.z, kTMaxD);
+        const DiffHit ph = diff_closest(S.nodes, S.tris, rq, S.status);
+        if (diff_vertex<MODE, MASK, kPhaseInline>(S, A, P, depth, ph, contrib, delta, g, io) == kStepEnd) break;
+    }
+    return P.L;
 }
 
 // MODE kPrimal writes each sample's radiance; kReplaySuffix re-runs the primal in the thread (kRecord, keeping
@@ -543,6 +606,162 @@ void launch_diff(Scene* s, const DiffArgs& A, int grid, cudaStream_t cs) {
     else k_diff<MODE, sh::kAllBsdfs><<<grid, kDiffThreads, 0, cs>>>(scene_view(s), A);
 }
 
+// Wavefront form of the sample loop for kPrimal and kReplayTotal. Per bounce: the closest hits of the queued rays
+// (the persistent traversal kernel, lanes whose ray is done fetch the next), a pass over the vertices that records
+// each one's shadow ray and BSDF-MIS ray, their traversals, and a pass that completes the vertices with those
+// results and queues the continuation rays. Both passes run diff_vertex on the same state (the RNG counter is part
+// of it), so a sample's arithmetic and random numbers are the loop's; the instruction footprint of each kernel is a
+// fraction of the loop's.
+struct DiffWave {
+    float4* st;        // sample state, 6 float4 per sample: (origin, rng) (dir, last_spec) (Tv) (Tc) (L) (rem)
+    lgb_ray* rays[2];  // ray queues of consecutive bounces
+    uint32_t* qidx[2]; // sample of each queued ray
+    lgb_hit* hits;
+    lgb_ray* srays;    // per queue slot: the vertex's shadow ray (tmin > tmax: none)
+    uint32_t* sbits;   // their occlusion bits
+    lgb_ray* mrays;    // per queue slot: the vertex's BSDF-MIS ray
+    lgb_hit* mhits;
+    uint32_t* counts;  // queue lengths per bounce [kDiffMaxDepth + 1], then 3 fetch counters per bounce
+    uint32_t n;        // samples: npix * spp, sample i = frame (i / npix), pixel (i % npix)
+};
+__device__ __forceinline__ float4* wst(const DiffWave& W, int c, uint32_t i) { return W.st + ((size_t)c * W.n + i); }
+__device__ __forceinline__ void store_dpath(const DiffWave& W, uint32_t i, const DPath& P) {
+    *wst(W, 0, i) = f4(P.origin, __uint_as_float(P.seed.w));
+    *wst(W, 1, i) = f4(P.dir, __uint_as_float(P.last_spec ? 1u : 0u));
+    *wst(W, 2, i) = f4(P.Tv, 0.0f);
+    *wst(W, 3, i) = f4(P.Tc, 0.0f);
+    *wst(W, 4, i) = f4(P.L, 0.0f);
+    *wst(W, 5, i) = f4(P.rem, 0.0f);
+}
+__device__ __forceinline__ DPath load_dpath(const DiffWave& W, const DiffArgs& A, uint32_t i) {
+    const uint32_t pix = i % A.npix, frame = A.frame0 + i / A.npix;
+    const float4 a = *wst(W, 0, i), b = *wst(W, 1, i), c = *wst(W, 2, i), d = *wst(W, 3, i), e = *wst(W, 4, i),
+                 f = *wst(W, 5, i);
+    DPath P;
+    P.seed = make_uint4(pix % A.width, pix / A.width, frame, __float_as_uint(a.w));
+    P.origin = V3(a.x, a.y, a.z);
+    P.dir = V3(b.x, b.y, b.z);
+    P.last_spec = __float_as_uint(b.w) != 0u;
+    P.Tv = V3(c.x, c.y, c.z); P.Tc = V3(d.x, d.y, d.z); P.L = V3(e.x, e.y, e.z); P.rem = V3(f.x, f.y, f.z);
+    return P;
+}
+__device__ __forceinline__ uint32_t diff_append(uint32_t* counter) {
+    const uint32_t mask = __activemask();
+    const int leader = __ffs(mask) - 1;
+    const int lane = (int)(threadIdx.x & 31u);
+    uint32_t first = 0;
+    if (lane == leader) first = atomicAdd(counter, (uint32_t)__popc(mask));
+    first = __shfl_sync(mask, first, leader);
+    return first + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+__device__ __forceinline__ void push_diff_ray(const DiffWave& W, int q, uint32_t* counter, uint32_t i, const DPath& P) {
+    const uint32_t j = diff_append(counter);
+    W.qidx[q][j] = i;
+    float4* r = reinterpret_cast<float4*>(&W.rays[q][j]);
+    r[0] = make_float4(P.origin.x, P.origin.y, P.origin.z, kTMinD);
+    r[1] = make_float4(P.dir.x, P.dir.y, P.dir.z, kTMaxD);
+}
+
+constexpr int kDiffTraceMinBlocks = 9;
+constexpr int kDiffRefill = 16;
+__global__ void __launch_bounds__(kDiffThreads, kDiffTraceMinBlocks)
+    k_diff_trace(SceneView S, const lgb_ray* __restrict__ rays, lgb_hit* __restrict__ hits, const uint32_t* count,
+                 uint32_t* fetch) {
+    trace_persistent<false, false, false, 0, kDiffThreads, kDiffRefill>(S.nodes, S.tris, rays, hits, nullptr, 0u, count,
+                                                                      fetch, S.status, nullptr, nullptr, nullptr);
+}
+__global__ void __launch_bounds__(kDiffThreads, kDiffTraceMinBlocks)
+    k_diff_trace_any(SceneView S, const lgb_ray* __restrict__ rays, uint32_t* __restrict__ bits, const uint32_t* count,
+                     uint32_t* fetch) {
+    trace_persistent<true, false, false, 0, kDiffThreads, kDiffRefill>(S.nodes, S.tris, rays, nullptr, bits, 0u, count,
+                                                                     fetch, S.status, nullptr, nullptr, nullptr);
+}
+
+// The camera rays of every sample into queue 0; the replay skips the samples the loop form skips (zero d loss /
+// d pixel, a primal sample marked not finite).
+template <int MODE>
+__global__ void __launch_bounds__(kDiffThreads) k_diff_wave_init(DiffArgs A, DiffWave W) {
+    const float inv = 1.0f / (float)A.spp;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < W.n; i += gridDim.x * blockDim.x) {
+        const uint32_t pix = i % A.npix;
+        v3 total = V3(0.0f);
+        if (MODE == kReplayTotal) {
+            const float4 di = A.dimage[pix];
+            if (di.x * inv == 0.0f && di.y * inv == 0.0f && di.z * inv == 0.0f) continue;
+            const float4 tot = A.primal[i];
+            if (tot.w == 0.0f) continue;
+            total = V3(tot.x, tot.y, tot.z);
+        }
+        const DPath P = diff_begin(A, pix, A.frame0 + i / A.npix, total);
+        store_dpath(W, i, P);
+        push_diff_ray(W, 0, W.counts, i, P);
+    }
+}
+
+// One pass over the vertices of bounce `depth`: PHASE kPhaseRays records their rays, kPhaseResults completes them.
+template <int MODE, uint32_t MASK, int PHASE>
+__global__ void __launch_bounds__(kDiffThreads, kDiffMinBlocks) k_diff_wave(SceneView S, DiffArgs A, DiffWave W, int depth) {
+    __shared__ float sh_grad[4 * kDiffRegMaterials];
+    constexpr bool GRAD = MODE != kPrimal && PHASE == kPhaseResults;
+    GradAcc g{sh_grad, sh_grad + kDiffRegMaterials};
+    if (GRAD) {
+        for (int t = threadIdx.x; t < 4 * kDiffRegMaterials; t += blockDim.x) sh_grad[t] = 0.0f;
+        __syncthreads();
+    }
+    const uint32_t n = W.counts[depth];
+    const int q = depth & 1;
+    const float inv = 1.0f / (float)A.spp;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t i = W.qidx[q][j];
+        DPath P = load_dpath(W, A, i);
+        const lgb_hit hh = W.hits[j];
+        const DiffHit ph{hh.prim, hh.t, hh.u, hh.v};
+        v3 delta = V3(0.0f);
+        if (MODE != kPrimal) {
+            const float4 di = A.dimage[i % A.npix];
+            delta = V3(di.x * inv, di.y * inv, di.z * inv);
+        }
+        VertexIO io;
+        if (PHASE == kPhaseRays) {
+            io.sray[0] = io.mray[0] = make_float4(0.0f, 0.0f, 0.0f, 1.0f);  // tmin > tmax: no ray
+            io.sray[1] = io.mray[1] = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+        } else {
+            io.occluded = ((W.sbits[j >> 5] >> (j & 31u)) & 1u) != 0u;
+            const lgb_hit mh = W.mhits[j];
+            io.mhit = DiffHit{mh.prim, mh.t, mh.u, mh.v};
+        }
+        const int r = diff_vertex<MODE, MASK, PHASE>(S, A, P, depth, ph, nullptr, delta, g, io);
+        if (PHASE == kPhaseRays) {
+            float4* sr = reinterpret_cast<float4*>(&W.srays[j]);
+            float4* mr = reinterpret_cast<float4*>(&W.mrays[j]);
+            sr[0] = io.sray[0]; sr[1] = io.sray[1];
+            mr[0] = io.mray[0]; mr[1] = io.mray[1];
+        } else if (r == kStepContinue) {
+            store_dpath(W, i, P);
+            push_diff_ray(W, q ^ 1, W.counts + depth + 1, i, P);
+        } else if (MODE == kPrimal) {
+            // a sample whose radiance is not finite counts as zero and is marked (w = 0) so the replay skips it;
+            // Lumen's film drops such samples (path.rgen:102-104)
+            const v3 L = P.L;
+            const bool ok = isfinite(L.x) && isfinite(L.y) && isfinite(L.z);
+            A.samples[i] = ok ? make_float4(L.x, L.y, L.z, 1.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+    }
+    if (GRAD) {
+        __syncthreads();
+        const uint32_t nm = min(A.num_materials, (uint32_t)kDiffRegMaterials);
+        for (uint32_t t = threadIdx.x; t < nm; t += blockDim.x) {
+            if (A.rough && sh_grad[t] != 0.0f) atomicAdd(&A.g_rough[t], sh_grad[t]);
+            if (A.emis) {
+                for (int c = 0; c < 3; c++) {
+                    const float e = sh_grad[kDiffRegMaterials + 3 * t + c];
+                    if (e != 0.0f) atomicAdd(&A.g_emis[3 * t + c], e);
+                }
+            }
+        }
+    }
+}
+
 // Film = mean of the spp samples of each pixel, summed in frame order.
 __global__ void k_mean(const float4* __restrict__ samples, uint32_t npix, uint32_t spp, float4* __restrict__ film) {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
@@ -606,6 +825,70 @@ int diff_grid(Ctx* ctx, uint32_t n) {
     return (int)std::min<uint32_t>((n + kDiffThreads - 1) / kDiffThreads, (uint32_t)sms * 16u);
 }
 
+size_t align256d(size_t x) { return (x + 255) & ~(size_t)255; }
+
+template <int MODE, uint32_t MASK>
+void diff_wave_passes(Scene* s, const DiffArgs& A, const DiffWave& W, int bounces, int grid, int trace_grid, cudaStream_t cs) {
+    const SceneView S = scene_view(s);
+    for (int d = 0; d < bounces; d++) {
+        uint32_t* f = W.counts + (kDiffMaxDepth + 1) + 3 * d;  // fetch counters of the bounce's three traversals
+        k_diff_trace<<<trace_grid, kDiffThreads, 0, cs>>>(S, W.rays[d & 1], W.hits, W.counts + d, f);
+        k_diff_wave<MODE, MASK, kPhaseRays><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d);
+        cudaMemsetAsync(W.sbits, 0, 4ull * ((W.n + 31) / 32), cs);
+        k_diff_trace_any<<<trace_grid, kDiffThreads, 0, cs>>>(S, W.srays, W.sbits, W.counts + d, f + 1);
+        k_diff_trace<<<trace_grid, kDiffThreads, 0, cs>>>(S, W.mrays, W.mhits, W.counts + d, f + 2);
+        k_diff_wave<MODE, MASK, kPhaseResults><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d);
+    }
+}
+
+// The wavefront form (kPrimal or kReplayTotal) of one lgb_diff_render / lgb_adjoint_path call.
+template <int MODE>
+lgb_status diff_wave(Scene* s, const DiffArgs& A, cudaStream_t cs) {
+    Ctx* ctx = s->ctx;
+    DiffWave W;
+    W.n = A.npix * A.spp;
+    const size_t n = W.n;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { const size_t o = off; off += align256d(bytes); return o; };
+    const size_t o_st = take(sizeof(float4) * 6 * n), o_r0 = take(sizeof(lgb_ray) * n), o_r1 = take(sizeof(lgb_ray) * n),
+                 o_q0 = take(4 * n), o_q1 = take(4 * n), o_h = take(sizeof(lgb_hit) * n), o_sr = take(sizeof(lgb_ray) * n),
+                 o_sb = take(4 * ((n + 31) / 32)), o_mr = take(sizeof(lgb_ray) * n), o_mh = take(sizeof(lgb_hit) * n),
+                 o_c = take(4 * (size_t)(kDiffMaxDepth + 1 + 3 * kDiffMaxDepth));
+    if (s->diffw_buf_bytes < off) {
+        cudaFree(s->diffw_buf);
+        s->diffw_buf = nullptr;
+        s->diffw_buf_bytes = 0;
+        LGB_CUDA_TRY(ctx, cudaMalloc(&s->diffw_buf, off));
+        s->diffw_buf_bytes = off;
+    }
+    char* b = (char*)s->diffw_buf;
+    W.st = reinterpret_cast<float4*>(b + o_st);
+    W.rays[0] = reinterpret_cast<lgb_ray*>(b + o_r0);
+    W.rays[1] = reinterpret_cast<lgb_ray*>(b + o_r1);
+    W.qidx[0] = reinterpret_cast<uint32_t*>(b + o_q0);
+    W.qidx[1] = reinterpret_cast<uint32_t*>(b + o_q1);
+    W.hits = reinterpret_cast<lgb_hit*>(b + o_h);
+    W.srays = reinterpret_cast<lgb_ray*>(b + o_sr);
+    W.sbits = reinterpret_cast<uint32_t*>(b + o_sb);
+    W.mrays = reinterpret_cast<lgb_ray*>(b + o_mr);
+    W.mhits = reinterpret_cast<lgb_hit*>(b + o_mh);
+    W.counts = reinterpret_cast<uint32_t*>(b + o_c);
+    LGB_CUDA_TRY(ctx, cudaMemsetAsync(W.counts, 0, 4 * (size_t)(kDiffMaxDepth + 1 + 3 * kDiffMaxDepth), cs));
+    const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
+    const int grid = diff_grid(ctx, W.n);
+    int tb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tb, k_diff_trace, kDiffThreads, 0) != cudaSuccess || tb < 1) tb = 1;
+    const int trace_grid = (int)std::min<uint64_t>((n + kDiffThreads - 1) / kDiffThreads, (uint64_t)tb * sms);
+    // a path ends at depth max_depth - 1 at the latest (path.rgen:60)
+    const int bounces = std::max(1, std::min(A.max_depth, kDiffMaxDepth));
+    k_diff_wave_init<MODE><<<grid, kDiffThreads, 0, cs>>>(A, W);
+    constexpr uint32_t kDC = LGB_BSDF_DIFFUSE | LGB_BSDF_CONDUCTOR;
+    if ((s->bsdf_mask & ~kDC) == 0) diff_wave_passes<MODE, kDC>(s, A, W, bounces, grid, trace_grid, cs);
+    else diff_wave_passes<MODE, sh::kAllBsdfs>(s, A, W, bounces, grid, trace_grid, cs);
+    LGB_CUDA_TRY(ctx, cudaGetLastError());
+    return LGB_OK;
+}
+
 }  // namespace
 
 extern "C" LGB_API lgb_status lgb_diff_render(lgb_scene* s, const lgb_camera* cam, const lgb_path_params* p,
@@ -632,7 +915,8 @@ extern "C" LGB_API lgb_status lgb_diff_render(lgb_scene* s, const lgb_camera* ca
         A.samples = reinterpret_cast<float4*>(s->diff_buf);
     }
     const cudaStream_t cs = (cudaStream_t)stream;
-    launch_diff<kPrimal>(s, A, diff_grid(s->ctx, A.npix * spp), cs);
+    st = diff_wave<kPrimal>(s, A, cs);
+    if (st != LGB_OK) return st;
     k_mean<<<diff_grid(s->ctx, A.npix), kDiffThreads, 0, cs>>>(A.samples, A.npix, spp, reinterpret_cast<float4*>(d_film));
     LGB_CUDA_TRY(s->ctx, cudaGetLastError());
     return LGB_OK;
@@ -663,8 +947,12 @@ extern "C" LGB_API lgb_status lgb_adjoint_path(lgb_scene* s, const lgb_camera* c
     A.g_emis = grads->emission;
     const cudaStream_t cs = (cudaStream_t)stream;
     const int grid = diff_grid(s->ctx, A.npix * spp);
-    if (A.primal) launch_diff<kReplayTotal>(s, A, grid, cs);
-    else launch_diff<kReplaySuffix>(s, A, grid, cs);
+    if (A.primal) {
+        st = diff_wave<kReplayTotal>(s, A, cs);
+        if (st != LGB_OK) return st;
+    } else {
+        launch_diff<kReplaySuffix>(s, A, grid, cs);
+    }
     LGB_CUDA_TRY(s->ctx, cudaGetLastError());
     return LGB_OK;
 }

@@ -121,6 +121,8 @@ struct Scene {
     void* capture_stream = nullptr;  // private stream used only to record graphs
     void* diff_buf = nullptr;        // per-sample radiance of the differentiable renderer
     size_t diff_buf_bytes = 0;
+    void* diffw_buf = nullptr;       // wavefront state of the differentiable renderer (paths, queues, rays)
+    size_t diffw_buf_bytes = 0;
     void* vcm_buf = nullptr;         // VCM state kept between iterations (light vertices, counts, splats, table)
     size_t vcm_buf_bytes = 0;
     uint32_t vcm_w = 0, vcm_h = 0, vcm_per = 0;

@@ -699,8 +699,12 @@ __global__ void __launch_bounds__(kDiffThreads) k_diff_wave_init(DiffArgs A, Dif
 }
 
 // One pass over the vertices of bounce `depth`: PHASE kPhaseRays records their rays, kPhaseResults completes them.
+// The completion pass runs once per class of BSDF types: it takes the vertices whose material type is in `cls`
+// (a miss, or a type without lobes, counts as `miss_cls`), and MASK keeps only those lobes in the kernel, so each launch's code is a fraction
+// of the loop's (the pass stalls on instruction fetch otherwise).
 template <int MODE, uint32_t MASK, int PHASE>
-__global__ void __launch_bounds__(kDiffThreads, kDiffMinBlocks) k_diff_wave(SceneView S, DiffArgs A, DiffWave W, int depth) {
+__global__ void __launch_bounds__(kDiffThreads, kDiffMinBlocks)
+    k_diff_wave(SceneView S, DiffArgs A, DiffWave W, int depth, uint32_t cls, uint32_t miss_cls) {
     __shared__ float sh_grad[4 * kDiffRegMaterials];
     constexpr bool GRAD = MODE != kPrimal && PHASE == kPhaseResults;
     GradAcc g{sh_grad, sh_grad + kDiffRegMaterials};
@@ -712,9 +716,14 @@ __global__ void __launch_bounds__(kDiffThreads, kDiffMinBlocks) k_diff_wave(Scen
     const int q = depth & 1;
     const float inv = 1.0f / (float)A.spp;
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const lgb_hit hh = W.hits[j];
+        if (PHASE == kPhaseResults) {
+            uint32_t ty = hh.prim == LGB_NO_HIT ? miss_cls : S.mats[S.meshes[S.tri_mesh[hh.prim]].material_index].bsdf_type;
+            if ((ty & sh::kAllBsdfs) == 0u) ty = miss_cls;  // a type without lobes (its BSDF is zero in every class)
+            if ((ty & cls) == 0u) continue;
+        }
         const uint32_t i = W.qidx[q][j];
         DPath P = load_dpath(W, A, i);
-        const lgb_hit hh = W.hits[j];
         const DiffHit ph{hh.prim, hh.t, hh.u, hh.v};
         v3 delta = V3(0.0f);
         if (MODE != kPrimal) {
@@ -827,17 +836,29 @@ int diff_grid(Ctx* ctx, uint32_t n) {
 
 size_t align256d(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// BSDF classes of the completion pass: diffuse, conductor, and the other types together.
+constexpr uint32_t kDiffClsD = LGB_BSDF_DIFFUSE, kDiffClsC = LGB_BSDF_CONDUCTOR;
+constexpr uint32_t kDiffClsRest = sh::kAllBsdfs & ~(LGB_BSDF_DIFFUSE | LGB_BSDF_CONDUCTOR);
+
 template <int MODE, uint32_t MASK>
 void diff_wave_passes(Scene* s, const DiffArgs& A, const DiffWave& W, int bounces, int grid, int trace_grid, cudaStream_t cs) {
     const SceneView S = scene_view(s);
+    const uint32_t used = s->bsdf_mask;
+    // a missed ray is completed by the first class the scene has (its BSDF code is not reached)
+    const uint32_t miss_cls = (used & kDiffClsD) ? kDiffClsD : ((used & kDiffClsC) ? kDiffClsC : kDiffClsRest);
     for (int d = 0; d < bounces; d++) {
         uint32_t* f = W.counts + (kDiffMaxDepth + 1) + 3 * d;  // fetch counters of the bounce's three traversals
         k_diff_trace<<<trace_grid, kDiffThreads, 0, cs>>>(S, W.rays[d & 1], W.hits, W.counts + d, f);
-        k_diff_wave<MODE, MASK, kPhaseRays><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d);
+        k_diff_wave<MODE, MASK, kPhaseRays><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, ~0u, miss_cls);
         cudaMemsetAsync(W.sbits, 0, 4ull * ((W.n + 31) / 32), cs);
         k_diff_trace_any<<<trace_grid, kDiffThreads, 0, cs>>>(S, W.srays, W.sbits, W.counts + d, f + 1);
         k_diff_trace<<<trace_grid, kDiffThreads, 0, cs>>>(S, W.mrays, W.mhits, W.counts + d, f + 2);
-        k_diff_wave<MODE, MASK, kPhaseResults><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d);
+        if ((used | miss_cls) & kDiffClsD)
+            k_diff_wave<MODE, kDiffClsD, kPhaseResults><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, kDiffClsD, miss_cls);
+        if ((used | miss_cls) & kDiffClsC)
+            k_diff_wave<MODE, kDiffClsC, kPhaseResults><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, kDiffClsC, miss_cls);
+        if ((used | miss_cls) & kDiffClsRest)
+            k_diff_wave<MODE, kDiffClsRest, kPhaseResults><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, kDiffClsRest, miss_cls);
     }
 }
 

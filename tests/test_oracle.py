@@ -428,3 +428,24 @@ def test_bdpt_oracle_spot_cone_and_depth(oracle):
     short = _bdpt_frames(oracle, arrays, 24, 24, 8, 2)[2]["film"][:, :3].mean()
     long = _bdpt_frames(oracle, arrays, 24, 24, 8, 8)[2]["film"][:, :3].mean()
     assert 0.0 < short < long
+
+
+def test_bdpt_oracle_every_bsdf_type():
+    """The oracle's BDPT on a loaded scene with diffuse, conductor, dielectric and principled materials, a spot
+    light (a delta light: vertex 0 has pdf_fwd = 0 and is skipped by the MIS sums) and an emissive lamp (an area
+    light), so the s = 1 strategies' MIS weight often reads the flags of a light other than the one they sampled
+    (kept from the reference): deterministic, finite and lit."""
+    import os
+    import oracle_lib
+    from lumen_gb300 import build, host_scene
+    if not os.path.exists(host_scene.HOST_LIB):
+        build.build_library()
+    here = os.path.dirname(os.path.abspath(__file__))
+    arrays, info = host_scene.load_scene(os.path.join(here, "golden", "scenes", "mixed_bdpt.json"))
+    assert int(info.path_length) == 5 and len(arrays.lights) == 2
+    assert sorted(int(f) & 7 for f in arrays.lights["light_flags"]) == [1, 2]  # spot, area
+    assert set(int(t) for t in arrays.materials["bsdf_type"]) >= {1, 8, 16, 32}
+    ora = oracle_lib.Oracle()
+    films = [_bdpt_frames(ora, arrays, 20, 16, 3, 5)[2]["film"] for _ in range(2)]
+    assert np.array_equal(films[0], films[1])
+    assert np.isfinite(films[0]).all() and films[0][:, :3].mean() > 0.0

@@ -238,7 +238,7 @@ class DiffRender(torch.autograd.Function):
 def test_autograd_adam_recovers_target(diff_scene):
     """200 Adam steps from the scene's values towards a target rendered with another seeded texture, other
     roughnesses and another emission; every step uses fresh frames, and the adjoint replays frames independent
-    of the forward's. 256^2 puts about two pixels across each of the 64 x 64 texels; texel recovery is judged
+    of the forward's. 256^2 puts about two pixels across each of the 64 x 64 texels; texel recovery is measured
     on the texels the camera sees best (primary hits)."""
     arrays, sc, _ = diff_scene
     w = h = 256

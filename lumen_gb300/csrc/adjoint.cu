@@ -621,9 +621,15 @@ struct DiffWave {
     uint32_t* sbits;   // their occlusion bits
     lgb_ray* mrays;    // per queue slot: the vertex's BSDF-MIS ray
     lgb_hit* mhits;
-    uint32_t* counts;  // queue lengths per bounce [kDiffMaxDepth + 1], then 3 fetch counters per bounce
+    uint32_t* counts;  // queue lengths per bounce [kDiffMaxDepth + 1], then 3 fetch counters per bounce, then
+                       // the lengths of the 3 BSDF-class lists per bounce
+    uint32_t* cls[3];  // per BSDF class: the queue slots of the bounce's vertices in that class
     uint32_t n;        // samples: npix * spp, sample i = frame (i / npix), pixel (i % npix)
 };
+constexpr int kDiffCountWords = (kDiffMaxDepth + 1) + 3 * kDiffMaxDepth + 3 * kDiffMaxDepth;
+__device__ __forceinline__ uint32_t* class_counts(const DiffWave& W, int depth) {
+    return W.counts + (kDiffMaxDepth + 1) + 3 * kDiffMaxDepth + 3 * depth;
+}
 __device__ __forceinline__ float4* wst(const DiffWave& W, int c, uint32_t i) { return W.st + ((size_t)c * W.n + i); }
 __device__ __forceinline__ void store_dpath(const DiffWave& W, uint32_t i, const DPath& P) {
     *wst(W, 0, i) = f4(P.origin, __uint_as_float(P.seed.w));
@@ -653,6 +659,18 @@ __device__ __forceinline__ uint32_t diff_append(uint32_t* counter) {
     if (lane == leader) first = atomicAdd(counter, (uint32_t)__popc(mask));
     first = __shfl_sync(mask, first, leader);
     return first + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+// One slot of list `c` (of three, counters at `counters`) for each calling lane; lanes with the same list share
+// one atomic.
+__device__ __forceinline__ uint32_t diff_append_to(uint32_t* counters, int c) {
+    const uint32_t mask = __activemask();
+    const uint32_t peers = __match_any_sync(mask, c);
+    const int leader = __ffs(peers) - 1;
+    const int lane = (int)(threadIdx.x & 31u);
+    uint32_t first = 0;
+    if (lane == leader) first = atomicAdd(counters + c, (uint32_t)__popc(peers));
+    first = __shfl_sync(peers, first, leader);
+    return first + (uint32_t)__popc(peers & ((1u << lane) - 1u));
 }
 __device__ __forceinline__ void push_diff_ray(const DiffWave& W, int q, uint32_t* counter, uint32_t i, const DPath& P) {
     const uint32_t j = diff_append(counter);
@@ -698,13 +716,14 @@ __global__ void __launch_bounds__(kDiffThreads) k_diff_wave_init(DiffArgs A, Dif
     }
 }
 
-// One pass over the vertices of bounce `depth`: PHASE kPhaseRays records their rays, kPhaseResults completes them.
-// The completion pass runs once per class of BSDF types: it takes the vertices whose material type is in `cls`
-// (a miss, or a type without lobes, counts as `miss_cls`), and MASK keeps only those lobes in the kernel, so each launch's code is a fraction
-// of the loop's (the pass stalls on instruction fetch otherwise).
+// One pass over the vertices of bounce `depth`: PHASE kPhaseRays records their rays and sorts the vertices into
+// three lists by the class of their material's BSDF type (diffuse, conductor, the rest; a miss or a type without
+// lobes goes to class miss_cls), kPhaseResults completes the vertices of one class (cls). MASK keeps only that
+// class's lobes in the completion kernel, so each launch's code is a fraction of the loop's (the pass stalls on
+// instruction fetch otherwise).
 template <int MODE, uint32_t MASK, int PHASE>
 __global__ void __launch_bounds__(kDiffThreads, kDiffMinBlocks)
-    k_diff_wave(SceneView S, DiffArgs A, DiffWave W, int depth, uint32_t cls, uint32_t miss_cls) {
+    k_diff_wave(SceneView S, DiffArgs A, DiffWave W, int depth, int cls, int miss_cls) {
     __shared__ float sh_grad[4 * kDiffRegMaterials];
     constexpr bool GRAD = MODE != kPrimal && PHASE == kPhaseResults;
     GradAcc g{sh_grad, sh_grad + kDiffRegMaterials};
@@ -712,16 +731,12 @@ __global__ void __launch_bounds__(kDiffThreads, kDiffMinBlocks)
         for (int t = threadIdx.x; t < 4 * kDiffRegMaterials; t += blockDim.x) sh_grad[t] = 0.0f;
         __syncthreads();
     }
-    const uint32_t n = W.counts[depth];
+    const uint32_t n = PHASE == kPhaseResults ? class_counts(W, depth)[cls] : W.counts[depth];
     const int q = depth & 1;
     const float inv = 1.0f / (float)A.spp;
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const uint32_t j = PHASE == kPhaseResults ? W.cls[cls][t] : t;
         const lgb_hit hh = W.hits[j];
-        if (PHASE == kPhaseResults) {
-            uint32_t ty = hh.prim == LGB_NO_HIT ? miss_cls : S.mats[S.meshes[S.tri_mesh[hh.prim]].material_index].bsdf_type;
-            if ((ty & sh::kAllBsdfs) == 0u) ty = miss_cls;  // a type without lobes (its BSDF is zero in every class)
-            if ((ty & cls) == 0u) continue;
-        }
         const uint32_t i = W.qidx[q][j];
         DPath P = load_dpath(W, A, i);
         const DiffHit ph{hh.prim, hh.t, hh.u, hh.v};
@@ -745,6 +760,9 @@ __global__ void __launch_bounds__(kDiffThreads, kDiffMinBlocks)
             float4* mr = reinterpret_cast<float4*>(&W.mrays[j]);
             sr[0] = io.sray[0]; sr[1] = io.sray[1];
             mr[0] = io.mray[0]; mr[1] = io.mray[1];
+            const uint32_t ty = hh.prim == LGB_NO_HIT ? 0u : S.mats[S.meshes[S.tri_mesh[hh.prim]].material_index].bsdf_type;
+            const int c = (ty & LGB_BSDF_DIFFUSE) ? 0 : ((ty & LGB_BSDF_CONDUCTOR) ? 1 : ((ty & sh::kAllBsdfs) ? 2 : miss_cls));
+            W.cls[c][diff_append_to(class_counts(W, depth), c)] = j;
         } else if (r == kStepContinue) {
             store_dpath(W, i, P);
             push_diff_ray(W, q ^ 1, W.counts + depth + 1, i, P);
@@ -844,21 +862,20 @@ template <int MODE, uint32_t MASK>
 void diff_wave_passes(Scene* s, const DiffArgs& A, const DiffWave& W, int bounces, int grid, int trace_grid, cudaStream_t cs) {
     const SceneView S = scene_view(s);
     const uint32_t used = s->bsdf_mask;
-    // a missed ray is completed by the first class the scene has (its BSDF code is not reached)
-    const uint32_t miss_cls = (used & kDiffClsD) ? kDiffClsD : ((used & kDiffClsC) ? kDiffClsC : kDiffClsRest);
+    // misses and types without lobes are completed with the first class the scene has (no BSDF code is reached)
+    const int miss_cls = (used & kDiffClsD) ? 0 : ((used & kDiffClsC) ? 1 : 2);
+    const bool has[3] = {(used & kDiffClsD) != 0u || miss_cls == 0, (used & kDiffClsC) != 0u || miss_cls == 1,
+                         (used & kDiffClsRest) != 0u || miss_cls == 2};
     for (int d = 0; d < bounces; d++) {
         uint32_t* f = W.counts + (kDiffMaxDepth + 1) + 3 * d;  // fetch counters of the bounce's three traversals
         k_diff_trace<<<trace_grid, kDiffThreads, 0, cs>>>(S, W.rays[d & 1], W.hits, W.counts + d, f);
-        k_diff_wave<MODE, MASK, kPhaseRays><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, ~0u, miss_cls);
+        k_diff_wave<MODE, MASK, kPhaseRays><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, -1, miss_cls);
         cudaMemsetAsync(W.sbits, 0, 4ull * ((W.n + 31) / 32), cs);
         k_diff_trace_any<<<trace_grid, kDiffThreads, 0, cs>>>(S, W.srays, W.sbits, W.counts + d, f + 1);
         k_diff_trace<<<trace_grid, kDiffThreads, 0, cs>>>(S, W.mrays, W.mhits, W.counts + d, f + 2);
-        if ((used | miss_cls) & kDiffClsD)
-            k_diff_wave<MODE, kDiffClsD, kPhaseResults><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, kDiffClsD, miss_cls);
-        if ((used | miss_cls) & kDiffClsC)
-            k_diff_wave<MODE, kDiffClsC, kPhaseResults><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, kDiffClsC, miss_cls);
-        if ((used | miss_cls) & kDiffClsRest)
-            k_diff_wave<MODE, kDiffClsRest, kPhaseResults><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, kDiffClsRest, miss_cls);
+        if (has[0]) k_diff_wave<MODE, kDiffClsD, kPhaseResults><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, 0, miss_cls);
+        if (has[1]) k_diff_wave<MODE, kDiffClsC, kPhaseResults><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, 1, miss_cls);
+        if (has[2]) k_diff_wave<MODE, kDiffClsRest, kPhaseResults><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, 2, miss_cls);
     }
 }
 
@@ -874,7 +891,7 @@ lgb_status diff_wave(Scene* s, const DiffArgs& A, cudaStream_t cs) {
     const size_t o_st = take(sizeof(float4) * 6 * n), o_r0 = take(sizeof(lgb_ray) * n), o_r1 = take(sizeof(lgb_ray) * n),
                  o_q0 = take(4 * n), o_q1 = take(4 * n), o_h = take(sizeof(lgb_hit) * n), o_sr = take(sizeof(lgb_ray) * n),
                  o_sb = take(4 * ((n + 31) / 32)), o_mr = take(sizeof(lgb_ray) * n), o_mh = take(sizeof(lgb_hit) * n),
-                 o_c = take(4 * (size_t)(kDiffMaxDepth + 1 + 3 * kDiffMaxDepth));
+                 o_c = take(4 * (size_t)kDiffCountWords), o_l0 = take(4 * n), o_l1 = take(4 * n), o_l2 = take(4 * n);
     if (s->diffw_buf_bytes < off) {
         cudaFree(s->diffw_buf);
         s->diffw_buf = nullptr;
@@ -894,7 +911,10 @@ lgb_status diff_wave(Scene* s, const DiffArgs& A, cudaStream_t cs) {
     W.mrays = reinterpret_cast<lgb_ray*>(b + o_mr);
     W.mhits = reinterpret_cast<lgb_hit*>(b + o_mh);
     W.counts = reinterpret_cast<uint32_t*>(b + o_c);
-    LGB_CUDA_TRY(ctx, cudaMemsetAsync(W.counts, 0, 4 * (size_t)(kDiffMaxDepth + 1 + 3 * kDiffMaxDepth), cs));
+    W.cls[0] = reinterpret_cast<uint32_t*>(b + o_l0);
+    W.cls[1] = reinterpret_cast<uint32_t*>(b + o_l1);
+    W.cls[2] = reinterpret_cast<uint32_t*>(b + o_l2);
+    LGB_CUDA_TRY(ctx, cudaMemsetAsync(W.counts, 0, 4 * (size_t)kDiffCountWords, cs));
     const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
     const int grid = diff_grid(ctx, W.n);
     int tb = 0;

@@ -187,7 +187,7 @@ struct Sampled {
 // calc_mis_weight (bdpt_commons.glsl:269-471) on copies of the two subpaths: the reference patches the
 // path buffers in place and restores them afterwards.
 float mis_weight(const Ctx& X, int s, int t, const Sampled& sampled, const PV* Lp, const PV* Cp) {
-    if (s + t == 2) return 1.0f;
+    if (s + t == 2 || (X.p->check_flags & 2u)) return 1.0f;
     PV L[130], C[130];
     for (int i = 0; i < s; i++) L[i] = Lp[i];
     for (int i = 0; i < t; i++) C[i] = Cp[i];
@@ -395,6 +395,11 @@ void pixel(const Ctx& X, uint32_t x, uint32_t y, PixelOut& out) {
         for (int s = 0; s <= nl; s++) {
             const int depth = s + t - 2;
             if (depth > X.p->max_depth - 1 || depth < 0 || (s == 1 && t == 1)) continue;
+            if ((X.p->check_flags & 1u) &&
+                (s + t - 1 != X.p->check_len || (X.p->check_s >= 0 && s != X.p->check_s))) {
+                if (s == 1 && t >= 2) seed.w += 4u;  // the draws of bdpt_connect's light sample
+                continue;
+            }
             if (t == 1) {
                 int32_t cx = 0, cy = 0;
                 bool have = false;

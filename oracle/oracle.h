@@ -200,6 +200,12 @@ struct orc_bdpt_params {
     uint32_t seed;                 // RNG frame value = frame_num ^ seed
     uint32_t frame_num;
     float spot_angle;              // degrees, 0 = the fixed 30 / 25 degree cone
+    // Consistency checks of the restatement (0 = the integrator as the reference runs it). Bit 0: only the
+    // strategies with path length s + t - 1 == check_len (and s == check_s when check_s >= 0) contribute; a
+    // skipped s = 1 strategy still draws its four random numbers, so the others see the same ones. Bit 1: every
+    // MIS weight is 1 (each strategy's own unweighted estimate).
+    uint32_t check_flags;
+    int32_t check_len, check_s;
 };
 void orc_bdpt_iteration(void* scene, const float inv_view[16], const float inv_proj[16], const float view[16],
                         const float proj[16], uint32_t width, uint32_t height, const orc_bdpt_params* p, float* film,

@@ -65,7 +65,8 @@ class RestirParams(C.Structure):
 
 class BdptParams(C.Structure):
     _fields_ = [("max_depth", C.c_int32), ("num_lights", C.c_int32), ("light_triangle_count", C.c_int32),
-                ("seed", C.c_uint32), ("frame_num", C.c_uint32), ("spot_angle", C.c_float)]
+                ("seed", C.c_uint32), ("frame_num", C.c_uint32), ("spot_angle", C.c_float),
+                ("check_flags", C.c_uint32), ("check_len", C.c_int32), ("check_s", C.c_int32)]
 
 
 VCM_VERTEX_BYTES = 104

@@ -385,7 +385,7 @@ def test_restir_oracle_is_deterministic_and_matches_direct_light(oracle):
     assert 0.6 * direct < min(levels) and max(levels) < 1.1 * direct, (levels, direct)
 
 
-def _bdpt_frames(oracle, arrays, w, h, frames, depth=6, seed=7, spot_angle=0.0):
+def _bdpt_frames(oracle, arrays, w, h, frames, depth=6, seed=7, spot_angle=0.0, check=(0, 0, -1)):
     import oracle_lib
     from lumen_gb300.scene import camera_forward, camera_lookat
     sc = oracle.scene(arrays)
@@ -396,6 +396,7 @@ def _bdpt_frames(oracle, arrays, w, h, frames, depth=6, seed=7, spot_angle=0.0):
         p = oracle_lib.BdptParams()
         p.max_depth, p.num_lights, p.light_triangle_count = depth, len(arrays.lights), arrays.light_triangle_count
         p.seed, p.frame_num, p.spot_angle = seed, f, spot_angle
+        p.check_flags, p.check_len, p.check_s = check
         oracle_lib.bdpt_iteration(sc, cam, view, proj, p, st)
     return sc, cam, st
 
@@ -449,3 +450,22 @@ def test_bdpt_oracle_every_bsdf_type():
     films = [_bdpt_frames(ora, arrays, 20, 16, 3, 5)[2]["film"] for _ in range(2)]
     assert np.array_equal(films[0], films[1])
     assert np.isfinite(films[0]).all() and films[0][:, :3].mean() > 0.0
+
+
+def test_bdpt_oracle_strategies_agree(oracle):
+    """No Lumen output exists to pin the BDPT restatement, so its pdfs and MIS weights are checked against each
+    other. For paths of 2 and 3 segments on the Cornell box, each connection strategy alone (MIS weight 1: light
+    tracing, vertex connections, next-event estimation, the camera path hitting the emitter) is an estimate of
+    the same radiance, and so is the MIS-weighted sum over them: all agree within 10 % at 64 frames of 32 x 32
+    (observed within 4 %). Restricting the film to one strategy keeps the random numbers of the others, so the
+    weighted parts add up to the weighted total to rounding."""
+    cb = procedural.cornell_box()
+    mean = lambda check: float(_bdpt_frames(oracle, cb, 32, 32, 64, check=check)[2]["film"][:, :3].mean())
+    for k in (2, 3):
+        total = mean((1, k, -1))
+        assert total > 0.0
+        for s in range(k + 1):
+            alone = mean((3, k, s))
+            assert abs(alone / total - 1.0) < 0.10, (k, s, alone, total)
+        parts = sum(mean((1, k, s)) for s in range(k + 1))
+        assert abs(parts - total) <= 1e-5 * total, (k, parts, total)

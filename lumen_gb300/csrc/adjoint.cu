@@ -613,7 +613,7 @@ void launch_diff(Scene* s, const DiffArgs& A, int grid, cudaStream_t cs) {
 // of it), so a sample's arithmetic and random numbers are the loop's; the instruction footprint of each kernel is a
 // fraction of the loop's.
 struct DiffWave {
-    float4* st;        // sample state, 6 float4 per sample: (origin, rng) (dir, last_spec) (Tv) (Tc) (L) (rem)
+    float4* st;        // sample state, 6 consecutive float4 per sample: (origin, rng) (dir, last_spec) (Tv) (Tc) (L) (rem)
     lgb_ray* rays[2];  // ray queues of consecutive bounces
     uint32_t* qidx[2]; // sample of each queued ray
     lgb_hit* hits;
@@ -630,7 +630,9 @@ constexpr int kDiffCountWords = (kDiffMaxDepth + 1) + 3 * kDiffMaxDepth + 3 * kD
 __device__ __forceinline__ uint32_t* class_counts(const DiffWave& W, int depth) {
     return W.counts + (kDiffMaxDepth + 1) + 3 * kDiffMaxDepth + 3 * depth;
 }
-__device__ __forceinline__ float4* wst(const DiffWave& W, int c, uint32_t i) { return W.st + ((size_t)c * W.n + i); }
+// A sample's 96 B of state are contiguous: the completion passes visit samples out of queue order (per-class
+// lists), and a scattered sample then costs three full 32 B sectors.
+__device__ __forceinline__ float4* wst(const DiffWave& W, int c, uint32_t i) { return W.st + ((size_t)i * 6 + c); }
 __device__ __forceinline__ void store_dpath(const DiffWave& W, uint32_t i, const DPath& P) {
     *wst(W, 0, i) = f4(P.origin, __uint_as_float(P.seed.w));
     *wst(W, 1, i) = f4(P.dir, __uint_as_float(P.last_spec ? 1u : 0u));

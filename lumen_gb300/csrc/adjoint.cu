@@ -536,9 +536,10 @@ __device__ v3 diff_path(const SceneView& S, const DiffArgs& A, uint32_t pix, uin
     return P.L;
 }
 
-// MODE kPrimal writes each sample's radiance; kReplaySuffix re-runs the primal in the thread (kRecord, keeping
-// the per-depth radiance in local memory) and then replays; kReplayTotal replays once from the stored radiance
-// of each sample.
+// The loop form, one thread per sample. MODE kPrimal writes each sample's radiance; kReplaySuffix re-runs the
+// primal in the thread (kRecord, keeping the per-depth radiance in local memory) and then replays; kReplayTotal
+// replays once from the stored radiance of each sample. The library runs kPrimal and kReplayTotal as wavefronts
+// (diff_wave below) and this kernel for kReplaySuffix, the replay without stored samples.
 template <int MODE, uint32_t MASK>
 __global__ void __launch_bounds__(kDiffThreads, kDiffMinBlocks) k_diff(SceneView S, DiffArgs A) {
     __shared__ float sh_grad[4 * kDiffRegMaterials];

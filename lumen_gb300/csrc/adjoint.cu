@@ -862,7 +862,8 @@ constexpr uint32_t kDiffClsD = LGB_BSDF_DIFFUSE, kDiffClsC = LGB_BSDF_CONDUCTOR;
 constexpr uint32_t kDiffClsRest = sh::kAllBsdfs & ~(LGB_BSDF_DIFFUSE | LGB_BSDF_CONDUCTOR);
 
 template <int MODE, uint32_t MASK>
-void diff_wave_passes(Scene* s, const DiffArgs& A, const DiffWave& W, int bounces, int grid, int trace_grid, cudaStream_t cs) {
+cudaError_t diff_wave_passes(Scene* s, const DiffArgs& A, const DiffWave& W, int bounces, int grid, int trace_grid,
+                             cudaStream_t cs) {
     const SceneView S = scene_view(s);
     const uint32_t used = s->bsdf_mask;
     // misses and types without lobes are completed with the first class the scene has (no BSDF code is reached)
@@ -873,13 +874,17 @@ void diff_wave_passes(Scene* s, const DiffArgs& A, const DiffWave& W, int bounce
         uint32_t* f = W.counts + (kDiffMaxDepth + 1) + 3 * d;  // fetch counters of the bounce's three traversals
         k_diff_trace<<<trace_grid, kDiffThreads, 0, cs>>>(S, W.rays[d & 1], W.hits, W.counts + d, f);
         k_diff_wave<MODE, MASK, kPhaseRays><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, -1, miss_cls);
-        cudaMemsetAsync(W.sbits, 0, 4ull * ((W.n + 31) / 32), cs);
+        const cudaError_t me = cudaMemsetAsync(W.sbits, 0, 4ull * ((W.n + 31) / 32), cs);
+        if (me != cudaSuccess) return me;
         k_diff_trace_any<<<trace_grid, kDiffThreads, 0, cs>>>(S, W.srays, W.sbits, W.counts + d, f + 1);
         k_diff_trace<<<trace_grid, kDiffThreads, 0, cs>>>(S, W.mrays, W.mhits, W.counts + d, f + 2);
         if (has[0]) k_diff_wave<MODE, kDiffClsD, kPhaseResults><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, 0, miss_cls);
         if (has[1]) k_diff_wave<MODE, kDiffClsC, kPhaseResults><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, 1, miss_cls);
         if (has[2]) k_diff_wave<MODE, kDiffClsRest, kPhaseResults><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, 2, miss_cls);
+        const cudaError_t le = cudaGetLastError();
+        if (le != cudaSuccess) return le;
     }
+    return cudaSuccess;
 }
 
 // The wavefront form (kPrimal or kReplayTotal) of one lgb_diff_render / lgb_adjoint_path call.
@@ -927,8 +932,8 @@ lgb_status diff_wave(Scene* s, const DiffArgs& A, cudaStream_t cs) {
     const int bounces = std::max(1, std::min(A.max_depth, kDiffMaxDepth));
     k_diff_wave_init<MODE><<<grid, kDiffThreads, 0, cs>>>(A, W);
     constexpr uint32_t kDC = LGB_BSDF_DIFFUSE | LGB_BSDF_CONDUCTOR;
-    if ((s->bsdf_mask & ~kDC) == 0) diff_wave_passes<MODE, kDC>(s, A, W, bounces, grid, trace_grid, cs);
-    else diff_wave_passes<MODE, sh::kAllBsdfs>(s, A, W, bounces, grid, trace_grid, cs);
+    if ((s->bsdf_mask & ~kDC) == 0) LGB_CUDA_TRY(ctx, (diff_wave_passes<MODE, kDC>(s, A, W, bounces, grid, trace_grid, cs)));
+    else LGB_CUDA_TRY(ctx, (diff_wave_passes<MODE, sh::kAllBsdfs>(s, A, W, bounces, grid, trace_grid, cs)));
     LGB_CUDA_TRY(ctx, cudaGetLastError());
     return LGB_OK;
 }

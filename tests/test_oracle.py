@@ -469,3 +469,15 @@ def test_bdpt_oracle_strategies_agree(oracle):
             assert abs(alone / total - 1.0) < 0.10, (k, s, alone, total)
         parts = sum(mean((1, k, s)) for s in range(k + 1))
         assert abs(parts - total) <= 1e-5 * total, (k, parts, total)
+
+
+def test_bdpt_oracle_path_length_one_known_answer(oracle):
+    """With path length 1 the only strategy is the camera ray hitting the emitter (s = 0, t = 2: throughput 1, MIS
+    weight 1, bdpt.rgen:52-58), so every pixel of the film is exactly the emission of what its centre sees: 17 on
+    the Cornell box's emitter, 0 elsewhere, in every frame."""
+    cb = procedural.cornell_box()
+    film = _bdpt_frames(oracle, cb, 32, 32, 3, depth=1)[2]["film"][:, :3]
+    lit = (film > 0.0).any(axis=1)
+    assert lit.sum() > 0
+    assert np.array_equal(film[lit], np.full((int(lit.sum()), 3), 17.0, np.float32))
+    assert not film[~lit].any()

@@ -292,6 +292,20 @@ def _vcm_oracle_run(oracle, arrays, w, h, iters, depth, flags, use_vm=1, spot_an
     return sc, cam, st
 
 
+
+def test_vcm_oracle_max_depth_one_known_answer(oracle):
+    """At max depth 1 every subpath has one segment: the light pass stops before its camera connection
+    (vcm_commons.glsl:367-372), the eye pass's light connection needs depth < max_depth (:565), and a merge's
+    path length (:269) exceeds the maximum. So each pixel's single sample is exactly the emission its jittered
+    camera ray sees: 17 on the Cornell box's emitter, else 0 (black sky), and no splat is written."""
+    cb = procedural.cornell_box()
+    _, _, st = _vcm_oracle_run(oracle, cb, 32, 32, 1, 1, 0)
+    film = st["film"][:, :3]
+    lit = (film > 0.0).any(axis=1)
+    assert lit.sum() > 0
+    assert np.array_equal(film[lit], np.full((int(lit.sum()), 3), 17.0, np.float32))
+    assert not film[~lit].any() and not st["splat"].any()
+
 def test_vcm_oracle_is_deterministic_and_energy_consistent(oracle):
     """With every connection accumulated (LGB_VCM_ACCUMULATE) and a non-reflecting emitter, VCM converges to the
     path tracer's image. (With the white emitter of the Cornell box the path tracer itself gains energy from its

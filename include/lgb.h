@@ -194,6 +194,12 @@ LGB_API lgb_status lgb_trace_closest(lgb_scene* scene, const lgb_ray* d_rays, lg
                                      void* stream);
 LGB_API lgb_status lgb_trace_any(lgb_scene* scene, const lgb_ray* d_rays, uint32_t* d_occluded_bits, uint32_t n,
                                  void* stream);
+/* Node-visit budget of one ray in this scene's lgb_trace_closest / lgb_trace_any queries (device, host-buffer and
+ * counted forms). 0 restores the default, 2^22 visits, which no well-formed tree reaches. A ray that runs out of
+ * budget ends with what it has found so far and sets bit 2 of the scene's device status word; the next lgb_sync
+ * returns LGB_ERR_DEVICE_STATUS and clears the word. No counterpart in Lumen (the driver bounds its own
+ * traversal): it lets a caller exercise that error path on a sound tree, with nothing faulting or hanging. */
+LGB_API lgb_status lgb_scene_set_visit_limit(lgb_scene* scene, uint32_t max_visits);
 /* Same query as lgb_trace_closest, also adding the 8-wide nodes and triangles each ray fetched into
  * d_counters[0] and d_counters[1] (device uint64). For bytes-per-ray accounting. */
 LGB_API lgb_status lgb_trace_closest_counted(lgb_scene* scene, const lgb_ray* d_rays, lgb_hit* d_hits, uint32_t n,
@@ -224,7 +230,9 @@ LGB_API lgb_status lgb_render_path(lgb_scene* scene, const lgb_camera* camera, c
  * library holds until exit, so images are limited to 16384 pixels (e.g. 128 x 128) and larger ones are
  * rejected with LGB_ERR_INVALID_ARGUMENT. All calls share that array: calls that overlap on the GPU race,
  * so order them on one stream. The first call on a device looks the array up; make it before any stream
- * capture. */
+ * capture. The address is looked up once per device for the life of the process: after cudaDeviceReset (or
+ * anything else that destroys and recreates the device's primary context) it is stale, so do not call this
+ * entry point again in that process. */
 LGB_API lgb_status lgb_render_path_noalloc(lgb_scene* scene, const lgb_camera* camera, const lgb_path_params* params,
                                            uint32_t frame0, uint32_t spp, float* d_film, void* stream);
 
@@ -315,6 +323,24 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* scene, const lgb_camera* camera,
 LGB_API lgb_status lgb_vcm_grid(lgb_ctx* ctx, const float* d_pos4, uint32_t n, const float scene_min[3],
                                 const float scene_max[3], float radius, uint32_t screen_size, uint32_t* d_count,
                                 uint32_t* d_rep, void* stream);
+
+/* The VCM state a scene keeps between iterations, as device pointers owned by the scene (valid until the next
+ * lgb_vcm_iteration with another image size or max_depth, or lgb_scene_destroy). Lumen keeps the same data in
+ * its "VCM Light Vertices", "Light Path Count" and "Photon Buffer" buffers (VCM.cpp:11-31). For inspection
+ * and tests: read them after the iteration's stream has finished. */
+typedef struct lgb_vcm_state {
+    const float* vertices;          /* 6 float4 per light vertex, vertex k of light subpath i at i * per_path + k;
+                                       the first float4 holds the position */
+    const uint32_t* path_counts;    /* stored vertices per light subpath (screen entries) */
+    const uint32_t* table_count;    /* photons per hash slot (table_size entries) */
+    const uint32_t* table_rep;      /* per slot, the index of the last vertex in vertex order */
+    uint32_t screen, per_path, table_size;
+    int32_t grid_res[3];            /* cells per axis of the last iteration's grid */
+    float radius;                   /* merge radius of the last iteration */
+    float scene_min[3], scene_max[3];
+    uint32_t reserved;
+} lgb_vcm_state;
+LGB_API lgb_status lgb_vcm_state_get(const lgb_scene* scene, lgb_vcm_state* out);
 
 /* The forward matrices of a camera (view and projection, column-major), inverted in double from the camera's
  * inverse matrices and rounded to float: what lgb_vcm_iteration projects light vertices with. */

@@ -136,6 +136,13 @@ class VcmParams(C.Structure):
                 ("reserved", C.c_uint32)]
 
 
+class VcmState(C.Structure):
+    _fields_ = [("vertices", C.c_void_p), ("path_counts", C.c_void_p), ("table_count", C.c_void_p),
+                ("table_rep", C.c_void_p), ("screen", C.c_uint32), ("per_path", C.c_uint32),
+                ("table_size", C.c_uint32), ("grid_res", C.c_int32 * 3), ("radius", C.c_float),
+                ("scene_min", C.c_float * 3), ("scene_max", C.c_float * 3), ("reserved", C.c_uint32)]
+
+
 class SppmParams(C.Structure):
     _fields_ = [("sky_col", C.c_float * 3), ("max_depth", C.c_int32), ("num_lights", C.c_int32),
                 ("light_triangle_count", C.c_int32), ("dir_light_idx", C.c_uint32), ("base_radius", C.c_float),
@@ -165,6 +172,7 @@ SIGNATURES = {
     "lgb_scene_create": ([C.c_void_p, C.POINTER(SceneDesc), C.POINTER(C.c_void_p)], C.c_int32),
     "lgb_scene_destroy": ([C.c_void_p], None),
     "lgb_bvh_build": ([C.c_void_p, C.POINTER(BuildOpts), C.POINTER(BuildStats)], C.c_int32),
+    "lgb_scene_set_visit_limit": ([C.c_void_p, C.c_uint32], C.c_int32),
     "lgb_trace_closest": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p], C.c_int32),
     "lgb_trace_any": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p], C.c_int32),
     "lgb_trace_closest_counted": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p], C.c_int32),
@@ -189,6 +197,7 @@ SIGNATURES = {
                                  C.c_void_p, C.c_void_p], C.c_int32),
     "lgb_vcm_grid": ([C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float,
                       C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int32),
+    "lgb_vcm_state_get": ([C.c_void_p, C.POINTER(VcmState)], C.c_int32),
     "lgb_camera_forward": ([C.POINTER(Camera), C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int32),
     "lgb_batch_create": ([C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, C.POINTER(C.c_void_p)], C.c_int32),
     "lgb_batch_destroy": ([C.c_void_p], None),

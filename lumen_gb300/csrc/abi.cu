@@ -259,6 +259,12 @@ LGB_API lgb_status lgb_scene_create(lgb_ctx* ctx, const lgb_scene_desc* d, lgb_s
     return LGB_OK;
 }
 
+LGB_API lgb_status lgb_scene_set_visit_limit(lgb_scene* s, uint32_t max_visits) {
+    if (!s) return LGB_ERR_INVALID_ARGUMENT;
+    s->visit_limit = max_visits;
+    return LGB_OK;
+}
+
 LGB_API void lgb_scene_destroy(lgb_scene* s) {
     if (!s) return;
     Ctx* c = s->ctx;

@@ -112,6 +112,7 @@ struct Scene {
     std::vector<lgb_mesh> h_meshes;
     BvhDevice bvh;
     uint32_t* d_status = nullptr;  // device status word
+    uint32_t visit_limit = 0;      // node visits per ray of the public queries; 0 = kMaxVisits
     uint32_t* d_ray_counter = nullptr;  // work counter of the persistent trace kernels
     // path-tracer work buffers (grown on demand)
     void* pt_buf = nullptr;
@@ -126,6 +127,9 @@ struct Scene {
     void* vcm_buf = nullptr;         // VCM state kept between iterations (light vertices, counts, splats, table)
     size_t vcm_buf_bytes = 0;
     uint32_t vcm_w = 0, vcm_h = 0, vcm_per = 0;
+    size_t vcm_o_verts = 0, vcm_o_counts = 0, vcm_o_gc = 0, vcm_o_gr = 0;  // offsets into vcm_buf
+    float vcm_radius = 0.0f, vcm_mn[3] = {}, vcm_mx[3] = {};                 // grid of the last iteration
+    int vcm_res[3] = {};
     void* bdpt_buf = nullptr;        // BDPT path buffers, strategy contributions and splat image (per frame)
     size_t bdpt_buf_bytes = 0;
     void* sppm_buf = nullptr;        // SPPM state kept between frames (visible points, photons, table, bounds)

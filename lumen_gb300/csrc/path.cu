@@ -773,7 +773,8 @@ lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* p
 // Every GPU that loads the library holds the array (6 MiB) until the process exits. All calls share it, so
 // calls that overlap on the GPU (another stream, another thread) race on it; order them on one stream.
 // The first call on a device takes the array's address there (cudaGetSymbolAddress); make that first call
-// before any stream capture.
+// before any stream capture. The address is kept for the life of the process, so it is stale after a
+// cudaDeviceReset that recreates the device's primary context.
 // ---------------------------------------------------------------------------------------------------------
 namespace lgb {
 namespace {

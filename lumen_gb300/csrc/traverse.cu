@@ -22,15 +22,28 @@ constexpr int kTraceSharedStack = 8;
 // Idle lanes a warp waits for before fetching new rays. Measured with the approximate box-test reciprocal,
 // closest / any Mrays/s: refill at 1 idle lane 1176 / 2350, at 8: 1185 / 2680, at 16: 1047 / 2485.
 constexpr int kTraceRefill = 8;
+#ifndef LGB_TRACE_TRI_MIN
+#define LGB_TRACE_TRI_MIN 0
+#endif
+#ifndef LGB_TRACE_DEFER_UV
+#define LGB_TRACE_DEFER_UV 0
+#endif
+#ifndef LGB_TRACE_REFILL
+#define LGB_TRACE_REFILL kTraceRefill
+#endif
 template <bool ANY, bool COUNT>
 __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks) k_trace(const WideNode* __restrict__ nodes, const WideTri* __restrict__ tris,
                                                          const lgb_ray* __restrict__ rays, lgb_hit* __restrict__ hits,
                                                          uint32_t* __restrict__ bits, uint32_t n, uint32_t* ray_counter,
-                                                         uint32_t* status, unsigned long long* counters) {
+                                                         uint32_t* status, unsigned long long* counters,
+                                                         uint32_t max_visits) {
     __shared__ uint2 s_stack[kTraceSharedStack * kTraceThreads];
-    trace_persistent<ANY, COUNT, true, kTraceSharedStack, kTraceThreads, kTraceRefill>(
-        nodes, tris, rays, hits, bits, n, nullptr, ray_counter, status, counters, nullptr, s_stack);
+    trace_persistent<ANY, COUNT, true, kTraceSharedStack, kTraceThreads, LGB_TRACE_REFILL, LGB_TRACE_TRI_MIN,
+                     LGB_TRACE_DEFER_UV != 0>(
+        nodes, tris, rays, hits, bits, n, nullptr, ray_counter, status, counters, nullptr, s_stack, max_visits);
 }
+
+uint32_t visit_budget(const Scene* s) { return s->visit_limit ? s->visit_limit : kMaxVisits; }
 
 template <bool ANY, bool COUNT> int persistent_grid(Ctx* ctx, uint32_t n) {
     static int blocks_per_sm = 0;
@@ -52,10 +65,10 @@ lgb_status launch_trace_closest(Scene* s, const lgb_ray* rays, lgb_hit* hits, ui
     if (counters)
         k_trace<false, true><<<persistent_grid<false, true>(s->ctx, n), kTraceThreads, 0, st>>>(
             s->bvh.nodes, s->bvh.tris, rays, hits, nullptr, n, s->d_ray_counter, s->d_status,
-            reinterpret_cast<unsigned long long*>(counters));
+            reinterpret_cast<unsigned long long*>(counters), visit_budget(s));
     else
         k_trace<false, false><<<persistent_grid<false, false>(s->ctx, n), kTraceThreads, 0, st>>>(
-            s->bvh.nodes, s->bvh.tris, rays, hits, nullptr, n, s->d_ray_counter, s->d_status, nullptr);
+            s->bvh.nodes, s->bvh.tris, rays, hits, nullptr, n, s->d_ray_counter, s->d_status, nullptr, visit_budget(s));
     LGB_CUDA_TRY(s->ctx, cudaGetLastError());
     return LGB_OK;
 }
@@ -170,7 +183,7 @@ lgb_status launch_trace_any(Scene* s, const lgb_ray* rays, uint32_t* bits, uint3
     LGB_CUDA_TRY(s->ctx, cudaMemsetAsync(s->d_ray_counter, 0, sizeof(uint32_t), st));
     LGB_CUDA_TRY(s->ctx, cudaMemsetAsync(bits, 0, sizeof(uint32_t) * ((n + 31) / 32), st));
     k_trace<true, false><<<persistent_grid<true, false>(s->ctx, n), kTraceThreads, 0, st>>>(
-        s->bvh.nodes, s->bvh.tris, rays, nullptr, bits, n, s->d_ray_counter, s->d_status, nullptr);
+        s->bvh.nodes, s->bvh.tris, rays, nullptr, bits, n, s->d_ray_counter, s->d_status, nullptr, visit_budget(s));
     LGB_CUDA_TRY(s->ctx, cudaGetLastError());
     return LGB_OK;
 }

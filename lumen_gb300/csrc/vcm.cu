@@ -776,6 +776,9 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
     spot_cone(p->spot_angle, A.spot_cos_width, A.spot_cos_falloff);
     A.radius = p->radius;
     grid_resolution(A.mn, A.mx, A.radius, A.res);
+    s->vcm_o_verts = o_verts; s->vcm_o_counts = o_counts; s->vcm_o_gc = o_gc; s->vcm_o_gr = o_gr;
+    s->vcm_radius = A.radius;
+    for (int k = 0; k < 3; k++) { s->vcm_mn[k] = A.mn[k]; s->vcm_mx[k] = A.mx[k]; s->vcm_res[k] = A.res[k]; }
     A.verts = reinterpret_cast<float4*>(base + o_verts);
     A.counts = reinterpret_cast<uint32_t*>(base + o_counts);
     A.splat = reinterpret_cast<float*>(base + o_splat);
@@ -848,6 +851,27 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
     k_vcm_eye_init<<<grid, kVcmThreads, 0, st>>>(A, W);
     for (int d = 1; d <= A.max_depth; d++) bounce(1, d);
     LGB_CUDA_TRY(ctx, cudaGetLastError());
+    return LGB_OK;
+}
+
+LGB_API lgb_status lgb_vcm_state_get(const lgb_scene* s, lgb_vcm_state* out) {
+    if (!s || !out) return LGB_ERR_INVALID_ARGUMENT;
+    if (!s->vcm_buf) return set_error(s->ctx, LGB_ERR_NOT_READY, "lgb_vcm_iteration has not run on this scene");
+    const char* base = static_cast<const char*>(s->vcm_buf);
+    std::memset(out, 0, sizeof(*out));
+    out->vertices = reinterpret_cast<const float*>(base + s->vcm_o_verts);
+    out->path_counts = reinterpret_cast<const uint32_t*>(base + s->vcm_o_counts);
+    out->table_count = reinterpret_cast<const uint32_t*>(base + s->vcm_o_gc);
+    out->table_rep = reinterpret_cast<const uint32_t*>(base + s->vcm_o_gr);
+    out->screen = s->vcm_w * s->vcm_h;
+    out->per_path = s->vcm_per;
+    out->table_size = 10u * out->screen;
+    out->radius = s->vcm_radius;
+    for (int k = 0; k < 3; k++) {
+        out->grid_res[k] = s->vcm_res[k];
+        out->scene_min[k] = s->vcm_mn[k];
+        out->scene_max[k] = s->vcm_mx[k];
+    }
     return LGB_OK;
 }
 

@@ -65,6 +65,11 @@ def dielectric(ior, roughness=0.0, albedo=(1.0, 1.0, 1.0), thin=0) -> np.ndarray
                         thin=thin)
 
 
+def glass(ior) -> np.ndarray:
+    """"type": "glass" (LumenScene.cpp:380-384): smooth specular transmission only, no reflection lobe."""
+    return new_material(ior=ior, bsdf_type=abi.BSDF_GLASS, bsdf_props=abi.FLAG_SPECULAR | abi.FLAG_TRANSMISSION)
+
+
 def principled(albedo, roughness=0.5, metallic=0.0, ior=1.0, spec_trans=0.0, clearcoat=0.0, clearcoat_gloss=1.0,
                specular_tint=0.0, anisotropy=0.0, flatness=0.0) -> np.ndarray:
     """"type": "principled" (LumenScene.cpp:444-475)."""
@@ -251,6 +256,10 @@ class GpuScene:
         self.stats = stats
         return stats
 
+    def set_visit_limit(self, max_visits: int):
+        """lgb_scene_set_visit_limit: node visits one ray of the public queries may make (0 = default)."""
+        _check(self.lib, self.ctx.handle, self.lib.lgb_scene_set_visit_limit(self.handle, max_visits))
+
     def trace_closest(self, rays, hits, n=None, stream=None):
         n = rays.shape[0] if n is None else n
         _check(self.lib, self.ctx.handle,
@@ -296,6 +305,12 @@ class GpuScene:
         _check(self.lib, self.ctx.handle,
                self.lib.lgb_vcm_iteration(self.handle, C.byref(cam), C.byref(params), C.c_void_p(film.data_ptr()),
                                           C.c_void_p(stream)))
+
+    def vcm_state(self) -> abi.VcmState:
+        """lgb_vcm_state_get: device pointers and grid of the VCM state kept in the scene."""
+        out = abi.VcmState()
+        _check(self.lib, self.ctx.handle, self.lib.lgb_vcm_state_get(self.handle, C.byref(out)))
+        return out
 
     def restir_di_iteration(self, cam: abi.Camera, params: abi.RestirParams, film, prev_cam: abi.Camera = None,
                             stream=None):

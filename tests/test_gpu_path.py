@@ -95,6 +95,8 @@ def _material_scene(kind):
         extra = S.principled((0.8, 0.3, 0.2), roughness=0.4, metallic=0.3, ior=1.5, clearcoat=0.5)
     elif kind == "principled_glass":
         extra = S.principled((0.9, 0.9, 0.9), roughness=0.2, ior=1.5, spec_trans=0.8)
+    elif kind == "glass":
+        extra = S.glass(1.5)
     elif kind == "mirror":
         extra = S.new_material(bsdf_type=abi.BSDF_MIRROR, bsdf_props=abi.FLAG_SPECULAR | abi.FLAG_REFLECTION)
     else:
@@ -108,7 +110,7 @@ def _material_scene(kind):
 
 
 @pytest.mark.parametrize("kind", ["conductor", "dielectric", "rough_dielectric", "principled", "principled_glass",
-                                  "mirror"])
+                                  "mirror", "glass"])
 def test_materials_match_oracle(ctx, oracle, kind):
     cb = _material_scene(kind)
     sc = GpuScene(ctx, cb)

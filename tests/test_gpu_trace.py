@@ -244,3 +244,29 @@ def test_context_outlives_its_scenes_whatever_the_destroy_order(ctx):
     hits = gpu_closest(other, rays)
     assert (hits["prim"] != 0xFFFFFFFF).any()
     other.close()
+
+
+def test_visit_budget_sets_the_device_status_word(ctx, oracle):
+    """The error path of the bounded traversal loop, driven without any fault: a per-ray budget of 2 node visits
+    runs out on a sound 100k-triangle tree, the kernel sets the visit-limit bit of the scene's status word and
+    every ray ends; lgb_sync reports LGB_ERR_DEVICE_STATUS once and clears the word, and with the default budget
+    restored the same query is clean and equals the oracle."""
+    arrays = procedural.traversal_scene(sphere_freq=60, n_random=30_000)
+    rays = procedural.incoherent_rays(arrays, 50_000, seed=9)
+    sc = GpuScene(ctx, arrays)
+    sc.build()
+    d_rays = torch.from_numpy(rays).cuda()
+    d_hits = torch.zeros((len(rays), 4), dtype=torch.int32, device="cuda")
+    sc.set_visit_limit(2)
+    sc.trace_closest(d_rays, d_hits)
+    with pytest.raises(abi.LgbError) as e:
+        sc.sync()
+    assert e.value.status == 5 and "visit limit" in str(e.value)
+    d_bits = torch.zeros(((len(rays) + 31) // 32,), dtype=torch.int32, device="cuda")
+    sc.trace_any(d_rays, d_bits)
+    with pytest.raises(abi.LgbError):
+        sc.sync()
+    sc.sync()  # the word was cleared by the failing sync
+    sc.set_visit_limit(0)
+    got = gpu_closest(sc, rays)
+    assert_hits_equal(got, oracle.bvh(arrays.tri_verts()).closest(rays))

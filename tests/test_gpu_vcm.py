@@ -52,6 +52,49 @@ def test_photon_table_is_bit_exact(ctx, oracle):
     assert int(count.abs().sum()) == 0
 
 
+class _DeviceArray:
+    """A device buffer owned by the library, seen by torch through the CUDA array interface (no copy)."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), False),
+                                         "version": 2}
+
+
+def test_photon_table_is_bit_exact_on_caustics_light_vertices(ctx, oracle):
+    """The table of one iteration of the caustics configuration (1024^2 light subpaths on the 200k-triangle
+    torus, depth 10, radius 0.01 x scene radius): the oracle's sequential table built from the GPU's own light
+    vertices equals the GPU's sort-and-scan table bit for bit."""
+    from oracle_lib import vcm_grid as oracle_grid
+    arrays = procedural.vcm_scene()
+    sc = GpuScene(ctx, arrays)
+    sc.build()
+    w = h = 1024
+    depth = 10
+    cam = camera_lookat(arrays.camera_pos, arrays.camera_dir, arrays.fov, w, h)
+    film = torch.zeros((w * h, 4), dtype=torch.float32, device="cuda")
+    r = vcm_radius(scene_radius(arrays), 1.0, 0, 0.75)
+    sc.vcm_iteration(cam, vcm_params(arrays, depth, r, 11, 12, 0, spot_angle=20.0), film)
+    sc.sync()
+    st = sc.vcm_state()
+    assert st.screen == w * h and st.per_path == depth + 1 and st.table_size == 10 * w * h
+    nv = st.screen * st.per_path
+    verts = torch.as_tensor(_DeviceArray(st.vertices, (nv, 6, 4), "<f4"), device="cuda")
+    counts = torch.as_tensor(_DeviceArray(st.path_counts, (st.screen,), "<i4"), device="cuda").cpu().numpy()
+    pos4 = verts[:, 0, :].cpu().numpy().copy()
+    used = (np.arange(nv) % st.per_path) < np.repeat(counts, st.per_path)
+    pos4[:, 3] = np.where(used, 1.0, -1.0)
+    got_c = torch.as_tensor(_DeviceArray(st.table_count, (st.table_size,), "<i4"), device="cuda").cpu().numpy()
+    got_r = torch.as_tensor(_DeviceArray(st.table_rep, (st.table_size,), "<i4"), device="cuda").cpu().numpy()
+    want_c, want_r = oracle_grid(oracle, pos4, list(st.scene_min), list(st.scene_max), st.radius, st.screen)
+    assert used.sum() > 1_000_000, "the light pass stored too few vertices to exercise the table"
+    assert int(want_c.sum()) == int(used.sum())
+    assert np.array_equal(got_c.view(np.uint32), want_c)
+    occupied = want_c > 0
+    assert np.array_equal(got_r.view(np.uint32)[occupied], want_r[occupied])
+    assert (want_c > 1).sum() > 10_000
+    sc.close()
+
+
 def _run_both(ctx, oracle, arrays, w, h, iters, depth, flags=0, use_vm=1, alpha=2.0 / 3.0, factor=1.0, spot_angle=0.0):
     from oracle_lib import VcmParams
     sc = GpuScene(ctx, arrays)
@@ -100,6 +143,17 @@ def test_caustics_scene_with_merging_matches_oracle(ctx, oracle, spot_angle):
     assert frac >= 0.95, f"only {frac:.4f} of pixels agree"
     np.testing.assert_allclose(got[:, :3].mean(0), want[:, :3].mean(0), rtol=0.02)
     assert got[:, :3].mean() > 0.0
+
+
+def test_caustics_configuration_matches_oracle(ctx, oracle):
+    """The caustics configuration itself (200k-triangle dielectric torus, 20 degree spot, depth 10, alpha 0.75)
+    at 96^2: pixel by pixel against the oracle over four iterations with merging."""
+    arrays = procedural.vcm_scene()
+    got, want = _run_both(ctx, oracle, arrays, 96, 96, 4, 10, alpha=0.75, spot_angle=20.0)
+    assert not np.isnan(got).any()
+    frac = close_fraction(got[:, :3], want[:, :3])
+    assert frac >= 0.95, f"only {frac:.4f} of pixels agree"
+    np.testing.assert_allclose(got[:, :3].mean(0), want[:, :3].mean(0), rtol=0.02)
 
 
 def test_spot_cone_narrows_the_lit_area(ctx, oracle):

@@ -11,8 +11,8 @@ import pytest
 
 from lumen_gb300 import abi
 
-REF = os.environ.get("LUMEN_REFERENCE_DIR", "/root/reference")
-SCENES = sorted(glob.glob(os.path.join(REF, "scenes", "**", "*.json"), recursive=True))
+REF = os.environ.get("LUMEN_REFERENCE_DIR", "")
+SCENES = sorted(glob.glob(os.path.join(REF, "scenes", "**", "*.json"), recursive=True)) if REF else []
 TYPES = {"diffuse": abi.BSDF_DIFFUSE, "mirror": abi.BSDF_MIRROR, "glass": abi.BSDF_GLASS,
          "dielectric": abi.BSDF_DIELECTRIC, "conductor": abi.BSDF_CONDUCTOR, "principled": abi.BSDF_PRINCIPLED}
 

@@ -20,7 +20,6 @@ from __future__ import annotations
 import argparse
 import json
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -117,6 +116,33 @@ def make_workload(cache=True):
     return arrays, rays
 
 
+TRAVERSAL_SOURCES = ("lumen_gb300/csrc/traverse.cuh", "lumen_gb300/csrc/traverse.cu", "lumen_gb300/csrc/lgb_internal.cuh")
+
+
+def measured_traffic(rays: int) -> dict:
+    """DRAM and L2 bytes of one launch of the closest-hit kernel from the committed ncu record
+    (profiles/trace_closest_incoherent_1M.ncu.json), scaled to `rays`, when the record was taken of the traversal
+    sources being run (same SHA-256 over TRAVERSAL_SOURCES); otherwise nulls and the reason."""
+    import hashlib
+    none = {"dram_bytes": None, "l2_bytes": None, "l2_bytes_per_ray": None, "dram_bytes_per_ray": None}
+    path = os.path.join(ROOT, "profiles", "trace_closest_incoherent_1M.ncu.json")
+    if not os.path.exists(path):
+        return {**none, "source": "no ncu record"}
+    with open(path) as f:
+        rec = json.load(f)
+    h = hashlib.sha256()
+    for name in TRAVERSAL_SOURCES:
+        with open(os.path.join(ROOT, name), "rb") as f:
+            h.update(f.read())
+    if rec.get("source_sha256") != h.hexdigest():
+        return {**none, "source": "ncu record is of other traversal sources (stale): not used"}
+    per_ray_dram = rec["dram_bytes_per_ray"]
+    return {"dram_bytes": per_ray_dram * rays, "l2_bytes": rec["l2_bytes_per_ray"] * rays,
+            "l2_bytes_per_ray": rec["l2_bytes_per_ray"], "dram_bytes_per_ray": per_ray_dram,
+            "source": "ncu record of this kernel version (profiles/trace_closest_incoherent_1M.ncu.json): "
+                      + rec["command"]}
+
+
 def measure_l2_peak(device: int) -> float:
     """Read bandwidth of a 32 MB L2-resident buffer streamed 64 times by every SM (lgb_measure_l2_read_gbs)."""
     import ctypes as C
@@ -126,22 +152,28 @@ def measure_l2_peak(device: int) -> float:
     return out.value if st == abi.LGB_OK else float("nan")
 
 
-def cpu_oracle_rate(arrays, rays, seconds=12.0, threads=None):
-    """Rays/s of the CPU oracle on a bounded sample; returns (rays_per_s, sample_rays, threads)."""
+CPU_WINDOW = 100_000  # rays per timed step of the CPU oracle
+
+
+def cpu_oracle_steps(arrays, rays, steps, warmup, threads=None):
+    """The CPU oracle (binary SAH BVH, same watertight test) on all host threads: each step traces one window of
+    CPU_WINDOW contiguous rays at a seeded random offset of the 4M incoherent set; returns (Mrays/s per timed step,
+    threads). Both the cpu_baseline of the GPU line and --impl reference time it this way."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_lib
     ora = oracle_lib.Oracle()
     threads = threads or (os.cpu_count() or 1)
     bvh = ora.bvh(arrays.tri_verts())
-    probe = rays[:20000]
-    t0 = time.perf_counter()
-    bvh.closest(probe, threads)
-    rate = len(probe) / (time.perf_counter() - t0)
-    n = int(min(len(rays), max(20000, rate * seconds)))
-    t0 = time.perf_counter()
-    bvh.closest(rays[:n], threads)
-    dt = time.perf_counter() - t0
-    return n / dt, n, threads
+    rng = np.random.default_rng(11)
+    vals = []
+    for step in range(warmup + steps):
+        idx = int(rng.integers(0, len(rays) - CPU_WINDOW))
+        t0 = time.perf_counter()
+        bvh.closest(rays[idx:idx + CPU_WINDOW], threads)
+        dt = time.perf_counter() - t0
+        if step >= warmup:
+            vals.append(CPU_WINDOW / dt / 1e6)
+    return vals, threads
 
 
 def cpu_integrator_rate(kind, arrays, w, h, frames, depth, **kw):
@@ -226,7 +258,9 @@ def cornell_secondary(torch, ctx_cls, scene_cls, local, cpu_leg: bool):
     out = {"workload": "Cornell box 36 triangles, 256x256, 16 spp, max depth 8, FP32", "ms": ms,
            "msamples_per_s": w * h * spp / (ms * 1e-3) / 1e6, "mean_radiance": float(film[:, :3].mean()),
            "graph": "bounce loop captured once as a CUDA graph and replayed"}
-    out["rmse_vs_fp64_2048spp"] = reference_rmse(torch, ctx, film, "cornell_256_fp64_ref.npy")
+    out["rmse_vs_fp64"] = {"value": reference_rmse(torch, ctx, film, "cornell_256_fp64_ref.npy"),
+                           "render": "this 16-spp film, 256x256",
+                           "reference": "FP64 CPU oracle, 2048 spp (tests/golden/cornell_256_fp64_ref.npy)"}
     if cpu_leg:
         sys.path.insert(0, os.path.join(ROOT, "tests"))
         import oracle_lib
@@ -307,7 +341,8 @@ def adjoint_secondary(torch, ctx_cls, scene_cls, local):
                         "roughness + emission, L2 image loss", "primal_ms": mp, "adjoint_ms": ma,
             "primal_plus_adjoint_over_primal": (mp + ma) / mp,
             "primal_msamples_per_s": w * h * spp / (mp * 1e-3) / 1e6,
-            "primal_rmse_vs_fp64_512spp": rmse,
+            "rmse_vs_fp64": {"value": rmse, "render": "the primal image, 32 spp, 512x512",
+                             "reference": "FP64 CPU oracle, 512 spp (tests/golden/diff_512_fp64_ref.npy)"},
             "grad_norms": {"texels": float(gt.norm()), "roughness": float(gr.norm()), "emission": float(ge.norm())}}
 
 
@@ -370,12 +405,29 @@ def batch_secondary(torch, ctx_cls, scene_cls, local):
     ms_batch = timed(batched)
     batch.sync(cs)
     max_diff = max(float((fa - fb).abs().max()) for fa, fb in zip(films_a, films_b))
+    # convergence: three of the scenes at 128^2 with their own spp, batched and scene by scene, against the
+    # committed FP64 oracle references (2048 spp, independent frames)
+    rmse = []
+    for idx in (1, 13, 21):
+        a = arrays[idx]
+        spp = cfg[idx][4]
+        cam = camera_lookat(a.camera_pos, a.camera_dir, a.fov, 128, 128)
+        fa = torch.zeros((128 * 128, 4), dtype=torch.float32, device="cuda")
+        fb = torch.zeros((128 * 128, 4), dtype=torch.float32, device="cuda")
+        scenes[idx].render_path(cam, path_params(a, 12), 0, spp, fa, stream=cs)
+        batch.render([Batch.job(idx, cam, path_params(a, 12), 0, spp, fb)], stream=cs)
+        batch.sync(cs)
+        ref = f"batch_scene{idx}_128_fp64_ref.npy"
+        rmse.append({"scene": idx, "triangles": cfg[idx][1], "spp": spp,
+                     "per_scene": reference_rmse(torch, ctx, fa, ref), "batched": reference_rmse(torch, ctx, fb, ref)})
     res = {"workload": "32 scenes, 10k-2M triangles (log-uniform, 14.3M total), 128^2-1024^2, 8-64 spp, depth 12, "
                        "principled (80 %) and dielectric (20 %) materials, 1-8 quad lights",
            "samples": samples, "per_scene_ms": ms_alone, "batched_ms": ms_batch,
            "per_scene_msamples_per_s": samples / (ms_alone * 1e-3) / 1e6,
            "batched_msamples_per_s": samples / (ms_batch * 1e-3) / 1e6,
            "speedup": ms_alone / ms_batch, "films_max_abs_diff": max_diff,
+           "rmse_vs_fp64": {"scenes": rmse, "render": "128x128 at the scene's own spp",
+                            "reference": "FP64 CPU oracle, 2048 spp (tests/golden/batch_scene*_128_fp64_ref.npy)"},
            "tuned": {"path_capacity": best.path_capacity, "work_blocks_per_sm": best.work_blocks_per_sm,
                      "stack": "shared" if best.stack_placement == 1 else "local"},
            "tune_s": tune_s, "scene_generation_s": gen_s}
@@ -462,7 +514,7 @@ def vcm_secondary(torch, ctx_cls, scene_cls, local, cpu_leg=False, iters=63):
     e1.synchronize()
     sc.sync(cs)
     ms = e0.elapsed_time(e1) / iters
-    # convergence: the same 64 iterations at 256^2 against the committed 1024-iteration oracle render
+    # convergence: the same 64 iterations at 256^2 against the committed 2048-iteration FP64 oracle render
     w2 = h2 = 256
     cam2 = camera_lookat(arrays.camera_pos, arrays.camera_dir, arrays.fov, w2, h2)
     film2 = torch.zeros((w2 * h2, 4), dtype=torch.float32, device="cuda")
@@ -470,14 +522,16 @@ def vcm_secondary(torch, ctx_cls, scene_cls, local, cpu_leg=False, iters=63):
         sc.vcm_iteration(cam2, vcm_params(arrays, 10, vcm_radius(R, 1.0, i, 0.75), 1000 + i, 5000 + i, i,
                                           spot_angle=20.0), film2, stream=cs)
     sc.sync(cs)
-    rmse = reference_rmse(torch, ctx, film2, "vcm_torus_256_ref.npy")
+    rmse = reference_rmse(torch, ctx, film2, "vcm_torus_256_fp64_ref.npy")
     out = {"workload": "VCM: dielectric torus (200k triangles, IOR 1.5) on a diffuse plane, spot light L = 100 "
                        "with a 20 degree cone, 1024x1024, 1M light subpaths per iteration, max depth 10, radius "
                        "0.01 x scene radius, alpha 0.75, 64 iterations",
            "ms_per_iteration": ms, "msamples_per_s": w * h / (ms * 1e-3) / 1e6,
            "light_plus_eye_paths_per_s": 2 * w * h / (ms * 1e-3),
            "mean_radiance": float(film[:, :3].mean()), "iterations_timed": iters,
-           "rmse_256_64it_vs_oracle_1024it": rmse}
+           "rmse_vs_fp64": {"value": rmse, "render": "64 iterations at 256x256 (same seeds and radii)",
+                            "reference": "FP64 CPU oracle, 2048 iterations at 256x256 "
+                                         "(tests/golden/vcm_torus_256_fp64_ref.npy)"}}
     sc.close()
     if cpu_leg:
         out["cpu_baseline"] = cpu_integrator_rate("vcm", arrays, 256, 256, 8, 10, spot_angle=20.0)
@@ -612,27 +666,15 @@ def run_reference(args):
     if rank != 0:
         return
     arrays, rays = make_workload()
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import oracle_lib
-    ora = oracle_lib.Oracle()
-    threads = os.cpu_count() or 1
-    bvh = ora.bvh(arrays.tri_verts())
-    sample = 100_000
-    rng = np.random.default_rng(11)
-    vals = []
-    for step in range(args.warmup + args.steps):
-        idx = rng.integers(0, len(rays) - sample)
-        t0 = time.perf_counter()
-        bvh.closest(rays[idx:idx + sample], threads)
-        dt = time.perf_counter() - t0
-        if step >= args.warmup:
-            vals.append(sample / dt / 1e6)
+    vals, threads = cpu_oracle_steps(arrays, rays, args.steps, args.warmup)
+    sample = CPU_WINDOW
     value = float(np.median(vals))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": sample / (value * 1e6) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "rays_per_step": sample, "sample": "contiguous 100k-ray windows"},
+        "config": {"workload": WORKLOAD, "rays_per_step": sample,
+                   "sample": f"one window of {sample} contiguous rays of the 4M incoherent set per step"},
         "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
                          "sample": f"{sample} rays per step of the 4M incoherent set"},
         "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -716,20 +758,13 @@ def run_gpu(args):
         peak_src = "measured"
     l2_peak = measure_l2_peak(local)
     achieved = bytes_per_ray * n / (step_ms * 1e-3) / 1e9
-    # DRAM bytes per ray of one ncu capture of this launch (dram__bytes_read.sum + dram__bytes_write.sum over the
-    # rays of the launch), kept in the kernel's profile summary as `traffic_bytes_per_ray: X`.
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "trace_closest_incoherent_1M.md")
-    if os.path.exists(prof):
-        with open(prof) as f:
-            m = re.search(r"traffic_bytes_per_ray:\s*([0-9.]+)", f.read())
-        if m:
-            traffic = float(m.group(1)) * n
+    prof = measured_traffic(n)
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
-        rate, sample, threads = cpu_oracle_rate(arrays, rays)
-        cpu = {"value": rate / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
-               "sample": f"first {sample} of the 4M incoherent rays on the oracle binary SAH BVH (build untimed)"}
+        vals, threads = cpu_oracle_steps(arrays, rays, 20, 3)
+        cpu = {"value": float(np.median(vals)), "unit": "Mrays/s", "cores": threads, "kind": "port",
+               "sample": f"median of 20 windows of {CPU_WINDOW} contiguous rays of the 4M incoherent set (3 warm-up), "
+                         "oracle binary SAH BVH, build untimed; the same method as --impl reference"}
     secondary = {}
     if not args.no_secondary:
         secondary["traversal"] = traversal_secondary(torch, sc, rays, flush, stream)
@@ -753,12 +788,17 @@ def run_gpu(args):
         "e2e": {"value": e2e, "unit": "Mrays/s", "h2d_bytes_per_step": int(rays.nbytes),
                 "d2h_bytes_per_step": int(n * 16), "api": "lgb_trace_closest_host (pinned host buffers: the trace "
                 "kernel loads the rays from and stores the hits to host memory over NVLink-C2C)", "hits_equal_device_query": bool(e2e_check)},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": traffic, "peak_source": peak_src,
+        "roofline": {"bound": "l2", "achieved": achieved, "peak": l2_peak, "unit": "GB/s",
+                     "frac": achieved / l2_peak, "traffic": prof["dram_bytes"],
+                     "peak_source": "measured in this run: lgb_measure_l2_read_gbs, a 32 MB L2-resident buffer "
+                                    "read by every SM",
                      "bytes_per_ray": bytes_per_ray, "nodes_per_ray": n_nodes, "tris_per_ray": n_tris,
-                     "l2_read_peak_gbs": l2_peak, "frac_of_l2_peak": achieved / l2_peak,
-                     "note": "achieved counts ray + hit + 80 B per node and 48 B per triangle fetched; the "
-                             "working set (BVH + triangles) is L2-resident, so frac_of_l2_peak is the binding one"},
+                     "l2_bytes_measured": prof["l2_bytes"], "l2_bytes_per_ray_measured": prof["l2_bytes_per_ray"],
+                     "dram_bytes_per_ray_measured": prof["dram_bytes_per_ray"], "traffic_source": prof["source"],
+                     "hbm_peak": hbm_peak, "hbm_peak_source": peak_src, "frac_of_hbm_peak": achieved / hbm_peak,
+                     "note": "achieved counts ray + hit + 80 B per node and 48 B per triangle fetched (algorithmic "
+                             "bytes); the node and triangle working set is L2-resident, so the L2 read peak bounds "
+                             "the kernel; traffic is the DRAM bytes of one ncu capture of this kernel version"},
         "cpu_baseline": cpu,
         "clocks": clk,
         "gpu_launches": args.steps,

@@ -172,8 +172,14 @@ typedef struct lgb_path_params {
     uint32_t reserved[3];
 } lgb_path_params;
 
-/* ---- context (stands in for the Vulkan device/context, VulkanBase.cpp) ---- */
-LGB_API lgb_status lgb_create(lgb_ctx** out, int device);
+/* ---- context (stands in for the Vulkan device/context, VulkanBase.cpp) ----
+ * tuning_cache_path: a text file in which lgb_batch_tune keeps its choices, keyed by the device (name, SM count,
+ * compute capability), the library's ABI version and the shape of the tuned batch, so that later processes on
+ * the same kind of device skip the timing runs; null = no cache. The file is created when missing; a cache that
+ * cannot be read or written is ignored (tuning then times the candidates as without one). Lumen keeps its
+ * compiled pipelines in a cache keyed by pass name and shader macros (RenderGraph.h:241-284); this is the
+ * counterpart for the choices of the autotuner. */
+LGB_API lgb_status lgb_create(lgb_ctx** out, int device, const char* tuning_cache_path);
 LGB_API void lgb_destroy(lgb_ctx* ctx);
 LGB_API const char* lgb_last_error(const lgb_ctx* ctx);
 LGB_API uint32_t lgb_abi_version(void);
@@ -217,6 +223,12 @@ LGB_API lgb_status lgb_trace_any_host(lgb_scene* scene, const lgb_ray* h_rays, u
 /* ---- camera helper (Camera.h:67-123, Integrator.cpp:60-72): fills out->inv_view/inv_projection ---- */
 LGB_API lgb_status lgb_camera_lookat(const float pos[3], const float dir[3], float fov_deg, uint32_t width,
                                      uint32_t height, lgb_camera* out);
+
+/* The same camera from a camera-to-world matrix (column-major, as glm stores Lumen's Camera::camera after
+ * Camera::update_view_matrix, Camera.h:27-39): inv_view = camera_to_world, the projection as above. For cameras
+ * given by a matrix rather than a position and direction (Mitsuba sensors, LumenScene.cpp:64-68). */
+LGB_API lgb_status lgb_camera_from_matrix(const float camera_to_world[16], float fov_deg, uint32_t width,
+                                          uint32_t height, lgb_camera* out);
 
 /* ---- the Path integrator (Path::render, Path.cpp:27-59, i.e. path.rgen for frames frame0..frame0+spp-1).
  *      d_film is RGBA32F width*height (float4 per pixel), updated in place. ---- */
@@ -444,7 +456,8 @@ typedef struct lgb_batch_opts {
     uint32_t trace_blocks_per_sm;  /* grid of the persistent traversal kernels; 0 = as many as fit */
     uint32_t stack_placement;      /* traversal stack: LGB_STACK_LOCAL (0) per-thread local memory, or
                                       LGB_STACK_SHARED: its bottom 8 entries in shared memory */
-    uint32_t reserved[4];
+    uint32_t from_cache;           /* written by lgb_batch_tune: 1 when the choice came from the tuning cache */
+    uint32_t reserved[3];
 } lgb_batch_opts;
 #define LGB_STACK_LOCAL 0u
 #define LGB_STACK_SHARED 1u
@@ -459,7 +472,8 @@ LGB_API lgb_status lgb_batch_render(lgb_batch* batch, const lgb_batch_job* jobs,
                                     const lgb_batch_opts* opts, void* stream);
 /* Autotuner: times lgb_batch_render over candidate queue sizes and grids on a reduced copy of `jobs` (a
  * quarter of each job's frames, films untouched), keeps the fastest for later renders and writes it to *best.
- * Waits for `stream`. */
+ * With a tuning cache (lgb_create) a batch of the same shape on the same kind of device takes the cached choice
+ * without timing anything (best->from_cache = 1); a new choice is added to the cache. Waits for `stream`. */
 LGB_API lgb_status lgb_batch_tune(lgb_batch* batch, const lgb_batch_job* jobs, uint32_t num_jobs,
                                   lgb_batch_opts* best, void* stream);
 /* Waits for `stream` and reports faults recorded by the batch's traversal or by any of its scenes. */

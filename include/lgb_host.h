@@ -30,10 +30,14 @@ typedef struct lgbh_scene_info {
     float base_radius;    /* SPPM integrator block (SPPMConfig::base_radius) */
     float radius_factor;  /* VCM integrator block (VCMConfig::radius_factor) */
     int32_t enable_vm;    /* VCM integrator block (VCMConfig::enable_vm) */
+    int32_t cam_use_matrix;   /* 1: the camera is cam_matrix (Mitsuba sensors), not cam_pos / cam_dir */
+    float cam_matrix[16];     /* camera-to-world, column-major, for lgb_camera_from_matrix */
 } lgbh_scene_info;
 
-/* Loads a Lumen JSON scene and its OBJ (LumenScene::load_lumen_scene, LumenScene.cpp:231-513). On failure
- * returns LGB_ERR_INVALID_ARGUMENT and copies the message into err (up to errlen bytes). */
+/* Loads a Lumen JSON scene and its OBJ (LumenScene::load_lumen_scene, LumenScene.cpp:231-513), or a Mitsuba
+ * XML scene and its OBJ shapes when the path ends in ".xml" (LumenScene::load_mitsuba_scene,
+ * LumenScene.cpp:514-690). On failure returns LGB_ERR_INVALID_ARGUMENT and copies the message into err (up to
+ * errlen bytes). */
 LGB_API lgb_status lgbh_scene_load(const char* json_path, lgbh_scene** out, char* err, size_t errlen);
 LGB_API void lgbh_scene_free(lgbh_scene* s);
 /* The loaded arrays as an lgb_scene_desc (pointers stay valid until lgbh_scene_free). */

@@ -119,7 +119,7 @@ class BatchJob(C.Structure):
 class BatchOpts(C.Structure):
     _fields_ = [("path_capacity", C.c_uint32), ("work_blocks_per_sm", C.c_uint32),
                 ("trace_blocks_per_sm", C.c_uint32), ("stack_placement", C.c_uint32),
-                ("reserved", C.c_uint32 * 4)]
+                ("from_cache", C.c_uint32), ("reserved", C.c_uint32 * 3)]
 
 
 STACK_LOCAL, STACK_SHARED = 0, 1  # lgb_batch_opts.stack_placement
@@ -166,7 +166,7 @@ class RestirParams(C.Structure):
 # Every exported symbol with its argument and result types (the declarations of include/lgb.h).
 SIGNATURES = {
     "lgb_abi_version": ([], C.c_uint32),
-    "lgb_create": ([C.POINTER(C.c_void_p), C.c_int], C.c_int32),
+    "lgb_create": ([C.POINTER(C.c_void_p), C.c_int, C.c_char_p], C.c_int32),
     "lgb_destroy": ([C.c_void_p], None),
     "lgb_last_error": ([C.c_void_p], C.c_char_p),
     "lgb_scene_create": ([C.c_void_p, C.POINTER(SceneDesc), C.POINTER(C.c_void_p)], C.c_int32),
@@ -180,6 +180,8 @@ SIGNATURES = {
     "lgb_trace_any_host": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p], C.c_int32),
     "lgb_camera_lookat": ([C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_float, C.c_uint32, C.c_uint32,
                            C.POINTER(Camera)], C.c_int32),
+    "lgb_camera_from_matrix": ([C.POINTER(C.c_float), C.c_float, C.c_uint32, C.c_uint32, C.POINTER(Camera)],
+                               C.c_int32),
     "lgb_render_path": ([C.c_void_p, C.POINTER(Camera), C.POINTER(PathParams), C.c_uint32, C.c_uint32, C.c_void_p,
                          C.c_void_p], C.c_int32),
     "lgb_render_path_noalloc": ([C.c_void_p, C.POINTER(Camera), C.POINTER(PathParams), C.c_uint32, C.c_uint32,

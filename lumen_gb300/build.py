@@ -44,7 +44,7 @@ def build_library(verbose: bool = False) -> str:
     return lib
 
 
-HOST_SOURCES = ["lumen_scene.cpp", "integrator.cpp", "host_capi.cpp"]
+HOST_SOURCES = ["lumen_scene.cpp", "mitsuba_xml.cpp", "integrator.cpp", "host_capi.cpp"]
 
 
 def build_host(lib: str) -> str:

@@ -108,9 +108,9 @@ using namespace lgb;
 
 extern "C" {
 
-LGB_API uint32_t lgb_abi_version(void) { return 1u; }
+LGB_API uint32_t lgb_abi_version(void) { return 2u; }
 
-LGB_API lgb_status lgb_create(lgb_ctx** out, int device) {
+LGB_API lgb_status lgb_create(lgb_ctx** out, int device, const char* tuning_cache_path) {
     if (!out) return LGB_ERR_INVALID_ARGUMENT;
     *out = nullptr;
     int count = 0;
@@ -120,6 +120,7 @@ LGB_API lgb_status lgb_create(lgb_ctx** out, int device) {
     lgb_ctx* c = new (std::nothrow) lgb_ctx();
     if (!c) return LGB_ERR_OUT_OF_MEMORY;
     c->device = device;
+    if (tuning_cache_path) c->tuning_cache = tuning_cache_path;
     cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
     *out = c;
     return LGB_OK;
@@ -357,20 +358,40 @@ LGB_API lgb_status lgb_sync(lgb_scene* s, void* stream) {
     return LGB_OK;
 }
 
-LGB_API lgb_status lgb_camera_lookat(const float pos[3], const float dir[3], float fov_deg, uint32_t width,
-                                     uint32_t height, lgb_camera* out) {
-    if (!pos || !dir || !out || width == 0 || height == 0 || !(fov_deg > 0.0f && fov_deg < 180.0f))
-        return LGB_ERR_INVALID_ARGUMENT;
-    // Projection of Camera.h:109-116: starts from the identity, so [3][3] stays 1.
+// Projection of Camera.h:109-116 (column-major; it starts from the identity, so [3][3] stays 1).
+static void lumen_projection(float fov_deg, uint32_t width, uint32_t height, double P[16]) {
     const float cam_near = 0.01f, cam_far = 1000.0f;
     const float aspect = (float)width / (float)height;
     const float half = fov_deg / 2.0f * (3.14159265358979323846f / 180.0f);
-    double P[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    for (int i = 0; i < 16; i++) P[i] = (i % 5 == 0) ? 1.0 : 0.0;
     P[0] = 1.0f / (aspect * tanf(half));
     P[5] = -1.0f / tanf(half);
     P[10] = cam_far / (cam_near - cam_far);
     P[11] = -1.0;
     P[14] = cam_near * cam_far / (cam_near - cam_far);
+}
+
+LGB_API lgb_status lgb_camera_from_matrix(const float camera_to_world[16], float fov_deg, uint32_t width,
+                                          uint32_t height, lgb_camera* out) {
+    if (!camera_to_world || !out || width == 0 || height == 0 || !(fov_deg > 0.0f && fov_deg < 180.0f))
+        return LGB_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < 16; i++)
+        if (!std::isfinite(camera_to_world[i])) return LGB_ERR_INVALID_ARGUMENT;
+    double P[16], ip[16];
+    lumen_projection(fov_deg, width, height, P);
+    invert4(P, ip);
+    for (int i = 0; i < 16; i++) { out->inv_view[i] = camera_to_world[i]; out->inv_projection[i] = (float)ip[i]; }
+    out->width = width;
+    out->height = height;
+    return LGB_OK;
+}
+
+LGB_API lgb_status lgb_camera_lookat(const float pos[3], const float dir[3], float fov_deg, uint32_t width,
+                                     uint32_t height, lgb_camera* out) {
+    if (!pos || !dir || !out || width == 0 || height == 0 || !(fov_deg > 0.0f && fov_deg < 180.0f))
+        return LGB_ERR_INVALID_ARGUMENT;
+    double P[16];
+    lumen_projection(fov_deg, width, height, P);
     // View: left-handed look-at with up (0, 1, 0) (Camera.h:74).
     double f[3] = {dir[0], dir[1], dir[2]};
     double fl = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);

@@ -225,9 +225,28 @@ __device__ __forceinline__ void add_rough_grad(const DiffArgs& A, GradAcc& g, co
     atomicAdd(m < kDiffRegMaterials ? &g.rough[m] : &A.g_rough[m], v);
 }
 
+// Warp-aggregated float4 reduction into base[idx]: the active lanes with the same index form one group
+// (__match_any_sync); its lowest lane sums the group's values, taken from each member by shuffles within the
+// group, and issues the one 16-byte reduction. Neighbouring pixels of a coherent bounce land on the same texels,
+// so most groups hold several lanes; a lane alone in its group reduces directly.
+__device__ __forceinline__ void red_add_f4_aggregated(float4* base, uint32_t idx, float4 v) {
+    const unsigned active = __activemask();
+    const unsigned peers = __match_any_sync(active, idx);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    unsigned rest = peers & ~(1u << leader);
+    while (rest) {  // every member runs the same iterations: the group shares `peers`
+        const int m = __ffs(rest) - 1;
+        rest &= rest - 1u;
+        const float x = __shfl_sync(peers, v.x, m), y = __shfl_sync(peers, v.y, m), z = __shfl_sync(peers, v.z, m);
+        if (lane == leader) { v.x += x; v.y += y; v.z += z; }
+    }
+    if (lane == leader) atomicAdd(base + idx, v);
+}
+
 // Texel gradients of one vertex. All BSDF values of a textured diffuse vertex share the texture lookup, so
 // their d loss / d ln f add up first: f_c = base_c * tex_c / pi gives d loss / d texel_{i,c} = sf_c * w_i / tex_c,
-// one float4 reduction per bilinear tap.
+// one warp-aggregated float4 reduction per bilinear tap.
 __device__ __forceinline__ void flush_texel_grad(const DiffArgs& A, const EvalMat& e, v3 sf) {
     if (!e.textured || e.m.type != LGB_BSDF_DIFFUSE) return;
     if (sf.x == 0.0f && sf.y == 0.0f && sf.z == 0.0f) return;
@@ -237,7 +256,7 @@ __device__ __forceinline__ void flush_texel_grad(const DiffArgs& A, const EvalMa
     for (int k = 0; k < 4; k++) {
         const float w = e.tex_w[k];
         if (w == 0.0f) continue;
-        atomicAdd(&A.g_tex[e.tex_i[k]], make_float4(s.x * w, s.y * w, s.z * w, 0.0f));
+        red_add_f4_aggregated(A.g_tex, e.tex_i[k], make_float4(s.x * w, s.y * w, s.z * w, 0.0f));
     }
 }
 
@@ -685,16 +704,26 @@ __device__ __forceinline__ void push_diff_ray(const DiffWave& W, int q, uint32_t
 
 constexpr int kDiffTraceMinBlocks = 9;
 constexpr int kDiffRefill = 16;
+#ifdef LGB_DIFF_POSTPONE
+constexpr bool kDiffPostpone = LGB_DIFF_POSTPONE != 0;
+#else
+constexpr bool kDiffPostpone = false;
+#endif
+#ifdef LGB_DIFF_TRI_MIN
+constexpr int kDiffTriMin = LGB_DIFF_TRI_MIN;
+#else
+constexpr int kDiffTriMin = 0;
+#endif
 __global__ void __launch_bounds__(kDiffThreads, kDiffTraceMinBlocks)
     k_diff_trace(SceneView S, const lgb_ray* __restrict__ rays, lgb_hit* __restrict__ hits, const uint32_t* count,
                  uint32_t* fetch) {
-    trace_persistent<false, false, false, 0, kDiffThreads, kDiffRefill>(S.nodes, S.tris, rays, hits, nullptr, 0u, count,
+    trace_persistent<false, false, kDiffPostpone, 0, kDiffThreads, kDiffRefill, kDiffTriMin>(S.nodes, S.tris, rays, hits, nullptr, 0u, count,
                                                                       fetch, S.status, nullptr, nullptr, nullptr);
 }
 __global__ void __launch_bounds__(kDiffThreads, kDiffTraceMinBlocks)
     k_diff_trace_any(SceneView S, const lgb_ray* __restrict__ rays, uint32_t* __restrict__ bits, const uint32_t* count,
                      uint32_t* fetch) {
-    trace_persistent<true, false, false, 0, kDiffThreads, kDiffRefill>(S.nodes, S.tris, rays, nullptr, bits, 0u, count,
+    trace_persistent<true, false, kDiffPostpone, 0, kDiffThreads, kDiffRefill, kDiffTriMin>(S.nodes, S.tris, rays, nullptr, bits, 0u, count,
                                                                      fetch, S.status, nullptr, nullptr, nullptr);
 }
 

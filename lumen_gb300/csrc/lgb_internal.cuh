@@ -73,6 +73,7 @@ struct Scene;
 struct Ctx {
     int device = 0;
     std::string last_error;
+    std::string tuning_cache;  // lgb_batch_tune's cache file, empty = none
     int sm_count = 0;
     uint32_t users = 0;     // scenes and batches made with this context and not destroyed yet
     bool released = false;  // lgb_destroy was called while users > 0: freed with the last user

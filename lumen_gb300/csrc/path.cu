@@ -16,9 +16,14 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
+#include <fstream>
+#include <map>
 #include <mutex>
+#include <sstream>
 #include <string>
+#include <unistd.h>
 
 #include "path_common.cuh"
 
@@ -193,7 +198,16 @@ __global__ void __launch_bounds__(kThreads) k_camera(const Params* __restrict__ 
 //   one postponed triangle per iteration, 1    336 / 280
 // SK: bottom stack entries per thread in shared memory (0: the whole stack in local memory, the default here:
 // 8 shared entries cost 1 % on the two scenes above, 465 / 296). The batch autotuner tries both placements.
+#ifdef LGB_QUEUE_POSTPONE
+constexpr bool kQueuePostpone = LGB_QUEUE_POSTPONE != 0;
+#else
 constexpr bool kQueuePostpone = false;
+#endif
+#ifdef LGB_QUEUE_TRI_MIN
+constexpr int kQueueTriMin = LGB_QUEUE_TRI_MIN;
+#else
+constexpr int kQueueTriMin = 0;
+#endif
 constexpr int kQueueTraceMinBlocks = 9;
 constexpr int kQueueSharedStack = 8;  // entries when the stack placement is LGB_STACK_SHARED
 // Idle lanes a warp waits for before fetching new rays. Cornell / batch scene, Msamples/s, with the MIS
@@ -204,7 +218,7 @@ __global__ void __launch_bounds__(kThreads, kQueueTraceMinBlocks)
     k_q_trace_closest(SceneView S, const lgb_ray* __restrict__ rays, lgb_hit* __restrict__ hits,
                       const uint32_t* count_ptr, uint32_t* ray_counter, const uint32_t* __restrict__ roots) {
     __shared__ uint2 s_stack[SK > 0 ? SK * kThreads : 1];
-    trace_persistent<false, false, kQueuePostpone, SK, kThreads, kQueueRefill>(
+    trace_persistent<false, false, kQueuePostpone, SK, kThreads, kQueueRefill, kQueueTriMin>(
         S.nodes, S.tris, rays, hits, nullptr, 0u, count_ptr, ray_counter, S.status, nullptr, roots, s_stack);
 }
 template <int SK>
@@ -212,7 +226,7 @@ __global__ void __launch_bounds__(kThreads, kQueueTraceMinBlocks)
     k_q_trace_any(SceneView S, const lgb_ray* __restrict__ rays, uint32_t* __restrict__ bits,
                   const uint32_t* count_ptr, uint32_t* ray_counter, const uint32_t* __restrict__ roots) {
     __shared__ uint2 s_stack[SK > 0 ? SK * kThreads : 1];
-    trace_persistent<true, false, kQueuePostpone, SK, kThreads, kQueueRefill>(
+    trace_persistent<true, false, kQueuePostpone, SK, kThreads, kQueueRefill, kQueueTriMin>(
         S.nodes, S.tris, rays, nullptr, bits, 0u, count_ptr, ray_counter, S.status, nullptr, roots, s_stack);
 }
 
@@ -1081,8 +1095,85 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
 // Times every candidate (queue size x shading grid, stack in local memory) on a quarter of each job's frames,
 // films untouched, then the best of them with the stack bottom in shared memory; the first run of a candidate
 // records its graph, the second is timed.
+// ---- the tuning cache (lgb_create's tuning_cache_path) ----
+// One line per choice: "<key> <path_capacity> <work_blocks_per_sm> <trace_blocks_per_sm> <stack_placement>". The
+// key names the device (name, SM count, compute capability), the ABI version and the batch's shape: job count,
+// and the powers of two of its samples, of its largest image and of its triangles, its deepest path and the union
+// of its scenes' BSDF types. A later line replaces an earlier one with the same key.
+std::string tune_key(const Batch* b, const lgb_batch_job* jobs, uint32_t n) {
+    cudaDeviceProp prop;
+    std::memset(&prop, 0, sizeof(prop));
+    cudaGetDeviceProperties(&prop, b->ctx->device);
+    std::string dev = prop.name;
+    for (char& ch : dev)
+        if (ch == ' ' || ch == '\t' || ch == ';') ch = '_';
+    uint64_t samples = 0, tris = 0;
+    uint32_t max_npix = 1, depth = 0, bsdf = 0;
+    std::vector<bool> seen(b->scenes.size(), false);
+    for (uint32_t i = 0; i < n; i++) {
+        const lgb_batch_job& j = jobs[i];
+        const uint64_t npix = (uint64_t)j.camera.width * j.camera.height;
+        samples += npix * j.spp;
+        max_npix = std::max<uint32_t>(max_npix, (uint32_t)npix);
+        depth = std::max<uint32_t>(depth, (uint32_t)std::max(j.params.max_depth, 0));
+        const Scene* s = b->scenes[j.scene];
+        bsdf |= s->bsdf_mask;
+        if (!seen[j.scene]) { seen[j.scene] = true; tris += s->num_tris; }
+    }
+    auto lg = [](uint64_t v) { int k = 0; while (v > 1) { v >>= 1; k++; } return k; };
+    std::ostringstream k;
+    k << "dev=" << dev << ";sm=" << prop.multiProcessorCount << ";cc=" << prop.major << "." << prop.minor
+      << ";abi=" << lgb_abi_version() << ";jobs=" << n << ";samples=2^" << lg(samples) << ";pix=2^" << lg(max_npix)
+      << ";tris=2^" << lg(tris) << ";depth=" << depth << ";bsdf=" << bsdf;
+    return k.str();
+}
+
+std::map<std::string, lgb_batch_opts> read_tune_cache(const std::string& path) {
+    std::map<std::string, lgb_batch_opts> m;
+    std::ifstream f(path);
+    std::string line;
+    while (std::getline(f, line)) {
+        std::istringstream ls(line);
+        std::string key;
+        lgb_batch_opts o{};
+        if (ls >> key >> o.path_capacity >> o.work_blocks_per_sm >> o.trace_blocks_per_sm >> o.stack_placement)
+            m[key] = o;
+    }
+    return m;
+}
+
+// Adds or replaces one entry: the file is rewritten through a temporary file renamed over it, so a reader never
+// sees half a file.
+void write_tune_cache(const std::string& path, const std::string& key, const lgb_batch_opts& o) {
+    std::map<std::string, lgb_batch_opts> m = read_tune_cache(path);
+    m[key] = o;
+    const std::string tmp = path + ".tmp." + std::to_string((long)getpid());
+    {
+        std::ofstream f(tmp, std::ios::trunc);
+        if (!f) return;
+        for (const auto& e : m)
+            f << e.first << ' ' << e.second.path_capacity << ' ' << e.second.work_blocks_per_sm << ' '
+              << e.second.trace_blocks_per_sm << ' ' << e.second.stack_placement << '\n';
+        if (!f) { std::remove(tmp.c_str()); return; }
+    }
+    if (std::rename(tmp.c_str(), path.c_str()) != 0) std::remove(tmp.c_str());
+}
+
 lgb_status batch_tune(Batch* b, const lgb_batch_job* jobs, uint32_t n, lgb_batch_opts* best, cudaStream_t st) {
     Ctx* ctx = b->ctx;
+    std::string key;
+    if (!ctx->tuning_cache.empty()) {
+        key = tune_key(b, jobs, n);
+        const auto cache = read_tune_cache(ctx->tuning_cache);
+        const auto it = cache.find(key);
+        if (it != cache.end()) {
+            b->tuned = true;
+            b->tuned_opts = it->second;
+            b->tuned_opts.from_cache = 0;
+            if (best) { *best = it->second; best->from_cache = 1; }
+            return LGB_OK;
+        }
+    }
     std::vector<lgb_batch_job> reduced(jobs, jobs + n);
     uint32_t max_npix = 1;
     for (auto& j : reduced) {
@@ -1132,6 +1223,7 @@ lgb_status batch_tune(Batch* b, const lgb_batch_job* jobs, uint32_t n, lgb_batch
     b->tuned = true;
     b->tuned_opts = best_o;
     if (best) *best = best_o;
+    if (!key.empty()) write_tune_cache(ctx->tuning_cache, key, best_o);
     return LGB_OK;
 }
 

@@ -94,46 +94,6 @@ __device__ __forceinline__ bool tri_intersect(const RayQ& r, float4 a, float4 b,
     return true;
 }
 
-// The same test returning the unnormalised barycentrics V, W and det instead of u = V / det and v = W / det, for
-// a caller that divides only once, for its final hit.
-__device__ __forceinline__ bool tri_intersect_raw(const RayQ& r, float4 a, float4 b, float4 c, float tlim, float& t_out,
-                                                  float& v_out, float& w_out, float& det_out) {
-    const float A0 = __fsub_rn(a.x, r.ox), A1 = __fsub_rn(a.y, r.oy), A2 = __fsub_rn(a.z, r.oz);
-    const float B0 = __fsub_rn(b.x, r.ox), B1 = __fsub_rn(b.y, r.oy), B2 = __fsub_rn(b.z, r.oz);
-    const float C0 = __fsub_rn(c.x, r.ox), C1 = __fsub_rn(c.y, r.oy), C2 = __fsub_rn(c.z, r.oz);
-    const float Akx = comp(A0, A1, A2, r.kx), Aky = comp(A0, A1, A2, r.ky), Akz = comp(A0, A1, A2, r.kz);
-    const float Bkx = comp(B0, B1, B2, r.kx), Bky = comp(B0, B1, B2, r.ky), Bkz = comp(B0, B1, B2, r.kz);
-    const float Ckx = comp(C0, C1, C2, r.kx), Cky = comp(C0, C1, C2, r.ky), Ckz = comp(C0, C1, C2, r.kz);
-    const float Ax = __fsub_rn(Akx, __fmul_rn(r.Sx, Akz));
-    const float Ay = __fsub_rn(Aky, __fmul_rn(r.Sy, Akz));
-    const float Bx = __fsub_rn(Bkx, __fmul_rn(r.Sx, Bkz));
-    const float By = __fsub_rn(Bky, __fmul_rn(r.Sy, Bkz));
-    const float Cx = __fsub_rn(Ckx, __fmul_rn(r.Sx, Ckz));
-    const float Cy = __fsub_rn(Cky, __fmul_rn(r.Sy, Ckz));
-    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
-    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
-    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
-    if (U == 0.0f || V == 0.0f || W == 0.0f) {
-        U = __double2float_rn(__dsub_rn(__dmul_rn((double)Cx, (double)By), __dmul_rn((double)Cy, (double)Bx)));
-        V = __double2float_rn(__dsub_rn(__dmul_rn((double)Ax, (double)Cy), __dmul_rn((double)Ay, (double)Cx)));
-        W = __double2float_rn(__dsub_rn(__dmul_rn((double)Bx, (double)Ay), __dmul_rn((double)By, (double)Ax)));
-    }
-    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
-    const float det = __fadd_rn(__fadd_rn(U, V), W);
-    if (det == 0.0f) return false;
-    const float Az = __fmul_rn(r.Sz, Akz);
-    const float Bz = __fmul_rn(r.Sz, Bkz);
-    const float Cz = __fmul_rn(r.Sz, Ckz);
-    const float T = __fadd_rn(__fadd_rn(__fmul_rn(U, Az), __fmul_rn(V, Bz)), __fmul_rn(W, Cz));
-    const float t = __fdiv_rn(T, det);
-    if (!(t >= r.tmin && t <= tlim)) return false;
-    t_out = t;
-    v_out = V;
-    w_out = W;
-    det_out = det;
-    return true;
-}
-
 __device__ __forceinline__ uint4 ldg4(const void* p) { return __ldg(reinterpret_cast<const uint4*>(p)); }
 __device__ __forceinline__ float4 ldg4f(const void* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
 
@@ -262,10 +222,9 @@ __device__ __forceinline__ void intersect_node(const RayQ& r, const WideNode* __
 //   others wait), never both. A warp runs a triangle iteration once at least TRI_MIN of its lanes have a
 //   pending triangle, or when every active lane has one. Each lane still tests and visits in its own order, so
 //   hits are unchanged; what changes is that a warp no longer issues both code paths in one iteration.
-//   DEFER_UV: the closest-hit candidates keep V, W and det, and u = V / det, v = W / det are divided once, for
-//   the final hit (same divisions, same results).
-template <bool ANY, bool COUNT, bool POSTPONE = true, int SK = 0, int THREADS = 128, int REFILL = 1, int TRI_MIN = 0,
-          bool DEFER_UV = false>
+//   TRI_MIN < 0: the same with a relative threshold, a triangle iteration once at least 1 / -TRI_MIN of the
+//   active lanes have a pending triangle.
+template <bool ANY, bool COUNT, bool POSTPONE = true, int SK = 0, int THREADS = 128, int REFILL = 1, int TRI_MIN = 0>
 __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ nodes, const WideTri* __restrict__ tris,
                                                  const lgb_ray* __restrict__ rays, lgb_hit* __restrict__ hits,
                                                  uint32_t* __restrict__ occ_bits, uint32_t n, const uint32_t* count_ptr,
@@ -284,7 +243,7 @@ __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ no
     uint2* const my_stack = SK > 0 ? sstack + threadIdx.x : nullptr;
     int sp = 0;
     uint32_t ray_id = 0, g_base = 0, g_hm = 0, best = LGB_NO_HIT, visits = 0;
-    float t_best = 0.0f, u_best = 0.0f, v_best = 0.0f, det_best = 1.0f;
+    float t_best = 0.0f, u_best = 0.0f, v_best = 0.0f;
     uint32_t n_nodes = 0, n_tris = 0;
     uint32_t p_base = 0, p_hits = 0;  // leaf triangles of the last node visited that are still to be tested
     bool active = false, exhausted = false;
@@ -317,11 +276,12 @@ __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ no
             }
         }
         bool tri_phase = false;
-        if (POSTPONE && TRI_MIN > 0) {
+        if (POSTPONE && TRI_MIN != 0) {
             const uint32_t act = __ballot_sync(FULL, active);
             if (act == 0u) break;
             const uint32_t tri = __ballot_sync(FULL, active && p_hits != 0u);
-            tri_phase = tri != 0u && (__popc(tri) >= TRI_MIN || tri == act);
+            const bool enough = TRI_MIN > 0 ? __popc(tri) >= TRI_MIN : __popc(tri) * (-TRI_MIN) >= __popc(act);
+            tri_phase = tri != 0u && (enough || tri == act);
         } else if (!__any_sync(FULL, active)) {
             break;
         }
@@ -338,10 +298,8 @@ __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ no
                 const WideTri* tp = tris + p_base + k;
                 const float4 a = ldg4f(&tp->a), b = ldg4f(&tp->b), c = ldg4f(&tp->c);
                 if (COUNT) n_tris++;
-                float t, u, v, dt;
-                const bool hit = DEFER_UV && !ANY ? tri_intersect_raw(r, a, b, c, t_best, t, u, v, dt)
-                                                  : tri_intersect(r, a, b, c, ANY ? r.tmax : t_best, t, u, v);
-                if (hit) {
+                float t, u, v;
+                if (tri_intersect(r, a, b, c, ANY ? r.tmax : t_best, t, u, v)) {
                     if (ANY) {
                         occluded = true;
                         done = true;
@@ -352,7 +310,6 @@ __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ no
                             best = prim;
                             u_best = u;
                             v_best = v;
-                            if (DEFER_UV) det_best = dt;
                         }
                     }
                 }
@@ -411,11 +368,8 @@ __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ no
                                 const WideTri* tp = tris + p_base + k;
                                 const float4 a = ldg4f(&tp->a), b = ldg4f(&tp->b), c = ldg4f(&tp->c);
                                 if (COUNT) n_tris++;
-                                float t, u, v, dt;
-                                const bool hit = DEFER_UV && !ANY
-                                                     ? tri_intersect_raw(r, a, b, c, t_best, t, u, v, dt)
-                                                     : tri_intersect(r, a, b, c, ANY ? r.tmax : t_best, t, u, v);
-                                if (hit) {
+                                float t, u, v;
+                                if (tri_intersect(r, a, b, c, ANY ? r.tmax : t_best, t, u, v)) {
                                     if (ANY) {
                                         occluded = true;
                                         done = true;
@@ -427,7 +381,6 @@ __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ no
                                         best = prim;
                                         u_best = u;
                                         v_best = v;
-                                        if (DEFER_UV) det_best = dt;
                                     }
                                 }
                             }
@@ -439,10 +392,6 @@ __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ no
                 if (ANY) {
                     if (occluded) atomicOr(&occ_bits[ray_id >> 5], 1u << (ray_id & 31u));
                 } else {
-                    if (DEFER_UV && best != LGB_NO_HIT) {
-                        u_best = __fdiv_rn(u_best, det_best);
-                        v_best = __fdiv_rn(v_best, det_best);
-                    }
                     uint4 out = make_uint4(best, __float_as_uint(best == LGB_NO_HIT ? 0.0f : t_best),
                                            __float_as_uint(u_best), __float_as_uint(v_best));
                     reinterpret_cast<uint4*>(hits)[ray_id] = out;

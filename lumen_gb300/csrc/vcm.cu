@@ -201,16 +201,26 @@ __device__ __forceinline__ void push_ray(const Wave& W, int q, uint32_t* counter
 
 constexpr int kWaveTraceMinBlocks = 9;
 constexpr int kWaveRefill = 16;
+#ifdef LGB_WAVE_POSTPONE
+constexpr bool kWavePostpone = LGB_WAVE_POSTPONE != 0;
+#else
+constexpr bool kWavePostpone = false;
+#endif
+#ifdef LGB_WAVE_TRI_MIN
+constexpr int kWaveTriMin = LGB_WAVE_TRI_MIN;
+#else
+constexpr int kWaveTriMin = 0;
+#endif
 __global__ void __launch_bounds__(kVcmThreads, kWaveTraceMinBlocks)
     k_vcm_trace(SceneView S, const lgb_ray* __restrict__ rays, lgb_hit* __restrict__ hits, const uint32_t* count,
                 uint32_t* fetch) {
-    trace_persistent<false, false, false, 0, kVcmThreads, kWaveRefill>(S.nodes, S.tris, rays, hits, nullptr, 0u, count,
+    trace_persistent<false, false, kWavePostpone, 0, kVcmThreads, kWaveRefill, kWaveTriMin>(S.nodes, S.tris, rays, hits, nullptr, 0u, count,
                                                                      fetch, S.status, nullptr, nullptr, nullptr);
 }
 __global__ void __launch_bounds__(kVcmThreads, kWaveTraceMinBlocks)
     k_vcm_trace_any(SceneView S, const lgb_ray* __restrict__ rays, uint32_t* __restrict__ bits, const uint32_t* count,
                     uint32_t* fetch) {
-    trace_persistent<true, false, false, 0, kVcmThreads, kWaveRefill>(S.nodes, S.tris, rays, nullptr, bits, 0u, count,
+    trace_persistent<true, false, kWavePostpone, 0, kVcmThreads, kWaveRefill, kWaveTriMin>(S.nodes, S.tris, rays, nullptr, bits, 0u, count,
                                                                     fetch, S.status, nullptr, nullptr, nullptr);
 }
 

@@ -70,6 +70,8 @@ LGB_API lgb_status lgbh_scene_get_info(lgbh_scene* s, lgbh_scene_info* out) {
     out->base_radius = sc.config.base_radius;
     out->radius_factor = sc.config.radius_factor;
     out->enable_vm = sc.config.enable_vm ? 1 : 0;
+    out->cam_use_matrix = sc.config.cam.use_matrix ? 1 : 0;
+    for (int i = 0; i < 16; i++) out->cam_matrix[i] = sc.config.cam.cam_matrix[i];
     return LGB_OK;
 }
 
@@ -89,7 +91,7 @@ LGB_API lgb_status lgbh_render_path(const char* json_path, int device, uint32_t 
                                     const char* out_pfm, float* host_rgba, char* err, size_t errlen) {
     if (!json_path || width == 0 || height == 0) return LGB_ERR_INVALID_ARGUMENT;
     lgb_ctx* ctx = nullptr;
-    lgb_status st = lgb_create(&ctx, device);
+    lgb_status st = lgb_create(&ctx, device, nullptr);
     if (st != LGB_OK) {
         put_err("lgb_create failed", err, errlen);
         return st;
@@ -118,6 +120,10 @@ LGB_API lgb_status lgbh_render_path(const char* json_path, int device, uint32_t 
             throw std::runtime_error("film read-back failed");
         if (out_pfm) lgbh::write_image(out_pfm, film.data(), width, height);
         if (host_rgba) std::memcpy(host_rgba, film.data(), film.size() * 4);
+    } catch (const lgbh::LgbCallError& e) {
+        put_err(e.what(), err, errlen);
+        lgb_destroy(ctx);
+        return e.status;
     } catch (const std::exception& e) {
         put_err(e.what(), err, errlen);
         lgb_destroy(ctx);

@@ -8,7 +8,7 @@
 namespace lgbh {
 
 void Integrator::check(lgb_status st, const char* what) {
-    if (st != LGB_OK) throw std::runtime_error(std::string(what) + ": " + lgb_last_error(ctx));
+    if (st != LGB_OK) throw LgbCallError(st, std::string(what) + ": " + lgb_last_error(ctx));
 }
 
 void Integrator::init() {
@@ -22,7 +22,10 @@ void Integrator::init() {
 
 bool Integrator::update() {
     const CameraSettings& c = lumen_scene->config.cam;
-    check(lgb_camera_lookat(c.pos, c.dir, c.fov, width, height, &cam), "lgb_camera_lookat");
+    if (c.use_matrix)
+        check(lgb_camera_from_matrix(c.cam_matrix, c.fov, width, height, &cam), "lgb_camera_from_matrix");
+    else
+        check(lgb_camera_lookat(c.pos, c.dir, c.fov, width, height, &cam), "lgb_camera_lookat");
     return updated;
 }
 

@@ -3,12 +3,19 @@
 #pragma once
 #include <cstdint>
 #include <memory>
+#include <stdexcept>
 #include <string>
 
 #include "lgb.h"
 #include "lumen_scene.h"
 
 namespace lgbh {
+
+// A failed lgb_* call inside an integrator, with its status.
+struct LgbCallError : std::runtime_error {
+    LgbCallError(lgb_status s, const std::string& msg) : std::runtime_error(msg), status(s) {}
+    lgb_status status;
+};
 
 class Integrator {
   public:

@@ -10,6 +10,7 @@
 #include <stdexcept>
 
 #include "json.h"
+#include "mitsuba_xml.h"
 
 namespace lgbh {
 namespace {
@@ -49,6 +50,16 @@ long obj_index(const std::string& tok, size_t count) {
     if (i > 0) return i - 1;
     if (i < 0) return (long)count + i;
     return -1;
+}
+
+// reflectance_to_conductor_eta_k (LumenScene.cpp:47-50): eta = 1, k = 2 sqrt(r) / sqrt(max(1 - r, 0.001)), with
+// r clamped to [0, 0.9999].
+void conductor_from_reflectance(const float refl[3], lgb_material& m) {
+    for (int a = 0; a < 3; a++) {
+        const float r = std::min(std::max(refl[a], 0.0f), 0.9999f);
+        m.albedo[a] = 1.0f;
+        m.k[a] = 2.0f * std::sqrt(r) / std::sqrt(std::max(1.0f - r, 0.001f));
+    }
 }
 
 }  // namespace
@@ -149,7 +160,12 @@ void LumenScene::load_obj(const std::string& path) {
     }
 }
 
-void LumenScene::load(const std::string& json_path) {
+void LumenScene::load(const std::string& path) {
+    if (path.size() >= 4 && path.compare(path.size() - 4, 4, ".xml") == 0) load_mitsuba(path);
+    else load_json(path);
+}
+
+void LumenScene::load_json(const std::string& json_path) {
     const Json j = parse_json(read_file(json_path));
     const std::string root = dir_of(json_path);
     // integrator block (LumenScene.cpp:237-247)
@@ -210,12 +226,9 @@ void LumenScene::load(const std::string& json_path) {
             m.bsdf_type = LGB_BSDF_CONDUCTOR;
             m.roughness = b["roughness"].f(0.0f);
             if (!b["reflectance"].is_null()) {
-                // reflectance_to_conductor_eta_k (LumenScene.cpp:47-50): eta = 1, k = 2 sqrt(r) / sqrt(max(1 - r, 0.001))
-                for (int a = 0; a < 3; a++) {
-                    const float r = std::min(std::max((float)b["reflectance"][a].as_number(), 0.0f), 0.9999f);
-                    m.albedo[a] = 1.0f;
-                    m.k[a] = 2.0f * std::sqrt(r) / std::sqrt(std::max(1.0f - r, 0.001f));
-                }
+                float r[3];
+                for (int a = 0; a < 3; a++) r[a] = (float)b["reflectance"][a].as_number();
+                conductor_from_reflectance(r, m);
             }
             if (!b["edge_tint"].is_null()) {
                 // Gulbrandsen's artist-friendly mapping (JCGT 3(4) 2014), as LumenScene.cpp:425-435 applies it
@@ -269,6 +282,277 @@ void LumenScene::load(const std::string& json_path) {
     const float zero3[3] = {0, 0, 0}, z3[3] = {0, 0, 1};
     vec3_of(cam["position"], config.cam.pos, zero3);
     vec3_of(cam["dir"], config.cam.dir, z3);
+    // lights of the "lights" block (LumenScene.cpp:494-512); bounds and area lights follow in finish_lights
+    const Json& jl = j["lights"];
+    std::vector<lgb_light> listed;
+    for (size_t i = 0; i < jl.size(); i++) {
+        const Json& L = jl[i];
+        lgb_light l;
+        std::memset(&l, 0, sizeof(l));
+        vec3_of(L["pos"], l.pos, zero3);
+        vec3_of(L["dir"], l.to, zero3);
+        vec3_of(L["L"], l.L, zero3);
+        const std::string type = L["type"].is_null() ? std::string() : L["type"].as_string();
+        if (type == "spot") l.light_flags = LGB_LIGHT_SPOT | (1u << 4) | (1u << 5);
+        else if (type == "directional") l.light_flags = LGB_LIGHT_DIRECTIONAL | (1u << 5);
+        else throw std::runtime_error("unknown light type '" + type + "'");
+        listed.push_back(l);
+    }
+    finish_lights(listed);
+}
+
+// Mitsuba XML scenes as LumenScene::load_mitsuba_scene reads them (LumenScene.cpp:514-690, over
+// MitsubaParser.cpp:5-147):
+//  - integrator: its type selects the integrator, max_depth is the path length, enable_vm the VCM switch;
+//  - sensor: fov / 2 becomes the camera's fov (LumenScene.cpp:530); its to_world matrix is copied into glm without
+//    transposing (MitsubaParser.cpp:29-35), so the camera sits at the matrix's translation, and the render loop
+//    rebuilds the camera from the Euler angles of its rotation (Camera.h:87-105, then update_view_matrix,
+//    Camera.h:27-39): with R = Rx(a) Ry(b) Rz(c) the rotation of to_world, the camera used is T Ry(b) Rx(a) Rz(c);
+//  - bsdf: twosided / mask wrappers are unwrapped to their first nested BSDF, keeping the outer id; the albedo is
+//    the RGB property named "reflectance" (else another RGB property whose name contains "reflectance"), the
+//    roughness sqrt(alpha), the IOR int_ior, the texture the filename of a nested texture; types map as
+//    LumenScene.cpp:601-660 maps them;
+//  - shape: an OBJ file (one mesh per file), its to_world transform (applied to positions and normals here; Lumen
+//    passes it as the instance transform, the same geometry) and the BSDF its last reference names;
+//  - emitter: sunsky becomes a directional light (L = 100 sun_color sun_scale) and sets the sky colour, which
+//    the renderers then refuse as they refuse JSON directional lights. The reference iterates an unordered map of
+//    properties, so whether sun_scale is applied depends on its hashing; here it always is.
+// One extension: a shape's nested area emitter gives that shape an emissive copy of its material (radiance
+// = the emitter's "radiance" RGB). Lumen ignores nested emitters, so no Mitsuba scene would otherwise hold an area
+// light. Other emitter types are refused.
+void LumenScene::load_mitsuba(const std::string& path) {
+    const MtsScene sc = parse_mitsuba(read_file(path));
+    const std::string root = dir_of(path);
+    struct Bsdf {
+        std::string name, type, texture;
+        float albedo[3] = {1, 1, 1};
+        float roughness = 0.0f, ior = 1.0f;
+    };
+    struct Shape {
+        std::string file;
+        int bsdf = -1;
+        double m[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+        bool emits = false;
+        float L[3] = {0, 0, 0};
+    };
+    std::vector<Bsdf> bsdfs;
+    std::vector<Shape> shapes;
+    std::vector<lgb_light> listed;
+    bool have_sensor = false;
+    double cam_m[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    double sensor_fov = 90.0;
+    for (const MtsObject* o : sc.objects) {
+        if (o->kind == "integrator") {
+            config.integrator = o->plugin;
+            std::transform(config.integrator.begin(), config.integrator.end(), config.integrator.begin(), ::tolower);
+            if (const MtsProperty* p = o->prop("max_depth")) config.path_length = (int)p->number;
+            if (const MtsProperty* p = o->prop("enable_vm")) config.enable_vm = p->boolean;
+        } else if (o->kind == "sensor") {
+            have_sensor = true;
+            if (const MtsProperty* p = o->prop("fov")) sensor_fov = p->number;
+            if (const MtsProperty* p = o->prop("to_world"))
+                if (p->kind == MtsProperty::TRANSFORM) std::memcpy(cam_m, p->m, sizeof(cam_m));
+        } else if (o->kind == "bsdf") {
+            Bsdf b;
+            b.name = o->id;
+            const MtsObject* in = o;
+            while ((in->plugin == "twosided" || in->plugin == "mask") && !in->anonymous.empty()) in = in->anonymous[0];
+            b.type = in->plugin;
+            const MtsProperty* refl = nullptr;
+            for (const auto& pr : in->props)
+                if (pr.second.kind == MtsProperty::COLOR && pr.first.find("reflectance") != std::string::npos)
+                    if (!refl || pr.first == "reflectance") refl = &pr.second;
+            if (refl)
+                for (int a = 0; a < 3; a++) b.albedo[a] = (float)refl->v[a];
+            if (const MtsProperty* p = in->prop("alpha")) b.roughness = (float)std::sqrt(p->number);
+            if (const MtsProperty* p = in->prop("int_ior")) b.ior = (float)p->number;
+            for (const auto& nc : in->named)
+                if (nc.second->kind == "texture")
+                    if (const MtsProperty* f = nc.second->prop("filename")) b.texture = f->text;
+            bsdfs.push_back(b);
+        } else if (o->kind == "shape") {
+            Shape sh;
+            if (const MtsProperty* p = o->prop("filename")) sh.file = p->text;
+            if (const MtsProperty* p = o->prop("to_world"))
+                if (p->kind == MtsProperty::TRANSFORM) std::memcpy(sh.m, p->m, sizeof(sh.m));
+            for (const MtsObject* c : o->anonymous) {
+                if (c->kind == "emitter") {
+                    if (c->plugin != "area") throw std::runtime_error("Mitsuba: shape emitter '" + c->plugin + "' is not supported");
+                    sh.emits = true;
+                    if (const MtsProperty* p = c->prop("radiance"))
+                        for (int a = 0; a < 3; a++) sh.L[a] = (float)p->v[a];
+                    continue;
+                }
+                for (size_t i = 0; i < bsdfs.size(); i++)
+                    if (bsdfs[i].name == c->id) sh.bsdf = (int)i;
+            }
+            if (sh.file.empty()) {
+                std::fprintf(stderr, "lgbh: Mitsuba shape '%s' has no OBJ file and is skipped (as Lumen skips it)\n",
+                             o->plugin.c_str());
+                continue;
+            }
+            if (o->plugin != "obj") throw std::runtime_error("Mitsuba: shape type '" + o->plugin + "' is not read (OBJ only)");
+            if (sh.bsdf < 0) throw std::runtime_error("Mitsuba: shape '" + sh.file + "' names no BSDF defined before it");
+            shapes.push_back(sh);
+        } else if (o->kind == "emitter") {
+            if (o->plugin != "sunsky")
+                throw std::runtime_error("Mitsuba: emitter type '" + o->plugin +
+                                         "' is not read (Lumen's reader maps 'sunsky' only; area emitters go inside a shape)");
+            lgb_light l;
+            std::memset(&l, 0, sizeof(l));
+            l.light_flags = LGB_LIGHT_DIRECTIONAL | (1u << 5);
+            const MtsProperty* dir = o->prop("sun_direction");
+            const MtsProperty* col = o->prop("sun_color");
+            const MtsProperty* scale = o->prop("sun_scale");
+            const MtsProperty* sky = o->prop("sky_color");
+            for (int a = 0; a < 3; a++) {
+                l.pos[a] = dir ? (float)dir->v[a] : 0.0f;
+                l.L[a] = 100.0f * (col ? (float)col->v[a] : 0.0f) * (scale ? (float)scale->number : 1.0f);
+                if (sky) config.sky_col[a] = (float)sky->v[a];
+            }
+            listed.push_back(l);
+        }
+    }
+    // meshes (LumenScene.cpp:537-587): one per OBJ file, in shape order, transformed to world space
+    for (const Shape& sh : shapes) {
+        const size_t m0 = meshes.size();
+        load_obj(root + sh.file);
+        if (meshes.size() == m0) throw std::runtime_error("Mitsuba: " + sh.file + " has no faces");
+        lgb_mesh merged = meshes[m0];
+        merged.tri_count = 0;
+        for (size_t k = m0; k < meshes.size(); k++) merged.tri_count += meshes[k].tri_count;
+        for (uint32_t k = 0; k < 3 * merged.tri_count; k++) indices[merged.index_offset + k] = k;
+        meshes.resize(m0);
+        mesh_names.resize(m0);
+        merged.material_index = (uint32_t)sh.bsdf;
+        meshes.push_back(merged);
+        mesh_names.push_back(sh.file);
+        const double* M = sh.m;
+        bool ident = true;
+        for (int i = 0; i < 16; i++) ident = ident && M[i] == ((i % 5 == 0) ? 1.0 : 0.0);
+        if (!ident) {
+            // normals by the inverse transpose of the upper 3x3 (its cofactor matrix, up to a scale that the
+            // normalisation removes)
+            const double a = M[0], b = M[1], c = M[2], d = M[4], e = M[5], f = M[6], g = M[8], h = M[9], i = M[10];
+            const double cof[9] = {e * i - f * h, f * g - d * i, d * h - e * g,
+                                   c * h - b * i, a * i - c * g, b * g - a * h,
+                                   b * f - c * e, c * d - a * f, a * e - b * d};
+            for (size_t v = merged.vertex_offset; v < merged.vertex_offset + 3ull * merged.tri_count; v++) {
+                float* p = &positions[3 * v];
+                float* n = &normals[3 * v];
+                const double px = p[0], py = p[1], pz = p[2], nx = n[0], ny = n[1], nz = n[2];
+                for (int r = 0; r < 3; r++) p[r] = (float)(M[4 * r] * px + M[4 * r + 1] * py + M[4 * r + 2] * pz + M[4 * r + 3]);
+                double q[3];
+                for (int r = 0; r < 3; r++) q[r] = cof[3 * r] * nx + cof[3 * r + 1] * ny + cof[3 * r + 2] * nz;
+                const double l = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+                for (int r = 0; r < 3; r++) n[r] = l > 0.0 ? (float)(q[r] / l) : 0.0f;
+            }
+        }
+    }
+    // materials (LumenScene.cpp:589-660); make_default_principled leaves every field but these at zero
+    materials.assign(std::max<size_t>(bsdfs.size(), 1), default_material());
+    for (size_t bi = 0; bi < bsdfs.size(); bi++) {
+        const Bsdf& b = bsdfs[bi];
+        lgb_material& m = materials[bi];
+        if (!b.texture.empty()) {
+            const std::string tex = root + b.texture;
+            if (tex.size() >= 4 && tex.compare(tex.size() - 4, 4, ".pfm") == 0) {
+                textures.push_back(read_pfm(tex));
+                m.texture_id = (int)textures.size() - 1;
+            } else {
+                std::fprintf(stderr, "lgbh: texture %s skipped (only PFM textures are read)\n", tex.c_str());
+            }
+        }
+        for (int a = 0; a < 3; a++) m.albedo[a] = b.albedo[a];
+        m.roughness = b.roughness;
+        if (b.type == "diffuse") {
+            m.bsdf_type = LGB_BSDF_DIFFUSE;
+            m.bsdf_props = LGB_FLAG_DIFFUSE | LGB_FLAG_REFLECTION;
+        } else if (b.type == "roughplastic" || b.type == "roughdielectric" || b.type == "dielectric" || b.type == "plastic") {
+            m.bsdf_type = LGB_BSDF_PRINCIPLED;
+            m.ior = b.ior;
+            if (m.roughness < 1.0f) m.bsdf_props |= LGB_FLAG_DIFFUSE | LGB_FLAG_REFLECTION;
+            if (m.ior != 1.0f) m.bsdf_props |= LGB_FLAG_TRANSMISSION;
+            m.bsdf_props |= m.roughness > 0.08f ? LGB_FLAG_GLOSSY : LGB_FLAG_SPECULAR;
+            if (b.type == "roughdielectric" || b.type == "dielectric") {
+                m.spec_trans = 1.0f;
+                m.metallic = 0.0f;
+            } else {  // Mitsuba's plastics mapped as LumenScene.cpp:629-635 maps them
+                m.metallic = 1.0f;
+                m.subsurface = 0.1f;
+                m.spec_trans = 0.5f;
+                m.thin = 1;
+            }
+        } else if (b.type == "conductor" || b.type == "roughconductor") {
+            m.bsdf_type = LGB_BSDF_CONDUCTOR;
+            conductor_from_reflectance(b.albedo, m);
+            m.bsdf_props = LGB_FLAG_REFLECTION | (m.roughness > 0.08f ? LGB_FLAG_GLOSSY : LGB_FLAG_SPECULAR);
+        } else if (b.type == "glass") {
+            m.bsdf_type = LGB_BSDF_GLASS;
+            m.bsdf_props = LGB_FLAG_SPECULAR | LGB_FLAG_TRANSMISSION;
+            m.ior = b.ior;
+        } else {
+            std::fprintf(stderr, "lgbh: Mitsuba bsdf type '%s' is not one Lumen's loader maps; the material reflects "
+                                 "nothing\n", b.type.c_str());
+        }
+    }
+    // the extension: emissive copies of the materials of shapes with an area emitter
+    for (size_t k = 0; k < shapes.size(); k++) {
+        if (!shapes[k].emits) continue;
+        lgb_material em = materials[meshes[k].material_index];
+        for (int a = 0; a < 3; a++) em.emissive_factor[a] = shapes[k].L[a];
+        materials.push_back(em);
+        meshes[k].material_index = (uint32_t)materials.size() - 1;
+    }
+    // camera (LumenScene.cpp:528-534, 59-68; Camera.h:87-105, 27-39)
+    if (have_sensor) {
+        config.cam.use_matrix = true;
+        config.cam.fov = (float)(sensor_fov / 2.0);
+        const double* M = cam_m;
+        double R[3][3];
+        for (int c = 0; c < 3; c++) {  // rotation: the upper 3x3 with its columns normalised (scale removed)
+            const double l = std::sqrt(M[c] * M[c] + M[4 + c] * M[4 + c] + M[8 + c] * M[8 + c]);
+            for (int r = 0; r < 3; r++) R[r][c] = l > 0.0 ? M[4 * r + c] / l : 0.0;
+        }
+        const double ax = std::atan2(-R[1][2], R[2][2]);
+        const double ay = std::asin(std::min(1.0, std::max(-1.0, R[0][2])));
+        const double az = std::atan2(-R[0][1], R[0][0]);
+        auto rot = [](int axis, double t, double out[3][3]) {
+            const double c = std::cos(t), s = std::sin(t);
+            for (int r = 0; r < 3; r++)
+                for (int q = 0; q < 3; q++) out[r][q] = r == q ? 1.0 : 0.0;
+            const int u = (axis + 1) % 3, v = (axis + 2) % 3;
+            out[u][u] = c; out[u][v] = -s; out[v][u] = s; out[v][v] = c;
+        };
+        auto mul = [](const double a[3][3], const double b[3][3], double out[3][3]) {
+            double t[3][3];
+            for (int r = 0; r < 3; r++)
+                for (int q = 0; q < 3; q++) t[r][q] = a[r][0] * b[0][q] + a[r][1] * b[1][q] + a[r][2] * b[2][q];
+            std::memcpy(out, t, sizeof(t));
+        };
+        double Ry[3][3], Rx[3][3], Rz[3][3], C[3][3];
+        rot(1, ay, Ry);
+        rot(0, ax, Rx);
+        rot(2, az, Rz);
+        mul(Ry, Rx, C);
+        mul(C, Rz, C);
+        float* out = config.cam.cam_matrix;  // column-major
+        for (int c = 0; c < 3; c++) {
+            for (int r = 0; r < 3; r++) out[4 * c + r] = (float)C[r][c];
+            out[4 * c + 3] = 0.0f;
+        }
+        out[12] = (float)M[3];
+        out[13] = (float)M[7];
+        out[14] = (float)M[11];
+        out[15] = 1.0f;
+        for (int a = 0; a < 3; a++) config.cam.pos[a] = out[12 + a];
+    }
+    finish_lights(listed);
+}
+
+// Scene bounds, then the light list as LumenScene::load_scene builds it (LumenScene.cpp:70-113): every mesh with
+// an emissive material becomes an area light, then the listed lights follow with the scene's centre and radius.
+void LumenScene::finish_lights(const std::vector<lgb_light>& listed) {
     // scene bounds (LumenScene.cpp:732-751): from the meshes' vertex bounds; a degenerate box becomes [-1, 1]^3
     float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (size_t i = 0; i < positions.size(); i += 3)
@@ -279,7 +563,6 @@ void LumenScene::load(const std::string& json_path) {
     float d2 = 0.0f;
     for (int a = 0; a < 3; a++) { bbox_min[a] = lo[a]; bbox_max[a] = hi[a]; d2 += (hi[a] - lo[a]) * (hi[a] - lo[a]); }
     radius = std::sqrt(d2) * 0.5f;
-    // lights (LumenScene.cpp:74-113): emissive meshes become area lights, then the JSON lights
     total_light_triangle_cnt = 0;
     for (size_t s = 0; s < meshes.size(); s++) {
         const lgb_material& mat = materials[meshes[s].material_index];
@@ -306,21 +589,13 @@ void LumenScene::load(const std::string& json_path) {
             }
         }
     }
-    const Json& jl = j["lights"];
-    for (size_t i = 0; i < jl.size(); i++) {
-        const Json& L = jl[i];
-        lgb_light l;
-        std::memset(&l, 0, sizeof(l));
+    for (size_t i = 0; i < listed.size(); i++) {
+        lgb_light l = listed[i];
+        std::memset(l.world_matrix, 0, sizeof(l.world_matrix));
         for (int k = 0; k < 4; k++) l.world_matrix[5 * k] = 1.0f;
-        vec3_of(L["pos"], l.pos, zero3);
-        vec3_of(L["dir"], l.to, zero3);
-        vec3_of(L["L"], l.L, zero3);
-        const std::string type = L["type"].is_null() ? std::string() : L["type"].as_string();
-        if (type == "spot") l.light_flags = LGB_LIGHT_SPOT | (1u << 4) | (1u << 5);
-        else if (type == "directional") l.light_flags = LGB_LIGHT_DIRECTIONAL | (1u << 5);
-        else throw std::runtime_error("unknown light type '" + type + "'");
         l.world_radius = radius;
         for (int a = 0; a < 3; a++) l.world_center[a] = 0.5f * (bbox_max[a] + bbox_min[a]);
+        // the index into the listed lights, as LumenScene.cpp:104-106 records it
         if ((l.light_flags & 7u) == LGB_LIGHT_DIRECTIONAL) dir_light_idx = (uint32_t)i;
         total_light_triangle_cnt++;
         lights.push_back(l);

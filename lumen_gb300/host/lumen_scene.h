@@ -19,6 +19,10 @@ struct CameraSettings {  // SceneConfig.h:6-11
     float fov = 45.0f;
     float pos[3] = {0, 0, 0};
     float dir[3] = {0, 0, 1};
+    // Mitsuba sensors give a matrix instead (LumenScene.cpp:64-68): the camera-to-world matrix the render loop
+    // uses, column-major, after Lumen's Euler-angle round trip (see LumenScene::load_mitsuba).
+    bool use_matrix = false;
+    float cam_matrix[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
 };
 
 struct SceneConfig {  // SceneConfig.h:15-63 (the fields the Path and VCM integrators read)
@@ -33,8 +37,9 @@ struct SceneConfig {  // SceneConfig.h:15-63 (the fields the Path and VCM integr
 
 class LumenScene {
   public:
-    // Loads a Lumen JSON scene and the OBJ it names. Throws std::runtime_error with a message on failure.
-    void load(const std::string& json_path);
+    // Loads a Lumen JSON scene and the OBJ it names, or a Mitsuba XML scene and its OBJ shapes (by extension,
+    // as LumenScene::load_scene, LumenScene.cpp:52-57). Throws std::runtime_error with a message on failure.
+    void load(const std::string& path);
 
     // Flat arrays, exactly as the C ABI takes them.
     std::vector<float> positions, normals, uvs;  // 3, 3, 2 floats per vertex
@@ -54,6 +59,9 @@ class LumenScene {
     std::vector<lgb_texture> texture_views() const;
 
   private:
+    void load_json(const std::string& path);
+    void load_mitsuba(const std::string& path);
+    void finish_lights(const std::vector<lgb_light>& listed);
     void load_obj(const std::string& path);
     mutable std::vector<lgb_texture> tex_views_;
 };

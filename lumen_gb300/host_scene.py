@@ -17,7 +17,8 @@ class SceneInfo(C.Structure):
                 ("path_length", C.c_int32), ("sky_col", C.c_float * 3), ("light_triangle_count", C.c_uint32),
                 ("dir_light_idx", C.c_uint32), ("total_light_area", C.c_float), ("bbox_min", C.c_float * 3),
                 ("bbox_max", C.c_float * 3), ("radius", C.c_float), ("base_radius", C.c_float),
-                ("radius_factor", C.c_float), ("enable_vm", C.c_int32)]
+                ("radius_factor", C.c_float), ("enable_vm", C.c_int32), ("cam_use_matrix", C.c_int32),
+                ("cam_matrix", C.c_float * 16)]
 
 
 _lib = None
@@ -46,7 +47,8 @@ def load():
 
 
 def load_scene(json_path: str):
-    """Loads a Lumen JSON scene with the C++ loader; returns (SceneArrays, SceneInfo)."""
+    """Loads a Lumen JSON scene (or a Mitsuba XML scene, by extension) with the C++ loader; returns
+    (SceneArrays, SceneInfo)."""
     lib = load()
     h = C.c_void_p()
     err = C.create_string_buffer(512)
@@ -94,7 +96,8 @@ def write_image(path: str, film: np.ndarray, width: int, height: int):
 
 
 def render_path(json_path: str, width: int, height: int, spp: int, out_pfm: str | None = None, device: int = 0):
-    """Headless render through the C++ Integrator mirror; returns the RGBA32F film as an (H*W, 4) array."""
+    """Headless render through the C++ Integrator mirror; returns the RGBA32F film as an (H*W, 4) array. The scene is
+    a Lumen JSON or a Mitsuba XML file."""
     lib = load()
     film = np.zeros((width * height, 4), np.float32)
     err = C.create_string_buffer(512)

@@ -179,13 +179,24 @@ def camera_lookat(pos, direction, fov, width, height) -> abi.Camera:
     return cam
 
 
+def camera_from_matrix(camera_to_world, fov, width, height) -> abi.Camera:
+    """lgb_camera_from_matrix: camera_to_world is 16 floats, column-major (as lgbh_scene_info.cam_matrix)."""
+    lib = abi.load()
+    cam = abi.Camera()
+    m = (C.c_float * 16)(*[float(x) for x in camera_to_world])
+    st = lib.lgb_camera_from_matrix(m, float(fov), int(width), int(height), C.byref(cam))
+    if st != abi.LGB_OK:
+        raise abi.LgbError(st, "lgb_camera_from_matrix")
+    return cam
+
+
 class Context:
     """An lgb_ctx on one CUDA device (the counterpart of Lumen's Vulkan context)."""
 
-    def __init__(self, device: int = 0):
+    def __init__(self, device: int = 0, tuning_cache: str | None = None):
         self.lib = abi.load()
         h = C.c_void_p()
-        st = self.lib.lgb_create(C.byref(h), device)
+        st = self.lib.lgb_create(C.byref(h), device, tuning_cache.encode() if tuning_cache else None)
         if st != abi.LGB_OK:
             raise abi.LgbError(st, f"lgb_create(device={device})")
         self.handle = h

@@ -121,6 +121,8 @@ void orc_render_samples(void* scene, const float inv_view[16], const float inv_p
                         const orc_path_params* params, const uint32_t* pixels, uint32_t n_pixels,
                         float* out_rgb, uint8_t* out_nan, int fp64, int nthreads);
 // Progressive film exactly as path.rgen:102-112 writes it: frames [frame0, frame0+spp) into film (RGBA32F).
+void orc_render_mean_f64(void* h, const float inv_view[16], const float inv_proj[16], const orc_path_params* params,
+                         uint32_t frame0, uint32_t spp, double* out, int nthreads);
 void orc_render_film(void* scene, const float inv_view[16], const float inv_proj[16],
                      const orc_path_params* params, uint32_t frame0, uint32_t spp, float* film, int fp64,
                      int nthreads);
@@ -157,6 +159,9 @@ void orc_vcm_iteration(void* scene, const float inv_view[16], const float inv_pr
                        const float proj[16], uint32_t width, uint32_t height, const orc_vcm_params* p,
                        orc_vcm_vertex* verts, uint32_t* counts, float* splat, uint32_t* grid_count, uint32_t* grid_rep,
                        float* film, int nthreads);
+void orc_vcm_render_f64(void* scene, const float inv_view[16], const float inv_proj[16], const float view[16],
+                        const float proj[16], uint32_t width, uint32_t height, const orc_vcm_params* params,
+                        uint32_t n_iters, double* film, int nthreads);
 // SPPM (SPPM.cpp:78-184): one frame. vp (W*H*32 floats), photons (W*H*max_depth*16 floats), grid_count and
 // grid_rep (10*W*H) and film (W*H*4, row-major) persist across frames; vp must be zero before frame 0. The
 // visible-point and photon layouts are the library's (8 and 4 float4, integer fields stored as their bits).

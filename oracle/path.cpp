@@ -348,6 +348,29 @@ void orc_render_samples(void* h, const float inv_view[16], const float inv_proj[
     });
 }
 
+// Converged reference renders: the plain FP64 mean of the samples of frames [frame0, frame0 + spp) per pixel
+// (NaN samples skipped), into out (npix * 3 doubles). Unlike the progressive film it does not assume the frames
+// start at 0, so a reference can use frames the renders it is compared with do not.
+void orc_render_mean_f64(void* h, const float inv_view[16], const float inv_proj[16], const orc_path_params* params,
+                         uint32_t frame0, uint32_t spp, double* out, int nthreads) {
+    const Scene& s = *(Scene*)h;
+    const uint32_t n = params->size_x * params->size_y;
+    parallel_for(n, nthreads, [&](uint32_t pix) {
+        const uint32_t x = pix % params->size_x, y = pix / params->size_x;
+        orc_path_params pc = *params;
+        double sum[3] = {0.0, 0.0, 0.0};
+        uint32_t valid = 0;
+        for (uint32_t f = frame0; f < frame0 + spp; f++) {
+            pc.frame_num = f;
+            const V3<double> col = path_sample<double>(s, load_m4<double>(inv_view), load_m4<double>(inv_proj), pc, x, y);
+            if (std::isnan(luminance(col))) continue;
+            sum[0] += col.x; sum[1] += col.y; sum[2] += col.z;
+            valid++;
+        }
+        for (int k = 0; k < 3; k++) out[3 * (size_t)pix + k] = valid ? sum[k] / valid : 0.0;
+    });
+}
+
 void orc_render_film(void* h, const float inv_view[16], const float inv_proj[16], const orc_path_params* params,
                      uint32_t frame0, uint32_t spp, float* film, int fp64, int nthreads) {
     const Scene& s = *(Scene*)h;

@@ -116,6 +116,10 @@ class Oracle:
         L.orc_vcm_iteration.argtypes = [C.c_void_p] + [C.POINTER(C.c_float)] * 4 + [
             C.c_uint32, C.c_uint32, C.POINTER(VcmParams), C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_float),
             C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_float), C.c_int]
+        L.orc_render_mean_f64.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_void_p,
+                                          C.c_uint32, C.c_uint32, C.POINTER(C.c_double), C.c_int]
+        L.orc_vcm_render_f64.argtypes = [C.c_void_p] + [C.POINTER(C.c_float)] * 4 + [
+            C.c_uint32, C.c_uint32, C.POINTER(VcmParams), C.c_uint32, C.POINTER(C.c_double), C.c_int]
         L.orc_sppm_iteration.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_uint32,
                                          C.c_uint32, C.POINTER(SppmParams), C.POINTER(C.c_float),
                                          C.POINTER(C.c_float), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
@@ -278,6 +282,16 @@ class OracleScene:
                                      threads or (os.cpu_count() or 1))
         return film
 
+    def mean_f64(self, cam, max_depth, width, height, frame0, spp, threads=0):
+        """Plain FP64 mean (npix, 3) of the path samples of frames [frame0, frame0 + spp), NaN samples skipped."""
+        iv = np.ascontiguousarray(np.array(cam.inv_view[:], np.float32))
+        ip = np.ascontiguousarray(np.array(cam.inv_projection[:], np.float32))
+        out = np.zeros((width * height, 3), np.float64)
+        p = self._params(max_depth, width, height, frame0)
+        self.ora.lib.orc_render_mean_f64(self.h, _p(iv), _p(ip), C.byref(p), frame0, spp,
+                                         out.ctypes.data_as(C.POINTER(C.c_double)), threads or (os.cpu_count() or 1))
+        return out
+
     def diff(self, cam, max_depth, width, height, frame0, spp, tex_id=-1, texels=None, rough=None, emis=None,
              fp64=True, threads=0):
         """Mean image (npix, 3) float64 of the detached differentiable estimator over frames [frame0, frame0+spp).
@@ -320,6 +334,18 @@ class OracleScene:
                                        _p(state["grid_rep"], C.c_uint32), _p(state["film"]),
                                        threads or (os.cpu_count() or 1))
         return state["film"]
+
+    def vcm_render_f64(self, cam, view, proj, params_list, threads=0):
+        """len(params_list) VCM iterations in FP64 (converged reference renders); returns the progressive film as
+        (W*H, 4) float64."""
+        f32 = lambda a: np.ascontiguousarray(np.array(a, np.float32).reshape(16))
+        iv, ip, vw, pj = f32(cam.inv_view[:]), f32(cam.inv_projection[:]), f32(view), f32(proj)
+        arr = (VcmParams * len(params_list))(*params_list)
+        film = np.zeros((cam.width * cam.height, 4), np.float64)
+        self.ora.lib.orc_vcm_render_f64(self.h, _p(iv), _p(ip), _p(vw), _p(pj), cam.width, cam.height, arr,
+                                        len(params_list), film.ctypes.data_as(C.POINTER(C.c_double)),
+                                        threads or (os.cpu_count() or 1))
+        return film
 
 
 def sppm_state(width, height, max_depth):

@@ -31,7 +31,7 @@ def test_exports_every_declared_symbol(lib):
         assert hasattr(lib, n), f"{n} is declared in lgb.h but not exported"
         assert n in abi.SIGNATURES, f"{n} has no ctypes signature"
     assert set(abi.SIGNATURES) == set(names)
-    assert lib.lgb_abi_version() == 1
+    assert lib.lgb_abi_version() == 2
 
 
 def test_struct_layouts():

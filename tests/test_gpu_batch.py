@@ -175,3 +175,42 @@ def test_batch_error_paths(ctx, scenes):
     batch.render([Batch.job(0, cam, path_params(arrays, DEPTH), 0, 2, film)])
     batch.sync()
     assert film[:, :3].mean().item() > 0.0
+
+
+def test_tuning_cache_persists_choices(tmp_path):
+    """lgb_create's tuning cache: the first tune of a batch times the candidates and records the choice; a second
+    context on the same cache file (a later process on the same kind of device) gets that choice without timing
+    anything, and a batch of another shape is tuned and added as a second entry."""
+    path = str(tmp_path / "tuning.txt")
+
+    def tune(ctx, jobs):
+        scs = []
+        for seed, tris in ((7, 2000), (8, 12000), (9, 5000)):
+            arrays = procedural.batch_scene(seed, tris)
+            sc = GpuScene(ctx, arrays)
+            sc.build()
+            scs.append((arrays, sc))
+        films = _films(jobs)
+        batch = Batch(ctx, [sc for _, sc in scs])
+        js = [Batch.job(si, _camera(scs[si][0], w, h), path_params(scs[si][0], DEPTH), 0, spp, films[k])
+              for k, (si, w, h, _, spp) in enumerate(jobs)]
+        best = batch.tune(js)
+        batch.sync()
+        batch.close()
+        return best
+
+    jobs = [(0, 48, 40, 0, 3), (1, 64, 64, 0, 5), (2, 32, 32, 0, 2)]
+    first = tune(Context(0, tuning_cache=path), jobs)
+    assert first.from_cache == 0
+    lines = open(path).read().splitlines()
+    assert len(lines) == 1 and ";abi=2;jobs=3;" in lines[0]
+    second = tune(Context(0, tuning_cache=path), jobs)
+    assert second.from_cache == 1
+    assert (second.path_capacity, second.work_blocks_per_sm, second.stack_placement) == \
+        (first.path_capacity, first.work_blocks_per_sm, first.stack_placement)
+    other = tune(Context(0, tuning_cache=path), jobs[:2])
+    assert other.from_cache == 0
+    assert len(open(path).read().splitlines()) == 2
+    # an unreadable cache is ignored: tuning still works
+    bad = tune(Context(0, tuning_cache=str(tmp_path / "missing_dir" / "t.txt")), jobs)
+    assert bad.from_cache == 0

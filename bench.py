@@ -337,13 +337,94 @@ def adjoint_secondary(torch, ctx_cls, scene_cls, local):
     sc.sync(cs)
     mp, ma = float(np.median(tp)), float(np.median(ta))
     rmse = reference_rmse(torch, ctx, film, "diff_512_fp64_ref.npy")
+    grad_norms = {"texels": float(gt.norm()), "roughness": float(gr.norm()), "emission": float(ge.norm())}
+    adam = adam_recovery(torch, sc, arrays, cam, params, w, h, spp, cs)
     return {"workload": "differentiable Cornell box, 512x512, 32 spp, max depth 6, 64x64 RGB texels + per-material "
                         "roughness + emission, L2 image loss", "primal_ms": mp, "adjoint_ms": ma,
             "primal_plus_adjoint_over_primal": (mp + ma) / mp,
             "primal_msamples_per_s": w * h * spp / (mp * 1e-3) / 1e6,
             "rmse_vs_fp64": {"value": rmse, "render": "the primal image, 32 spp, 512x512",
                              "reference": "FP64 CPU oracle, 512 spp (tests/golden/diff_512_fp64_ref.npy)"},
-            "grad_norms": {"texels": float(gt.norm()), "roughness": float(gr.norm()), "emission": float(ge.norm())}}
+            "grad_norms": grad_norms, "adam_200_steps": adam}
+
+
+def adam_recovery(torch, sc, arrays, cam, params, w, h, spp, cs, steps=200):
+    """200 Adam steps at the configuration's size (512^2, 32 spp per step) from the scene's parameters towards a
+    target rendered (256 spp) with another seeded texture (seed 6), box roughnesses 0.2 / 0.3 and emission
+    (14, 12.5, 11). Each step renders fresh frames with lgb_diff_render (sampling with the current values) and
+    replays independent frames with lgb_adjoint_path for d (mean squared image error) / d parameter. Reports the
+    parameter RMSE against the target before and after (texels: those the camera sees directly), the image loss
+    and the time per step. The replay frames get their own primal with stored samples, so the adjoint runs as the
+    wavefront replay of stored samples (three wavefront passes per step)."""
+    from lumen_gb300 import abi, procedural
+    emitter, short, tall = 3, 5, 6
+    tex_t = torch.from_numpy(procedural.albedo_texture(6)).cuda()
+    rough_t = torch.from_numpy(arrays.materials["roughness"].astype(np.float32)).cuda()
+    rough_t[short], rough_t[tall] = 0.2, 0.3
+    emis_t = torch.from_numpy(arrays.materials["emissive_factor"].astype(np.float32)).cuda()
+    emis_t[emitter] = torch.tensor([14.0, 12.5, 11.0])
+    npix = w * h
+    target = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
+    sc.diff_render(cam, params, 1 << 20, 256, target, 0, tex_t, rough_t, emis_t, stream=cs)
+    tex = torch.from_numpy(np.ascontiguousarray(arrays.textures[0])).cuda()
+    rough = torch.from_numpy(arrays.materials["roughness"].astype(np.float32)).cuda()
+    emis = torch.from_numpy(arrays.materials["emissive_factor"].astype(np.float32)).cuda()
+    # texels the camera sees directly: the texel gradient of the image sum at path length 2
+    vis = torch.zeros_like(tex)
+    ones = torch.ones((npix, 4), dtype=torch.float32, device="cuda")
+    p2 = abi.PathParams.from_buffer_copy(params)
+    p2.max_depth = 2
+    sc.adjoint_path(cam, p2, 0, 4, ones, 0, tex, rough, emis, vis, torch.zeros_like(rough), torch.zeros_like(emis),
+                    stream=cs)
+    torch.cuda.synchronize()
+    vis = vis[..., :3].abs().sum(-1)
+    mask = vis > torch.quantile(vis[vis > 0], 0.5)
+
+    def rmse():
+        return {"texels_seen": float((tex - tex_t)[..., :3][mask].pow(2).mean().sqrt()),
+                "roughness": float((rough - rough_t)[[short, tall]].pow(2).mean().sqrt()),
+                "emission": float((emis - emis_t)[emitter].pow(2).mean().sqrt())}
+
+    film = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
+    replay = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
+    samples = torch.empty((spp * npix, 4), dtype=torch.float32, device="cuda")
+
+    def image_loss():
+        sc.diff_render(cam, params, 1 << 22, 64, film, 0, tex, rough, emis, stream=cs)
+        return float(((film[:, :3] - target[:, :3]) ** 2).mean())
+
+    before, loss0 = rmse(), image_loss()
+    state = [(p, torch.zeros_like(p), torch.zeros_like(p), lr) for p, lr in ((tex, 0.05), (rough, 0.01), (emis, 0.2))]
+    g = [torch.zeros_like(tex), torch.zeros_like(rough), torch.zeros_like(emis)]
+    b1, b2, eps = 0.9, 0.999, 1e-8
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for step in range(steps):
+        sc.diff_render(cam, params, step * spp, spp, film, 0, tex, rough, emis, flags=abi.DIFF_SAMPLE_PARAMS,
+                       stream=cs)
+        dimage = (film - target) * (2.0 / (3 * npix))
+        dimage[:, 3] = 0.0
+        for x in g:
+            x.zero_()
+        sc.diff_render(cam, params, (1 << 24) + step * spp, spp, replay, 0, tex, rough, emis, samples=samples,
+                       flags=abi.DIFF_SAMPLE_PARAMS, stream=cs)
+        sc.adjoint_path(cam, params, (1 << 24) + step * spp, spp, dimage, 0, tex, rough, emis, g[0], g[1], g[2],
+                        samples=samples, flags=abi.DIFF_SAMPLE_PARAMS, stream=cs)
+        t = step + 1
+        for (p, m, v, lr), gr in zip(state, g):
+            m.mul_(b1).add_(gr, alpha=1 - b1)
+            v.mul_(b2).addcmul_(gr, gr, value=1 - b2)
+            p.sub_(lr * (m / (1 - b1 ** t)) / ((v / (1 - b2 ** t)).sqrt() + eps))
+        tex.clamp_(0.01, 1.0)
+        rough.clamp_(0.1, 1.0)
+        emis.clamp_(min=0.0)
+    e1.record(stream)
+    e1.synchronize()
+    after, loss1 = rmse(), image_loss()
+    return {"steps": steps, "spp_per_step": spp, "ms_per_step": e0.elapsed_time(e1) / steps,
+            "parameter_rmse_before": before, "parameter_rmse_after": after,
+            "image_loss_64spp_before": loss0, "image_loss_64spp_after": loss1}
 
 
 def batch_secondary(torch, ctx_cls, scene_cls, local):

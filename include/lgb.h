@@ -136,7 +136,8 @@ typedef struct lgb_scene_desc {
 } lgb_scene_desc;
 
 typedef struct lgb_build_opts {
-    uint32_t leaf_max;        /* triangles per 8-wide leaf slot, 1..3 (0 = default 3) */
+    uint32_t leaf_max;        /* triangles per 8-wide leaf slot, 1..3 (0 = by scene size: 1 from 2^19 triangles,
+                                 2 from 2^15, else 3) */
     uint32_t treelet_rounds;  /* SAH treelet restructuring passes (0 = default 3, 0xFFFFFFFF = none) */
     uint32_t reserved[6];
 } lgb_build_opts;

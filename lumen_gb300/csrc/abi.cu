@@ -204,7 +204,10 @@ LGB_API lgb_status lgb_scene_create(lgb_ctx* ctx, const lgb_scene_desc* d, lgb_s
     s->num_vertices = d->num_vertices;
     s->num_meshes = d->num_meshes;
     s->num_materials = d->num_materials;
-    for (uint32_t i = 0; i < d->num_materials; i++) s->bsdf_mask |= d->materials[i].bsdf_type;
+    for (uint32_t i = 0; i < d->num_materials; i++) {
+        s->bsdf_mask |= d->materials[i].bsdf_type;
+        s->shade_classes |= 1u << shade_class(d->materials[i].bsdf_type);
+    }
     s->num_lights = d->num_lights;
     for (uint32_t i = 0; i < d->num_lights; i++)
         if ((d->lights[i].light_flags & 7u) == LGB_LIGHT_DIRECTIONAL) s->num_directional++;

@@ -109,6 +109,7 @@ struct Scene {
     std::vector<void*> texture_buffers;
     uint32_t num_meshes = 0, num_materials = 0, num_lights = 0, num_textures = 0;
     uint32_t bsdf_mask = 0;  // union of the materials' LGB_BSDF_* types
+    uint32_t shade_classes = 0;  // bit per shading class of the path tracer some material falls in (shade_class)
     std::vector<uint32_t> h_mesh_first_tri;
     std::vector<lgb_mesh> h_meshes;
     BvhDevice bvh;
@@ -169,6 +170,12 @@ struct Batch {
     bool tuned = false;
     lgb_batch_opts tuned_opts{};
 };
+
+// Shading class of a material type in the wavefront path tracer: 0 diffuse, 1 conductor, 3 principled, 2 every
+// other type (mirror, glass, dielectric, and types no BSDF handles, which still add their emission).
+__host__ __device__ inline int shade_class(uint32_t bsdf_type) {
+    return bsdf_type == LGB_BSDF_DIFFUSE ? 0 : bsdf_type == LGB_BSDF_CONDUCTOR ? 1 : bsdf_type == LGB_BSDF_PRINCIPLED ? 3 : 2;
+}
 
 // Error helpers: record a message on the context and return a status.
 lgb_status set_error(Ctx* ctx, lgb_status st, const std::string& msg);

@@ -40,18 +40,18 @@ constexpr int kThreads = 128;
 
 enum MatClass { CLS_DIFFUSE = 0, CLS_CONDUCTOR = 1, CLS_SPECULAR = 2, CLS_PRINCIPLED = 3, NUM_CLS = 4 };
 
-// NEE record: the light-sampling state that pt_commons.glsl keeps in registers across its two traces.
+// NEE record: the light-sampling state that pt_commons.glsl keeps in registers across its two traces, 80 bytes.
+// Both terms already carry the throughput and the light pick pdf (T * x / light_pick_pdf, path.rgen:76-78), so
+// the resolve adds the light sample's term when its shadow ray is unoccluded and the BSDF-MIS term times its MIS
+// weight 1 / (1 + pdf_pos_a / (g * pdf)) when the MIS ray hits the sampled light triangle.
 struct __align__(16) NeeRec {
-    float4 term1;   // xyz: mis * f * |cos| * Le / pdf_w of the light sample; w: pdf_pos_w
-    float4 T;       // xyz: throughput at the shading point; w: light_pick_pdf
-    float4 f2;      // xyz: BSDF-MIS sample value; w: its pdf (0 = no MIS ray)
-    float4 m;       // x: |cos| of the MIS sample, y: light pdf_pos_a, z: light prim (bits), w: flags (bits)
-    float4 Le;      // xyz: light radiance, w: path id (bits)
+    float4 light;   // xyz: T * mis * f * |cos| * Le / pdf_w / light_pick_pdf (0 when pdf_w is 0); w: path id (bits)
+    float4 bsdf;    // xyz: T * f2 * |cos2| * Le / pdf2 / light_pick_pdf; w: pdf_pos_a / pdf2, or -1 without a MIS term
     float4 pos;     // xyz: shading position; w: shading prim (bits)
-    float4 ns;      // xyz: shading normal as the hit payload holds it (not face-forwarded); w unused
-    float4 wi2;     // xyz: BSDF-MIS direction
+    float4 ns;      // xyz: shading normal as the hit payload holds it (not face-forwarded); w: slot of the BSDF-MIS
+                    // ray in the MIS queue (bits), 0xFFFFFFFF when no ray was queued
+    float4 wi2;     // xyz: BSDF-MIS direction; w: sampled light prim (bits)
 };
-enum : uint32_t { NEE_AREA = 1u };
 
 struct Params {
     float iv[16], ip[16];
@@ -86,14 +86,16 @@ struct Buffers {
     lgb_ray* mrays;
     lgb_hit* mhits;
     uint32_t* sbits;
-    uint32_t* counters; // [0] cur, [1] next, [2] nee, [3..6] class counts, [8..10] trace work counters
+    uint32_t* counters; // [0] cur, [1] next, [2] nee, [3..6] class counts, [8..10] trace work counters,
+                        // [11] queued BSDF-MIS rays
     Params* params;     // per-chunk parameters in device memory, so that a captured graph can be replayed
     uint32_t cap;       // path capacity of the arena
     // batched rendering only (null otherwise)
     uint32_t* job;       // job of each path
     uint32_t* root;      // BVH root node of each ray of the current queue
     uint32_t* root_next; // ... of the continuation rays being enqueued
-    uint32_t* nroot;     // ... of the shadow and BSDF-MIS rays
+    uint32_t* nroot;     // ... of the shadow rays
+    uint32_t* mroot;     // ... of the queued BSDF-MIS rays
     const JobRec* jobs;
     const BatchChunk* chunk;
 };
@@ -133,14 +135,7 @@ __device__ __forceinline__ uint32_t find_segment(const BatchChunk& C, uint32_t i
 }
 
 
-__device__ __forceinline__ int class_of(uint32_t bsdf_type) {
-    switch (bsdf_type) {
-        case LGB_BSDF_DIFFUSE: return CLS_DIFFUSE;
-        case LGB_BSDF_CONDUCTOR: return CLS_CONDUCTOR;
-        case LGB_BSDF_PRINCIPLED: return CLS_PRINCIPLED;
-        default: return CLS_SPECULAR;
-    }
-}
+__device__ __forceinline__ int class_of(uint32_t bsdf_type) { return shade_class(bsdf_type); }
 
 
 // ---------------- kernels ----------------
@@ -436,15 +431,13 @@ __global__ void __launch_bounds__(kThreads, kShadeMinBlocks) k_shade(SceneView S
                                            make_float4(c.px, c.py, c.pz, 0.0f), rq.tmax, tt, tu, tv))
                             mray.tmax = -1.0f;
                     }
-                    rec.term1 = f4(term1, pdf_w);
-                    rec.T = f4(T, lpp);
-                    rec.f2 = f4(f2, pdf2);
-                    rec.m = make_float4(fabsf(cos2), pdf_a, __uint_as_float(lprim),
-                                        __uint_as_float(ltype == LGB_LIGHT_AREA ? NEE_AREA : 0u));
-                    rec.Le = f4(Le, __uint_as_float(p));
+                    const bool mis_term = ltype == LGB_LIGHT_AREA && pdf2 != 0.0f;
+                    rec.light = f4(T * term1 / lpp, __uint_as_float(p));
+                    rec.bsdf = mis_term ? f4(T * (f2 * fabsf(cos2) * Le / pdf2) / lpp, pdf_a / pdf2)
+                                        : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
                     rec.pos = f4(h.pos, __uint_as_float(hit.prim));
-                    rec.ns = f4(h.n_s, 0.0f);
-                    rec.wi2 = f4(wi2, 0.0f);
+                    rec.ns = f4(h.n_s, __uint_as_float(0xFFFFFFFFu));
+                    rec.wi2 = f4(wi2, __uint_as_float(lprim));
                 }
                 float pdf, cos_t;
                 v3 dir_next;
@@ -474,11 +467,20 @@ __global__ void __launch_bounds__(kThreads, kShadeMinBlocks) k_shade(SceneView S
             store_ray(&B.rays_next[cslot], next_ray);
             if (BATCH) B.root_next[cslot] = root;
         }
+        // Only BSDF-MIS rays with a non-empty interval are queued (those the pre-test above did not end); the NEE
+        // record keeps the ray's queue slot. A record without a queued ray resolves as a miss, as its empty ray
+        // would have.
+        const bool mis_ray = nee && mray.tmax >= mray.tmin;
+        const uint32_t mslot = agg_slot(&B.counters[11], mis_ray);
+        if (mis_ray) {
+            store_ray(&B.mrays[mslot], mray);
+            if (BATCH) B.mroot[mslot] = root;
+            rec.ns.w = __uint_as_float(mslot);
+        }
         const uint32_t nslot = agg_slot(&B.counters[2], nee);
         if (nee) {
             B.nee[nslot] = rec;
             store_ray(&B.srays[nslot], sray);
-            store_ray(&B.mrays[nslot], mray);
             if (BATCH) B.nroot[nslot] = root;
         }
     }
@@ -493,16 +495,15 @@ __global__ void __launch_bounds__(kThreads) k_nee_resolve(SceneView S0, Buffers 
     const uint32_t n = B.counters[2];
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         const NeeRec rec = B.nee[r];
-        const uint32_t p = __float_as_uint(rec.Le.w);
+        const uint32_t p = __float_as_uint(rec.light.w);
         const SceneView S = BATCH ? B.jobs[B.job[p]].S : S0;
         const bool occluded = (B.sbits[r >> 5] >> (r & 31)) & 1u;
-        v3 res = V3(0.0f);
-        if (!occluded && rec.term1.w > 0.0f) res = res + f3(rec.term1);
-        const uint32_t flags = __float_as_uint(rec.m.w);
-        const float pdf2 = rec.f2.w;
-        if ((flags & NEE_AREA) && pdf2 != 0.0f) {
-            const lgb_hit mh = B.mhits[r];
-            const uint32_t lprim = __float_as_uint(rec.m.z);
+        v3 add = V3(0.0f);
+        if (!occluded) add = f3(rec.light);
+        if (rec.bsdf.w >= 0.0f) {
+            const uint32_t mslot = __float_as_uint(rec.ns.w);
+            const lgb_hit mh = mslot != 0xFFFFFFFFu ? B.mhits[mslot] : lgb_hit{LGB_NO_HIT, 0.0f, 0.0f, 0.0f};
+            const uint32_t lprim = __float_as_uint(rec.wi2.w);
             const uint32_t pl_prim = mh.prim == LGB_NO_HIT ? __float_as_uint(rec.pos.w) : mh.prim;
             if (pl_prim == lprim) {
                 v3 pl_pos, pl_ns;
@@ -517,12 +518,11 @@ __global__ void __launch_bounds__(kThreads) k_nee_resolve(SceneView S0, Buffers 
                 const v3 wi2 = f3(rec.wi2);
                 const float wl = length(pl_pos - f3(rec.pos));
                 const float g = fabsf(dot(pl_ns, -wi2)) / (wl * wl);
-                const float mis = 1.0f / (1.0f + rec.m.y / (g * pdf2));
-                res = res + f3(rec.f2) * mis * rec.m.x * f3(rec.Le) / pdf2;
+                const float mis = 1.0f / (1.0f + rec.bsdf.w / g);
+                add = add + f3(rec.bsdf) * mis;
             }
         }
         float4 c = B.col[p];
-        const v3 add = f3(rec.T) * res / rec.T.w;
         c.x = c.x + add.x; c.y = c.y + add.y; c.z = c.z + add.z;
         B.col[p] = c;
     }
@@ -535,7 +535,7 @@ __global__ void k_rotate(uint32_t* counters) {
         counters[1] = 0u;
         counters[2] = 0u;
         for (int c = 0; c < NUM_CLS; c++) counters[3 + c] = 0u;
-        counters[8] = counters[9] = counters[10] = 0u;
+        counters[8] = counters[9] = counters[10] = counters[11] = 0u;
     }
 }
 
@@ -622,7 +622,7 @@ size_t carve(char* base, uint32_t cap, Buffers& B, bool batch = false) {
     B.counters = (uint32_t*)take(64);
     B.params = (Params*)take(sizeof(Params));
     B.cap = cap;
-    B.job = B.root = B.root_next = B.nroot = nullptr;
+    B.job = B.root = B.root_next = B.nroot = B.mroot = nullptr;
     B.jobs = nullptr;
     B.chunk = nullptr;
     if (batch) {
@@ -630,6 +630,7 @@ size_t carve(char* base, uint32_t cap, Buffers& B, bool batch = false) {
         B.root = (uint32_t*)take(4ull * cap);
         B.root_next = (uint32_t*)take(4ull * cap);
         B.nroot = (uint32_t*)take(4ull * cap);
+        B.mroot = (uint32_t*)take(4ull * cap);
         B.jobs = (const JobRec*)take(sizeof(JobRec) * kMaxBatchJobs);
         B.chunk = (const BatchChunk*)take(sizeof(BatchChunk));
     }
@@ -656,8 +657,8 @@ template <int SK> void launch_queue_traces(const SceneView& S, const Buffers& B,
         k_q_trace_closest<SK><<<g.trace, kThreads, 0, st>>>(S, B.rays, B.hits, B.counters + 0, B.counters + 8, B.root);
     } else {
         k_q_trace_any<SK><<<g.trace, kThreads, 0, st>>>(S, B.srays, B.sbits, B.counters + 2, B.counters + 9, B.nroot);
-        k_q_trace_closest<SK><<<g.trace, kThreads, 0, st>>>(S, B.mrays, B.mhits, B.counters + 2, B.counters + 10,
-                                                            B.nroot);
+        k_q_trace_closest<SK><<<g.trace, kThreads, 0, st>>>(S, B.mrays, B.mhits, B.counters + 11, B.counters + 10,
+                                                            B.mroot);
     }
 }
 // first: the continuation rays' closest hits; else the shadow rays and the BSDF-MIS rays of the bounce.
@@ -668,18 +669,19 @@ void queue_traces(const SceneView& S, const Buffers& B, Grids g, cudaStream_t st
 
 // One chunk of frames: camera rays, `bounces` bounces, film. Every kernel reads its parameters from device
 // memory (B.params, or the job table and chunk record when batched), so this sequence can be captured once and
-// replayed with new parameters.
+// replayed with new parameters. `classes` (bit c: shading class c) names the classes the scene's materials fall
+// in; the shading kernels of the other classes would always find an empty list and are not launched.
 template <bool BATCH>
-cudaError_t launch_chunk(const SceneView& S, Buffers B, int bounces, Grids g, cudaStream_t st) {
+cudaError_t launch_chunk(const SceneView& S, Buffers B, int bounces, Grids g, uint32_t classes, cudaStream_t st) {
     k_init_counters<BATCH><<<1, 32, 0, st>>>(B, B.params);
     k_camera<BATCH><<<g.work, kThreads, 0, st>>>(B.params, B);
     for (int depth = 0; depth < bounces; depth++) {
         queue_traces(S, B, g, st, true);
         k_classify<BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B);
-        k_shade<CLS_DIFFUSE, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
-        k_shade<CLS_CONDUCTOR, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
-        k_shade<CLS_SPECULAR, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
-        k_shade<CLS_PRINCIPLED, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        if (classes & (1u << CLS_DIFFUSE)) k_shade<CLS_DIFFUSE, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        if (classes & (1u << CLS_CONDUCTOR)) k_shade<CLS_CONDUCTOR, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        if (classes & (1u << CLS_SPECULAR)) k_shade<CLS_SPECULAR, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        if (classes & (1u << CLS_PRINCIPLED)) k_shade<CLS_PRINCIPLED, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
         k_clear_bits<<<g.work, kThreads, 0, st>>>(B.sbits, B.counters + 2);
         queue_traces(S, B, g, st, false);
         k_nee_resolve<BATCH><<<g.work, kThreads, 0, st>>>(S, B);
@@ -692,6 +694,12 @@ cudaError_t launch_chunk(const SceneView& S, Buffers B, int bounces, Grids g, cu
     return cudaGetLastError();
 }
 
+
+uint32_t batch_classes(const Batch* b) {
+    uint32_t c = 0;
+    for (const Scene* s : b->scenes) c |= s->shade_classes;
+    return c;
+}
 
 Params make_params(const lgb_camera* cam, const lgb_path_params* pp, uint32_t cap, float* film) {
     Params P;
@@ -738,7 +746,8 @@ lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* p
     cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
     LGB_CUDA_TRY(ctx, cudaStreamIsCapturing(st, &cap_status));
     const bool use_graph = cap_status == cudaStreamCaptureStatusNone;
-    const uint64_t key[6] = {(uint64_t)(uintptr_t)s->pt_buf, cap, (uint64_t)bounces, (uint64_t)(uintptr_t)S.nodes,
+    const uint64_t key[6] = {(uint64_t)(uintptr_t)s->pt_buf, cap, (uint64_t)bounces | ((uint64_t)s->shade_classes << 40),
+                             (uint64_t)(uintptr_t)S.nodes,
                              (uint64_t)(uintptr_t)S.tris, ((uint64_t)g.work << 32) | (uint32_t)g.trace};
     if (use_graph && (!s->pt_graph || std::memcmp(key, s->pt_graph_key, sizeof(key)) != 0)) {
         if (s->pt_graph) { cudaGraphExecDestroy((cudaGraphExec_t)s->pt_graph); s->pt_graph = nullptr; }
@@ -746,7 +755,7 @@ lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* p
         const cudaStream_t cs = (cudaStream_t)s->capture_stream;
         cudaGraph_t graph = nullptr;
         LGB_CUDA_TRY(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-        const cudaError_t le = launch_chunk<false>(S, B, bounces, g, cs);
+        const cudaError_t le = launch_chunk<false>(S, B, bounces, g, s->shade_classes, cs);
         const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
         if (le != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_error(ctx, le, "capturing the bounce loop"); }
         if (ce != cudaSuccess) return cuda_error(ctx, ce, "cudaStreamEndCapture");
@@ -764,7 +773,7 @@ lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* p
         if (use_graph) {
             LGB_CUDA_TRY(ctx, cudaGraphLaunch((cudaGraphExec_t)s->pt_graph, st));
         } else {
-            LGB_CUDA_TRY(ctx, launch_chunk<false>(S, B, bounces, g, st));
+            LGB_CUDA_TRY(ctx, launch_chunk<false>(S, B, bounces, g, s->shade_classes, st));
         }
     }
     LGB_CUDA_TRY(ctx, cudaGetLastError());
@@ -844,7 +853,7 @@ lgb_status render_path_noalloc(Scene* s, const lgb_camera* cam, const lgb_path_p
         // The arena keeps the previous call's contents: the parameters and counters are rewritten here, the
         // occlusion bits before every shadow query, and every other array is written before it is read.
         k_set_params<<<1, 1, 0, st>>>(P, B.params);
-        LGB_CUDA_TRY(ctx, launch_chunk<false>(S, B, bounces, g, st));
+        LGB_CUDA_TRY(ctx, launch_chunk<false>(S, B, bounces, g, s->shade_classes, st));
     }
     return LGB_OK;
 }
@@ -1061,7 +1070,8 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
     cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
     LGB_CUDA_TRY(ctx, cudaStreamIsCapturing(st, &cap_status));
     const bool use_graph = cap_status == cudaStreamCaptureStatusNone;
-    const uint64_t key[6] = {(uint64_t)(uintptr_t)b->buf, cap, (uint64_t)bounces | ((uint64_t)g.shared_stack << 32),
+    const uint64_t key[6] = {(uint64_t)(uintptr_t)b->buf, cap,
+                             (uint64_t)bounces | ((uint64_t)g.shared_stack << 32) | ((uint64_t)batch_classes(b) << 40),
                              (uint64_t)(uintptr_t)b->nodes, (uint64_t)(uintptr_t)b->tris,
                              ((uint64_t)g.work << 32) | (uint32_t)g.trace};
     if (use_graph && (!b->graph || std::memcmp(key, b->graph_key, sizeof(key)) != 0)) {
@@ -1070,7 +1080,7 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
         const cudaStream_t cs = (cudaStream_t)b->capture_stream;
         cudaGraph_t graph = nullptr;
         LGB_CUDA_TRY(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-        const cudaError_t le = launch_chunk<true>(F, B, bounces, g, cs);
+        const cudaError_t le = launch_chunk<true>(F, B, bounces, g, batch_classes(b), cs);
         const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
         if (le != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_error(ctx, le, "capturing the batch bounce loop"); }
         if (ce != cudaSuccess) return cuda_error(ctx, ce, "cudaStreamEndCapture");
@@ -1086,7 +1096,7 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
     for (const BatchChunk& C : chunks) {
         k_set_chunk<<<1, 1, 0, st>>>(C, const_cast<BatchChunk*>(B.chunk));
         if (use_graph) LGB_CUDA_TRY(ctx, cudaGraphLaunch((cudaGraphExec_t)b->graph, st));
-        else LGB_CUDA_TRY(ctx, launch_chunk<true>(F, B, bounces, g, st));
+        else LGB_CUDA_TRY(ctx, launch_chunk<true>(F, B, bounces, g, batch_classes(b), st));
     }
     LGB_CUDA_TRY(ctx, cudaGetLastError());
     return LGB_OK;

@@ -1,7 +1,8 @@
 // The photon table shared by the photon integrators (VCM, SPPM): grid cells and their hash slot
 // (vcm_commons.glsl:17-23, utils.glsl:62-65, with get_grid_idx's discarded clamp kept), the grid resolution of
 // VCM.cpp:144-147, and the table itself made deterministic: every photon slot is keyed by its hash slot (unused
-// slots by the table size), a stable radix sort orders (slot, photon id), and two run-boundary kernels write per
+// slots by the table size, below 2^31, so 32-bit keys), a stable radix sort orders (slot, photon id), and two
+// run-boundary kernels write per
 // slot the number of photons and the highest photon id, which is the photon a sequential writer leaves last.
 #pragma once
 #include <cuda_runtime.h>
@@ -27,18 +28,18 @@ __device__ __forceinline__ uint32_t grid_hash(int3 p, uint32_t screen) {
 }
 
 // Run starts: rep[slot] = first sorted position (temporarily).
-__global__ void k_table_run_first(const uint64_t* __restrict__ keys, uint32_t n, uint32_t table, uint32_t* rep) {
+__global__ void k_table_run_first(const uint32_t* __restrict__ keys, uint32_t n, uint32_t table, uint32_t* rep) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint64_t k = keys[i];
+        const uint32_t k = keys[i];
         if (k >= table) continue;
         if (i == 0 || keys[i - 1] != k) rep[k] = i;
     }
 }
 // Run ends: count = length of the run, rep = its last vertex id.
-__global__ void k_table_run_last(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t n,
+__global__ void k_table_run_last(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint32_t n,
                                uint32_t table, uint32_t* count, uint32_t* rep) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint64_t k = keys[i];
+        const uint32_t k = keys[i];
         if (k >= table) continue;
         if (i == n - 1 || keys[i + 1] != k) {
             count[k] = i - rep[k] + 1u;
@@ -75,7 +76,7 @@ inline int table_grid_blocks(Ctx* ctx, uint64_t n) {
 }
 
 // Sorts (keys, vals) in place (k0/v0 end up holding the result) and writes the table (count and rep zeroed first).
-inline lgb_status build_table(Ctx* ctx, uint64_t*& k0, uint32_t*& v0, uint64_t*& k1, uint32_t*& v1, uint32_t* sort_counts, uint32_t n,
+inline lgb_status build_table(Ctx* ctx, uint32_t*& k0, uint32_t*& v0, uint32_t*& k1, uint32_t*& v1, uint32_t* sort_counts, uint32_t n,
                        uint32_t table, uint32_t* count, uint32_t* rep, cudaStream_t st) {
     LGB_CUDA_TRY(ctx, cudaMemsetAsync(count, 0, sizeof(uint32_t) * table, st));
     LGB_CUDA_TRY(ctx, cudaMemsetAsync(rep, 0, sizeof(uint32_t) * table, st));

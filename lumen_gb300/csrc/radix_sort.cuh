@@ -1,4 +1,4 @@
-// LSD radix sort of (64-bit key, 32-bit value) pairs, 8 bits per pass, stable: per-block digit histograms,
+// LSD radix sort of (32- or 64-bit key, 32-bit value) pairs, 8 bits per pass, stable: per-block digit histograms,
 // one exclusive scan over all (digit, block) counts, and a scatter that ranks equal digits within each warp
 // with __match_any_sync so that equal keys keep their input order. Shared by the BVH builder (Morton codes)
 // and the photon grid (hash slots). The scan runs in three steps over tiles of 4096 counts (tile sums, a scan of
@@ -25,7 +25,8 @@ inline size_t radix_sort_scratch_words(uint32_t n) {
     return m + (m + SCAN_TILE - 1) / SCAN_TILE;
 }
 
-__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint64_t* __restrict__ keys, uint32_t n, int shift,
+template <class KeyT>
+__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const KeyT* __restrict__ keys, uint32_t n, int shift,
                                                         uint32_t* counts, uint32_t nblocks) {
     __shared__ uint32_t h[256];
     h[threadIdx.x] = 0;
@@ -153,8 +154,9 @@ inline void scan_exclusive(uint32_t* data, uint32_t m, cudaStream_t st) {
     k_scan_tile_apply<<<nt, SCAN_THREADS, 0, st>>>(data, m, sums);
 }
 
-__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
-                                                           uint64_t* __restrict__ kout, uint32_t* __restrict__ vout,
+template <class KeyT>
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const KeyT* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                                           KeyT* __restrict__ kout, uint32_t* __restrict__ vout,
                                                            uint32_t n, int shift, const uint32_t* __restrict__ offsets,
                                                            uint32_t nblocks) {
     __shared__ uint32_t base_off[256];
@@ -168,7 +170,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t* __res
         __syncthreads();
         const size_t idx = tile + (size_t)r * RS_THREADS + tid;
         const bool valid = idx < n;
-        uint64_t key = valid ? kin[idx] : 0ull;
+        KeyT key = valid ? kin[idx] : KeyT(0);
         uint32_t val = valid ? vin[idx] : 0u;
         uint32_t digit = valid ? ((uint32_t)(key >> shift) & 0xffu) : (256u + lane);
         uint32_t peers = __match_any_sync(0xffffffffu, digit);
@@ -194,17 +196,19 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint64_t* __res
     }
 }
 
-// Sorts n pairs by the low 8 * passes bits of the keys; counts must hold radix_sort_scratch_words(n) words. The
-// result ends in (k0, v0) or (k1, v1): the function swaps the pointers so that k0 / v0 name the sorted arrays.
-inline cudaError_t radix_sort_pairs(uint64_t*& k0, uint32_t*& v0, uint64_t*& k1, uint32_t*& v1, uint32_t* counts,
+// Sorts n pairs by the low 8 * passes bits of the keys (KeyT uint32_t or uint64_t); counts must hold
+// radix_sort_scratch_words(n) words. The result ends in (k0, v0) or (k1, v1): the function swaps the pointers so
+// that k0 / v0 name the sorted arrays.
+template <class KeyT>
+inline cudaError_t radix_sort_pairs(KeyT*& k0, uint32_t*& v0, KeyT*& k1, uint32_t*& v1, uint32_t* counts,
                                     uint32_t n, int passes, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     const uint32_t nblocks = (n + RS_TILE - 1) / RS_TILE;
     for (int pass = 0; pass < passes; pass++) {
         const int shift = pass * 8;
-        k_rs_hist<<<nblocks, RS_THREADS, 0, st>>>(k0, n, shift, counts, nblocks);
+        k_rs_hist<KeyT><<<nblocks, RS_THREADS, 0, st>>>(k0, n, shift, counts, nblocks);
         scan_exclusive(counts, 256 * nblocks, st);
-        k_rs_scatter<<<nblocks, RS_THREADS, 0, st>>>(k0, v0, k1, v1, n, shift, counts, nblocks);
+        k_rs_scatter<KeyT><<<nblocks, RS_THREADS, 0, st>>>(k0, v0, k1, v1, n, shift, counts, nblocks);
         std::swap(k0, k1);
         std::swap(v0, v1);
     }

@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(kSppmThreads) k_sppm_light(SceneView S, SppmAr
 }
 
 // Table keys: the hash slot of every photon slot that holds a photon, the table size for the others.
-__global__ void k_sppm_keys(SppmArgs A, uint32_t table, uint64_t* keys, uint32_t* vals) {
+__global__ void k_sppm_keys(SppmArgs A, uint32_t table, uint32_t* keys, uint32_t* vals) {
     const uint32_t n = A.screen * (uint32_t)A.max_depth;
     const float mn[3] = {A.bounds[0], A.bounds[1], A.bounds[2]}, mx[3] = {A.bounds[3], A.bounds[4], A.bounds[5]};
     const int res[3] = {A.grid_res[0], A.grid_res[1], A.grid_res[2]};
@@ -461,7 +461,7 @@ lgb_status sppm_iteration(Scene* s, const lgb_camera* cam, const lgb_sppm_params
     const size_t o_vp = take(sizeof(float4) * kPointF4 * (size_t)screen);
     const size_t o_ph = take(sizeof(float4) * kPhotonF4 * (size_t)nph);
     const size_t o_gc = take(4ull * table), o_gr = take(4ull * table);
-    const size_t o_k0 = take(8ull * nph), o_k1 = take(8ull * nph), o_v0 = take(4ull * nph), o_v1 = take(4ull * nph);
+    const size_t o_k0 = take(4ull * nph), o_k1 = take(4ull * nph), o_v0 = take(4ull * nph), o_v1 = take(4ull * nph);
     const size_t o_sc = take(4ull * radix_sort_scratch_words(nph));
     const size_t o_bd = take(4ull * 8), o_ob = take(4ull * 8), o_gres = take(4ull * 4);
     const bool fresh = !s->sppm_buf || s->sppm_w != cam->width || s->sppm_h != cam->height || s->sppm_depth != per ||
@@ -508,8 +508,8 @@ lgb_status sppm_iteration(Scene* s, const lgb_camera* cam, const lgb_sppm_params
     k_sppm_bounds<<<(int)std::min<uint32_t>((screen + 255) / 256, (uint32_t)sms * 8u), 256, 0, st>>>(A, ob);
     k_sppm_grid<<<1, 32, 0, st>>>(A, ob);
     k_sppm_light<<<grid, kSppmThreads, 0, st>>>(S, A);
-    uint64_t* k0 = reinterpret_cast<uint64_t*>(base + o_k0);
-    uint64_t* k1 = reinterpret_cast<uint64_t*>(base + o_k1);
+    uint32_t* k0 = reinterpret_cast<uint32_t*>(base + o_k0);
+    uint32_t* k1 = reinterpret_cast<uint32_t*>(base + o_k1);
     uint32_t* v0 = reinterpret_cast<uint32_t*>(base + o_v0);
     uint32_t* v1 = reinterpret_cast<uint32_t*>(base + o_v1);
     k_sppm_keys<<<table_grid_blocks(ctx, nph), 256, 0, st>>>(A, table, k0, v0);

@@ -19,15 +19,18 @@ constexpr int kTraceMinBlocks = 9;
 // 4M incoherent rays / 1M triangles, closest / any Mrays/s: 0 entries 1133 / 2280, 4: 1137 / 2318,
 // 8: 1142 / 2335, 12: 1142 / 2323.
 constexpr int kTraceSharedStack = 8;
-// Idle lanes a warp waits for before fetching new rays. Measured with the approximate box-test reciprocal,
-// closest / any Mrays/s: refill at 1 idle lane 1176 / 2350, at 8: 1185 / 2680, at 16: 1047 / 2485.
-constexpr int kTraceRefill = 8;
-// Warp-uniform triangle and node iterations (TRI_MIN of trace_persistent): a triangle iteration once a quarter
+// Idle lanes a warp waits for before fetching new rays. Measured with the approximate box-test reciprocal and
+// mixed iterations, closest / any Mrays/s: refill at 1 idle lane 1176 / 2350, at 8: 1185 / 2680, at 16: 1047 /
+// 2485. With warp-uniform triangle iterations (below) and one triangle per leaf slot: at 8: 1317 / 3048, at 4:
+// 1370 / 3013, at 3: 1368 / 2939, at 2: 1356 / 2765.
+constexpr int kTraceRefill = 4;
+// Warp-uniform triangle and node iterations (TRI_MIN of trace_persistent): a triangle iteration once a fifth
 // of the active lanes have a pending leaf triangle. Measured on GB300, 4M incoherent rays / 1M triangles,
-// closest / any Mrays/s (hits bit-identical): mixed iterations 1182 / 2664; fixed thresholds 2: 1170 / 2463,
-// 4: 1244 / 2724, 6: 1247 / 2814, 8: 1219 / 2814, 12: 1110 / 2699, 20: 803 / 2186; a third of the active lanes
-// 1208 / 2853; a quarter 1252 / 2866.
-constexpr int kTraceTriMin = -4;
+// closest / any Mrays/s (hits bit-identical), refill at 8 and three triangles per leaf slot: mixed iterations
+// 1182 / 2664; fixed thresholds 2: 1170 / 2463, 4: 1244 / 2724, 6: 1247 / 2814, 8: 1219 / 2814, 12: 1110 / 2699,
+// 20: 803 / 2186; a third of the active lanes 1208 / 2853; a quarter 1252 / 2866; a fifth 1267 / 2853. With the
+// refill at 4 and one triangle per leaf slot: a quarter 1370 / 3013, a fifth 1386 / 2995.
+constexpr int kTraceTriMin = -5;
 #ifdef LGB_TRACE_TRI_MIN
 #define LGB_TRACE_TRI_MIN_ LGB_TRACE_TRI_MIN
 #else

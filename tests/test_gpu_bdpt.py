@@ -11,6 +11,8 @@ import os
 import numpy as np
 import pytest
 
+import parity_log
+
 import oracle_lib
 from lumen_gb300 import abi, build, procedural
 from lumen_gb300.scene import Context, GpuScene, bdpt_params, camera_forward, camera_lookat
@@ -29,7 +31,11 @@ def ctx():
 
 def close_fraction(a, b, rtol=1e-3, atol=1e-5):
     ok = np.abs(a - b) <= rtol * np.maximum(np.abs(b), 1e-6) + atol
-    return ok.all(axis=1).mean()
+    frac = ok.all(axis=1).mean()
+    parity_log.record(frac, rtol)
+    if rtol != 1e-4:  # also the per-sample tolerance of the path tracer, for the record only
+        parity_log.record((np.abs(a - b) <= 1e-4 * np.maximum(np.abs(b), 1e-6) + 1e-7).all(axis=1).mean(), 1e-4)
+    return frac
 
 
 def _run_both(ctx, oracle, arrays, w, h, frames, depth, spot_angle=0.0, seed=4242):
@@ -57,10 +63,10 @@ def test_bdpt_matches_oracle_cornell(ctx, oracle):
     cb = procedural.cornell_box()
     got, want = _run_both(ctx, oracle, cb, 48, 40, 1, 6)
     assert (got[:, 3] == 1.0).all() and not np.isnan(got).any()
-    assert close_fraction(got[:, :3], want[:, :3]) >= 0.97
+    assert close_fraction(got[:, :3], want[:, :3]) >= 0.99
     np.testing.assert_allclose(got[:, :3].mean(0), want[:, :3].mean(0), rtol=0.005)
     got4, want4 = _run_both(ctx, oracle, cb, 48, 40, 4, 6)
-    assert close_fraction(got4[:, :3], want4[:, :3]) >= 0.95
+    assert close_fraction(got4[:, :3], want4[:, :3]) >= 0.99
     np.testing.assert_allclose(got4[:, :3].mean(0), want4[:, :3].mean(0), rtol=0.005)
 
 
@@ -71,7 +77,7 @@ def test_bdpt_path_lengths_match_oracle(ctx, oracle, depth):
     cb = procedural.cornell_box()
     got, want = _run_both(ctx, oracle, cb, 32, 32, 2, depth)
     assert not np.isnan(got).any()
-    assert close_fraction(got[:, :3], want[:, :3]) >= 0.95
+    assert close_fraction(got[:, :3], want[:, :3]) >= 0.99
     np.testing.assert_allclose(got[:, :3].mean(0), want[:, :3].mean(0), rtol=0.01)
 
 
@@ -80,7 +86,7 @@ def test_bdpt_caustics_scene_matches_oracle(ctx, oracle):
     arrays = procedural.vcm_scene(100, 40)
     got, want = _run_both(ctx, oracle, arrays, 64, 64, 2, 8, spot_angle=20.0)
     assert not np.isnan(got).any() and got[:, :3].mean() > 0.0
-    assert close_fraction(got[:, :3], want[:, :3]) >= 0.95
+    assert close_fraction(got[:, :3], want[:, :3]) >= 0.99
     np.testing.assert_allclose(got[:, :3].mean(0), want[:, :3].mean(0), rtol=0.02)
 
 
@@ -91,7 +97,7 @@ def test_bdpt_mixed_materials_match_oracle(ctx, oracle):
     arrays, _ = host_scene.load_scene(os.path.join(HERE, "golden", "scenes", "mixed_sppm.json"))
     got, want = _run_both(ctx, oracle, arrays, 40, 30, 2, 5)
     assert not np.isnan(got).any() and got[:, :3].mean() > 0.0
-    assert close_fraction(got[:, :3], want[:, :3]) >= 0.95
+    assert close_fraction(got[:, :3], want[:, :3]) >= 0.99
     np.testing.assert_allclose(got[:, :3].mean(0), want[:, :3].mean(0), rtol=0.02)
 
 

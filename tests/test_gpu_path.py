@@ -8,6 +8,8 @@ import os
 import numpy as np
 import pytest
 
+import parity_log
+
 from lumen_gb300 import abi, build, procedural
 from lumen_gb300.scene import Context, GpuScene, camera_lookat, path_params
 
@@ -42,7 +44,9 @@ def gpu_samples(sc, cb, w, h, frame, depth=8):
 
 def close_fraction(a, b):
     ok = np.abs(a - b) <= RTOL * np.maximum(np.abs(b), 1e-6) + 1e-7
-    return ok.all(axis=1).mean()
+    frac = ok.all(axis=1).mean()
+    parity_log.record(frac, RTOL)
+    return frac
 
 
 @pytest.mark.parametrize("frame", [0, 5])

@@ -9,6 +9,8 @@ import os
 import numpy as np
 import pytest
 
+import parity_log
+
 import oracle_lib
 from lumen_gb300 import abi, build, procedural
 from lumen_gb300.scene import Context, GpuScene, camera_forward, camera_lookat, restir_params
@@ -26,7 +28,11 @@ def ctx():
 
 def close_fraction(a, b, rtol=1e-3, atol=1e-5):
     ok = np.abs(a - b) <= rtol * np.maximum(np.abs(b), 1e-6) + atol
-    return ok.all(axis=1).mean()
+    frac = ok.all(axis=1).mean()
+    parity_log.record(frac, rtol)
+    if rtol != 1e-4:  # also the per-sample tolerance of the path tracer, for the record only
+        parity_log.record((np.abs(a - b) <= 1e-4 * np.maximum(np.abs(b), 1e-6) + 1e-7).all(axis=1).mean(), 1e-4)
+    return frac
 
 
 def _run_both(ctx, oracle, arrays, w, h, frames, flags=0, spot_angle=0.0, accumulate=1):
@@ -56,9 +62,9 @@ def test_restir_matches_oracle_cornell(ctx, oracle, flags):
     cb = procedural.cornell_box()
     got, want = _run_both(ctx, oracle, cb, 48, 48, 1, flags)
     assert (got[:, 3] == 1.0).all() and not np.isnan(got).any()
-    assert close_fraction(got[:, :3], want[:, :3]) >= 0.97
+    assert close_fraction(got[:, :3], want[:, :3]) >= 0.99
     got6, want6 = _run_both(ctx, oracle, cb, 48, 48, 6, flags)
-    assert close_fraction(got6[:, :3], want6[:, :3]) >= 0.9
+    assert close_fraction(got6[:, :3], want6[:, :3]) >= 0.99
     np.testing.assert_allclose(got6[:, :3].mean(0), want6[:, :3].mean(0), rtol=0.03)
 
 
@@ -66,7 +72,7 @@ def test_restir_spot_light_matches_oracle(ctx, oracle):
     arrays = procedural.vcm_scene(100, 40)
     got, want = _run_both(ctx, oracle, arrays, 48, 48, 3, abi.RESTIR_SPATIAL_COUNT_FIX, spot_angle=20.0)
     assert got[:, :3].mean() > 0.0
-    assert close_fraction(got[:, :3], want[:, :3]) >= 0.9
+    assert close_fraction(got[:, :3], want[:, :3]) >= 0.99
     np.testing.assert_allclose(got[:, :3].mean(0), want[:, :3].mean(0), rtol=0.03)
 
 

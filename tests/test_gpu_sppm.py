@@ -9,6 +9,8 @@ import os
 import numpy as np
 import pytest
 
+import parity_log
+
 import oracle_lib
 from lumen_gb300 import abi, build, procedural
 from lumen_gb300.scene import Context, GpuScene, camera_lookat, sppm_params
@@ -26,7 +28,11 @@ def ctx():
 
 def close_fraction(a, b, rtol=1e-3, atol=1e-5):
     ok = np.abs(a - b) <= rtol * np.maximum(np.abs(b), 1e-6) + atol
-    return ok.all(axis=1).mean()
+    frac = ok.all(axis=1).mean()
+    parity_log.record(frac, rtol)
+    if rtol != 1e-4:  # also the per-sample tolerance of the path tracer, for the record only
+        parity_log.record((np.abs(a - b) <= 1e-4 * np.maximum(np.abs(b), 1e-6) + 1e-7).all(axis=1).mean(), 1e-4)
+    return frac
 
 
 def _run_both(ctx, oracle, arrays, w, h, frames, depth, base_radius=0.03, spot_angle=0.0, sky=(0.0, 0.0, 0.0)):
@@ -55,9 +61,9 @@ def test_sppm_matches_oracle_cornell(ctx, oracle):
     cb = procedural.cornell_box()
     got, want = _run_both(ctx, oracle, cb, 48, 48, 1, 6)
     assert (got[:, 3] == 1.0).all() and not np.isnan(got).any()
-    assert close_fraction(got[:, :3], want[:, :3]) >= 0.97
+    assert close_fraction(got[:, :3], want[:, :3]) >= 0.99
     got8, want8 = _run_both(ctx, oracle, cb, 48, 48, 8, 6, sky=(0.2, 0.3, 0.4))
-    assert close_fraction(got8[:, :3], want8[:, :3]) >= 0.95
+    assert close_fraction(got8[:, :3], want8[:, :3]) >= 0.99
     np.testing.assert_allclose(got8[:, :3].mean(0), want8[:, :3].mean(0), rtol=0.01)
 
 
@@ -65,7 +71,7 @@ def test_sppm_caustics_scene_matches_oracle(ctx, oracle):
     arrays = procedural.vcm_scene(100, 40)
     got, want = _run_both(ctx, oracle, arrays, 64, 64, 4, 10, base_radius=0.05, spot_angle=20.0)
     assert not np.isnan(got).any() and got[:, :3].mean() > 0.0
-    assert close_fraction(got[:, :3], want[:, :3]) >= 0.95
+    assert close_fraction(got[:, :3], want[:, :3]) >= 0.99
     np.testing.assert_allclose(got[:, :3].mean(0), want[:, :3].mean(0), rtol=0.02)
 
 

@@ -12,6 +12,8 @@ import os
 import numpy as np
 import pytest
 
+import parity_log
+
 from lumen_gb300 import abi, build, procedural
 from lumen_gb300.scene import (Context, GpuScene, camera_forward, camera_lookat, scene_radius, vcm_grid, vcm_params,
                                vcm_radius)
@@ -29,7 +31,11 @@ def ctx():
 
 def close_fraction(a, b, rtol=1e-3, atol=1e-5):
     ok = np.abs(a - b) <= rtol * np.maximum(np.abs(b), 1e-6) + atol
-    return ok.all(axis=1).mean()
+    frac = ok.all(axis=1).mean()
+    parity_log.record(frac, rtol)
+    if rtol != 1e-4:  # also the per-sample tolerance of the path tracer, for the record only
+        parity_log.record((np.abs(a - b) <= 1e-4 * np.maximum(np.abs(b), 1e-6) + 1e-7).all(axis=1).mean(), 1e-4)
+    return frac
 
 
 def test_photon_table_is_bit_exact(ctx, oracle):
@@ -127,11 +133,11 @@ def test_iteration_matches_oracle_cornell(ctx, oracle):
     cb = procedural.cornell_box()
     got, want = _run_both(ctx, oracle, cb, 48, 48, 1, 8)
     frac = close_fraction(got[:, :3], want[:, :3])
-    assert frac >= 0.97, f"only {frac:.4f} of pixels agree"
+    assert frac >= 0.99, f"only {frac:.4f} of pixels agree"
     assert (got[:, 3] == 1.0).all()
     got8, want8 = _run_both(ctx, oracle, cb, 48, 48, 8, 8)
     np.testing.assert_allclose(got8[:, :3].mean(0), want8[:, :3].mean(0), rtol=0.01)
-    assert close_fraction(got8[:, :3], want8[:, :3]) >= 0.9
+    assert close_fraction(got8[:, :3], want8[:, :3]) >= 0.99
 
 
 @pytest.mark.parametrize("spot_angle", [0.0, 20.0])
@@ -140,7 +146,7 @@ def test_caustics_scene_with_merging_matches_oracle(ctx, oracle, spot_angle):
     got, want = _run_both(ctx, oracle, arrays, 64, 64, 4, 10, alpha=0.75, spot_angle=spot_angle)
     assert not np.isnan(got).any()
     frac = close_fraction(got[:, :3], want[:, :3])
-    assert frac >= 0.95, f"only {frac:.4f} of pixels agree"
+    assert frac >= 0.99, f"only {frac:.4f} of pixels agree"
     np.testing.assert_allclose(got[:, :3].mean(0), want[:, :3].mean(0), rtol=0.02)
     assert got[:, :3].mean() > 0.0
 
@@ -152,7 +158,7 @@ def test_caustics_configuration_matches_oracle(ctx, oracle):
     got, want = _run_both(ctx, oracle, arrays, 96, 96, 4, 10, alpha=0.75, spot_angle=20.0)
     assert not np.isnan(got).any()
     frac = close_fraction(got[:, :3], want[:, :3])
-    assert frac >= 0.95, f"only {frac:.4f} of pixels agree"
+    assert frac >= 0.99, f"only {frac:.4f} of pixels agree"
     np.testing.assert_allclose(got[:, :3].mean(0), want[:, :3].mean(0), rtol=0.02)
 
 
@@ -160,7 +166,7 @@ def test_spot_cone_narrows_the_lit_area(ctx, oracle):
     arrays = procedural.vcm_scene(100, 40)
     wide, _ = _run_both(ctx, oracle, arrays, 48, 48, 1, 4, alpha=0.75)
     narrow, want = _run_both(ctx, oracle, arrays, 48, 48, 1, 4, alpha=0.75, spot_angle=10.0)
-    assert close_fraction(narrow[:, :3], want[:, :3]) >= 0.95
+    assert close_fraction(narrow[:, :3], want[:, :3]) >= 0.99
     lit = lambda img: int((img[:, :3].sum(1) > 1e-4).sum())
     assert 0 < lit(narrow) < lit(wide)
 
@@ -168,7 +174,7 @@ def test_spot_cone_narrows_the_lit_area(ctx, oracle):
 def test_accumulate_option_matches_oracle(ctx, oracle):
     cb = procedural.cornell_box()
     got, want = _run_both(ctx, oracle, cb, 32, 32, 2, 8, flags=abi.VCM_ACCUMULATE)
-    assert close_fraction(got[:, :3], want[:, :3]) >= 0.95
+    assert close_fraction(got[:, :3], want[:, :3]) >= 0.99
     base, _ = _run_both(ctx, oracle, cb, 32, 32, 2, 8)
     assert got[:, :3].mean() >= base[:, :3].mean()
 

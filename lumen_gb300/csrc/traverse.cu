@@ -18,7 +18,11 @@ constexpr int kTraceMinBlocks = 9;
 // Bottom entries of each thread's traversal stack kept in shared memory (8 KB per block). Measured on GB300,
 // 4M incoherent rays / 1M triangles, closest / any Mrays/s: 0 entries 1133 / 2280, 4: 1137 / 2318,
 // 8: 1142 / 2335, 12: 1142 / 2323.
+#ifdef LGB_TRACE_SK
+constexpr int kTraceSharedStack = LGB_TRACE_SK;
+#else
 constexpr int kTraceSharedStack = 8;
+#endif
 // Idle lanes a warp waits for before fetching new rays. Measured with the approximate box-test reciprocal and
 // mixed iterations, closest / any Mrays/s: refill at 1 idle lane 1176 / 2350, at 8: 1185 / 2680, at 16: 1047 /
 // 2485. With warp-uniform triangle iterations (below) and one triangle per leaf slot: at 8: 1317 / 3048, at 4:

@@ -26,12 +26,10 @@ def ctx():
     return Context(0)
 
 
-def close_fraction(a, b, rtol=1e-3, atol=1e-5):
+def close_fraction(a, b, rtol=1e-4, atol=1e-7):
     ok = np.abs(a - b) <= rtol * np.maximum(np.abs(b), 1e-6) + atol
     frac = ok.all(axis=1).mean()
     parity_log.record(frac, rtol)
-    if rtol != 1e-4:  # also the per-sample tolerance of the path tracer, for the record only
-        parity_log.record((np.abs(a - b) <= 1e-4 * np.maximum(np.abs(b), 1e-6) + 1e-7).all(axis=1).mean(), 1e-4)
     return frac
 
 

@@ -134,6 +134,8 @@ def test_iteration_matches_oracle_cornell(ctx, oracle):
     got, want = _run_both(ctx, oracle, cb, 48, 48, 1, 8)
     frac = close_fraction(got[:, :3], want[:, :3])
     assert frac >= 0.99, f"only {frac:.4f} of pixels agree"
+    # at the path tracer's per-sample tolerance too: only the order of the float splat sums differs
+    assert close_fraction(got[:, :3], want[:, :3], rtol=1e-4, atol=1e-7) >= 0.99
     assert (got[:, 3] == 1.0).all()
     got8, want8 = _run_both(ctx, oracle, cb, 48, 48, 8, 8)
     np.testing.assert_allclose(got8[:, :3].mean(0), want8[:, :3].mean(0), rtol=0.01)
@@ -159,6 +161,7 @@ def test_caustics_configuration_matches_oracle(ctx, oracle):
     assert not np.isnan(got).any()
     frac = close_fraction(got[:, :3], want[:, :3])
     assert frac >= 0.99, f"only {frac:.4f} of pixels agree"
+    assert close_fraction(got[:, :3], want[:, :3], rtol=1e-4, atol=1e-7) >= 0.95
     np.testing.assert_allclose(got[:, :3].mean(0), want[:, :3].mean(0), rtol=0.02)
 
 

@@ -163,10 +163,15 @@ struct Batch {
     void* buf = nullptr;
     size_t buf_bytes = 0;
     void* graph = nullptr;
-    uint64_t graph_key[6] = {};
+    uint64_t graph_key[8] = {};
     void* capture_stream = nullptr;
     void* staging = nullptr;        // pinned host copy of the job table
     void* staging_event = nullptr;  // recorded after the table's upload, before the staging is reused
+    // the render's chunk records in device memory, walked by the graph's device-driven loop
+    void* d_chunks = nullptr;       // BatchChunk[chunk_cap]
+    void* chunk_staging = nullptr;  // pinned host copy of them
+    uint32_t chunk_cap = 0;
+    uint32_t* d_loop = nullptr;     // [0] index of the chunk being rendered, [1] chunk count
     bool tuned = false;
     lgb_batch_opts tuned_opts{};
 };

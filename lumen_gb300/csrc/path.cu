@@ -907,6 +907,28 @@ __global__ void k_set_chunk(BatchChunk C, BatchChunk* dst) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *dst = C;
 }
 
+// The device-driven chunk loop of a batch render: the body of the graph's WHILE node starts by copying chunk
+// loop[0] of the uploaded records into the chunk record the kernels read, and ends by advancing loop[0] and
+// setting the loop condition to loop[0] < loop[1]. loop[0] grows by one per iteration and loop[1] is the
+// chunk count of the call, so the loop runs exactly that many times.
+__global__ void k_next_chunk(const BatchChunk* __restrict__ chunks, const uint32_t* __restrict__ loop, BatchChunk* dst) {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(chunks + loop[0]);
+    uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+    constexpr uint32_t words = sizeof(BatchChunk) / 4;
+    static_assert(sizeof(BatchChunk) % 4 == 0, "chunk record of whole words");
+    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) d[i] = src[i];
+}
+__global__ void k_loop_next(cudaGraphConditionalHandle h, uint32_t* loop) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const uint32_t next = loop[0] + 1u;
+        loop[0] = next;
+        cudaGraphSetConditional(h, next < loop[1] ? 1u : 0u);
+    }
+}
+__global__ void k_loop_init(uint32_t* loop, uint32_t n) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) { loop[0] = 0u; loop[1] = n; }
+}
+
 void free_batch(Batch* b) {
     cudaSetDevice(b->ctx->device);
     if (b->graph) cudaGraphExecDestroy((cudaGraphExec_t)b->graph);
@@ -916,6 +938,9 @@ void free_batch(Batch* b) {
         cudaEventDestroy((cudaEvent_t)b->staging_event);
     }
     if (b->staging) cudaFreeHost(b->staging);
+    if (b->chunk_staging) cudaFreeHost(b->chunk_staging);
+    cudaFree(b->d_chunks);
+    cudaFree(b->d_loop);
     cudaFree(b->buf);
     cudaFree(b->nodes);
     cudaFree(b->tris);
@@ -957,6 +982,7 @@ lgb_status batch_create(Ctx* ctx, Scene* const* scenes, uint32_t n, Batch* b) {
     LGB_CUDA_TRY(ctx, cudaGetLastError());
     LGB_CUDA_TRY(ctx, cudaDeviceSynchronize());
     LGB_CUDA_TRY(ctx, cudaMallocHost(&b->staging, sizeof(JobRec) * kMaxBatchJobs));
+    LGB_CUDA_TRY(ctx, cudaMalloc(&b->d_loop, 2 * sizeof(uint32_t)));
     cudaEvent_t ev;
     LGB_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     b->staging_event = ev;
@@ -1060,6 +1086,30 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
         stage[j].root = b->roots[jobs[j].scene];
     }
     LGB_CUDA_TRY(ctx, cudaMemcpyAsync(const_cast<JobRec*>(B.jobs), stage, sizeof(JobRec) * n, cudaMemcpyHostToDevice, st));
+    std::vector<BatchChunk> chunks;
+    plan_chunks(jobs, n, cap, write_film, chunks);
+    const uint32_t nch = (uint32_t)chunks.size();
+    cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+    LGB_CUDA_TRY(ctx, cudaStreamIsCapturing(st, &cap_status));
+    const bool use_graph = cap_status == cudaStreamCaptureStatusNone;
+    if (use_graph && nch > 0) {
+        // The chunk records, staged in pinned memory (free once the previous call's uploads are done, which the
+        // staging event waited for above) and uploaded on the stream for the graph's device-driven loop.
+        if (nch > b->chunk_cap) {
+            if (b->graph) { cudaGraphExecDestroy((cudaGraphExec_t)b->graph); b->graph = nullptr; }
+            if (b->chunk_staging) cudaFreeHost(b->chunk_staging);
+            b->chunk_staging = nullptr;
+            cudaFree(b->d_chunks);
+            b->d_chunks = nullptr;
+            b->chunk_cap = 0;
+            const uint32_t want = std::max(nch, 16u);
+            LGB_CUDA_TRY(ctx, cudaMalloc(&b->d_chunks, sizeof(BatchChunk) * want));
+            LGB_CUDA_TRY(ctx, cudaMallocHost(&b->chunk_staging, sizeof(BatchChunk) * want));
+            b->chunk_cap = want;
+        }
+        std::memcpy(b->chunk_staging, chunks.data(), sizeof(BatchChunk) * nch);
+        LGB_CUDA_TRY(ctx, cudaMemcpyAsync(b->d_chunks, b->chunk_staging, sizeof(BatchChunk) * nch, cudaMemcpyHostToDevice, st));
+    }
     LGB_CUDA_TRY(ctx, cudaEventRecord((cudaEvent_t)b->staging_event, st));
 
     SceneView F;
@@ -1067,37 +1117,61 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
     F.nodes = b->nodes;
     F.tris = b->tris;
     F.status = b->d_status;
-    cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
-    LGB_CUDA_TRY(ctx, cudaStreamIsCapturing(st, &cap_status));
-    const bool use_graph = cap_status == cudaStreamCaptureStatusNone;
-    const uint64_t key[6] = {(uint64_t)(uintptr_t)b->buf, cap,
+    if (nch == 0) return LGB_OK;
+    if (!use_graph) {  // the caller is capturing this stream: the chunks go into its capture one after another
+        for (const BatchChunk& C : chunks) {
+            k_set_chunk<<<1, 1, 0, st>>>(C, const_cast<BatchChunk*>(B.chunk));
+            LGB_CUDA_TRY(ctx, launch_chunk<true>(F, B, bounces, g, batch_classes(b), st));
+        }
+        LGB_CUDA_TRY(ctx, cudaGetLastError());
+        return LGB_OK;
+    }
+    // One graph renders every chunk of the call: a WHILE node whose body selects the next chunk record, runs the
+    // captured bounce loop over it and advances the loop (k_next_chunk, launch_chunk, k_loop_next). It depends on
+    // the arena, the forest, the bounce count, the grids and the chunk-record array, not on the jobs.
+    const uint64_t key[8] = {(uint64_t)(uintptr_t)b->buf, cap,
                              (uint64_t)bounces | ((uint64_t)g.shared_stack << 32) | ((uint64_t)batch_classes(b) << 40),
                              (uint64_t)(uintptr_t)b->nodes, (uint64_t)(uintptr_t)b->tris,
-                             ((uint64_t)g.work << 32) | (uint32_t)g.trace};
-    if (use_graph && (!b->graph || std::memcmp(key, b->graph_key, sizeof(key)) != 0)) {
+                             ((uint64_t)g.work << 32) | (uint32_t)g.trace, (uint64_t)(uintptr_t)b->d_chunks,
+                             (uint64_t)(uintptr_t)b->d_loop};
+    if (!b->graph || std::memcmp(key, b->graph_key, sizeof(key)) != 0) {
         if (b->graph) { cudaGraphExecDestroy((cudaGraphExec_t)b->graph); b->graph = nullptr; }
         if (!b->capture_stream) LGB_CUDA_TRY(ctx, cudaStreamCreateWithFlags((cudaStream_t*)&b->capture_stream, cudaStreamNonBlocking));
         const cudaStream_t cs = (cudaStream_t)b->capture_stream;
-        cudaGraph_t graph = nullptr;
-        LGB_CUDA_TRY(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-        const cudaError_t le = launch_chunk<true>(F, B, bounces, g, batch_classes(b), cs);
-        const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
-        if (le != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_error(ctx, le, "capturing the batch bounce loop"); }
-        if (ce != cudaSuccess) return cuda_error(ctx, ce, "cudaStreamEndCapture");
+        cudaGraph_t top = nullptr;
+        LGB_CUDA_TRY(ctx, cudaGraphCreate(&top, 0));
+        cudaGraphConditionalHandle cond;
+        cudaError_t e = cudaGraphConditionalHandleCreate(&cond, top, 1u, cudaGraphCondAssignDefault);
+        cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};  // the remaining fields zero
+        np.conditional.handle = cond;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t loop_node = nullptr;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&loop_node, top, nullptr, nullptr, 0, &np);
+        if (e != cudaSuccess) { cudaGraphDestroy(top); return cuda_error(ctx, e, "building the batch's chunk loop"); }
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) { cudaGraphDestroy(top); return cuda_error(ctx, e, "cudaStreamBeginCaptureToGraph"); }
+        k_next_chunk<<<1, 256, 0, cs>>>(reinterpret_cast<const BatchChunk*>(b->d_chunks), b->d_loop,
+                                        const_cast<BatchChunk*>(B.chunk));
+        cudaError_t le = launch_chunk<true>(F, B, bounces, g, batch_classes(b), cs);
+        k_loop_next<<<1, 32, 0, cs>>>(cond, b->d_loop);
+        if (le == cudaSuccess) le = cudaGetLastError();
+        cudaGraph_t captured = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(cs, &captured);
+        if (le != cudaSuccess || ce != cudaSuccess) {
+            cudaGraphDestroy(top);
+            return cuda_error(ctx, le != cudaSuccess ? le : ce, "capturing the batch bounce loop");
+        }
         cudaGraphExec_t exec = nullptr;
-        const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-        cudaGraphDestroy(graph);
+        const cudaError_t ie = cudaGraphInstantiate(&exec, top, 0);
+        cudaGraphDestroy(top);
         if (ie != cudaSuccess) return cuda_error(ctx, ie, "cudaGraphInstantiate");
         b->graph = exec;
         std::memcpy(b->graph_key, key, sizeof(key));
     }
-    std::vector<BatchChunk> chunks;
-    plan_chunks(jobs, n, cap, write_film, chunks);
-    for (const BatchChunk& C : chunks) {
-        k_set_chunk<<<1, 1, 0, st>>>(C, const_cast<BatchChunk*>(B.chunk));
-        if (use_graph) LGB_CUDA_TRY(ctx, cudaGraphLaunch((cudaGraphExec_t)b->graph, st));
-        else LGB_CUDA_TRY(ctx, launch_chunk<true>(F, B, bounces, g, batch_classes(b), st));
-    }
+    k_loop_init<<<1, 1, 0, st>>>(b->d_loop, nch);
+    LGB_CUDA_TRY(ctx, cudaGraphLaunch((cudaGraphExec_t)b->graph, st));
     LGB_CUDA_TRY(ctx, cudaGetLastError());
     return LGB_OK;
 }

@@ -510,7 +510,8 @@ def batch_secondary(torch, ctx_cls, scene_cls, local):
            "rmse_vs_fp64": {"scenes": rmse, "render": "128x128 at the scene's own spp",
                             "reference": "FP64 CPU oracle, 2048 spp (tests/golden/batch_scene*_128_fp64_ref.npy)"},
            "tuned": {"path_capacity": best.path_capacity, "work_blocks_per_sm": best.work_blocks_per_sm,
-                     "stack": "shared" if best.stack_placement == 1 else "local"},
+                     "stack": "shared" if best.stack_placement == 1 else "local",
+                     "path_regeneration": best.chunk_paths != 1},
            "tune_s": tune_s, "scene_generation_s": gen_s}
     batch.close()
     for sc in scenes:

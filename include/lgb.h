@@ -458,7 +458,10 @@ typedef struct lgb_batch_opts {
     uint32_t stack_placement;      /* traversal stack: LGB_STACK_LOCAL (0) per-thread local memory, or
                                       LGB_STACK_SHARED: its bottom 8 entries in shared memory */
     uint32_t from_cache;           /* written by lgb_batch_tune: 1 when the choice came from the tuning cache */
-    uint32_t reserved[3];
+    uint32_t chunk_paths;          /* path regeneration: paths per chunk, run through the path_capacity slots
+                                      (an ended path's slot takes the chunk's next path); 0 = 16 x path_capacity
+                                      (at most 2^27), 1 = no regeneration (chunks of at most path_capacity) */
+    uint32_t reserved[2];
 } lgb_batch_opts;
 #define LGB_STACK_LOCAL 0u
 #define LGB_STACK_SHARED 1u
@@ -468,11 +471,16 @@ typedef struct lgb_batch_opts {
 LGB_API lgb_status lgb_batch_create(lgb_ctx* ctx, lgb_scene* const* scenes, uint32_t num_scenes, lgb_batch** out);
 LGB_API void lgb_batch_destroy(lgb_batch* batch);
 /* Renders up to 128 jobs. opts null = the options lgb_batch_tune chose, else the defaults. Jobs are cut into
- * chunks of whole frames; a chunk holds frames of several jobs. */
+ * chunks of whole frames; a chunk holds frames of several jobs. With path regeneration (the default) a chunk
+ * holds up to chunk_paths paths and runs through path_capacity slots: a slot whose path ended takes the chunk's
+ * next path, and each job's film receives its frames in order once the chunk's last path has ended. Every path is
+ * computed as lgb_render_path computes it, so films are bit-identical to rendering each job alone. On a stream
+ * that the caller is capturing, the chunks are captured one after another without regeneration. */
 LGB_API lgb_status lgb_batch_render(lgb_batch* batch, const lgb_batch_job* jobs, uint32_t num_jobs,
                                     const lgb_batch_opts* opts, void* stream);
-/* Autotuner: times lgb_batch_render over candidate queue sizes and grids on a reduced copy of `jobs` (a
- * quarter of each job's frames, films untouched), keeps the fastest for later renders and writes it to *best.
+/* Autotuner: times lgb_batch_render over candidate queue sizes, grids, stack placements and with or without path
+ * regeneration on a reduced copy of `jobs` (a quarter of each job's frames, films untouched), keeps the fastest
+ * for later renders and writes it to *best.
  * With a tuning cache (lgb_create) a batch of the same shape on the same kind of device takes the cached choice
  * without timing anything (best->from_cache = 1); a new choice is added to the cache. Waits for `stream`. */
 LGB_API lgb_status lgb_batch_tune(lgb_batch* batch, const lgb_batch_job* jobs, uint32_t num_jobs,

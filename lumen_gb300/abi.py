@@ -119,7 +119,7 @@ class BatchJob(C.Structure):
 class BatchOpts(C.Structure):
     _fields_ = [("path_capacity", C.c_uint32), ("work_blocks_per_sm", C.c_uint32),
                 ("trace_blocks_per_sm", C.c_uint32), ("stack_placement", C.c_uint32),
-                ("from_cache", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+                ("from_cache", C.c_uint32), ("chunk_paths", C.c_uint32), ("reserved", C.c_uint32 * 2)]
 
 
 STACK_LOCAL, STACK_SHARED = 0, 1  # lgb_batch_opts.stack_placement

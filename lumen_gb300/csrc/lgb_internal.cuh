@@ -163,7 +163,7 @@ struct Batch {
     void* buf = nullptr;
     size_t buf_bytes = 0;
     void* graph = nullptr;
-    uint64_t graph_key[8] = {};
+    uint64_t graph_key[10] = {};
     void* capture_stream = nullptr;
     void* staging = nullptr;        // pinned host copy of the job table
     void* staging_event = nullptr;  // recorded after the table's upload, before the staging is reused
@@ -172,6 +172,9 @@ struct Batch {
     void* chunk_staging = nullptr;  // pinned host copy of them
     uint32_t chunk_cap = 0;
     uint32_t* d_loop = nullptr;     // [0] index of the chunk being rendered, [1] chunk count
+    void* col_out = nullptr;        // float4 per path of the largest chunk: path regeneration's radiance output
+    uint64_t col_out_paths = 0;
+    bool regen_refused = false;     // the device refused the nested loop graph of path regeneration
     bool tuned = false;
     lgb_batch_opts tuned_opts{};
 };

@@ -87,7 +87,8 @@ struct Buffers {
     lgb_hit* mhits;
     uint32_t* sbits;
     uint32_t* counters; // [0] cur, [1] next, [2] nee, [3..6] class counts, [8..10] trace work counters,
-                        // [11] queued BSDF-MIS rays
+                        // [11] queued BSDF-MIS rays; batched only: [12] paths ended this bounce, [13] paths of
+                        // the chunk started so far
     Params* params;     // per-chunk parameters in device memory, so that a captured graph can be replayed
     uint32_t cap;       // path capacity of the arena
     // batched rendering only (null otherwise)
@@ -98,6 +99,11 @@ struct Buffers {
     uint32_t* mroot;     // ... of the queued BSDF-MIS rays
     const JobRec* jobs;
     const BatchChunk* chunk;
+    // batched rendering with path regeneration: a slot freed by an ended path takes the chunk's next path
+    uint32_t* pid;       // chunk path (segment-major, as path_off + frame * npix + pixel) held by each slot
+    uint32_t* done;      // slots whose path ended this bounce
+    float4* col_out;     // final radiance of every path of the chunk, by chunk path
+    const float4* film_src;  // what the film kernel reads by chunk path: col (one slot per path) or col_out
 };
 
 // Batched rendering: several scenes and cameras share one wavefront. Every job (a scene, a camera, path
@@ -140,46 +146,56 @@ __device__ __forceinline__ int class_of(uint32_t bsdf_type) { return shade_class
 
 // ---------------- kernels ----------------
 
-// path.rgen:22-46: the seed is (x, y, frame, 0); two draws jitter the pixel.
+// path.rgen:22-46: the seed is (x, y, frame, 0); two draws jitter the pixel. Starts chunk path `id` (batched:
+// segment-major over the chunk's segments; else frame-major over the chunk's frames) in arena slot `slot`, with
+// its camera ray at position q of a ray queue (rays, slots and, batched, BVH roots).
+template <bool BATCH>
+__device__ __forceinline__ void start_path(const Params* __restrict__ Pp, const Buffers& B, uint32_t id, uint32_t slot,
+                                           lgb_ray* rays, uint32_t* qlist, uint32_t* roots, uint32_t q) {
+    uint32_t local = id, frame0 = 0u, job = 0u;
+    if (BATCH) {
+        const Segment& sg = B.chunk->seg[find_segment<false>(*B.chunk, id)];
+        local = id - sg.path_off;
+        frame0 = sg.frame0;
+        job = sg.job;
+    } else {
+        frame0 = Pp->frame0;
+    }
+    const Params& P = BATCH ? B.jobs[job].P : *Pp;
+    const uint32_t pix = local % P.npix, f = frame0 + local / P.npix;
+    const uint32_t x = pix % P.width, y = pix / P.width;
+    uint4 seed = make_uint4(x, y, f, 0u);
+    const float px = (float)x + 0.5f, py = (float)y + 0.5f;
+    const float r0 = rnd(seed) - 0.5f;
+    const float r1 = rnd(seed) - 0.5f;
+    const float u = (px + r0) / (float)P.width, v = (py + r1) / (float)P.height;
+    const float dx = u * 2.0f - 1.0f, dy = v * 2.0f - 1.0f;
+    const float4 origin = mat_vec(P.iv, 0.0f, 0.0f, 0.0f, 1.0f);
+    const float4 target = mat_vec(P.ip, dx, dy, 1.0f, 1.0f);
+    const v3 tn = normalize(V3(target.x, target.y, target.z));
+    const float4 dir = mat_vec(P.iv, tn.x, tn.y, tn.z, 0.0f);
+    B.pix[slot] = pix;
+    B.frame[slot] = f;
+    B.w[slot] = seed.w;
+    B.flags[slot] = 0u;
+    B.T[slot] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    B.col[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    qlist[q] = slot;
+    if (BATCH) {
+        B.job[slot] = job;
+        B.pid[slot] = id;
+        roots[q] = B.jobs[job].root;
+    }
+    store_ray(&rays[q], make_ray(V3(origin.x, origin.y, origin.z), kTMin, V3(dir.x, dir.y, dir.z), kTMax));
+}
+
+// The chunk's first paths, path i in slot i: every path of a chunk that fits the arena; batched, the first
+// `cap` paths of a larger chunk, whose other paths start as slots free up (k_regen).
 template <bool BATCH>
 __global__ void __launch_bounds__(kThreads) k_camera(const Params* __restrict__ Pp, Buffers B) {
-    const uint32_t n = BATCH ? B.chunk->npaths : Pp->npix * Pp->nframes;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t local = i, frame0 = 0u, job = 0u;
-        if (BATCH) {
-            const Segment& sg = B.chunk->seg[find_segment<false>(*B.chunk, i)];
-            local = i - sg.path_off;
-            frame0 = sg.frame0;
-            job = sg.job;
-        } else {
-            frame0 = Pp->frame0;
-        }
-        const Params& P = BATCH ? B.jobs[job].P : *Pp;
-        const uint32_t pix = local % P.npix, f = frame0 + local / P.npix;
-        const uint32_t x = pix % P.width, y = pix / P.width;
-        uint4 seed = make_uint4(x, y, f, 0u);
-        const float px = (float)x + 0.5f, py = (float)y + 0.5f;
-        const float r0 = rnd(seed) - 0.5f;
-        const float r1 = rnd(seed) - 0.5f;
-        const float u = (px + r0) / (float)P.width, v = (py + r1) / (float)P.height;
-        const float dx = u * 2.0f - 1.0f, dy = v * 2.0f - 1.0f;
-        const float4 origin = mat_vec(P.iv, 0.0f, 0.0f, 0.0f, 1.0f);
-        const float4 target = mat_vec(P.ip, dx, dy, 1.0f, 1.0f);
-        const v3 tn = normalize(V3(target.x, target.y, target.z));
-        const float4 dir = mat_vec(P.iv, tn.x, tn.y, tn.z, 0.0f);
-        B.pix[i] = pix;
-        B.frame[i] = f;
-        B.w[i] = seed.w;
-        B.flags[i] = 0u;
-        B.T[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-        B.col[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        B.q_cur[i] = i;
-        if (BATCH) {
-            B.job[i] = job;
-            B.root[i] = B.jobs[job].root;
-        }
-        store_ray(&B.rays[i], make_ray(V3(origin.x, origin.y, origin.z), kTMin, V3(dir.x, dir.y, dir.z), kTMax));
-    }
+    const uint32_t n = BATCH ? min(B.chunk->npaths, B.cap) : Pp->npix * Pp->nframes;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        start_path<BATCH>(Pp, B, i, i, B.rays, B.q_cur, B.root, i);
 }
 
 // Closest-hit / any-hit over a device-counted queue of rays, persistent with dynamic fetch; `roots` gives each
@@ -234,11 +250,14 @@ __global__ void __launch_bounds__(kThreads) k_classify(SceneView S0, const Param
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
         const uint32_t i = base + threadIdx.x;
         int cls = -1;
+        bool ended = false;
+        uint32_t p = 0u;
         if (i < n) {
             const uint32_t prim = B.hits[i].prim;
-            const uint32_t p = B.q_cur[i];
+            p = B.q_cur[i];
             const uint32_t job = BATCH ? B.job[p] : 0u;
             if (prim == LGB_NO_HIT) {
+                ended = true;
                 const Params& P = BATCH ? B.jobs[job].P : *Pp;
                 const uint32_t depth = B.flags[p] & 0xffffu;
                 if (depth > 0 || P.direct_lighting == 1u) {
@@ -258,6 +277,10 @@ __global__ void __launch_bounds__(kThreads) k_classify(SceneView S0, const Param
         for (int c = 0; c < NUM_CLS; c++) {
             const uint32_t slot = agg_slot(&B.counters[3 + c], cls == c);
             if (cls == c) B.q_cls[(size_t)c * B.cap + slot] = i;
+        }
+        if (BATCH) {  // a missed path ends here; its slot is listed for regeneration
+            const uint32_t dslot = agg_slot(&B.counters[12], ended);
+            if (ended) B.done[dslot] = p;
         }
     }
 }
@@ -291,7 +314,7 @@ __device__ __forceinline__ v3 cls_eval(v3 n_s, v3 wo, const Mat& m, bool ff, v3 
 // and wants occupancy (Cornell / batch scene 550 / 354 Msamples/s against 549 / 349 uncapped at 140 registers).
 constexpr int kShadeMinBlocks = 4;
 template <int CLS, bool BATCH>
-__global__ void __launch_bounds__(kThreads, kShadeMinBlocks) k_shade(SceneView S0, const Params* __restrict__ Pp, Buffers B, int depth) {
+__global__ void __launch_bounds__(kThreads, kShadeMinBlocks) k_shade(SceneView S0, const Params* __restrict__ Pp, Buffers B, int bounce) {
     const uint32_t n = B.counters[3 + CLS];
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t* list = B.q_cls + (size_t)CLS * B.cap;
@@ -313,6 +336,8 @@ __global__ void __launch_bounds__(kThreads, kShadeMinBlocks) k_shade(SceneView S
             const uint32_t pix = B.pix[p], frame = B.frame[p];
             uint4 seed = seed_of(pix, P.width, frame, B.w[p]);
             const uint32_t fl = B.flags[p];
+            // batched, paths of different depths share a bounce (regeneration): each path's own depth
+            const int depth = BATCH ? (int)(fl & 0xffffu) : bounce;
             const bool last_specular = (fl >> 16) & 1u;
             v3 T = f3(B.T[p]);
             v3 col = f3(B.col[p]);
@@ -467,6 +492,11 @@ __global__ void __launch_bounds__(kThreads, kShadeMinBlocks) k_shade(SceneView S
             store_ray(&B.rays_next[cslot], next_ray);
             if (BATCH) B.root_next[cslot] = root;
         }
+        if (BATCH) {  // an ended path's slot is listed for regeneration (its NEE record still resolves first)
+            const bool ended = k < n && !cont;
+            const uint32_t dslot = agg_slot(&B.counters[12], ended);
+            if (ended) B.done[dslot] = p;
+        }
         // Only BSDF-MIS rays with a non-empty interval are queued (those the pre-test above did not end); the NEE
         // record keeps the ray's queue slot. A record without a queued ray resolves as a miss, as its empty ray
         // would have.
@@ -535,7 +565,34 @@ __global__ void k_rotate(uint32_t* counters) {
         counters[1] = 0u;
         counters[2] = 0u;
         for (int c = 0; c < NUM_CLS; c++) counters[3 + c] = 0u;
-        counters[8] = counters[9] = counters[10] = counters[11] = 0u;
+        counters[8] = counters[9] = counters[10] = counters[11] = counters[12] = 0u;
+    }
+}
+
+// Path regeneration (batched): after the bounce's NEE records have resolved, every slot on the ended list hands its
+// path's radiance to col_out, and the first of them take the chunk's next paths, whose camera rays are appended
+// to the continuation queue behind the continuing paths. k_rotate_regen then makes both the next bounce's queue.
+__global__ void __launch_bounds__(kThreads) k_regen(Buffers B) {
+    const uint32_t nd = B.counters[12], base = B.counters[1], next = B.counters[13];
+    const uint32_t nn = min(nd, B.chunk->npaths - next);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nd; i += gridDim.x * blockDim.x) {
+        const uint32_t slot = B.done[i];
+        B.col_out[B.pid[slot]] = B.col[slot];
+        if (i < nn) start_path<true>(nullptr, B, next + i, slot, B.rays_next, B.q_next, B.root_next, base + i);
+    }
+}
+__global__ void k_rotate_regen(uint32_t* counters, const BatchChunk* __restrict__ chunk, cudaGraphConditionalHandle h) {
+    if (threadIdx.x == 0) {
+        const uint32_t next = counters[13];
+        const uint32_t nn = min(counters[12], chunk->npaths - next);
+        const uint32_t live = counters[1] + nn;
+        counters[0] = live;
+        counters[13] = next + nn;
+        counters[1] = 0u;
+        counters[2] = 0u;
+        for (int c = 0; c < NUM_CLS; c++) counters[3 + c] = 0u;
+        counters[8] = counters[9] = counters[10] = counters[11] = counters[12] = 0u;
+        cudaGraphSetConditional(h, live > 0u ? 1u : 0u);
     }
 }
 
@@ -545,7 +602,7 @@ __device__ __forceinline__ void film_frames(const Params& P, const Buffers& B, f
     float4 px = film[pix];
     for (uint32_t k = 0; k < nframes; k++) {
         const uint32_t f = frame0 + k;
-        const float4 c4 = B.col[path_off + (size_t)k * P.npix + pix];
+        const float4 c4 = B.film_src[path_off + (size_t)k * P.npix + pix];
         const v3 col = f3(c4);
         if (P.film_mode == 1u) {
             px = make_float4(col.x, col.y, col.z, 1.0f);
@@ -587,8 +644,8 @@ __global__ void k_clear_bits(uint32_t* bits, const uint32_t* count_ptr) {
 
 template <bool BATCH>
 __global__ void k_init_counters(Buffers B, const Params* __restrict__ Pp) {
-    if (threadIdx.x < 16)
-        B.counters[threadIdx.x] = threadIdx.x == 0 ? (BATCH ? B.chunk->npaths : Pp->npix * Pp->nframes) : 0u;
+    const uint32_t n = BATCH ? min(B.chunk->npaths, B.cap) : Pp->npix * Pp->nframes;
+    if (threadIdx.x < 16) B.counters[threadIdx.x] = threadIdx.x == 0 || (BATCH && threadIdx.x == 13) ? n : 0u;
 }
 
 __global__ void k_set_params(Params P, Params* dst) {
@@ -625,6 +682,9 @@ size_t carve(char* base, uint32_t cap, Buffers& B, bool batch = false) {
     B.job = B.root = B.root_next = B.nroot = B.mroot = nullptr;
     B.jobs = nullptr;
     B.chunk = nullptr;
+    B.pid = B.done = nullptr;
+    B.col_out = nullptr;
+    B.film_src = B.col;
     if (batch) {
         B.job = (uint32_t*)take(4ull * cap);
         B.root = (uint32_t*)take(4ull * cap);
@@ -633,6 +693,8 @@ size_t carve(char* base, uint32_t cap, Buffers& B, bool batch = false) {
         B.mroot = (uint32_t*)take(4ull * cap);
         B.jobs = (const JobRec*)take(sizeof(JobRec) * kMaxBatchJobs);
         B.chunk = (const BatchChunk*)take(sizeof(BatchChunk));
+        B.pid = (uint32_t*)take(4ull * cap);
+        B.done = (uint32_t*)take(4ull * cap);
     }
     return off;
 }
@@ -667,30 +729,55 @@ void queue_traces(const SceneView& S, const Buffers& B, Grids g, cudaStream_t st
     else launch_queue_traces<0>(S, B, g, st, first);
 }
 
-// One chunk of frames: camera rays, `bounces` bounces, film. Every kernel reads its parameters from device
-// memory (B.params, or the job table and chunk record when batched), so this sequence can be captured once and
-// replayed with new parameters. `classes` (bit c: shading class c) names the classes the scene's materials fall
-// in; the shading kernels of the other classes would always find an empty list and are not launched.
+// One bounce over the live queue: closest hits, classification, shading per class, shadow and BSDF-MIS traces,
+// NEE resolve. `classes` (bit c: shading class c) names the classes the scene's materials fall in; the shading
+// kernels of the other classes would always find an empty list and are not launched.
+template <bool BATCH>
+void launch_bounce(const SceneView& S, const Buffers& B, int depth, Grids g, uint32_t classes, cudaStream_t st) {
+    queue_traces(S, B, g, st, true);
+    k_classify<BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B);
+    if (classes & (1u << CLS_DIFFUSE)) k_shade<CLS_DIFFUSE, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+    if (classes & (1u << CLS_CONDUCTOR)) k_shade<CLS_CONDUCTOR, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+    if (classes & (1u << CLS_SPECULAR)) k_shade<CLS_SPECULAR, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+    if (classes & (1u << CLS_PRINCIPLED)) k_shade<CLS_PRINCIPLED, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+    k_clear_bits<<<g.work, kThreads, 0, st>>>(B.sbits, B.counters + 2);
+    queue_traces(S, B, g, st, false);
+    k_nee_resolve<BATCH><<<g.work, kThreads, 0, st>>>(S, B);
+}
+
+void swap_queues(Buffers& B) {
+    std::swap(B.rays, B.rays_next);
+    std::swap(B.q_cur, B.q_next);
+    std::swap(B.root, B.root_next);
+}
+
+// One chunk of frames that fits the arena: camera rays, `bounces` bounces, film. Every kernel reads its
+// parameters from device memory (B.params, or the job table and chunk record when batched), so this sequence can
+// be captured once and replayed with new parameters.
 template <bool BATCH>
 cudaError_t launch_chunk(const SceneView& S, Buffers B, int bounces, Grids g, uint32_t classes, cudaStream_t st) {
     k_init_counters<BATCH><<<1, 32, 0, st>>>(B, B.params);
     k_camera<BATCH><<<g.work, kThreads, 0, st>>>(B.params, B);
     for (int depth = 0; depth < bounces; depth++) {
-        queue_traces(S, B, g, st, true);
-        k_classify<BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B);
-        if (classes & (1u << CLS_DIFFUSE)) k_shade<CLS_DIFFUSE, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
-        if (classes & (1u << CLS_CONDUCTOR)) k_shade<CLS_CONDUCTOR, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
-        if (classes & (1u << CLS_SPECULAR)) k_shade<CLS_SPECULAR, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
-        if (classes & (1u << CLS_PRINCIPLED)) k_shade<CLS_PRINCIPLED, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
-        k_clear_bits<<<g.work, kThreads, 0, st>>>(B.sbits, B.counters + 2);
-        queue_traces(S, B, g, st, false);
-        k_nee_resolve<BATCH><<<g.work, kThreads, 0, st>>>(S, B);
+        launch_bounce<BATCH>(S, B, depth, g, classes, st);
         k_rotate<<<1, 32, 0, st>>>(B.counters);
-        std::swap(B.rays, B.rays_next);
-        std::swap(B.q_cur, B.q_next);
-        std::swap(B.root, B.root_next);
+        swap_queues(B);
     }
     k_film<BATCH><<<g.work, kThreads, 0, st>>>(B.params, B);
+    return cudaGetLastError();
+}
+
+// The body of a regenerating chunk's bounce loop: two bounces (the ray queues alternate between them), each
+// followed by regeneration and the queue rotation that sets the loop's condition (some path still live). A
+// bounce over an empty queue finds every count zero and does nothing.
+cudaError_t launch_regen_bounces(const SceneView& S, Buffers B, Grids g, uint32_t classes,
+                                 cudaGraphConditionalHandle h, cudaStream_t st) {
+    for (int k = 0; k < 2; k++) {
+        launch_bounce<true>(S, B, 0, g, classes, st);
+        k_regen<<<g.work, kThreads, 0, st>>>(B);
+        k_rotate_regen<<<1, 32, 0, st>>>(B.counters, B.chunk, h);
+        swap_queues(B);
+    }
     return cudaGetLastError();
 }
 
@@ -892,6 +979,8 @@ namespace {
 
 constexpr uint32_t kBatchDefaultCap = 1u << 21;
 constexpr uint32_t kBatchMaxCap = 1u << 24;
+constexpr uint64_t kBatchChunkPaths = 16;             // default regenerating chunk: 16 x the path capacity
+constexpr uint64_t kBatchMaxChunkPaths = 1ull << 27;  // 2 GB of radiance output
 
 __global__ void k_relocate(const WideNode* __restrict__ src, uint32_t n, uint32_t node_off, uint32_t tri_off,
                            WideNode* __restrict__ dst) {
@@ -928,6 +1017,93 @@ __global__ void k_loop_next(cudaGraphConditionalHandle h, uint32_t* loop) {
 __global__ void k_loop_init(uint32_t* loop, uint32_t n) {
     if (threadIdx.x == 0 && blockIdx.x == 0) { loop[0] = 0u; loop[1] = n; }
 }
+// Enters a regenerating chunk's bounce loop while it has live paths.
+__global__ void k_bounce_loop_begin(cudaGraphConditionalHandle h, const uint32_t* counters) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(h, counters[0] > 0u ? 1u : 0u);
+}
+
+// Adds a WHILE node with handle `h` (created on `g`) to graph `g` after `deps`; returns its body graph.
+cudaError_t add_while(cudaGraph_t g, const cudaGraphNode_t* deps, size_t ndeps, cudaGraphConditionalHandle h,
+                      cudaGraphNode_t* node, cudaGraph_t* body) {
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};  // the remaining fields zero
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    const cudaError_t e = cudaGraphAddNode(node, g, deps, nullptr, ndeps, &np);
+    if (e == cudaSuccess) *body = np.conditional.phGraph_out[0];
+    return e;
+}
+
+// The graph of one batch render: a WHILE loop over the call's chunk records. Without regeneration its body is
+// k_next_chunk, the captured fixed bounce loop of launch_chunk and k_loop_next. With regeneration (B.col_out
+// set) the body starts the chunk's first paths, runs a nested WHILE loop of bounces with regeneration until no
+// path is live, then writes the films.
+cudaError_t build_batch_graph(Batch* b, const SceneView& F, const Buffers& B, int bounces, Grids g, uint32_t classes,
+                              cudaStream_t cs, cudaGraphExec_t* out) {
+    cudaStream_t cs2 = nullptr;  // captures the nested loop's body while cs captures the outer body
+    cudaError_t e = B.col_out ? cudaStreamCreateWithFlags(&cs2, cudaStreamNonBlocking) : cudaSuccess;
+    if (e != cudaSuccess) return e;
+    cudaGraph_t top = nullptr;
+    e = cudaGraphCreate(&top, 0);
+    if (e != cudaSuccess) { if (cs2) cudaStreamDestroy(cs2); return e; }
+    cudaGraphConditionalHandle cond;
+    cudaGraphNode_t loop_node = nullptr;
+    cudaGraph_t body = nullptr;
+    e = cudaGraphConditionalHandleCreate(&cond, top, 1u, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) e = add_while(top, nullptr, 0, cond, &loop_node, &body);
+    if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(top);
+        if (cs2) cudaStreamDestroy(cs2);
+        return e;
+    }
+    cudaGraph_t captured = nullptr;
+    k_next_chunk<<<1, 256, 0, cs>>>(reinterpret_cast<const BatchChunk*>(b->d_chunks), b->d_loop,
+                                    const_cast<BatchChunk*>(B.chunk));
+    if (!B.col_out) {
+        e = launch_chunk<true>(F, B, bounces, g, classes, cs);
+    } else {
+        k_init_counters<true><<<1, 32, 0, cs>>>(B, B.params);
+        k_camera<true><<<g.work, kThreads, 0, cs>>>(B.params, B);
+        // the nested bounce loop, added to the body after what has been captured so far
+        cudaGraphConditionalHandle inner;
+        cudaStreamCaptureStatus cst;
+        cudaGraph_t cg = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        cudaGraphNode_t inner_node = nullptr;
+        cudaGraph_t inner_body = nullptr;
+        e = cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, nullptr, &nd);
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&inner, cg, 0u, 0u);
+        if (e == cudaSuccess) {
+            k_bounce_loop_begin<<<1, 32, 0, cs>>>(inner, B.counters);
+            e = cudaStreamGetCaptureInfo(cs, &cst, nullptr, &cg, &deps, nullptr, &nd);
+        }
+        if (e == cudaSuccess) e = add_while(cg, deps, nd, inner, &inner_node, &inner_body);
+        if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(cs, &inner_node, nullptr, 1, cudaStreamSetCaptureDependencies);
+        if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(cs2, inner_body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            const cudaError_t le = launch_regen_bounces(F, B, g, classes, inner, cs2);
+            cudaGraph_t ig = nullptr;
+            const cudaError_t ce = cudaStreamEndCapture(cs2, &ig);
+            e = le != cudaSuccess ? le : ce;
+        }
+        if (e == cudaSuccess) {
+            k_film<true><<<g.work, kThreads, 0, cs>>>(B.params, B);
+            e = cudaGetLastError();
+        }
+    }
+    k_loop_next<<<1, 32, 0, cs>>>(cond, b->d_loop);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    const cudaError_t ce = cudaStreamEndCapture(cs, &captured);
+    if (e == cudaSuccess) e = ce;
+    if (cs2) cudaStreamDestroy(cs2);
+    cudaGraphExec_t exec = nullptr;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, top, 0);
+    cudaGraphDestroy(top);
+    if (e == cudaSuccess) *out = exec;
+    return e;
+}
 
 void free_batch(Batch* b) {
     cudaSetDevice(b->ctx->device);
@@ -941,6 +1117,7 @@ void free_batch(Batch* b) {
     if (b->chunk_staging) cudaFreeHost(b->chunk_staging);
     cudaFree(b->d_chunks);
     cudaFree(b->d_loop);
+    cudaFree(b->col_out);
     cudaFree(b->buf);
     cudaFree(b->nodes);
     cudaFree(b->tris);
@@ -1086,12 +1263,35 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
         stage[j].root = b->roots[jobs[j].scene];
     }
     LGB_CUDA_TRY(ctx, cudaMemcpyAsync(const_cast<JobRec*>(B.jobs), stage, sizeof(JobRec) * n, cudaMemcpyHostToDevice, st));
-    std::vector<BatchChunk> chunks;
-    plan_chunks(jobs, n, cap, write_film, chunks);
-    const uint32_t nch = (uint32_t)chunks.size();
     cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
     LGB_CUDA_TRY(ctx, cudaStreamIsCapturing(st, &cap_status));
     const bool use_graph = cap_status == cudaStreamCaptureStatusNone;
+    // Path regeneration (in the call's own graph): chunks of up to chunk_paths paths run through the arena's `cap`
+    // slots, each ended path's slot taking the chunk's next path, so the queues stay full until the chunk's last
+    // paths; the radiance of every path goes to col_out for the film.
+    const bool regen = use_graph && !b->regen_refused && o.chunk_paths != 1u;
+    uint64_t chunk_limit = cap;
+    if (regen) {
+        const uint64_t want = o.chunk_paths > 1u ? o.chunk_paths : kBatchChunkPaths * (uint64_t)cap;
+        chunk_limit = std::max<uint64_t>(cap, std::min<uint64_t>(want, kBatchMaxChunkPaths));
+    }
+    std::vector<BatchChunk> chunks;
+    plan_chunks(jobs, n, (uint32_t)chunk_limit, write_film, chunks);
+    const uint32_t nch = (uint32_t)chunks.size();
+    if (regen) {
+        uint64_t most = 0;
+        for (const BatchChunk& C : chunks) most = std::max<uint64_t>(most, C.npaths);
+        if (b->col_out_paths < most) {
+            if (b->graph) { cudaGraphExecDestroy((cudaGraphExec_t)b->graph); b->graph = nullptr; }
+            cudaFree(b->col_out);
+            b->col_out = nullptr;
+            b->col_out_paths = 0;
+            LGB_CUDA_TRY(ctx, cudaMalloc(&b->col_out, sizeof(float4) * most));
+            b->col_out_paths = most;
+        }
+        B.col_out = reinterpret_cast<float4*>(b->col_out);
+        B.film_src = B.col_out;
+    }
     if (use_graph && nch > 0) {
         // The chunk records, staged in pinned memory (free once the previous call's uploads are done, which the
         // staging event waited for above) and uploaded on the stream for the graph's device-driven loop.
@@ -1126,47 +1326,26 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
         LGB_CUDA_TRY(ctx, cudaGetLastError());
         return LGB_OK;
     }
-    // One graph renders every chunk of the call: a WHILE node whose body selects the next chunk record, runs the
-    // captured bounce loop over it and advances the loop (k_next_chunk, launch_chunk, k_loop_next). It depends on
-    // the arena, the forest, the bounce count, the grids and the chunk-record array, not on the jobs.
-    const uint64_t key[8] = {(uint64_t)(uintptr_t)b->buf, cap,
-                             (uint64_t)bounces | ((uint64_t)g.shared_stack << 32) | ((uint64_t)batch_classes(b) << 40),
-                             (uint64_t)(uintptr_t)b->nodes, (uint64_t)(uintptr_t)b->tris,
-                             ((uint64_t)g.work << 32) | (uint32_t)g.trace, (uint64_t)(uintptr_t)b->d_chunks,
-                             (uint64_t)(uintptr_t)b->d_loop};
+    // One graph renders every chunk of the call (build_batch_graph). It depends on the arena, the forest, the
+    // bounce count, the grids, the chunk-record array and the regeneration output, not on the jobs.
+    const uint64_t key[10] = {(uint64_t)(uintptr_t)b->buf, cap,
+                              (uint64_t)bounces | ((uint64_t)g.shared_stack << 32) | ((uint64_t)batch_classes(b) << 40),
+                              (uint64_t)(uintptr_t)b->nodes, (uint64_t)(uintptr_t)b->tris,
+                              ((uint64_t)g.work << 32) | (uint32_t)g.trace, (uint64_t)(uintptr_t)b->d_chunks,
+                              (uint64_t)(uintptr_t)b->d_loop, (uint64_t)(uintptr_t)B.col_out, regen ? 1u : 0u};
     if (!b->graph || std::memcmp(key, b->graph_key, sizeof(key)) != 0) {
         if (b->graph) { cudaGraphExecDestroy((cudaGraphExec_t)b->graph); b->graph = nullptr; }
         if (!b->capture_stream) LGB_CUDA_TRY(ctx, cudaStreamCreateWithFlags((cudaStream_t*)&b->capture_stream, cudaStreamNonBlocking));
-        const cudaStream_t cs = (cudaStream_t)b->capture_stream;
-        cudaGraph_t top = nullptr;
-        LGB_CUDA_TRY(ctx, cudaGraphCreate(&top, 0));
-        cudaGraphConditionalHandle cond;
-        cudaError_t e = cudaGraphConditionalHandleCreate(&cond, top, 1u, cudaGraphCondAssignDefault);
-        cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};  // the remaining fields zero
-        np.conditional.handle = cond;
-        np.conditional.type = cudaGraphCondTypeWhile;
-        np.conditional.size = 1;
-        cudaGraphNode_t loop_node = nullptr;
-        if (e == cudaSuccess) e = cudaGraphAddNode(&loop_node, top, nullptr, nullptr, 0, &np);
-        if (e != cudaSuccess) { cudaGraphDestroy(top); return cuda_error(ctx, e, "building the batch's chunk loop"); }
-        cudaGraph_t body = np.conditional.phGraph_out[0];
-        e = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
-        if (e != cudaSuccess) { cudaGraphDestroy(top); return cuda_error(ctx, e, "cudaStreamBeginCaptureToGraph"); }
-        k_next_chunk<<<1, 256, 0, cs>>>(reinterpret_cast<const BatchChunk*>(b->d_chunks), b->d_loop,
-                                        const_cast<BatchChunk*>(B.chunk));
-        cudaError_t le = launch_chunk<true>(F, B, bounces, g, batch_classes(b), cs);
-        k_loop_next<<<1, 32, 0, cs>>>(cond, b->d_loop);
-        if (le == cudaSuccess) le = cudaGetLastError();
-        cudaGraph_t captured = nullptr;
-        const cudaError_t ce = cudaStreamEndCapture(cs, &captured);
-        if (le != cudaSuccess || ce != cudaSuccess) {
-            cudaGraphDestroy(top);
-            return cuda_error(ctx, le != cudaSuccess ? le : ce, "capturing the batch bounce loop");
-        }
         cudaGraphExec_t exec = nullptr;
-        const cudaError_t ie = cudaGraphInstantiate(&exec, top, 0);
-        cudaGraphDestroy(top);
-        if (ie != cudaSuccess) return cuda_error(ctx, ie, "cudaGraphInstantiate");
+        cudaError_t e = build_batch_graph(b, F, B, bounces, g, batch_classes(b), (cudaStream_t)b->capture_stream, &exec);
+        if (e != cudaSuccess && regen) {
+            // A device or driver without nested conditional loops: render this and later calls without
+            // regeneration (the chunks are re-planned to fit the arena).
+            cudaGetLastError();
+            b->regen_refused = true;
+            return batch_render(b, jobs, n, o, write_film, st);
+        }
+        if (e != cudaSuccess) return cuda_error(ctx, e, "building the batch render graph");
         b->graph = exec;
         std::memcpy(b->graph_key, key, sizeof(key));
     }
@@ -1176,11 +1355,9 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
     return LGB_OK;
 }
 
-// Times every candidate (queue size x shading grid, stack in local memory) on a quarter of each job's frames,
-// films untouched, then the best of them with the stack bottom in shared memory; the first run of a candidate
-// records its graph, the second is timed.
 // ---- the tuning cache (lgb_create's tuning_cache_path) ----
-// One line per choice: "<key> <path_capacity> <work_blocks_per_sm> <trace_blocks_per_sm> <stack_placement>". The
+// One line per choice: "<key> <path_capacity> <work_blocks_per_sm> <trace_blocks_per_sm> <stack_placement>
+// <chunk_paths>". The
 // key names the device (name, SM count, compute capability), the ABI version and the batch's shape: job count,
 // and the powers of two of its samples, of its largest image and of its triangles, its deepest path and the union
 // of its scenes' BSDF types. A later line replaces an earlier one with the same key.
@@ -1220,8 +1397,11 @@ std::map<std::string, lgb_batch_opts> read_tune_cache(const std::string& path) {
         std::istringstream ls(line);
         std::string key;
         lgb_batch_opts o{};
-        if (ls >> key >> o.path_capacity >> o.work_blocks_per_sm >> o.trace_blocks_per_sm >> o.stack_placement)
+        if (ls >> key >> o.path_capacity >> o.work_blocks_per_sm >> o.trace_blocks_per_sm >> o.stack_placement) {
+            uint32_t chunk = 0;
+            if (ls >> chunk) o.chunk_paths = chunk;  // absent in lines written before path regeneration
             m[key] = o;
+        }
     }
     return m;
 }
@@ -1237,12 +1417,15 @@ void write_tune_cache(const std::string& path, const std::string& key, const lgb
         if (!f) return;
         for (const auto& e : m)
             f << e.first << ' ' << e.second.path_capacity << ' ' << e.second.work_blocks_per_sm << ' '
-              << e.second.trace_blocks_per_sm << ' ' << e.second.stack_placement << '\n';
+              << e.second.trace_blocks_per_sm << ' ' << e.second.stack_placement << ' ' << e.second.chunk_paths << '\n';
         if (!f) { std::remove(tmp.c_str()); return; }
     }
     if (std::rename(tmp.c_str(), path.c_str()) != 0) std::remove(tmp.c_str());
 }
 
+// Times every candidate (queue size x shading grid, stack in local memory, path regeneration) on a quarter of each
+// job's frames, films untouched, then the best of them with the stack bottom in shared memory, then the best
+// without path regeneration; the first run of a candidate records its graph, the second is timed.
 lgb_status batch_tune(Batch* b, const lgb_batch_job* jobs, uint32_t n, lgb_batch_opts* best, cudaStream_t st) {
     Ctx* ctx = b->ctx;
     std::string key;
@@ -1299,6 +1482,11 @@ lgb_status batch_tune(Batch* b, const lgb_batch_job* jobs, uint32_t n, lgb_batch
     if (result == LGB_OK && have) {
         lgb_batch_opts o = best_o;
         o.stack_placement = LGB_STACK_SHARED;
+        trial(o);
+    }
+    if (result == LGB_OK && have && !b->regen_refused) {  // the best so far without path regeneration
+        lgb_batch_opts o = best_o;
+        o.chunk_paths = 1u;
         trial(o);
     }
     cudaEventDestroy(e0);

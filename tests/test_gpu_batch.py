@@ -94,18 +94,23 @@ def _start_films(scenes):
     return [pre.get(k) for k in range(len(JOBS))]
 
 
-@pytest.mark.parametrize("capacity,stack", [(0, 0), (4096, 0), (6000, 0), (0, 1), (6000, 1)])
-def test_batched_films_equal_films_rendered_alone(ctx, scenes, capacity, stack):
+# chunk_paths: 0 = path regeneration with the default chunk (16 x the capacity: here one chunk whose ~60k paths
+# run through 4096 or 6000 slots), 1 = no regeneration (chunks of at most the capacity), 20000 = regeneration over
+# several chunks, each ending with its films before the next starts.
+@pytest.mark.parametrize("capacity,stack,chunk", [(0, 0, 0), (4096, 0, 0), (6000, 0, 0), (0, 1, 0), (6000, 1, 0),
+                                                  (4096, 0, 1), (6000, 0, 1), (4096, 0, 20000), (6000, 1, 20000)])
+def test_batched_films_equal_films_rendered_alone(ctx, scenes, capacity, stack, chunk):
     start = _start_films(scenes)
     want = _films(JOBS, start)
     _alone(scenes, JOBS, want)
     got = _films(JOBS, start)
     opts = None
-    if capacity or stack:
+    if capacity or stack or chunk:
         opts = abi.BatchOpts()
         opts.path_capacity = capacity  # below some images: raised to the largest image
         opts.work_blocks_per_sm = 4
         opts.stack_placement = stack  # the stack's bottom in shared memory gives the same hits
+        opts.chunk_paths = chunk
     _batched(ctx, scenes, JOBS, got, opts)
     for k in range(len(JOBS)):
         a, b = got[k].cpu().numpy(), want[k].cpu().numpy()

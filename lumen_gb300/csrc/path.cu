@@ -242,7 +242,20 @@ __global__ void __launch_bounds__(kThreads, kQueueTraceMinBlocks)
 }
 
 // path.rgen:49-55: a miss adds the sky colour (shade_atmosphere without a directional light returns
-// sky_col, commons.glsl:157-159) and ends the path; hits are binned by material class.
+// sky_col, commons.glsl:157-159) and ends the path.
+__device__ __forceinline__ void miss_sky(const Params& P, const Buffers& B, uint32_t p) {
+    const uint32_t depth = B.flags[p] & 0xffffu;
+    if (depth > 0 || P.direct_lighting == 1u) {
+        const float4 T = B.T[p];
+        float4 c = B.col[p];
+        c.x = c.x + T.x * P.sky[0];
+        c.y = c.y + T.y * P.sky[1];
+        c.z = c.z + T.z * P.sky[2];
+        B.col[p] = c;
+    }
+}
+
+// Misses end their paths (miss_sky); hits are binned by material class.
 template <bool BATCH>
 __global__ void __launch_bounds__(kThreads) k_classify(SceneView S0, const Params* __restrict__ Pp, Buffers B) {
     const uint32_t n = B.counters[0];
@@ -258,16 +271,7 @@ __global__ void __launch_bounds__(kThreads) k_classify(SceneView S0, const Param
             const uint32_t job = BATCH ? B.job[p] : 0u;
             if (prim == LGB_NO_HIT) {
                 ended = true;
-                const Params& P = BATCH ? B.jobs[job].P : *Pp;
-                const uint32_t depth = B.flags[p] & 0xffffu;
-                if (depth > 0 || P.direct_lighting == 1u) {
-                    const float4 T = B.T[p];
-                    float4 c = B.col[p];
-                    c.x = c.x + T.x * P.sky[0];
-                    c.y = c.y + T.y * P.sky[1];
-                    c.z = c.z + T.z * P.sky[2];
-                    B.col[p] = c;
-                }
+                miss_sky(BATCH ? B.jobs[job].P : *Pp, B, p);
             } else {
                 const SceneView S = BATCH ? B.jobs[job].S : S0;
                 cls = class_of(S.mats[S.meshes[S.tri_mesh[prim]].material_index].bsdf_type);
@@ -309,13 +313,14 @@ __device__ __forceinline__ v3 cls_eval(v3 n_s, v3 wo, const Mat& m, bool ff, v3 
     return eval_bsdf(n_s, wo, m, ff, wi, pdf);
 }
 
-// One bounce of path.rgen:56-100 for the hits of one material class.
+// One bounce of path.rgen:56-100 for the hits of one material class. SOLE (a scene whose materials all fall in
+// this class): the kernel takes the whole queue in place of k_classify, a miss ending its path as there.
 // Registers capped for 4 blocks per SM (128): the diffuse kernel reads and writes ~400 B of path state per path
 // and wants occupancy (Cornell / batch scene 550 / 354 Msamples/s against 549 / 349 uncapped at 140 registers).
 constexpr int kShadeMinBlocks = 4;
-template <int CLS, bool BATCH>
+template <int CLS, bool BATCH, bool SOLE = false>
 __global__ void __launch_bounds__(kThreads, kShadeMinBlocks) k_shade(SceneView S0, const Params* __restrict__ Pp, Buffers B, int bounce) {
-    const uint32_t n = B.counters[3 + CLS];
+    const uint32_t n = SOLE ? B.counters[0] : B.counters[3 + CLS];
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t* list = B.q_cls + (size_t)CLS * B.cap;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -325,166 +330,170 @@ __global__ void __launch_bounds__(kThreads, kShadeMinBlocks) k_shade(SceneView S
         lgb_ray next_ray, sray, mray;
         NeeRec rec;
         if (k < n) {
-            const uint32_t qi = list[k];
+            const uint32_t qi = SOLE ? k : list[k];
             p = B.q_cur[qi];
             const uint32_t job = BATCH ? B.job[p] : 0u;
             const Params& P = BATCH ? B.jobs[job].P : *Pp;
             const SceneView S = BATCH ? B.jobs[job].S : S0;
             if (BATCH) root = B.jobs[job].root;
             const lgb_hit hit = B.hits[qi];
-            const lgb_ray ray = B.rays[qi];
-            const uint32_t pix = B.pix[p], frame = B.frame[p];
-            uint4 seed = seed_of(pix, P.width, frame, B.w[p]);
-            const uint32_t fl = B.flags[p];
-            // batched, paths of different depths share a bounce (regeneration): each path's own depth
-            const int depth = BATCH ? (int)(fl & 0xffffu) : bounce;
-            const bool last_specular = (fl >> 16) & 1u;
-            v3 T = f3(B.T[p]);
-            v3 col = f3(B.col[p]);
-            const HitAttr h = resolve_hit(S, hit.prim, hit.u, hit.v);
-            const Mat m = load_material(S, h.mat, h.u, h.v);
-            if ((depth == 0 && P.direct_lighting == 1u) || last_specular) col = col + T * m.emissive;
-            if (depth < P.max_depth - 1) {
-                const v3 direction = V3(ray.dx, ray.dy, ray.dz);
-                const v3 wo = -direction;
-                v3 n_s = h.n_s;
-                bool side = true;
-                v3 n_g = h.n_g;
-                if (dot(h.n_g, wo) < 0.0f) n_g = -n_g;
-                if (dot(n_g, h.n_s) < 0.0f) { n_s = -n_s; side = false; }
-                const v3 origin = offset_ray(h.pos, n_g);
-                const bool spec = has_prop(m.props, LGB_FLAG_SPECULAR);
-                if (!spec && (depth > 0 || P.direct_lighting == 1u) && P.num_lights <= 0) {
-                    // No light to sample: Lumen would read past its light buffer; here the four draws are
-                    // consumed and nothing is added.
-                    for (int k = 0; k < 4; k++) (void)rnd(seed);
-                } else if (!spec && (depth > 0 || P.direct_lighting == 1u)) {
-                    // uniform_sample_light (pt_commons.glsl:3-42) and sample_light_Li (commons.glsl:224-300)
-                    nee = true;
-                    const float lpp = 1.0f / (float)P.light_tri_count;
-                    const float q0 = rnd(seed), q1 = rnd(seed), q2 = rnd(seed), q3 = rnd(seed);
-                    const uint32_t li = (uint32_t)(q0 * (float)P.num_lights);
-                    const lgb_light* L = &S.lights[li];
-                    const uint32_t lflags = L->light_flags, ltype = lflags & 7u;
-                    v3 Le = V3(0.0f), wi = V3(0.0f);
-                    float wi_len = 0.0f, pdf_w = 0.0f, pdf_a = 0.0f;
-                    uint32_t lprim = LGB_NO_HIT, lio = 0u, lvo = 0u;
-                    if (ltype == LGB_LIGHT_AREA) {
-                        const lgb_mesh pm = S.meshes[L->prim_mesh_idx];
-                        const uint32_t tri = (uint32_t)(q1 * (float)L->num_triangles);
-                        lprim = S.mesh_first[L->prim_mesh_idx] + tri;
-                        const uint32_t io = pm.index_offset + 3u * tri;
-                        lio = io;
-                        lvo = pm.vertex_offset;
-                        const DevVertex a = S.verts[S.idx[io] + pm.vertex_offset];
-                        const DevVertex b = S.verts[S.idx[io + 1] + pm.vertex_offset];
-                        const DevVertex c = S.verts[S.idx[io + 2] + pm.vertex_offset];
-                        const float su = 1.0f - sqrtf(q2), sv = q3 * sqrtf(q2);
-                        const float b0 = 1.0f - su - sv;
-                        const v3 v0 = V3(a.px, a.py, a.pz), v1 = V3(b.px, b.py, b.pz), v2 = V3(c.px, c.py, c.pz);
-                        const v3 et0 = v1 - v0, et1 = v2 - v0;
-                        const v3 lpos = v0 * b0 + v1 * su + v2 * sv;
-                        const v3 ln = normalize(normalize(V3(a.nx, a.ny, a.nz) * b0 + V3(b.nx, b.ny, b.nz) * su +
-                                                          V3(c.nx, c.ny, c.nz) * sv));
-                        const float tri_pdf = 2.0f / length(cross(et0, et1));
-                        const lgb_material* lm = &S.mats[pm.material_index];
-                        Le = V3(lm->emissive_factor[0], lm->emissive_factor[1], lm->emissive_factor[2]);
-                        wi = lpos - h.pos;
-                        const float l2 = dot(wi, wi);
-                        wi_len = sqrtf(l2);
-                        wi = wi / wi_len;
-                        const float cfl = fabsf(dot(ln, -wi));
-                        pdf_a = tri_pdf;
-                        pdf_w = pdf_a * l2 / cfl;
-                    } else if (ltype == LGB_LIGHT_SPOT) {
-                        const v3 lp = V3(L->pos[0], L->pos[1], L->pos[2]);
-                        wi = lp - h.pos;
-                        const float l2 = dot(wi, wi);
-                        wi_len = sqrtf(l2);
-                        wi = wi / wi_len;
-                        const v3 ldir = normalize(V3(L->to[0], L->to[1], L->to[2]) - lp);
-                        const float cfl = dot(-wi, ldir);
-                        const float cw = cosf(LGB_PI / 6.0f), cf = cosf(25.0f * LGB_PI / 180.0f);
-                        float fall;
-                        if (cfl < cw) fall = 0.0f;
-                        else if (cfl >= cf) fall = 1.0f;
-                        else { const float d = (cfl - cw) / (cf - cw); fall = (d * d) * (d * d); }
-                        pdf_a = 1.0f;
-                        pdf_w = l2;
-                        Le = V3(L->L[0], L->L[1], L->L[2]) * fall;
-                    } else {
-                        const v3 dir = normalize(V3(L->pos[0], L->pos[1], L->pos[2]) - V3(L->to[0], L->to[1], L->to[2]));
-                        const v3 lp = h.pos + dir * (2.0f * L->world_radius);
-                        wi = lp - h.pos;
-                        wi_len = length(wi);
-                        wi = wi / wi_len;
-                        pdf_a = 1.0f;
-                        pdf_w = 1.0f;
-                        Le = V3(L->L[0], L->L[1], L->L[2]);
+            if (SOLE && hit.prim == LGB_NO_HIT) {
+                miss_sky(P, B, p);
+            } else {
+                const lgb_ray ray = B.rays[qi];
+                const uint32_t pix = B.pix[p], frame = B.frame[p];
+                uint4 seed = seed_of(pix, P.width, frame, B.w[p]);
+                const uint32_t fl = B.flags[p];
+                // batched, paths of different depths share a bounce (regeneration): each path's own depth
+                const int depth = BATCH ? (int)(fl & 0xffffu) : bounce;
+                const bool last_specular = (fl >> 16) & 1u;
+                v3 T = f3(B.T[p]);
+                v3 col = f3(B.col[p]);
+                const HitAttr h = resolve_hit(S, hit.prim, hit.u, hit.v);
+                const Mat m = load_material(S, h.mat, h.u, h.v);
+                if ((depth == 0 && P.direct_lighting == 1u) || last_specular) col = col + T * m.emissive;
+                if (depth < P.max_depth - 1) {
+                    const v3 direction = V3(ray.dx, ray.dy, ray.dz);
+                    const v3 wo = -direction;
+                    v3 n_s = h.n_s;
+                    bool side = true;
+                    v3 n_g = h.n_g;
+                    if (dot(h.n_g, wo) < 0.0f) n_g = -n_g;
+                    if (dot(n_g, h.n_s) < 0.0f) { n_s = -n_s; side = false; }
+                    const v3 origin = offset_ray(h.pos, n_g);
+                    const bool spec = has_prop(m.props, LGB_FLAG_SPECULAR);
+                    if (!spec && (depth > 0 || P.direct_lighting == 1u) && P.num_lights <= 0) {
+                        // No light to sample: Lumen would read past its light buffer; here the four draws are
+                        // consumed and nothing is added.
+                        for (int k = 0; k < 4; k++) (void)rnd(seed);
+                    } else if (!spec && (depth > 0 || P.direct_lighting == 1u)) {
+                        // uniform_sample_light (pt_commons.glsl:3-42) and sample_light_Li (commons.glsl:224-300)
+                        nee = true;
+                        const float lpp = 1.0f / (float)P.light_tri_count;
+                        const float q0 = rnd(seed), q1 = rnd(seed), q2 = rnd(seed), q3 = rnd(seed);
+                        const uint32_t li = (uint32_t)(q0 * (float)P.num_lights);
+                        const lgb_light* L = &S.lights[li];
+                        const uint32_t lflags = L->light_flags, ltype = lflags & 7u;
+                        v3 Le = V3(0.0f), wi = V3(0.0f);
+                        float wi_len = 0.0f, pdf_w = 0.0f, pdf_a = 0.0f;
+                        uint32_t lprim = LGB_NO_HIT, lio = 0u, lvo = 0u;
+                        if (ltype == LGB_LIGHT_AREA) {
+                            const lgb_mesh pm = S.meshes[L->prim_mesh_idx];
+                            const uint32_t tri = (uint32_t)(q1 * (float)L->num_triangles);
+                            lprim = S.mesh_first[L->prim_mesh_idx] + tri;
+                            const uint32_t io = pm.index_offset + 3u * tri;
+                            lio = io;
+                            lvo = pm.vertex_offset;
+                            const DevVertex a = S.verts[S.idx[io] + pm.vertex_offset];
+                            const DevVertex b = S.verts[S.idx[io + 1] + pm.vertex_offset];
+                            const DevVertex c = S.verts[S.idx[io + 2] + pm.vertex_offset];
+                            const float su = 1.0f - sqrtf(q2), sv = q3 * sqrtf(q2);
+                            const float b0 = 1.0f - su - sv;
+                            const v3 v0 = V3(a.px, a.py, a.pz), v1 = V3(b.px, b.py, b.pz), v2 = V3(c.px, c.py, c.pz);
+                            const v3 et0 = v1 - v0, et1 = v2 - v0;
+                            const v3 lpos = v0 * b0 + v1 * su + v2 * sv;
+                            const v3 ln = normalize(normalize(V3(a.nx, a.ny, a.nz) * b0 + V3(b.nx, b.ny, b.nz) * su +
+                                                              V3(c.nx, c.ny, c.nz) * sv));
+                            const float tri_pdf = 2.0f / length(cross(et0, et1));
+                            const lgb_material* lm = &S.mats[pm.material_index];
+                            Le = V3(lm->emissive_factor[0], lm->emissive_factor[1], lm->emissive_factor[2]);
+                            wi = lpos - h.pos;
+                            const float l2 = dot(wi, wi);
+                            wi_len = sqrtf(l2);
+                            wi = wi / wi_len;
+                            const float cfl = fabsf(dot(ln, -wi));
+                            pdf_a = tri_pdf;
+                            pdf_w = pdf_a * l2 / cfl;
+                        } else if (ltype == LGB_LIGHT_SPOT) {
+                            const v3 lp = V3(L->pos[0], L->pos[1], L->pos[2]);
+                            wi = lp - h.pos;
+                            const float l2 = dot(wi, wi);
+                            wi_len = sqrtf(l2);
+                            wi = wi / wi_len;
+                            const v3 ldir = normalize(V3(L->to[0], L->to[1], L->to[2]) - lp);
+                            const float cfl = dot(-wi, ldir);
+                            const float cw = cosf(LGB_PI / 6.0f), cf = cosf(25.0f * LGB_PI / 180.0f);
+                            float fall;
+                            if (cfl < cw) fall = 0.0f;
+                            else if (cfl >= cf) fall = 1.0f;
+                            else { const float d = (cfl - cw) / (cf - cw); fall = (d * d) * (d * d); }
+                            pdf_a = 1.0f;
+                            pdf_w = l2;
+                            Le = V3(L->L[0], L->L[1], L->L[2]) * fall;
+                        } else {
+                            const v3 dir = normalize(V3(L->pos[0], L->pos[1], L->pos[2]) - V3(L->to[0], L->to[1], L->to[2]));
+                            const v3 lp = h.pos + dir * (2.0f * L->world_radius);
+                            wi = lp - h.pos;
+                            wi_len = length(wi);
+                            wi = wi / wi_len;
+                            pdf_a = 1.0f;
+                            pdf_w = 1.0f;
+                            Le = V3(L->L[0], L->L[1], L->L[2]);
+                        }
+                        const v3 sp = offset_ray2(h.pos, n_s);
+                        float bsdf_pdf;
+                        const float cos_x = dot(n_s, wi);
+                        const v3 f = cls_eval<CLS>(n_s, wo, m, side, wi, bsdf_pdf);
+                        v3 term1 = V3(0.0f);
+                        if (pdf_w > 0.0f) {
+                            const float mis = ((lflags >> 5) & 1u) ? 1.0f : 1.0f / (1.0f + bsdf_pdf / pdf_w);
+                            term1 = mis * f * fabsf(cos_x) * Le / pdf_w;
+                        }
+                        // The shadow ray only matters when the light sample can contribute.
+                        sray = make_ray(sp, 0.0f, wi, pdf_w > 0.0f ? wi_len - kEps : -1.0f);
+                        v3 f2 = V3(0.0f), wi2 = V3(0.0f);
+                        float pdf2 = 0.0f, cos2 = 0.0f;
+                        if (ltype == LGB_LIGHT_AREA) {
+                            const float b0r = rnd(seed), b1r = rnd(seed), b2r = rnd(seed);
+                            f2 = cls_sample<CLS>(n_s, wo, m, side, wi2, pdf2, cos2, V3(b0r, b1r, b2r));
+                        }
+                        mray = make_ray(sp, kTMin, wi2, pdf2 != 0.0f ? kTMax : -1.0f);
+                        // The MIS ray only counts when its closest hit is the sampled light triangle. Unless the
+                        // shading point is on that triangle (a miss then reuses the shading point's own payload), a
+                        // ray that fails the traversal's watertight test against it (same ray, same vertices) cannot
+                        // count: it gets an empty interval, which the trace kernel ends at once as a miss, and a miss
+                        // resolves to no contribution exactly as the traced ray would have.
+                        if (pdf2 != 0.0f && lprim != hit.prim) {
+                            const DevVertex a = S.verts[S.idx[lio] + lvo];
+                            const DevVertex b = S.verts[S.idx[lio + 1] + lvo];
+                            const DevVertex c = S.verts[S.idx[lio + 2] + lvo];
+                            const RayQ rq = make_rayq(mray.ox, mray.oy, mray.oz, mray.tmin, mray.dx, mray.dy, mray.dz,
+                                                      mray.tmax);
+                            float tt, tu, tv;
+                            if (!tri_intersect(rq, make_float4(a.px, a.py, a.pz, 0.0f), make_float4(b.px, b.py, b.pz, 0.0f),
+                                               make_float4(c.px, c.py, c.pz, 0.0f), rq.tmax, tt, tu, tv))
+                                mray.tmax = -1.0f;
+                        }
+                        const bool mis_term = ltype == LGB_LIGHT_AREA && pdf2 != 0.0f;
+                        rec.light = f4(T * term1 / lpp, __uint_as_float(p));
+                        rec.bsdf = mis_term ? f4(T * (f2 * fabsf(cos2) * Le / pdf2) / lpp, pdf_a / pdf2)
+                                            : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+                        rec.pos = f4(h.pos, __uint_as_float(hit.prim));
+                        rec.ns = f4(h.n_s, __uint_as_float(0xFFFFFFFFu));
+                        rec.wi2 = f4(wi2, __uint_as_float(lprim));
                     }
-                    const v3 sp = offset_ray2(h.pos, n_s);
-                    float bsdf_pdf;
-                    const float cos_x = dot(n_s, wi);
-                    const v3 f = cls_eval<CLS>(n_s, wo, m, side, wi, bsdf_pdf);
-                    v3 term1 = V3(0.0f);
-                    if (pdf_w > 0.0f) {
-                        const float mis = ((lflags >> 5) & 1u) ? 1.0f : 1.0f / (1.0f + bsdf_pdf / pdf_w);
-                        term1 = mis * f * fabsf(cos_x) * Le / pdf_w;
+                    float pdf, cos_t;
+                    v3 dir_next;
+                    const float c0 = rnd(seed), c1 = rnd(seed), c2 = rnd(seed);
+                    const v3 f = cls_sample<CLS>(n_s, wo, m, side, dir_next, pdf, cos_t, V3(c0, c1, c2));
+                    if (pdf != 0.0f) {
+                        T = T * (f * fabsf(cos_t) / pdf);
+                        float rr_scale = 1.0f;
+                        if (has_prop(m.props, LGB_FLAG_TRANSMISSION)) rr_scale *= side ? 1.0f / m.ior : m.ior;
+                        cont = true;
+                        if (depth > kRRMinDepth) {
+                            const float rr = fminf(0.95f, luminance(T) * rr_scale);
+                            if (rr == 0.0f || rr < rnd(seed)) cont = false;
+                            else T = T / rr;
+                        }
+                        next_ray = make_ray(origin, kTMin, dir_next, kTMax);
                     }
-                    // The shadow ray only matters when the light sample can contribute.
-                    sray = make_ray(sp, 0.0f, wi, pdf_w > 0.0f ? wi_len - kEps : -1.0f);
-                    v3 f2 = V3(0.0f), wi2 = V3(0.0f);
-                    float pdf2 = 0.0f, cos2 = 0.0f;
-                    if (ltype == LGB_LIGHT_AREA) {
-                        const float b0r = rnd(seed), b1r = rnd(seed), b2r = rnd(seed);
-                        f2 = cls_sample<CLS>(n_s, wo, m, side, wi2, pdf2, cos2, V3(b0r, b1r, b2r));
-                    }
-                    mray = make_ray(sp, kTMin, wi2, pdf2 != 0.0f ? kTMax : -1.0f);
-                    // The MIS ray only counts when its closest hit is the sampled light triangle. Unless the
-                    // shading point is on that triangle (a miss then reuses the shading point's own payload), a
-                    // ray that fails the traversal's watertight test against it (same ray, same vertices) cannot
-                    // count: it gets an empty interval, which the trace kernel ends at once as a miss, and a miss
-                    // resolves to no contribution exactly as the traced ray would have.
-                    if (pdf2 != 0.0f && lprim != hit.prim) {
-                        const DevVertex a = S.verts[S.idx[lio] + lvo];
-                        const DevVertex b = S.verts[S.idx[lio + 1] + lvo];
-                        const DevVertex c = S.verts[S.idx[lio + 2] + lvo];
-                        const RayQ rq = make_rayq(mray.ox, mray.oy, mray.oz, mray.tmin, mray.dx, mray.dy, mray.dz,
-                                                  mray.tmax);
-                        float tt, tu, tv;
-                        if (!tri_intersect(rq, make_float4(a.px, a.py, a.pz, 0.0f), make_float4(b.px, b.py, b.pz, 0.0f),
-                                           make_float4(c.px, c.py, c.pz, 0.0f), rq.tmax, tt, tu, tv))
-                            mray.tmax = -1.0f;
-                    }
-                    const bool mis_term = ltype == LGB_LIGHT_AREA && pdf2 != 0.0f;
-                    rec.light = f4(T * term1 / lpp, __uint_as_float(p));
-                    rec.bsdf = mis_term ? f4(T * (f2 * fabsf(cos2) * Le / pdf2) / lpp, pdf_a / pdf2)
-                                        : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
-                    rec.pos = f4(h.pos, __uint_as_float(hit.prim));
-                    rec.ns = f4(h.n_s, __uint_as_float(0xFFFFFFFFu));
-                    rec.wi2 = f4(wi2, __uint_as_float(lprim));
+                    B.flags[p] = (uint32_t)(depth + 1) | (spec ? (1u << 16) : 0u);
                 }
-                float pdf, cos_t;
-                v3 dir_next;
-                const float c0 = rnd(seed), c1 = rnd(seed), c2 = rnd(seed);
-                const v3 f = cls_sample<CLS>(n_s, wo, m, side, dir_next, pdf, cos_t, V3(c0, c1, c2));
-                if (pdf != 0.0f) {
-                    T = T * (f * fabsf(cos_t) / pdf);
-                    float rr_scale = 1.0f;
-                    if (has_prop(m.props, LGB_FLAG_TRANSMISSION)) rr_scale *= side ? 1.0f / m.ior : m.ior;
-                    cont = true;
-                    if (depth > kRRMinDepth) {
-                        const float rr = fminf(0.95f, luminance(T) * rr_scale);
-                        if (rr == 0.0f || rr < rnd(seed)) cont = false;
-                        else T = T / rr;
-                    }
-                    next_ray = make_ray(origin, kTMin, dir_next, kTMax);
-                }
-                B.flags[p] = (uint32_t)(depth + 1) | (spec ? (1u << 16) : 0u);
+                B.w[p] = seed.w;
+                B.T[p] = f4(T, 0.0f);
+                B.col[p] = f4(col, 0.0f);
             }
-            B.w[p] = seed.w;
-            B.T[p] = f4(T, 0.0f);
-            B.col[p] = f4(col, 0.0f);
         }
         const uint32_t cslot = agg_slot(&B.counters[1], cont);
         if (cont) {
@@ -735,11 +744,23 @@ void queue_traces(const SceneView& S, const Buffers& B, Grids g, cudaStream_t st
 template <bool BATCH>
 void launch_bounce(const SceneView& S, const Buffers& B, int depth, Grids g, uint32_t classes, cudaStream_t st) {
     queue_traces(S, B, g, st, true);
-    k_classify<BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B);
-    if (classes & (1u << CLS_DIFFUSE)) k_shade<CLS_DIFFUSE, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
-    if (classes & (1u << CLS_CONDUCTOR)) k_shade<CLS_CONDUCTOR, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
-    if (classes & (1u << CLS_SPECULAR)) k_shade<CLS_SPECULAR, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
-    if (classes & (1u << CLS_PRINCIPLED)) k_shade<CLS_PRINCIPLED, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+    bool sole = false;
+    if constexpr (!BATCH) {
+        // One shading class (the Cornell box: all diffuse): its kernel takes the queue without k_classify.
+        sole = true;
+        if (classes == (1u << CLS_DIFFUSE)) k_shade<CLS_DIFFUSE, false, true><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        else if (classes == (1u << CLS_CONDUCTOR)) k_shade<CLS_CONDUCTOR, false, true><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        else if (classes == (1u << CLS_SPECULAR)) k_shade<CLS_SPECULAR, false, true><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        else if (classes == (1u << CLS_PRINCIPLED)) k_shade<CLS_PRINCIPLED, false, true><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        else sole = false;
+    }
+    if (!sole) {
+        k_classify<BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B);
+        if (classes & (1u << CLS_DIFFUSE)) k_shade<CLS_DIFFUSE, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        if (classes & (1u << CLS_CONDUCTOR)) k_shade<CLS_CONDUCTOR, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        if (classes & (1u << CLS_SPECULAR)) k_shade<CLS_SPECULAR, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+        if (classes & (1u << CLS_PRINCIPLED)) k_shade<CLS_PRINCIPLED, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
+    }
     k_clear_bits<<<g.work, kThreads, 0, st>>>(B.sbits, B.counters + 2);
     queue_traces(S, B, g, st, false);
     k_nee_resolve<BATCH><<<g.work, kThreads, 0, st>>>(S, B);

@@ -238,6 +238,9 @@ __device__ __forceinline__ void trace_persistent(const WideNode* __restrict__ no
     const int lane = threadIdx.x & 31;
     const uint32_t lanemask_lt = (1u << lane) - 1u;
     if (count_ptr) n = *count_ptr;
+    // A warp whose first thread's index is at or past the ray count could take no ray in its first fetch: it leaves
+    // at once, so a short queue (a bounce's tail, the BSDF-MIS rays) costs its launch, not one atomic per warp.
+    if (blockIdx.x * blockDim.x + (threadIdx.x & ~31u) >= n) return;
     RayQ r;
     uint2 stack[kStackSize - SK];
     uint2* const my_stack = SK > 0 ? sstack + threadIdx.x : nullptr;

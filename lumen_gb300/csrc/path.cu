@@ -1468,7 +1468,7 @@ lgb_status batch_tune(Batch* b, const lgb_batch_job* jobs, uint32_t n, lgb_batch
         if (j.spp) j.spp = std::max(1u, (j.spp + 3u) / 4u);
         max_npix = std::max(max_npix, j.camera.width * j.camera.height);
     }
-    const uint32_t caps[] = {1u << 20, 1u << 21, 1u << 22};
+    const uint32_t caps[] = {1u << 20, 1u << 21, 1u << 22, 1u << 23};
     const uint32_t works[] = {4u, 8u, 16u};
     cudaEvent_t e0, e1;
     LGB_CUDA_TRY(ctx, cudaEventCreate(&e0));
@@ -1489,7 +1489,7 @@ lgb_status batch_tune(Batch* b, const lgb_batch_job* jobs, uint32_t n, lgb_batch
         if (result == LGB_OK && (!have || ms < best_ms)) { best_ms = ms; best_o = o; have = true; }
     };
     for (uint32_t c : caps) {
-        if (c < max_npix && c != caps[2]) continue;  // smaller than one frame: the larger candidates cover it
+        if (c < max_npix && c != caps[3]) continue;  // smaller than one frame: the larger candidates cover it
         for (uint32_t w : works) {
             lgb_batch_opts o{};
             o.path_capacity = c;

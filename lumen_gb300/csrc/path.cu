@@ -4,10 +4,11 @@
 // kernels over path state kept as structure-of-arrays in HBM:
 //   k_camera          path.rgen:28-46   one path per (pixel, frame), jittered camera ray
 //   k_q_trace_closest path.rgen:48      continuation rays of the live queue
-//   k_classify        path.rgen:49-55   misses add the sky and end; hits are binned by material class
+//   k_classify        path.rgen:49-55   misses add the sky and end; hits are binned by material class (a
+//                                       scene of one class skips it: its shading kernel takes the queue)
 //   k_shade<CLASS>    path.rgen:56-100  ray.rchit hit resolve, emission, NEE light sample + shadow ray,
 //                                       BSDF-MIS ray, BSDF sample, throughput, Russian roulette, enqueue
-//   k_q_trace_any / k_q_trace_closest   shadow and BSDF-MIS rays (pt_commons.glsl:21,32)
+//   k_q_trace_nee     pt_commons.glsl:21,32  BSDF-MIS rays (closest) and shadow rays (any) in one launch
 //   k_nee_resolve     pt_commons.glsl:20-41 combination of the two light-sampling strategies
 //   k_film            path.rgen:102-112 NaN drop and progressive mean, frames in order
 // Every kernel reads its work count from device memory, so one render issues no host synchronisation.
@@ -232,13 +233,21 @@ __global__ void __launch_bounds__(kThreads, kQueueTraceMinBlocks)
     trace_persistent<false, false, kQueuePostpone, SK, kThreads, kQueueRefill, kQueueTriMin>(
         S.nodes, S.tris, rays, hits, nullptr, 0u, count_ptr, ray_counter, S.status, nullptr, roots, s_stack);
 }
+// A bounce's two NEE queries in one launch: the queued BSDF-MIS rays (closest hit) first, then the shadow rays
+// (any hit). The MIS queue is short but its rays are long, so the warps that take them start at once and then
+// join the shadow rays, whose queue the other warps are already draining; as two launches, the MIS trace ran alone
+// at the end of every bounce, bound by the latency of its few rays (Cornell box: 17 us of each 180-330 us bounce).
 template <int SK>
 __global__ void __launch_bounds__(kThreads, kQueueTraceMinBlocks)
-    k_q_trace_any(SceneView S, const lgb_ray* __restrict__ rays, uint32_t* __restrict__ bits,
-                  const uint32_t* count_ptr, uint32_t* ray_counter, const uint32_t* __restrict__ roots) {
+    k_q_trace_nee(SceneView S, const lgb_ray* __restrict__ srays, uint32_t* __restrict__ sbits,
+                  const uint32_t* scount, uint32_t* sctr, const uint32_t* __restrict__ sroots,
+                  const lgb_ray* __restrict__ mrays, lgb_hit* __restrict__ mhits, const uint32_t* mcount,
+                  uint32_t* mctr, const uint32_t* __restrict__ mroots) {
     __shared__ uint2 s_stack[SK > 0 ? SK * kThreads : 1];
+    trace_persistent<false, false, kQueuePostpone, SK, kThreads, kQueueRefill, kQueueTriMin>(
+        S.nodes, S.tris, mrays, mhits, nullptr, 0u, mcount, mctr, S.status, nullptr, mroots, s_stack);
     trace_persistent<true, false, kQueuePostpone, SK, kThreads, kQueueRefill, kQueueTriMin>(
-        S.nodes, S.tris, rays, nullptr, bits, 0u, count_ptr, ray_counter, S.status, nullptr, roots, s_stack);
+        S.nodes, S.tris, srays, nullptr, sbits, 0u, scount, sctr, S.status, nullptr, sroots, s_stack);
 }
 
 // path.rgen:49-55: a miss adds the sky colour (shade_atmosphere without a directional light returns
@@ -317,7 +326,11 @@ __device__ __forceinline__ v3 cls_eval(v3 n_s, v3 wo, const Mat& m, bool ff, v3 
 // this class): the kernel takes the whole queue in place of k_classify, a miss ending its path as there.
 // Registers capped for 4 blocks per SM (128): the diffuse kernel reads and writes ~400 B of path state per path
 // and wants occupancy (Cornell / batch scene 550 / 354 Msamples/s against 549 / 349 uncapped at 140 registers).
+#ifdef LGB_SHADE_MIN_BLOCKS
+constexpr int kShadeMinBlocks = LGB_SHADE_MIN_BLOCKS;
+#else
 constexpr int kShadeMinBlocks = 4;
+#endif
 template <int CLS, bool BATCH, bool SOLE = false>
 __global__ void __launch_bounds__(kThreads, kShadeMinBlocks) k_shade(SceneView S0, const Params* __restrict__ Pp, Buffers B, int bounce) {
     const uint32_t n = SOLE ? B.counters[0] : B.counters[3 + CLS];
@@ -727,9 +740,8 @@ template <int SK> void launch_queue_traces(const SceneView& S, const Buffers& B,
     if (first) {
         k_q_trace_closest<SK><<<g.trace, kThreads, 0, st>>>(S, B.rays, B.hits, B.counters + 0, B.counters + 8, B.root);
     } else {
-        k_q_trace_any<SK><<<g.trace, kThreads, 0, st>>>(S, B.srays, B.sbits, B.counters + 2, B.counters + 9, B.nroot);
-        k_q_trace_closest<SK><<<g.trace, kThreads, 0, st>>>(S, B.mrays, B.mhits, B.counters + 11, B.counters + 10,
-                                                            B.mroot);
+        k_q_trace_nee<SK><<<g.trace, kThreads, 0, st>>>(S, B.srays, B.sbits, B.counters + 2, B.counters + 9, B.nroot,
+                                                        B.mrays, B.mhits, B.counters + 11, B.counters + 10, B.mroot);
     }
 }
 // first: the continuation rays' closest hits; else the shadow rays and the BSDF-MIS rays of the bounce.

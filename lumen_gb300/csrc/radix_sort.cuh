@@ -1,12 +1,17 @@
-// LSD radix sort of (32- or 64-bit key, 32-bit value) pairs, 8 bits per pass, stable: per-block digit histograms,
-// one exclusive scan over all (digit, block) counts, and a scatter that ranks equal digits within each warp
-// with __match_any_sync so that equal keys keep their input order. Shared by the BVH builder (Morton codes)
-// and the photon grid (hash slots). The scan runs in three steps over tiles of 4096 counts (tile sums, a scan of
-// the sums, each tile scanned in shared memory from its offset), all with coalesced loads and stores.
+// LSD radix sort of (32- or 64-bit key, 32-bit value) pairs, 8 bits per pass, stable, reduce-then-scan over a
+// persistent grid: each block owns one contiguous range of tiles for the whole pass. Per pass, a histogram kernel
+// counts each block's digits (one read of the keys), one exclusive scan over the (digit, block) counts gives every
+// block the output position of its first key of each digit, and the scatter kernel walks the block's tiles in
+// order, advancing its per-digit positions tile by tile in shared memory. Within a tile the keys are ranked per
+// warp with __match_any_sync, staged in digit order in shared memory and written out with consecutive threads on
+// consecutive keys, so each digit's run of the tile lands contiguously. Blocks never wait for one another, and
+// the count array has 256 entries per block of the grid rather than per tile. Shared by the BVH builder (Morton
+// codes) and the photon tables (hash slots).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <utility>
 
 namespace lgb {
@@ -15,29 +20,45 @@ namespace {
 constexpr int RS_THREADS = 256;
 constexpr int RS_ITEMS = 8;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
+constexpr int RS_MAX_BLOCKS = 1024;  // blocks of the persistent grid: a bound on the (digit, block) counts
 constexpr int SCAN_THREADS = 512;
 constexpr int SCAN_ITEMS = 8;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
-// Words of scratch radix_sort_pairs needs for n pairs: the (digit, block) counts and one sum per scan tile.
+inline uint32_t rs_tiles(uint32_t n) { return (n + RS_TILE - 1) / RS_TILE; }
+
+// Words of scratch radix_sort_pairs needs: the (digit, block) counts and one sum per scan tile.
 inline size_t radix_sort_scratch_words(uint32_t n) {
-    const size_t m = 256 * (size_t)((n + RS_TILE - 1) / RS_TILE);
+    (void)n;
+    const size_t m = 256 * (size_t)RS_MAX_BLOCKS;
     return m + (m + SCAN_TILE - 1) / SCAN_TILE;
 }
 
+// Tiles [t0, t1) of block b of a grid of g blocks over `tiles` tiles.
+__device__ __forceinline__ void rs_range(uint32_t tiles, uint32_t b, uint32_t g, uint32_t& t0, uint32_t& t1) {
+    t0 = (uint32_t)((uint64_t)tiles * b / g);
+    t1 = (uint32_t)((uint64_t)tiles * (b + 1) / g);
+}
+
+// Digit counts of each block's range: one shared-memory histogram per warp (fewer collisions on skewed keys, such
+// as the hash slots of clustered photons), summed into counts[digit * gridDim.x + block].
 template <class KeyT>
 __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const KeyT* __restrict__ keys, uint32_t n, int shift,
-                                                        uint32_t* counts, uint32_t nblocks) {
-    __shared__ uint32_t h[256];
-    h[threadIdx.x] = 0;
+                                                        uint32_t tiles, uint32_t* __restrict__ counts) {
+    __shared__ uint32_t h[RS_THREADS / 32][256];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int w = 0; w < RS_THREADS / 32; w++) h[w][tid] = 0;
     __syncthreads();
-    size_t base = (size_t)blockIdx.x * RS_TILE;
-    for (int k = 0; k < RS_ITEMS; k++) {
-        size_t idx = base + (size_t)k * RS_THREADS + threadIdx.x;
-        if (idx < n) atomicAdd(&h[(uint32_t)(keys[idx] >> shift) & 0xffu], 1u);
-    }
+    uint32_t t0, t1;
+    rs_range(tiles, blockIdx.x, gridDim.x, t0, t1);
+    const size_t e = min((size_t)t1 * RS_TILE, (size_t)n);
+#pragma unroll 8
+    for (size_t i = (size_t)t0 * RS_TILE + tid; i < e; i += RS_THREADS)
+        atomicAdd(&h[warp][(uint32_t)(keys[i] >> shift) & 0xffu], 1u);
     __syncthreads();
-    counts[(size_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+    uint32_t c = 0;
+    for (int w = 0; w < RS_THREADS / 32; w++) c += h[w][tid];
+    counts[(size_t)tid * gridDim.x + blockIdx.x] = c;
 }
 
 // Exclusive scan of m counts in place, one block of 1024 threads.
@@ -47,7 +68,6 @@ __global__ void __launch_bounds__(1024) k_scan_single(uint32_t* data, uint32_t m
     const uint32_t b = threadIdx.x * per, e = min(m, b + per);
     uint32_t sum = 0;
     for (uint32_t i = b; i < e; i++) sum += data[i];
-    // block exclusive scan of sum
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t x = sum;
     for (int o = 1; o < 32; o <<= 1) {
@@ -154,46 +174,127 @@ inline void scan_exclusive(uint32_t* data, uint32_t m, cudaStream_t st) {
     k_scan_tile_apply<<<nt, SCAN_THREADS, 0, st>>>(data, m, sums);
 }
 
+// The scatter of each block's range of tiles (see the header comment). offsets: the scanned (digit, block) counts.
 template <class KeyT>
 __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const KeyT* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                            KeyT* __restrict__ kout, uint32_t* __restrict__ vout,
-                                                           uint32_t n, int shift, const uint32_t* __restrict__ offsets,
-                                                           uint32_t nblocks) {
-    __shared__ uint32_t base_off[256];
-    __shared__ uint32_t warp_cnt[RS_THREADS / 32][256];
+                                                           uint32_t n, int shift, uint32_t tiles,
+                                                           const uint32_t* __restrict__ offsets) {
+    constexpr int WARPS = RS_THREADS / 32;
+    __shared__ uint32_t out_off[256];     // output position of the next key of each digit
+    __shared__ uint32_t tile_start[256];  // position of each digit's first key in the sorted tile
+    __shared__ uint32_t wcnt[WARPS][256]; // per-warp digit counts, then each warp's first position within a digit
+    __shared__ KeyT skey[RS_TILE];
+    __shared__ uint32_t sval[RS_TILE];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    base_off[tid] = offsets[(size_t)tid * nblocks + blockIdx.x];
     const uint32_t lanemask_lt = (1u << lane) - 1u;
-    const size_t tile = (size_t)blockIdx.x * RS_TILE;
-    for (int r = 0; r < RS_ITEMS; r++) {
-        for (int w = 0; w < RS_THREADS / 32; w++) warp_cnt[w][tid] = 0;
+    out_off[tid] = offsets[(size_t)tid * gridDim.x + blockIdx.x];
+    uint32_t t0, t1;
+    rs_range(tiles, blockIdx.x, gridDim.x, t0, t1);
+    const uint32_t wbase = (uint32_t)warp * (RS_ITEMS * 32);  // each warp owns RS_TILE / 8 consecutive keys
+    // The pairs of the block's next tile are loaded into registers while the current one is ranked and written.
+    KeyT key[RS_ITEMS];
+    uint32_t val[RS_ITEMS];
+    auto load = [&](uint32_t t, KeyT* k, uint32_t* v) {
+        const size_t tile = (size_t)t * RS_TILE;
+        const uint32_t tn = (uint32_t)min((size_t)RS_TILE, (size_t)n - tile);
+#pragma unroll
+        for (int r = 0; r < RS_ITEMS; r++) {
+            const uint32_t i = wbase + (uint32_t)r * 32 + lane;
+            const bool valid = i < tn;
+            k[r] = valid ? kin[tile + i] : KeyT(0);
+            v[r] = valid ? vin[tile + i] : 0u;
+        }
+    };
+    if (t0 < t1) load(t0, key, val);
+    for (uint32_t t = t0; t < t1; t++) {
+        KeyT nkey[RS_ITEMS];
+        uint32_t nval[RS_ITEMS];
+        if (t + 1 < t1) load(t + 1, nkey, nval);
+        for (int w = 0; w < WARPS; w++) wcnt[w][tid] = 0;
         __syncthreads();
-        const size_t idx = tile + (size_t)r * RS_THREADS + tid;
-        const bool valid = idx < n;
-        KeyT key = valid ? kin[idx] : KeyT(0);
-        uint32_t val = valid ? vin[idx] : 0u;
-        uint32_t digit = valid ? ((uint32_t)(key >> shift) & 0xffu) : (256u + lane);
-        uint32_t peers = __match_any_sync(0xffffffffu, digit);
-        uint32_t rank = __popc(peers & lanemask_lt);
-        int leader = __ffs(peers) - 1;
-        if (valid && lane == leader) warp_cnt[warp][digit] = __popc(peers);
-        __syncthreads();
-        uint32_t running = 0;
-        for (int w = 0; w < RS_THREADS / 32; w++) {
-            uint32_t c = warp_cnt[w][tid];
-            warp_cnt[w][tid] = running;
-            running += c;
+        const size_t tile = (size_t)t * RS_TILE;
+        const uint32_t tile_n = (uint32_t)min((size_t)RS_TILE, (size_t)n - tile);
+        uint32_t slot[RS_ITEMS];
+        // ranks within the warp, round after round (input order)
+#pragma unroll
+        for (int r = 0; r < RS_ITEMS; r++) {
+            const uint32_t i = wbase + (uint32_t)r * 32 + lane;
+            const bool valid = i < tile_n;
+            const uint32_t digit = valid ? ((uint32_t)(key[r] >> shift) & 0xffu) : (256u + lane);
+            const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+            const uint32_t before = valid ? wcnt[warp][digit] : 0u;
+            slot[r] = before + __popc(peers & lanemask_lt);
+            __syncwarp();
+            if (valid && (__ffs(peers) - 1) == lane) wcnt[warp][digit] = before + __popc(peers);
+            __syncwarp();
         }
         __syncthreads();
-        if (valid) {
-            uint32_t pos = base_off[digit] + warp_cnt[warp][digit] + rank;
-            kout[pos] = key;
-            vout[pos] = val;
+        // digit tid: the warps' counts in warp order and the tile's count
+        uint32_t cnt = 0;
+        for (int w = 0; w < WARPS; w++) {
+            const uint32_t c = wcnt[w][tid];
+            wcnt[w][tid] = cnt;
+            cnt += c;
+        }
+        tile_start[tid] = cnt;
+        __syncthreads();
+        if (warp == 0) {  // the tile's digit starts: exclusive scan of the 256 counts, 8 per lane
+            uint32_t v[8], sum = 0;
+            for (int j = 0; j < 8; j++) { v[j] = tile_start[lane * 8 + j]; sum += v[j]; }
+            uint32_t x = sum;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            uint32_t e = x - sum;
+            for (int j = 0; j < 8; j++) { tile_start[lane * 8 + j] = e; e += v[j]; }
         }
         __syncthreads();
-        base_off[tid] += running;
+        // the tile in digit order in shared memory (stable: warp-major, as the input) ...
+#pragma unroll
+        for (int r = 0; r < RS_ITEMS; r++) {
+            const uint32_t i = wbase + (uint32_t)r * 32 + lane;
+            if (i < tile_n) {
+                const uint32_t digit = (uint32_t)(key[r] >> shift) & 0xffu;
+                const uint32_t pos = tile_start[digit] + wcnt[warp][digit] + slot[r];
+                skey[pos] = key[r];
+                sval[pos] = val[r];
+            }
+        }
         __syncthreads();
+        // ... and each digit's run of it to its place in the output
+        for (uint32_t i = tid; i < tile_n; i += RS_THREADS) {
+            const KeyT k = skey[i];
+            const uint32_t digit = (uint32_t)(k >> shift) & 0xffu;
+            const uint32_t pos = out_off[digit] + (i - tile_start[digit]);
+            kout[pos] = k;
+            vout[pos] = sval[i];
+        }
+        __syncthreads();
+        out_off[tid] += cnt;
+#pragma unroll
+        for (int r = 0; r < RS_ITEMS; r++) {
+            key[r] = nkey[r];
+            val[r] = nval[r];
+        }
     }
+}
+
+// Blocks of the persistent grid: as many as stay resident at once (at most RS_MAX_BLOCKS, at most one per tile).
+template <class KeyT>
+inline uint32_t rs_grid(uint32_t tiles) {
+    static int per_sm = 0;  // resident blocks of the scatter kernel per SM (the same on every device of a build)
+    if (per_sm <= 0) {
+        int v = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_rs_scatter<KeyT>, RS_THREADS, 0);
+        per_sm = std::max(v, 1);
+    }
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint32_t g = (uint32_t)std::max(sms, 1) * (uint32_t)per_sm;
+    return std::max(1u, std::min({g, tiles, (uint32_t)RS_MAX_BLOCKS}));
 }
 
 // Sorts n pairs by the low 8 * passes bits of the keys (KeyT uint32_t or uint64_t); counts must hold
@@ -203,12 +304,13 @@ template <class KeyT>
 inline cudaError_t radix_sort_pairs(KeyT*& k0, uint32_t*& v0, KeyT*& k1, uint32_t*& v1, uint32_t* counts,
                                     uint32_t n, int passes, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    const uint32_t nblocks = (n + RS_TILE - 1) / RS_TILE;
+    const uint32_t tiles = rs_tiles(n);
+    const uint32_t g = rs_grid<KeyT>(tiles);
     for (int pass = 0; pass < passes; pass++) {
         const int shift = pass * 8;
-        k_rs_hist<KeyT><<<nblocks, RS_THREADS, 0, st>>>(k0, n, shift, counts, nblocks);
-        scan_exclusive(counts, 256 * nblocks, st);
-        k_rs_scatter<KeyT><<<nblocks, RS_THREADS, 0, st>>>(k0, v0, k1, v1, n, shift, counts, nblocks);
+        k_rs_hist<KeyT><<<g, RS_THREADS, 0, st>>>(k0, n, shift, tiles, counts);
+        scan_exclusive(counts, 256 * g, st);
+        k_rs_scatter<KeyT><<<g, RS_THREADS, 0, st>>>(k0, v0, k1, v1, n, shift, tiles, counts);
         std::swap(k0, k1);
         std::swap(v0, v1);
     }

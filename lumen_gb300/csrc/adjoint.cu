@@ -720,11 +720,16 @@ __global__ void __launch_bounds__(kDiffThreads, kDiffTraceMinBlocks)
     trace_persistent<false, false, kDiffPostpone, 0, kDiffThreads, kDiffRefill, kDiffTriMin>(S.nodes, S.tris, rays, hits, nullptr, 0u, count,
                                                                       fetch, S.status, nullptr, nullptr, nullptr);
 }
+// A bounce's BSDF-MIS rays (closest hit) and shadow rays (any hit) in one launch, the MIS rays first: warps move on
+// to the shadow rays as the MIS queue runs dry, so neither trace ends the bounce alone on its last few rays.
 __global__ void __launch_bounds__(kDiffThreads, kDiffTraceMinBlocks)
-    k_diff_trace_any(SceneView S, const lgb_ray* __restrict__ rays, uint32_t* __restrict__ bits, const uint32_t* count,
-                     uint32_t* fetch) {
-    trace_persistent<true, false, kDiffPostpone, 0, kDiffThreads, kDiffRefill, kDiffTriMin>(S.nodes, S.tris, rays, nullptr, bits, 0u, count,
-                                                                     fetch, S.status, nullptr, nullptr, nullptr);
+    k_diff_trace_nee(SceneView S, const lgb_ray* __restrict__ mrays, lgb_hit* __restrict__ mhits,
+                     const lgb_ray* __restrict__ srays, uint32_t* __restrict__ sbits, const uint32_t* count,
+                     uint32_t* mfetch, uint32_t* sfetch) {
+    trace_persistent<false, false, kDiffPostpone, 0, kDiffThreads, kDiffRefill, kDiffTriMin>(S.nodes, S.tris, mrays, mhits, nullptr, 0u, count,
+                                                                      mfetch, S.status, nullptr, nullptr, nullptr);
+    trace_persistent<true, false, kDiffPostpone, 0, kDiffThreads, kDiffRefill, kDiffTriMin>(S.nodes, S.tris, srays, nullptr, sbits, 0u, count,
+                                                                     sfetch, S.status, nullptr, nullptr, nullptr);
 }
 
 // The camera rays of every sample into queue 0; the replay skips the samples the loop form skips (zero d loss /
@@ -905,8 +910,8 @@ cudaError_t diff_wave_passes(Scene* s, const DiffArgs& A, const DiffWave& W, int
         k_diff_wave<MODE, MASK, kPhaseRays><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, -1, miss_cls);
         const cudaError_t me = cudaMemsetAsync(W.sbits, 0, 4ull * ((W.n + 31) / 32), cs);
         if (me != cudaSuccess) return me;
-        k_diff_trace_any<<<trace_grid, kDiffThreads, 0, cs>>>(S, W.srays, W.sbits, W.counts + d, f + 1);
-        k_diff_trace<<<trace_grid, kDiffThreads, 0, cs>>>(S, W.mrays, W.mhits, W.counts + d, f + 2);
+        k_diff_trace_nee<<<trace_grid, kDiffThreads, 0, cs>>>(S, W.mrays, W.mhits, W.srays, W.sbits, W.counts + d, f + 2,
+                                                              f + 1);
         if (has[0]) k_diff_wave<MODE, kDiffClsD, kPhaseResults><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, 0, miss_cls);
         if (has[1]) k_diff_wave<MODE, kDiffClsC, kPhaseResults><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, 1, miss_cls);
         if (has[2]) k_diff_wave<MODE, kDiffClsRest, kPhaseResults><<<grid, kDiffThreads, 0, cs>>>(S, A, W, d, 2, miss_cls);

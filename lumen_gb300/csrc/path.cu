@@ -534,6 +534,9 @@ __global__ void __launch_bounds__(kThreads, kShadeMinBlocks) k_shade(SceneView S
             B.nee[nslot] = rec;
             store_ray(&B.srays[nslot], sray);
             if (BATCH) B.nroot[nslot] = root;
+            // The shadow ray's occlusion word starts at zero: every record's writer clears its word (the lanes
+            // of a warp write the same one or two words), before the any-hit launch sets the bits.
+            B.sbits[nslot >> 5] = 0u;
         }
     }
 }
@@ -658,12 +661,6 @@ __global__ void __launch_bounds__(kThreads) k_film(const Params* __restrict__ Pp
     }
 }
 
-// Zeroes the occlusion words of this bounce's shadow queries (device-counted, so it can sit in a graph).
-__global__ void k_clear_bits(uint32_t* bits, const uint32_t* count_ptr) {
-    const uint32_t words = (*count_ptr + 31u) / 32u;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < words; i += gridDim.x * blockDim.x) bits[i] = 0u;
-}
-
 template <bool BATCH>
 __global__ void k_init_counters(Buffers B, const Params* __restrict__ Pp) {
     const uint32_t n = BATCH ? min(B.chunk->npaths, B.cap) : Pp->npix * Pp->nframes;
@@ -773,7 +770,6 @@ void launch_bounce(const SceneView& S, const Buffers& B, int depth, Grids g, uin
         if (classes & (1u << CLS_SPECULAR)) k_shade<CLS_SPECULAR, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
         if (classes & (1u << CLS_PRINCIPLED)) k_shade<CLS_PRINCIPLED, BATCH><<<g.work, kThreads, 0, st>>>(S, B.params, B, depth);
     }
-    k_clear_bits<<<g.work, kThreads, 0, st>>>(B.sbits, B.counters + 2);
     queue_traces(S, B, g, st, false);
     k_nee_resolve<BATCH><<<g.work, kThreads, 0, st>>>(S, B);
 }

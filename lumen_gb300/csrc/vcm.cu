@@ -372,11 +372,31 @@ struct EyeHit {
     float area;
 };
 
-// vcm_connect_light (vcm_commons.glsl:146-204)
+// Eye-pass connections with their visibility deferred: each candidate is a shadow ray and the radiance it adds
+// when not occluded. A vertex's candidates take consecutive slots of the shadow queue (the light connection
+// first, then one per light-subpath vertex in order); k_vcm_eye_resolve combines them once the any-hit launch has
+// traced them. An unused slot keeps an empty ray and the marker kNoCandidate.
+constexpr uint32_t kNoCandidate = 0xFFFFFFFFu;
+__device__ __forceinline__ void put_candidate(const Wave& W, uint32_t slot, v3 origin, v3 dir, float tmax, v3 c) {
+    float4* r = reinterpret_cast<float4*>(&W.srays[slot]);
+    r[0] = make_float4(origin.x, origin.y, origin.z, 0.0f);
+    r[1] = make_float4(dir.x, dir.y, dir.z, tmax);
+    W.spay[slot] = make_float4(c.x, c.y, c.z, 0.0f);
+    W.sbits[slot >> 5] = 0u;  // the lanes of a warp clear their words before the any-hit launch sets bits
+}
+__device__ __forceinline__ void put_empty(const Wave& W, uint32_t slot) {
+    float4* r = reinterpret_cast<float4*>(&W.srays[slot]);
+    r[0] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    r[1] = make_float4(0.0f, 0.0f, 1.0f, -1.0f);
+    W.spay[slot] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(kNoCandidate));
+    W.sbits[slot >> 5] = 0u;
+}
+
+// vcm_connect_light (vcm_commons.glsl:146-204), the visibility test deferred: the candidate goes to `slot`.
 template <uint32_t MASK>
-__device__ v3 connect_light(const SceneView& S, const VcmArgs& A, uint4& seed, const EyeHit& h, v3 n_s, v3 wo, const Mat& mat,
-                            bool side, float eta_vm, const VState& cs, float& pdf_rev) {
-    v3 res = V3(0.0f);
+__device__ void connect_light(const SceneView& S, const VcmArgs& A, const Wave& W, uint32_t slot, uint4& seed,
+                              const EyeHit& h, v3 n_s, v3 wo, const Mat& mat, bool side, float eta_vm, const VState& cs,
+                              float& pdf_rev) {
     const float q0 = rnd(seed), q1 = rnd(seed), q2 = rnd(seed), q3 = rnd(seed);
     const Incidence li = sample_light_Li_pos(S, lights_of(A), q0, q1, q2, q3, h.pos);
     const float cos_x = dot(li.wi, n_s);
@@ -384,27 +404,27 @@ __device__ v3 connect_light(const SceneView& S, const VcmArgs& A, uint4& seed, c
     float pdf_fwd;
     const v3 f = eval_bsdf_rev<MASK>(n_s, wo, mat, side, li.wi, pdf_fwd, pdf_rev, true);
     if (!is_zero3(f)) {
-        const RayQ q = make_rayq(origin.x, origin.y, origin.z, 0.0f, li.wi.x, li.wi.y, li.wi.z, li.wi_len - kEpsV);
-        if (!trace_any_single(S.nodes, S.tris, q, S.status)) {
-            if (light_delta(li.flags)) pdf_fwd = 0.0f;
-            const float ltc = (float)A.light_tri_count;
-            const float w_light = pdf_fwd / (li.pdf_pos_w / ltc);
-            const float w_cam = li.pdf_pos_dir_w * fabsf(cos_x) / (li.pdf_pos_w * li.cos_y) *
-                                (eta_vm + cs.d_vcm + cs.d_vc * pdf_rev);
-            const float mis = 1.0f / (1.0f + w_light + w_cam);
-            if (mis > 0.0f) res = mis * fabsf(cos_x) * f * cs.thr * li.L / (li.pdf_pos_w / ltc);
-        }
+        if (light_delta(li.flags)) pdf_fwd = 0.0f;
+        const float ltc = (float)A.light_tri_count;
+        const float w_light = pdf_fwd / (li.pdf_pos_w / ltc);
+        const float w_cam = li.pdf_pos_dir_w * fabsf(cos_x) / (li.pdf_pos_w * li.cos_y) *
+                            (eta_vm + cs.d_vcm + cs.d_vc * pdf_rev);
+        const float mis = 1.0f / (1.0f + w_light + w_cam);
+        const v3 c = mis > 0.0f ? mis * fabsf(cos_x) * f * cs.thr * li.L / (li.pdf_pos_w / ltc) : V3(0.0f);
+        put_candidate(W, slot, origin, li.wi, li.wi_len - kEpsV, c);
+    } else {
+        put_empty(W, slot);
     }
-    return res;
 }
 
-// vcm_connect_light_vertices (vcm_commons.glsl:206-251)
+// vcm_connect_light_vertices (vcm_commons.glsl:206-251), the visibility tests deferred: candidate i goes to slot
+// first + i (slots first .. first + len_path - 1, unused ones left empty).
 template <uint32_t MASK>
-__device__ v3 connect_light_vertices(const SceneView& S, const VcmArgs& A, const float4* lv, uint32_t len_path, int depth,
-                                     const EyeHit& h, v3 n_s, v3 wo, const Mat& mat, bool side, float eta_vm,
-                                     const VState& cs, float pdf_rev) {
-    v3 res = V3(0.0f);
-    for (uint32_t i = 0; i < len_path; i++) {
+__device__ void connect_light_vertices(const SceneView& S, const VcmArgs& A, const Wave& W, uint32_t first,
+                                       const float4* lv, uint32_t len_path, int depth, const EyeHit& h, v3 n_s, v3 wo,
+                                       const Mat& mat, bool side, float eta_vm, const VState& cs, float pdf_rev) {
+    uint32_t i = 0;
+    for (; i < len_path; i++) {
         const LVert v = load_lvert(lv + (size_t)i * kVertexF4);
         if (v.path_len + (uint32_t)depth - 1u >= (uint32_t)A.max_depth) break;
         v3 dir = v.pos - h.pos;
@@ -414,25 +434,21 @@ __device__ v3 connect_light_vertices(const SceneView& S, const VcmArgs& A, const
         const float cos_cam = dot(n_s, dir);
         const float cos_light = dot(v.n_s, -dir);
         const float G = cos_light * cos_cam / len_sqr;
-        if (!(G > 0.0f)) continue;
+        if (!(G > 0.0f)) { put_empty(W, first + i); continue; }
         float cam_pdf_fwd, unused, light_pdf_fwd, light_pdf_rev;
         const v3 f_cam = eval_bsdf_rev<MASK>(n_s, wo, mat, side, dir, cam_pdf_fwd, unused, false);
         const Mat lm = load_material(S, v.mat, v.u, v.v);
         const v3 f_light = eval_bsdf_rev<MASK>(v.n_s, v.wo, lm, v.side == 1u, -dir, light_pdf_fwd, light_pdf_rev, true);
-        if (is_zero3(f_light) || is_zero3(f_cam)) continue;
+        if (is_zero3(f_light) || is_zero3(f_cam)) { put_empty(W, first + i); continue; }
         cam_pdf_fwd *= fabsf(cos_light) / len_sqr;
         light_pdf_fwd *= fabsf(cos_cam) / len_sqr;
         const float w_light = cam_pdf_fwd * (eta_vm + v.d_vcm + light_pdf_rev * v.d_vc);
         const float w_camera = light_pdf_fwd * (eta_vm + cs.d_vcm + pdf_rev * cs.d_vc);
         const float mis = 1.0f / (1.0f + w_camera + w_light);
         const v3 origin = offset_ray2(h.pos, n_s);
-        const RayQ q = make_rayq(origin.x, origin.y, origin.z, 0.0f, dir.x, dir.y, dir.z, len - kEpsV);
-        if (!trace_any_single(S.nodes, S.tris, q, S.status)) {
-            const v3 c = mis * G * cs.thr * v.thr * f_cam * f_light;
-            res = A.accumulate ? res + c : c;
-        }
+        put_candidate(W, first + i, origin, dir, len - kEpsV, mis * G * cs.thr * v.thr * f_cam * f_light);
     }
-    return res;
+    for (; i < len_path; i++) put_empty(W, first + i);
 }
 
 // vcm_merge_light_vertices (vcm_commons.glsl:254-296) over the slot table (count, representative photon)
@@ -479,6 +495,10 @@ __device__ v3 merge(const VcmArgs& A, int depth, const EyeHit& h, v3 n_s, v3 wo,
 __global__ void __launch_bounds__(kVcmThreads) k_vcm_eye_init(VcmArgs A, Wave W) {
     const CamV cam = cam_setup(A);
     uint32_t* const qc = W.qcount + (A.max_depth + 1);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {  // the shadow queue, read by the light pass's splats, starts empty
+        W.scount[0] = 0u;
+        W.scount[1] = 0u;
+    }
     for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < A.screen; pix += gridDim.x * blockDim.x) {
         const uint32_t x = pix % A.W, y = pix / A.W;
         uint4 seed = make_uint4(x, y, A.eye_seed, 0u);
@@ -502,8 +522,26 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_eye_init(VcmArgs A, Wave W)
     }
 }
 
-// vcm_trace_eye, one bounce (depth) of the queued eye subpaths: emission, light connection, connections to the
-// light subpath's vertices, merging, the next direction; a subpath that ends writes its pixel (vcm_eye.rgen:80-97).
+// Slots of the shadow queue for each lane's count k, consecutive per lane: an exclusive scan over the warp and one
+// atomic per warp. Every lane of the warp calls it.
+__device__ __forceinline__ uint32_t warp_alloc(uint32_t* counter, uint32_t k) {
+    const int lane = (int)(threadIdx.x & 31u);
+    uint32_t x = k;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    uint32_t first = 0;
+    if (lane == 31 && x) first = atomicAdd(counter, x);
+    first = __shfl_sync(0xffffffffu, first, 31);
+    return first + x - k;
+}
+
+// vcm_trace_eye, one bounce (depth) of the queued eye subpaths: emission, the light connection and the connections
+// to the light subpath's vertices (queued as shadow-ray candidates), merging, the next direction. The radiance so
+// far goes to the path state with the candidates' slots; k_vcm_eye_resolve adds the visible candidates and writes
+// the pixel of a subpath that ends (vcm_eye.rgen:80-97).
 template <uint32_t MASK>
 __global__ void __launch_bounds__(kVcmThreads) k_vcm_eye_step(SceneView S, VcmArgs A, Wave W, int depth) {
     const Etas eta = etas(A);
@@ -512,11 +550,27 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_eye_step(SceneView S, VcmAr
     const int cur = (depth - 1) & 1;
     uint32_t* const qc = W.qcount + (A.max_depth + 1);
     const uint32_t n = qc[depth - 1];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t pix = W.qidx[cur][i];
-        const lgb_hit hit = W.hits[i];
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < n;
+        uint32_t pix = 0u, kl = 0u, kv = 0u;
+        lgb_hit hit{LGB_NO_HIT, 0.0f, 0.0f, 0.0f};
+        float4 s4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (valid) {
+            pix = W.qidx[cur][i];
+            hit = W.hits[i];
+            s4 = *sq(W.es, 4, A.screen, pix);
+            if (hit.prim != LGB_NO_HIT) {
+                // at most one light connection and max_depth - depth vertex connections: the i-th stored vertex of
+                // a light subpath has path_len >= i + 2, so connect_light_vertices stops before that many
+                kl = depth < A.max_depth ? 1u : 0u;
+                kv = min(__float_as_uint(s4.y), (uint32_t)(A.max_depth - depth));
+            }
+        }
+        const uint32_t first = warp_alloc(W.scount, kl + kv);
+        if (!valid) continue;
         const float4 s0 = *sq(W.es, 0, A.screen, pix), s1 = *sq(W.es, 1, A.screen, pix), s2 = *sq(W.es, 2, A.screen, pix),
-                     s3 = *sq(W.es, 3, A.screen, pix), s4 = *sq(W.es, 4, A.screen, pix);
+                     s3 = *sq(W.es, 3, A.screen, pix);
         VState cs;
         cs.pos = V3(s0.x, s0.y, s0.z); cs.d_vcm = s0.w;
         cs.wi = V3(s1.x, s1.y, s1.z); cs.d_vc = s1.w;
@@ -524,7 +578,7 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_eye_step(SceneView S, VcmAr
         v3 col = V3(s3.x, s3.y, s3.z);
         const uint32_t x = pix % A.W, y = pix / A.W;
         uint4 seed = make_uint4(x, y, A.eye_seed, __float_as_uint(s3.w));
-        const uint32_t lp = __float_as_uint(s4.x), lp_len = __float_as_uint(s4.y);
+        const uint32_t lp = __float_as_uint(s4.x);
         const float4* lv = A.verts + (size_t)lp * per * kVertexF4;
         bool done = true;
         if (hit.prim == LGB_NO_HIT) {
@@ -559,8 +613,15 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_eye_step(SceneView S, VcmAr
                 col = col + cs.thr * Le;
             }
             float pdf_rev = 0.0f;
-            if (!spec && depth < A.max_depth) col = col + connect_light<MASK>(S, A, seed, eh, n_s, wo, mat, side, eta.vm, cs, pdf_rev);
-            if (!spec) col = col + connect_light_vertices<MASK>(S, A, lv, lp_len, depth, eh, n_s, wo, mat, side, eta.vm, cs, pdf_rev);
+            if (kl) {
+                if (!spec) connect_light<MASK>(S, A, W, first, seed, eh, n_s, wo, mat, side, eta.vm, cs, pdf_rev);
+                else put_empty(W, first);
+            }
+            if (!spec) {
+                connect_light_vertices<MASK>(S, A, W, first + kl, lv, kv, depth, eh, n_s, wo, mat, side, eta.vm, cs, pdf_rev);
+            } else {
+                for (uint32_t j = 0; j < kv; j++) put_empty(W, first + kl + j);
+            }
             if (!spec && A.use_vm == 1) col = col + merge<MASK>(A, depth, eh, n_s, wo, mat, side, eta.vc, cs, norm);
             if (depth < A.max_depth) {
                 const float c0 = rnd(seed), c1 = rnd(seed), c2 = rnd(seed);
@@ -589,15 +650,53 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_eye_step(SceneView S, VcmAr
                 }
             }
         }
+        *sq(W.es, 3, A.screen, pix) = make_float4(col.x, col.y, col.z, __uint_as_float(seed.w));
+        *sq(W.es, 4, A.screen, pix) = make_float4(s4.x, s4.y, __uint_as_float(first),
+                                                  __uint_as_float(kv | (kl << 16) | (done ? 0x80000000u : 0u)));
         if (!done) {
             *sq(W.es, 0, A.screen, pix) = f4(cs.pos, cs.d_vcm);
             *sq(W.es, 1, A.screen, pix) = f4(cs.wi, cs.d_vc);
             *sq(W.es, 2, A.screen, pix) = f4(cs.thr, cs.d_vm);
-            *sq(W.es, 3, A.screen, pix) = make_float4(col.x, col.y, col.z, __uint_as_float(seed.w));
             push_ray(W, depth & 1, qc + depth, pix, cs.pos, kTMinV, cs.wi, kTMaxV);
+        }
+    }
+}
+
+// After the any-hit launch over a bounce's candidates: the light connection when visible, then the vertex
+// connections in order (vcm_commons.glsl:247: each visible one adds to the result, or, Lumen's default, replaces
+// it), added to the eye subpath's radiance; a subpath that ended this bounce writes its pixel (vcm_eye.rgen:80-97).
+// Block 0 also resets the shadow queue's counters for the next bounce (nothing here reads them).
+__global__ void __launch_bounds__(kVcmThreads) k_vcm_eye_resolve(VcmArgs A, Wave W, int depth) {
+    const int cur = (depth - 1) & 1;
+    const uint32_t n = (W.qcount + (A.max_depth + 1))[depth - 1];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        W.scount[0] = 0u;
+        W.scount[1] = 0u;
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t pix = W.qidx[cur][i];
+        const float4 s3 = *sq(W.es, 3, A.screen, pix), s4 = *sq(W.es, 4, A.screen, pix);
+        const uint32_t first = __float_as_uint(s4.z), kw = __float_as_uint(s4.w);
+        const uint32_t kl = (kw >> 16) & 1u, kv = kw & 0xffffu;
+        v3 col = V3(s3.x, s3.y, s3.z);
+        auto visible = [&](uint32_t slot, v3& c) {
+            const float4 pay = W.spay[slot];
+            if (__float_as_uint(pay.w) == kNoCandidate || ((W.sbits[slot >> 5] >> (slot & 31u)) & 1u)) return false;
+            c = V3(pay.x, pay.y, pay.z);
+            return true;
+        };
+        v3 c;
+        if (kl && visible(first, c)) col = col + c;
+        v3 res = V3(0.0f);
+        for (uint32_t j = 0; j < kv; j++)
+            if (visible(first + kl + j, c)) res = A.accumulate ? res + c : c;
+        col = col + res;
+        if (!(kw & 0x80000000u)) {
+            *sq(W.es, 3, A.screen, pix) = make_float4(col.x, col.y, col.z, s3.w);
             continue;
         }
         if (isnan(luminance(col))) continue;  // vcm_eye.rgen:80-83: no film write, the splat stays
+        const uint32_t x = pix % A.W, y = pix / A.W;
         const uint32_t sidx = x * A.H + y;
         col = col + V3(A.splat[3 * sidx], A.splat[3 * sidx + 1], A.splat[3 * sidx + 2]);
         A.splat[3 * sidx] = 0.0f;
@@ -841,6 +940,9 @@ LGB_API lgb_status lgb_vcm_iteration(lgb_scene* s, const lgb_camera* cam, const 
             if (lobes == kVcmLobesDG) k_vcm_eye_step<kVcmLobesDG><<<grid, kVcmThreads, 0, st>>>(S, A, W, d);
             else if (lobes == kVcmLobesDGC) k_vcm_eye_step<kVcmLobesDGC><<<grid, kVcmThreads, 0, st>>>(S, A, W, d);
             else k_vcm_eye_step<kAllBsdfs><<<grid, kVcmThreads, 0, st>>>(S, A, W, d);
+            // the bounce's connection candidates: one any-hit launch, then their sums into the subpaths
+            k_vcm_trace_any<<<trace_grid, kVcmThreads, 0, st>>>(S, W.srays, W.sbits, W.scount, W.scount + 1);
+            k_vcm_eye_resolve<<<grid, kVcmThreads, 0, st>>>(A, W, d);
         }
     };
     k_vcm_light_init<<<grid, kVcmThreads, 0, st>>>(S, A, W);

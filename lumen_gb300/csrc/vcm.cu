@@ -193,8 +193,8 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter) {
 __device__ __forceinline__ void push_ray(const Wave& W, int q, uint32_t* counter, uint32_t path, v3 o, float tmin, v3 d,
                                          float tmax) {
     const uint32_t j = warp_append(counter);
-    W.qidx[q][j] = path;
-    float4* r = reinterpret_cast<float4*>(&W.rays[q][j]);
+    (q ? W.qidx[1] : W.qidx[0])[j] = path;  // selects, not an indexed copy of the pointer arrays in local memory
+    float4* r = reinterpret_cast<float4*>(&(q ? W.rays[1] : W.rays[0])[j]);
     r[0] = make_float4(o.x, o.y, o.z, tmin);
     r[1] = make_float4(d.x, d.y, d.z, tmax);
 }
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_light_step(SceneView S, Vcm
     const int cur = (depth - 1) & 1;
     const uint32_t n = W.qcount[depth - 1];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t li = W.qidx[cur][i];
+        const uint32_t li = (cur ? W.qidx[1] : W.qidx[0])[i];
         const lgb_hit hit = W.hits[i];
         const float4 s0 = *sq(W.ls, 0, A.screen, li), s1 = *sq(W.ls, 1, A.screen, li), s2 = *sq(W.ls, 2, A.screen, li),
                      s3 = *sq(W.ls, 3, A.screen, li);
@@ -557,7 +557,7 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_eye_step(SceneView S, VcmAr
         lgb_hit hit{LGB_NO_HIT, 0.0f, 0.0f, 0.0f};
         float4 s4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (valid) {
-            pix = W.qidx[cur][i];
+            pix = (cur ? W.qidx[1] : W.qidx[0])[i];
             hit = W.hits[i];
             s4 = *sq(W.es, 4, A.screen, pix);
             if (hit.prim != LGB_NO_HIT) {
@@ -674,22 +674,20 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_eye_resolve(VcmArgs A, Wave
         W.scount[1] = 0u;
     }
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t pix = W.qidx[cur][i];
+        const uint32_t pix = (cur ? W.qidx[1] : W.qidx[0])[i];
         const float4 s3 = *sq(W.es, 3, A.screen, pix), s4 = *sq(W.es, 4, A.screen, pix);
         const uint32_t first = __float_as_uint(s4.z), kw = __float_as_uint(s4.w);
         const uint32_t kl = (kw >> 16) & 1u, kv = kw & 0xffffu;
         v3 col = V3(s3.x, s3.y, s3.z);
-        auto visible = [&](uint32_t slot, v3& c) {
-            const float4 pay = W.spay[slot];
-            if (__float_as_uint(pay.w) == kNoCandidate || ((W.sbits[slot >> 5] >> (slot & 31u)) & 1u)) return false;
-            c = V3(pay.x, pay.y, pay.z);
-            return true;
-        };
-        v3 c;
-        if (kl && visible(first, c)) col = col + c;
         v3 res = V3(0.0f);
-        for (uint32_t j = 0; j < kv; j++)
-            if (visible(first + kl + j, c)) res = A.accumulate ? res + c : c;
+        for (uint32_t j = 0; j < kl + kv; j++) {
+            const uint32_t slot = first + j;
+            const float4 pay = W.spay[slot];
+            if (__float_as_uint(pay.w) == kNoCandidate || ((W.sbits[slot >> 5] >> (slot & 31u)) & 1u)) continue;
+            const v3 c = V3(pay.x, pay.y, pay.z);
+            if (j < kl) col = col + c;  // the light connection
+            else res = A.accumulate ? res + c : c;
+        }
         col = col + res;
         if (!(kw & 0x80000000u)) {
             *sq(W.es, 3, A.screen, pix) = make_float4(col.x, col.y, col.z, s3.w);

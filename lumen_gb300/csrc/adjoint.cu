@@ -647,6 +647,9 @@ struct DiffWave {
     uint32_t n;        // samples: npix * spp, sample i = frame (i / npix), pixel (i % npix)
 };
 constexpr int kDiffCountWords = (kDiffMaxDepth + 1) + 3 * kDiffMaxDepth + 3 * kDiffMaxDepth;
+__device__ __forceinline__ uint32_t* cls_list(const DiffWave& W, int c) {
+    return c == 0 ? W.cls[0] : (c == 1 ? W.cls[1] : W.cls[2]);
+}
 __device__ __forceinline__ uint32_t* class_counts(const DiffWave& W, int depth) {
     return W.counts + (kDiffMaxDepth + 1) + 3 * kDiffMaxDepth + 3 * depth;
 }
@@ -696,8 +699,8 @@ __device__ __forceinline__ uint32_t diff_append_to(uint32_t* counters, int c) {
 }
 __device__ __forceinline__ void push_diff_ray(const DiffWave& W, int q, uint32_t* counter, uint32_t i, const DPath& P) {
     const uint32_t j = diff_append(counter);
-    W.qidx[q][j] = i;
-    float4* r = reinterpret_cast<float4*>(&W.rays[q][j]);
+    (q ? W.qidx[1] : W.qidx[0])[j] = i;  // selects: an indexed pointer array would be copied to local memory
+    float4* r = reinterpret_cast<float4*>(&(q ? W.rays[1] : W.rays[0])[j]);
     r[0] = make_float4(P.origin.x, P.origin.y, P.origin.z, kTMinD);
     r[1] = make_float4(P.dir.x, P.dir.y, P.dir.z, kTMaxD);
 }
@@ -772,9 +775,9 @@ __global__ void __launch_bounds__(kDiffThreads, kDiffMinBlocks)
     const int q = depth & 1;
     const float inv = 1.0f / (float)A.spp;
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const uint32_t j = PHASE == kPhaseResults ? W.cls[cls][t] : t;
+        const uint32_t j = PHASE == kPhaseResults ? cls_list(W, cls)[t] : t;
         const lgb_hit hh = W.hits[j];
-        const uint32_t i = W.qidx[q][j];
+        const uint32_t i = (q ? W.qidx[1] : W.qidx[0])[j];
         DPath P = load_dpath(W, A, i);
         const DiffHit ph{hh.prim, hh.t, hh.u, hh.v};
         v3 delta = V3(0.0f);
@@ -799,7 +802,7 @@ __global__ void __launch_bounds__(kDiffThreads, kDiffMinBlocks)
             mr[0] = io.mray[0]; mr[1] = io.mray[1];
             const uint32_t ty = hh.prim == LGB_NO_HIT ? 0u : S.mats[S.meshes[S.tri_mesh[hh.prim]].material_index].bsdf_type;
             const int c = (ty & LGB_BSDF_DIFFUSE) ? 0 : ((ty & LGB_BSDF_CONDUCTOR) ? 1 : ((ty & sh::kAllBsdfs) ? 2 : miss_cls));
-            W.cls[c][diff_append_to(class_counts(W, depth), c)] = j;
+            cls_list(W, c)[diff_append_to(class_counts(W, depth), c)] = j;
         } else if (r == kStepContinue) {
             store_dpath(W, i, P);
             push_diff_ray(W, q ^ 1, W.counts + depth + 1, i, P);

@@ -1008,7 +1008,11 @@ namespace {
 
 constexpr uint32_t kBatchDefaultCap = 1u << 21;
 constexpr uint32_t kBatchMaxCap = 1u << 24;
+#ifdef LGB_BATCH_CHUNK_PATHS
+constexpr uint64_t kBatchChunkPaths = LGB_BATCH_CHUNK_PATHS;
+#else
 constexpr uint64_t kBatchChunkPaths = 16;             // default regenerating chunk: 16 x the path capacity
+#endif
 constexpr uint64_t kBatchMaxChunkPaths = 1ull << 27;  // 2 GB of radiance output
 
 __global__ void k_relocate(const WideNode* __restrict__ src, uint32_t n, uint32_t node_off, uint32_t tri_off,

@@ -474,13 +474,14 @@ LGB_API void lgb_batch_destroy(lgb_batch* batch);
  * chunks of whole frames; a chunk holds frames of several jobs. With path regeneration (the default) a chunk
  * holds up to chunk_paths paths and runs through path_capacity slots: a slot whose path ended takes the chunk's
  * next path, and each job's film receives its frames in order once the chunk's last path has ended. Every path is
- * computed as lgb_render_path computes it, so films are bit-identical to rendering each job alone. On a stream
- * that the caller is capturing, the chunks are captured one after another without regeneration. */
+ * computed as lgb_render_path computes it, so films are bit-identical to rendering each job alone. A call is one
+ * launch of the batch's own CUDA graph; on a stream that the caller is capturing it returns LGB_ERR_UNSUPPORTED. */
 LGB_API lgb_status lgb_batch_render(lgb_batch* batch, const lgb_batch_job* jobs, uint32_t num_jobs,
                                     const lgb_batch_opts* opts, void* stream);
-/* Autotuner: times lgb_batch_render over candidate queue sizes, grids, stack placements and with or without path
- * regeneration on a reduced copy of `jobs` (a quarter of each job's frames, films untouched), keeps the fastest
- * for later renders and writes it to *best.
+/* Autotuner: screens lgb_batch_render over candidate queue sizes and grids on a reduced copy of `jobs` (a quarter
+ * of each job's frames), times the three fastest on `jobs` themselves, then the best of them with the other stack
+ * placement and without path regeneration (films untouched throughout), keeps the fastest for later renders and
+ * writes it to *best.
  * With a tuning cache (lgb_create) a batch of the same shape on the same kind of device takes the cached choice
  * without timing anything (best->from_cache = 1); a new choice is added to the cache. Waits for `stream`. */
 LGB_API lgb_status lgb_batch_tune(lgb_batch* batch, const lgb_batch_job* jobs, uint32_t num_jobs,

@@ -35,6 +35,7 @@ void free_scene(Scene* s) {
     cudaFree(s->d_vertices);
     cudaFree(s->d_indices);
     cudaFree(s->d_tri_mesh);
+    cudaFree(s->d_tri_class);
     cudaFree(s->d_meshes);
     cudaFree(s->d_mesh_first_tri);
     cudaFree(s->d_materials);
@@ -176,12 +177,14 @@ LGB_API lgb_status lgb_scene_create(lgb_ctx* ctx, const lgb_scene_desc* d, lgb_s
     }
     std::vector<float> tv(9 * (size_t)ntri);
     std::vector<uint32_t> tri_mesh(ntri);
+    std::vector<uint8_t> tri_class(ntri);
     float bmin[3] = {INFINITY, INFINITY, INFINITY}, bmax[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (uint32_t m = 0; m < d->num_meshes; m++) {
         const lgb_mesh& pm = d->meshes[m];
         for (uint32_t t = 0; t < pm.tri_count; t++) {
             uint32_t g = first_tri[m] + t;
             tri_mesh[g] = m;
+            tri_class[g] = (uint8_t)shade_class(d->materials[pm.material_index].bsdf_type);
             for (int k = 0; k < 3; k++) {
                 uint64_t v = (uint64_t)d->indices[pm.index_offset + 3 * t + k] + pm.vertex_offset;
                 if (v >= d->num_vertices)
@@ -233,6 +236,7 @@ LGB_API lgb_status lgb_scene_create(lgb_ctx* ctx, const lgb_scene_desc* d, lgb_s
     UP(&s->d_vertices, verts.data(), verts.size());
     UP(&s->d_indices, d->indices, d->num_indices);
     UP(&s->d_tri_mesh, tri_mesh.data(), tri_mesh.size());
+    UP(&s->d_tri_class, tri_class.data(), tri_class.size());
     UP(&s->d_meshes, d->meshes, d->num_meshes);
     UP(&s->d_mesh_first_tri, first_tri.data(), first_tri.size());
     UP(&s->d_materials, d->materials, d->num_materials);

@@ -101,6 +101,7 @@ struct Scene {
     DevVertex* d_vertices = nullptr;
     uint32_t* d_indices = nullptr;
     uint32_t* d_tri_mesh = nullptr;  // global triangle -> mesh
+    uint8_t* d_tri_class = nullptr;  // global triangle -> shading class of its material (shade_class)
     lgb_mesh* d_meshes = nullptr;
     uint32_t* d_mesh_first_tri = nullptr;
     lgb_material* d_materials = nullptr;

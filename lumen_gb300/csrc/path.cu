@@ -142,7 +142,6 @@ __device__ __forceinline__ uint32_t find_segment(const BatchChunk& C, uint32_t i
 }
 
 
-__device__ __forceinline__ int class_of(uint32_t bsdf_type) { return shade_class(bsdf_type); }
 
 
 // ---------------- kernels ----------------
@@ -283,7 +282,7 @@ __global__ void __launch_bounds__(kThreads) k_classify(SceneView S0, const Param
                 miss_sky(BATCH ? B.jobs[job].P : *Pp, B, p);
             } else {
                 const SceneView S = BATCH ? B.jobs[job].S : S0;
-                cls = class_of(S.mats[S.meshes[S.tri_mesh[prim]].material_index].bsdf_type);
+                cls = S.tri_class[prim];
             }
         }
 #pragma unroll
@@ -1032,10 +1031,6 @@ __global__ void k_relocate(const WideNode* __restrict__ src, uint32_t n, uint32_
     }
 }
 
-__global__ void k_set_chunk(BatchChunk C, BatchChunk* dst) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) *dst = C;
-}
-
 // The device-driven chunk loop of a batch render: the body of the graph's WHILE node starts by copying chunk
 // loop[0] of the uploaded records into the chunk record the kernels read, and ends by advancing loop[0] and
 // setting the loop condition to loop[0] < loop[1]. loop[0] grows by one per iteration and loop[1] is the
@@ -1267,6 +1262,12 @@ void plan_chunks(const lgb_batch_job* jobs, uint32_t n, uint32_t cap, bool write
 lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const lgb_batch_opts& o, bool write_film,
                         cudaStream_t st) {
     Ctx* ctx = b->ctx;
+    // A call is one launch of the batch's own graph, whose job table and chunk records are uploaded from pinned
+    // staging on the stream; inside a caller's capture those uploads would replay whatever the staging holds then.
+    cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+    LGB_CUDA_TRY(ctx, cudaStreamIsCapturing(st, &cap_status));
+    if (cap_status != cudaStreamCaptureStatusNone)
+        return set_error(ctx, LGB_ERR_UNSUPPORTED, "lgb_batch_render cannot be captured: each call is one launch of its own graph");
     uint32_t max_npix = 1;
     int bounces = 1;
     for (uint32_t j = 0; j < n; j++) {
@@ -1303,13 +1304,10 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
         stage[j].root = b->roots[jobs[j].scene];
     }
     LGB_CUDA_TRY(ctx, cudaMemcpyAsync(const_cast<JobRec*>(B.jobs), stage, sizeof(JobRec) * n, cudaMemcpyHostToDevice, st));
-    cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
-    LGB_CUDA_TRY(ctx, cudaStreamIsCapturing(st, &cap_status));
-    const bool use_graph = cap_status == cudaStreamCaptureStatusNone;
     // Path regeneration (in the call's own graph): chunks of up to chunk_paths paths run through the arena's `cap`
     // slots, each ended path's slot taking the chunk's next path, so the queues stay full until the chunk's last
     // paths; the radiance of every path goes to col_out for the film.
-    const bool regen = use_graph && !b->regen_refused && o.chunk_paths != 1u;
+    const bool regen = !b->regen_refused && o.chunk_paths != 1u;
     uint64_t chunk_limit = cap;
     if (regen) {
         const uint64_t want = o.chunk_paths > 1u ? o.chunk_paths : kBatchChunkPaths * (uint64_t)cap;
@@ -1332,7 +1330,7 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
         B.col_out = reinterpret_cast<float4*>(b->col_out);
         B.film_src = B.col_out;
     }
-    if (use_graph && nch > 0) {
+    if (nch > 0) {
         // The chunk records, staged in pinned memory (free once the previous call's uploads are done, which the
         // staging event waited for above) and uploaded on the stream for the graph's device-driven loop.
         if (nch > b->chunk_cap) {
@@ -1358,14 +1356,6 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
     F.tris = b->tris;
     F.status = b->d_status;
     if (nch == 0) return LGB_OK;
-    if (!use_graph) {  // the caller is capturing this stream: the chunks go into its capture one after another
-        for (const BatchChunk& C : chunks) {
-            k_set_chunk<<<1, 1, 0, st>>>(C, const_cast<BatchChunk*>(B.chunk));
-            LGB_CUDA_TRY(ctx, launch_chunk<true>(F, B, bounces, g, batch_classes(b), st));
-        }
-        LGB_CUDA_TRY(ctx, cudaGetLastError());
-        return LGB_OK;
-    }
     // One graph renders every chunk of the call (build_batch_graph). It depends on the arena, the forest, the
     // bounce count, the grids, the chunk-record array and the regeneration output, not on the jobs.
     const uint64_t key[10] = {(uint64_t)(uintptr_t)b->buf, cap,
@@ -1463,9 +1453,10 @@ void write_tune_cache(const std::string& path, const std::string& key, const lgb
     if (std::rename(tmp.c_str(), path.c_str()) != 0) std::remove(tmp.c_str());
 }
 
-// Times every candidate (queue size x shading grid, stack in local memory, path regeneration) on a quarter of each
-// job's frames, films untouched, then the best of them with the stack bottom in shared memory, then the best
-// without path regeneration; the first run of a candidate records its graph, the best of the next two counts.
+// Screens every candidate (queue size x shading grid, stack in local memory, path regeneration) on a quarter of
+// each job's frames, then times the three fastest on the full jobs, then the best of those with the stack bottom
+// in shared memory and without path regeneration; films untouched throughout. The first run of a candidate
+// records its graph, the second is timed.
 lgb_status batch_tune(Batch* b, const lgb_batch_job* jobs, uint32_t n, lgb_batch_opts* best, cudaStream_t st) {
     Ctx* ctx = b->ctx;
     std::string key;
@@ -1492,23 +1483,21 @@ lgb_status batch_tune(Batch* b, const lgb_batch_job* jobs, uint32_t n, lgb_batch
     cudaEvent_t e0, e1;
     LGB_CUDA_TRY(ctx, cudaEventCreate(&e0));
     LGB_CUDA_TRY(ctx, cudaEventCreate(&e1));
-    float best_ms = 0.0f;
-    lgb_batch_opts best_o{};
-    bool have = false;
     lgb_status result = LGB_OK;
-    auto trial = [&](const lgb_batch_opts& o) {
+    // One candidate on a job list: the first run records its graph, the second is timed.
+    auto trial = [&](const lgb_batch_opts& o, const lgb_batch_job* js) {
         float ms = 0.0f;
-        for (int rep = 0; rep < 3 && result == LGB_OK; rep++) {  // the first run records the graph; best of two
+        for (int rep = 0; rep < 2 && result == LGB_OK; rep++) {
             cudaEventRecord(e0, st);
-            result = batch_render(b, reduced.data(), n, o, false, st);
+            result = batch_render(b, js, n, o, false, st);
             cudaEventRecord(e1, st);
             if (result == LGB_OK && cudaEventSynchronize(e1) != cudaSuccess) result = cuda_error(ctx, cudaGetLastError(), "batch tuning");
-            float t = 0.0f;
-            if (result == LGB_OK) cudaEventElapsedTime(&t, e0, e1);
-            if (rep == 1 || (rep == 2 && t < ms)) ms = t;
+            if (result == LGB_OK) cudaEventElapsedTime(&ms, e0, e1);
         }
-        if (result == LGB_OK && (!have || ms < best_ms)) { best_ms = ms; best_o = o; have = true; }
+        return ms;
     };
+    // Screen: every queue size x shading grid on the reduced jobs.
+    std::vector<std::pair<float, lgb_batch_opts>> screened;
     for (uint32_t c : caps) {
         if (c < max_npix && c != caps[3]) continue;  // smaller than one frame: the larger candidates cover it
         for (uint32_t w : works) {
@@ -1516,20 +1505,34 @@ lgb_status batch_tune(Batch* b, const lgb_batch_job* jobs, uint32_t n, lgb_batch
             o.path_capacity = c;
             o.work_blocks_per_sm = w;
             o.stack_placement = LGB_STACK_LOCAL;
-            trial(o);
+            const float ms = trial(o, reduced.data());
             if (result != LGB_OK) break;
+            screened.push_back({ms, o});
         }
         if (result != LGB_OK) break;
     }
+    // Confirm on the full jobs: the three fastest of the screen (a quarter of the frames favours smaller queues
+    // than the whole batch does), then the best of them with the stack bottom in shared memory and without
+    // path regeneration.
+    float best_ms = 0.0f;
+    lgb_batch_opts best_o{};
+    bool have = false;
+    auto confirm = [&](const lgb_batch_opts& o) {
+        const float ms = trial(o, jobs);
+        if (result == LGB_OK && (!have || ms < best_ms)) { best_ms = ms; best_o = o; have = true; }
+    };
+    std::sort(screened.begin(), screened.end(),
+              [](const std::pair<float, lgb_batch_opts>& x, const std::pair<float, lgb_batch_opts>& y) { return x.first < y.first; });
+    for (size_t i = 0; i < screened.size() && i < 3 && result == LGB_OK; i++) confirm(screened[i].second);
     if (result == LGB_OK && have) {
         lgb_batch_opts o = best_o;
         o.stack_placement = LGB_STACK_SHARED;
-        trial(o);
+        confirm(o);
     }
-    if (result == LGB_OK && have && !b->regen_refused) {  // the best so far without path regeneration
+    if (result == LGB_OK && have && !b->regen_refused) {
         lgb_batch_opts o = best_o;
         o.chunk_paths = 1u;
-        trial(o);
+        confirm(o);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -15,6 +15,7 @@ struct SceneView {
     const DevVertex* verts;
     const uint32_t* idx;
     const uint32_t* tri_mesh;
+    const uint8_t* tri_class;  // shading class per triangle (shade_class of its material)
     const lgb_mesh* meshes;
     const uint32_t* mesh_first;
     const lgb_material* mats;
@@ -115,7 +116,7 @@ __device__ __forceinline__ Mat load_material(const SceneView& S, uint32_t idx, f
 inline SceneView scene_view(Scene* s) {
     SceneView S;
     S.nodes = s->bvh.nodes; S.tris = s->bvh.tris; S.verts = s->d_vertices; S.idx = s->d_indices;
-    S.tri_mesh = s->d_tri_mesh; S.meshes = s->d_meshes; S.mesh_first = s->d_mesh_first_tri; S.mats = s->d_materials;
+    S.tri_mesh = s->d_tri_mesh; S.tri_class = s->d_tri_class; S.meshes = s->d_meshes; S.mesh_first = s->d_mesh_first_tri; S.mats = s->d_materials;
     S.lights = s->d_lights; S.texs = s->d_textures; S.status = s->d_status;
     return S;
 }

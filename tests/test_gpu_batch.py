@@ -4,6 +4,7 @@ Every path of a batch is seeded and computed as lgb_render_path computes it, so 
 bit-identical to the film of the same job rendered alone, whatever the chunking (small path capacities force
 chunks that mix segments of several jobs and split jobs across chunks)."""
 import os
+import warnings
 
 import numpy as np
 import pytest
@@ -180,6 +181,32 @@ def test_batch_error_paths(ctx, scenes):
     batch.render([Batch.job(0, cam, path_params(arrays, DEPTH), 0, 2, film)])
     batch.sync()
     assert film[:, :3].mean().item() > 0.0
+
+
+def test_batch_render_refuses_a_capturing_stream(ctx, scenes):
+    """A render is one launch of the batch's own graph; inside a caller's stream capture it is refused (its job
+    table upload would replay later staging) and nothing is captured."""
+    arrays, sc = scenes[0]
+    batch = Batch(ctx, [sc])
+    film = torch.zeros((32 * 32, 4), dtype=torch.float32, device="cuda")
+    job = Batch.job(0, _camera(arrays, 32, 32), path_params(arrays, DEPTH), 0, 1, film)
+    side = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(side):
+        graph.capture_begin()
+        try:
+            with pytest.raises(abi.LgbError) as e:
+                batch.render([job], stream=side.cuda_stream)
+        finally:
+            with warnings.catch_warnings():  # the captured graph is empty, which torch reports
+                warnings.simplefilter("ignore")
+                graph.capture_end()
+    assert e.value.status == 6  # LGB_ERR_UNSUPPORTED
+    batch.render([job])  # the batch is still usable
+    batch.sync()
+    assert film[:, :3].mean().item() > 0.0
+    batch.close()
 
 
 def test_tuning_cache_persists_choices(tmp_path):

@@ -223,7 +223,11 @@ constexpr int kQueueTraceMinBlocks = 9;
 constexpr int kQueueSharedStack = 8;  // entries when the stack placement is LGB_STACK_SHARED
 // Idle lanes a warp waits for before fetching new rays. Cornell / batch scene, Msamples/s, with the MIS
 // pre-test of k_shade: refill at 8 idle lanes 542 / 356, at 16: 550 / 354, at 32: 566 / 329.
+#ifdef LGB_QUEUE_REFILL
+constexpr int kQueueRefill = LGB_QUEUE_REFILL;
+#else
 constexpr int kQueueRefill = 16;
+#endif
 template <int SK>
 __global__ void __launch_bounds__(kThreads, kQueueTraceMinBlocks)
     k_q_trace_closest(SceneView S, const lgb_ray* __restrict__ rays, lgb_hit* __restrict__ hits,

@@ -200,7 +200,12 @@ __device__ __forceinline__ void push_ray(const Wave& W, int q, uint32_t* counter
 }
 
 constexpr int kWaveTraceMinBlocks = 9;
-constexpr int kWaveRefill = 16;
+// Idle lanes a warp waits for before fetching new rays: caustics iteration 7.64 ms at 16, 7.48 at 8, 7.49 at 4.
+#ifdef LGB_WAVE_REFILL
+constexpr int kWaveRefill = LGB_WAVE_REFILL;
+#else
+constexpr int kWaveRefill = 8;
+#endif
 // Leaf triangles postponed one per loop iteration, with warp-uniform triangle and node iterations once a quarter
 // of the active lanes hold a pending triangle (trace_persistent's TRI_MIN): the caustics configuration's VCM
 // iteration 8.29 -> 8.01 ms on GB300 against a node's leaf triangles tested in the iteration that visits it.

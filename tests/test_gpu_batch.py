@@ -119,6 +119,31 @@ def test_batched_films_equal_films_rendered_alone(ctx, scenes, capacity, stack, 
         assert (a[:, 3] == 1.0).all() and a[:, :3].mean() > 0.0
 
 
+@pytest.mark.parametrize("chunk", [0, 1])
+def test_batched_jobs_of_different_depths(ctx, scenes, chunk):
+    """Jobs with path depths 1, 2, 5 and 12 in one batch: with regeneration the wavefront holds paths of every depth
+    at once (each path reads its own depth), and every film still equals the job rendered alone."""
+    depths = [1, 2, 5, 12]
+    jobs = [(0, 40, 32, 0, 3), (1, 48, 48, 0, 4), (2, 32, 40, 0, 5), (3, 56, 48, 0, 2)]
+    want = _films(jobs)
+    for k, (si, w, h, frame0, spp) in enumerate(jobs):
+        arrays, sc = scenes[si]
+        sc.render_path(_camera(arrays, w, h), path_params(arrays, depths[k]), frame0, spp, want[k])
+        sc.sync()
+    got = _films(jobs)
+    batch = Batch(ctx, [sc for _, sc in scenes])
+    js = [Batch.job(si, _camera(scenes[si][0], w, h), path_params(scenes[si][0], depths[k]), frame0, spp, got[k])
+          for k, (si, w, h, frame0, spp) in enumerate(jobs)]
+    opts = abi.BatchOpts()
+    opts.path_capacity = 4096  # raised to the largest image; the ~22k paths then regenerate through the slots
+    opts.chunk_paths = chunk
+    batch.render(js, opts)
+    batch.sync()
+    for k in range(len(jobs)):
+        assert np.array_equal(got[k].cpu().numpy(), want[k].cpu().numpy()), f"job {k} (depth {depths[k]})"
+    batch.close()
+
+
 def test_tuner_picks_options_and_leaves_films(ctx, scenes):
     films = _films(JOBS)
     for f in films:

@@ -511,7 +511,8 @@ def batch_secondary(torch, ctx_cls, scene_cls, local):
                             "reference": "FP64 CPU oracle, 2048 spp (tests/golden/batch_scene*_128_fp64_ref.npy)"},
            "tuned": {"path_capacity": best.path_capacity, "work_blocks_per_sm": best.work_blocks_per_sm,
                      "stack": "shared" if best.stack_placement == 1 else "local",
-                     "path_regeneration": best.chunk_paths != 1},
+                     "path_regeneration": best.chunk_paths != 1,
+                     "traversal": {0: "by size", 1: "coherent", 2: "incoherent"}.get(best.traversal, "?")},
            "tune_s": tune_s, "scene_generation_s": gen_s}
     batch.close()
     for sc in scenes:

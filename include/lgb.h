@@ -232,7 +232,8 @@ LGB_API lgb_status lgb_camera_from_matrix(const float camera_to_world[16], float
                                           uint32_t height, lgb_camera* out);
 
 /* ---- the Path integrator (Path::render, Path.cpp:27-59, i.e. path.rgen for frames frame0..frame0+spp-1).
- *      d_film is RGBA32F width*height (float4 per pixel), updated in place. ---- */
+ *      d_film is RGBA32F width*height (float4 per pixel), updated in place. Scenes of 2^15 triangles or more
+ *      trace their ray queues with the incoherent traversal variant (see lgb_batch_opts.traversal). ---- */
 LGB_API lgb_status lgb_render_path(lgb_scene* scene, const lgb_camera* camera, const lgb_path_params* params,
                                    uint32_t frame0, uint32_t spp, float* d_film, void* stream);
 
@@ -461,10 +462,17 @@ typedef struct lgb_batch_opts {
     uint32_t chunk_paths;          /* path regeneration: paths per chunk, run through the path_capacity slots
                                       (an ended path's slot takes the chunk's next path); 0 = 16 x path_capacity
                                       (at most 2^27), 1 = no regeneration (chunks of at most path_capacity) */
-    uint32_t reserved[2];
+    uint32_t traversal;            /* traversal variant of the path tracer's ray queues: LGB_TRAVERSAL_AUTO (0) by
+                                      the batch's triangle count (incoherent from 2^15), _COHERENT (a node's leaf
+                                      triangles tested when it is visited) or _INCOHERENT (one postponed leaf
+                                      triangle per lane and iteration); every variant gives the same hits */
+    uint32_t reserved[1];
 } lgb_batch_opts;
 #define LGB_STACK_LOCAL 0u
 #define LGB_STACK_SHARED 1u
+#define LGB_TRAVERSAL_AUTO 0u
+#define LGB_TRAVERSAL_COHERENT 1u
+#define LGB_TRAVERSAL_INCOHERENT 2u
 
 /* Copies the BVHs of `scenes` (each built with lgb_bvh_build) into one forest. The scenes must outlive the
  * batch; rebuilding a scene's BVH afterwards makes lgb_batch_render refuse the batch (LGB_ERR_NOT_READY). */

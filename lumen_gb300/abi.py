@@ -119,10 +119,12 @@ class BatchJob(C.Structure):
 class BatchOpts(C.Structure):
     _fields_ = [("path_capacity", C.c_uint32), ("work_blocks_per_sm", C.c_uint32),
                 ("trace_blocks_per_sm", C.c_uint32), ("stack_placement", C.c_uint32),
-                ("from_cache", C.c_uint32), ("chunk_paths", C.c_uint32), ("reserved", C.c_uint32 * 2)]
+                ("from_cache", C.c_uint32), ("chunk_paths", C.c_uint32), ("traversal", C.c_uint32),
+                ("reserved", C.c_uint32 * 1)]
 
 
 STACK_LOCAL, STACK_SHARED = 0, 1  # lgb_batch_opts.stack_placement
+TRAVERSAL_AUTO, TRAVERSAL_COHERENT, TRAVERSAL_INCOHERENT = 0, 1, 2  # lgb_batch_opts.traversal
 VCM_ACCUMULATE = 1
 RESTIR_SPATIAL_COUNT_FIX = 1
 

@@ -199,16 +199,18 @@ __global__ void __launch_bounds__(kThreads) k_camera(const Params* __restrict__ 
 }
 
 // Closest-hit / any-hit over a device-counted queue of rays, persistent with dynamic fetch; `roots` gives each
-// ray's BVH root in a batch forest (null: one BVH rooted at node 0). Registers are sized for 9 blocks per SM. The
-// path tracer's rays are mostly short and coherent (Cornell box, 1.4M-triangle batch scene): a node's leaf
-// triangles are tested in the iteration that reaches it, not one per iteration as in the incoherent trace
-// kernel. Measured on GB300, Cornell 256x256x16 spp / batch scene 704x704x8 spp, Msamples/s:
-//   leaf triangles in one iteration, 9 blocks  467 / 299
-//   leaf triangles in one iteration, 1 block   414 / 277
-//   one postponed triangle per iteration, 9    392 / 294
-//   one postponed triangle per iteration, 1    336 / 280
-// SK: bottom stack entries per thread in shared memory (0: the whole stack in local memory, the default here:
-// 8 shared entries cost 1 % on the two scenes above, 465 / 296). The batch autotuner tries both placements.
+// ray's BVH root in a batch forest (null: one BVH rooted at node 0). Registers are sized for 9 blocks per SM.
+// Two traversal variants (INC):
+//  - coherent (false): a node's leaf triangles are tested in the iteration that reaches it and a warp refetches
+//    once 16 lanes are idle; best for small scenes whose short rays stay together (Cornell box 256x256x16 spp:
+//    677 Msamples/s against 659 and 635 with the incoherent settings below);
+//  - incoherent (true): the headline trace kernel's settings, one postponed leaf triangle per lane and iteration
+//    with warp-uniform triangle iterations once a fifth of the active lanes hold one, and a refetch at 4 idle lanes;
+//    for large scenes whose secondary rays diverge (the 32-scene batch's scenes rendered one by one: 417 against
+//    413 Msamples/s; the tuned batch itself lands within its run-to-run spread either way).
+// The single-scene renderer takes the incoherent variant from kIncoherentTris triangles; the batch tuner times
+// both. SK: bottom stack entries per thread in shared memory (0: the whole stack in local memory); the batch
+// autotuner tries both placements.
 #ifdef LGB_QUEUE_POSTPONE
 constexpr bool kQueuePostpone = LGB_QUEUE_POSTPONE != 0;
 #else
@@ -219,37 +221,46 @@ constexpr int kQueueTriMin = LGB_QUEUE_TRI_MIN;
 #else
 constexpr int kQueueTriMin = 0;
 #endif
-constexpr int kQueueTraceMinBlocks = 9;
-constexpr int kQueueSharedStack = 8;  // entries when the stack placement is LGB_STACK_SHARED
-// Idle lanes a warp waits for before fetching new rays. Cornell / batch scene, Msamples/s, with the MIS
-// pre-test of k_shade: refill at 8 idle lanes 542 / 356, at 16: 550 / 354, at 32: 566 / 329.
 #ifdef LGB_QUEUE_REFILL
 constexpr int kQueueRefill = LGB_QUEUE_REFILL;
 #else
 constexpr int kQueueRefill = 16;
 #endif
-template <int SK>
+constexpr int kQueueTraceMinBlocks = 9;
+constexpr int kQueueSharedStack = 8;  // entries when the stack placement is LGB_STACK_SHARED
+constexpr uint32_t kIncoherentTris = 1u << 15;
+template <bool INC> struct QueueTrace {  // coherent
+    static constexpr bool postpone = kQueuePostpone;
+    static constexpr int tri_min = kQueueTriMin, refill = kQueueRefill;
+};
+template <> struct QueueTrace<true> {  // incoherent
+    static constexpr bool postpone = true;
+    static constexpr int tri_min = -5, refill = 4;
+};
+template <int SK, bool INC>
 __global__ void __launch_bounds__(kThreads, kQueueTraceMinBlocks)
     k_q_trace_closest(SceneView S, const lgb_ray* __restrict__ rays, lgb_hit* __restrict__ hits,
                       const uint32_t* count_ptr, uint32_t* ray_counter, const uint32_t* __restrict__ roots) {
+    using Q = QueueTrace<INC>;
     __shared__ uint2 s_stack[SK > 0 ? SK * kThreads : 1];
-    trace_persistent<false, false, kQueuePostpone, SK, kThreads, kQueueRefill, kQueueTriMin>(
+    trace_persistent<false, false, Q::postpone, SK, kThreads, Q::refill, Q::tri_min>(
         S.nodes, S.tris, rays, hits, nullptr, 0u, count_ptr, ray_counter, S.status, nullptr, roots, s_stack);
 }
 // A bounce's two NEE queries in one launch: the queued BSDF-MIS rays (closest hit) first, then the shadow rays
 // (any hit). The MIS queue is short but its rays are long, so the warps that take them start at once and then
 // join the shadow rays, whose queue the other warps are already draining; as two launches, the MIS trace ran alone
 // at the end of every bounce, bound by the latency of its few rays (Cornell box: 17 us of each 180-330 us bounce).
-template <int SK>
+template <int SK, bool INC>
 __global__ void __launch_bounds__(kThreads, kQueueTraceMinBlocks)
     k_q_trace_nee(SceneView S, const lgb_ray* __restrict__ srays, uint32_t* __restrict__ sbits,
                   const uint32_t* scount, uint32_t* sctr, const uint32_t* __restrict__ sroots,
                   const lgb_ray* __restrict__ mrays, lgb_hit* __restrict__ mhits, const uint32_t* mcount,
                   uint32_t* mctr, const uint32_t* __restrict__ mroots) {
+    using Q = QueueTrace<INC>;
     __shared__ uint2 s_stack[SK > 0 ? SK * kThreads : 1];
-    trace_persistent<false, false, kQueuePostpone, SK, kThreads, kQueueRefill, kQueueTriMin>(
+    trace_persistent<false, false, Q::postpone, SK, kThreads, Q::refill, Q::tri_min>(
         S.nodes, S.tris, mrays, mhits, nullptr, 0u, mcount, mctr, S.status, nullptr, mroots, s_stack);
-    trace_persistent<true, false, kQueuePostpone, SK, kThreads, kQueueRefill, kQueueTriMin>(
+    trace_persistent<true, false, Q::postpone, SK, kThreads, Q::refill, Q::tri_min>(
         S.nodes, S.tris, srays, nullptr, sbits, 0u, scount, sctr, S.status, nullptr, sroots, s_stack);
 }
 
@@ -731,30 +742,37 @@ constexpr int kWorkBlocksPerSm = 8;
 struct Grids {
     int work, trace;
     bool shared_stack;  // the traversal kernels keep the bottom of their stack in shared memory
+    bool incoherent;    // the traversal kernels' incoherent variant (QueueTrace<true>)
 };
 
-Grids path_grids(Ctx* ctx, bool shared_stack = false) {
-    int trace_blocks = 0;
+Grids path_grids(Ctx* ctx, bool shared_stack, bool incoherent) {
+    int trace_blocks = 0;  // the same register budget for every variant
     if (shared_stack)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&trace_blocks, k_q_trace_closest<kQueueSharedStack>, kThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&trace_blocks, k_q_trace_closest<kQueueSharedStack, false>, kThreads, 0);
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&trace_blocks, k_q_trace_closest<0>, kThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&trace_blocks, k_q_trace_closest<0, false>, kThreads, 0);
     const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
-    return Grids{sms * kWorkBlocksPerSm, sms * std::max(trace_blocks, 1), shared_stack};
+    return Grids{sms * kWorkBlocksPerSm, sms * std::max(trace_blocks, 1), shared_stack, incoherent};
 }
 
-template <int SK> void launch_queue_traces(const SceneView& S, const Buffers& B, Grids g, cudaStream_t st, bool first) {
+template <int SK, bool INC>
+void launch_queue_traces(const SceneView& S, const Buffers& B, Grids g, cudaStream_t st, bool first) {
     if (first) {
-        k_q_trace_closest<SK><<<g.trace, kThreads, 0, st>>>(S, B.rays, B.hits, B.counters + 0, B.counters + 8, B.root);
+        k_q_trace_closest<SK, INC><<<g.trace, kThreads, 0, st>>>(S, B.rays, B.hits, B.counters + 0, B.counters + 8, B.root);
     } else {
-        k_q_trace_nee<SK><<<g.trace, kThreads, 0, st>>>(S, B.srays, B.sbits, B.counters + 2, B.counters + 9, B.nroot,
-                                                        B.mrays, B.mhits, B.counters + 11, B.counters + 10, B.mroot);
+        k_q_trace_nee<SK, INC><<<g.trace, kThreads, 0, st>>>(S, B.srays, B.sbits, B.counters + 2, B.counters + 9, B.nroot,
+                                                             B.mrays, B.mhits, B.counters + 11, B.counters + 10, B.mroot);
     }
 }
 // first: the continuation rays' closest hits; else the shadow rays and the BSDF-MIS rays of the bounce.
 void queue_traces(const SceneView& S, const Buffers& B, Grids g, cudaStream_t st, bool first) {
-    if (g.shared_stack) launch_queue_traces<kQueueSharedStack>(S, B, g, st, first);
-    else launch_queue_traces<0>(S, B, g, st, first);
+    if (g.shared_stack) {
+        if (g.incoherent) launch_queue_traces<kQueueSharedStack, true>(S, B, g, st, first);
+        else launch_queue_traces<kQueueSharedStack, false>(S, B, g, st, first);
+    } else {
+        if (g.incoherent) launch_queue_traces<0, true>(S, B, g, st, first);
+        else launch_queue_traces<0, false>(S, B, g, st, first);
+    }
 }
 
 // One bounce over the live queue: closest hits, classification, shading per class, shadow and BSDF-MIS traces,
@@ -864,7 +882,7 @@ lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* p
     carve((char*)s->pt_buf, cap, B);
     const SceneView S = scene_view(s);
     Params P = make_params(cam, pp, cap, film);
-    const Grids g = path_grids(ctx);
+    const Grids g = path_grids(ctx, false, s->num_tris >= kIncoherentTris);
     const int bounces = std::max(pp->max_depth, 1);
     // The bounce loop of a chunk is captured once into a CUDA graph and replayed; the graph depends only on the
     // arena layout, the scene's device arrays and the bounce count, while everything per call travels in
@@ -872,7 +890,8 @@ lgb_status render_path(Scene* s, const lgb_camera* cam, const lgb_path_params* p
     cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
     LGB_CUDA_TRY(ctx, cudaStreamIsCapturing(st, &cap_status));
     const bool use_graph = cap_status == cudaStreamCaptureStatusNone;
-    const uint64_t key[6] = {(uint64_t)(uintptr_t)s->pt_buf, cap, (uint64_t)bounces | ((uint64_t)s->shade_classes << 40),
+    const uint64_t key[6] = {(uint64_t)(uintptr_t)s->pt_buf, cap,
+                             (uint64_t)bounces | ((uint64_t)g.incoherent << 32) | ((uint64_t)s->shade_classes << 40),
                              (uint64_t)(uintptr_t)S.nodes,
                              (uint64_t)(uintptr_t)S.tris, ((uint64_t)g.work << 32) | (uint32_t)g.trace};
     if (use_graph && (!s->pt_graph || std::memcmp(key, s->pt_graph_key, sizeof(key)) != 0)) {
@@ -971,7 +990,7 @@ lgb_status render_path_noalloc(Scene* s, const lgb_camera* cam, const lgb_path_p
     carve(arena, cap, B);
     const SceneView S = scene_view(s);
     Params P = make_params(cam, pp, cap, film);
-    const Grids g = path_grids(ctx);
+    const Grids g = path_grids(ctx, false, s->num_tris >= kIncoherentTris);
     const int bounces = std::max(pp->max_depth, 1);
     for (uint32_t done = 0; done < spp; done += frames_per_chunk) {
         P.frame0 = frame0 + done;
@@ -1294,7 +1313,11 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
     const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
     if (o.stack_placement > LGB_STACK_SHARED)
         return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "stack_placement must be LGB_STACK_LOCAL or LGB_STACK_SHARED");
-    Grids g = path_grids(ctx, o.stack_placement == LGB_STACK_SHARED);
+    if (o.traversal > LGB_TRAVERSAL_INCOHERENT)
+        return set_error(ctx, LGB_ERR_INVALID_ARGUMENT, "traversal must be LGB_TRAVERSAL_AUTO, _COHERENT or _INCOHERENT");
+    const bool incoherent = o.traversal == LGB_TRAVERSAL_AUTO ? b->num_tris >= kIncoherentTris
+                                                               : o.traversal == LGB_TRAVERSAL_INCOHERENT;
+    Grids g = path_grids(ctx, o.stack_placement == LGB_STACK_SHARED, incoherent);
     if (o.work_blocks_per_sm) g.work = sms * (int)std::min(o.work_blocks_per_sm, 64u);
     if (o.trace_blocks_per_sm) g.trace = std::min(g.trace, sms * (int)o.trace_blocks_per_sm);
 
@@ -1363,7 +1386,8 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
     // One graph renders every chunk of the call (build_batch_graph). It depends on the arena, the forest, the
     // bounce count, the grids, the chunk-record array and the regeneration output, not on the jobs.
     const uint64_t key[10] = {(uint64_t)(uintptr_t)b->buf, cap,
-                              (uint64_t)bounces | ((uint64_t)g.shared_stack << 32) | ((uint64_t)batch_classes(b) << 40),
+                              (uint64_t)bounces | ((uint64_t)g.shared_stack << 32) | ((uint64_t)g.incoherent << 33) |
+                                  ((uint64_t)batch_classes(b) << 40),
                               (uint64_t)(uintptr_t)b->nodes, (uint64_t)(uintptr_t)b->tris,
                               ((uint64_t)g.work << 32) | (uint32_t)g.trace, (uint64_t)(uintptr_t)b->d_chunks,
                               (uint64_t)(uintptr_t)b->d_loop, (uint64_t)(uintptr_t)B.col_out, regen ? 1u : 0u};
@@ -1391,7 +1415,7 @@ lgb_status batch_render(Batch* b, const lgb_batch_job* jobs, uint32_t n, const l
 
 // ---- the tuning cache (lgb_create's tuning_cache_path) ----
 // One line per choice: "<key> <path_capacity> <work_blocks_per_sm> <trace_blocks_per_sm> <stack_placement>
-// <chunk_paths>". The
+// <chunk_paths> <traversal>". The
 // key names the device (name, SM count, compute capability), the ABI version and the batch's shape: job count,
 // and the powers of two of its samples, of its largest image and of its triangles, its deepest path and the union
 // of its scenes' BSDF types. A later line replaces an earlier one with the same key.
@@ -1432,8 +1456,9 @@ std::map<std::string, lgb_batch_opts> read_tune_cache(const std::string& path) {
         std::string key;
         lgb_batch_opts o{};
         if (ls >> key >> o.path_capacity >> o.work_blocks_per_sm >> o.trace_blocks_per_sm >> o.stack_placement) {
-            uint32_t chunk = 0;
+            uint32_t chunk = 0, traversal = 0;
             if (ls >> chunk) o.chunk_paths = chunk;  // absent in lines written before path regeneration
+            if (ls >> traversal) o.traversal = traversal;  // absent in lines written before the traversal variants
             m[key] = o;
         }
     }
@@ -1451,7 +1476,8 @@ void write_tune_cache(const std::string& path, const std::string& key, const lgb
         if (!f) return;
         for (const auto& e : m)
             f << e.first << ' ' << e.second.path_capacity << ' ' << e.second.work_blocks_per_sm << ' '
-              << e.second.trace_blocks_per_sm << ' ' << e.second.stack_placement << ' ' << e.second.chunk_paths << '\n';
+              << e.second.trace_blocks_per_sm << ' ' << e.second.stack_placement << ' ' << e.second.chunk_paths << ' '
+              << e.second.traversal << '\n';
         if (!f) { std::remove(tmp.c_str()); return; }
     }
     if (std::rename(tmp.c_str(), path.c_str()) != 0) std::remove(tmp.c_str());
@@ -1459,7 +1485,7 @@ void write_tune_cache(const std::string& path, const std::string& key, const lgb
 
 // Screens every candidate (queue size x shading grid, stack in local memory, path regeneration) on a quarter of
 // each job's frames, then times the three fastest on the full jobs, then the best of those with the stack bottom
-// in shared memory and without path regeneration; films untouched throughout. The first run of a candidate
+// in shared memory, with the other traversal variant and without path regeneration; films untouched throughout. The first run of a candidate
 // records its graph, the second is timed.
 lgb_status batch_tune(Batch* b, const lgb_batch_job* jobs, uint32_t n, lgb_batch_opts* best, cudaStream_t st) {
     Ctx* ctx = b->ctx;
@@ -1531,6 +1557,11 @@ lgb_status batch_tune(Batch* b, const lgb_batch_job* jobs, uint32_t n, lgb_batch
     if (result == LGB_OK && have) {
         lgb_batch_opts o = best_o;
         o.stack_placement = LGB_STACK_SHARED;
+        confirm(o);
+    }
+    if (result == LGB_OK && have) {  // the other traversal variant than the scene size picks
+        lgb_batch_opts o = best_o;
+        o.traversal = b->num_tris >= kIncoherentTris ? LGB_TRAVERSAL_COHERENT : LGB_TRAVERSAL_INCOHERENT;
         confirm(o);
     }
     if (result == LGB_OK && have && !b->regen_refused) {

@@ -98,20 +98,23 @@ def _start_films(scenes):
 # chunk_paths: 0 = path regeneration with the default chunk (16 x the capacity: here one chunk whose ~60k paths
 # run through 4096 or 6000 slots), 1 = no regeneration (chunks of at most the capacity), 20000 = regeneration over
 # several chunks, each ending with its films before the next starts.
-@pytest.mark.parametrize("capacity,stack,chunk", [(0, 0, 0), (4096, 0, 0), (6000, 0, 0), (0, 1, 0), (6000, 1, 0),
-                                                  (4096, 0, 1), (6000, 0, 1), (4096, 0, 20000), (6000, 1, 20000)])
-def test_batched_films_equal_films_rendered_alone(ctx, scenes, capacity, stack, chunk):
+# traversal: 0 = by the batch's size (coherent here), 2 = the incoherent variant (same hits, other warp schedule).
+@pytest.mark.parametrize("capacity,stack,chunk,traversal", [
+    (0, 0, 0, 0), (4096, 0, 0, 0), (6000, 0, 0, 0), (0, 1, 0, 0), (6000, 1, 0, 0), (4096, 0, 1, 0), (6000, 0, 1, 0),
+    (4096, 0, 20000, 0), (6000, 1, 20000, 0), (4096, 0, 0, 2), (6000, 1, 20000, 2)])
+def test_batched_films_equal_films_rendered_alone(ctx, scenes, capacity, stack, chunk, traversal):
     start = _start_films(scenes)
     want = _films(JOBS, start)
     _alone(scenes, JOBS, want)
     got = _films(JOBS, start)
     opts = None
-    if capacity or stack or chunk:
+    if capacity or stack or chunk or traversal:
         opts = abi.BatchOpts()
         opts.path_capacity = capacity  # below some images: raised to the largest image
         opts.work_blocks_per_sm = 4
         opts.stack_placement = stack  # the stack's bottom in shared memory gives the same hits
         opts.chunk_paths = chunk
+        opts.traversal = traversal
     _batched(ctx, scenes, JOBS, got, opts)
     for k in range(len(JOBS)):
         a, b = got[k].cpu().numpy(), want[k].cpu().numpy()
@@ -141,6 +144,32 @@ def test_batched_jobs_of_different_depths(ctx, scenes, chunk):
     batch.sync()
     for k in range(len(jobs)):
         assert np.array_equal(got[k].cpu().numpy(), want[k].cpu().numpy()), f"job {k} (depth {depths[k]})"
+    batch.close()
+
+
+def test_large_scene_traversal_variants_agree(ctx):
+    """A 40 000-triangle scene renders alone with the incoherent traversal variant (from 2^15 triangles); the same
+    job batched with the coherent variant forced gives the same film."""
+    arrays = procedural.batch_scene(11, 40000)
+    sc = GpuScene(ctx, arrays)
+    sc.build()
+    cam = _camera(arrays, 64, 48)
+    alone = torch.zeros((64 * 48, 4), dtype=torch.float32, device="cuda")
+    sc.render_path(cam, path_params(arrays, DEPTH), 0, 4, alone)
+    sc.sync()
+    batched = torch.zeros_like(alone)
+    batch = Batch(ctx, [sc])
+    opts = abi.BatchOpts()
+    opts.traversal = abi.TRAVERSAL_COHERENT
+    batch.render([Batch.job(0, cam, path_params(arrays, DEPTH), 0, 4, batched)], opts)
+    batch.sync()
+    a, b = alone.cpu().numpy(), batched.cpu().numpy()
+    assert np.array_equal(a, b), f"max diff {np.abs(a - b).max()}"
+    assert a[:, :3].mean() > 0.0
+    bad = abi.BatchOpts()
+    bad.traversal = 3
+    with pytest.raises(abi.LgbError):
+        batch.render([Batch.job(0, cam, path_params(arrays, DEPTH), 0, 1, batched)], bad)
     batch.close()
 
 

@@ -202,8 +202,8 @@ __global__ void __launch_bounds__(kThreads) k_camera(const Params* __restrict__ 
 // ray's BVH root in a batch forest (null: one BVH rooted at node 0). Registers are sized for 9 blocks per SM.
 // Two traversal variants (INC):
 //  - coherent (false): a node's leaf triangles are tested in the iteration that reaches it and a warp refetches
-//    once 16 lanes are idle; best for small scenes whose short rays stay together (Cornell box 256x256x16 spp:
-//    677 Msamples/s against 659 and 635 with the incoherent settings below);
+//    once all its lanes are idle; best for small scenes whose short rays stay together (Cornell box 256x256x16
+//    spp: 694 Msamples/s, 672 refetching at 16 idle lanes, 659 and 635 with the incoherent settings below);
 //  - incoherent (true): the headline trace kernel's settings, one postponed leaf triangle per lane and iteration
 //    with warp-uniform triangle iterations once a fifth of the active lanes hold one, and a refetch at 4 idle lanes;
 //    for large scenes whose secondary rays diverge (the 32-scene batch's scenes rendered one by one: 417 against
@@ -224,7 +224,7 @@ constexpr int kQueueTriMin = 0;
 #ifdef LGB_QUEUE_REFILL
 constexpr int kQueueRefill = LGB_QUEUE_REFILL;
 #else
-constexpr int kQueueRefill = 16;
+constexpr int kQueueRefill = 32;
 #endif
 constexpr int kQueueTraceMinBlocks = 9;
 constexpr int kQueueSharedStack = 8;  // entries when the stack placement is LGB_STACK_SHARED

@@ -38,6 +38,12 @@ constexpr int kDiffRegMaterials = 8;  // roughness/emission gradients held in re
 #endif
 constexpr int kDiffThreads = LGB_DIFF_THREADS;      // threads per block of the path kernels
 constexpr int kDiffMinBlocks = LGB_DIFF_MIN_BLOCKS; // resident blocks per SM the register budget is sized for
+// The wave kernels' register budget: 4 blocks per SM (128 registers, a few spilled) against 1 (163 registers):
+// 512x512x32 primal / replay 13.6 / 19.1 ms against 14.8 / 21.0.
+#ifndef LGB_DIFF_WAVE_MIN_BLOCKS
+#define LGB_DIFF_WAVE_MIN_BLOCKS 4
+#endif
+constexpr int kDiffWaveMinBlocks = LGB_DIFF_WAVE_MIN_BLOCKS;
 constexpr float kTMinD = 0.001f, kTMaxD = 10000.0f, kEpsD = 0.001f;
 
 #ifndef LGB_DIFF_OUTLINE
@@ -768,7 +774,7 @@ __global__ void __launch_bounds__(kDiffThreads) k_diff_wave_init(DiffArgs A, Dif
 // class's lobes in the completion kernel, so each launch's code is a fraction of the loop's (the pass stalls on
 // instruction fetch otherwise).
 template <int MODE, uint32_t MASK, int PHASE>
-__global__ void __launch_bounds__(kDiffThreads, kDiffMinBlocks)
+__global__ void __launch_bounds__(kDiffThreads, kDiffWaveMinBlocks)
     k_diff_wave(SceneView S, DiffArgs A, DiffWave W, int depth, int cls, int miss_cls) {
     __shared__ float sh_grad[4 * kDiffRegMaterials];
     constexpr bool GRAD = MODE != kPrimal && PHASE == kPhaseResults;

@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(kThreads) k_camera(const Params* __restrict__ 
 //    once all its lanes are idle; best for small scenes whose short rays stay together (Cornell box 256x256x16
 //    spp: 694 Msamples/s, 672 refetching at 16 idle lanes, 659 and 635 with the incoherent settings below);
 //  - incoherent (true): the headline trace kernel's settings, one postponed leaf triangle per lane and iteration
-//    with warp-uniform triangle iterations once a fifth of the active lanes hold one, and a refetch at 4 idle lanes;
+//    with warp-uniform triangle iterations once a fifth of the active lanes hold one, and a refetch at 8 idle lanes;
 //    for large scenes whose secondary rays diverge (the 32-scene batch's scenes rendered one by one: 417 against
 //    413 Msamples/s; the tuned batch itself lands within its run-to-run spread either way).
 // The single-scene renderer takes the incoherent variant from kIncoherentTris triangles; the batch tuner times
@@ -233,9 +233,12 @@ template <bool INC> struct QueueTrace {  // coherent
     static constexpr bool postpone = kQueuePostpone;
     static constexpr int tri_min = kQueueTriMin, refill = kQueueRefill;
 };
+#ifndef LGB_QUEUE_INC_REFILL
+#define LGB_QUEUE_INC_REFILL 8  // the 32-scene batch: 550-554 Msamples/s at 8 idle lanes, 542-548 at 4, 540-545 at 16
+#endif
 template <> struct QueueTrace<true> {  // incoherent
     static constexpr bool postpone = true;
-    static constexpr int tri_min = -5, refill = 4;
+    static constexpr int tri_min = -5, refill = LGB_QUEUE_INC_REFILL;
 };
 template <int SK, bool INC>
 __global__ void __launch_bounds__(kThreads, kQueueTraceMinBlocks)

@@ -1,6 +1,7 @@
 // LSD radix sort of (32- or 64-bit key, 32-bit value) pairs, 8 bits per pass, stable, reduce-then-scan over a
 // persistent grid: each block owns one contiguous range of tiles for the whole pass. Per pass, a histogram kernel
-// counts each block's digits (one read of the keys), one exclusive scan over the (digit, block) counts gives every
+// counts each block's digits (one read of the keys) and adds them into the pass's digit totals, one warp per digit
+// scans that digit's block counts from the digit's start (the totals of the digits below it), which gives every
 // block the output position of its first key of each digit, and the scatter kernel walks the block's tiles in
 // order, advancing its per-digit positions tile by tile in shared memory. Within a tile the keys are ranked per
 // warp with __match_any_sync, staged in digit order in shared memory and written out with consecutive threads on
@@ -33,17 +34,14 @@ constexpr int RS_MIN_BLOCKS = 3;
 #endif
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 constexpr int RS_MAX_BLOCKS = 1024;  // blocks of the persistent grid: a bound on the (digit, block) counts
-constexpr int SCAN_THREADS = 512;
-constexpr int SCAN_ITEMS = 8;
-constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 inline uint32_t rs_tiles(uint32_t n) { return (n + RS_TILE - 1) / RS_TILE; }
 
-// Words of scratch radix_sort_pairs needs: the (digit, block) counts and one sum per scan tile.
+// Words of scratch radix_sort_pairs needs: the (digit, block) counts, then two sets of digit totals (one per pass,
+// alternating).
 inline size_t radix_sort_scratch_words(uint32_t n) {
     (void)n;
-    const size_t m = 256 * (size_t)RS_MAX_BLOCKS;
-    return m + (m + SCAN_TILE - 1) / SCAN_TILE;
+    return 256 * (size_t)RS_MAX_BLOCKS + 512;
 }
 
 // Tiles [t0, t1) of block b of a grid of g blocks over `tiles` tiles.
@@ -53,10 +51,12 @@ __device__ __forceinline__ void rs_range(uint32_t tiles, uint32_t b, uint32_t g,
 }
 
 // Digit counts of each block's range: one shared-memory histogram per warp (fewer collisions on skewed keys, such
-// as the hash slots of clustered photons), summed into counts[digit * gridDim.x + block].
+// as the hash slots of clustered photons), summed into counts[digit * gridDim.x + block] and added into the
+// pass's digit totals (zeroed before the launch).
 template <class KeyT>
 __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const KeyT* __restrict__ keys, uint32_t n, int shift,
-                                                        uint32_t tiles, uint32_t* __restrict__ counts) {
+                                                        uint32_t tiles, uint32_t* __restrict__ counts,
+                                                        uint32_t* __restrict__ totals) {
     __shared__ uint32_t h[RS_THREADS / 32][256];
     const int tid = threadIdx.x, warp = tid >> 5;
     for (int w = 0; w < RS_THREADS / 32; w++) h[w][tid] = 0;
@@ -71,119 +71,39 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const KeyT* __restrict__
     uint32_t c = 0;
     for (int w = 0; w < RS_THREADS / 32; w++) c += h[w][tid];
     counts[(size_t)tid * gridDim.x + blockIdx.x] = c;
+    if (c) atomicAdd(&totals[tid], c);
 }
 
-// Exclusive scan of m counts in place, one block of 1024 threads.
-__global__ void __launch_bounds__(1024) k_scan_single(uint32_t* data, uint32_t m) {
-    __shared__ uint32_t warp_sums[32];
-    const uint32_t per = (m + 1023) / 1024;
-    const uint32_t b = threadIdx.x * per, e = min(m, b + per);
+// Output positions of every (digit, block): one warp per digit scans that digit's g block counts in place, from
+// the digit's start (the digits below it, summed from the totals). Replaces a general scan of all 256 x g counts.
+// Also zeroes the other set of totals, which the next pass's histogram accumulates into.
+__global__ void __launch_bounds__(128) k_rs_digit_offsets(uint32_t* __restrict__ counts, const uint32_t* __restrict__ totals,
+                                                          uint32_t* __restrict__ next_totals, uint32_t g) {
+    const uint32_t d = blockIdx.x * 4u + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (d >= 256u) return;
+    if (lane == 0) next_totals[d] = 0u;
+    uint32_t below = 0;
+    for (uint32_t k = (uint32_t)lane; k < d; k += 32u) below += totals[k];
+    below = __reduce_add_sync(0xffffffffu, below);
+    // Lane l scans the consecutive counts [l * per, (l + 1) * per) of the digit's row: the lane sums, one warp scan,
+    // then the row is rewritten from the lane's start.
+    uint32_t* row = counts + (size_t)d * g;
+    const uint32_t per = (g + 31u) / 32u;
+    const uint32_t b0 = min(g, (uint32_t)lane * per), b1 = min(g, b0 + per);
     uint32_t sum = 0;
-    for (uint32_t i = b; i < e; i++) sum += data[i];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t i = b0; i < b1; i++) sum += row[i];
     uint32_t x = sum;
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) warp_sums[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t w = warp_sums[lane];
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w += y;
-        }
-        warp_sums[lane] = w;
-    }
-    __syncthreads();
-    uint32_t excl = x - sum + (warp > 0 ? warp_sums[warp - 1] : 0u);
-    for (uint32_t i = b; i < e; i++) {
-        uint32_t c = data[i];
-        data[i] = excl;
-        excl += c;
-    }
-}
-
-// Sum of each SCAN_TILE-count tile of data[0, m) into sums[tile].
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile_sums(const uint32_t* __restrict__ data, uint32_t m,
-                                                                 uint32_t* __restrict__ sums) {
-    __shared__ uint32_t ws[SCAN_THREADS / 32];
-    const size_t base = (size_t)blockIdx.x * SCAN_TILE;
-    uint32_t s = 0;
-    for (int k = 0; k < SCAN_ITEMS; k++) {
-        const size_t i = base + (size_t)k * SCAN_THREADS + threadIdx.x;
-        if (i < m) s += data[i];
-    }
-    s = __reduce_add_sync(0xffffffffu, s);
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        uint32_t v = threadIdx.x < SCAN_THREADS / 32 ? ws[threadIdx.x] : 0u;
-        v = __reduce_add_sync(0xffffffffu, v);
-        if (threadIdx.x == 0) sums[blockIdx.x] = v;
-    }
-}
-
-// Exclusive scan of one tile of data[0, m) in place, starting from sums[tile] (0 when sums is null): the tile is
-// staged in shared memory, each thread scans SCAN_ITEMS consecutive counts, and the thread totals are scanned
-// across the block.
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile_apply(uint32_t* __restrict__ data, uint32_t m,
-                                                                  const uint32_t* __restrict__ sums) {
-    __shared__ uint32_t tile[SCAN_TILE];
-    __shared__ uint32_t ws[SCAN_THREADS / 32];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const size_t base = (size_t)blockIdx.x * SCAN_TILE;
-    for (int k = 0; k < SCAN_ITEMS; k++) {
-        const int i = k * SCAN_THREADS + tid;
-        tile[i] = base + i < m ? data[base + i] : 0u;
-    }
-    __syncthreads();
-    uint32_t v[SCAN_ITEMS];
-    uint32_t sum = 0;
-    for (int j = 0; j < SCAN_ITEMS; j++) {
-        v[j] = tile[tid * SCAN_ITEMS + j];
-        sum += v[j];
-    }
-    uint32_t x = sum;  // inclusive scan of the thread totals within the warp
     for (int o = 1; o < 32; o <<= 1) {
         const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
         if (lane >= o) x += y;
     }
-    if (lane == 31) ws[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t w = lane < SCAN_THREADS / 32 ? ws[lane] : 0u;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w += y;
-        }
-        if (lane < SCAN_THREADS / 32) ws[lane] = w;
+    uint32_t run = below + x - sum;
+    for (uint32_t i = b0; i < b1; i++) {
+        const uint32_t c = row[i];
+        row[i] = run;
+        run += c;
     }
-    __syncthreads();
-    uint32_t excl = x - sum + (warp > 0 ? ws[warp - 1] : 0u) + (sums ? sums[blockIdx.x] : 0u);
-    for (int j = 0; j < SCAN_ITEMS; j++) {
-        tile[tid * SCAN_ITEMS + j] = excl;
-        excl += v[j];
-    }
-    __syncthreads();
-    for (int k = 0; k < SCAN_ITEMS; k++) {
-        const int i = k * SCAN_THREADS + tid;
-        if (base + i < m) data[base + i] = tile[i];
-    }
-}
-
-// Exclusive scan of data[0, m) in place; data must have room for the tile sums after the m counts.
-inline void scan_exclusive(uint32_t* data, uint32_t m, cudaStream_t st) {
-    const uint32_t nt = (m + SCAN_TILE - 1) / SCAN_TILE;
-    if (nt <= 1) {
-        k_scan_tile_apply<<<1, SCAN_THREADS, 0, st>>>(data, m, nullptr);
-        return;
-    }
-    uint32_t* sums = data + m;
-    k_scan_tile_sums<<<nt, SCAN_THREADS, 0, st>>>(data, m, sums);
-    k_scan_single<<<1, 1024, 0, st>>>(sums, nt);
-    k_scan_tile_apply<<<nt, SCAN_THREADS, 0, st>>>(data, m, sums);
 }
 
 // The scatter of each block's range of tiles (see the header comment). offsets: the scanned (digit, block) counts.
@@ -318,10 +238,15 @@ inline cudaError_t radix_sort_pairs(KeyT*& k0, uint32_t*& v0, KeyT*& k1, uint32_
     if (n == 0) return cudaSuccess;
     const uint32_t tiles = rs_tiles(n);
     const uint32_t g = rs_grid<KeyT>(tiles);
+    uint32_t* totals = counts + 256 * (size_t)RS_MAX_BLOCKS;
+    const cudaError_t e = cudaMemsetAsync(totals, 0, 256 * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
     for (int pass = 0; pass < passes; pass++) {
         const int shift = pass * 8;
-        k_rs_hist<KeyT><<<g, RS_THREADS, 0, st>>>(k0, n, shift, tiles, counts);
-        scan_exclusive(counts, 256 * g, st);
+        uint32_t* cur = totals + 256 * (pass & 1);
+        uint32_t* next = totals + 256 * ((pass + 1) & 1);
+        k_rs_hist<KeyT><<<g, RS_THREADS, 0, st>>>(k0, n, shift, tiles, counts, cur);
+        k_rs_digit_offsets<<<64, 128, 0, st>>>(counts, cur, next, g);
         k_rs_scatter<KeyT><<<g, RS_THREADS, 0, st>>>(k0, v0, k1, v1, n, shift, tiles, counts);
         std::swap(k0, k1);
         std::swap(v0, v1);

@@ -64,8 +64,25 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const KeyT* __restrict__
     uint32_t t0, t1;
     rs_range(tiles, blockIdx.x, gridDim.x, t0, t1);
     const size_t e = min((size_t)t1 * RS_TILE, (size_t)n);
+    size_t i0 = (size_t)t0 * RS_TILE;
+    if constexpr (sizeof(KeyT) == 4) {
+        if ((reinterpret_cast<uintptr_t>(keys) & 15u) == 0) {
+            // four keys per load (a range starts on a tile, so on a 16-byte boundary)
+            const uint4* kv = reinterpret_cast<const uint4*>(keys + i0);
+            const size_t nv = i0 < e ? (e - i0) / 4 : 0;
+#pragma unroll 4
+            for (size_t j = tid; j < nv; j += RS_THREADS) {
+                const uint4 k = kv[j];
+                atomicAdd(&h[warp][(k.x >> shift) & 0xffu], 1u);
+                atomicAdd(&h[warp][(k.y >> shift) & 0xffu], 1u);
+                atomicAdd(&h[warp][(k.z >> shift) & 0xffu], 1u);
+                atomicAdd(&h[warp][(k.w >> shift) & 0xffu], 1u);
+            }
+            i0 += nv * 4;
+        }
+    }
 #pragma unroll 8
-    for (size_t i = (size_t)t0 * RS_TILE + tid; i < e; i += RS_THREADS)
+    for (size_t i = i0 + tid; i < e; i += RS_THREADS)
         atomicAdd(&h[warp][(uint32_t)(keys[i] >> shift) & 0xffu], 1u);
     __syncthreads();
     uint32_t c = 0;
@@ -74,35 +91,47 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const KeyT* __restrict__
     if (c) atomicAdd(&totals[tid], c);
 }
 
-// Output positions of every (digit, block): one warp per digit scans that digit's g block counts in place, from
-// the digit's start (the digits below it, summed from the totals). Replaces a general scan of all 256 x g counts.
-// Also zeroes the other set of totals, which the next pass's histogram accumulates into.
-__global__ void __launch_bounds__(128) k_rs_digit_offsets(uint32_t* __restrict__ counts, const uint32_t* __restrict__ totals,
+// Output positions of every (digit, block): block d scans digit d's g block counts in place (each thread up to
+// RS_MAX_BLOCKS / 256 consecutive counts, held in registers), starting from the digit's start, the sum of the
+// totals of the digits below it. Replaces a general scan of all 256 x g counts. Also zeroes the other set of
+// totals, which the next pass's histogram accumulates into.
+__global__ void __launch_bounds__(256) k_rs_digit_offsets(uint32_t* __restrict__ counts, const uint32_t* __restrict__ totals,
                                                           uint32_t* __restrict__ next_totals, uint32_t g) {
-    const uint32_t d = blockIdx.x * 4u + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    if (d >= 256u) return;
-    if (lane == 0) next_totals[d] = 0u;
-    uint32_t below = 0;
-    for (uint32_t k = (uint32_t)lane; k < d; k += 32u) below += totals[k];
-    below = __reduce_add_sync(0xffffffffu, below);
-    // Lane l scans the consecutive counts [l * per, (l + 1) * per) of the digit's row: the lane sums, one warp scan,
-    // then the row is rewritten from the lane's start.
+    constexpr int PER = RS_MAX_BLOCKS / 256;
+    __shared__ uint32_t ws[8];
+    __shared__ uint32_t wb[8];
+    const uint32_t d = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     uint32_t* row = counts + (size_t)d * g;
-    const uint32_t per = (g + 31u) / 32u;
-    const uint32_t b0 = min(g, (uint32_t)lane * per), b1 = min(g, b0 + per);
+    uint32_t c[PER];
     uint32_t sum = 0;
-    for (uint32_t i = b0; i < b1; i++) sum += row[i];
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+        const uint32_t i = (uint32_t)tid * PER + k;
+        c[k] = i < g ? row[i] : 0u;
+        sum += c[k];
+    }
+    uint32_t below = (uint32_t)tid < d ? totals[tid] : 0u;
+    below = __reduce_add_sync(0xffffffffu, below);
     uint32_t x = sum;
     for (int o = 1; o < 32; o <<= 1) {
         const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
         if (lane >= o) x += y;
     }
-    uint32_t run = below + x - sum;
-    for (uint32_t i = b0; i < b1; i++) {
-        const uint32_t c = row[i];
-        row[i] = run;
-        run += c;
+    if (lane == 31) ws[warp] = x;
+    if (lane == 0) wb[warp] = below;
+    __syncthreads();
+    if (tid == 0) next_totals[d] = 0u;
+    uint32_t run = x - sum;
+    for (int w = 0; w < 8; w++) {
+        run += w < warp ? ws[w] : 0u;
+        run += wb[w];
+    }
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+        const uint32_t i = (uint32_t)tid * PER + k;
+        if (i < g) row[i] = run;
+        run += c[k];
     }
 }
 
@@ -246,7 +275,7 @@ inline cudaError_t radix_sort_pairs(KeyT*& k0, uint32_t*& v0, KeyT*& k1, uint32_
         uint32_t* cur = totals + 256 * (pass & 1);
         uint32_t* next = totals + 256 * ((pass + 1) & 1);
         k_rs_hist<KeyT><<<g, RS_THREADS, 0, st>>>(k0, n, shift, tiles, counts, cur);
-        k_rs_digit_offsets<<<64, 128, 0, st>>>(counts, cur, next, g);
+        k_rs_digit_offsets<<<256, 256, 0, st>>>(counts, cur, next, g);
         k_rs_scatter<KeyT><<<g, RS_THREADS, 0, st>>>(k0, v0, k1, v1, n, shift, tiles, counts);
         std::swap(k0, k1);
         std::swap(v0, v1);

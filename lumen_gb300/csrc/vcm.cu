@@ -39,6 +39,13 @@ constexpr int kVcmStepMinBlocks = LGB_VCM_STEP_MIN_BLOCKS;
 #else
 constexpr int kVcmStepMinBlocks = 4;
 #endif
+// The light step alone at 6 blocks per SM (80 registers, a few bytes of spill; 104 at 4): caustics iteration 7.27
+// against 7.39 ms (5 blocks: 7.32; 7 or 8: 7.27). The eye step spills heavily below 128 registers.
+#ifdef LGB_VCM_LIGHT_STEP_MIN_BLOCKS
+constexpr int kVcmLightStepMinBlocks = LGB_VCM_LIGHT_STEP_MIN_BLOCKS;
+#else
+constexpr int kVcmLightStepMinBlocks = 6;
+#endif
 constexpr int kMaxMergeCells = 16;
 constexpr float kTMinV = 0.001f, kTMaxV = 10000.0f, kEpsV = 0.001f;
 constexpr int kVertexF4 = 6;  // light vertex = 6 x float4 (96 bytes)
@@ -292,7 +299,7 @@ __global__ void __launch_bounds__(kVcmThreads) k_vcm_light_init(SceneView S, Vcm
 // vcm_fill_light, one bounce (depth) of the queued light subpaths: vertex store, camera connection, the next
 // direction; a subpath that ends writes its vertex count.
 template <uint32_t MASK>
-__global__ void __launch_bounds__(kVcmThreads, kVcmStepMinBlocks) k_vcm_light_step(SceneView S, VcmArgs A, Wave W, int depth) {
+__global__ void __launch_bounds__(kVcmThreads, kVcmLightStepMinBlocks) k_vcm_light_step(SceneView S, VcmArgs A, Wave W, int depth) {
     const CamV cam = cam_setup(A);
     const Etas eta = etas(A);
     const uint32_t per = (uint32_t)(A.max_depth + 1);

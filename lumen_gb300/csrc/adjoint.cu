@@ -44,6 +44,12 @@ constexpr int kDiffMinBlocks = LGB_DIFF_MIN_BLOCKS; // resident blocks per SM th
 #define LGB_DIFF_WAVE_MIN_BLOCKS 4
 #endif
 constexpr int kDiffWaveMinBlocks = LGB_DIFF_WAVE_MIN_BLOCKS;
+// The primal's completion kernels at 5 blocks per SM (96 registers, some spilled; 117-127 at 4): primal 13.63 ->
+// 13.31 ms (6 blocks, 80 registers: 13.28). The replay's completion kernels spill at 4 already; the rays kernels
+// (64-72 registers) are not limited by the budget (8 blocks per SM measured the same).
+#ifndef LGB_DIFF_PRIMAL_MIN_BLOCKS
+#define LGB_DIFF_PRIMAL_MIN_BLOCKS 5
+#endif
 constexpr float kTMinD = 0.001f, kTMaxD = 10000.0f, kEpsD = 0.001f;
 
 #ifndef LGB_DIFF_OUTLINE
@@ -774,7 +780,8 @@ __global__ void __launch_bounds__(kDiffThreads) k_diff_wave_init(DiffArgs A, Dif
 // class's lobes in the completion kernel, so each launch's code is a fraction of the loop's (the pass stalls on
 // instruction fetch otherwise).
 template <int MODE, uint32_t MASK, int PHASE>
-__global__ void __launch_bounds__(kDiffThreads, kDiffWaveMinBlocks)
+__global__ void __launch_bounds__(kDiffThreads, (MODE == kPrimal && PHASE == kPhaseResults) ? LGB_DIFF_PRIMAL_MIN_BLOCKS
+                                                                                        : kDiffWaveMinBlocks)
     k_diff_wave(SceneView S, DiffArgs A, DiffWave W, int depth, int cls, int miss_cls) {
     __shared__ float sh_grad[4 * kDiffRegMaterials];
     constexpr bool GRAD = MODE != kPrimal && PHASE == kPhaseResults;

@@ -44,11 +44,14 @@ constexpr int kDiffMinBlocks = LGB_DIFF_MIN_BLOCKS; // resident blocks per SM th
 #define LGB_DIFF_WAVE_MIN_BLOCKS 4
 #endif
 constexpr int kDiffWaveMinBlocks = LGB_DIFF_WAVE_MIN_BLOCKS;
-// The primal's completion kernels at 5 blocks per SM (96 registers, some spilled; 117-127 at 4): primal 13.63 ->
-// 13.31 ms (6 blocks, 80 registers: 13.28). The replay's completion kernels spill at 4 already; the rays kernels
-// (64-72 registers) are not limited by the budget (8 blocks per SM measured the same).
+// The completion kernels at 5 blocks per SM (96 registers, some spilled): primal 13.63 -> 13.31 ms (117-127
+// registers at 4; 6 blocks, 80 registers: 13.28), replay 19.13 -> 18.79 ms (128 registers at 4; 3 blocks without
+// spills: 21.07). The rays kernels (64-72 registers) stay at 4 (the primal measured 0.8 % slower at 5).
 #ifndef LGB_DIFF_PRIMAL_MIN_BLOCKS
 #define LGB_DIFF_PRIMAL_MIN_BLOCKS 5
+#endif
+#ifndef LGB_DIFF_REPLAY_MIN_BLOCKS
+#define LGB_DIFF_REPLAY_MIN_BLOCKS 5
 #endif
 constexpr float kTMinD = 0.001f, kTMaxD = 10000.0f, kEpsD = 0.001f;
 
@@ -780,8 +783,9 @@ __global__ void __launch_bounds__(kDiffThreads) k_diff_wave_init(DiffArgs A, Dif
 // class's lobes in the completion kernel, so each launch's code is a fraction of the loop's (the pass stalls on
 // instruction fetch otherwise).
 template <int MODE, uint32_t MASK, int PHASE>
-__global__ void __launch_bounds__(kDiffThreads, (MODE == kPrimal && PHASE == kPhaseResults) ? LGB_DIFF_PRIMAL_MIN_BLOCKS
-                                                                                        : kDiffWaveMinBlocks)
+__global__ void __launch_bounds__(kDiffThreads, PHASE != kPhaseResults ? kDiffWaveMinBlocks
+                                                : MODE == kPrimal       ? LGB_DIFF_PRIMAL_MIN_BLOCKS
+                                                                        : LGB_DIFF_REPLAY_MIN_BLOCKS)
     k_diff_wave(SceneView S, DiffArgs A, DiffWave W, int depth, int cls, int miss_cls) {
     __shared__ float sh_grad[4 * kDiffRegMaterials];
     constexpr bool GRAD = MODE != kPrimal && PHASE == kPhaseResults;

@@ -25,8 +25,9 @@ constexpr int RS_ITEMS = LGB_RS_ITEMS;
 constexpr int RS_ITEMS = 8;
 #endif
 // Register budget of the 32-bit-key scatter: 3 blocks per SM (85 registers; 109 unbounded). On the VCM's 11.5 M
-// keys, per pass under ncu: histogram 13.4 + scan 10.8 + scatter 46.7 us against 16.5 + 10.6 + 49.2 unbounded and
-// 12.3 + 10.3 + 60.5 at 4 blocks (64 registers, spilling). 64-bit keys keep the unbounded budget (they would spill).
+// keys, per pass under ncu (histogram + scatter): 13.4 + 46.7 us against 16.5 + 49.2 unbounded and 12.3 + 60.5 at
+// 4 blocks (64 registers, spilling); the grid, and so the histogram's, follows the scatter's occupancy. 64-bit keys
+// keep the unbounded budget (they would spill).
 #ifdef LGB_RS_MIN_BLOCKS
 constexpr int RS_MIN_BLOCKS = LGB_RS_MIN_BLOCKS;
 #else

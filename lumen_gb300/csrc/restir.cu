@@ -159,7 +159,8 @@ __device__ void combine_reservoir(const SceneView& S, const LightSet& Ls, const 
 }
 
 // temporal_pass.rgen:7-233 (without the path-traced colour, which the output pass never reads)
-__global__ void __launch_bounds__(kRestirThreads) k_restir_temporal(SceneView S, RestirArgs A) {
+// Registers for 4 blocks per SM (144 unbounded): a 256 x 256 frame's 512 blocks then fit one wave on 152 SMs.
+__global__ void __launch_bounds__(kRestirThreads, 4) k_restir_temporal(SceneView S, RestirArgs A) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < A.screen; i += gridDim.x * blockDim.x) {
         const uint32_t x = i / A.H, y = i % A.H;
         uint4 seed = make_uint4(x, y, A.seed_frame, 0u);
